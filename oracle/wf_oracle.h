@@ -1,0 +1,91 @@
+/* CPU restatement of the WeldFormFEM explicit updated-Lagrangian step.
+ *
+ * TEST INFRASTRUCTURE ONLY. This is the oracle the CUDA path is checked
+ * against, and the "port" CPU baseline that bench.py times. Only tests/,
+ * __graft_entry__.smoke() and bench.py's CPU-baseline leg may load it; the
+ * product library never links or calls it.
+ *
+ * Every routine restates one reference routine (file:line in its comment)
+ * with the same operation order, so that with -ffp-contract=off it agrees bit
+ * for bit with the reference compiled from its own sources (oracle/_ref).
+ * The API mirrors the product's C ABI (include/wf.h) with a wfo_ prefix.
+ */
+#ifndef WF_ORACLE_H
+#define WF_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct wfo_domain wfo_domain;
+
+/* Material_ / Elastic_ (include/common/Material.cuh:15-156). */
+typedef struct {
+  int model;      /* 0 = bilinear (linear isotropic hardening), 1 = Hollomon */
+  double E, nu, rho;
+  double sy0;     /* initial yield stress */
+  double H;       /* hardening modulus d(sigma_y)/d(eps_p), model 0 */
+  double hol_K, hol_m; /* Hollomon sigma_y = K (eps_p + eps0)^m, model 1 */
+} wfo_material;
+
+wfo_domain *wfo_create(void);
+void wfo_destroy(wfo_domain *d);
+void wfo_set_threads(wfo_domain *d, int nthreads);
+
+/* Domain_d::AddBoxLength(V, L, r, red_int=true, tritetra) (Domain_d.C:1136). */
+int wfo_add_box_length(wfo_domain *d, const double V[3], const double L[3], double r,
+                       int tritetra);
+/* SetDimension + setNodElem, as Domain_d::CreateFromLSDyna (Domain_d.C:1647). */
+int wfo_set_mesh(wfo_domain *d, int64_t nn, int64_t ne, int npe, const double *xyz,
+                 const int32_t *elnod);
+int wfo_set_nodes(wfo_domain *d, const double *xyz);
+void wfo_sizes(const wfo_domain *d, int64_t *nn, int64_t *ne, int *npe, int64_t *nodel_tot);
+void wfo_get_connectivity(const wfo_domain *d, int32_t *elnod, int32_t *nodel,
+                          int32_t *nodel_loc, int32_t *offset, int32_t *count);
+
+int wfo_set_materials(wfo_domain *d, int nmat, const wfo_material *m);
+int wfo_set_elem_materials(wfo_domain *d, const int32_t *ids);
+int wfo_add_bc_vel_node(wfo_domain *d, int64_t node, int dim, double val);
+int wfo_allocate_bcs(wfo_domain *d);
+int wfo_set_reaction_nodes(wfo_domain *d, int64_t n, const int32_t *nodes, int dim);
+
+void wfo_set_dt(wfo_domain *d, double dt);
+void wfo_set_end_time(wfo_domain *d, double t);
+void wfo_set_hourglass(wfo_domain *d, double coef);
+void wfo_set_press_algorithm(wfo_domain *d, int alg);
+void wfo_set_stab(wfo_domain *d, const double s[10]);
+void wfo_set_artif_visc(wfo_domain *d, double alpha, double beta);
+/* 0: lumped mass recomputed every step from the current volume, as the
+ * reference loop does (Solver_explicit.C:605-607); 1: mass fixed at its
+ * initial value, as the reference's one-element test driver does
+ * (src/common/test_1el_3D.cpp:269-270). */
+void wfo_set_mass_mode(wfo_domain *d, int mode);
+/* Rigid flat die z = z0 + vz t, penalty + Coulomb (Contact.C:58-323). */
+void wfo_set_contact_plane(wfo_domain *d, double z0, double vz, double kpen, double mu,
+                           const int32_t *cand_nodes, int64_t ncand);
+
+int wfo_init(wfo_domain *d);
+int wfo_run(wfo_domain *d, int64_t nsteps);
+/* Steps until Time >= end_t, as `while (Time < end_t)` (Solver_explicit.C:346). */
+int64_t wfo_solve(wfo_domain *d);
+double wfo_time(const wfo_domain *d);
+
+/* Readback. Node vectors: 0 x, 1 v, 2 a, 3 u, 4 prev_a, 5 fi, 6 u_dt, 7 contforce.
+ * Node scalars: 0 mass, 1 voln, 2 p_node. Element scalars: 0 vol, 1 vol0, 2 detJ,
+ * 3 p, 4 pl_strain, 5 sigma_y, 6 rho. Element tensors (Voigt xx,yy,zz,xy,yz,xz):
+ * 0 sigma, 1 tau, 2 eps, 3 str_rate, 4 rot_rate. */
+int wfo_get_node_vec(const wfo_domain *d, int which, double *out);
+int wfo_get_node_scalar(wfo_domain *d, int which, double *out);
+int wfo_get_elem_scalar(const wfo_domain *d, int which, double *out);
+int wfo_get_elem_tensor(const wfo_domain *d, int which, double *out);
+/* dN/dx * detJ as [E][3][npe]. */
+void wfo_get_derivs(const wfo_domain *d, double *out);
+void wfo_get_elem_forces(const wfo_domain *d, double *f, double *fhg);
+int64_t wfo_get_reaction(const wfo_domain *d, double *out, int64_t cap);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

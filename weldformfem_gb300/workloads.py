@@ -1,0 +1,270 @@
+"""Synthetic workloads: box meshes, seeded perturbations, materials and BCs.
+
+The reference publishes no benchmark data set; its test decks are small
+cubes (validation/*.txt, src/common/main_1_elem_3d.C). The workloads here
+are the five configurations of the measurement plan, generated on the host
+from a counter-based RNG so that every backend (the CUDA library, the CPU
+oracle, the reference compiled from source) receives bit-identical inputs:
+
+  C0  10^3 hexahedra, cube of side 10 mm, hourglass 0.1, 5000 steps
+  C1  40x40x60 cells x 6 tetrahedra (576,000), 20x20x30 mm, +-0.15h, 2000 steps
+  C2  256x256x128 hexahedra (8.39 M), h = 1 mm, +-0.1h, rigid die, 1000 steps
+  C3  1024 independent cubes, n ~ U{6..40}, per-specimen material, 2000 steps
+  C4  32^3 hexahedra, 8 octant materials (the C0 cube, h = 0.3125 mm), 4000 steps
+
+Meshes use the numbering of Domain_d::AddBoxLength (Domain_d.C:1136-1504).
+Velocity BCs follow the reference drivers: symmetry planes x=0, y=0, z=0
+(AddBCVelNode with value 0) and a prescribed top velocity. The time step is
+dt = 0.3 * h_min / sqrt(E / rho) with h_min the shortest element edge.
+"""
+from __future__ import annotations
+
+import dataclasses
+from typing import Callable, Optional
+
+import numpy as np
+
+SEED_BASE = 0x5EED0000
+_M64 = (1 << 64) - 1
+
+STEEL = dict(model=0, E=200e9, nu=0.3, rho=7850.0, sy0=300e6, H=1e9)
+
+
+def splitmix64(seed: int, n: int, offset: int = 0) -> np.ndarray:
+    """Counter-based splitmix64 stream: value i is mix(seed + (offset+i+1)*golden)."""
+    with np.errstate(over="ignore"):
+        i = np.arange(offset + 1, offset + n + 1, dtype=np.uint64)
+        z = np.uint64(seed & _M64) + i * np.uint64(0x9E3779B97F4A7C15)
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        z = z ^ (z >> np.uint64(31))
+    return z
+
+
+def uniform_pm1(seed: int, n: int, offset: int = 0) -> np.ndarray:
+    """Uniform doubles in [-1, 1) from the top 53 bits of splitmix64."""
+    z = splitmix64(seed, n, offset) >> np.uint64(11)
+    return z.astype(np.float64) * (2.0 ** -52) - 1.0
+
+
+def box_counts(L, r):
+    """Element counts per axis exactly as AddBoxLength truncates them."""
+    return tuple(int(float(L[k]) / (2.0 * float(r))) for k in range(3))
+
+
+def box_coords(L, r, origin=(0.0, 0.0, 0.0)) -> np.ndarray:
+    """Node coordinates of AddBoxLength: repeated addition of 2r (Domain_d.C:1215-1235)."""
+    nel = box_counts(L, r)
+    xs = []
+    for k, n in enumerate(nel):
+        v = float(origin[k])
+        col = []
+        for _ in range(n + 1):
+            col.append(v)
+            v = v + 2.0 * r
+        xs.append(np.array(col))
+    zz, yy, xx = np.meshgrid(xs[2], xs[1], xs[0], indexing="ij")
+    return np.stack([xx.ravel(), yy.ravel(), zz.ravel()], axis=1)
+
+
+def perturb_interior(x: np.ndarray, nel, h: float, frac: float, seed: int) -> np.ndarray:
+    """Moves every node not on a boundary face by U[-frac h, +frac h] per axis."""
+    nx, ny, nz = (n + 1 for n in nel)
+    idx = np.arange(x.shape[0])
+    i, j, k = idx % nx, (idx // nx) % ny, idx // (nx * ny)
+    interior = (i > 0) & (i < nx - 1) & (j > 0) & (j < ny - 1) & (k > 0) & (k < nz - 1)
+    out = x.copy()
+    sel = np.nonzero(interior)[0]
+    du = uniform_pm1(seed, 3 * sel.size).reshape(-1, 3) * (frac * h)
+    out[sel] += du
+    return out
+
+
+def hex_edges():
+    return [(0, 1), (1, 2), (2, 3), (3, 0), (4, 5), (5, 6), (6, 7), (7, 4),
+            (0, 4), (1, 5), (2, 6), (3, 7)]
+
+
+TET_EDGES = [(0, 1), (0, 2), (0, 3), (1, 2), (1, 3), (2, 3)]
+
+
+def min_edge_length(x: np.ndarray, elnod: np.ndarray) -> float:
+    """Shortest element edge, length = sqrt(dx*dx + dy*dy + dz*dz)."""
+    edges = hex_edges() if elnod.shape[1] == 8 else TET_EDGES
+    best = np.inf
+    for a, b in edges:
+        d = x[elnod[:, b]] - x[elnod[:, a]]
+        ln = np.sqrt(d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1] + d[:, 2] * d[:, 2])
+        best = min(best, float(ln.min()))
+    return best
+
+
+def box_elnod(nel, tritetra: bool) -> np.ndarray:
+    """Connectivity of AddBoxLength (hex x-fastest, optional six-tet split)."""
+    nx, ny, nz = nel
+    nnodz = (nx + 1) * (ny + 1)
+    ez, ey, ex = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    ez, ey, ex = ez.ravel(), ey.ravel(), ex.ravel()
+    nb1 = nnodz * ez + (nx + 1) * ey + ex
+    nb2 = nnodz * ez + (nx + 1) * (ey + 1) + ex
+    h = np.stack([nb1, nb1 + 1, nb2 + 1, nb2, nb1 + nnodz, nb1 + nnodz + 1,
+                  nb2 + nnodz + 1, nb2 + nnodz], axis=1)
+    if not tritetra:
+        return h.astype(np.int32)
+    T = np.array([[0, 1, 3, 5], [1, 2, 3, 5], [0, 5, 3, 4], [4, 5, 3, 7], [5, 6, 3, 7],
+                  [5, 2, 3, 6]])
+    return h[:, T].reshape(-1, 4).astype(np.int32)
+
+
+@dataclasses.dataclass
+class Case:
+    name: str
+    L: tuple
+    r: float
+    tritetra: bool = False
+    perturb: float = 0.0
+    seed: int = SEED_BASE
+    materials: list = dataclasses.field(default_factory=lambda: [dict(STEEL)])
+    elem_mat: Optional[np.ndarray] = None
+    bc: str = "sym_top"          # "sym_top": symmetry + top vz; "bottom_z": bottom fixed in z
+    top_vz: float = -1.0
+    hg: float = 0.0
+    dt: Optional[float] = None   # None: 0.3 h_min / sqrt(E / rho)
+    dt_factor: float = 0.3
+    steps: int = 1
+    contact: Optional[dict] = None   # dict(v=5.0, kfac=10.0, mu=0.1)
+    press_alg: int = 0
+    mass_mode: int = 0
+
+    # derived --------------------------------------------------------
+    @property
+    def nel(self):
+        return box_counts(self.L, self.r)
+
+    @property
+    def h(self):
+        return 2.0 * self.r
+
+    def coords(self) -> np.ndarray:
+        x = box_coords(self.L, self.r)
+        if self.perturb:
+            x = perturb_interior(x, self.nel, self.h, self.perturb, self.seed)
+        return x
+
+    def elnod(self) -> np.ndarray:
+        return box_elnod(self.nel, self.tritetra)
+
+    @property
+    def n_elem(self):
+        nx, ny, nz = self.nel
+        return nx * ny * nz * (6 if self.tritetra else 1)
+
+    @property
+    def n_node(self):
+        nx, ny, nz = self.nel
+        return (nx + 1) * (ny + 1) * (nz + 1)
+
+    def time_step(self, x=None) -> float:
+        if self.dt is not None:
+            return float(self.dt)
+        if x is None:
+            x = self.coords()
+        hmin = min_edge_length(x, self.elnod()) if self.perturb else self.h
+        m = self.materials[0]
+        return self.dt_factor * hmin / np.sqrt(m["E"] / m["rho"])
+
+    def bcs(self, x0=None):
+        """Velocity BC list (node, dof, value) in node order."""
+        if x0 is None:
+            x0 = box_coords(self.L, self.r)
+        nx, ny, nz = (n + 1 for n in self.nel)
+        idx = np.arange(x0.shape[0])
+        i, j, k = idx % nx, (idx // nx) % ny, idx // (nx * ny)
+        out = []
+        if self.bc == "sym_top":
+            for n in idx:
+                if i[n] == 0:
+                    out.append((int(n), 0, 0.0))
+                if j[n] == 0:
+                    out.append((int(n), 1, 0.0))
+                if k[n] == 0:
+                    out.append((int(n), 2, 0.0))
+                if k[n] == nz - 1:
+                    out.append((int(n), 2, float(self.top_vz)))
+        elif self.bc == "bottom_z":
+            for n in idx[k == 0]:
+                out.append((int(n), 2, 0.0))
+        else:
+            raise ValueError(self.bc)
+        return out
+
+    def top_nodes(self) -> np.ndarray:
+        nx, ny, nz = (n + 1 for n in self.nel)
+        return np.arange(nx * ny * (nz - 1), nx * ny * nz, dtype=np.int32)
+
+    def contact_params(self):
+        c = self.contact
+        m = self.materials[0]
+        return dict(z0=float(self.L[2]), vz=-float(c["v"]), kpen=float(c["kfac"]) * m["E"] * self.h,
+                    mu=float(c["mu"]))
+
+
+def apply(dom, case: Case, x=None, with_bcs=True):
+    """Sets up any domain backend (same method names) for `case` and returns dt."""
+    dom.add_box(case.L, case.r, case.tritetra)
+    if x is None:
+        x = case.coords()
+    if case.perturb:
+        dom.set_nodes(x)
+    dom.set_materials(case.materials, case.elem_mat)
+    if with_bcs:
+        dom.add_bcs(case.bcs())
+    if case.hg:
+        dom.set_hourglass(case.hg)
+    if case.press_alg:
+        dom.set_press_algorithm(case.press_alg)
+    if case.mass_mode and hasattr(dom, "set_mass_mode"):
+        dom.set_mass_mode(case.mass_mode)
+    if case.contact:
+        cp = case.contact_params()
+        dom.set_contact_plane(cp["z0"], cp["vz"], cp["kpen"], cp["mu"], case.top_nodes())
+    else:
+        dom.set_reaction_nodes(case.top_nodes(), 2)
+    dt = case.time_step(x)
+    dom.set_dt(dt)
+    return dt
+
+
+def octant_ids(case: Case) -> np.ndarray:
+    """Octant index (0..7) of each hexahedron of a box case, x-fastest bits."""
+    nx, ny, nz = case.nel
+    ez, ey, ex = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    return ((ex.ravel() >= nx // 2).astype(np.int32) + 2 * (ey.ravel() >= ny // 2)
+            + 4 * (ez.ravel() >= nz // 2)).astype(np.int32)
+
+
+def config(cid: int, steps: Optional[int] = None, scale: Optional[tuple] = None) -> Case:
+    """The named configurations; `scale` overrides the cell counts (same h)."""
+    if cid == 0:
+        c = Case("C0 hex 10^3", L=(0.01, 0.01, 0.01), r=0.0005, hg=0.1, steps=5000)
+    elif cid == 1:
+        c = Case("C1 tet 40x40x60x6", L=(0.02, 0.02, 0.03), r=0.00025, tritetra=True,
+                 perturb=0.15, seed=SEED_BASE + 1, steps=2000)
+    elif cid == 2:
+        c = Case("C2 hex 256x256x128 die", L=(0.256, 0.256, 0.128), r=0.0005, perturb=0.1,
+                 seed=SEED_BASE + 2, hg=0.1, bc="bottom_z",
+                 contact=dict(v=5.0, kfac=10.0, mu=0.1), steps=1000)
+    elif cid == 4:
+        c = Case("C4 hex 32^3 octants", L=(0.01, 0.01, 0.01), r=0.00015625, hg=0.1, steps=4000)
+        c.materials = [dict(STEEL) for _ in range(8)]
+        c.elem_mat = octant_ids(c)
+    else:
+        raise ValueError(f"unknown configuration {cid}")
+    if scale is not None:
+        h = c.h
+        c.L = tuple(float(n) * h for n in scale)
+        if c.elem_mat is not None:
+            c.elem_mat = octant_ids(c)
+    if steps is not None:
+        c.steps = steps
+    return c
