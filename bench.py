@@ -1,0 +1,373 @@
+"""Benchmark of the explicit step on the roofline workload (one JSON line).
+
+Workload (default): the rigid-die compression case, 256 x 256 x 128
+reduced-integration hexahedra (8,388,608 elements, 8,520,321 nodes, h = 1 mm,
+interior nodes perturbed by +-0.1 h), viscous hourglass 0.1, penalty plane
+contact with Coulomb friction 0.1, mixed precision (FP32 element arithmetic,
+compensated positions, FP64 reaction sums). One "step" is one explicit time
+step over the whole mesh. The same steps are run in FP64 for the
+mixed/FP64 ratio and the error of the mixed path against FP64.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+`--impl reference` times the CPU implementation of the reference's loop on
+the host cores (the C restatement in oracle/, all cores) on a bounded
+sample of the same workload and prints the same line with impl=reference.
+Under torchrun (N > 1) the workload does not shard: every rank runs an
+independent replica on its own GPU and the value is the total over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+from weldformfem_gb300 import workloads as W  # noqa: E402
+
+METRIC = "element-steps/s"
+UNIT = "element-steps/s"
+
+# Algorithmic bytes per launch of each phase, per element (E) and per node (N)
+# of the mixed-precision hexahedral kernels: every array touched once.
+#   geometry: elnod 32 E + positions 24 N + volume 4 E
+#   nodal   : offsets 4 N + slots 32 E + volume 4 E + node constants 8 N + J ratio, mass 8 N
+#   elements: elnod 32 E + positions 24 N + predicted velocity 12 N + J ratio 4 N
+#             + deviatoric stress RW 48 E + plastic strain RW 8 E + element forces 96 E
+#   nodes   : offsets 4 N + slots 32 E + element forces 96 E + BC code, flags, mass 9 N
+#             + positions RW 48 N + velocity RW 24 N + accel RW 24 N + predicted velocity 12 N
+PHASES = ["geometry", "nodal", "elements", "nodes"]
+ALG_BYTES_HEX_MIXED = {"geometry": (36, 24), "nodal": (36, 20), "elements": (184, 40),
+                       "nodes": (128, 121)}
+# FP64 state per element-step (SURVEY-style compulsory bytes), for reference.
+KERNEL_NAMES = {"geometry": "k_geometry", "nodal": "k_nodal", "elements": "k_elements",
+                "nodes": "k_nodes"}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[3:7]):
+                if val.lower() in ("active", "1"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            j = json.load(f)
+        return float(j["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def kernel_traffic(phase):
+    """DRAM bytes per launch from the committed ncu summary, if present."""
+    p = os.path.join(ROOT, "profiles", "kernel_traffic.txt")
+    try:
+        for ln in open(p):
+            parts = ln.split()
+            if len(parts) >= 2 and parts[0] == phase:
+                return float(parts[1])
+    except OSError:
+        pass
+    return None
+
+
+def build_domain(wf, case, prec, x, device):
+    d = wf.Domain(prec, device=device)
+    W.apply(d, case, x=x)
+    d.init()
+    d.sync()
+    return d
+
+
+def run_ours(args):
+    import torch
+
+    import weldformfem_gb300 as wf
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    device = local
+    torch.cuda.set_device(device)
+    case = W.config(args.config, scale=tuple(args.scale) if args.scale else None)
+    K, Wm = args.steps, args.warmup
+    x = case.coords()
+    E = case.n_elem
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+
+    # ---- mixed precision, graph launches: the headline -------------------------
+    dm = build_domain(wf, case, wf.WF_MIXED, x, device)
+    dm.run(Wm)
+    dm.sync()
+    stream = torch.cuda.ExternalStream(dm.stream_handle(), device=device)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = ClockSampler(device)
+    barrier()
+    torch.cuda.synchronize(device)
+    launches0 = dm.launch_count()
+    clocks.start()
+    ev0.record(stream)
+    dm.run(K)
+    ev1.record(stream)
+    ev1.synchronize()
+    torch.cuda.synchronize(device)
+    clk = clocks.stop()
+    barrier()
+    ms_total = ev0.elapsed_time(ev1)
+    launches = dm.launch_count() - launches0
+    # per-phase breakdown (direct launches, CUDA events around each kernel)
+    dm.set_phase_timing(True)
+    kp = max(10, min(K, 100))
+    dm.run(kp)
+    ms_phase, nph = dm.phase_times()
+    dm.set_phase_timing(False)
+    ms_phase = ms_phase / max(nph, 1)
+
+    # ---- FP64 plain: same steps from the same initial state ----------------------
+    df = build_domain(wf, case, wf.WF_FP64, x, device)
+    df.run(Wm)
+    df.sync()
+    fstream = torch.cuda.ExternalStream(df.stream_handle(), device=device)
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record(fstream)
+    df.run(K)
+    f1.record(fstream)
+    f1.synchronize()
+    ms_fp64 = f0.elapsed_time(f1)
+
+    # errors of mixed vs FP64 over the first W + K steps (same inputs)
+    nrun = Wm + K
+    rm, rf = dm.reaction()[:nrun], df.reaction()[:nrun]
+    um, uf = None, None
+    dm2 = build_domain(wf, case, wf.WF_MIXED, x, device)
+    dm2.run(nrun)
+    um, uf = dm2.node_vec("u"), df.node_vec("u")
+    plm, plf = dm2.elem_scalar("pl_strain"), df.elem_scalar("pl_strain")
+    rel = lambda a, b: float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+    err = {"reaction": rel(rm, rf), "displacement": rel(um, uf),
+           "pl_strain": rel(plm, plf) if np.max(np.abs(plf)) > 0 else 0.0,
+           "steps": nrun}
+    del dm2, df
+
+    # ---- end to end through the C ABI from host buffers ------------------------------
+    torch.cuda.synchronize(device)
+    t0 = time.perf_counter()
+    de = wf.Domain(wf.WF_MIXED, device=device)
+    de.set_mesh(x, case.elnod())
+    W.apply_options(de, case, x=x)
+    de.init()
+    de.run(K)
+    u_host = de.node_vec("u")
+    r_host = de.reaction()
+    de.sync()
+    t_e2e = time.perf_counter() - t0
+    h2d, d2h = de.transfer_bytes()
+    assert u_host.shape[0] == case.n_node and r_host.shape[0] == K
+    del de
+
+    # ---- aggregate over ranks ---------------------------------------------------------------
+    ms_step = ms_total / K
+    if world > 1:
+        import torch.distributed as dist
+
+        t = torch.tensor([ms_total, t_e2e], dtype=torch.float64, device=f"cuda:{device}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_total, t_e2e = float(t[0]), float(t[1])
+        ms_step = ms_total / K
+    value = world * E * K / (ms_total * 1e-3)
+    fp64_value = E * K / (ms_fp64 * 1e-3)
+
+    # ---- roofline of the dominant kernel -------------------------------------------------
+    peak, peak_kind = measured_peak()
+    dom = int(np.argmax(ms_phase))
+    ph = PHASES[dom]
+    be, bn = ALG_BYTES_HEX_MIXED[ph]
+    alg_bytes = be * E + bn * case.n_node
+    achieved = alg_bytes / (ms_phase[dom] * 1e-3) / 1e9
+    roof = {"bound": "hbm", "kernel": KERNEL_NAMES[ph], "achieved": round(achieved, 1),
+            "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "traffic": kernel_traffic(ph),
+            "alg_bytes_per_launch": alg_bytes, "ms_per_launch": round(float(ms_phase[dom]), 4),
+            "phases_ms": {p: round(float(m), 4) for p, m in zip(PHASES, ms_phase)}}
+    step_alg = sum(ALG_BYTES_HEX_MIXED[p][0] * E + ALG_BYTES_HEX_MIXED[p][1] * case.n_node
+                   for p in PHASES)
+    roof["step_achieved_gbs"] = round(step_alg / (ms_step * 1e-3) / 1e9, 1)
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_baseline(case, x, args.cpu_steps)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world,
+            "steps": K, "warmup": Wm, "ms_per_step": round(ms_step, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 (f64-compensated positions, f64 reaction sums)", "data": "synthetic",
+            "config": {"workload": case.name, "elements": E, "nodes": case.n_node,
+                       "precision": "mixed", "parallelism": "replicas" if world > 1 else "single",
+                       "l2": "working set ~3.5 GB per replica, larger than L2; no flush"},
+            "fp64": {"value": round(fp64_value, 1), "ms_per_step": round(ms_fp64 / K, 4)},
+            "mixed_over_fp64": round(value / world / fp64_value, 3),
+            "error_vs_fp64": err,
+            "e2e": {"value": round(E * K / t_e2e, 1), "unit": UNIT,
+                    "h2d_bytes_per_step": int(h2d / K), "d2h_bytes_per_step": int(d2h / K),
+                    "seconds": round(t_e2e, 3),
+                    "includes": "mesh upload, init, K steps, displacement + reaction readback"},
+            "gpu_launches": int(launches),
+            "roofline": roof,
+            "cpu_baseline": cpu,
+            "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+def cpu_baseline(case, x, steps):
+    """The oracle (C restatement of the reference loop) on all host cores."""
+    from oracle import orabind
+
+    threads = os.cpu_count() or 1
+    d = orabind.OracleDomain(threads=threads)
+    W.apply(d, case, x=x)
+    d.init()
+    t0 = time.perf_counter()
+    d.step(steps)
+    t = time.perf_counter() - t0
+    return {"value": round(case.n_elem * steps / t, 1), "unit": UNIT, "cores": threads,
+            "kind": "port", "sample": f"{case.name}: {steps} steps on the full mesh, setup excluded"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    case = W.config(args.config, scale=tuple(args.scale) if args.scale else None)
+    x = case.coords()
+    from oracle import orabind
+
+    threads = os.cpu_count() or 1
+    d = orabind.OracleDomain(threads=threads)
+    W.apply(d, case, x=x)
+    d.init()
+    d.step(max(1, min(args.warmup, 1)))
+    # each step is one full time step of the workload; the count is bounded so
+    # that the run ends within a few minutes on the host cores
+    t0 = time.perf_counter()
+    d.step(1)
+    per = time.perf_counter() - t0
+    n = int(max(1, min(args.steps, 60.0 / max(per, 1e-9))))
+    t0 = time.perf_counter()
+    d.step(n)
+    t = time.perf_counter() - t0
+    value = case.n_elem * n / t
+    line = {
+        "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": 0, "steps": n,
+        "warmup": 2, "ms_per_step": round(t / n * 1e3, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "impl": "reference",
+        "config": {"workload": case.name, "elements": case.n_elem, "nodes": case.n_node,
+                   "precision": "fp64"},
+        "cpu_baseline": {"value": round(value, 1), "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{n} time steps of the full workload (bounded to ~60 s)"},
+        "e2e": {"value": round(value, 1), "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", type=int, default=2)
+    ap.add_argument("--scale", type=int, nargs=3, default=None)
+    ap.add_argument("--cpu-steps", type=int, default=2)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,206 @@
+/* weldform-gb300: C ABI of the GB300 explicit updated-Lagrangian step.
+ *
+ * Drop-in for the solve loop of the reference's MetFEM::Domain_d
+ * (include/common/Domain_d.h:231-1044, loop in src/explicit/Solver_explicit.C:
+ * 101-1271). Each entry point names the reference member it replaces.
+ *
+ * Conventions
+ *  - Every function returns wf_status; none exits or prints. wf_last_error()
+ *    gives a one-line message for the last failing call on a domain.
+ *  - Host pointers are borrowed for the duration of the call only. Device
+ *    memory is owned by the library; one CUDA stream per domain. A domain
+ *    handle is not thread-safe.
+ *  - Node vectors are interleaved x[3n+d] and element tensors are Voigt
+ *    [xx, yy, zz, xy, yz, xz], as the reference's arrays (Domain_d.h:841-1043).
+ *  - Precision: WF_FP64 computes every quantity in FP64 with the reference's
+ *    operation order; WF_MIXED computes element arithmetic in FP32 and keeps
+ *    FP64 for nodal positions, displacements, the time step and reaction sums.
+ */
+#ifndef WF_H
+#define WF_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define WF_API __attribute__((visibility("default")))
+#else
+#define WF_API
+#endif
+
+typedef enum {
+  WF_OK = 0,
+  WF_ERR_ARG = 1,         /* invalid argument (null, out of range, wrong size) */
+  WF_ERR_STATE = 2,       /* call out of order (e.g. run before init) */
+  WF_ERR_CUDA = 3,        /* CUDA runtime error (no device, launch failure) */
+  WF_ERR_NOMEM = 4,       /* host or device allocation failed */
+  WF_ERR_UNSUPPORTED = 5, /* option not supported in the selected mode */
+  WF_ERR_NONFINITE = 6,   /* non-finite state detected by the device checks */
+  WF_ERR_TIMEOUT = 7      /* a bounded device wait ran out */
+} wf_status;
+
+typedef enum { WF_FP64 = 0, WF_MIXED = 1 } wf_precision;
+
+typedef enum { WF_MAT_BILINEAR = 0, WF_MAT_HOLLOMON = 1 } wf_material_model;
+
+/* Material_ + Elastic_ (include/common/Material.cuh:15-156). BILINEAR is
+ * linear isotropic hardening sigma_y = sy0 + H eps_p. HOLLOMON is the
+ * reference law sigma_y = K (eps_p + sy0/E)^m past the plateau
+ * (Material.cuh:353-395). cs0 = sqrt(K_bulk / rho) as the reference drivers
+ * set it (src/explicit/main.C:507). */
+typedef struct {
+  int32_t model;
+  double E, nu, rho;
+  double sy0, H;
+  double hol_K, hol_m;
+} wf_material;
+
+/* StabilizationParams (Domain_d.h:139-152), used by pressure algorithm 0;
+ * all zero by default as in the reference constructor (Domain_d.h:292-303). */
+typedef struct {
+  double alpha_free, alpha_contact, hg_coeff_free, hg_coeff_contact;
+  double av_coeff_div, av_coeff_bulk, log_factor, pspg_scale, p_pspg_bulkfac, J_min;
+} wf_stab;
+
+/* Node vector fields for wf_get_node_field. */
+enum {
+  WF_NODE_X = 0, WF_NODE_V = 1, WF_NODE_A = 2, WF_NODE_U = 3, WF_NODE_PREV_A = 4,
+  WF_NODE_FI = 5, WF_NODE_CONTFORCE = 7
+};
+/* Node scalar fields. */
+enum { WF_NODE_MASS = 0, WF_NODE_VOLN = 1, WF_NODE_PRESSURE = 2 };
+/* Element scalar fields. */
+enum {
+  WF_ELEM_VOL = 0, WF_ELEM_VOL0 = 1, WF_ELEM_DETJ = 2, WF_ELEM_P = 3,
+  WF_ELEM_PL_STRAIN = 4, WF_ELEM_SIGMA_Y = 5, WF_ELEM_RHO = 6
+};
+/* Element tensor fields (Voigt, 6 per element). */
+enum { WF_ELEM_SIGMA = 0, WF_ELEM_TAU = 1, WF_ELEM_EPS = 2, WF_ELEM_STR_RATE = 3, WF_ELEM_ROT_RATE = 4 };
+
+typedef struct wf_domain wf_domain;
+
+/* Domain_d::Domain_d (Domain_d.h:245). Selects device 0 unless
+ * wf_domain_create_on_device is used. */
+WF_API wf_status wf_domain_create(wf_domain **out);
+WF_API wf_status wf_domain_create_on_device(wf_domain **out, int device);
+/* Domain_d::Free (Domain_d.C:786-900). */
+WF_API wf_status wf_domain_destroy(wf_domain *d);
+WF_API const char *wf_last_error(const wf_domain *d);
+WF_API const char *wf_status_string(wf_status s);
+WF_API int32_t wf_abi_version(void);
+
+/* ---- mesh ---------------------------------------------------------------- */
+/* Domain_d::AddBoxLength(V, L, r, red_int, tritetra) (Domain_d.C:1136-1504):
+ * structured box of hexahedra (tritetra = 0) or six tetrahedra per cell,
+ * same node and element numbering, node->element lists element-ascending.
+ * Only 3-D, one-point integration (red_int != 0) is supported. */
+WF_API wf_status wf_add_box_length(wf_domain *d, const double V[3], const double L[3], double r,
+                                   int32_t red_int, int32_t tritetra);
+/* Domain_d::CreateFromLSDyna / setNodElem (Domain_d.C:1508-1699): explicit
+ * nodes (xyz[3*nn]) and connectivity (elnod[ne*npe], npe = 8 or 4). */
+WF_API wf_status wf_set_mesh(wf_domain *d, int64_t nn, int64_t ne, int32_t npe, const double *xyz,
+                             const int32_t *elnod);
+/* Domain_d::setNode (Domain_d.C:2473) for one node, and for all nodes. */
+WF_API wf_status wf_set_node(wf_domain *d, int64_t n, double x, double y, double z);
+WF_API wf_status wf_set_nodes(wf_domain *d, const double *xyz);
+/* getNodeCount / getElemCount (Domain_d.h:561-563). */
+WF_API wf_status wf_get_sizes(const wf_domain *d, int64_t *nn, int64_t *ne, int32_t *npe,
+                              int64_t *nodel_total);
+/* m_elnod, m_nodel, m_nodel_loc, m_nodel_offset, m_nodel_count (Domain_d.h:961-965). */
+WF_API wf_status wf_get_connectivity(const wf_domain *d, int32_t *elnod, int32_t *nodel,
+                                     int32_t *nodel_loc, int32_t *offset, int32_t *count);
+
+/* ---- material ------------------------------------------------------------ */
+/* Domain_d::setDensity (Domain_d.C:952). */
+WF_API wf_status wf_set_density(wf_domain *d, double rho);
+/* Domain_d::AssignMaterial (Domain_d.C:903): material table; entry 0 is the
+ * default of every element. Sets the density of every element to mats[0].rho. */
+WF_API wf_status wf_set_materials(wf_domain *d, int32_t nmat, const wf_material *mats);
+/* Per-element material index (the reference's mat[e] pointers). */
+WF_API wf_status wf_set_elem_materials(wf_domain *d, const int32_t *ids);
+
+/* ---- boundary conditions -------------------------------------------------- */
+/* Domain_d::AddBCVelNode (Domain_d.C:1057). */
+WF_API wf_status wf_add_bc_vel_node(wf_domain *d, int64_t node, int32_t dim, double val);
+/* Domain_d::AddBCVelZone (Domain_d.C:432-452); *count = nodes inside. */
+WF_API wf_status wf_add_bc_vel_zone(wf_domain *d, const double start[3], const double end[3],
+                                    const double vel[3], int64_t *count);
+/* Domain_d::AllocateBCs (Domain_d.C:1063). */
+WF_API wf_status wf_allocate_bcs(wf_domain *d);
+
+/* ---- options ---------------------------------------------------------------- */
+WF_API wf_status wf_set_dt(wf_domain *d, double dt);         /* SetDT (Domain_d.h:635) */
+WF_API wf_status wf_set_end_time(wf_domain *d, double t);    /* SetEndTime (Domain_d.h:636) */
+WF_API wf_status wf_set_precision(wf_domain *d, int32_t precision);
+/* Viscous hourglass coefficient of 1-point hexahedra (0 = off): the 3-D form
+ * of the reference's test driver (src/common/test_1el_3D.cpp:159-199). */
+WF_API wf_status wf_set_hourglass(wf_domain *d, double coef);
+/* m_press_algorithm (Domain_d.h:672): 0 = nodal-averaged J (default), 1 = ANP. */
+WF_API wf_status wf_set_press_algorithm(wf_domain *d, int32_t alg);
+WF_API wf_status wf_set_stab(wf_domain *d, const wf_stab *s);          /* m_stab */
+WF_API wf_status wf_set_artif_visc(wf_domain *d, double alpha, double beta); /* m_artifvisc */
+/* 0: lumped mass recomputed each step from the current volume (reference
+ * loop, Solver_explicit.C:605-607); 1: mass kept at its initial value. */
+WF_API wf_status wf_set_mass_mode(wf_domain *d, int32_t mode);
+/* Reaction history: per step, sum over `nodes` of the assembled internal
+ * force component `dim` (recorded after assembly). */
+WF_API wf_status wf_set_reaction_nodes(wf_domain *d, int64_t n, const int32_t *nodes, int32_t dim);
+/* Rigid flat die with outward normal -z at z = z0 + vz*t, acting on the
+ * candidate nodes (Domain_d::CalcContactForces, Contact.C:31-334, for one
+ * plane): normal stiffness min(kpen, 0.2 m / dt^2) as the reference caps it,
+ * Coulomb coefficient mu. With contact on, the reaction history records the
+ * sum of normal contact forces. */
+WF_API wf_status wf_set_contact_plane(wf_domain *d, double z0, double vz, double kpen, double mu,
+                                      int64_t ncand, const int32_t *cand_nodes);
+
+/* ---- run ---------------------------------------------------------------------- */
+/* Preamble of SolveChungHulbert (Solver_explicit.C:120-268): uploads the
+ * mesh, imposes initial BCs, computes initial geometry, volumes and masses. */
+WF_API wf_status wf_init(wf_domain *d);
+/* nsteps iterations of the loop body (Solver_explicit.C:346-1167). */
+WF_API wf_status wf_run(wf_domain *d, int64_t nsteps);
+/* Domain_d::SolveChungHulbert: steps while Time < end time; *nsteps = count. */
+WF_API wf_status wf_solve(wf_domain *d, int64_t *nsteps);
+WF_API wf_status wf_get_time(const wf_domain *d, double *t, int64_t *step);
+/* Waits for the domain's stream and reports any device-side error status. */
+WF_API wf_status wf_sync(wf_domain *d);
+/* Minimum element edge length of the current mesh (device reduction). */
+WF_API wf_status wf_min_edge_length(wf_domain *d, double *hmin);
+/* Per-phase timing. While on, wf_run launches the four kernels of each step
+ * directly (no graph) with CUDA events around each, on the domain's stream.
+ * wf_get_phase_times returns the accumulated milliseconds of the geometry,
+ * nodal, element and node phases (ms[4]) and the steps timed; reset != 0
+ * clears the accumulators after reading. */
+WF_API wf_status wf_set_phase_timing(wf_domain *d, int32_t on);
+WF_API wf_status wf_get_phase_times(wf_domain *d, double ms[4], int64_t *steps, int32_t reset);
+/* Number of kernels this domain has launched since wf_init (graph nodes
+ * included). */
+WF_API wf_status wf_get_launch_count(const wf_domain *d, int64_t *n);
+/* The domain's CUDA stream (a cudaStream_t), for callers that order their
+ * own work or CUDA events after the domain's kernels. */
+WF_API wf_status wf_get_stream(const wf_domain *d, void **stream);
+/* Bytes copied host->device and device->host by this domain so far. */
+WF_API wf_status wf_get_transfer_bytes(const wf_domain *d, int64_t *h2d, int64_t *d2h);
+
+/* ---- readback (host buffers) -------------------------------------------------- */
+WF_API wf_status wf_get_node_field(wf_domain *d, int32_t field, double *out);   /* 3*nn */
+WF_API wf_status wf_get_node_scalar(wf_domain *d, int32_t field, double *out);  /* nn */
+WF_API wf_status wf_get_elem_scalar(wf_domain *d, int32_t field, double *out);  /* ne */
+WF_API wf_status wf_get_elem_tensor(wf_domain *d, int32_t field, double *out);  /* 6*ne */
+/* getDispVec / getVelVec over all nodes (Domain_d.h:476-489). */
+WF_API wf_status wf_get_disp(wf_domain *d, double *out);
+WF_API wf_status wf_get_vel(wf_domain *d, double *out);
+WF_API wf_status wf_get_pl_strain(wf_domain *d, double *out);
+/* Reaction history since wf_init: *n = steps recorded; copies min(cap, *n). */
+WF_API wf_status wf_get_reaction_history(wf_domain *d, double *out, int64_t cap, int64_t *n);
+/* Overwrites the nodal state (x, v, prev_a, u; any may be null) from host. */
+WF_API wf_status wf_set_node_state(wf_domain *d, const double *x, const double *v,
+                                   const double *prev_a, const double *u);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* WF_H */

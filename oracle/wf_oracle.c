@@ -834,20 +834,20 @@ static void calc_hourglass(wfo_domain *d) {
  * normal force -(k d + 0.2 c_crit v_n) n with c_crit = 2 m sqrt(k / m),
  * tangential trial force -k * (accumulated slip), capped at mu |F_n| in the
  * sliding direction (slip reset when sliding). The stiffness is the given
- * penalty k (instead of min(E A / l, 0.2 m / dt^2)); forces of candidate
+ * penalty k in place of E A / l, still capped at 0.2 m / dt^2; forces of candidate
  * nodes out of contact are cleared (the reference keeps stale values). The
  * per-node normal-force magnitude feeds the contact reaction (Contact.C:326). */
 static void calc_contact(wfo_domain *d) {
   const double dt = d->dt;
   const double zd = d->c_z0 + d->c_vz * d->time;
   const double nz = -1.0;
-  const double k = d->c_kpen;
+  const double kpen = d->c_kpen;
   OMP_FOR
   for (int64_t i = 0; i < d->nn; i++) {
     d->cfn[i] = 0.0;
     if (!d->cand[i]) continue;
     double *cf = &d->contforce[3 * i];
-    double gap = nz * d->x[3 * i + 2] - nz * zd;
+    double gap = zd - d->x[3 * i + 2];
     if (!(gap < 0)) {
       cf[0] = cf[1] = cf[2] = 0.0;
       continue;
@@ -855,6 +855,10 @@ static void calc_contact(wfo_domain *d) {
     double m = d->mass[i];
     const double *vi = &d->v[3 * i];
     double v_reln = vi[2] * nz;
+    /* kcont = min(k_geometric, 0.2 m / dt^2) (Contact.C:190-193), with the
+     * given penalty as the geometric stiffness */
+    double kmass = 0.2 * m / (dt * dt);
+    double k = (kmass < kpen) ? kmass : kpen;
     double omega = sqrt(k / m);
     double ccrit = 2.0 * m * omega;
     double F_damp = 0.2 * ccrit * v_reln;

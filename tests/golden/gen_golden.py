@@ -1,0 +1,153 @@
+"""Generates the golden fixtures under tests/golden/ from the reference itself.
+
+Runs the reference WeldFormFEM CPU code, compiled from its own sources into
+oracle/_ref/libwfref.so (oracle/build_ref.sh), on small cases and stores the
+results as .npz files; also extracts the known-answer values of the
+reference's validation/ files into validation_kats.json. The fixtures travel
+with the repository so that tests can pin the oracle where the reference
+checkout is absent.
+
+Usage: python tests/golden/gen_golden.py /path/to/reference
+"""
+from __future__ import annotations
+
+import json
+import os
+import re
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle import refbind as R  # noqa: E402
+from weldformfem_gb300 import workloads as W  # noqa: E402
+
+HOLLOMON = dict(model=1, E=200e9, nu=0.3, rho=7850.0, sy0=300e6, hol_K=600e6, hol_m=0.2)
+STAB = [0.3, 0.7, 0.2, 0.08, 0.15, 0.15, 0.8, 0.2, 0.05, 0.0]
+
+
+def cases():
+    """(name, Case, steps, mode, extra) with mode 'step' (harness loop) or 'verbatim'."""
+    out = []
+    c = W.config(0, scale=(4, 4, 4))
+    out.append(("hex4_hg_linear", c, 300, "step", dict(linear=True)))
+    c = W.config(1, scale=(3, 3, 4))
+    out.append(("tet3x3x4_linear", c, 300, "step", dict(linear=True)))
+    c = W.config(0, scale=(3, 3, 3))
+    c.hg = 0.0
+    c.materials = [dict(HOLLOMON)]
+    out.append(("hex3_hollomon_verbatim", c, 400, "verbatim", {}))
+    c = W.config(0, scale=(2, 2, 3))
+    c.hg = 0.0
+    c.tritetra = True
+    c.materials = [dict(HOLLOMON)]
+    out.append(("tet2x2x3_hollomon_verbatim", c, 400, "verbatim", {}))
+    c = W.config(1, scale=(2, 3, 3))
+    c.press_alg = 1
+    c.materials = [dict(HOLLOMON)]
+    # pressure algorithm 1 accumulates the element pressure across steps and
+    # diverges within a few dozen steps (as in the reference): pin 12 steps
+    out.append(("tet_anp_alg1", c, 12, "step", {}))
+    c = W.config(0, scale=(3, 3, 4))
+    c.perturb = 0.1
+    c.seed = W.SEED_BASE + 7
+    c.materials = [dict(HOLLOMON)]
+    out.append(("hex_stab_av", c, 200, "step", dict(stab=STAB, av=(0.2, 0.1))))
+    c = W.config(4, scale=(4, 4, 4))
+    mats = []
+    for i in range(8):
+        m = dict(W.STEEL)
+        m["E"] *= 0.9 + 0.03 * i
+        m["sy0"] *= 0.8 + 0.05 * i
+        m["H"] *= 0.7 + 0.1 * i
+        mats.append(m)
+    c.materials = mats
+    out.append(("hex_octants_linear", c, 300, "step", dict(linear=True)))
+    return out
+
+
+def run_case(name, case, steps, mode, extra):
+    d = R.RefDomain()
+    dt = W.apply(d, case)
+    if extra.get("linear"):
+        d.set_linear_hardening(True)
+    if "stab" in extra:
+        d.set_stab(np.array(extra["stab"], float))
+    if "av" in extra:
+        d.set_artif_visc(*extra["av"])
+    if mode == "verbatim":
+        d.set_end_time(steps * dt)
+        with tempfile.TemporaryDirectory() as td:
+            d.solve_verbatim(td)
+    else:
+        d.init()
+        d.step(steps)
+    elnod, nodel, loc, off, cnt = d.conn()
+    res = dict(
+        dt=np.float64(dt), steps=np.int64(steps),
+        elnod=elnod, nodel=nodel, nodel_loc=loc, nodel_offset=off, nodel_count=cnt,
+        x=d.node_vec("x"), u=d.node_vec("u"), v=d.node_vec("v"), a=d.node_vec("a"),
+        fi=d.node_vec("fi"), mass=d.node_scalar("mass"),
+        vol=d.elem_scalar("vol"), p=d.elem_scalar("p"), pl_strain=d.elem_scalar("pl_strain"),
+        sigma=d.elem_tensor("sigma"), tau=d.elem_tensor("tau"), eps=d.elem_tensor("eps"),
+        p_node=d.node_scalar("p_node"),
+    )
+    if mode == "step":
+        res["reaction"] = d.reaction()
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **res)
+    meta = dict(name=name, mode=mode, steps=steps, extra={k: list(v) if isinstance(v, tuple) else v
+                                                           for k, v in extra.items()})
+    return meta
+
+
+def parse_validation(ref_root):
+    """Known-answer values of validation/1elem_3d_red_int_f_0.06.txt and
+    validation/1step_red_int_cube3D_hf_c_0.06.txt (one 0.1 m hexahedron)."""
+    txt = open(os.path.join(ref_root, "validation", "1elem_3d_red_int_f_0.06.txt")).read()
+
+    def block(after, title, rows=8):
+        i = txt.index(after)
+        j = txt.index(title, i)
+        lines = txt[j:].splitlines()[1:1 + rows]
+        return [[float(v) for v in ln.split()] for ln in lines]
+
+    kats = {
+        "source": "validation/1elem_3d_red_int_f_0.06.txt, "
+                  "validation/1step_red_int_cube3D_hf_c_0.06.txt",
+        "hg006_disp": block("C++", "DISPLACEMENTS"),
+        "hg006_vel": block("C++", "VELOCITIES"),
+        "nohg_disp": block("NO HG", "DISPLACEMENTS"),
+        "nohg_vel": block("NO HG", "VELOCITIES"),
+    }
+    t1 = open(os.path.join(ref_root, "validation", "1step_red_int_cube3D_hf_c_0.06.txt")).read()
+    i = t1.index("INITIAL DERIVATIVE MATRIX")
+    rows = t1[i:].splitlines()[1:4]
+    kats["dHdxy_detJ"] = [[float(v) for v in r.split()] for r in rows]
+    m = re.search(r"dt\s*=\s*([0-9.eE+-]+)", txt + t1)
+    kats["dt"] = 0.8e-5 if m is None else float(m.group(1))
+    kats["setup"] = dict(L=0.1, r=0.05, E=206e9, nu=0.3, rho=7850.0, dt=0.8e-5, t_end=1.0e-3,
+                         hg=0.06)
+    return kats
+
+
+def main():
+    if len(sys.argv) < 2:
+        print(__doc__)
+        sys.exit(2)
+    ref_root = sys.argv[1]
+    subprocess.check_call([os.path.join(ROOT, "oracle", "build_ref.sh"), ref_root])
+    metas = [run_case(*c) for c in cases()]
+    with open(os.path.join(HERE, "cases.json"), "w") as f:
+        json.dump(metas, f, indent=1)
+    with open(os.path.join(HERE, "validation_kats.json"), "w") as f:
+        json.dump(parse_validation(ref_root), f, indent=1)
+    print("wrote", len(metas), "fixtures")
+
+
+if __name__ == "__main__":
+    main()

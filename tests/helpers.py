@@ -1,0 +1,68 @@
+"""Shared test helpers: running one case on several backends and comparing."""
+from __future__ import annotations
+
+import json
+import os
+
+import numpy as np
+
+from weldformfem_gb300 import workloads as W
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+HOLLOMON = dict(model=1, E=200e9, nu=0.3, rho=7850.0, sy0=300e6, hol_K=600e6, hol_m=0.2)
+STAB = [0.3, 0.7, 0.2, 0.08, 0.15, 0.15, 0.8, 0.2, 0.05, 0.0]
+
+
+def golden_cases():
+    """The cases of tests/golden/gen_golden.py, rebuilt without the reference."""
+    import importlib.util
+
+    spec = importlib.util.spec_from_file_location("gen_golden", os.path.join(GOLDEN, "gen_golden.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.cases()
+
+
+def load_golden(name):
+    return dict(np.load(os.path.join(GOLDEN, f"{name}.npz")))
+
+
+def kats():
+    with open(os.path.join(GOLDEN, "validation_kats.json")) as f:
+        return json.load(f)
+
+
+def setup(dom, case, extra=None):
+    """Applies a case to a backend; returns dt. `extra` as in gen_golden."""
+    extra = extra or {}
+    dt = W.apply(dom, case)
+    if "stab" in extra:
+        dom.set_stab(np.array(extra["stab"], float))
+    if "av" in extra:
+        dom.set_artif_visc(*extra["av"])
+    return dt
+
+
+def rel_err(a, b):
+    """max |a - b| / max |b| (0 when both vanish)."""
+    a = np.asarray(a, float)
+    b = np.asarray(b, float)
+    scale = np.max(np.abs(b)) if b.size else 0.0
+    diff = np.max(np.abs(a - b)) if b.size else 0.0
+    if scale == 0.0:
+        return float(diff)
+    return float(diff / scale)
+
+
+STATE_FIELDS = [("node_vec", "x"), ("node_vec", "u"), ("node_vec", "v"), ("node_vec", "a"),
+                ("node_vec", "fi"), ("node_scalar", "mass"), ("elem_scalar", "vol"),
+                ("elem_scalar", "p"), ("elem_scalar", "pl_strain"), ("elem_tensor", "sigma"),
+                ("elem_tensor", "tau"), ("elem_tensor", "eps")]
+
+
+def compare_state(a, b, fields=STATE_FIELDS):
+    """Relative errors of a against b over the standard state fields."""
+    out = {}
+    for kind, name in fields:
+        out[name] = rel_err(getattr(a, kind)(name), getattr(b, kind)(name))
+    return out

@@ -1,0 +1,69 @@
+"""Mixed-precision CUDA path against the FP64 oracle (GPU).
+
+The mixed path computes element arithmetic in FP32 (positions as compensated
+float pairs, reaction sums in FP64), so it is not bit-compatible; these tests
+bound its error against the FP64 oracle on the same inputs. Tolerances
+(max |mixed - fp64| / max |fp64|): displacement 1e-4, reaction history 1e-3,
+equivalent plastic strain 1e-2 (elements at the yield onset switch branch
+with O(eps_f32) changes of the trial stress).
+"""
+import numpy as np
+import pytest
+
+import weldformfem_gb300 as wf
+from oracle import orabind as O
+from tests import helpers as H
+from weldformfem_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def errors(case, steps):
+    d = wf.Domain(wf.WF_MIXED)
+    W.apply(d, case)
+    d.init()
+    d.run(steps)
+    o = O.OracleDomain()
+    W.apply(o, case)
+    o.init()
+    o.step(steps)
+    return {"u": H.rel_err(d.node_vec("u"), o.node_vec("u")),
+            "x": H.rel_err(d.node_vec("x"), o.node_vec("x")),
+            "reaction": H.rel_err(d.reaction(), o.reaction()),
+            "pl": H.rel_err(d.elem_scalar("pl_strain"), o.elem_scalar("pl_strain")),
+            "sigma": H.rel_err(d.elem_tensor("sigma"), o.elem_tensor("sigma"))}
+
+
+@pytest.mark.parametrize("cid,scale,steps", [
+    (0, None, 2000),            # config 0 hexahedra + hourglass
+    (1, (8, 8, 12), 800),       # perturbed tetrahedra
+    (2, (16, 16, 8), 600),      # perturbed hexahedra, rigid die, friction
+])
+def test_mixed_error_vs_fp64(cid, scale, steps):
+    e = errors(W.config(cid, scale=scale), steps)
+    assert e["u"] <= 1e-4, e
+    assert e["x"] <= 1e-6, e
+    assert e["reaction"] <= 1e-3, e
+    assert e["pl"] <= 1e-2, e
+
+
+def test_mixed_deterministic():
+    case = W.config(2, scale=(12, 12, 6))
+    outs = []
+    for _ in range(2):
+        d = wf.Domain(wf.WF_MIXED)
+        W.apply(d, case)
+        d.init()
+        d.run(100)
+        outs.append((d.node_vec("x"), d.reaction()))
+    np.testing.assert_array_equal(outs[0][0], outs[1][0])
+    np.testing.assert_array_equal(outs[0][1], outs[1][1])
+
+
+def test_mixed_rejects_unsupported_options():
+    d = wf.Domain(wf.WF_MIXED)
+    W.apply(d, W.config(1, scale=(2, 2, 2)))
+    d.set_press_algorithm(1)
+    with pytest.raises(wf.WfError) as e:
+        d.init()
+    assert e.value.status == 5

@@ -1,0 +1,144 @@
+"""FP64 CUDA path against the oracle / reference fixtures (GPU).
+
+Tolerance: every state field within 1e-9 relative (max |gpu - ref| divided by
+max |ref|) after N steps, the bar the FP64 path is specified to; connectivity
+and node->element lists bit-exact. Observed errors are far below the bar:
+the kernels follow the reference's operation order with FMA contraction off,
+so only pow() in the hourglass coefficient rounds differently.
+"""
+import numpy as np
+import pytest
+
+import weldformfem_gb300 as wf
+from oracle import orabind as O
+from tests import helpers as H
+from weldformfem_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-9
+CASES = H.golden_cases()
+IDS = [c[0] for c in CASES]
+
+
+def gpu_run(case, steps, mode="step", extra=None, precision=wf.WF_FP64):
+    d = wf.Domain(precision)
+    dt = H.setup(d, case, extra)
+    d.init()
+    if mode == "verbatim":
+        d.set_end_time(steps * dt)
+        assert d.solve() == steps
+    else:
+        d.run(steps)
+    return d, dt
+
+
+@pytest.mark.parametrize("name,case,steps,mode,extra", CASES, ids=IDS)
+def test_fp64_matches_reference_fixture(name, case, steps, mode, extra):
+    g = H.load_golden(name)
+    d, dt = gpu_run(case, steps, mode, extra)
+    elnod, nodel, loc, off, cnt = d.conn()
+    np.testing.assert_array_equal(elnod, g["elnod"])
+    np.testing.assert_array_equal(nodel, g["nodel"])
+    np.testing.assert_array_equal(loc, g["nodel_loc"])
+    np.testing.assert_array_equal(off, g["nodel_offset"])
+    np.testing.assert_array_equal(cnt, g["nodel_count"])
+    got = {"x": d.node_vec("x"), "u": d.node_vec("u"), "v": d.node_vec("v"),
+           "a": d.node_vec("a"), "fi": d.node_vec("fi"), "mass": d.node_scalar("mass"),
+           "vol": d.elem_scalar("vol"), "p": d.elem_scalar("p"),
+           "pl_strain": d.elem_scalar("pl_strain"), "sigma": d.elem_tensor("sigma"),
+           "tau": d.elem_tensor("tau"), "eps": d.elem_tensor("eps"),
+           "p_node": d.node_scalar("p_node")}
+    for k, v in got.items():
+        err = H.rel_err(v, g[k])
+        assert err <= TOL, f"{name}: {k} rel err {err:.3e}"
+    if "reaction" in g:
+        r = d.reaction()
+        assert r.shape == g["reaction"].shape
+        assert H.rel_err(r, g["reaction"]) <= TOL
+
+
+def test_fp64_config0_full_run_matches_oracle():
+    """Config 0 as specified: 10^3 hexahedra, hourglass 0.1, 5000 steps."""
+    case = W.config(0)
+    d, _ = gpu_run(case, case.steps)
+    o = O.OracleDomain()
+    W.apply(o, case)
+    o.init()
+    o.step(case.steps)
+    errs = H.compare_state(d, o)
+    assert max(errs.values()) <= TOL, errs
+    assert H.rel_err(d.reaction(), o.reaction()) <= TOL
+    assert d.elem_scalar("pl_strain").max() > 1e-3  # the run is plastic
+
+
+def test_fp64_contact_plane_matches_oracle():
+    """Config 2 physics on a small perturbed block: rigid die, friction."""
+    case = W.config(2, scale=(12, 10, 6))
+    d, _ = gpu_run(case, 400)
+    o = O.OracleDomain()
+    W.apply(o, case)
+    o.init()
+    o.step(400)
+    errs = H.compare_state(d, o)
+    assert max(errs.values()) <= TOL, errs
+    assert H.rel_err(d.node_vec("contforce"), o.node_vec("contforce")) <= TOL
+    r = d.reaction()
+    assert r.max() > 0.0
+    assert H.rel_err(r, o.reaction()) <= TOL
+
+
+def test_fp64_tets_perturbed_matches_oracle():
+    case = W.config(1, scale=(6, 5, 8))
+    d, _ = gpu_run(case, 500)
+    o = O.OracleDomain()
+    W.apply(o, case)
+    o.init()
+    o.step(500)
+    errs = H.compare_state(d, o)
+    assert max(errs.values()) <= TOL, errs
+
+
+def test_graph_and_direct_launches_agree_bitwise():
+    case = W.config(0, scale=(5, 5, 5))
+    a, _ = gpu_run(case, 70)       # 2 graph launches of 32 steps + 6 direct steps
+    b = wf.Domain()
+    W.apply(b, case)
+    b.init()
+    for _ in range(70):
+        b.run(1)                   # direct launches only
+    for f in ("x", "v", "u"):
+        np.testing.assert_array_equal(a.node_vec(f), b.node_vec(f))
+    np.testing.assert_array_equal(a.reaction(), b.reaction())
+
+
+def test_min_edge_length_reduction():
+    case = W.config(1, scale=(6, 6, 6))
+    d = wf.Domain()
+    W.apply(d, case)
+    d.init()
+    x = case.coords()
+    assert d.min_edge_length() == W.min_edge_length(x, case.elnod())
+
+
+def test_api_errors():
+    d = wf.Domain()
+    with pytest.raises(wf.WfError) as e:
+        d.init()
+    assert e.value.status == 2          # no mesh: call out of order
+    d.add_box((0.004, 0.004, 0.004), 0.0005)
+    with pytest.raises(wf.WfError) as e:
+        d.add_bcs([(10 ** 6, 0, 0.0)])  # node out of range
+    assert e.value.status == 1
+    with pytest.raises(wf.WfError) as e:
+        d.init()                        # no material
+    assert e.value.status == 2
+    d.set_materials([W.STEEL])
+    with pytest.raises(wf.WfError):
+        d.init()                        # no time step
+    with pytest.raises(wf.WfError) as e:
+        d.run(1)
+    assert e.value.status == 2
+    bad = wf.Domain()
+    with pytest.raises(wf.WfError) as e:
+        bad.set_mesh(np.zeros((4, 3)), np.array([[0, 1, 2, 7]], np.int32))
+    assert e.value.status == 1

@@ -1,0 +1,336 @@
+"""weldformfem_gb300: GB300-native explicit updated-Lagrangian step.
+
+Python mirror of the C ABI in include/wf.h (the library is
+weldformfem_gb300/_lib/libwf_gb300.so, built by weldformfem_gb300/build.py).
+`Domain` exposes the reference's Domain_d vocabulary (AddBoxLength, setNode,
+AssignMaterial, AddBCVelNode, AllocateBCs, SetDT, SolveChungHulbert, ...)
+under Python names. There is no CPU fallback: constructing a Domain without
+the CUDA library or without a GPU raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import workloads  # noqa: F401  (re-exported helper)
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libwf_gb300.so")
+
+WF_FP64, WF_MIXED = 0, 1
+STATUS = {0: "ok", 1: "invalid argument", 2: "call out of order", 3: "CUDA error",
+          4: "out of memory", 5: "unsupported option", 6: "non-finite state",
+          7: "device wait timed out"}
+
+NODE_VEC = {"x": 0, "v": 1, "a": 2, "u": 3, "prev_a": 4, "fi": 5, "contforce": 7}
+NODE_SCALAR = {"mass": 0, "voln": 1, "p_node": 2}
+ELEM_SCALAR = {"vol": 0, "vol0": 1, "detJ": 2, "p": 3, "pl_strain": 4, "sigma_y": 5, "rho": 6}
+ELEM_TENSOR = {"sigma": 0, "tau": 1, "eps": 2, "str_rate": 3, "rot_rate": 4}
+
+
+class WfError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class WfMaterial(C.Structure):
+    _fields_ = [("model", C.c_int32), ("E", C.c_double), ("nu", C.c_double),
+                ("rho", C.c_double), ("sy0", C.c_double), ("H", C.c_double),
+                ("hol_K", C.c_double), ("hol_m", C.c_double)]
+
+
+class WfStab(C.Structure):
+    _fields_ = [(n, C.c_double) for n in (
+        "alpha_free", "alpha_contact", "hg_coeff_free", "hg_coeff_contact", "av_coeff_div",
+        "av_coeff_bulk", "log_factor", "pspg_scale", "p_pspg_bulkfac", "J_min")]
+
+
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_lib = None
+
+# name -> (argtypes); every function returns wf_status (int)
+_SIGS = {
+    "wf_domain_create": [C.POINTER(C.c_void_p)],
+    "wf_domain_create_on_device": [C.POINTER(C.c_void_p), C.c_int],
+    "wf_domain_destroy": [C.c_void_p],
+    "wf_add_box_length": [C.c_void_p, _dp, _dp, C.c_double, C.c_int32, C.c_int32],
+    "wf_set_mesh": [C.c_void_p, C.c_int64, C.c_int64, C.c_int32, _dp, _ip],
+    "wf_set_node": [C.c_void_p, C.c_int64, C.c_double, C.c_double, C.c_double],
+    "wf_set_nodes": [C.c_void_p, _dp],
+    "wf_get_sizes": [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                     C.POINTER(C.c_int32), C.POINTER(C.c_int64)],
+    "wf_get_connectivity": [C.c_void_p, _ip, _ip, _ip, _ip, _ip],
+    "wf_set_density": [C.c_void_p, C.c_double],
+    "wf_set_materials": [C.c_void_p, C.c_int32, C.POINTER(WfMaterial)],
+    "wf_set_elem_materials": [C.c_void_p, _ip],
+    "wf_add_bc_vel_node": [C.c_void_p, C.c_int64, C.c_int32, C.c_double],
+    "wf_add_bc_vel_zone": [C.c_void_p, _dp, _dp, _dp, C.POINTER(C.c_int64)],
+    "wf_allocate_bcs": [C.c_void_p],
+    "wf_set_dt": [C.c_void_p, C.c_double],
+    "wf_set_end_time": [C.c_void_p, C.c_double],
+    "wf_set_precision": [C.c_void_p, C.c_int32],
+    "wf_set_hourglass": [C.c_void_p, C.c_double],
+    "wf_set_press_algorithm": [C.c_void_p, C.c_int32],
+    "wf_set_stab": [C.c_void_p, C.POINTER(WfStab)],
+    "wf_set_artif_visc": [C.c_void_p, C.c_double, C.c_double],
+    "wf_set_mass_mode": [C.c_void_p, C.c_int32],
+    "wf_set_reaction_nodes": [C.c_void_p, C.c_int64, _ip, C.c_int32],
+    "wf_set_contact_plane": [C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_double,
+                             C.c_int64, _ip],
+    "wf_init": [C.c_void_p],
+    "wf_run": [C.c_void_p, C.c_int64],
+    "wf_solve": [C.c_void_p, C.POINTER(C.c_int64)],
+    "wf_get_time": [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int64)],
+    "wf_sync": [C.c_void_p],
+    "wf_min_edge_length": [C.c_void_p, C.POINTER(C.c_double)],
+    "wf_get_node_field": [C.c_void_p, C.c_int32, _dp],
+    "wf_get_node_scalar": [C.c_void_p, C.c_int32, _dp],
+    "wf_get_elem_scalar": [C.c_void_p, C.c_int32, _dp],
+    "wf_get_elem_tensor": [C.c_void_p, C.c_int32, _dp],
+    "wf_get_disp": [C.c_void_p, _dp],
+    "wf_get_vel": [C.c_void_p, _dp],
+    "wf_get_pl_strain": [C.c_void_p, _dp],
+    "wf_get_reaction_history": [C.c_void_p, _dp, C.c_int64, C.POINTER(C.c_int64)],
+    "wf_set_node_state": [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p],
+    "wf_set_phase_timing": [C.c_void_p, C.c_int32],
+    "wf_get_phase_times": [C.c_void_p, _dp, C.POINTER(C.c_int64), C.c_int32],
+    "wf_get_launch_count": [C.c_void_p, C.POINTER(C.c_int64)],
+    "wf_get_stream": [C.c_void_p, C.POINTER(C.c_void_p)],
+    "wf_get_transfer_bytes": [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)],
+}
+
+
+def lib():
+    """Loads the CUDA library; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"CUDA library missing: {LIB_PATH} (run weldformfem_gb300/build.py)")
+    L = C.CDLL(LIB_PATH)
+    for name, args in _SIGS.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = C.c_int
+    L.wf_last_error.argtypes = [C.c_void_p]
+    L.wf_last_error.restype = C.c_char_p
+    L.wf_status_string.argtypes = [C.c_int]
+    L.wf_status_string.restype = C.c_char_p
+    L.wf_abi_version.argtypes = []
+    L.wf_abi_version.restype = C.c_int32
+    _lib = L
+    return L
+
+
+class Domain:
+    """One GPU domain (MetFEM::Domain_d drop-in) driven through the C ABI."""
+
+    def __init__(self, precision: int = WF_FP64, device: int = 0):
+        L = lib()
+        h = C.c_void_p()
+        st = L.wf_domain_create_on_device(C.byref(h), int(device))
+        if st != 0:
+            raise WfError(st, "wf_domain_create: no usable CUDA device")
+        self.h = h
+        self.precision = precision
+        self._call("wf_set_precision", int(precision))
+
+    def _call(self, name, *args):
+        st = getattr(lib(), name)(self.h, *args)
+        if st != 0:
+            raise WfError(st, f"{name}: {lib().wf_last_error(self.h).decode()}")
+        return st
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().wf_domain_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # mesh -------------------------------------------------------------
+    def add_box(self, L, r, tritetra=False, origin=(0.0, 0.0, 0.0)):
+        self._call("wf_add_box_length", np.array(origin, float), np.array(L, float), float(r), 1,
+                   int(bool(tritetra)))
+
+    def set_mesh(self, x, elnod):
+        x = np.ascontiguousarray(x, np.float64).reshape(-1)
+        elnod = np.ascontiguousarray(elnod, np.int32)
+        ne, npe = elnod.shape
+        self._call("wf_set_mesh", x.size // 3, ne, npe, x, elnod.reshape(-1))
+
+    def set_nodes(self, x):
+        self._call("wf_set_nodes", np.ascontiguousarray(x, np.float64).reshape(-1))
+
+    def sizes(self):
+        nn, ne, tot = C.c_int64(), C.c_int64(), C.c_int64()
+        npe = C.c_int32()
+        self._call("wf_get_sizes", C.byref(nn), C.byref(ne), C.byref(npe), C.byref(tot))
+        return nn.value, ne.value, npe.value, tot.value
+
+    @property
+    def nn(self):
+        return self.sizes()[0]
+
+    @property
+    def ne(self):
+        return self.sizes()[1]
+
+    @property
+    def npe(self):
+        return self.sizes()[2]
+
+    def conn(self):
+        nn, ne, npe, tot = self.sizes()
+        elnod = np.zeros(ne * npe, np.int32)
+        nodel = np.zeros(tot, np.int32)
+        loc = np.zeros(tot, np.int32)
+        off = np.zeros(nn, np.int32)
+        cnt = np.zeros(nn, np.int32)
+        self._call("wf_get_connectivity", elnod, nodel, loc, off, cnt)
+        return elnod.reshape(ne, npe), nodel, loc, off, cnt
+
+    # setup ------------------------------------------------------------
+    def set_materials(self, mats, elem_ids=None):
+        arr = (WfMaterial * len(mats))()
+        for i, m in enumerate(mats):
+            arr[i] = WfMaterial(int(m.get("model", 0)), float(m["E"]), float(m["nu"]),
+                                float(m["rho"]), float(m.get("sy0", 1e10)), float(m.get("H", 0.0)),
+                                float(m.get("hol_K", 1.0)), float(m.get("hol_m", 1.0)))
+        self._call("wf_set_materials", len(mats), arr)
+        if elem_ids is not None:
+            self._call("wf_set_elem_materials", np.ascontiguousarray(elem_ids, np.int32))
+
+    def set_hourglass(self, coef):
+        self._call("wf_set_hourglass", float(coef))
+
+    def set_press_algorithm(self, alg):
+        self._call("wf_set_press_algorithm", int(alg))
+
+    def set_stab(self, s10):
+        s = WfStab(*[float(v) for v in s10])
+        self._call("wf_set_stab", C.byref(s))
+
+    def set_artif_visc(self, a, b):
+        self._call("wf_set_artif_visc", float(a), float(b))
+
+    def set_mass_mode(self, mode):
+        self._call("wf_set_mass_mode", int(mode))
+
+    def add_bcs(self, bcs):
+        for node, dim, val in bcs:
+            self._call("wf_add_bc_vel_node", int(node), int(dim), float(val))
+        self._call("wf_allocate_bcs")
+
+    def add_bc_vel_zone(self, start, end, vel):
+        c = C.c_int64()
+        self._call("wf_add_bc_vel_zone", np.array(start, float), np.array(end, float),
+                   np.array(vel, float), C.byref(c))
+        return c.value
+
+    def set_reaction_nodes(self, nodes, dim=2):
+        nodes = np.ascontiguousarray(nodes, np.int32)
+        self._call("wf_set_reaction_nodes", nodes.size, nodes, int(dim))
+
+    def set_contact_plane(self, z0, vz, kpen, mu, cand_nodes):
+        cand = np.ascontiguousarray(cand_nodes, np.int32)
+        self._call("wf_set_contact_plane", float(z0), float(vz), float(kpen), float(mu),
+                   cand.size, cand)
+
+    def set_dt(self, dt):
+        self._call("wf_set_dt", float(dt))
+
+    def set_end_time(self, t):
+        self._call("wf_set_end_time", float(t))
+
+    # run --------------------------------------------------------------
+    def init(self):
+        self._call("wf_init")
+
+    def step(self, n=1):
+        self._call("wf_run", int(n))
+
+    def run(self, n):
+        self._call("wf_run", int(n))
+
+    def solve(self):
+        n = C.c_int64()
+        self._call("wf_solve", C.byref(n))
+        return n.value
+
+    def sync(self):
+        self._call("wf_sync")
+
+    @property
+    def time(self):
+        t = C.c_double()
+        s = C.c_int64()
+        self._call("wf_get_time", C.byref(t), C.byref(s))
+        return t.value
+
+    def min_edge_length(self):
+        h = C.c_double()
+        self._call("wf_min_edge_length", C.byref(h))
+        return h.value
+
+    def set_phase_timing(self, on=True):
+        self._call("wf_set_phase_timing", int(bool(on)))
+
+    def phase_times(self, reset=True):
+        """(ms[4] of geometry, nodal, element, node phases; steps timed)."""
+        ms = np.zeros(4)
+        n = C.c_int64()
+        self._call("wf_get_phase_times", ms, C.byref(n), int(bool(reset)))
+        return ms, n.value
+
+    def stream_handle(self):
+        """The domain's cudaStream_t as an integer (for torch.cuda.ExternalStream)."""
+        p = C.c_void_p()
+        self._call("wf_get_stream", C.byref(p))
+        return p.value or 0
+
+    def transfer_bytes(self):
+        a, b = C.c_int64(), C.c_int64()
+        self._call("wf_get_transfer_bytes", C.byref(a), C.byref(b))
+        return a.value, b.value
+
+    def launch_count(self):
+        n = C.c_int64()
+        self._call("wf_get_launch_count", C.byref(n))
+        return n.value
+
+    # readback ---------------------------------------------------------
+    def node_vec(self, name):
+        out = np.zeros(self.nn * 3)
+        self._call("wf_get_node_field", NODE_VEC[name], out)
+        return out.reshape(-1, 3)
+
+    def node_scalar(self, name):
+        out = np.zeros(self.nn)
+        self._call("wf_get_node_scalar", NODE_SCALAR[name], out)
+        return out
+
+    def elem_scalar(self, name):
+        out = np.zeros(self.ne)
+        self._call("wf_get_elem_scalar", ELEM_SCALAR[name], out)
+        return out
+
+    def elem_tensor(self, name):
+        out = np.zeros(self.ne * 6)
+        self._call("wf_get_elem_tensor", ELEM_TENSOR[name], out)
+        return out.reshape(-1, 6)
+
+    def reaction(self):
+        n = C.c_int64()
+        self._call("wf_get_reaction_history", np.zeros(1), 0, C.byref(n))
+        out = np.zeros(max(n.value, 1))
+        self._call("wf_get_reaction_history", out, n.value, C.byref(n))
+        return out[: n.value]

@@ -1,0 +1,1200 @@
+// Host side of the C ABI (include/wf.h): domain lifecycle, mesh and
+// node->element lists, BC tables, device buffers, the step loop (captured in
+// CUDA graphs) and readback.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <new>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "wf_internal.cuh"
+
+using namespace wf;
+
+struct wf_domain {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  // host mesh
+  int32_t npe = 0;
+  int64_t nn = 0, ne = 0, np = 0;
+  std::vector<double> x;          // interleaved [3 nn]
+  std::vector<int32_t> elnod;     // [ne npe]
+  std::vector<int32_t> nodel, nodel_loc, nodel_off, nodel_cnt;
+  // materials
+  std::vector<wf_material> mats;
+  std::vector<int32_t> emat;
+  double rho_all = 0.0;
+  bool rho_set = false;
+  // BCs (AddBCVelNode staging)
+  std::vector<int64_t> bc_nod[3];
+  std::vector<double> bc_val[3];
+  bool bcs_allocated = false;
+  // options
+  double dt = 0.0, end_t = 0.0;
+  int precision = WF_FP64;
+  double hg = 0.0;
+  int press_alg = 0, mass_mode = 0;
+  wf_stab stab{};
+  double av[2] = {0.0, 0.0};
+  std::vector<int32_t> react_nodes;
+  int react_dim = 2;
+  bool contact = false;
+  double c_z0 = 0, c_vz = 0, c_k = 0, c_mu = 0;
+  std::vector<int32_t> cand;
+  // device
+  bool initialized = false;
+  std::vector<void *> allocs;
+  StepParams P{};
+  Fp64State S{};
+  MixState M{};
+  float *mvol = nullptr;          // mixed: element volume scratch
+  double *rho0_dev = nullptr;
+  int node_grid = 0;
+  int64_t hist_cap = 0;
+  int64_t host_step = 0;          // steps launched since init
+  double host_time = 0.0;         // Time accumulated on the host (mirror)
+  bool mix_valid_fp64 = false;    // FP64 export of the mixed state is current
+  // graphs
+  cudaGraphExec_t graph = nullptr;
+  int graph_steps = 0;
+  // per-phase timing
+  bool phase_timing = false;
+  std::vector<cudaEvent_t> ev_pool;   // 5 events per timed step
+  size_t ev_used = 0;
+  double phase_ms[4] = {0, 0, 0, 0};
+  int64_t phase_steps = 0;
+  int64_t launches = 0;
+  int64_t h2d_bytes = 0, d2h_bytes = 0;
+};
+
+namespace {
+
+wf_status fail(wf_domain *d, wf_status s, const char *fmt, ...) {
+  if (d) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    d->err = buf;
+  }
+  return s;
+}
+
+#define CUDA_TRY(call)                                                                   \
+  do {                                                                                   \
+    cudaError_t e_ = (call);                                                             \
+    if (e_ != cudaSuccess)                                                               \
+      return fail(d, e_ == cudaErrorMemoryAllocation ? WF_ERR_NOMEM : WF_ERR_CUDA,       \
+                  "%s: %s", #call, cudaGetErrorString(e_));                              \
+  } while (0)
+
+template <typename T>
+cudaError_t dalloc(wf_domain *d, T **p, size_t count) {
+  void *q = nullptr;
+  cudaError_t e = cudaMalloc(&q, std::max<size_t>(count, 1) * sizeof(T));
+  if (e != cudaSuccess) return e;
+  d->allocs.push_back(q);
+  *p = static_cast<T *>(q);
+  return cudaMemsetAsync(q, 0, std::max<size_t>(count, 1) * sizeof(T), d->stream);
+}
+
+void free_device(wf_domain *d) {
+  if (d->graph) {
+    cudaGraphExecDestroy(d->graph);
+    d->graph = nullptr;
+  }
+  for (void *p : d->allocs) cudaFree(p);
+  d->allocs.clear();
+  for (cudaEvent_t ev : d->ev_pool) cudaEventDestroy(ev);
+  d->ev_pool.clear();
+  d->ev_used = 0;
+  d->S = Fp64State{};
+  d->M = MixState{};
+  d->mvol = nullptr;
+  d->initialized = false;
+}
+
+// Node -> element lists, element-ascending per node (setNodElem,
+// Domain_d.C:1508-1611; tail of AddBoxLength, :1436-1481).
+bool build_nodel(wf_domain *d) {
+  d->nodel_cnt.assign(d->nn, 0);
+  for (int32_t n : d->elnod) {
+    if (n < 0 || n >= d->nn) return false;
+    d->nodel_cnt[n]++;
+  }
+  d->nodel_off.assign(d->nn + 1, 0);
+  int64_t tot = 0;
+  for (int64_t n = 0; n < d->nn; n++) {
+    d->nodel_off[n] = (int32_t)tot;
+    tot += d->nodel_cnt[n];
+  }
+  d->nodel_off[d->nn] = (int32_t)tot;
+  d->nodel.assign(tot, 0);
+  d->nodel_loc.assign(tot, 0);
+  std::vector<int32_t> fill(d->nn, 0);
+  for (int64_t e = 0; e < d->ne; e++)
+    for (int a = 0; a < d->npe; a++) {
+      int32_t n = d->elnod[e * d->npe + a];
+      int64_t k = d->nodel_off[n] + fill[n]++;
+      d->nodel[k] = (int32_t)e;
+      d->nodel_loc[k] = a;
+    }
+  return true;
+}
+
+void reset_mesh(wf_domain *d) {
+  free_device(d);
+  for (int k = 0; k < 3; k++) {
+    d->bc_nod[k].clear();
+    d->bc_val[k].clear();
+  }
+  d->emat.clear();
+  d->react_nodes.clear();
+  d->cand.clear();
+  d->contact = false;
+  d->bcs_allocated = false;
+}
+
+wf_status need_mesh(wf_domain *d) {
+  if (!d) return WF_ERR_ARG;
+  if (d->nn <= 0) return fail(d, WF_ERR_STATE, "no mesh defined");
+  return WF_OK;
+}
+
+}  // namespace
+
+// Definitions of the functions declared extern "C" in wf.h (C linkage is
+// inherited from those declarations).
+
+WF_API int32_t wf_abi_version(void) { return 1; }
+
+WF_API const char *wf_status_string(wf_status s) {
+  switch (s) {
+    case WF_OK: return "ok";
+    case WF_ERR_ARG: return "invalid argument";
+    case WF_ERR_STATE: return "call out of order";
+    case WF_ERR_CUDA: return "CUDA error";
+    case WF_ERR_NOMEM: return "out of memory";
+    case WF_ERR_UNSUPPORTED: return "unsupported option";
+    case WF_ERR_NONFINITE: return "non-finite state";
+    case WF_ERR_TIMEOUT: return "device wait timed out";
+  }
+  return "unknown status";
+}
+
+WF_API const char *wf_last_error(const wf_domain *d) { return d ? d->err.c_str() : "null domain"; }
+
+WF_API wf_status wf_domain_create_on_device(wf_domain **out, int device) {
+  if (!out) return WF_ERR_ARG;
+  *out = nullptr;
+  int count = 0;
+  cudaError_t e = cudaGetDeviceCount(&count);
+  if (e != cudaSuccess || count <= device || device < 0) return WF_ERR_CUDA;
+  wf_domain *d = new (std::nothrow) wf_domain();
+  if (!d) return WF_ERR_NOMEM;
+  d->device = device;
+  if (cudaSetDevice(device) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&d->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete d;
+    return WF_ERR_CUDA;
+  }
+  *out = d;
+  return WF_OK;
+}
+
+WF_API wf_status wf_domain_create(wf_domain **out) { return wf_domain_create_on_device(out, 0); }
+
+WF_API wf_status wf_domain_destroy(wf_domain *d) {
+  if (!d) return WF_ERR_ARG;
+  cudaSetDevice(d->device);
+  if (d->stream) cudaStreamSynchronize(d->stream);
+  free_device(d);
+  if (d->stream) cudaStreamDestroy(d->stream);
+  delete d;
+  return WF_OK;
+}
+
+// ---- mesh -----------------------------------------------------------------
+WF_API wf_status wf_add_box_length(wf_domain *d, const double V[3], const double L[3], double r,
+                                   int32_t red_int, int32_t tritetra) {
+  if (!d || !V || !L) return WF_ERR_ARG;
+  if (!red_int) return fail(d, WF_ERR_UNSUPPORTED, "only one-point (reduced) integration");
+  if (!(L[2] > 0.0)) return fail(d, WF_ERR_UNSUPPORTED, "only 3-D boxes (L.z > 0)");
+  if (!(r > 0.0)) return fail(d, WF_ERR_ARG, "r must be positive");
+  int nel[3];
+  for (int k = 0; k < 3; k++) nel[k] = (int)(L[k] / (2.0 * r));
+  if (nel[0] <= 0 || nel[1] <= 0 || nel[2] <= 0)
+    return fail(d, WF_ERR_ARG, "box smaller than one element");
+  reset_mesh(d);
+  d->npe = tritetra ? 4 : 8;
+  d->nn = (int64_t)(nel[0] + 1) * (nel[1] + 1) * (nel[2] + 1);
+  d->ne = (int64_t)nel[0] * nel[1] * nel[2] * (tritetra ? 6 : 1);
+  if (d->ne * d->npe >= (int64_t)INT32_MAX) return fail(d, WF_ERR_ARG, "mesh too large");
+  d->x.resize(3 * d->nn);
+  // coordinates by repeated addition of 2r (Domain_d.C:1215-1235)
+  int64_t p = 0;
+  double Xz = V[2];
+  for (int k = 0; k <= nel[2]; k++) {
+    double Xy = V[1];
+    for (int j = 0; j <= nel[1]; j++) {
+      double Xx = V[0];
+      for (int i = 0; i <= nel[0]; i++) {
+        d->x[3 * p] = Xx;
+        d->x[3 * p + 1] = Xy;
+        d->x[3 * p + 2] = Xz;
+        p++;
+        Xx = Xx + 2.0 * r;
+      }
+      Xy = Xy + 2.0 * r;
+    }
+    Xz = Xz + 2 * r;
+  }
+  d->elnod.resize(d->ne * d->npe);
+  static const int T[6][4] = {{0, 1, 3, 5}, {1, 2, 3, 5}, {0, 5, 3, 4},
+                              {4, 5, 3, 7}, {5, 6, 3, 7}, {5, 2, 3, 6}};
+  const int64_t nnodz = (int64_t)(nel[0] + 1) * (nel[1] + 1);
+  int64_t ei = 0;
+  for (int ez = 0; ez < nel[2]; ez++)
+    for (int ey = 0; ey < nel[1]; ey++)
+      for (int ex = 0; ex < nel[0]; ex++) {
+        const int64_t nb1 = nnodz * ez + (int64_t)(nel[0] + 1) * ey + ex;
+        const int64_t nb2 = nnodz * ez + (int64_t)(nel[0] + 1) * (ey + 1) + ex;
+        const int32_t h[8] = {(int32_t)nb1, (int32_t)(nb1 + 1), (int32_t)(nb2 + 1),
+                              (int32_t)nb2, (int32_t)(nb1 + nnodz), (int32_t)(nb1 + nnodz + 1),
+                              (int32_t)(nb2 + nnodz + 1), (int32_t)(nb2 + nnodz)};
+        if (!tritetra) {
+          for (int a = 0; a < 8; a++) d->elnod[ei + a] = h[a];
+          ei += 8;
+        } else {
+          for (int t = 0; t < 6; t++) {
+            for (int a = 0; a < 4; a++) d->elnod[ei + a] = h[T[t][a]];
+            ei += 4;
+          }
+        }
+      }
+  build_nodel(d);
+  return WF_OK;
+}
+
+WF_API wf_status wf_set_mesh(wf_domain *d, int64_t nn, int64_t ne, int32_t npe, const double *xyz,
+                             const int32_t *elnod) {
+  if (!d || !xyz || !elnod || nn <= 0 || ne <= 0) return WF_ERR_ARG;
+  if (npe != 4 && npe != 8)
+    return fail(d, WF_ERR_UNSUPPORTED, "npe must be 8 (hexahedra) or 4 (tetrahedra)");
+  if (ne * npe >= (int64_t)INT32_MAX || nn >= (int64_t)INT32_MAX)
+    return fail(d, WF_ERR_ARG, "mesh too large");
+  reset_mesh(d);
+  d->npe = npe;
+  d->nn = nn;
+  d->ne = ne;
+  d->x.assign(xyz, xyz + 3 * nn);
+  d->elnod.assign(elnod, elnod + ne * npe);
+  if (!build_nodel(d)) {
+    d->nn = d->ne = 0;
+    return fail(d, WF_ERR_ARG, "connectivity references a node outside [0, nn)");
+  }
+  return WF_OK;
+}
+
+WF_API wf_status wf_set_node(wf_domain *d, int64_t n, double x, double y, double z) {
+  wf_status s = need_mesh(d);
+  if (s) return s;
+  if (n < 0 || n >= d->nn) return fail(d, WF_ERR_ARG, "node %lld out of range", (long long)n);
+  if (d->initialized) return fail(d, WF_ERR_STATE, "setNode after init");
+  d->x[3 * n] = x;
+  d->x[3 * n + 1] = y;
+  d->x[3 * n + 2] = z;
+  return WF_OK;
+}
+
+WF_API wf_status wf_set_nodes(wf_domain *d, const double *xyz) {
+  wf_status s = need_mesh(d);
+  if (s) return s;
+  if (!xyz) return WF_ERR_ARG;
+  if (d->initialized) return fail(d, WF_ERR_STATE, "setNode after init");
+  std::memcpy(d->x.data(), xyz, sizeof(double) * 3 * d->nn);
+  return WF_OK;
+}
+
+WF_API wf_status wf_get_sizes(const wf_domain *d, int64_t *nn, int64_t *ne, int32_t *npe,
+                              int64_t *tot) {
+  if (!d) return WF_ERR_ARG;
+  if (nn) *nn = d->nn;
+  if (ne) *ne = d->ne;
+  if (npe) *npe = d->npe;
+  if (tot) *tot = (int64_t)d->nodel.size();
+  return WF_OK;
+}
+
+WF_API wf_status wf_get_connectivity(const wf_domain *d, int32_t *elnod, int32_t *nodel,
+                                     int32_t *nodel_loc, int32_t *offset, int32_t *count) {
+  if (!d) return WF_ERR_ARG;
+  if (elnod) std::copy(d->elnod.begin(), d->elnod.end(), elnod);
+  if (nodel) std::copy(d->nodel.begin(), d->nodel.end(), nodel);
+  if (nodel_loc) std::copy(d->nodel_loc.begin(), d->nodel_loc.end(), nodel_loc);
+  if (offset) std::copy(d->nodel_off.begin(), d->nodel_off.begin() + d->nn, offset);
+  if (count) std::copy(d->nodel_cnt.begin(), d->nodel_cnt.end(), count);
+  return WF_OK;
+}
+
+// ---- material -------------------------------------------------------------
+WF_API wf_status wf_set_density(wf_domain *d, double rho) {
+  if (!d || !(rho > 0.0)) return WF_ERR_ARG;
+  d->rho_all = rho;
+  d->rho_set = true;
+  return WF_OK;
+}
+
+WF_API wf_status wf_set_materials(wf_domain *d, int32_t nmat, const wf_material *mats) {
+  if (!d || nmat <= 0 || !mats) return WF_ERR_ARG;
+  for (int i = 0; i < nmat; i++) {
+    const wf_material &m = mats[i];
+    if (!(m.E > 0) || !(m.rho > 0) || !(m.nu > -1.0 && m.nu < 0.5))
+      return fail(d, WF_ERR_ARG, "material %d: need E > 0, rho > 0, -1 < nu < 0.5", i);
+    if (m.model != WF_MAT_BILINEAR && m.model != WF_MAT_HOLLOMON)
+      return fail(d, WF_ERR_UNSUPPORTED, "material %d: model %d", i, m.model);
+    if (m.model == WF_MAT_HOLLOMON && !(m.hol_K > 0 && m.hol_m > 0))
+      return fail(d, WF_ERR_ARG, "material %d: Hollomon needs K > 0, m > 0", i);
+  }
+  d->mats.assign(mats, mats + nmat);
+  d->rho_all = mats[0].rho;
+  d->rho_set = true;
+  return WF_OK;
+}
+
+WF_API wf_status wf_set_elem_materials(wf_domain *d, const int32_t *ids) {
+  wf_status s = need_mesh(d);
+  if (s) return s;
+  if (!ids) return WF_ERR_ARG;
+  for (int64_t e = 0; e < d->ne; e++)
+    if (ids[e] < 0 || ids[e] >= (int32_t)d->mats.size())
+      return fail(d, WF_ERR_ARG, "element %lld: material id %d out of range", (long long)e, ids[e]);
+  d->emat.assign(ids, ids + d->ne);
+  return WF_OK;
+}
+
+// ---- BCs --------------------------------------------------------------------
+WF_API wf_status wf_add_bc_vel_node(wf_domain *d, int64_t node, int32_t dim, double val) {
+  wf_status s = need_mesh(d);
+  if (s) return s;
+  if (dim < 0 || dim > 2) return fail(d, WF_ERR_ARG, "dim must be 0, 1 or 2");
+  if (node < 0 || node >= d->nn) return fail(d, WF_ERR_ARG, "node %lld out of range", (long long)node);
+  d->bc_nod[dim].push_back(node);
+  d->bc_val[dim].push_back(val);
+  d->bcs_allocated = false;
+  return WF_OK;
+}
+
+WF_API wf_status wf_add_bc_vel_zone(wf_domain *d, const double start[3], const double end[3],
+                                    const double vel[3], int64_t *count) {
+  wf_status s = need_mesh(d);
+  if (s) return s;
+  if (!start || !end || !vel) return WF_ERR_ARG;
+  int64_t c = 0;
+  for (int64_t a = 0; a < d->nn; a++) {
+    bool in = true;
+    for (int k = 0; k < 3; k++)
+      if (d->x[3 * a + k] < start[k] || d->x[3 * a + k] > end[k]) in = false;
+    if (in) {
+      for (int k = 0; k < 3; k++) {
+        d->bc_nod[k].push_back(a);
+        d->bc_val[k].push_back(vel[k]);
+      }
+      c++;
+    }
+  }
+  if (count) *count = c;
+  d->bcs_allocated = false;
+  return WF_OK;
+}
+
+WF_API wf_status wf_allocate_bcs(wf_domain *d) {
+  wf_status s = need_mesh(d);
+  if (s) return s;
+  d->bcs_allocated = true;
+  return WF_OK;
+}
+
+// ---- options ------------------------------------------------------------------
+WF_API wf_status wf_set_dt(wf_domain *d, double dt) {
+  if (!d || !(dt > 0.0) || !std::isfinite(dt)) return WF_ERR_ARG;
+  d->dt = dt;
+  if (d->graph) {
+    cudaGraphExecDestroy(d->graph);
+    d->graph = nullptr;
+  }
+  return WF_OK;
+}
+
+WF_API wf_status wf_set_end_time(wf_domain *d, double t) {
+  if (!d) return WF_ERR_ARG;
+  d->end_t = t;
+  return WF_OK;
+}
+
+WF_API wf_status wf_set_precision(wf_domain *d, int32_t prec) {
+  if (!d || (prec != WF_FP64 && prec != WF_MIXED)) return WF_ERR_ARG;
+  if (d->initialized) return fail(d, WF_ERR_STATE, "precision must be set before init");
+  d->precision = prec;
+  return WF_OK;
+}
+
+WF_API wf_status wf_set_hourglass(wf_domain *d, double coef) {
+  if (!d || !(coef >= 0.0)) return WF_ERR_ARG;
+  if (d->initialized) return fail(d, WF_ERR_STATE, "options must be set before init");
+  d->hg = coef;
+  return WF_OK;
+}
+
+WF_API wf_status wf_set_press_algorithm(wf_domain *d, int32_t alg) {
+  if (!d || (alg != 0 && alg != 1)) return WF_ERR_ARG;
+  if (d->initialized) return fail(d, WF_ERR_STATE, "options must be set before init");
+  d->press_alg = alg;
+  return WF_OK;
+}
+
+WF_API wf_status wf_set_stab(wf_domain *d, const wf_stab *st) {
+  if (!d || !st) return WF_ERR_ARG;
+  if (d->initialized) return fail(d, WF_ERR_STATE, "options must be set before init");
+  d->stab = *st;
+  return WF_OK;
+}
+
+WF_API wf_status wf_set_artif_visc(wf_domain *d, double alpha, double beta) {
+  if (!d) return WF_ERR_ARG;
+  if (d->initialized) return fail(d, WF_ERR_STATE, "options must be set before init");
+  d->av[0] = alpha;
+  d->av[1] = beta;
+  return WF_OK;
+}
+
+WF_API wf_status wf_set_mass_mode(wf_domain *d, int32_t mode) {
+  if (!d || (mode != 0 && mode != 1)) return WF_ERR_ARG;
+  if (d->initialized) return fail(d, WF_ERR_STATE, "options must be set before init");
+  d->mass_mode = mode;
+  return WF_OK;
+}
+
+WF_API wf_status wf_set_reaction_nodes(wf_domain *d, int64_t n, const int32_t *nodes, int32_t dim) {
+  wf_status s = need_mesh(d);
+  if (s) return s;
+  if ((n > 0 && !nodes) || dim < 0 || dim > 2) return WF_ERR_ARG;
+  for (int64_t i = 0; i < n; i++)
+    if (nodes[i] < 0 || nodes[i] >= d->nn) return fail(d, WF_ERR_ARG, "reaction node out of range");
+  if (d->initialized) return fail(d, WF_ERR_STATE, "options must be set before init");
+  d->react_nodes.assign(nodes, nodes + n);
+  d->react_dim = dim;
+  return WF_OK;
+}
+
+WF_API wf_status wf_set_contact_plane(wf_domain *d, double z0, double vz, double kpen, double mu,
+                                      int64_t ncand, const int32_t *cand) {
+  wf_status s = need_mesh(d);
+  if (s) return s;
+  if ((ncand > 0 && !cand) || !(kpen > 0) || !(mu >= 0)) return WF_ERR_ARG;
+  for (int64_t i = 0; i < ncand; i++)
+    if (cand[i] < 0 || cand[i] >= d->nn) return fail(d, WF_ERR_ARG, "contact node out of range");
+  if (d->initialized) return fail(d, WF_ERR_STATE, "options must be set before init");
+  d->contact = true;
+  d->c_z0 = z0;
+  d->c_vz = vz;
+  d->c_k = kpen;
+  d->c_mu = mu;
+  d->cand.assign(cand, cand + ncand);
+  return WF_OK;
+}
+
+// ---- init -------------------------------------------------------------------------
+namespace {
+
+template <typename T>
+cudaError_t upload(wf_domain *d, T **dst, const std::vector<T> &src) {
+  cudaError_t e = dalloc(d, dst, src.size());
+  if (e != cudaSuccess) return e;
+  if (src.empty()) return cudaSuccess;
+  d->h2d_bytes += (int64_t)(src.size() * sizeof(T));
+  return cudaMemcpyAsync(*dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice,
+                         d->stream);
+}
+
+// Per-node BC code: bits 0..2 = constrained dofs, bits 3.. = index of the
+// node's value triple; for repeated entries the later one wins, as the serial
+// BC loops of the reference (Domain_d.C:1109-1134) leave it.
+void bc_tables(wf_domain *d, std::vector<uint32_t> &code, std::vector<double> &vals) {
+  std::vector<uint8_t> mask(d->nn, 0);
+  std::vector<double> v3(3 * d->nn, 0.0);
+  for (int k = 0; k < 3; k++)
+    for (size_t i = 0; i < d->bc_nod[k].size(); i++) {
+      const int64_t n = d->bc_nod[k][i];
+      mask[n] |= (uint8_t)(1u << k);
+      v3[3 * n + k] = d->bc_val[k][i];
+    }
+  std::map<std::tuple<double, double, double>, uint32_t> sets;
+  vals.assign(3, 0.0);
+  sets[std::make_tuple(0.0, 0.0, 0.0)] = 0;
+  code.assign(d->nn, 0u);
+  for (int64_t n = 0; n < d->nn; n++) {
+    if (!mask[n]) continue;
+    auto key = std::make_tuple(v3[3 * n], v3[3 * n + 1], v3[3 * n + 2]);
+    uint32_t id;
+    auto it = sets.find(key);
+    if (it == sets.end()) {
+      id = (uint32_t)(vals.size() / 3);
+      sets[key] = id;
+      vals.push_back(v3[3 * n]);
+      vals.push_back(v3[3 * n + 1]);
+      vals.push_back(v3[3 * n + 2]);
+    } else {
+      id = it->second;
+    }
+    code[n] = (id << 3) | mask[n];
+  }
+}
+
+template <typename T>
+std::vector<T> soa3(const std::vector<double> &aos, int64_t nn, int64_t np) {
+  std::vector<T> out(3 * np, T(0));
+  for (int64_t n = 0; n < nn; n++)
+    for (int k = 0; k < 3; k++) out[k * np + n] = (T)aos[3 * n + k];
+  return out;
+}
+
+}  // namespace
+
+WF_API wf_status wf_init(wf_domain *d) {
+  wf_status s = need_mesh(d);
+  if (s) return s;
+  if (d->mats.empty()) return fail(d, WF_ERR_STATE, "no material assigned (AssignMaterial)");
+  if (!(d->dt > 0.0)) return fail(d, WF_ERR_STATE, "time step not set (SetDT)");
+  if (d->precision == WF_MIXED) {
+    if (d->press_alg != 0 || d->av[0] != 0.0 || d->av[1] != 0.0)
+      return fail(d, WF_ERR_UNSUPPORTED, "mixed precision supports pressure algorithm 0 without "
+                                         "artificial viscosity");
+    const double *sp = &d->stab.alpha_free;
+    for (int i = 0; i < 10; i++)
+      if (sp[i] != 0.0)
+        return fail(d, WF_ERR_UNSUPPORTED, "mixed precision supports default stabilisation only");
+  }
+  CUDA_TRY(cudaSetDevice(d->device));
+  free_device(d);
+  const int64_t nn = d->nn, ne = d->ne;
+  const int64_t np = (nn + 31) / 32 * 32;
+  d->np = np;
+  StepParams &P = d->P;
+  P = StepParams{};
+  P.nn = nn;
+  P.ne = ne;
+  P.np = np;
+  P.npe = d->npe;
+  P.mass_mode = d->mass_mode;
+  P.press_alg = d->press_alg;
+  P.react_dim = d->react_dim;
+  P.contact = d->contact ? 1 : 0;
+  const double *sp = &d->stab.alpha_free;
+  for (int i = 0; i < 10; i++) {
+    P.stab[i] = sp[i];
+    if (sp[i] != 0.0) P.stab_on = 1;
+  }
+  P.av[0] = d->av[0];
+  P.av[1] = d->av[1];
+  P.av_on = (d->av[0] != 0.0 || d->av[1] != 0.0) ? 1 : 0;
+  P.hg_on = (d->hg != 0.0 && d->npe == 8) ? 1 : 0;
+  P.hg_coef = d->hg;
+  const double rho_b = 0.818200;  // Solver_explicit.C:193-197
+  P.alpha = (2.0 * rho_b - 1.0) / (1.0 + rho_b);
+  P.beta = (5.0 - 3.0 * rho_b) / ((1.0 + rho_b) * (1.0 + rho_b) * (2.0 - rho_b));
+  P.gamma = 1.5 - P.alpha;
+  P.fcorr = 1.0 / (1.0 - P.alpha);
+  P.dt = d->dt;
+  P.c_z0 = d->c_z0;
+  P.c_vz = d->c_vz;
+  P.c_k = d->c_k;
+  P.c_mu = d->c_mu;
+
+  // connectivity (SoA elnod), node lists as slots e*npe + local
+  std::vector<int32_t> elsoa(ne * d->npe);
+  for (int64_t e = 0; e < ne; e++)
+    for (int a = 0; a < d->npe; a++) elsoa[a * ne + e] = d->elnod[e * d->npe + a];
+  std::vector<int32_t> slots(d->nodel.size());
+  for (size_t k = 0; k < slots.size(); k++) slots[k] = d->nodel[k] * d->npe + d->nodel_loc[k];
+  int32_t *el = nullptr, *off = nullptr, *sl = nullptr;
+  CUDA_TRY(upload(d, &el, elsoa));
+  CUDA_TRY(upload(d, &off, d->nodel_off));
+  CUDA_TRY(upload(d, &sl, slots));
+  P.elnod = el;
+  P.off = off;
+  P.slot = sl;
+  std::vector<uint32_t> code;
+  std::vector<double> vals;
+  bc_tables(d, code, vals);
+  uint32_t *bc = nullptr;
+  double *bcv = nullptr;
+  CUDA_TRY(upload(d, &bc, code));
+  CUDA_TRY(upload(d, &bcv, vals));
+  P.bc = bc;
+  P.bcval = bcv;
+  std::vector<uint8_t> flags(nn, 0);
+  for (int32_t n : d->react_nodes) flags[n] |= NF_REACTION;
+  for (int32_t n : d->cand) flags[n] |= NF_CONTACT;
+  uint8_t *fl = nullptr;
+  CUDA_TRY(upload(d, &fl, flags));
+  P.nflag = fl;
+  // materials (Elastic_, Material.cuh:24-27; InitHollomon, :90-104)
+  std::vector<MatDev> md(d->mats.size());
+  for (size_t i = 0; i < d->mats.size(); i++) {
+    const wf_material &m = d->mats[i];
+    MatDev &t = md[i];
+    t = MatDev{};
+    t.E = m.E;
+    t.K = m.E / (3.0 * (1.0 - 2.0 * m.nu));
+    t.G = m.E / (2.0 * (1.0 + m.nu));
+    t.sy0 = m.sy0;
+    t.H = m.H;
+    t.cs0 = std::sqrt(t.K / m.rho);
+    t.model = m.model;
+    t.hol_K = m.hol_K;
+    t.hol_m = m.hol_m;
+    if (m.model == WF_MAT_HOLLOMON) {
+      t.eps0 = m.sy0 / m.E;
+      t.eps1 = std::pow(m.sy0 / m.hol_K, 1. / m.hol_m);
+    }
+  }
+  MatDev *mdev = nullptr;
+  CUDA_TRY(upload(d, &mdev, md));
+  P.mats = mdev;
+  P.k0 = md[0].K;
+  if (!d->emat.empty()) {
+    int32_t *em = nullptr;
+    CUDA_TRY(upload(d, &em, d->emat));
+    P.emat = em;
+  }
+  // reaction history and step state
+  d->node_grid = (d->precision == WF_MIXED) ? mix_node_grid(nn) : fp64_node_grid(nn);
+  CUDA_TRY(dalloc(d, &P.partials, d->node_grid));
+  d->hist_cap = 1 << 16;
+  CUDA_TRY(dalloc(d, &P.hist, d->hist_cap));
+  P.hist_cap = d->hist_cap;
+  CUDA_TRY(dalloc(d, &P.st, 1));
+
+  // FP64 state (also the export target of the mixed state)
+  Fp64State &S = d->S;
+  std::vector<double> xs = soa3<double>(d->x, nn, np);
+  CUDA_TRY(upload(d, &S.x, xs));
+  const bool fp64 = d->precision == WF_FP64;
+  CUDA_TRY(dalloc(d, &S.v, 3 * np));
+  CUDA_TRY(dalloc(d, &S.pa, 3 * np));
+  CUDA_TRY(dalloc(d, &S.u, 3 * np));
+  CUDA_TRY(dalloc(d, &S.fi, 3 * np));
+  CUDA_TRY(dalloc(d, &S.cf, 3 * np));
+  CUDA_TRY(dalloc(d, &S.mass, np));
+  CUDA_TRY(dalloc(d, &S.voln, np));
+  CUDA_TRY(dalloc(d, &S.vol, ne));
+  CUDA_TRY(dalloc(d, &S.vol0, ne));
+  CUDA_TRY(dalloc(d, &S.rho, ne));
+  CUDA_TRY(dalloc(d, &S.detJ, ne));
+  CUDA_TRY(dalloc(d, &S.p, ne));
+  CUDA_TRY(dalloc(d, &S.pls, ne));
+  CUDA_TRY(dalloc(d, &S.sy, ne));
+  CUDA_TRY(dalloc(d, &S.tau, 6 * ne));
+  CUDA_TRY(dalloc(d, &S.sig, 6 * ne));
+  CUDA_TRY(dalloc(d, &S.eps, 6 * ne));
+  CUDA_TRY(dalloc(d, &S.jr, np));
+  CUDA_TRY(dalloc(d, &S.s0, np));
+  if (fp64) {
+    CUDA_TRY(dalloc(d, &S.vp, 3 * np));
+    CUDA_TRY(dalloc(d, &S.ut, 3 * np));
+    CUDA_TRY(dalloc(d, &S.sr, 6 * ne));
+    CUDA_TRY(dalloc(d, &S.rr, 6 * ne));
+    CUDA_TRY(dalloc(d, &S.fe, (size_t)ne * d->npe * 3));
+    if (P.hg_on) CUDA_TRY(dalloc(d, &S.fhg, (size_t)ne * d->npe * 3));
+  }
+  std::vector<double> rho0(ne, d->rho_all);
+  CUDA_TRY(upload(d, &d->rho0_dev, rho0));
+
+  // preamble (Solver_explicit.C:120-268): sigma_y = sy0, eps_p = 0; v = a = u
+  // = 0 then ImposeBCV per dimension -- the zeroing sits inside the dimension
+  // loop, so only the last dimension's BC values survive into step 1.
+  {
+    std::vector<double> sy(ne);
+    for (int64_t e = 0; e < ne; e++) sy[e] = d->mats[d->emat.empty() ? 0 : d->emat[e]].sy0;
+    CUDA_TRY(cudaMemcpyAsync(S.sy, sy.data(), sizeof(double) * ne, cudaMemcpyHostToDevice,
+                             d->stream));
+    d->h2d_bytes += (int64_t)(sizeof(double) * (ne + 3 * np));
+    std::vector<double> v0(3 * np, 0.0);
+    for (size_t i = 0; i < d->bc_nod[2].size(); i++)
+      v0[2 * np + d->bc_nod[2][i]] = d->bc_val[2][i];
+    CUDA_TRY(cudaMemcpyAsync(S.v, v0.data(), sizeof(double) * 3 * np, cudaMemcpyHostToDevice,
+                             d->stream));
+  }
+  fp64_geometry(P, S, d->stream, true);
+  CUDA_TRY(cudaMemcpyAsync(S.vol0, S.vol, sizeof(double) * ne, cudaMemcpyDeviceToDevice,
+                           d->stream));
+  fp64_density(P, S, d->rho0_dev, d->stream);
+  fp64_nodal(P, S, d->stream, 1);
+  CUDA_TRY(cudaGetLastError());
+  if (!fp64) {
+    MixState &M = d->M;
+    CUDA_TRY(dalloc(d, &M.xh, 3 * np));
+    CUDA_TRY(dalloc(d, &M.x0, 3 * np));
+    CUDA_TRY(dalloc(d, &M.v, 3 * np));
+    CUDA_TRY(dalloc(d, &M.vp, 3 * np));
+    CUDA_TRY(dalloc(d, &M.pa, 3 * np));
+    CUDA_TRY(dalloc(d, &M.cf, 3 * np));
+    CUDA_TRY(dalloc(d, &M.ut, 2 * np));
+    CUDA_TRY(dalloc(d, &M.mass, np));
+    CUDA_TRY(dalloc(d, &M.jr, np));
+    CUDA_TRY(dalloc(d, &M.nc, np));
+    CUDA_TRY(dalloc(d, &M.pls, ne));
+    CUDA_TRY(dalloc(d, &M.tau, 6 * ne));
+    CUDA_TRY(dalloc(d, &M.fe, (size_t)ne * d->npe * 3));
+    CUDA_TRY(dalloc(d, &d->mvol, ne));
+    std::vector<MatF> mf(md.size());
+    for (size_t i = 0; i < md.size(); i++) {
+      mf[i] = MatF{};
+      mf[i].K = (float)md[i].K;
+      mf[i].G = (float)md[i].G;
+      mf[i].sy0 = (float)md[i].sy0;
+      mf[i].H = (float)md[i].H;
+      mf[i].cs0 = (float)md[i].cs0;
+      mf[i].rho = (float)d->mats[i].rho;
+      mf[i].hol_K = (float)md[i].hol_K;
+      mf[i].hol_m = (float)md[i].hol_m;
+      mf[i].eps0 = (float)md[i].eps0;
+      mf[i].eps1 = (float)md[i].eps1;
+      mf[i].model = md[i].model;
+    }
+    MatF *mfd = nullptr;
+    CUDA_TRY(upload(d, &mfd, mf));
+    P.matf = mfd;
+    P.f_dt = (float)P.dt;
+    P.f_alpha = (float)P.alpha;
+    P.f_fcorr = (float)P.fcorr;
+    P.f_cu_pred = (float)((0.5 - P.beta) * P.dt);
+    P.f_cu_corr = (float)(P.beta * P.dt * P.dt);
+    P.f_cv_corr = (float)(P.gamma * P.dt);
+    P.f_cv_pred = (float)((1.0 - P.gamma) * P.dt);
+    P.f_hg_coef = (float)P.hg_coef;
+    P.f_c_k = (float)P.c_k;
+    P.f_c_mu = (float)P.c_mu;
+    mix_init(P, M, S, d->stream);
+    CUDA_TRY(cudaGetLastError());
+    d->mix_valid_fp64 = true;
+  }
+  CUDA_TRY(cudaStreamSynchronize(d->stream));
+  d->initialized = true;
+  d->host_step = 0;
+  d->host_time = 0.0;
+  d->launches = 0;
+  return WF_OK;
+}
+
+// ---- run --------------------------------------------------------------------------
+namespace {
+
+void launch_step(wf_domain *d) {
+  const StepParams &P = d->P;
+  if (d->precision == WF_FP64) {
+    fp64_geometry(P, d->S, d->stream, false);
+    fp64_nodal(P, d->S, d->stream, 0);
+    fp64_elements(P, d->S, d->stream);
+    fp64_nodes(P, d->S, d->stream, d->node_grid);
+  } else {
+    mix_geometry(P, d->M, d->mvol, d->stream);
+    mix_nodal(P, d->M, d->mvol, d->stream);
+    mix_elements(P, d->M, d->mvol, d->stream);
+    mix_nodes(P, d->M, d->stream, d->node_grid);
+  }
+}
+
+void launch_step_timed(wf_domain *d, cudaEvent_t *ev) {
+  const StepParams &P = d->P;
+  cudaEventRecord(ev[0], d->stream);
+  if (d->precision == WF_FP64) {
+    fp64_geometry(P, d->S, d->stream, false);
+    cudaEventRecord(ev[1], d->stream);
+    fp64_nodal(P, d->S, d->stream, 0);
+    cudaEventRecord(ev[2], d->stream);
+    fp64_elements(P, d->S, d->stream);
+    cudaEventRecord(ev[3], d->stream);
+    fp64_nodes(P, d->S, d->stream, d->node_grid);
+  } else {
+    mix_geometry(P, d->M, d->mvol, d->stream);
+    cudaEventRecord(ev[1], d->stream);
+    mix_nodal(P, d->M, d->mvol, d->stream);
+    cudaEventRecord(ev[2], d->stream);
+    mix_elements(P, d->M, d->mvol, d->stream);
+    cudaEventRecord(ev[3], d->stream);
+    mix_nodes(P, d->M, d->stream, d->node_grid);
+  }
+  cudaEventRecord(ev[4], d->stream);
+}
+
+// Folds the recorded events into the per-phase sums (waits for them).
+wf_status collect_phase_events(wf_domain *d) {
+  for (size_t i = 0; i + 5 <= d->ev_used; i += 5) {
+    CUDA_TRY(cudaEventSynchronize(d->ev_pool[i + 4]));
+    for (int k = 0; k < 4; k++) {
+      float ms = 0.f;
+      CUDA_TRY(cudaEventElapsedTime(&ms, d->ev_pool[i + k], d->ev_pool[i + k + 1]));
+      d->phase_ms[k] += ms;
+    }
+    d->phase_steps++;
+  }
+  d->ev_used = 0;
+  return WF_OK;
+}
+
+constexpr int kGraphSteps = 32;
+
+wf_status ensure_graph(wf_domain *d) {
+  if (d->graph) return WF_OK;
+  cudaGraph_t g = nullptr;
+  CUDA_TRY(cudaStreamBeginCapture(d->stream, cudaStreamCaptureModeThreadLocal));
+  for (int i = 0; i < kGraphSteps; i++) launch_step(d);
+  cudaError_t e = cudaStreamEndCapture(d->stream, &g);
+  if (e != cudaSuccess) return fail(d, WF_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
+  e = cudaGraphInstantiate(&d->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return fail(d, WF_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+  d->graph_steps = kGraphSteps;
+  return WF_OK;
+}
+
+}  // namespace
+
+WF_API wf_status wf_run(wf_domain *d, int64_t nsteps) {
+  if (!d || nsteps < 0) return WF_ERR_ARG;
+  if (!d->initialized) return fail(d, WF_ERR_STATE, "wf_init not called");
+  if (nsteps == 0) return WF_OK;
+  CUDA_TRY(cudaSetDevice(d->device));
+  if (d->host_step + nsteps > d->hist_cap) {
+    // grow the reaction history (device copy of what is recorded so far)
+    int64_t cap = d->hist_cap;
+    while (cap < d->host_step + nsteps) cap *= 2;
+    double *nh = nullptr;
+    CUDA_TRY(dalloc(d, &nh, cap));
+    CUDA_TRY(cudaMemcpyAsync(nh, d->P.hist, sizeof(double) * d->hist_cap, cudaMemcpyDeviceToDevice,
+                             d->stream));
+    d->P.hist = nh;
+    d->P.hist_cap = cap;
+    d->hist_cap = cap;
+    if (d->graph) {
+      cudaGraphExecDestroy(d->graph);
+      d->graph = nullptr;
+    }
+  }
+  d->P.dt = d->dt;
+  if (d->precision == WF_FP64)
+    fp64_predict(d->P, d->S, d->stream);
+  else
+    mix_predict(d->P, d->M, d->stream);
+  CUDA_TRY(cudaGetLastError());
+  d->launches += 1;
+  int64_t left = nsteps;
+  if (d->phase_timing) {
+    for (int64_t i = 0; i < nsteps; i++) {
+      if (d->ev_used + 5 > d->ev_pool.size()) {
+        wf_status cs = collect_phase_events(d);
+        if (cs) return cs;
+        if (d->ev_pool.size() < 5 * 256) {
+          while (d->ev_pool.size() < 5 * 256) {
+            cudaEvent_t ev;
+            CUDA_TRY(cudaEventCreate(&ev));
+            d->ev_pool.push_back(ev);
+          }
+        }
+      }
+      launch_step_timed(d, &d->ev_pool[d->ev_used]);
+      d->ev_used += 5;
+    }
+    left = 0;
+  }
+  d->launches += 4 * nsteps;
+  if (left >= kGraphSteps) {
+    wf_status s = ensure_graph(d);
+    if (s) return s;
+    while (left >= kGraphSteps) {
+      CUDA_TRY(cudaGraphLaunch(d->graph, d->stream));
+      left -= kGraphSteps;
+    }
+  }
+  for (int64_t i = 0; i < left; i++) launch_step(d);
+  CUDA_TRY(cudaGetLastError());
+  for (int64_t i = 0; i < nsteps; i++) d->host_time += d->dt;
+  d->host_step += nsteps;
+  d->mix_valid_fp64 = false;
+  return WF_OK;
+}
+
+WF_API wf_status wf_solve(wf_domain *d, int64_t *nsteps) {
+  if (!d) return WF_ERR_ARG;
+  if (!d->initialized) return fail(d, WF_ERR_STATE, "wf_init not called");
+  // count the iterations of `while (Time < end_t) { ...; Time += dt; }`
+  int64_t n = 0;
+  double t = d->host_time;
+  while (t < d->end_t) {
+    t += d->dt;
+    n++;
+  }
+  wf_status s = wf_run(d, n);
+  if (nsteps) *nsteps = n;
+  if (s) return s;
+  return wf_sync(d);
+}
+
+WF_API wf_status wf_sync(wf_domain *d) {
+  if (!d) return WF_ERR_ARG;
+  CUDA_TRY(cudaSetDevice(d->device));
+  CUDA_TRY(cudaStreamSynchronize(d->stream));
+  return WF_OK;
+}
+
+WF_API wf_status wf_get_time(const wf_domain *d, double *t, int64_t *step) {
+  if (!d) return WF_ERR_ARG;
+  if (t) *t = d->host_time;
+  if (step) *step = d->host_step;
+  return WF_OK;
+}
+
+WF_API wf_status wf_min_edge_length(wf_domain *d, double *hmin) {
+  wf_status s = need_mesh(d);
+  if (s) return s;
+  if (!hmin) return WF_ERR_ARG;
+  if (!d->initialized) return fail(d, WF_ERR_STATE, "wf_init not called");
+  CUDA_TRY(cudaSetDevice(d->device));
+  double *out = nullptr;
+  CUDA_TRY(dalloc(d, &out, 1));
+  if (d->precision == WF_MIXED && !d->mix_valid_fp64) {
+    mix_export(d->P, d->M, d->S, d->mvol, d->stream);
+    d->mix_valid_fp64 = true;
+  }
+  min_edge_length(d->P.elnod, d->S.x, d->np, d->ne, d->npe, out, d->stream);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaMemcpyAsync(hmin, out, sizeof(double), cudaMemcpyDeviceToHost, d->stream));
+  CUDA_TRY(cudaStreamSynchronize(d->stream));
+  return WF_OK;
+}
+
+// ---- readback --------------------------------------------------------------------
+namespace {
+
+wf_status ready_for_readback(wf_domain *d) {
+  if (!d) return WF_ERR_ARG;
+  if (!d->initialized) return fail(d, WF_ERR_STATE, "wf_init not called");
+  CUDA_TRY(cudaSetDevice(d->device));
+  if (d->precision == WF_MIXED && !d->mix_valid_fp64) {
+    mix_export(d->P, d->M, d->S, d->mvol, d->stream);
+    CUDA_TRY(cudaGetLastError());
+    d->mix_valid_fp64 = true;
+  }
+  return WF_OK;
+}
+
+wf_status copy_node3(wf_domain *d, const double *src, double *out) {
+  std::vector<double> tmp(3 * d->np);
+  d->d2h_bytes += (int64_t)(sizeof(double) * 3 * d->np);
+  CUDA_TRY(cudaMemcpyAsync(tmp.data(), src, sizeof(double) * 3 * d->np, cudaMemcpyDeviceToHost,
+                           d->stream));
+  CUDA_TRY(cudaStreamSynchronize(d->stream));
+  for (int64_t n = 0; n < d->nn; n++)
+    for (int k = 0; k < 3; k++) out[3 * n + k] = tmp[k * d->np + n];
+  return WF_OK;
+}
+
+wf_status copy_plain(wf_domain *d, const double *src, double *out, size_t count) {
+  d->d2h_bytes += (int64_t)(sizeof(double) * count);
+  CUDA_TRY(cudaMemcpyAsync(out, src, sizeof(double) * count, cudaMemcpyDeviceToHost, d->stream));
+  CUDA_TRY(cudaStreamSynchronize(d->stream));
+  return WF_OK;
+}
+
+}  // namespace
+
+WF_API wf_status wf_get_node_field(wf_domain *d, int32_t field, double *out) {
+  wf_status s = ready_for_readback(d);
+  if (s) return s;
+  if (!out) return WF_ERR_ARG;
+  const Fp64State &S = d->S;
+  switch (field) {
+    case WF_NODE_X: return copy_node3(d, S.x, out);
+    case WF_NODE_V: return copy_node3(d, S.v, out);
+    case WF_NODE_A:  // after a step the reference's a equals prev_a
+    case WF_NODE_PREV_A: return copy_node3(d, S.pa, out);
+    case WF_NODE_U: return copy_node3(d, S.u, out);
+    case WF_NODE_FI: return copy_node3(d, S.fi, out);
+    case WF_NODE_CONTFORCE: return copy_node3(d, S.cf, out);
+  }
+  return fail(d, WF_ERR_ARG, "unknown node field %d", field);
+}
+
+WF_API wf_status wf_get_node_scalar(wf_domain *d, int32_t field, double *out) {
+  wf_status s = ready_for_readback(d);
+  if (s) return s;
+  if (!out) return WF_ERR_ARG;
+  std::vector<double> tmp(d->np);
+  if (field == WF_NODE_MASS || field == WF_NODE_VOLN) {
+    s = copy_plain(d, field == WF_NODE_MASS ? d->S.mass : d->S.voln, tmp.data(), d->np);
+    if (s) return s;
+    std::copy(tmp.begin(), tmp.begin() + d->nn, out);
+    return WF_OK;
+  }
+  if (field == WF_NODE_PRESSURE) {
+    // calcNodalPressureFromElemental (Mechanical.C:1187-1213), serial order
+    std::vector<double> p(d->ne), vol(d->ne);
+    s = copy_plain(d, d->S.p, p.data(), d->ne);
+    if (s) return s;
+    s = copy_plain(d, d->S.vol, vol.data(), d->ne);
+    if (s) return s;
+    std::vector<double> acc(d->nn, 0.0);
+    for (int64_t n = 0; n < d->nn; n++) out[n] = 0.0;
+    for (int64_t e = 0; e < d->ne; e++)
+      for (int a = 0; a < d->npe; a++) {
+        int32_t nid = d->elnod[e * d->npe + a];
+        out[nid] += p[e] * vol[e];
+        acc[nid] += vol[e];
+      }
+    for (int64_t n = 0; n < d->nn; n++)
+      if (acc[n] > 0.0) out[n] /= acc[n];
+    return WF_OK;
+  }
+  return fail(d, WF_ERR_ARG, "unknown node scalar %d", field);
+}
+
+WF_API wf_status wf_get_elem_scalar(wf_domain *d, int32_t field, double *out) {
+  wf_status s = ready_for_readback(d);
+  if (s) return s;
+  if (!out) return WF_ERR_ARG;
+  const Fp64State &S = d->S;
+  const double *src = nullptr;
+  switch (field) {
+    case WF_ELEM_VOL: src = S.vol; break;
+    case WF_ELEM_VOL0: src = S.vol0; break;
+    case WF_ELEM_DETJ: src = S.detJ; break;
+    case WF_ELEM_P: src = S.p; break;
+    case WF_ELEM_PL_STRAIN: src = S.pls; break;
+    case WF_ELEM_SIGMA_Y: src = S.sy; break;
+    case WF_ELEM_RHO: src = S.rho; break;
+    default: return fail(d, WF_ERR_ARG, "unknown element scalar %d", field);
+  }
+  if (field == WF_ELEM_DETJ) {
+    // refresh detJ for the current coordinates
+    fp64_geometry(d->P, d->S, d->stream, true);
+    CUDA_TRY(cudaGetLastError());
+  }
+  return copy_plain(d, src, out, d->ne);
+}
+
+WF_API wf_status wf_get_elem_tensor(wf_domain *d, int32_t field, double *out) {
+  wf_status s = ready_for_readback(d);
+  if (s) return s;
+  if (!out) return WF_ERR_ARG;
+  const Fp64State &S = d->S;
+  const double *src = nullptr;
+  switch (field) {
+    case WF_ELEM_SIGMA: src = S.sig; break;
+    case WF_ELEM_TAU: src = S.tau; break;
+    case WF_ELEM_EPS: src = S.eps; break;
+    case WF_ELEM_STR_RATE: src = S.sr; break;
+    case WF_ELEM_ROT_RATE: src = S.rr; break;
+    default: return fail(d, WF_ERR_ARG, "unknown element tensor %d", field);
+  }
+  if (!src) return fail(d, WF_ERR_UNSUPPORTED, "field not kept in mixed precision");
+  std::vector<double> tmp(6 * d->ne);
+  s = copy_plain(d, src, tmp.data(), 6 * d->ne);
+  if (s) return s;
+  for (int64_t e = 0; e < d->ne; e++)
+    for (int c = 0; c < 6; c++) out[6 * e + c] = tmp[c * d->ne + e];
+  return WF_OK;
+}
+
+WF_API wf_status wf_get_disp(wf_domain *d, double *out) { return wf_get_node_field(d, WF_NODE_U, out); }
+WF_API wf_status wf_get_vel(wf_domain *d, double *out) { return wf_get_node_field(d, WF_NODE_V, out); }
+WF_API wf_status wf_get_pl_strain(wf_domain *d, double *out) {
+  return wf_get_elem_scalar(d, WF_ELEM_PL_STRAIN, out);
+}
+
+WF_API wf_status wf_get_reaction_history(wf_domain *d, double *out, int64_t cap, int64_t *n) {
+  if (!d) return WF_ERR_ARG;
+  if (!d->initialized) return fail(d, WF_ERR_STATE, "wf_init not called");
+  CUDA_TRY(cudaSetDevice(d->device));
+  const int64_t have = d->host_step;
+  if (n) *n = have;
+  const int64_t m = std::min(cap, have);
+  if (out && m > 0) {
+    d->d2h_bytes += (int64_t)(sizeof(double) * m);
+    CUDA_TRY(cudaMemcpyAsync(out, d->P.hist, sizeof(double) * m, cudaMemcpyDeviceToHost, d->stream));
+  }
+  CUDA_TRY(cudaStreamSynchronize(d->stream));
+  return WF_OK;
+}
+
+WF_API wf_status wf_set_node_state(wf_domain *d, const double *x, const double *v,
+                                   const double *prev_a, const double *u) {
+  if (!d) return WF_ERR_ARG;
+  if (!d->initialized) return fail(d, WF_ERR_STATE, "wf_init not called");
+  if (d->precision != WF_FP64)
+    return fail(d, WF_ERR_UNSUPPORTED, "node state upload is FP64-only");
+  CUDA_TRY(cudaSetDevice(d->device));
+  const double *srcs[4] = {x, v, prev_a, u};
+  double *dsts[4] = {d->S.x, d->S.v, d->S.pa, d->S.u};
+  for (int i = 0; i < 4; i++) {
+    if (!srcs[i]) continue;
+    std::vector<double> soa(3 * d->np, 0.0);
+    for (int64_t n = 0; n < d->nn; n++)
+      for (int k = 0; k < 3; k++) soa[k * d->np + n] = srcs[i][3 * n + k];
+    CUDA_TRY(cudaMemcpyAsync(dsts[i], soa.data(), sizeof(double) * 3 * d->np,
+                             cudaMemcpyHostToDevice, d->stream));
+    CUDA_TRY(cudaStreamSynchronize(d->stream));
+  }
+  return WF_OK;
+}
+
+
+
+WF_API wf_status wf_set_phase_timing(wf_domain *d, int32_t on) {
+  if (!d) return WF_ERR_ARG;
+  d->phase_timing = on != 0;
+  return WF_OK;
+}
+
+WF_API wf_status wf_get_phase_times(wf_domain *d, double ms[4], int64_t *steps, int32_t reset) {
+  if (!d || !ms) return WF_ERR_ARG;
+  CUDA_TRY(cudaSetDevice(d->device));
+  wf_status s = collect_phase_events(d);
+  if (s) return s;
+  for (int k = 0; k < 4; k++) ms[k] = d->phase_ms[k];
+  if (steps) *steps = d->phase_steps;
+  if (reset) {
+    for (int k = 0; k < 4; k++) d->phase_ms[k] = 0.0;
+    d->phase_steps = 0;
+  }
+  return WF_OK;
+}
+
+WF_API wf_status wf_get_launch_count(const wf_domain *d, int64_t *n) {
+  if (!d || !n) return WF_ERR_ARG;
+  *n = d->launches;
+  return WF_OK;
+}
+
+WF_API wf_status wf_get_stream(const wf_domain *d, void **stream) {
+  if (!d || !stream) return WF_ERR_ARG;
+  *stream = (void *)d->stream;
+  return WF_OK;
+}
+
+WF_API wf_status wf_get_transfer_bytes(const wf_domain *d, int64_t *h2d, int64_t *d2h) {
+  if (!d) return WF_ERR_ARG;
+  if (h2d) *h2d = d->h2d_bytes;
+  if (d2h) *d2h = d->d2h_bytes;
+  return WF_OK;
+}

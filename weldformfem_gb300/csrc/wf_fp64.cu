@@ -1,0 +1,667 @@
+// FP64 step kernels: the reference's arithmetic, operation for operation.
+//
+// This translation unit is compiled with --fmad=false so that every
+// expression rounds exactly as the reference CPU code does with FMA
+// contraction off (the reference build passes --fmad=false to nvcc,
+// src/common/CMakeLists.txt:16). One step is four launches:
+//   geometry  (element): J, detJ, volume             -> vol
+//   nodal     (node)   : volume sums, lumped mass, J ratio
+//   elements  (element): dN, D/W, pressure, Jaumann + radial return,
+//                        B^T sigma, hourglass        -> element forces
+//   nodes     (node)   : deterministic gather of element forces over the
+//                        node->element lists, contact, acceleration, BCs,
+//                        Chung-Hulbert corrector, position update and the
+//                        next step's predictor; reaction sum (last block).
+#include "wf_internal.cuh"
+
+namespace wf {
+namespace {
+
+constexpr int kElemThreads = 128;
+constexpr int kNodeThreads = 256;
+
+// Flanagan-Belytschko hourglass base vectors of the 8-node hexahedron
+// (test_1el_3D.cpp:166-169).
+__constant__ double c_hg_sig[4][8] = {{1., 1., -1., -1., -1., -1., 1., 1.},
+                                      {1., -1., -1., 1., -1., 1., 1., -1.},
+                                      {1., -1., 1., -1., 1., -1., 1., -1.},
+                                      {-1., 1., -1., 1., 1., -1., 1., -1.}};
+
+__device__ __forceinline__ double det3(const double J[3][3]) {
+  // Matrix::calcDet (include/common/Matrix.h:593-620)
+  return J[0][0] * J[1][1] * J[2][2] - J[0][0] * J[1][2] * J[2][1] -
+         J[0][1] * J[1][0] * J[2][2] + J[0][1] * J[1][2] * J[2][0] +
+         J[0][2] * J[1][0] * J[2][1] - J[0][2] * J[1][1] * J[2][0];
+}
+
+// Jacobian of the element from its node coordinates
+// (Domain_d.C:1822-1830 hexahedron, :1866-1870 tetrahedron).
+template <int NPE>
+__device__ __forceinline__ void jacobian(const double (&x2)[NPE][3], double J[3][3]) {
+  if constexpr (NPE == 8) {
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      J[0][k] = 0.125 * (-x2[0][k] + x2[1][k] + x2[2][k] - x2[3][k] - x2[4][k] + x2[5][k] +
+                         x2[6][k] - x2[7][k]);
+      J[1][k] = 0.125 * (-x2[0][k] - x2[1][k] + x2[2][k] + x2[3][k] - x2[4][k] - x2[5][k] +
+                         x2[6][k] + x2[7][k]);
+      J[2][k] = 0.125 * (-x2[0][k] - x2[1][k] - x2[2][k] - x2[3][k] + x2[4][k] + x2[5][k] +
+                         x2[6][k] + x2[7][k]);
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      J[0][k] = x2[1][k] - x2[0][k];
+      J[1][k] = x2[2][k] - x2[0][k];
+      J[2][k] = x2[3][k] - x2[0][k];
+    }
+  }
+}
+
+// dN/dx * detJ from the adjugate of J (AdjMat, Matrix.h:694-727;
+// Domain_d.C:1842-1851 hexahedron, :1881-1887 tetrahedron).
+template <int NPE>
+__device__ __forceinline__ void shape_derivs(const double J[3][3], double dH[3][NPE]) {
+  double inv[3][3];
+  inv[0][0] = (J[1][1] * J[2][2] - J[1][2] * J[2][1]);
+  inv[1][0] = -(J[1][0] * J[2][2] - J[1][2] * J[2][0]);
+  inv[2][0] = (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+  inv[0][1] = -(J[0][1] * J[2][2] - J[0][2] * J[2][1]);
+  inv[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]);
+  inv[2][1] = -(J[0][0] * J[2][1] - J[0][1] * J[2][0]);
+  inv[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]);
+  inv[1][2] = -(J[0][0] * J[1][2] - J[0][2] * J[1][0]);
+  inv[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]);
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const double a0 = inv[k][0], a1 = inv[k][1], a2 = inv[k][2];
+    if constexpr (NPE == 8) {
+      dH[k][0] = 0.125 * (-a0 - a1 - a2);
+      dH[k][1] = 0.125 * (a0 - a1 - a2);
+      dH[k][2] = 0.125 * (a0 + a1 - a2);
+      dH[k][3] = 0.125 * (-a0 + a1 - a2);
+      dH[k][4] = 0.125 * (-a0 - a1 + a2);
+      dH[k][5] = 0.125 * (a0 - a1 + a2);
+      dH[k][6] = 0.125 * (a0 + a1 + a2);
+      dH[k][7] = 0.125 * (-a0 + a1 + a2);
+    } else {
+      dH[k][0] = -a0 - a1 - a2;
+      dH[k][1] = a0;
+      dH[k][2] = a1;
+      dH[k][3] = a2;
+    }
+  }
+}
+
+template <int NPE>
+__device__ __forceinline__ double weight() {
+  return NPE == 8 ? 8.0 : 1.0 / 6.0;
+}
+
+template <int NPE>
+__device__ __forceinline__ void gather_x(const StepParams &P, const double *x, int64_t e,
+                                         double (&x2)[NPE][3], int32_t (&nid)[NPE]) {
+#pragma unroll
+  for (int a = 0; a < NPE; a++) nid[a] = __ldg(&P.elnod[a * P.ne + e]);
+#pragma unroll
+  for (int a = 0; a < NPE; a++) {
+    x2[a][0] = __ldg(&x[nid[a]]);
+    x2[a][1] = __ldg(&x[P.np + nid[a]]);
+    x2[a][2] = __ldg(&x[2 * P.np + nid[a]]);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// geometry: vol = 0.0 + detJ * w * 1.0 (Mechanical.C:264-293)
+template <int NPE>
+__global__ void __launch_bounds__(kElemThreads) k_geometry(StepParams P, Fp64State S,
+                                                           int store_detj) {
+  int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= P.ne) return;
+  double x2[NPE][3];
+  int32_t nid[NPE];
+  gather_x<NPE>(P, S.x, e, x2, nid);
+  double J[3][3];
+  jacobian<NPE>(x2, J);
+  double detJ = det3(J);
+  double v = 0.0;
+  v += detJ * weight<NPE>() * 1.0;
+  S.vol[e] = v;
+  if (store_detj) S.detJ[e] = detJ;
+}
+
+// ---------------------------------------------------------------------------
+// nodal: CalcNodalVol (Mechanical.C:1555-1572), CalcNodalMassFromVol
+// (:1576-1601) and the nodal volume ratio of calcElemPressure (:694-705).
+// init_mode 1 also forms the constant sum of initial volumes.
+template <int NPE>
+__global__ void __launch_bounds__(kNodeThreads) k_nodal(StepParams P, Fp64State S,
+                                                        int init_mode) {
+  int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= P.nn) return;
+  const int32_t b = __ldg(&P.off[n]), c = __ldg(&P.off[n + 1]) - b;
+  double s = 0.0, s0 = 0.0;
+  for (int32_t k = 0; k < c; k++) {
+    int32_t e = __ldg(&P.slot[b + k]) / NPE;
+    s += __ldg(&S.vol[e]);
+    if (init_mode) s0 += __ldg(&S.vol0[e]);
+  }
+  if (init_mode) S.s0[n] = s0;
+  else s0 = S.s0[n];
+  double voln = s;
+  voln /= NPE;
+  S.voln[n] = voln;
+  if (P.mass_mode == 0 || init_mode) {
+    double mass = 0.0;
+    const double f = 1.0;
+    for (int32_t k = 0; k < c; k++) {
+      int32_t e = __ldg(&P.slot[b + k]) / NPE;
+      mass += f * __ldg(&S.rho[e]) * voln / c;
+    }
+    S.mass[n] = mass;
+  }
+  S.jr[n] = s / s0;
+}
+
+// ---------------------------------------------------------------------------
+// tensor3 helpers in the reference's component algebra (Tensor3.C).
+enum { XX, XY, XZ, YX, YY, YZ, ZX, ZY, ZZ };
+
+// operator*(tensor3, tensor3) exactly as include/common/Tensor3.C:290-303
+// writes it (its off-diagonal entries pair the rows of both factors).
+__device__ __forceinline__ void t3_mul(const double *a, const double *b, double *r) {
+  r[XX] = a[XX] * b[XX] + a[XY] * b[YX] + a[XZ] * b[ZX];
+  r[XY] = a[XX] * b[YX] + a[XY] * b[YY] + a[XZ] * b[YZ];
+  r[XZ] = a[XX] * b[ZX] + a[XY] * b[ZY] + a[XZ] * b[ZZ];
+  r[YX] = a[YX] * b[XX] + a[YY] * b[YX] + a[YZ] * b[ZX];
+  r[YY] = a[YX] * b[YX] + a[YY] * b[YY] + a[YZ] * b[YZ];
+  r[YZ] = a[YX] * b[ZX] + a[YY] * b[ZY] + a[YZ] * b[ZZ];
+  r[ZX] = a[ZX] * b[XX] + a[ZY] * b[YX] + a[ZZ] * b[ZX];
+  r[ZY] = a[ZX] * b[YX] + a[ZY] * b[YY] + a[ZZ] * b[YZ];
+  r[ZZ] = a[ZX] * b[ZX] + a[ZY] * b[ZY] + a[ZZ] * b[ZZ];
+}
+
+__device__ __forceinline__ double idv(int i) {
+  return (i == XX || i == YY || i == ZZ) ? 1. : 0.;
+}
+
+__device__ __forceinline__ double hollomon_sy(double strain, const MatDev &m) {
+  if (strain + m.eps0 > m.eps1) return m.hol_K * pow(strain + m.eps0, m.hol_m);
+  return m.sy0;
+}
+__device__ __forceinline__ double hollomon_et(double strain, const MatDev &m) {
+  if (strain + m.eps0 > m.eps1) return m.hol_K * m.hol_m * pow(strain + m.eps0, (m.hol_m - 1.0));
+  return 0.;
+}
+
+// ---------------------------------------------------------------------------
+// elements: calcElemJAndDerivatives, calcElemStrainRates (Mechanical.C:41-126),
+// calcElemPressure (:691-819) or calcElemPressureANP (:1220-1250),
+// CalcStressStrain (:1664-1839), calcArtificialViscosity (:1948-1977),
+// calcElemForces (:375-481) and the 3-D viscous hourglass forces.
+template <int NPE>
+__global__ void __launch_bounds__(kElemThreads) k_elements(StepParams P, Fp64State S) {
+  int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= P.ne) return;
+  const int64_t ne = P.ne;
+  int32_t nid[NPE];
+  double dH[3][NPE];
+  double detJ;
+  {
+    double x2[NPE][3];
+    gather_x<NPE>(P, S.x, e, x2, nid);
+    double J[3][3];
+    jacobian<NPE>(x2, J);
+    shape_derivs<NPE>(J, dH);
+    detJ = det3(J);
+  }
+  double vol = 0.0;
+  vol += detJ * weight<NPE>() * 1.0;
+  const MatDev m = P.mats[P.emat ? __ldg(&P.emat[e]) : 0];
+
+  // strain rate and spin (str_rate / rot_rate, upper triangle)
+  double s00 = 0.0, s11 = 0.0, s22 = 0.0, s01 = 0.0, s12 = 0.0, s02 = 0.0;
+  double w01 = 0.0, w12 = 0.0, w02 = 0.0;
+  double hm[3][4];
+#pragma unroll
+  for (int k = 0; k < 3; k++)
+#pragma unroll
+    for (int j = 0; j < 4; j++) hm[k][j] = 0.0;
+  double div_v = 0.0;
+  const double f = 1.0 / detJ;
+#pragma unroll
+  for (int a = 0; a < NPE; a++) {
+    const double v0 = __ldg(&S.vp[nid[a]]);
+    const double v1 = __ldg(&S.vp[P.np + nid[a]]);
+    const double v2 = __ldg(&S.vp[2 * P.np + nid[a]]);
+    const double d0 = dH[0][a], d1 = dH[1][a], d2 = dH[2][a];
+    s00 = s00 + d0 * f * v0;
+    s11 = s11 + d1 * f * v1;
+    s22 = s22 + d2 * f * v2;
+    s01 = s01 + f * (d1 * v0 + d0 * v1);
+    w01 = w01 + f * (d1 * v0 - d0 * v1);
+    s12 = s12 + f * (d2 * v1 + d1 * v2);
+    s02 = s02 + f * (d2 * v0 + d0 * v2);
+    w12 = w12 + f * (d2 * v1 - d1 * v2);
+    w02 = w02 + f * (d2 * v0 - d0 * v2);
+    if (P.stab_on) div_v += d0 * v0 + d1 * v1 + d2 * v2;
+    if constexpr (NPE == 8) {
+      if (P.hg_on) {
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+          hm[0][j] += v0 * c_hg_sig[j][a];
+          hm[1][j] += v1 * c_hg_sig[j][a];
+          hm[2][j] += v2 * c_hg_sig[j][a];
+        }
+      }
+    }
+  }
+  s01 = s01 * 0.5; s02 = s02 * 0.5; s12 = s12 * 0.5;
+  w01 = w01 * 0.5; w02 = w02 * 0.5; w12 = w12 * 0.5;
+
+  // pressure
+  double p;
+  if (P.press_alg == 1) {
+    p = S.p[e];
+    for (int a = 0; a < NPE; a++) p += P.k0 * (1.0 - __ldg(&S.jr[nid[a]]));
+    p *= 0.25 * NPE;
+  } else {
+    const double K = m.K;
+    const double J_local = vol / __ldg(&S.vol0[e]);
+    double J_avg = 0.0;
+#pragma unroll
+    for (int a = 0; a < NPE; a++) J_avg += __ldg(&S.jr[nid[a]]);
+    J_avg /= NPE;
+    if (!P.stab_on) {
+      // All stabilisation parameters zero: J_bar = 0 * J_local + 1 * J_avg
+      // = J_avg and the 0 * log(J_bar) term adds only a signed zero.
+      double J_bar = J_avg;
+      if (J_bar < 0.0) J_bar = 0.2;
+      p = -K * (J_bar - 1.0);
+    } else {
+      const double *st = P.stab;
+      const double rho_e = S.rho[e];
+      const double h = pow(vol, 1.0 / 3.0);
+      bool is_contact = false;
+      if (P.contact) {
+        for (int a = 0; a < NPE; a++) {
+          double c0 = S.cf[nid[a]], c1 = S.cf[P.np + nid[a]], c2 = S.cf[2 * P.np + nid[a]];
+          if (c0 * c0 + c1 * c1 + c2 * c2 > 0) { is_contact = true; break; }
+        }
+      }
+      double alpha = is_contact ? st[1] : st[0];
+      double J_bar = alpha * J_local + (1 - alpha) * J_avg;
+      if (J_bar < st[9]) J_bar = 0.2;
+      double p_physical = -K * (st[6] * log(J_bar) + (1.0 - st[6]) * (J_bar - 1.0));
+      double c = sqrt(K / rho_e);
+      double tau = h / (2.0 * c);
+      double p_pspg = 0.0;
+      double p_hg = (is_contact ? st[3] : st[2]) * K * fabs(J_local - J_avg);
+      double p_q = 0.0;
+      if (div_v < 0.0) {
+        double t1 = st[7] * tau * div_v * K, t2 = st[8] * K;
+        p_pspg = (t2 < t1) ? t2 : t1;
+        double q1 = st[4] * rho_e * h * c * (-div_v);
+        double delta_J = 1.0 - J_local;
+        double q2 = st[5] * K * delta_J;
+        p_q = is_contact ? 0.5 * (q1 + q2) : ((q1 < q2) ? q2 : q1);
+      }
+      p = p_physical + p_pspg + p_hg + p_q;
+    }
+  }
+
+  // Jaumann rate + radial return (CalcStressStrain)
+  const double dt = P.dt;
+  double SS[9], SR[9], RR[9], RT[9], SRT[9], RS[9];
+  {
+    double t0 = S.tau[e], t1 = S.tau[ne + e], t2 = S.tau[2 * ne + e];
+    double t3 = S.tau[3 * ne + e], t4 = S.tau[4 * ne + e], t5 = S.tau[5 * ne + e];
+    SS[XX] = t0; SS[YY] = t1; SS[ZZ] = t2;
+    SS[XY] = SS[YX] = t3; SS[YZ] = SS[ZY] = t4; SS[XZ] = SS[ZX] = t5;
+  }
+  SR[XX] = s00; SR[YY] = s11; SR[ZZ] = s22;
+  SR[XY] = SR[YX] = s01; SR[YZ] = SR[ZY] = s12; SR[XZ] = SR[ZX] = s02;
+  RR[XX] = 0.0; RR[YY] = 0.0; RR[ZZ] = 0.0;
+  RR[XY] = w01; RR[YZ] = w12; RR[XZ] = w02;
+  RR[YX] = -w01; RR[ZY] = -w12; RR[ZX] = -w02;
+  RT[XX] = RR[XX]; RT[YY] = RR[YY]; RT[ZZ] = RR[ZZ];
+  RT[XY] = RR[YX]; RT[XZ] = RR[ZX]; RT[YX] = RR[XY];
+  RT[YZ] = RR[ZY]; RT[ZX] = RR[XZ]; RT[ZY] = RR[YZ];
+  t3_mul(SS, RT, SRT);
+  t3_mul(RR, SS, RS);
+  {
+    const double c = 1.0 / 3.0 * (SR[XX] + SR[YY] + SR[ZZ]);
+    const double g2 = 2.0 * m.G;
+#pragma unroll
+    for (int i = 0; i < 9; i++) {
+      double A = (SR[i] - idv(i) * c) * g2;
+      A = A + SRT[i];
+      A = A + RS[i];
+      SS[i] = SS[i] + A * dt;
+    }
+  }
+  double ST[9], Sd[9];
+#pragma unroll
+  for (int i = 0; i < 9; i++) ST[i] = idv(i) * (-p) + SS[i];
+  {
+    const double c2 = (1.0 / 3.0) * (ST[XX] + ST[YY] + ST[ZZ]);
+#pragma unroll
+    for (int i = 0; i < 9; i++) Sd[i] = ST[i] - idv(i) * c2;
+  }
+  const double J2 = 0.5 * (Sd[XX] * Sd[XX] + 2.0 * Sd[XY] * Sd[XY] + 2.0 * Sd[XZ] * Sd[XZ] +
+                           Sd[YY] * Sd[YY] + 2.0 * Sd[YZ] * Sd[YZ] + Sd[ZZ] * Sd[ZZ]);
+  const double sig_trial = sqrt(3.0 * J2);
+  double pls = S.pls[e];
+  double sy;
+  if (m.model == WF_MAT_HOLLOMON)
+    sy = hollomon_sy(pls, m);
+  else
+    sy = m.sy0 + m.H * pls;
+  if (sy < sig_trial) {
+    const double H = (m.model == WF_MAT_HOLLOMON) ? hollomon_et(pls, m) : m.H;
+    const double G = m.G;
+    const double dgamma = (sig_trial - sy) / (3.0 * G + H);
+    const double factor = 1.0 - (3.0 * G * dgamma) / sig_trial;
+#pragma unroll
+    for (int i = 0; i < 9; i++) SS[i] = Sd[i] * factor;
+    pls += dgamma;
+  }
+  double SG[9];
+#pragma unroll
+  for (int i = 0; i < 9; i++) SG[i] = idv(i) * (-p) + SS[i];
+  // total strain: eps = eps + dt * D
+  {
+    double e0 = S.eps[e], e1 = S.eps[ne + e], e2 = S.eps[2 * ne + e];
+    double e3 = S.eps[3 * ne + e], e4 = S.eps[4 * ne + e], e5 = S.eps[5 * ne + e];
+    S.eps[e] = e0 + s00 * dt;
+    S.eps[ne + e] = e1 + s11 * dt;
+    S.eps[2 * ne + e] = e2 + s22 * dt;
+    S.eps[3 * ne + e] = e3 + s01 * dt;
+    S.eps[4 * ne + e] = e4 + s12 * dt;
+    S.eps[5 * ne + e] = e5 + s02 * dt;
+  }
+  // artificial viscosity (serial in the reference; per element here)
+  if (P.av_on) {
+    const double c = sqrt(m.K / S.rho[e]);
+    const double eps_v = (s00 + s11 + s22);
+    if (fabs(eps_v) > 1e-12) {
+      const double l = pow(vol, 1.0 / 3.0);
+      double q = P.av[0] * c * fabs(eps_v) * l + P.av[1] * pow(eps_v * l, 2);
+      q = (1e9 < q) ? 1e9 : q;
+      const double qs = (eps_v > 0) ? -q : q;
+      SG[XX] += qs;
+      SG[YY] += qs;
+      SG[ZZ] += qs;
+    }
+  }
+  S.p[e] = p;
+  S.pls[e] = pls;
+  S.sy[e] = sy;
+  const double sg0 = SG[XX], sg1 = SG[YY], sg2 = SG[ZZ], sg3 = SG[XY], sg4 = SG[YZ],
+               sg5 = SG[XZ];
+  S.sig[e] = sg0; S.sig[ne + e] = sg1; S.sig[2 * ne + e] = sg2;
+  S.sig[3 * ne + e] = sg3; S.sig[4 * ne + e] = sg4; S.sig[5 * ne + e] = sg5;
+  S.tau[e] = SS[XX]; S.tau[ne + e] = SS[YY]; S.tau[2 * ne + e] = SS[ZZ];
+  S.tau[3 * ne + e] = SS[XY]; S.tau[4 * ne + e] = SS[YZ]; S.tau[5 * ne + e] = SS[XZ];
+  S.sr[e] = s00; S.sr[ne + e] = s11; S.sr[2 * ne + e] = s22;
+  S.sr[3 * ne + e] = s01; S.sr[4 * ne + e] = s12; S.sr[5 * ne + e] = s02;
+  S.rr[e] = 0.0; S.rr[ne + e] = 0.0; S.rr[2 * ne + e] = 0.0;
+  S.rr[3 * ne + e] = w01; S.rr[4 * ne + e] = w12; S.rr[5 * ne + e] = w02;
+
+  // element forces f = w * B^T sigma (3-D branch of calcElemForces)
+  double *fe = &S.fe[e * NPE * 3];
+  const double w = weight<NPE>();
+#pragma unroll
+  for (int a = 0; a < NPE; a++) {
+    const double d0 = dH[0][a], d1 = dH[1][a], d2 = dH[2][a];
+    double f0 = 0.0, f1 = 0.0, f2 = 0.0;
+    f0 += d0 * sg0 * 1.0;
+    f1 += d1 * sg1 * 1.0;
+    f2 += d2 * sg2 * 1.0;
+    f0 += d1 * sg3 + d2 * sg5;
+    f1 += d0 * sg3 + d2 * sg4;
+    f2 += d1 * sg4 + d0 * sg5;
+    fe[3 * a] = f0 * w;
+    fe[3 * a + 1] = f1 * w;
+    fe[3 * a + 2] = f2 * w;
+  }
+  if constexpr (NPE == 8) {
+    if (P.hg_on) {
+      const double ch = P.hg_coef * pow(vol, 0.6666666) * S.rho[e] * 0.25 * m.cs0;
+      double *fh = &S.fhg[e * 24];
+#pragma unroll
+      for (int i = 0; i < 8; i++) {
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+          double acc = 0.0;
+#pragma unroll
+          for (int j = 0; j < 4; j++) acc -= ch * hm[k][j] * c_hg_sig[j][i];
+          fh[3 * i + k] = acc;
+        }
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// deterministic block sum (fixed shuffle tree, warps combined in order)
+__device__ __forceinline__ double block_sum(double v, double *sh) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < (int)(blockDim.x >> 5); i++) t += sh[i];
+  }
+  return t;
+}
+
+// nodes: assemblyForces (Matrices.C:42-87) as a gather over the node's
+// element list, the non-finite clamp (Solver_explicit.C:777-785), plane
+// contact (Contact.C:58-323), calcAccel (Mechanical.C:321-341), ImposeBCA,
+// UpdateCorrectionAccVel (Domain_d.C:981-997), ImposeBCV,
+// UpdateCorrectionPos (:1005-1025) and the next step's UpdatePrediction
+// (:961-974) + ImposeBCV, which this kernel hands to the next step as vp.
+template <int NPE>
+__global__ void __launch_bounds__(kNodeThreads) k_nodes(StepParams P, Fp64State S) {
+  __shared__ double sh[kNodeThreads / 32];
+  __shared__ bool am_last;
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const double time = P.st->time;
+  double r = 0.0;
+  if (n < P.nn) {
+    const int64_t np = P.np;
+    const int32_t b = __ldg(&P.off[n]), c = __ldg(&P.off[n + 1]) - b;
+    double fi[3] = {0.0, 0.0, 0.0};
+    for (int32_t k = 0; k < c; k++) {
+      const int64_t base = (int64_t)__ldg(&P.slot[b + k]) * 3;
+      fi[0] += __ldg(&S.fe[base]);
+      fi[1] += __ldg(&S.fe[base + 1]);
+      fi[2] += __ldg(&S.fe[base + 2]);
+    }
+    if (P.hg_on) {
+      for (int32_t k = 0; k < c; k++) {
+        const int64_t base = (int64_t)__ldg(&P.slot[b + k]) * 3;
+        fi[0] -= __ldg(&S.fhg[base]);
+        fi[1] -= __ldg(&S.fhg[base + 1]);
+        fi[2] -= __ldg(&S.fhg[base + 2]);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      if (!isfinite(fi[k])) {
+        fi[k] = 0.0;
+        atomicOr(&P.st->status, 1u);
+      }
+      S.fi[k * np + n] = fi[k];
+    }
+    const uint8_t fl = P.nflag[n];
+    const double mass = S.mass[n];
+    double x[3], vold[3], vp[3], pa[3], u[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      x[k] = S.x[k * np + n];
+      vold[k] = S.v[k * np + n];
+      vp[k] = S.vp[k * np + n];
+      pa[k] = S.pa[k * np + n];
+      u[k] = S.u[k * np + n];
+    }
+    double cf[3] = {0.0, 0.0, 0.0};
+    if (P.contact && (fl & NF_CONTACT)) {
+      // rigid plane, outward normal (0, 0, -1), at z0 + vz * Time
+      const double zd = P.c_z0 + P.c_vz * time;
+      const double gap = zd - x[2];
+      if (gap < 0) {
+        // kcont = min(k_geometric, 0.2 m / dt^2) (Contact.C:190-193)
+        const double kmass = 0.2 * mass / (P.dt * P.dt);
+        const double k = (kmass < P.c_k) ? kmass : P.c_k;
+        const double v_reln = vp[2] * -1.0;
+        const double omega = sqrt(k / mass);
+        const double ccrit = 2.0 * mass * omega;
+        const double F_damp = 0.2 * ccrit * v_reln;
+        const double F_normal = k * gap;
+        const double cfz = -(F_normal + F_damp) * -1.0;
+        cf[2] = cfz;
+        r = fabs(cfz);
+        double ut0 = S.ut[n] + vp[0] * P.dt;
+        double ut1 = S.ut[np + n] + vp[1] * P.dt;
+        double ftx = -k * ut0, fty = -k * ut1;
+        const double ft_mag = sqrt(ftx * ftx + fty * fty);
+        const double ft_max = P.c_mu * fabs(cfz);
+        if (!(ft_mag <= ft_max)) {
+          const double vt = sqrt(vp[0] * vp[0] + vp[1] * vp[1]);
+          if (vt > 0.0) {
+            ftx = -ft_max * vp[0] / vt;
+            fty = -ft_max * vp[1] / vt;
+          } else {
+            ftx = fty = 0.0;
+          }
+          ut0 = ut1 = 0.0;
+        }
+        S.ut[n] = ut0;
+        S.ut[np + n] = ut1;
+        cf[0] += ftx;
+        cf[1] += fty;
+      }
+      S.cf[n] = cf[0];
+      S.cf[np + n] = cf[1];
+      S.cf[2 * np + n] = cf[2];
+    }
+    if (!P.contact && (fl & NF_REACTION)) r = fi[P.react_dim];
+    const uint32_t code = P.bc[n];
+    const double *bv = &P.bcval[3 * (code >> 3)];
+    const double dt = P.dt;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      double a = (0.0 - fi[k]) / mass;
+      if (P.contact) a += cf[k] / mass;
+      if (code & (1u << k)) a = 0.0;
+      a = P.fcorr * (a - P.alpha * pa[k]);
+      double v = vp[k] + P.gamma * dt * a;
+      if (code & (1u << k)) v = bv[k];
+      double udt = dt * (vold[k] + (0.5 - P.beta) * dt * pa[k]);
+      udt += P.beta * dt * dt * a;
+      x[k] += udt;
+      u[k] += udt;
+      double vnext = v + (1.0 - P.gamma) * dt * a;
+      if (code & (1u << k)) vnext = bv[k];
+      S.x[k * np + n] = x[k];
+      S.u[k * np + n] = u[k];
+      S.v[k * np + n] = v;
+      S.pa[k * np + n] = a;
+      S.vp[k * np + n] = vnext;
+    }
+  }
+  // reaction: block partial, then the last block to finish sums all partials
+  // (each thread a fixed strided subset, then a fixed tree): deterministic.
+  const double bs = block_sum(r, sh);
+  if (threadIdx.x == 0) {
+    P.partials[blockIdx.x] = bs;
+    __threadfence();
+    const unsigned prev = atomicAdd(&P.st->done_blocks, 1u);
+    am_last = (prev == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (am_last) {
+    __threadfence();
+    double t = 0.0;
+    for (unsigned i = threadIdx.x; i < gridDim.x; i += blockDim.x)
+      t += ((volatile double *)P.partials)[i];
+    const double tot = block_sum(t, sh);
+    if (threadIdx.x == 0) {
+      const long long s = P.st->step;
+      if (s < P.hist_cap) P.hist[s] = tot;
+      P.st->step = s + 1;
+      P.st->time = time + P.dt;
+      P.st->done_blocks = 0u;
+    }
+  }
+}
+
+// predictor for the first step of a run: vp = v + (1 - gamma) dt prev_a, BCs
+__global__ void k_predict(StepParams P, Fp64State S) {
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= P.nn) return;
+  const uint32_t code = P.bc[n];
+  const double *bv = &P.bcval[3 * (code >> 3)];
+  for (int k = 0; k < 3; k++) {
+    double v = S.v[k * P.np + n] + (1.0 - P.gamma) * P.dt * S.pa[k * P.np + n];
+    if (code & (1u << k)) v = bv[k];
+    S.vp[k * P.np + n] = v;
+  }
+}
+
+// calcElemDensity (Mechanical.C:295-319): rho = rho_0 * vol_0 / vol
+__global__ void k_density(StepParams P, Fp64State S, const double *rho0) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= P.ne) return;
+  S.rho[e] = rho0[e] * S.vol0[e] / S.vol[e];
+}
+
+inline unsigned grid_for(int64_t n, int threads) {
+  return (unsigned)((n + threads - 1) / threads);
+}
+
+}  // namespace
+
+int fp64_node_grid(int64_t nn) { return (int)grid_for(nn, kNodeThreads); }
+
+void fp64_geometry(const StepParams &P, const Fp64State &S, cudaStream_t st, bool store_detj) {
+  if (P.npe == 8)
+    k_geometry<8><<<grid_for(P.ne, kElemThreads), kElemThreads, 0, st>>>(P, S, store_detj);
+  else
+    k_geometry<4><<<grid_for(P.ne, kElemThreads), kElemThreads, 0, st>>>(P, S, store_detj);
+}
+
+void fp64_nodal(const StepParams &P, const Fp64State &S, cudaStream_t st, int init_mode) {
+  if (P.npe == 8)
+    k_nodal<8><<<grid_for(P.nn, kNodeThreads), kNodeThreads, 0, st>>>(P, S, init_mode);
+  else
+    k_nodal<4><<<grid_for(P.nn, kNodeThreads), kNodeThreads, 0, st>>>(P, S, init_mode);
+}
+
+void fp64_elements(const StepParams &P, const Fp64State &S, cudaStream_t st) {
+  if (P.npe == 8)
+    k_elements<8><<<grid_for(P.ne, kElemThreads), kElemThreads, 0, st>>>(P, S);
+  else
+    k_elements<4><<<grid_for(P.ne, kElemThreads), kElemThreads, 0, st>>>(P, S);
+}
+
+void fp64_nodes(const StepParams &P, const Fp64State &S, cudaStream_t st, int node_grid) {
+  if (P.npe == 8)
+    k_nodes<8><<<node_grid, kNodeThreads, 0, st>>>(P, S);
+  else
+    k_nodes<4><<<node_grid, kNodeThreads, 0, st>>>(P, S);
+}
+
+void fp64_predict(const StepParams &P, const Fp64State &S, cudaStream_t st) {
+  k_predict<<<grid_for(P.nn, kNodeThreads), kNodeThreads, 0, st>>>(P, S);
+}
+
+void fp64_density(const StepParams &P, const Fp64State &S, const double *rho0, cudaStream_t st) {
+  k_density<<<grid_for(P.ne, kElemThreads), kElemThreads, 0, st>>>(P, S, rho0);
+}
+
+}  // namespace wf

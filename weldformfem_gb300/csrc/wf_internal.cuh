@@ -1,0 +1,136 @@
+// Internal declarations of the GB300 explicit-step library (not installed).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "wf.h"
+
+namespace wf {
+
+// Per-material constants on the device (Elastic_ / Material_, Material.cuh).
+struct MatDev {
+  double K, G, sy0, H, cs0, hol_K, hol_m, eps0, eps1, E;
+  int32_t model;
+  int32_t pad;
+};
+
+// FP32 material constants of the mixed kernels.
+struct MatF {
+  float K, G, sy0, H, cs0, rho, hol_K, hol_m, eps0, eps1;
+  int32_t model;
+  int32_t pad;
+};
+
+// Device-resident scalars advanced by the node kernel of every step.
+struct StepState {
+  double time;        // Time of the reference loop (start of the current step)
+  long long step;     // steps completed since wf_init
+  unsigned int done_blocks;  // last-block-done counter of the node kernel
+  unsigned int status;       // bit 0: a non-finite internal force was cleared
+  long long first_bad_node;
+};
+
+// Node flags (uint8 per node).
+enum : uint8_t { NF_REACTION = 1, NF_CONTACT = 2 };
+
+// Kernel parameters shared by both precisions. Node arrays are SoA with
+// component stride np (padded node count); element arrays are SoA with
+// component stride ne unless noted.
+struct StepParams {
+  int64_t nn, ne, np;
+  int32_t npe;
+  int32_t mass_mode;
+  int32_t press_alg;
+  int32_t react_dim;
+  int32_t contact;
+  int32_t stab_on;
+  int32_t av_on;
+  int32_t hg_on;
+  double hg_coef;
+  double stab[10];
+  double av[2];
+  // Chung-Hulbert constants (Solver_explicit.C:193-197), host-computed
+  double alpha, beta, gamma, fcorr;  // fcorr = 1 / (1 - alpha)
+  double dt;
+  // contact plane
+  double c_z0, c_vz, c_k, c_mu;
+  // mesh
+  const int32_t *elnod;   // [npe][ne]
+  const int32_t *off;     // [nn + 1]
+  const int32_t *slot;    // [total]: e * npe + local node
+  const uint32_t *bc;     // [nn]: bits 0..2 constrained dofs, bits 3.. value set
+  const double *bcval;    // [nsets][3]
+  const uint8_t *nflag;   // [nn]
+  const MatDev *mats;
+  const int32_t *emat;    // [ne] or null
+  double k0;              // bulk modulus of material 0 (pressure algorithm 1)
+  // FP32 constants of the mixed kernels (host-rounded once)
+  float f_dt, f_alpha, f_fcorr;
+  float f_cu_pred;        // (0.5 - beta) * dt
+  float f_cu_corr;        // beta * dt * dt
+  float f_cv_corr;        // gamma * dt
+  float f_cv_pred;        // (1 - gamma) * dt
+  float f_hg_coef, f_c_k, f_c_mu;
+  const struct MatF *matf;
+  // reduction scratch
+  double *partials;       // [grid of the node kernel]
+  double *hist;           // [hist_cap]
+  int64_t hist_cap;
+  StepState *st;
+};
+
+// FP64 state (all doubles).
+struct Fp64State {
+  double *x, *v, *vp, *pa, *u, *fi, *cf, *ut;   // [3][np]
+  double *mass, *voln, *jr, *s0;                 // [np]
+  double *vol, *vol0, *rho, *p, *pls, *sy, *detJ;  // [ne]
+  double *tau, *sig, *eps, *sr, *rr;             // [6][ne]
+  double *fe, *fhg;                              // [ne][npe][3]
+};
+
+// Mixed state. Positions are compensated float pairs (hi + lo, ~48-bit
+// significand) so neither the element nor the node kernels issue FP64
+// instructions; displacements are x - x0, formed in FP64 on export.
+// Everything else is FP32.
+struct MixState {
+  float2 *xh;                     // [3][np] (hi, lo)
+  float *v, *vp, *pa;             // [3][np]
+  float *cf, *ut;                 // [3][np], [2][np] contact force / slip
+  float *mass, *jr;               // [np]
+  float2 *nc;                     // [np] (1 / sum of initial volumes, mean density)
+  float *pls;                     // [ne]
+  float *tau;                     // [6][ne]
+  float *fe;                      // [ne][npe][3] element force minus hourglass force
+  double *x0;                     // [3][np] initial positions (export only)
+};
+
+// ---- FP64 launchers (wf_fp64.cu) ------------------------------------------
+void fp64_geometry(const StepParams &P, const Fp64State &S, cudaStream_t st, bool store_detj);
+void fp64_nodal(const StepParams &P, const Fp64State &S, cudaStream_t st, int init_mode);
+void fp64_elements(const StepParams &P, const Fp64State &S, cudaStream_t st);
+void fp64_nodes(const StepParams &P, const Fp64State &S, cudaStream_t st, int node_grid);
+void fp64_predict(const StepParams &P, const Fp64State &S, cudaStream_t st);
+void fp64_density(const StepParams &P, const Fp64State &S, const double *rho0, cudaStream_t st);
+int fp64_node_grid(int64_t nn);
+
+// ---- Mixed launchers (wf_mixed.cu) ----------------------------------------
+void mix_init(const StepParams &P, const MixState &M, const Fp64State &S, cudaStream_t st);
+void mix_geometry(const StepParams &P, const MixState &M, float *vol, cudaStream_t st);
+void mix_nodal(const StepParams &P, const MixState &M, const float *vol, cudaStream_t st);
+void mix_elements(const StepParams &P, const MixState &M, const float *vol, cudaStream_t st);
+void mix_nodes(const StepParams &P, const MixState &M, cudaStream_t st, int node_grid);
+void mix_predict(const StepParams &P, const MixState &M, cudaStream_t st);
+void mix_export(const StepParams &P, const MixState &M, const Fp64State &S, const float *vol,
+                cudaStream_t st);
+int mix_node_grid(int64_t nn);
+
+// ---- reductions (wf_reduce.cu) ---------------------------------------------
+// Minimum element edge length over the mesh (exact: min is order-free).
+void min_edge_length(const int32_t *elnod, const double *x, int64_t np, int64_t ne, int npe,
+                     double *out_dev, cudaStream_t st);
+
+}  // namespace wf

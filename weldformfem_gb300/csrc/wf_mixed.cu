@@ -1,0 +1,600 @@
+// Mixed-precision step kernels: FP32 element and node arithmetic, positions
+// as compensated float pairs, reaction sums in FP64.
+//
+// Same four phases and the same formulas as the FP64 kernels (wf_fp64.cu),
+// including the reference's Jaumann-term tensor product, with these changes:
+//  * element geometry uses coordinates relative to the element's first node,
+//    formed from (hi, lo) float pairs, so no FP64 instruction is issued;
+//  * the element force written for assembly is f_elem - f_hourglass;
+//  * the lumped mass is voln * (mean density of the node's elements), the
+//    same quantity as the reference's sum of rho_e * voln / count;
+//  * with default options the pressure is -K (J_avg - 1) (pressure
+//    algorithm 0 with zero stabilisation, as the reference defaults);
+//  * displacements are x - x0 (exported in FP64), total strain is not kept.
+#include "wf_internal.cuh"
+
+namespace wf {
+namespace {
+
+constexpr int kElemThreads = 128;
+constexpr int kNodeThreads = 256;
+
+__constant__ float c_sig[4][8] = {{1.f, 1.f, -1.f, -1.f, -1.f, -1.f, 1.f, 1.f},
+                                  {1.f, -1.f, -1.f, 1.f, -1.f, 1.f, 1.f, -1.f},
+                                  {1.f, -1.f, 1.f, -1.f, 1.f, -1.f, 1.f, -1.f},
+                                  {-1.f, 1.f, -1.f, 1.f, 1.f, -1.f, 1.f, -1.f}};
+
+// (hi, lo) pair helpers ------------------------------------------------------
+__device__ __forceinline__ float2 split_d(double v) {
+  const float hi = (float)v;
+  return make_float2(hi, (float)(v - (double)hi));
+}
+// (hi, lo) + b with TwoSum and renormalisation (Knuth / Dekker).
+__device__ __forceinline__ float2 pair_add(float2 a, float b) {
+  const float s = __fadd_rn(a.x, b);
+  const float bb = __fsub_rn(s, a.x);
+  const float err = __fadd_rn(__fsub_rn(a.x, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  const float t = __fadd_rn(err, a.y);
+  const float hi = __fadd_rn(s, t);
+  const float lo = __fsub_rn(t, __fsub_rn(hi, s));
+  return make_float2(hi, lo);
+}
+// a - b for nearby points: hi parts subtract exactly when within a factor 2.
+__device__ __forceinline__ float pair_rel(float2 a, float2 b) {
+  return __fadd_rn(__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y));
+}
+
+template <int NPE>
+__device__ __forceinline__ float weightf() {
+  return NPE == 8 ? 8.0f : 1.0f / 6.0f;
+}
+
+template <int NPE>
+__device__ __forceinline__ void rel_coords(const StepParams &P, const MixState &M, int64_t e,
+                                           float (&r)[NPE][3], int32_t (&nid)[NPE]) {
+#pragma unroll
+  for (int a = 0; a < NPE; a++) nid[a] = __ldg(&P.elnod[a * P.ne + e]);
+  float2 o[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) o[k] = __ldg(&M.xh[k * P.np + nid[0]]);
+#pragma unroll
+  for (int k = 0; k < 3; k++) r[0][k] = 0.0f;
+#pragma unroll
+  for (int a = 1; a < NPE; a++)
+#pragma unroll
+    for (int k = 0; k < 3; k++) r[a][k] = pair_rel(__ldg(&M.xh[k * P.np + nid[a]]), o[k]);
+}
+
+template <int NPE>
+__device__ __forceinline__ void jacobian_f(const float (&x2)[NPE][3], float J[3][3]) {
+  if constexpr (NPE == 8) {
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      J[0][k] = 0.125f * (-x2[0][k] + x2[1][k] + x2[2][k] - x2[3][k] - x2[4][k] + x2[5][k] +
+                          x2[6][k] - x2[7][k]);
+      J[1][k] = 0.125f * (-x2[0][k] - x2[1][k] + x2[2][k] + x2[3][k] - x2[4][k] - x2[5][k] +
+                          x2[6][k] + x2[7][k]);
+      J[2][k] = 0.125f * (-x2[0][k] - x2[1][k] - x2[2][k] - x2[3][k] + x2[4][k] + x2[5][k] +
+                          x2[6][k] + x2[7][k]);
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      J[0][k] = x2[1][k] - x2[0][k];
+      J[1][k] = x2[2][k] - x2[0][k];
+      J[2][k] = x2[3][k] - x2[0][k];
+    }
+  }
+}
+
+__device__ __forceinline__ float det3f(const float J[3][3]) {
+  return J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) -
+         J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+         J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+}
+
+template <int NPE>
+__device__ __forceinline__ void shape_derivs_f(const float J[3][3], float dH[3][NPE]) {
+  float inv[3][3];
+  inv[0][0] = (J[1][1] * J[2][2] - J[1][2] * J[2][1]);
+  inv[1][0] = -(J[1][0] * J[2][2] - J[1][2] * J[2][0]);
+  inv[2][0] = (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+  inv[0][1] = -(J[0][1] * J[2][2] - J[0][2] * J[2][1]);
+  inv[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]);
+  inv[2][1] = -(J[0][0] * J[2][1] - J[0][1] * J[2][0]);
+  inv[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]);
+  inv[1][2] = -(J[0][0] * J[1][2] - J[0][2] * J[1][0]);
+  inv[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]);
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const float a0 = inv[k][0], a1 = inv[k][1], a2 = inv[k][2];
+    if constexpr (NPE == 8) {
+      dH[k][0] = 0.125f * (-a0 - a1 - a2);
+      dH[k][1] = 0.125f * (a0 - a1 - a2);
+      dH[k][2] = 0.125f * (a0 + a1 - a2);
+      dH[k][3] = 0.125f * (-a0 + a1 - a2);
+      dH[k][4] = 0.125f * (-a0 - a1 + a2);
+      dH[k][5] = 0.125f * (a0 - a1 + a2);
+      dH[k][6] = 0.125f * (a0 + a1 + a2);
+      dH[k][7] = 0.125f * (-a0 + a1 + a2);
+    } else {
+      dH[k][0] = -a0 - a1 - a2;
+      dH[k][1] = a0;
+      dH[k][2] = a1;
+      dH[k][3] = a2;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+template <int NPE>
+__global__ void __launch_bounds__(kElemThreads) k_geometry(StepParams P, MixState M,
+                                                           float *vol) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= P.ne) return;
+  float r[NPE][3];
+  int32_t nid[NPE];
+  rel_coords<NPE>(P, M, e, r, nid);
+  float J[3][3];
+  jacobian_f<NPE>(r, J);
+  vol[e] = det3f(J) * weightf<NPE>();
+}
+
+template <int NPE>
+__global__ void __launch_bounds__(kNodeThreads) k_nodal(StepParams P, MixState M,
+                                                        const float *vol) {
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= P.nn) return;
+  const int32_t b = __ldg(&P.off[n]), c = __ldg(&P.off[n + 1]) - b;
+  float s = 0.0f;
+  for (int32_t k = 0; k < c; k++) s += __ldg(&vol[__ldg(&P.slot[b + k]) / NPE]);
+  const float2 nc = __ldg(&M.nc[n]);
+  M.jr[n] = s * nc.x;
+  if (P.mass_mode == 0) M.mass[n] = (s * (1.0f / NPE)) * nc.y;
+}
+
+__device__ __forceinline__ float idf(int i) { return (i == 0 || i == 4 || i == 8) ? 1.f : 0.f; }
+
+// operator*(tensor3, tensor3) of include/common/Tensor3.C:290-303, FP32
+__device__ __forceinline__ void t3_mul_f(const float *a, const float *b, float *r) {
+  enum { XX, XY, XZ, YX, YY, YZ, ZX, ZY, ZZ };
+  r[XX] = a[XX] * b[XX] + a[XY] * b[YX] + a[XZ] * b[ZX];
+  r[XY] = a[XX] * b[YX] + a[XY] * b[YY] + a[XZ] * b[YZ];
+  r[XZ] = a[XX] * b[ZX] + a[XY] * b[ZY] + a[XZ] * b[ZZ];
+  r[YX] = a[YX] * b[XX] + a[YY] * b[YX] + a[YZ] * b[ZX];
+  r[YY] = a[YX] * b[YX] + a[YY] * b[YY] + a[YZ] * b[YZ];
+  r[YZ] = a[YX] * b[ZX] + a[YY] * b[ZY] + a[YZ] * b[ZZ];
+  r[ZX] = a[ZX] * b[XX] + a[ZY] * b[YX] + a[ZZ] * b[ZX];
+  r[ZY] = a[ZX] * b[YX] + a[ZY] * b[YY] + a[ZZ] * b[YZ];
+  r[ZZ] = a[ZX] * b[ZX] + a[ZY] * b[ZY] + a[ZZ] * b[ZZ];
+}
+
+template <int NPE>
+__global__ void __launch_bounds__(kElemThreads) k_elements(StepParams P, MixState M) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= P.ne) return;
+  const int64_t ne = P.ne;
+  int32_t nid[NPE];
+  float dH[3][NPE];
+  float detJ;
+  {
+    float r[NPE][3];
+    rel_coords<NPE>(P, M, e, r, nid);
+    float J[3][3];
+    jacobian_f<NPE>(r, J);
+    shape_derivs_f<NPE>(J, dH);
+    detJ = det3f(J);
+  }
+  const float vol = detJ * weightf<NPE>();
+  const MatF m = P.matf[P.emat ? __ldg(&P.emat[e]) : 0];
+
+  float s00 = 0.f, s11 = 0.f, s22 = 0.f, s01 = 0.f, s12 = 0.f, s02 = 0.f;
+  float w01 = 0.f, w12 = 0.f, w02 = 0.f;
+  float hm[3][4];
+#pragma unroll
+  for (int k = 0; k < 3; k++)
+#pragma unroll
+    for (int j = 0; j < 4; j++) hm[k][j] = 0.f;
+  float J_avg = 0.f;
+#pragma unroll
+  for (int a = 0; a < NPE; a++) {
+    const float v0 = __ldg(&M.vp[nid[a]]);
+    const float v1 = __ldg(&M.vp[P.np + nid[a]]);
+    const float v2 = __ldg(&M.vp[2 * P.np + nid[a]]);
+    const float d0 = dH[0][a], d1 = dH[1][a], d2 = dH[2][a];
+    s00 += d0 * v0;
+    s11 += d1 * v1;
+    s22 += d2 * v2;
+    s01 += d1 * v0 + d0 * v1;
+    w01 += d1 * v0 - d0 * v1;
+    s12 += d2 * v1 + d1 * v2;
+    s02 += d2 * v0 + d0 * v2;
+    w12 += d2 * v1 - d1 * v2;
+    w02 += d2 * v0 - d0 * v2;
+    J_avg += __ldg(&M.jr[nid[a]]);
+    if constexpr (NPE == 8) {
+      if (P.hg_on) {
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+          hm[0][j] += v0 * c_sig[j][a];
+          hm[1][j] += v1 * c_sig[j][a];
+          hm[2][j] += v2 * c_sig[j][a];
+        }
+      }
+    }
+  }
+  const float f = 1.0f / detJ;
+  const float fh = 0.5f * f;
+  s00 *= f; s11 *= f; s22 *= f;
+  s01 *= fh; s12 *= fh; s02 *= fh;
+  w01 *= fh; w12 *= fh; w02 *= fh;
+  J_avg *= (1.0f / NPE);
+  float J_bar = J_avg;
+  if (J_bar < 0.0f) J_bar = 0.2f;
+  const float p = -m.K * (J_bar - 1.0f);
+
+  // Jaumann rate + radial return
+  const float dt = P.f_dt;
+  float SS[9], SR[9], RR[9], RT[9], SRT[9], RS[9];
+  {
+    const float t0 = M.tau[e], t1 = M.tau[ne + e], t2 = M.tau[2 * ne + e];
+    const float t3 = M.tau[3 * ne + e], t4 = M.tau[4 * ne + e], t5 = M.tau[5 * ne + e];
+    SS[0] = t0; SS[4] = t1; SS[8] = t2;
+    SS[1] = SS[3] = t3; SS[5] = SS[7] = t4; SS[2] = SS[6] = t5;
+  }
+  SR[0] = s00; SR[4] = s11; SR[8] = s22;
+  SR[1] = SR[3] = s01; SR[5] = SR[7] = s12; SR[2] = SR[6] = s02;
+  RR[0] = 0.f; RR[4] = 0.f; RR[8] = 0.f;
+  RR[1] = w01; RR[5] = w12; RR[2] = w02;
+  RR[3] = -w01; RR[7] = -w12; RR[6] = -w02;
+  RT[0] = 0.f; RT[4] = 0.f; RT[8] = 0.f;
+  RT[1] = RR[3]; RT[2] = RR[6]; RT[3] = RR[1];
+  RT[5] = RR[7]; RT[6] = RR[2]; RT[7] = RR[5];
+  t3_mul_f(SS, RT, SRT);
+  t3_mul_f(RR, SS, RS);
+  {
+    const float c = (1.0f / 3.0f) * (SR[0] + SR[4] + SR[8]);
+    const float g2 = 2.0f * m.G;
+#pragma unroll
+    for (int i = 0; i < 9; i++) SS[i] = SS[i] + ((SR[i] - idf(i) * c) * g2 + SRT[i] + RS[i]) * dt;
+  }
+  // deviatoric trial stress: s = tau - tr(tau)/3 I (the pressure part cancels)
+  float Sd[9];
+  {
+    const float c2 = (1.0f / 3.0f) * ((SS[0] - p) + (SS[4] - p) + (SS[8] - p));
+#pragma unroll
+    for (int i = 0; i < 9; i++) Sd[i] = (SS[i] - idf(i) * p) - idf(i) * c2;
+  }
+  const float J2 = 0.5f * (Sd[0] * Sd[0] + 2.0f * Sd[1] * Sd[1] + 2.0f * Sd[2] * Sd[2] +
+                           Sd[4] * Sd[4] + 2.0f * Sd[5] * Sd[5] + Sd[8] * Sd[8]);
+  const float sig_trial = sqrtf(3.0f * J2);
+  float pls = M.pls[e];
+  float sy;
+  if (m.model == WF_MAT_HOLLOMON)
+    sy = (pls + m.eps0 > m.eps1) ? m.hol_K * powf(pls + m.eps0, m.hol_m) : m.sy0;
+  else
+    sy = m.sy0 + m.H * pls;
+  if (sy < sig_trial) {
+    const float H = (m.model == WF_MAT_HOLLOMON)
+                        ? ((pls + m.eps0 > m.eps1)
+                               ? m.hol_K * m.hol_m * powf(pls + m.eps0, m.hol_m - 1.0f)
+                               : 0.f)
+                        : m.H;
+    const float dgamma = (sig_trial - sy) / (3.0f * m.G + H);
+    const float factor = 1.0f - (3.0f * m.G * dgamma) / sig_trial;
+#pragma unroll
+    for (int i = 0; i < 9; i++) SS[i] = Sd[i] * factor;
+    pls += dgamma;
+  }
+  M.pls[e] = pls;
+  M.tau[e] = SS[0]; M.tau[ne + e] = SS[4]; M.tau[2 * ne + e] = SS[8];
+  M.tau[3 * ne + e] = SS[1]; M.tau[4 * ne + e] = SS[5]; M.tau[5 * ne + e] = SS[2];
+  const float sg0 = SS[0] - p, sg1 = SS[4] - p, sg2 = SS[8] - p;
+  const float sg3 = SS[1], sg4 = SS[5], sg5 = SS[2];
+
+  // element force minus hourglass force
+  const float w = weightf<NPE>();
+  float ch = 0.f;
+  if constexpr (NPE == 8) {
+    if (P.hg_on) ch = P.f_hg_coef * powf(vol, 0.6666666f) * m.rho * 0.25f * m.cs0;
+  }
+  float out[NPE * 3];
+#pragma unroll
+  for (int a = 0; a < NPE; a++) {
+    const float d0 = dH[0][a], d1 = dH[1][a], d2 = dH[2][a];
+    float f0 = (d0 * sg0 + d1 * sg3 + d2 * sg5) * w;
+    float f1 = (d1 * sg1 + d0 * sg3 + d2 * sg4) * w;
+    float f2 = (d2 * sg2 + d1 * sg4 + d0 * sg5) * w;
+    if constexpr (NPE == 8) {
+      if (P.hg_on) {
+        float g0 = 0.f, g1 = 0.f, g2 = 0.f;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+          g0 += hm[0][j] * c_sig[j][a];
+          g1 += hm[1][j] * c_sig[j][a];
+          g2 += hm[2][j] * c_sig[j][a];
+        }
+        // f_hg = -ch * sum_j h_j Gamma_j; assembly subtracts it
+        f0 += ch * g0;
+        f1 += ch * g1;
+        f2 += ch * g2;
+      }
+    }
+    out[3 * a] = f0;
+    out[3 * a + 1] = f1;
+    out[3 * a + 2] = f2;
+  }
+  float4 *dst = reinterpret_cast<float4 *>(&M.fe[e * NPE * 3]);
+#pragma unroll
+  for (int q = 0; q < NPE * 3 / 4; q++)
+    dst[q] = make_float4(out[4 * q], out[4 * q + 1], out[4 * q + 2], out[4 * q + 3]);
+}
+
+// ---------------------------------------------------------------------------
+// Block sum in a fixed order (shuffle tree per warp, warps in index order);
+// warps with no nonzero value skip their FP64 shuffles. Valid in thread 0.
+__device__ __forceinline__ double block_sum_sparse(double v, bool nz, double *sh) {
+  const unsigned any = __ballot_sync(0xffffffffu, nz);
+  if (any) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  }
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = any ? v : 0.0;
+  __syncthreads();
+  double t = 0.0;
+  if (threadIdx.x == 0)
+    for (int i = 0; i < (int)(blockDim.x >> 5); i++) t += sh[i];
+  return t;
+}
+
+template <int NPE>
+__global__ void __launch_bounds__(kNodeThreads) k_nodes(StepParams P, MixState M) {
+  __shared__ double sh[kNodeThreads / 32];
+  __shared__ bool am_last;
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  float r = 0.0f;
+  if (n < P.nn) {
+    const int64_t np = P.np;
+    const int32_t b = __ldg(&P.off[n]), c = __ldg(&P.off[n + 1]) - b;
+    float fi0 = 0.f, fi1 = 0.f, fi2 = 0.f;
+    for (int32_t k = 0; k < c; k++) {
+      const float *src = &M.fe[(int64_t)__ldg(&P.slot[b + k]) * 3];
+      fi0 += __ldg(src);
+      fi1 += __ldg(src + 1);
+      fi2 += __ldg(src + 2);
+    }
+    float fi[3] = {fi0, fi1, fi2};
+#pragma unroll
+    for (int k = 0; k < 3; k++)
+      if (!isfinite(fi[k])) {
+        fi[k] = 0.f;
+        atomicOr(&P.st->status, 1u);
+      }
+    const uint8_t fl = P.nflag[n];
+    const float mass = M.mass[n];
+    const float inv_m = 1.0f / mass;
+    float2 x[3];
+    float vold[3], vp[3], pa[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      x[k] = M.xh[k * np + n];
+      vold[k] = M.v[k * np + n];
+      vp[k] = M.vp[k * np + n];
+      pa[k] = M.pa[k * np + n];
+    }
+    float cf[3] = {0.f, 0.f, 0.f};
+    if (P.contact && (fl & NF_CONTACT)) {
+      const double zd = P.c_z0 + P.c_vz * P.st->time;
+      const float gap = (float)(zd - ((double)x[2].x + (double)x[2].y));
+      if (gap < 0.f) {
+        const float kmass = 0.2f * mass / (P.f_dt * P.f_dt);
+        const float k = (kmass < P.f_c_k) ? kmass : P.f_c_k;
+        const float v_reln = -vp[2];
+        const float ccrit = 2.0f * mass * sqrtf(k * inv_m);
+        const float cfz = k * gap + 0.2f * ccrit * v_reln;
+        cf[2] = cfz;
+        r = fabsf(cfz);
+        float ut0 = M.ut[n] + vp[0] * P.f_dt;
+        float ut1 = M.ut[np + n] + vp[1] * P.f_dt;
+        float ftx = -k * ut0, fty = -k * ut1;
+        const float ft_max = P.f_c_mu * fabsf(cfz);
+        if (!(sqrtf(ftx * ftx + fty * fty) <= ft_max)) {
+          const float vt = sqrtf(vp[0] * vp[0] + vp[1] * vp[1]);
+          if (vt > 0.f) {
+            ftx = -ft_max * vp[0] / vt;
+            fty = -ft_max * vp[1] / vt;
+          } else {
+            ftx = fty = 0.f;
+          }
+          ut0 = ut1 = 0.f;
+        }
+        M.ut[n] = ut0;
+        M.ut[np + n] = ut1;
+        cf[0] = ftx;
+        cf[1] = fty;
+      }
+      M.cf[n] = cf[0];
+      M.cf[np + n] = cf[1];
+      M.cf[2 * np + n] = cf[2];
+    }
+    if (!P.contact && (fl & NF_REACTION)) r = fi[P.react_dim];
+    const uint32_t code = P.bc[n];
+    const double *bvd = &P.bcval[3 * (code >> 3)];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      const bool fixed = (code >> k) & 1u;
+      float a = (cf[k] - fi[k]) * inv_m;
+      if (fixed) a = 0.f;
+      a = P.f_fcorr * (a - P.f_alpha * pa[k]);
+      float v = vp[k] + P.f_cv_corr * a;
+      const float bv = fixed ? (float)__ldg(&bvd[k]) : 0.f;
+      if (fixed) v = bv;
+      const float udt = P.f_dt * (vold[k] + P.f_cu_pred * pa[k]) + P.f_cu_corr * a;
+      x[k] = pair_add(x[k], udt);
+      float vnext = v + P.f_cv_pred * a;
+      if (fixed) vnext = bv;
+      M.xh[k * np + n] = x[k];
+      M.v[k * np + n] = v;
+      M.pa[k * np + n] = a;
+      M.vp[k * np + n] = vnext;
+    }
+  }
+  // reaction: only warps holding a contribution reduce (FP64, fixed order);
+  // the last block to finish sums all block partials with the whole block.
+  const double bs = block_sum_sparse((double)r, r != 0.0f, sh);
+  if (threadIdx.x == 0) {
+    P.partials[blockIdx.x] = bs;
+    __threadfence();
+    const unsigned prev = atomicAdd(&P.st->done_blocks, 1u);
+    am_last = (prev == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (am_last) {
+    __threadfence();
+    double t = 0.0;
+    for (unsigned i = threadIdx.x; i < gridDim.x; i += blockDim.x)
+      t += ((volatile double *)P.partials)[i];
+    const double tot = block_sum_sparse(t, t != 0.0, sh);
+    if (threadIdx.x == 0) {
+      const long long s = P.st->step;
+      if (s < P.hist_cap) P.hist[s] = tot;
+      P.st->step = s + 1;
+      P.st->time = P.st->time + P.dt;
+      P.st->done_blocks = 0u;
+    }
+  }
+}
+
+__global__ void k_predict(StepParams P, MixState M) {
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= P.nn) return;
+  const uint32_t code = P.bc[n];
+  for (int k = 0; k < 3; k++) {
+    float v = M.v[k * P.np + n] + P.f_cv_pred * M.pa[k * P.np + n];
+    if ((code >> k) & 1u) v = (float)P.bcval[3 * (code >> 3) + k];
+    M.vp[k * P.np + n] = v;
+  }
+}
+
+// Copies the FP64 initial state (after the preamble) into the mixed arrays.
+template <int NPE>
+__global__ void k_init_nodes(StepParams P, MixState M, Fp64State S) {
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= P.nn) return;
+  const int64_t np = P.np;
+  for (int k = 0; k < 3; k++) {
+    const double x = S.x[k * np + n];
+    M.xh[k * np + n] = split_d(x);
+    M.x0[k * np + n] = x;
+    M.v[k * np + n] = (float)S.v[k * np + n];
+    M.pa[k * np + n] = 0.f;
+  }
+  M.mass[n] = (float)S.mass[n];
+  const int32_t b = P.off[n], c = P.off[n + 1] - b;
+  double rs = 0.0;
+  for (int32_t k = 0; k < c; k++) rs += S.rho[P.slot[b + k] / NPE];
+  M.nc[n] = make_float2((float)(1.0 / S.s0[n]), (float)(rs / c));
+}
+
+// Writes the mixed state into the FP64 arrays read back by the host.
+template <int NPE>
+__global__ void k_export_nodes(StepParams P, MixState M, Fp64State S) {
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= P.nn) return;
+  const int64_t np = P.np;
+  for (int k = 0; k < 3; k++) {
+    const float2 h = M.xh[k * np + n];
+    const double x = (double)h.x + (double)h.y;
+    S.x[k * np + n] = x;
+    S.u[k * np + n] = x - M.x0[k * np + n];
+    S.v[k * np + n] = M.v[k * np + n];
+    S.pa[k * np + n] = M.pa[k * np + n];
+    S.cf[k * np + n] = M.cf[k * np + n];
+  }
+  S.mass[n] = M.mass[n];
+  S.jr[n] = M.jr[n];
+}
+
+template <int NPE>
+__global__ void k_export_elems(StepParams P, MixState M, Fp64State S, const float *vol) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= P.ne) return;
+  const int64_t ne = P.ne;
+  const MatF m = P.matf[P.emat ? P.emat[e] : 0];
+  float J_avg = 0.f;
+  for (int a = 0; a < NPE; a++) J_avg += M.jr[P.elnod[a * ne + e]];
+  J_avg *= (1.0f / NPE);
+  const float p = -m.K * ((J_avg < 0.f ? 0.2f : J_avg) - 1.0f);
+  S.p[e] = p;
+  S.vol[e] = vol[e];
+  const float pls = M.pls[e];
+  S.pls[e] = pls;
+  S.sy[e] = (m.model == WF_MAT_HOLLOMON)
+                ? ((pls + m.eps0 > m.eps1) ? m.hol_K * powf(pls + m.eps0, m.hol_m) : m.sy0)
+                : m.sy0 + m.H * pls;
+  for (int c = 0; c < 6; c++) {
+    const double t = M.tau[c * ne + e];
+    S.tau[c * ne + e] = t;
+    S.sig[c * ne + e] = (c < 3) ? t - (double)p : t;
+  }
+}
+
+inline unsigned grid_for(int64_t n, int threads) {
+  return (unsigned)((n + threads - 1) / threads);
+}
+
+}  // namespace
+
+int mix_node_grid(int64_t nn) { return (int)grid_for(nn, kNodeThreads); }
+
+void mix_init(const StepParams &P, const MixState &M, const Fp64State &S, cudaStream_t st) {
+  if (P.npe == 8)
+    k_init_nodes<8><<<grid_for(P.nn, kNodeThreads), kNodeThreads, 0, st>>>(P, M, S);
+  else
+    k_init_nodes<4><<<grid_for(P.nn, kNodeThreads), kNodeThreads, 0, st>>>(P, M, S);
+}
+
+void mix_geometry(const StepParams &P, const MixState &M, float *vol, cudaStream_t st) {
+  if (P.npe == 8)
+    k_geometry<8><<<grid_for(P.ne, kElemThreads), kElemThreads, 0, st>>>(P, M, vol);
+  else
+    k_geometry<4><<<grid_for(P.ne, kElemThreads), kElemThreads, 0, st>>>(P, M, vol);
+}
+
+void mix_nodal(const StepParams &P, const MixState &M, const float *vol, cudaStream_t st) {
+  if (P.npe == 8)
+    k_nodal<8><<<grid_for(P.nn, kNodeThreads), kNodeThreads, 0, st>>>(P, M, vol);
+  else
+    k_nodal<4><<<grid_for(P.nn, kNodeThreads), kNodeThreads, 0, st>>>(P, M, vol);
+}
+
+void mix_elements(const StepParams &P, const MixState &M, const float *, cudaStream_t st) {
+  if (P.npe == 8)
+    k_elements<8><<<grid_for(P.ne, kElemThreads), kElemThreads, 0, st>>>(P, M);
+  else
+    k_elements<4><<<grid_for(P.ne, kElemThreads), kElemThreads, 0, st>>>(P, M);
+}
+
+void mix_nodes(const StepParams &P, const MixState &M, cudaStream_t st, int node_grid) {
+  if (P.npe == 8)
+    k_nodes<8><<<node_grid, kNodeThreads, 0, st>>>(P, M);
+  else
+    k_nodes<4><<<node_grid, kNodeThreads, 0, st>>>(P, M);
+}
+
+void mix_predict(const StepParams &P, const MixState &M, cudaStream_t st) {
+  k_predict<<<grid_for(P.nn, kNodeThreads), kNodeThreads, 0, st>>>(P, M);
+}
+
+void mix_export(const StepParams &P, const MixState &M, const Fp64State &S, const float *vol,
+                cudaStream_t st) {
+  if (P.npe == 8) {
+    k_export_nodes<8><<<grid_for(P.nn, kNodeThreads), kNodeThreads, 0, st>>>(P, M, S);
+    k_export_elems<8><<<grid_for(P.ne, kElemThreads), kElemThreads, 0, st>>>(P, M, S, vol);
+  } else {
+    k_export_nodes<4><<<grid_for(P.nn, kNodeThreads), kNodeThreads, 0, st>>>(P, M, S);
+    k_export_elems<4><<<grid_for(P.ne, kElemThreads), kElemThreads, 0, st>>>(P, M, S, vol);
+  }
+}
+
+}  // namespace wf

@@ -209,13 +209,10 @@ class Case:
                     mu=float(c["mu"]))
 
 
-def apply(dom, case: Case, x=None, with_bcs=True):
-    """Sets up any domain backend (same method names) for `case` and returns dt."""
-    dom.add_box(case.L, case.r, case.tritetra)
+def apply_options(dom, case: Case, with_bcs=True, x=None):
+    """Everything after the mesh: materials, BCs, options, dt. Returns dt."""
     if x is None:
         x = case.coords()
-    if case.perturb:
-        dom.set_nodes(x)
     dom.set_materials(case.materials, case.elem_mat)
     if with_bcs:
         dom.add_bcs(case.bcs())
@@ -233,6 +230,16 @@ def apply(dom, case: Case, x=None, with_bcs=True):
     dt = case.time_step(x)
     dom.set_dt(dt)
     return dt
+
+
+def apply(dom, case: Case, x=None, with_bcs=True):
+    """Sets up any domain backend (same method names) for `case` and returns dt."""
+    dom.add_box(case.L, case.r, case.tritetra)
+    if x is None:
+        x = case.coords()
+    if case.perturb:
+        dom.set_nodes(x)
+    return apply_options(dom, case, with_bcs, x)
 
 
 def octant_ids(case: Case) -> np.ndarray:
