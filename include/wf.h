@@ -158,7 +158,9 @@ WF_API wf_status wf_set_contact_plane(wf_domain *d, double z0, double vz, double
 
 /* ---- run ---------------------------------------------------------------------- */
 /* Preamble of SolveChungHulbert (Solver_explicit.C:120-268): uploads the
- * mesh, imposes initial BCs, computes initial geometry, volumes and masses. */
+ * mesh, imposes initial BCs, computes initial geometry, volumes and masses.
+ * The time step may be set before or after (wf_min_edge_length works once
+ * the mesh is on the device); it must be set before wf_run. */
 WF_API wf_status wf_init(wf_domain *d);
 /* nsteps iterations of the loop body (Solver_explicit.C:346-1167). */
 WF_API wf_status wf_run(wf_domain *d, int64_t nsteps);

@@ -574,7 +574,6 @@ WF_API wf_status wf_init(wf_domain *d) {
   wf_status s = need_mesh(d);
   if (s) return s;
   if (d->mats.empty()) return fail(d, WF_ERR_STATE, "no material assigned (AssignMaterial)");
-  if (!(d->dt > 0.0)) return fail(d, WF_ERR_STATE, "time step not set (SetDT)");
   if (d->precision == WF_MIXED) {
     if (d->press_alg != 0 || d->av[0] != 0.0 || d->av[1] != 0.0)
       return fail(d, WF_ERR_UNSUPPORTED, "mixed precision supports pressure algorithm 0 without "
@@ -775,13 +774,8 @@ WF_API wf_status wf_init(wf_domain *d) {
     MatF *mfd = nullptr;
     CUDA_TRY(upload(d, &mfd, mf));
     P.matf = mfd;
-    P.f_dt = (float)P.dt;
     P.f_alpha = (float)P.alpha;
     P.f_fcorr = (float)P.fcorr;
-    P.f_cu_pred = (float)((0.5 - P.beta) * P.dt);
-    P.f_cu_corr = (float)(P.beta * P.dt * P.dt);
-    P.f_cv_corr = (float)(P.gamma * P.dt);
-    P.f_cv_pred = (float)((1.0 - P.gamma) * P.dt);
     P.f_hg_coef = (float)P.hg_coef;
     P.f_c_k = (float)P.c_k;
     P.f_c_mu = (float)P.c_mu;
@@ -853,6 +847,16 @@ wf_status collect_phase_events(wf_domain *d) {
   return WF_OK;
 }
 
+// Time-step dependent constants (FP64 and their FP32 roundings).
+void set_dt_constants(StepParams &P, double dt) {
+  P.dt = dt;
+  P.f_dt = (float)dt;
+  P.f_cu_pred = (float)((0.5 - P.beta) * dt);
+  P.f_cu_corr = (float)(P.beta * dt * dt);
+  P.f_cv_corr = (float)(P.gamma * dt);
+  P.f_cv_pred = (float)((1.0 - P.gamma) * dt);
+}
+
 constexpr int kGraphSteps = 32;
 
 wf_status ensure_graph(wf_domain *d) {
@@ -892,7 +896,8 @@ WF_API wf_status wf_run(wf_domain *d, int64_t nsteps) {
       d->graph = nullptr;
     }
   }
-  d->P.dt = d->dt;
+  if (!(d->dt > 0.0)) return fail(d, WF_ERR_STATE, "time step not set (SetDT)");
+  set_dt_constants(d->P, d->dt);
   if (d->precision == WF_FP64)
     fp64_predict(d->P, d->S, d->stream);
   else

@@ -114,7 +114,7 @@ __device__ __forceinline__ void gather_x(const StepParams &P, const double *x, i
 // ---------------------------------------------------------------------------
 // geometry: vol = 0.0 + detJ * w * 1.0 (Mechanical.C:264-293)
 template <int NPE>
-__global__ void __launch_bounds__(kElemThreads) k_geometry(StepParams P, Fp64State S,
+__global__ void __launch_bounds__(kElemThreads) k_fp64_geometry(StepParams P, Fp64State S,
                                                            int store_detj) {
   int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= P.ne) return;
@@ -135,7 +135,7 @@ __global__ void __launch_bounds__(kElemThreads) k_geometry(StepParams P, Fp64Sta
 // (:1576-1601) and the nodal volume ratio of calcElemPressure (:694-705).
 // init_mode 1 also forms the constant sum of initial volumes.
 template <int NPE>
-__global__ void __launch_bounds__(kNodeThreads) k_nodal(StepParams P, Fp64State S,
+__global__ void __launch_bounds__(kNodeThreads) k_fp64_nodal(StepParams P, Fp64State S,
                                                         int init_mode) {
   int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= P.nn) return;
@@ -200,7 +200,7 @@ __device__ __forceinline__ double hollomon_et(double strain, const MatDev &m) {
 // CalcStressStrain (:1664-1839), calcArtificialViscosity (:1948-1977),
 // calcElemForces (:375-481) and the 3-D viscous hourglass forces.
 template <int NPE>
-__global__ void __launch_bounds__(kElemThreads) k_elements(StepParams P, Fp64State S) {
+__global__ void __launch_bounds__(kElemThreads) k_fp64_elements(StepParams P, Fp64State S) {
   int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= P.ne) return;
   const int64_t ne = P.ne;
@@ -465,7 +465,7 @@ __device__ __forceinline__ double block_sum(double v, double *sh) {
 // UpdateCorrectionPos (:1005-1025) and the next step's UpdatePrediction
 // (:961-974) + ImposeBCV, which this kernel hands to the next step as vp.
 template <int NPE>
-__global__ void __launch_bounds__(kNodeThreads) k_nodes(StepParams P, Fp64State S) {
+__global__ void __launch_bounds__(kNodeThreads) k_fp64_nodes(StepParams P, Fp64State S) {
   __shared__ double sh[kNodeThreads / 32];
   __shared__ bool am_last;
   const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -601,7 +601,7 @@ __global__ void __launch_bounds__(kNodeThreads) k_nodes(StepParams P, Fp64State 
 }
 
 // predictor for the first step of a run: vp = v + (1 - gamma) dt prev_a, BCs
-__global__ void k_predict(StepParams P, Fp64State S) {
+__global__ void k_fp64_predict(StepParams P, Fp64State S) {
   const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= P.nn) return;
   const uint32_t code = P.bc[n];
@@ -614,7 +614,7 @@ __global__ void k_predict(StepParams P, Fp64State S) {
 }
 
 // calcElemDensity (Mechanical.C:295-319): rho = rho_0 * vol_0 / vol
-__global__ void k_density(StepParams P, Fp64State S, const double *rho0) {
+__global__ void k_fp64_density(StepParams P, Fp64State S, const double *rho0) {
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= P.ne) return;
   S.rho[e] = rho0[e] * S.vol0[e] / S.vol[e];
@@ -630,38 +630,38 @@ int fp64_node_grid(int64_t nn) { return (int)grid_for(nn, kNodeThreads); }
 
 void fp64_geometry(const StepParams &P, const Fp64State &S, cudaStream_t st, bool store_detj) {
   if (P.npe == 8)
-    k_geometry<8><<<grid_for(P.ne, kElemThreads), kElemThreads, 0, st>>>(P, S, store_detj);
+    k_fp64_geometry<8><<<grid_for(P.ne, kElemThreads), kElemThreads, 0, st>>>(P, S, store_detj);
   else
-    k_geometry<4><<<grid_for(P.ne, kElemThreads), kElemThreads, 0, st>>>(P, S, store_detj);
+    k_fp64_geometry<4><<<grid_for(P.ne, kElemThreads), kElemThreads, 0, st>>>(P, S, store_detj);
 }
 
 void fp64_nodal(const StepParams &P, const Fp64State &S, cudaStream_t st, int init_mode) {
   if (P.npe == 8)
-    k_nodal<8><<<grid_for(P.nn, kNodeThreads), kNodeThreads, 0, st>>>(P, S, init_mode);
+    k_fp64_nodal<8><<<grid_for(P.nn, kNodeThreads), kNodeThreads, 0, st>>>(P, S, init_mode);
   else
-    k_nodal<4><<<grid_for(P.nn, kNodeThreads), kNodeThreads, 0, st>>>(P, S, init_mode);
+    k_fp64_nodal<4><<<grid_for(P.nn, kNodeThreads), kNodeThreads, 0, st>>>(P, S, init_mode);
 }
 
 void fp64_elements(const StepParams &P, const Fp64State &S, cudaStream_t st) {
   if (P.npe == 8)
-    k_elements<8><<<grid_for(P.ne, kElemThreads), kElemThreads, 0, st>>>(P, S);
+    k_fp64_elements<8><<<grid_for(P.ne, kElemThreads), kElemThreads, 0, st>>>(P, S);
   else
-    k_elements<4><<<grid_for(P.ne, kElemThreads), kElemThreads, 0, st>>>(P, S);
+    k_fp64_elements<4><<<grid_for(P.ne, kElemThreads), kElemThreads, 0, st>>>(P, S);
 }
 
 void fp64_nodes(const StepParams &P, const Fp64State &S, cudaStream_t st, int node_grid) {
   if (P.npe == 8)
-    k_nodes<8><<<node_grid, kNodeThreads, 0, st>>>(P, S);
+    k_fp64_nodes<8><<<node_grid, kNodeThreads, 0, st>>>(P, S);
   else
-    k_nodes<4><<<node_grid, kNodeThreads, 0, st>>>(P, S);
+    k_fp64_nodes<4><<<node_grid, kNodeThreads, 0, st>>>(P, S);
 }
 
 void fp64_predict(const StepParams &P, const Fp64State &S, cudaStream_t st) {
-  k_predict<<<grid_for(P.nn, kNodeThreads), kNodeThreads, 0, st>>>(P, S);
+  k_fp64_predict<<<grid_for(P.nn, kNodeThreads), kNodeThreads, 0, st>>>(P, S);
 }
 
 void fp64_density(const StepParams &P, const Fp64State &S, const double *rho0, cudaStream_t st) {
-  k_density<<<grid_for(P.ne, kElemThreads), kElemThreads, 0, st>>>(P, S, rho0);
+  k_fp64_density<<<grid_for(P.ne, kElemThreads), kElemThreads, 0, st>>>(P, S, rho0);
 }
 
 }  // namespace wf

@@ -128,7 +128,7 @@ __device__ __forceinline__ void shape_derivs_f(const float J[3][3], float dH[3][
 
 // ---------------------------------------------------------------------------
 template <int NPE>
-__global__ void __launch_bounds__(kElemThreads) k_geometry(StepParams P, MixState M,
+__global__ void __launch_bounds__(kElemThreads) k_mix_geometry(StepParams P, MixState M,
                                                            float *vol) {
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= P.ne) return;
@@ -140,8 +140,11 @@ __global__ void __launch_bounds__(kElemThreads) k_geometry(StepParams P, MixStat
   vol[e] = det3f(J) * weightf<NPE>();
 }
 
+// Nodal volumes -> J ratio and lumped mass; for contact candidates also the
+// rigid-plane contact force (it needs only x, the predicted velocity and the
+// step's mass, all final here, so it is computed before the element phase).
 template <int NPE>
-__global__ void __launch_bounds__(kNodeThreads) k_nodal(StepParams P, MixState M,
+__global__ void __launch_bounds__(kNodeThreads) k_mix_nodal(StepParams P, MixState M,
                                                         const float *vol) {
   const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= P.nn) return;
@@ -150,7 +153,50 @@ __global__ void __launch_bounds__(kNodeThreads) k_nodal(StepParams P, MixState M
   for (int32_t k = 0; k < c; k++) s += __ldg(&vol[__ldg(&P.slot[b + k]) / NPE]);
   const float2 nc = __ldg(&M.nc[n]);
   M.jr[n] = s * nc.x;
-  if (P.mass_mode == 0) M.mass[n] = (s * (1.0f / NPE)) * nc.y;
+  float mass;
+  if (P.mass_mode == 0) {
+    mass = (s * (1.0f / NPE)) * nc.y;
+    M.mass[n] = mass;
+  } else {
+    mass = M.mass[n];
+  }
+  if (P.contact && (P.nflag[n] & NF_CONTACT)) {
+    // rigid plane, outward normal (0, 0, -1), at z0 + vz * Time
+    // (Domain_d::CalcContactForces, Contact.C:58-323, one plane)
+    const int64_t np = P.np;
+    const float2 xz = M.xh[2 * np + n];
+    const float vp0 = M.vp[n], vp1 = M.vp[np + n], vp2 = M.vp[2 * np + n];
+    const double zd = P.c_z0 + P.c_vz * P.st->time;
+    const float gap = (float)(zd - ((double)xz.x + (double)xz.y));
+    float cf0 = 0.f, cf1 = 0.f, cf2 = 0.f;
+    if (gap < 0.f) {
+      const float kmass = 0.2f * mass / (P.f_dt * P.f_dt);
+      const float k = (kmass < P.f_c_k) ? kmass : P.f_c_k;
+      const float ccrit = 2.0f * mass * sqrtf(k / mass);
+      cf2 = k * gap + 0.2f * ccrit * (-vp2);
+      float ut0 = M.ut[n] + vp0 * P.f_dt;
+      float ut1 = M.ut[np + n] + vp1 * P.f_dt;
+      float ftx = -k * ut0, fty = -k * ut1;
+      const float ft_max = P.f_c_mu * fabsf(cf2);
+      if (!(sqrtf(ftx * ftx + fty * fty) <= ft_max)) {
+        const float vt = sqrtf(vp0 * vp0 + vp1 * vp1);
+        if (vt > 0.f) {
+          ftx = -ft_max * vp0 / vt;
+          fty = -ft_max * vp1 / vt;
+        } else {
+          ftx = fty = 0.f;
+        }
+        ut0 = ut1 = 0.f;
+      }
+      M.ut[n] = ut0;
+      M.ut[np + n] = ut1;
+      cf0 = ftx;
+      cf1 = fty;
+    }
+    M.cf[n] = cf0;
+    M.cf[np + n] = cf1;
+    M.cf[2 * np + n] = cf2;
+  }
 }
 
 __device__ __forceinline__ float idf(int i) { return (i == 0 || i == 4 || i == 8) ? 1.f : 0.f; }
@@ -170,7 +216,7 @@ __device__ __forceinline__ void t3_mul_f(const float *a, const float *b, float *
 }
 
 template <int NPE>
-__global__ void __launch_bounds__(kElemThreads) k_elements(StepParams P, MixState M) {
+__global__ void __launch_bounds__(kElemThreads, 6) k_mix_elements(StepParams P, MixState M) {
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= P.ne) return;
   const int64_t ne = P.ne;
@@ -324,10 +370,9 @@ __global__ void __launch_bounds__(kElemThreads) k_elements(StepParams P, MixStat
     out[3 * a + 1] = f1;
     out[3 * a + 2] = f2;
   }
-  float4 *dst = reinterpret_cast<float4 *>(&M.fe[e * NPE * 3]);
+  // SoA by (local node, component): fe[(a * 3 + k) * ne + e]
 #pragma unroll
-  for (int q = 0; q < NPE * 3 / 4; q++)
-    dst[q] = make_float4(out[4 * q], out[4 * q + 1], out[4 * q + 2], out[4 * q + 3]);
+  for (int q = 0; q < NPE * 3; q++) M.fe[q * ne + e] = out[q];
 }
 
 // ---------------------------------------------------------------------------
@@ -348,7 +393,7 @@ __device__ __forceinline__ double block_sum_sparse(double v, bool nz, double *sh
 }
 
 template <int NPE>
-__global__ void __launch_bounds__(kNodeThreads) k_nodes(StepParams P, MixState M) {
+__global__ void __launch_bounds__(kNodeThreads) k_mix_nodes(StepParams P, MixState M) {
   __shared__ double sh[kNodeThreads / 32];
   __shared__ bool am_last;
   const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -356,12 +401,31 @@ __global__ void __launch_bounds__(kNodeThreads) k_nodes(StepParams P, MixState M
   if (n < P.nn) {
     const int64_t np = P.np;
     const int32_t b = __ldg(&P.off[n]), c = __ldg(&P.off[n + 1]) - b;
+    const int64_t ne = P.ne;
+    // gather over the node's element list in list order, eight entries at a
+    // time so that the slot and force loads of a chunk are all in flight
     float fi0 = 0.f, fi1 = 0.f, fi2 = 0.f;
-    for (int32_t k = 0; k < c; k++) {
-      const float *src = &M.fe[(int64_t)__ldg(&P.slot[b + k]) * 3];
-      fi0 += __ldg(src);
-      fi1 += __ldg(src + 1);
-      fi2 += __ldg(src + 2);
+    for (int32_t k0 = 0; k0 < c; k0 += 8) {
+      int32_t sl[8];
+#pragma unroll
+      for (int j = 0; j < 8; j++) sl[j] = (k0 + j < c) ? __ldg(&P.slot[b + k0 + j]) : -1;
+      float g0[8], g1[8], g2[8];
+#pragma unroll
+      for (int j = 0; j < 8; j++) {
+        g0[j] = g1[j] = g2[j] = 0.f;
+        if (sl[j] >= 0) {
+          const int64_t base = (int64_t)(sl[j] % NPE) * 3 * ne + sl[j] / NPE;
+          g0[j] = __ldg(&M.fe[base]);
+          g1[j] = __ldg(&M.fe[base + ne]);
+          g2[j] = __ldg(&M.fe[base + 2 * ne]);
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < 8; j++) {
+        fi0 += g0[j];
+        fi1 += g1[j];
+        fi2 += g2[j];
+      }
     }
     float fi[3] = {fi0, fi1, fi2};
 #pragma unroll
@@ -384,38 +448,10 @@ __global__ void __launch_bounds__(kNodeThreads) k_nodes(StepParams P, MixState M
     }
     float cf[3] = {0.f, 0.f, 0.f};
     if (P.contact && (fl & NF_CONTACT)) {
-      const double zd = P.c_z0 + P.c_vz * P.st->time;
-      const float gap = (float)(zd - ((double)x[2].x + (double)x[2].y));
-      if (gap < 0.f) {
-        const float kmass = 0.2f * mass / (P.f_dt * P.f_dt);
-        const float k = (kmass < P.f_c_k) ? kmass : P.f_c_k;
-        const float v_reln = -vp[2];
-        const float ccrit = 2.0f * mass * sqrtf(k * inv_m);
-        const float cfz = k * gap + 0.2f * ccrit * v_reln;
-        cf[2] = cfz;
-        r = fabsf(cfz);
-        float ut0 = M.ut[n] + vp[0] * P.f_dt;
-        float ut1 = M.ut[np + n] + vp[1] * P.f_dt;
-        float ftx = -k * ut0, fty = -k * ut1;
-        const float ft_max = P.f_c_mu * fabsf(cfz);
-        if (!(sqrtf(ftx * ftx + fty * fty) <= ft_max)) {
-          const float vt = sqrtf(vp[0] * vp[0] + vp[1] * vp[1]);
-          if (vt > 0.f) {
-            ftx = -ft_max * vp[0] / vt;
-            fty = -ft_max * vp[1] / vt;
-          } else {
-            ftx = fty = 0.f;
-          }
-          ut0 = ut1 = 0.f;
-        }
-        M.ut[n] = ut0;
-        M.ut[np + n] = ut1;
-        cf[0] = ftx;
-        cf[1] = fty;
-      }
-      M.cf[n] = cf[0];
-      M.cf[np + n] = cf[1];
-      M.cf[2 * np + n] = cf[2];
+      cf[0] = M.cf[n];
+      cf[1] = M.cf[np + n];
+      cf[2] = M.cf[2 * np + n];
+      r = fabsf(cf[2]);
     }
     if (!P.contact && (fl & NF_REACTION)) r = fi[P.react_dim];
     const uint32_t code = P.bc[n];
@@ -465,7 +501,7 @@ __global__ void __launch_bounds__(kNodeThreads) k_nodes(StepParams P, MixState M
   }
 }
 
-__global__ void k_predict(StepParams P, MixState M) {
+__global__ void k_mix_predict(StepParams P, MixState M) {
   const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= P.nn) return;
   const uint32_t code = P.bc[n];
@@ -478,7 +514,7 @@ __global__ void k_predict(StepParams P, MixState M) {
 
 // Copies the FP64 initial state (after the preamble) into the mixed arrays.
 template <int NPE>
-__global__ void k_init_nodes(StepParams P, MixState M, Fp64State S) {
+__global__ void k_mix_init_nodes(StepParams P, MixState M, Fp64State S) {
   const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= P.nn) return;
   const int64_t np = P.np;
@@ -498,7 +534,7 @@ __global__ void k_init_nodes(StepParams P, MixState M, Fp64State S) {
 
 // Writes the mixed state into the FP64 arrays read back by the host.
 template <int NPE>
-__global__ void k_export_nodes(StepParams P, MixState M, Fp64State S) {
+__global__ void k_mix_export_nodes(StepParams P, MixState M, Fp64State S) {
   const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= P.nn) return;
   const int64_t np = P.np;
@@ -516,7 +552,7 @@ __global__ void k_export_nodes(StepParams P, MixState M, Fp64State S) {
 }
 
 template <int NPE>
-__global__ void k_export_elems(StepParams P, MixState M, Fp64State S, const float *vol) {
+__global__ void k_mix_export_elems(StepParams P, MixState M, Fp64State S, const float *vol) {
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= P.ne) return;
   const int64_t ne = P.ne;
@@ -549,51 +585,51 @@ int mix_node_grid(int64_t nn) { return (int)grid_for(nn, kNodeThreads); }
 
 void mix_init(const StepParams &P, const MixState &M, const Fp64State &S, cudaStream_t st) {
   if (P.npe == 8)
-    k_init_nodes<8><<<grid_for(P.nn, kNodeThreads), kNodeThreads, 0, st>>>(P, M, S);
+    k_mix_init_nodes<8><<<grid_for(P.nn, kNodeThreads), kNodeThreads, 0, st>>>(P, M, S);
   else
-    k_init_nodes<4><<<grid_for(P.nn, kNodeThreads), kNodeThreads, 0, st>>>(P, M, S);
+    k_mix_init_nodes<4><<<grid_for(P.nn, kNodeThreads), kNodeThreads, 0, st>>>(P, M, S);
 }
 
 void mix_geometry(const StepParams &P, const MixState &M, float *vol, cudaStream_t st) {
   if (P.npe == 8)
-    k_geometry<8><<<grid_for(P.ne, kElemThreads), kElemThreads, 0, st>>>(P, M, vol);
+    k_mix_geometry<8><<<grid_for(P.ne, kElemThreads), kElemThreads, 0, st>>>(P, M, vol);
   else
-    k_geometry<4><<<grid_for(P.ne, kElemThreads), kElemThreads, 0, st>>>(P, M, vol);
+    k_mix_geometry<4><<<grid_for(P.ne, kElemThreads), kElemThreads, 0, st>>>(P, M, vol);
 }
 
 void mix_nodal(const StepParams &P, const MixState &M, const float *vol, cudaStream_t st) {
   if (P.npe == 8)
-    k_nodal<8><<<grid_for(P.nn, kNodeThreads), kNodeThreads, 0, st>>>(P, M, vol);
+    k_mix_nodal<8><<<grid_for(P.nn, kNodeThreads), kNodeThreads, 0, st>>>(P, M, vol);
   else
-    k_nodal<4><<<grid_for(P.nn, kNodeThreads), kNodeThreads, 0, st>>>(P, M, vol);
+    k_mix_nodal<4><<<grid_for(P.nn, kNodeThreads), kNodeThreads, 0, st>>>(P, M, vol);
 }
 
 void mix_elements(const StepParams &P, const MixState &M, const float *, cudaStream_t st) {
   if (P.npe == 8)
-    k_elements<8><<<grid_for(P.ne, kElemThreads), kElemThreads, 0, st>>>(P, M);
+    k_mix_elements<8><<<grid_for(P.ne, kElemThreads), kElemThreads, 0, st>>>(P, M);
   else
-    k_elements<4><<<grid_for(P.ne, kElemThreads), kElemThreads, 0, st>>>(P, M);
+    k_mix_elements<4><<<grid_for(P.ne, kElemThreads), kElemThreads, 0, st>>>(P, M);
 }
 
 void mix_nodes(const StepParams &P, const MixState &M, cudaStream_t st, int node_grid) {
   if (P.npe == 8)
-    k_nodes<8><<<node_grid, kNodeThreads, 0, st>>>(P, M);
+    k_mix_nodes<8><<<node_grid, kNodeThreads, 0, st>>>(P, M);
   else
-    k_nodes<4><<<node_grid, kNodeThreads, 0, st>>>(P, M);
+    k_mix_nodes<4><<<node_grid, kNodeThreads, 0, st>>>(P, M);
 }
 
 void mix_predict(const StepParams &P, const MixState &M, cudaStream_t st) {
-  k_predict<<<grid_for(P.nn, kNodeThreads), kNodeThreads, 0, st>>>(P, M);
+  k_mix_predict<<<grid_for(P.nn, kNodeThreads), kNodeThreads, 0, st>>>(P, M);
 }
 
 void mix_export(const StepParams &P, const MixState &M, const Fp64State &S, const float *vol,
                 cudaStream_t st) {
   if (P.npe == 8) {
-    k_export_nodes<8><<<grid_for(P.nn, kNodeThreads), kNodeThreads, 0, st>>>(P, M, S);
-    k_export_elems<8><<<grid_for(P.ne, kElemThreads), kElemThreads, 0, st>>>(P, M, S, vol);
+    k_mix_export_nodes<8><<<grid_for(P.nn, kNodeThreads), kNodeThreads, 0, st>>>(P, M, S);
+    k_mix_export_elems<8><<<grid_for(P.ne, kElemThreads), kElemThreads, 0, st>>>(P, M, S, vol);
   } else {
-    k_export_nodes<4><<<grid_for(P.nn, kNodeThreads), kNodeThreads, 0, st>>>(P, M, S);
-    k_export_elems<4><<<grid_for(P.ne, kElemThreads), kElemThreads, 0, st>>>(P, M, S, vol);
+    k_mix_export_nodes<4><<<grid_for(P.nn, kNodeThreads), kNodeThreads, 0, st>>>(P, M, S);
+    k_mix_export_elems<4><<<grid_for(P.ne, kElemThreads), kElemThreads, 0, st>>>(P, M, S, vol);
   }
 }
 

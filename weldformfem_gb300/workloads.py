@@ -209,10 +209,10 @@ class Case:
                     mu=float(c["mu"]))
 
 
-def apply_options(dom, case: Case, with_bcs=True, x=None):
-    """Everything after the mesh: materials, BCs, options, dt. Returns dt."""
-    if x is None:
-        x = case.coords()
+def apply_options(dom, case: Case, with_bcs=True, x=None, set_dt=True):
+    """Everything after the mesh: materials, BCs, options, dt. Returns dt
+    (None when set_dt is False: the caller sets it, e.g. from the device
+    min-edge reduction after init)."""
     dom.set_materials(case.materials, case.elem_mat)
     if with_bcs:
         dom.add_bcs(case.bcs())
@@ -227,9 +227,19 @@ def apply_options(dom, case: Case, with_bcs=True, x=None):
         dom.set_contact_plane(cp["z0"], cp["vz"], cp["kpen"], cp["mu"], case.top_nodes())
     else:
         dom.set_reaction_nodes(case.top_nodes(), 2)
+    if not set_dt:
+        return None
+    if x is None:
+        x = case.coords()
     dt = case.time_step(x)
     dom.set_dt(dt)
     return dt
+
+
+def cfl_dt(case: Case, hmin: float) -> float:
+    """dt = factor * h_min / sqrt(E / rho) of the first material."""
+    m = case.materials[0]
+    return case.dt_factor * hmin / np.sqrt(m["E"] / m["rho"])
 
 
 def apply(dom, case: Case, x=None, with_bcs=True):
