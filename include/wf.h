@@ -187,6 +187,31 @@ WF_API wf_status wf_get_stream(const wf_domain *d, void **stream);
 /* Bytes copied host->device and device->host by this domain so far. */
 WF_API wf_status wf_get_transfer_bytes(const wf_domain *d, int64_t *h2d, int64_t *d2h);
 
+/* ---- allocation-free entry point ------------------------------------------------ */
+/* No counterpart in the reference. For callers that cannot allocate device
+ * memory (code inside another framework's memory pool, loops that must not
+ * risk the synchronisation cudaMalloc/cudaFree can cause, hosts with a device
+ * budget fixed up front): the element volumes and per-node volume sums of
+ * the step's geometry and nodal phases (CalcElemVol, Mechanical.C:264-293;
+ * CalcNodalVol, :1555-1572), computed without any allocation. The caller
+ * passes device pointers: xyz[3*nn] interleaved coordinates, elnod[ne*npe]
+ * (npe 8 or 4), the node->element lists as wf_get_connectivity returns them
+ * (nodel_offset[nn], nodel_count[nn], nodel[total]) and voln[nn] for the
+ * result (sum of the node's element volumes divided by npe); work is queued
+ * on `stream` (a cudaStream_t, 0 for the default stream) and the call
+ * returns without waiting.
+ * The element volumes go to a static device array of WF_NOALLOC_MAX_ELEMS
+ * doubles (8 MiB) that every GPU which loads the library holds until exit;
+ * ne above that returns WF_ERR_UNSUPPORTED. The array is shared by all calls
+ * and keeps the last call's contents; calls that overlap on the GPU race.
+ * The first call on a device looks up the array's device address; make that
+ * first call before any stream capture. */
+#define WF_NOALLOC_MAX_ELEMS 1048576
+WF_API wf_status wf_nodal_volumes_noalloc(const double *xyz, const int32_t *elnod, int64_t nn,
+                                          int64_t ne, int32_t npe, const int32_t *nodel_offset,
+                                          const int32_t *nodel_count, const int32_t *nodel,
+                                          double *voln, void *stream);
+
 /* ---- readback (host buffers) -------------------------------------------------- */
 WF_API wf_status wf_get_node_field(wf_domain *d, int32_t field, double *out);   /* 3*nn */
 WF_API wf_status wf_get_node_scalar(wf_domain *d, int32_t field, double *out);  /* nn */

@@ -101,6 +101,9 @@ _SIGS = {
     "wf_get_launch_count": [C.c_void_p, C.POINTER(C.c_int64)],
     "wf_get_stream": [C.c_void_p, C.POINTER(C.c_void_p)],
     "wf_get_transfer_bytes": [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)],
+    # allocation-free nodal volumes: device pointers in, device pointer out
+    "wf_nodal_volumes_noalloc": [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_int32,
+                                 C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p],
 }
 
 

@@ -28,6 +28,7 @@ UNITS = {
     "wf_fp64.cu": ["--fmad=false"],
     "wf_mixed.cu": [],
     "wf_reduce.cu": [],
+    "wf_noalloc.cu": ["--fmad=false"],
 }
 
 
