@@ -21,11 +21,14 @@ constexpr int kElemThreads = 128;
 constexpr int kNodeThreads = 256;
 
 // Flanagan-Belytschko hourglass base vectors of the 8-node hexahedron
-// (test_1el_3D.cpp:166-169).
-__constant__ double c_hg_sig[4][8] = {{1., 1., -1., -1., -1., -1., 1., 1.},
-                                      {1., -1., -1., 1., -1., 1., 1., -1.},
-                                      {1., -1., 1., -1., 1., -1., 1., -1.},
-                                      {-1., 1., -1., 1., 1., -1., 1., -1.}};
+// (test_1el_3D.cpp:166-169), as compile-time signs.
+__device__ __forceinline__ constexpr int hg_sig(int j, int a) {
+  constexpr signed char t[4][8] = {{1, 1, -1, -1, -1, -1, 1, 1},
+                                   {1, -1, -1, 1, -1, 1, 1, -1},
+                                   {1, -1, 1, -1, 1, -1, 1, -1},
+                                   {-1, 1, -1, 1, 1, -1, 1, -1}};
+  return t[j][a];
+}
 
 __device__ __forceinline__ double det3(const double J[3][3]) {
   // Matrix::calcDet (include/common/Matrix.h:593-620)
@@ -163,28 +166,6 @@ __global__ void __launch_bounds__(kNodeThreads) k_fp64_nodal(StepParams P, Fp64S
   S.jr[n] = s / s0;
 }
 
-// ---------------------------------------------------------------------------
-// tensor3 helpers in the reference's component algebra (Tensor3.C).
-enum { XX, XY, XZ, YX, YY, YZ, ZX, ZY, ZZ };
-
-// operator*(tensor3, tensor3) exactly as include/common/Tensor3.C:290-303
-// writes it (its off-diagonal entries pair the rows of both factors).
-__device__ __forceinline__ void t3_mul(const double *a, const double *b, double *r) {
-  r[XX] = a[XX] * b[XX] + a[XY] * b[YX] + a[XZ] * b[ZX];
-  r[XY] = a[XX] * b[YX] + a[XY] * b[YY] + a[XZ] * b[YZ];
-  r[XZ] = a[XX] * b[ZX] + a[XY] * b[ZY] + a[XZ] * b[ZZ];
-  r[YX] = a[YX] * b[XX] + a[YY] * b[YX] + a[YZ] * b[ZX];
-  r[YY] = a[YX] * b[YX] + a[YY] * b[YY] + a[YZ] * b[YZ];
-  r[YZ] = a[YX] * b[ZX] + a[YY] * b[ZY] + a[YZ] * b[ZZ];
-  r[ZX] = a[ZX] * b[XX] + a[ZY] * b[YX] + a[ZZ] * b[ZX];
-  r[ZY] = a[ZX] * b[YX] + a[ZY] * b[YY] + a[ZZ] * b[YZ];
-  r[ZZ] = a[ZX] * b[ZX] + a[ZY] * b[ZY] + a[ZZ] * b[ZZ];
-}
-
-__device__ __forceinline__ double idv(int i) {
-  return (i == XX || i == YY || i == ZZ) ? 1. : 0.;
-}
-
 __device__ __forceinline__ double hollomon_sy(double strain, const MatDev &m) {
   if (strain + m.eps0 > m.eps1) return m.hol_K * pow(strain + m.eps0, m.hol_m);
   return m.sy0;
@@ -249,9 +230,12 @@ __global__ void __launch_bounds__(kElemThreads) k_fp64_elements(StepParams P, Fp
       if (P.hg_on) {
 #pragma unroll
         for (int j = 0; j < 4; j++) {
-          hm[0][j] += v0 * c_hg_sig[j][a];
-          hm[1][j] += v1 * c_hg_sig[j][a];
-          hm[2][j] += v2 * c_hg_sig[j][a];
+          // v * Gamma with Gamma = +-1 is exact: add or subtract
+          if (hg_sig(j, a) > 0) {
+            hm[0][j] += v0; hm[1][j] += v1; hm[2][j] += v2;
+          } else {
+            hm[0][j] -= v0; hm[1][j] -= v1; hm[2][j] -= v2;
+          }
         }
       }
     }
@@ -310,46 +294,43 @@ __global__ void __launch_bounds__(kElemThreads) k_fp64_elements(StepParams P, Fp
     }
   }
 
-  // Jaumann rate + radial return (CalcStressStrain)
+  // Jaumann rate + radial return (CalcStressStrain). The tensor3 algebra of
+  // the reference (Tensor3.C) written out on the six stored components: the
+  // addends that multiply an exact zero of the spin or of the identity's
+  // off-diagonal are dropped, which leaves every value unchanged (only the
+  // sign of an exact zero could differ) and saves FP64 instructions.
   const double dt = P.dt;
-  double SS[9], SR[9], RR[9], RT[9], SRT[9], RS[9];
+  double t0 = S.tau[e], t1 = S.tau[ne + e], t2 = S.tau[2 * ne + e];
+  double t3 = S.tau[3 * ne + e], t4 = S.tau[4 * ne + e], t5 = S.tau[5 * ne + e];
   {
-    double t0 = S.tau[e], t1 = S.tau[ne + e], t2 = S.tau[2 * ne + e];
-    double t3 = S.tau[3 * ne + e], t4 = S.tau[4 * ne + e], t5 = S.tau[5 * ne + e];
-    SS[XX] = t0; SS[YY] = t1; SS[ZZ] = t2;
-    SS[XY] = SS[YX] = t3; SS[YZ] = SS[ZY] = t4; SS[XZ] = SS[ZX] = t5;
-  }
-  SR[XX] = s00; SR[YY] = s11; SR[ZZ] = s22;
-  SR[XY] = SR[YX] = s01; SR[YZ] = SR[ZY] = s12; SR[XZ] = SR[ZX] = s02;
-  RR[XX] = 0.0; RR[YY] = 0.0; RR[ZZ] = 0.0;
-  RR[XY] = w01; RR[YZ] = w12; RR[XZ] = w02;
-  RR[YX] = -w01; RR[ZY] = -w12; RR[ZX] = -w02;
-  RT[XX] = RR[XX]; RT[YY] = RR[YY]; RT[ZZ] = RR[ZZ];
-  RT[XY] = RR[YX]; RT[XZ] = RR[ZX]; RT[YX] = RR[XY];
-  RT[YZ] = RR[ZY]; RT[ZX] = RR[XZ]; RT[ZY] = RR[YZ];
-  t3_mul(SS, RT, SRT);
-  t3_mul(RR, SS, RS);
-  {
-    const double c = 1.0 / 3.0 * (SR[XX] + SR[YY] + SR[ZZ]);
+    // SRT = tau * Trans(W), RS = W * tau with the product of Tensor3.C:290-303
+    const double srt0 = t3 * w01 + t5 * w02;    // xx
+    const double srt1 = t3 * w01 - t4 * w12;    // yy
+    const double srt2 = t5 * w02 + t4 * w12;    // zz
+    const double srt3 = t0 * w01 - t5 * w12;    // xy
+    const double srt4 = t3 * w02 + t1 * w12;    // yz
+    const double srt5 = t0 * w02 + t3 * w12;    // xz
+    const double rs0 = w01 * t3 + w02 * t5;
+    const double rs1 = w12 * t4 - w01 * t3;
+    const double rs2 = -(w02 * t5 + w12 * t4);
+    const double rs3 = w01 * t1 + w02 * t4;
+    const double rs4 = w12 * t2 - w01 * t5;
+    const double rs5 = w01 * t4 + w02 * t2;
+    const double c = 1.0 / 3.0 * (s00 + s11 + s22);
     const double g2 = 2.0 * m.G;
-#pragma unroll
-    for (int i = 0; i < 9; i++) {
-      double A = (SR[i] - idv(i) * c) * g2;
-      A = A + SRT[i];
-      A = A + RS[i];
-      SS[i] = SS[i] + A * dt;
-    }
+    t0 = t0 + (((s00 - c) * g2 + srt0) + rs0) * dt;
+    t1 = t1 + (((s11 - c) * g2 + srt1) + rs1) * dt;
+    t2 = t2 + (((s22 - c) * g2 + srt2) + rs2) * dt;
+    t3 = t3 + ((s01 * g2 + srt3) + rs3) * dt;
+    t4 = t4 + ((s12 * g2 + srt4) + rs4) * dt;
+    t5 = t5 + ((s02 * g2 + srt5) + rs5) * dt;
   }
-  double ST[9], Sd[9];
-#pragma unroll
-  for (int i = 0; i < 9; i++) ST[i] = idv(i) * (-p) + SS[i];
-  {
-    const double c2 = (1.0 / 3.0) * (ST[XX] + ST[YY] + ST[ZZ]);
-#pragma unroll
-    for (int i = 0; i < 9; i++) Sd[i] = ST[i] - idv(i) * c2;
-  }
-  const double J2 = 0.5 * (Sd[XX] * Sd[XX] + 2.0 * Sd[XY] * Sd[XY] + 2.0 * Sd[XZ] * Sd[XZ] +
-                           Sd[YY] * Sd[YY] + 2.0 * Sd[YZ] * Sd[YZ] + Sd[ZZ] * Sd[ZZ]);
+  // sigma_trial = -p I + tau; s_trial = sigma_trial - tr/3 I
+  const double st0 = t0 - p, st1 = t1 - p, st2 = t2 - p;
+  const double c2 = (1.0 / 3.0) * (st0 + st1 + st2);
+  const double d0s = st0 - c2, d1s = st1 - c2, d2s = st2 - c2;
+  const double J2 = 0.5 * (d0s * d0s + 2.0 * t3 * t3 + 2.0 * t5 * t5 + d1s * d1s +
+                           2.0 * t4 * t4 + d2s * d2s);
   const double sig_trial = sqrt(3.0 * J2);
   double pls = S.pls[e];
   double sy;
@@ -362,13 +343,11 @@ __global__ void __launch_bounds__(kElemThreads) k_fp64_elements(StepParams P, Fp
     const double G = m.G;
     const double dgamma = (sig_trial - sy) / (3.0 * G + H);
     const double factor = 1.0 - (3.0 * G * dgamma) / sig_trial;
-#pragma unroll
-    for (int i = 0; i < 9; i++) SS[i] = Sd[i] * factor;
+    t0 = d0s * factor; t1 = d1s * factor; t2 = d2s * factor;
+    t3 = t3 * factor; t4 = t4 * factor; t5 = t5 * factor;
     pls += dgamma;
   }
-  double SG[9];
-#pragma unroll
-  for (int i = 0; i < 9; i++) SG[i] = idv(i) * (-p) + SS[i];
+  double SG[6] = {t0 - p, t1 - p, t2 - p, t3, t4, t5};
   // total strain: eps = eps + dt * D
   {
     double e0 = S.eps[e], e1 = S.eps[ne + e], e2 = S.eps[2 * ne + e];
@@ -389,20 +368,19 @@ __global__ void __launch_bounds__(kElemThreads) k_fp64_elements(StepParams P, Fp
       double q = P.av[0] * c * fabs(eps_v) * l + P.av[1] * pow(eps_v * l, 2);
       q = (1e9 < q) ? 1e9 : q;
       const double qs = (eps_v > 0) ? -q : q;
-      SG[XX] += qs;
-      SG[YY] += qs;
-      SG[ZZ] += qs;
+      SG[0] += qs;
+      SG[1] += qs;
+      SG[2] += qs;
     }
   }
   S.p[e] = p;
   S.pls[e] = pls;
   S.sy[e] = sy;
-  const double sg0 = SG[XX], sg1 = SG[YY], sg2 = SG[ZZ], sg3 = SG[XY], sg4 = SG[YZ],
-               sg5 = SG[XZ];
+  const double sg0 = SG[0], sg1 = SG[1], sg2 = SG[2], sg3 = SG[3], sg4 = SG[4], sg5 = SG[5];
   S.sig[e] = sg0; S.sig[ne + e] = sg1; S.sig[2 * ne + e] = sg2;
   S.sig[3 * ne + e] = sg3; S.sig[4 * ne + e] = sg4; S.sig[5 * ne + e] = sg5;
-  S.tau[e] = SS[XX]; S.tau[ne + e] = SS[YY]; S.tau[2 * ne + e] = SS[ZZ];
-  S.tau[3 * ne + e] = SS[XY]; S.tau[4 * ne + e] = SS[YZ]; S.tau[5 * ne + e] = SS[XZ];
+  S.tau[e] = t0; S.tau[ne + e] = t1; S.tau[2 * ne + e] = t2;
+  S.tau[3 * ne + e] = t3; S.tau[4 * ne + e] = t4; S.tau[5 * ne + e] = t5;
   S.sr[e] = s00; S.sr[ne + e] = s11; S.sr[2 * ne + e] = s22;
   S.sr[3 * ne + e] = s01; S.sr[4 * ne + e] = s12; S.sr[5 * ne + e] = s02;
   S.rr[e] = 0.0; S.rr[ne + e] = 0.0; S.rr[2 * ne + e] = 0.0;
@@ -414,10 +392,8 @@ __global__ void __launch_bounds__(kElemThreads) k_fp64_elements(StepParams P, Fp
 #pragma unroll
   for (int a = 0; a < NPE; a++) {
     const double d0 = dH[0][a], d1 = dH[1][a], d2 = dH[2][a];
-    double f0 = 0.0, f1 = 0.0, f2 = 0.0;
-    f0 += d0 * sg0 * 1.0;
-    f1 += d1 * sg1 * 1.0;
-    f2 += d2 * sg2 * 1.0;
+    // 0.0 + d * sigma * 1.0 of the reference is d * sigma (exact)
+    double f0 = d0 * sg0, f1 = d1 * sg1, f2 = d2 * sg2;
     f0 += d1 * sg3 + d2 * sg5;
     f1 += d0 * sg3 + d2 * sg4;
     f2 += d1 * sg4 + d0 * sg5;
@@ -428,14 +404,23 @@ __global__ void __launch_bounds__(kElemThreads) k_fp64_elements(StepParams P, Fp
   if constexpr (NPE == 8) {
     if (P.hg_on) {
       const double ch = P.hg_coef * pow(vol, 0.6666666) * S.rho[e] * 0.25 * m.cs0;
+      double chm[3][4];
+#pragma unroll
+      for (int k = 0; k < 3; k++)
+#pragma unroll
+        for (int j = 0; j < 4; j++) chm[k][j] = ch * hm[k][j];
       double *fh = &S.fhg[e * 24];
 #pragma unroll
       for (int i = 0; i < 8; i++) {
 #pragma unroll
         for (int k = 0; k < 3; k++) {
+          // acc -= ch * h * Gamma with Gamma = +-1: exact sign flips
           double acc = 0.0;
 #pragma unroll
-          for (int j = 0; j < 4; j++) acc -= ch * hm[k][j] * c_hg_sig[j][i];
+          for (int j = 0; j < 4; j++) {
+            if (hg_sig(j, i) > 0) acc -= chm[k][j];
+            else acc += chm[k][j];
+          }
           fh[3 * i + k] = acc;
         }
       }

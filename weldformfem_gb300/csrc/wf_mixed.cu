@@ -19,10 +19,15 @@ namespace {
 constexpr int kElemThreads = 128;
 constexpr int kNodeThreads = 256;
 
-__constant__ float c_sig[4][8] = {{1.f, 1.f, -1.f, -1.f, -1.f, -1.f, 1.f, 1.f},
-                                  {1.f, -1.f, -1.f, 1.f, -1.f, 1.f, 1.f, -1.f},
-                                  {1.f, -1.f, 1.f, -1.f, 1.f, -1.f, 1.f, -1.f},
-                                  {-1.f, 1.f, -1.f, 1.f, 1.f, -1.f, 1.f, -1.f}};
+// Flanagan-Belytschko hourglass base vectors (test_1el_3D.cpp:166-169) as a
+// compile-time sign table: after unrolling, x * sign folds to +x or -x.
+__device__ __forceinline__ constexpr float c_sig_at(int j, int a) {
+  constexpr signed char t[4][8] = {{1, 1, -1, -1, -1, -1, 1, 1},
+                                   {1, -1, -1, 1, -1, 1, 1, -1},
+                                   {1, -1, 1, -1, 1, -1, 1, -1},
+                                   {-1, 1, -1, 1, 1, -1, 1, -1}};
+  return (float)t[j][a];
+}
 
 // (hi, lo) pair helpers ------------------------------------------------------
 __device__ __forceinline__ float2 split_d(double v) {
@@ -199,22 +204,6 @@ __global__ void __launch_bounds__(kNodeThreads) k_mix_nodal(StepParams P, MixSta
   }
 }
 
-__device__ __forceinline__ float idf(int i) { return (i == 0 || i == 4 || i == 8) ? 1.f : 0.f; }
-
-// operator*(tensor3, tensor3) of include/common/Tensor3.C:290-303, FP32
-__device__ __forceinline__ void t3_mul_f(const float *a, const float *b, float *r) {
-  enum { XX, XY, XZ, YX, YY, YZ, ZX, ZY, ZZ };
-  r[XX] = a[XX] * b[XX] + a[XY] * b[YX] + a[XZ] * b[ZX];
-  r[XY] = a[XX] * b[YX] + a[XY] * b[YY] + a[XZ] * b[YZ];
-  r[XZ] = a[XX] * b[ZX] + a[XY] * b[ZY] + a[XZ] * b[ZZ];
-  r[YX] = a[YX] * b[XX] + a[YY] * b[YX] + a[YZ] * b[ZX];
-  r[YY] = a[YX] * b[YX] + a[YY] * b[YY] + a[YZ] * b[YZ];
-  r[YZ] = a[YX] * b[ZX] + a[YY] * b[ZY] + a[YZ] * b[ZZ];
-  r[ZX] = a[ZX] * b[XX] + a[ZY] * b[YX] + a[ZZ] * b[ZX];
-  r[ZY] = a[ZX] * b[YX] + a[ZY] * b[YY] + a[ZZ] * b[YZ];
-  r[ZZ] = a[ZX] * b[ZX] + a[ZY] * b[ZY] + a[ZZ] * b[ZZ];
-}
-
 template <int NPE>
 __global__ void __launch_bounds__(kElemThreads, 6) k_mix_elements(StepParams P, MixState M) {
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -262,9 +251,9 @@ __global__ void __launch_bounds__(kElemThreads, 6) k_mix_elements(StepParams P, 
       if (P.hg_on) {
 #pragma unroll
         for (int j = 0; j < 4; j++) {
-          hm[0][j] += v0 * c_sig[j][a];
-          hm[1][j] += v1 * c_sig[j][a];
-          hm[2][j] += v2 * c_sig[j][a];
+          hm[0][j] += v0 * c_sig_at(j, a);
+          hm[1][j] += v1 * c_sig_at(j, a);
+          hm[2][j] += v2 * c_sig_at(j, a);
         }
       }
     }
@@ -279,40 +268,35 @@ __global__ void __launch_bounds__(kElemThreads, 6) k_mix_elements(StepParams P, 
   if (J_bar < 0.0f) J_bar = 0.2f;
   const float p = -m.K * (J_bar - 1.0f);
 
-  // Jaumann rate + radial return
+  // Jaumann rate + radial return. The reference's tensor3 product
+  // (Tensor3.C:290-303) written out for a symmetric tau and the spin W
+  // (antisymmetric, zero diagonal): only the six stored components are
+  // formed, terms that multiply a zero of W are dropped.
   const float dt = P.f_dt;
-  float SS[9], SR[9], RR[9], RT[9], SRT[9], RS[9];
+  float t0 = M.tau[e], t1 = M.tau[ne + e], t2 = M.tau[2 * ne + e];
+  float t3 = M.tau[3 * ne + e], t4 = M.tau[4 * ne + e], t5 = M.tau[5 * ne + e];
   {
-    const float t0 = M.tau[e], t1 = M.tau[ne + e], t2 = M.tau[2 * ne + e];
-    const float t3 = M.tau[3 * ne + e], t4 = M.tau[4 * ne + e], t5 = M.tau[5 * ne + e];
-    SS[0] = t0; SS[4] = t1; SS[8] = t2;
-    SS[1] = SS[3] = t3; SS[5] = SS[7] = t4; SS[2] = SS[6] = t5;
-  }
-  SR[0] = s00; SR[4] = s11; SR[8] = s22;
-  SR[1] = SR[3] = s01; SR[5] = SR[7] = s12; SR[2] = SR[6] = s02;
-  RR[0] = 0.f; RR[4] = 0.f; RR[8] = 0.f;
-  RR[1] = w01; RR[5] = w12; RR[2] = w02;
-  RR[3] = -w01; RR[7] = -w12; RR[6] = -w02;
-  RT[0] = 0.f; RT[4] = 0.f; RT[8] = 0.f;
-  RT[1] = RR[3]; RT[2] = RR[6]; RT[3] = RR[1];
-  RT[5] = RR[7]; RT[6] = RR[2]; RT[7] = RR[5];
-  t3_mul_f(SS, RT, SRT);
-  t3_mul_f(RR, SS, RS);
-  {
-    const float c = (1.0f / 3.0f) * (SR[0] + SR[4] + SR[8]);
+    // tau W^T                      W tau
+    const float srt0 = t3 * w01 + t5 * w02, rs0 = w01 * t3 + w02 * t5;    // xx
+    const float srt1 = t3 * w01 - t4 * w12, rs1 = w12 * t4 - w01 * t3;    // yy
+    const float srt2 = t5 * w02 + t4 * w12, rs2 = -(w02 * t5 + w12 * t4); // zz
+    const float srt3 = t0 * w01 - t5 * w12, rs3 = w01 * t1 + w02 * t4;    // xy
+    const float srt4 = t3 * w02 + t1 * w12, rs4 = w12 * t2 - w01 * t5;    // yz
+    const float srt5 = t0 * w02 + t3 * w12, rs5 = w01 * t4 + w02 * t2;    // xz
+    const float c = (1.0f / 3.0f) * (s00 + s11 + s22);
     const float g2 = 2.0f * m.G;
-#pragma unroll
-    for (int i = 0; i < 9; i++) SS[i] = SS[i] + ((SR[i] - idf(i) * c) * g2 + SRT[i] + RS[i]) * dt;
+    t0 += ((s00 - c) * g2 + srt0 + rs0) * dt;
+    t1 += ((s11 - c) * g2 + srt1 + rs1) * dt;
+    t2 += ((s22 - c) * g2 + srt2 + rs2) * dt;
+    t3 += (s01 * g2 + srt3 + rs3) * dt;
+    t4 += (s12 * g2 + srt4 + rs4) * dt;
+    t5 += (s02 * g2 + srt5 + rs5) * dt;
   }
-  // deviatoric trial stress: s = tau - tr(tau)/3 I (the pressure part cancels)
-  float Sd[9];
-  {
-    const float c2 = (1.0f / 3.0f) * ((SS[0] - p) + (SS[4] - p) + (SS[8] - p));
-#pragma unroll
-    for (int i = 0; i < 9; i++) Sd[i] = (SS[i] - idf(i) * p) - idf(i) * c2;
-  }
-  const float J2 = 0.5f * (Sd[0] * Sd[0] + 2.0f * Sd[1] * Sd[1] + 2.0f * Sd[2] * Sd[2] +
-                           Sd[4] * Sd[4] + 2.0f * Sd[5] * Sd[5] + Sd[8] * Sd[8]);
+  // deviatoric trial stress of sigma_trial = tau - p I
+  const float c2 = (1.0f / 3.0f) * ((t0 - p) + (t1 - p) + (t2 - p));
+  const float d0s = (t0 - p) - c2, d1s = (t1 - p) - c2, d2s = (t2 - p) - c2;
+  const float J2 = 0.5f * (d0s * d0s + 2.0f * t3 * t3 + 2.0f * t5 * t5 + d1s * d1s +
+                           2.0f * t4 * t4 + d2s * d2s);
   const float sig_trial = sqrtf(3.0f * J2);
   float pls = M.pls[e];
   float sy;
@@ -328,15 +312,15 @@ __global__ void __launch_bounds__(kElemThreads, 6) k_mix_elements(StepParams P, 
                         : m.H;
     const float dgamma = (sig_trial - sy) / (3.0f * m.G + H);
     const float factor = 1.0f - (3.0f * m.G * dgamma) / sig_trial;
-#pragma unroll
-    for (int i = 0; i < 9; i++) SS[i] = Sd[i] * factor;
+    t0 = d0s * factor; t1 = d1s * factor; t2 = d2s * factor;
+    t3 *= factor; t4 *= factor; t5 *= factor;
     pls += dgamma;
   }
   M.pls[e] = pls;
-  M.tau[e] = SS[0]; M.tau[ne + e] = SS[4]; M.tau[2 * ne + e] = SS[8];
-  M.tau[3 * ne + e] = SS[1]; M.tau[4 * ne + e] = SS[5]; M.tau[5 * ne + e] = SS[2];
-  const float sg0 = SS[0] - p, sg1 = SS[4] - p, sg2 = SS[8] - p;
-  const float sg3 = SS[1], sg4 = SS[5], sg5 = SS[2];
+  M.tau[e] = t0; M.tau[ne + e] = t1; M.tau[2 * ne + e] = t2;
+  M.tau[3 * ne + e] = t3; M.tau[4 * ne + e] = t4; M.tau[5 * ne + e] = t5;
+  const float sg0 = t0 - p, sg1 = t1 - p, sg2 = t2 - p;
+  const float sg3 = t3, sg4 = t4, sg5 = t5;
 
   // element force minus hourglass force
   const float w = weightf<NPE>();
@@ -356,9 +340,9 @@ __global__ void __launch_bounds__(kElemThreads, 6) k_mix_elements(StepParams P, 
         float g0 = 0.f, g1 = 0.f, g2 = 0.f;
 #pragma unroll
         for (int j = 0; j < 4; j++) {
-          g0 += hm[0][j] * c_sig[j][a];
-          g1 += hm[1][j] * c_sig[j][a];
-          g2 += hm[2][j] * c_sig[j][a];
+          g0 += hm[0][j] * c_sig_at(j, a);
+          g1 += hm[1][j] * c_sig_at(j, a);
+          g2 += hm[2][j] * c_sig_at(j, a);
         }
         // f_hg = -ch * sum_j h_j Gamma_j; assembly subtracts it
         f0 += ch * g0;
