@@ -125,6 +125,9 @@ WF_API wf_status wf_set_elem_materials(wf_domain *d, const int32_t *ids);
 /* ---- boundary conditions -------------------------------------------------- */
 /* Domain_d::AddBCVelNode (Domain_d.C:1057). */
 WF_API wf_status wf_add_bc_vel_node(wf_domain *d, int64_t node, int32_t dim, double val);
+/* AddBCVelNode for n entries at once, in order (node[i], dim[i], val[i]). */
+WF_API wf_status wf_add_bc_vel_nodes(wf_domain *d, int64_t n, const int64_t *node,
+                                     const int32_t *dim, const double *val);
 /* Domain_d::AddBCVelZone (Domain_d.C:432-452); *count = nodes inside. */
 WF_API wf_status wf_add_bc_vel_zone(wf_domain *d, const double start[3], const double end[3],
                                     const double vel[3], int64_t *count);
@@ -155,6 +158,20 @@ WF_API wf_status wf_set_reaction_nodes(wf_domain *d, int64_t n, const int32_t *n
  * sum of normal contact forces. */
 WF_API wf_status wf_set_contact_plane(wf_domain *d, double z0, double vz, double kpen, double mu,
                                       int64_t ncand, const int32_t *cand_nodes);
+
+/* ---- batched ensemble --------------------------------------------------------- */
+/* Declares the mesh a batch of nspec independent specimens (no counterpart in
+ * the reference, which runs one domain per process): specimen s owns elements
+ * [elem_off[s], elem_off[s+1]) and nodes [node_off[s], node_off[s+1]) and no
+ * element may reference another specimen's node. Each specimen advances with
+ * its own time step dt[s] (wf_set_dt is then not needed) and records its own
+ * reaction history over the reaction nodes it owns. All specimens step
+ * together in the same four launches. Not combinable with contact. */
+WF_API wf_status wf_set_specimens(wf_domain *d, int32_t nspec, const int64_t *elem_off,
+                                  const int64_t *node_off, const double *dt);
+/* Reaction history of one specimen: *n = steps recorded, copies min(cap, *n). */
+WF_API wf_status wf_get_specimen_reaction(wf_domain *d, int32_t spec, double *out, int64_t cap,
+                                          int64_t *n);
 
 /* ---- run ---------------------------------------------------------------------- */
 /* Preamble of SolveChungHulbert (Solver_explicit.C:120-268): uploads the

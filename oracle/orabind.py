@@ -194,8 +194,13 @@ class OracleDomain:
         lib().wfo_set_mass_mode(self.h, int(mode))
 
     def add_bcs(self, bcs):
+        """bcs: (node, dim, value) triples, or a tuple of three arrays."""
         L = lib()
-        for node, dim, val in bcs:
+        if isinstance(bcs, tuple) and len(bcs) == 3 and hasattr(bcs[0], "__len__"):
+            triples = zip(*bcs)
+        else:
+            triples = bcs
+        for node, dim, val in triples:
             self._check(L.wfo_add_bc_vel_node(self.h, int(node), int(dim), float(val)), "AddBCVelNode")
         L.wfo_allocate_bcs(self.h)
 

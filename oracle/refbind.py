@@ -186,6 +186,8 @@ class RefDomain:
 
     def add_bcs(self, bcs):
         L = lib()
+        if isinstance(bcs, tuple) and len(bcs) == 3 and hasattr(bcs[0], "__len__"):
+            bcs = list(zip(*bcs))
         for node, dim, val in bcs:
             L.wfr_add_bc_vel_node(self.h, int(node), int(dim), float(val))
         with _Silence():

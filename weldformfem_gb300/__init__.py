@@ -50,6 +50,7 @@ class WfStab(C.Structure):
 
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 _ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_lp = np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")
 _lib = None
 
 # name -> (argtypes); every function returns wf_status (int)
@@ -69,6 +70,9 @@ _SIGS = {
     "wf_set_elem_materials": [C.c_void_p, _ip],
     "wf_add_bc_vel_node": [C.c_void_p, C.c_int64, C.c_int32, C.c_double],
     "wf_add_bc_vel_zone": [C.c_void_p, _dp, _dp, _dp, C.POINTER(C.c_int64)],
+    "wf_add_bc_vel_nodes": [C.c_void_p, C.c_int64, _lp, _ip, _dp],
+    "wf_set_specimens": [C.c_void_p, C.c_int32, _lp, _lp, _dp],
+    "wf_get_specimen_reaction": [C.c_void_p, C.c_int32, _dp, C.c_int64, C.POINTER(C.c_int64)],
     "wf_allocate_bcs": [C.c_void_p],
     "wf_set_dt": [C.c_void_p, C.c_double],
     "wf_set_end_time": [C.c_void_p, C.c_double],
@@ -127,6 +131,19 @@ def lib():
     L.wf_abi_version.restype = C.c_int32
     _lib = L
     return L
+
+
+def _bc_arrays(bcs):
+    if isinstance(bcs, tuple) and len(bcs) == 3 and hasattr(bcs[0], "__len__") and \
+            not isinstance(bcs[0], tuple):
+        nodes, dims, vals = bcs
+    else:
+        arr = list(bcs)
+        nodes = [b[0] for b in arr]
+        dims = [b[1] for b in arr]
+        vals = [b[2] for b in arr]
+    return (np.ascontiguousarray(nodes, np.int64), np.ascontiguousarray(dims, np.int32),
+            np.ascontiguousarray(vals, np.float64))
 
 
 class Domain:
@@ -229,8 +246,9 @@ class Domain:
         self._call("wf_set_mass_mode", int(mode))
 
     def add_bcs(self, bcs):
-        for node, dim, val in bcs:
-            self._call("wf_add_bc_vel_node", int(node), int(dim), float(val))
+        """bcs: (node, dim, value) triples, or a tuple of three arrays."""
+        nodes, dims, vals = _bc_arrays(bcs)
+        self._call("wf_add_bc_vel_nodes", nodes.size, nodes, dims, vals)
         self._call("wf_allocate_bcs")
 
     def add_bc_vel_zone(self, start, end, vel):
@@ -250,6 +268,20 @@ class Domain:
 
     def set_dt(self, dt):
         self._call("wf_set_dt", float(dt))
+
+    def set_specimens(self, elem_off, node_off, dts):
+        """Batched ensemble: specimen s owns [elem_off[s], elem_off[s+1]) etc."""
+        eo = np.ascontiguousarray(elem_off, np.int64)
+        no = np.ascontiguousarray(node_off, np.int64)
+        dt = np.ascontiguousarray(dts, np.float64)
+        self._call("wf_set_specimens", dt.size, eo, no, dt)
+
+    def specimen_reaction(self, spec):
+        n = C.c_int64()
+        self._call("wf_get_specimen_reaction", int(spec), np.zeros(1), 0, C.byref(n))
+        out = np.zeros(max(n.value, 1))
+        self._call("wf_get_specimen_reaction", int(spec), out, n.value, C.byref(n))
+        return out[: n.value]
 
     def set_end_time(self, t):
         self._call("wf_set_end_time", float(t))

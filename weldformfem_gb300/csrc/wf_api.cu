@@ -73,6 +73,10 @@ struct wf_domain {
   int64_t phase_steps = 0;
   int64_t launches = 0;
   int64_t h2d_bytes = 0, d2h_bytes = 0;
+  // batched ensemble
+  int32_t nspec = 0;
+  std::vector<int64_t> spec_eoff, spec_noff;
+  std::vector<double> spec_dt;
 };
 
 namespace {
@@ -162,6 +166,10 @@ void reset_mesh(wf_domain *d) {
   d->cand.clear();
   d->contact = false;
   d->bcs_allocated = false;
+  d->nspec = 0;
+  d->spec_eoff.clear();
+  d->spec_noff.clear();
+  d->spec_dt.clear();
 }
 
 wf_status need_mesh(wf_domain *d) {
@@ -394,6 +402,23 @@ WF_API wf_status wf_add_bc_vel_node(wf_domain *d, int64_t node, int32_t dim, dou
   return WF_OK;
 }
 
+WF_API wf_status wf_add_bc_vel_nodes(wf_domain *d, int64_t n, const int64_t *node,
+                                     const int32_t *dim, const double *val) {
+  wf_status s = need_mesh(d);
+  if (s) return s;
+  if (n < 0 || (n > 0 && (!node || !dim || !val))) return WF_ERR_ARG;
+  for (int64_t i = 0; i < n; i++)
+    if (dim[i] < 0 || dim[i] > 2 || node[i] < 0 || node[i] >= d->nn)
+      return fail(d, WF_ERR_ARG, "entry %lld: node %lld dim %d out of range", (long long)i,
+                  (long long)node[i], dim[i]);
+  for (int64_t i = 0; i < n; i++) {
+    d->bc_nod[dim[i]].push_back(node[i]);
+    d->bc_val[dim[i]].push_back(val[i]);
+  }
+  d->bcs_allocated = false;
+  return WF_OK;
+}
+
 WF_API wf_status wf_add_bc_vel_zone(wf_domain *d, const double start[3], const double end[3],
                                     const double vel[3], int64_t *count) {
   wf_status s = need_mesh(d);
@@ -513,6 +538,56 @@ WF_API wf_status wf_set_contact_plane(wf_domain *d, double z0, double vz, double
   return WF_OK;
 }
 
+// ---- batched ensemble ------------------------------------------------------------
+WF_API wf_status wf_set_specimens(wf_domain *d, int32_t nspec, const int64_t *elem_off,
+                                  const int64_t *node_off, const double *dt) {
+  wf_status s = need_mesh(d);
+  if (s) return s;
+  if (nspec <= 0 || nspec > 65535 || !elem_off || !node_off || !dt)
+    return fail(d, WF_ERR_ARG, "need 1..65535 specimens and their offsets and time steps");
+  if (d->initialized) return fail(d, WF_ERR_STATE, "specimens must be set before init");
+  if (elem_off[0] != 0 || node_off[0] != 0 || elem_off[nspec] != d->ne || node_off[nspec] != d->nn)
+    return fail(d, WF_ERR_ARG, "specimen offsets must start at 0 and end at the mesh sizes");
+  for (int32_t k = 0; k < nspec; k++) {
+    if (elem_off[k + 1] <= elem_off[k] || node_off[k + 1] <= node_off[k])
+      return fail(d, WF_ERR_ARG, "specimen %d is empty or offsets decrease", k);
+    if (!(dt[k] > 0.0) || !std::isfinite(dt[k]))
+      return fail(d, WF_ERR_ARG, "specimen %d: time step must be positive", k);
+    for (int64_t e = elem_off[k]; e < elem_off[k + 1]; e++)
+      for (int a = 0; a < d->npe; a++) {
+        const int32_t n = d->elnod[e * d->npe + a];
+        if (n < node_off[k] || n >= node_off[k + 1])
+          return fail(d, WF_ERR_ARG, "element %lld references a node of another specimen",
+                      (long long)e);
+      }
+  }
+  d->nspec = nspec;
+  d->spec_eoff.assign(elem_off, elem_off + nspec + 1);
+  d->spec_noff.assign(node_off, node_off + nspec + 1);
+  d->spec_dt.assign(dt, dt + nspec);
+  return WF_OK;
+}
+
+WF_API wf_status wf_get_specimen_reaction(wf_domain *d, int32_t spec, double *out, int64_t cap,
+                                          int64_t *n) {
+  if (!d) return WF_ERR_ARG;
+  if (!d->initialized) return fail(d, WF_ERR_STATE, "wf_init not called");
+  if (spec < 0 || spec >= d->nspec) return fail(d, WF_ERR_ARG, "specimen %d out of range", spec);
+  CUDA_TRY(cudaSetDevice(d->device));
+  const int64_t have = d->host_step;
+  if (n) *n = have;
+  const int64_t m = std::min(cap, have);
+  if (out && m > 0) {
+    std::vector<double> all((size_t)m * d->nspec);
+    d->d2h_bytes += (int64_t)(sizeof(double) * all.size());
+    CUDA_TRY(cudaMemcpyAsync(all.data(), d->P.hist_spec, sizeof(double) * all.size(),
+                             cudaMemcpyDeviceToHost, d->stream));
+    CUDA_TRY(cudaStreamSynchronize(d->stream));
+    for (int64_t i = 0; i < m; i++) out[i] = all[(size_t)i * d->nspec + spec];
+  }
+  return WF_OK;
+}
+
 // ---- init -------------------------------------------------------------------------
 namespace {
 
@@ -583,6 +658,8 @@ WF_API wf_status wf_init(wf_domain *d) {
       if (sp[i] != 0.0)
         return fail(d, WF_ERR_UNSUPPORTED, "mixed precision supports default stabilisation only");
   }
+  if (d->nspec && d->contact)
+    return fail(d, WF_ERR_UNSUPPORTED, "contact is not supported in a batched ensemble");
   CUDA_TRY(cudaSetDevice(d->device));
   free_device(d);
   const int64_t nn = d->nn, ne = d->ne;
@@ -676,11 +753,50 @@ WF_API wf_status wf_init(wf_domain *d) {
     CUDA_TRY(upload(d, &em, d->emat));
     P.emat = em;
   }
+  // batched ensemble tables
+  if (d->nspec) {
+    const int32_t S_ = d->nspec;
+    P.nspec = S_;
+    std::vector<uint16_t> es(ne), ns(nn);
+    for (int32_t k = 0; k < S_; k++) {
+      for (int64_t e = d->spec_eoff[k]; e < d->spec_eoff[k + 1]; e++) es[e] = (uint16_t)k;
+      for (int64_t n = d->spec_noff[k]; n < d->spec_noff[k + 1]; n++) ns[n] = (uint16_t)k;
+    }
+    std::vector<SpecF> sf(S_);
+    for (int32_t k = 0; k < S_; k++) {
+      const double dt = d->spec_dt[k];
+      sf[k] = SpecF{(float)dt, (float)((0.5 - P.beta) * dt), (float)(P.beta * dt * dt),
+                    (float)(P.gamma * dt), (float)((1.0 - P.gamma) * dt), 0.f, 0.f, 0.f};
+    }
+    std::vector<int32_t> rl(d->react_nodes.begin(), d->react_nodes.end());
+    std::sort(rl.begin(), rl.end());
+    std::vector<int32_t> rloff(S_ + 1, 0);
+    for (int32_t n : rl) rloff[ns[n] + 1]++;
+    for (int32_t k = 0; k < S_; k++) rloff[k + 1] += rloff[k];
+    uint16_t *esd = nullptr, *nsd = nullptr;
+    double *sdt = nullptr;
+    SpecF *sfd = nullptr;
+    int32_t *rld = nullptr, *rlo = nullptr;
+    CUDA_TRY(upload(d, &esd, es));
+    CUDA_TRY(upload(d, &nsd, ns));
+    CUDA_TRY(upload(d, &sdt, d->spec_dt));
+    CUDA_TRY(upload(d, &sfd, sf));
+    CUDA_TRY(upload(d, &rld, rl));
+    CUDA_TRY(upload(d, &rlo, rloff));
+    P.espec = esd;
+    P.nspec_of = nsd;
+    P.spec_dt = sdt;
+    P.specf = sfd;
+    P.rlist = rld;
+    P.rl_off = rlo;
+    CUDA_TRY(dalloc(d, &P.rnode, np));
+  }
   // reaction history and step state
   d->node_grid = (d->precision == WF_MIXED) ? mix_node_grid(nn) : fp64_node_grid(nn);
   CUDA_TRY(dalloc(d, &P.partials, d->node_grid));
   d->hist_cap = 1 << 16;
   CUDA_TRY(dalloc(d, &P.hist, d->hist_cap));
+  if (d->nspec) CUDA_TRY(dalloc(d, &P.hist_spec, (size_t)d->hist_cap * d->nspec));
   P.hist_cap = d->hist_cap;
   CUDA_TRY(dalloc(d, &P.st, 1));
 
@@ -807,6 +923,7 @@ void launch_step(wf_domain *d) {
     mix_elements(P, d->M, d->mvol, d->stream);
     mix_nodes(P, d->M, d->stream, d->node_grid);
   }
+  if (P.nspec) spec_reaction(P, d->stream);
 }
 
 void launch_step_timed(wf_domain *d, cudaEvent_t *ev) {
@@ -829,6 +946,7 @@ void launch_step_timed(wf_domain *d, cudaEvent_t *ev) {
     cudaEventRecord(ev[3], d->stream);
     mix_nodes(P, d->M, d->stream, d->node_grid);
   }
+  if (P.nspec) spec_reaction(P, d->stream);
   cudaEventRecord(ev[4], d->stream);
 }
 
@@ -889,6 +1007,13 @@ WF_API wf_status wf_run(wf_domain *d, int64_t nsteps) {
     CUDA_TRY(cudaMemcpyAsync(nh, d->P.hist, sizeof(double) * d->hist_cap, cudaMemcpyDeviceToDevice,
                              d->stream));
     d->P.hist = nh;
+    if (d->nspec) {
+      double *ns = nullptr;
+      CUDA_TRY(dalloc(d, &ns, (size_t)cap * d->nspec));
+      CUDA_TRY(cudaMemcpyAsync(ns, d->P.hist_spec, sizeof(double) * d->hist_cap * d->nspec,
+                               cudaMemcpyDeviceToDevice, d->stream));
+      d->P.hist_spec = ns;
+    }
     d->P.hist_cap = cap;
     d->hist_cap = cap;
     if (d->graph) {
@@ -896,7 +1021,7 @@ WF_API wf_status wf_run(wf_domain *d, int64_t nsteps) {
       d->graph = nullptr;
     }
   }
-  if (!(d->dt > 0.0)) return fail(d, WF_ERR_STATE, "time step not set (SetDT)");
+  if (!(d->dt > 0.0) && !d->nspec) return fail(d, WF_ERR_STATE, "time step not set (SetDT)");
   set_dt_constants(d->P, d->dt);
   if (d->precision == WF_FP64)
     fp64_predict(d->P, d->S, d->stream);
@@ -923,7 +1048,7 @@ WF_API wf_status wf_run(wf_domain *d, int64_t nsteps) {
     }
     left = 0;
   }
-  d->launches += 4 * nsteps;
+  d->launches += (d->nspec ? 5 : 4) * nsteps;
   if (left >= kGraphSteps) {
     wf_status s = ensure_graph(d);
     if (s) return s;
@@ -943,6 +1068,7 @@ WF_API wf_status wf_run(wf_domain *d, int64_t nsteps) {
 WF_API wf_status wf_solve(wf_domain *d, int64_t *nsteps) {
   if (!d) return WF_ERR_ARG;
   if (!d->initialized) return fail(d, WF_ERR_STATE, "wf_init not called");
+  if (d->nspec) return fail(d, WF_ERR_UNSUPPORTED, "a batched ensemble runs with wf_run");
   // count the iterations of `while (Time < end_t) { ...; Time += dt; }`
   int64_t n = 0;
   double t = d->host_time;

@@ -299,7 +299,7 @@ __global__ void __launch_bounds__(kElemThreads) k_fp64_elements(StepParams P, Fp
   // addends that multiply an exact zero of the spin or of the identity's
   // off-diagonal are dropped, which leaves every value unchanged (only the
   // sign of an exact zero could differ) and saves FP64 instructions.
-  const double dt = P.dt;
+  const double dt = P.espec ? P.spec_dt[P.espec[e]] : P.dt;
   double t0 = S.tau[e], t1 = S.tau[ne + e], t2 = S.tau[2 * ne + e];
   double t3 = S.tau[3 * ne + e], t4 = S.tau[4 * ne + e], t5 = S.tau[5 * ne + e];
   {
@@ -534,10 +534,15 @@ __global__ void __launch_bounds__(kNodeThreads) k_fp64_nodes(StepParams P, Fp64S
       S.cf[np + n] = cf[1];
       S.cf[2 * np + n] = cf[2];
     }
-    if (!P.contact && (fl & NF_REACTION)) r = fi[P.react_dim];
+    if (!P.contact && (fl & NF_REACTION)) {
+      if (P.rnode)
+        P.rnode[n] = fi[P.react_dim];  // summed per specimen by the reaction kernel
+      else
+        r = fi[P.react_dim];
+    }
     const uint32_t code = P.bc[n];
     const double *bv = &P.bcval[3 * (code >> 3)];
-    const double dt = P.dt;
+    const double dt = P.nspec_of ? P.spec_dt[P.nspec_of[n]] : P.dt;
 #pragma unroll
     for (int k = 0; k < 3; k++) {
       double a = (0.0 - fi[k]) / mass;
@@ -592,7 +597,8 @@ __global__ void k_fp64_predict(StepParams P, Fp64State S) {
   const uint32_t code = P.bc[n];
   const double *bv = &P.bcval[3 * (code >> 3)];
   for (int k = 0; k < 3; k++) {
-    double v = S.v[k * P.np + n] + (1.0 - P.gamma) * P.dt * S.pa[k * P.np + n];
+    const double dt = P.nspec_of ? P.spec_dt[P.nspec_of[n]] : P.dt;
+    double v = S.v[k * P.np + n] + (1.0 - P.gamma) * dt * S.pa[k * P.np + n];
     if (code & (1u << k)) v = bv[k];
     S.vp[k * P.np + n] = v;
   }

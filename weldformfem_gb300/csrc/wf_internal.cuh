@@ -25,6 +25,11 @@ struct MatF {
   int32_t pad;
 };
 
+// FP32 time-step constants of one specimen of a batched ensemble.
+struct SpecF {
+  float dt, cu_pred, cu_corr, cv_corr, cv_pred, pad0, pad1, pad2;
+};
+
 // Device-resident scalars advanced by the node kernel of every step.
 struct StepState {
   double time;        // Time of the reference loop (start of the current step)
@@ -76,6 +81,16 @@ struct StepParams {
   float f_cv_pred;        // (1 - gamma) * dt
   float f_hg_coef, f_c_k, f_c_mu;
   const struct MatF *matf;
+  // batched ensemble (all null / zero for a single domain)
+  int32_t nspec;
+  const uint16_t *espec;  // [ne] specimen of each element
+  const uint16_t *nspec_of;  // [nn] specimen of each node
+  const double *spec_dt;  // [nspec]
+  const SpecF *specf;     // [nspec]
+  double *rnode;          // [nn] reaction contribution of each reaction node
+  const int32_t *rlist;   // reaction nodes grouped by specimen
+  const int32_t *rl_off;  // [nspec + 1]
+  double *hist_spec;      // [hist_cap][nspec]
   // reduction scratch
   double *partials;       // [grid of the node kernel]
   double *hist;           // [hist_cap]
@@ -129,6 +144,8 @@ void mix_export(const StepParams &P, const MixState &M, const Fp64State &S, cons
 int mix_node_grid(int64_t nn);
 
 // ---- reductions (wf_reduce.cu) ---------------------------------------------
+// Per-specimen reaction sums of the step just completed (batched ensemble).
+void spec_reaction(const StepParams &P, cudaStream_t st);
 // Minimum element edge length over the mesh (exact: min is order-free).
 void min_edge_length(const int32_t *elnod, const double *x, int64_t np, int64_t ne, int npe,
                      double *out_dev, cudaStream_t st);

@@ -155,7 +155,16 @@ __global__ void __launch_bounds__(kNodeThreads) k_mix_nodal(StepParams P, MixSta
   if (n >= P.nn) return;
   const int32_t b = __ldg(&P.off[n]), c = __ldg(&P.off[n + 1]) - b;
   float s = 0.0f;
-  for (int32_t k = 0; k < c; k++) s += __ldg(&vol[__ldg(&P.slot[b + k]) / NPE]);
+  for (int32_t k0 = 0; k0 < c; k0 += 8) {
+    int32_t sl[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) sl[j] = (k0 + j < c) ? __ldg(&P.slot[b + k0 + j]) : -1;
+    float g[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) g[j] = (sl[j] >= 0) ? __ldg(&vol[sl[j] / NPE]) : 0.0f;
+#pragma unroll
+    for (int j = 0; j < 8; j++) s += g[j];
+  }
   const float2 nc = __ldg(&M.nc[n]);
   M.jr[n] = s * nc.x;
   float mass;
@@ -272,7 +281,7 @@ __global__ void __launch_bounds__(kElemThreads, 6) k_mix_elements(StepParams P, 
   // (Tensor3.C:290-303) written out for a symmetric tau and the spin W
   // (antisymmetric, zero diagonal): only the six stored components are
   // formed, terms that multiply a zero of W are dropped.
-  const float dt = P.f_dt;
+  const float dt = P.espec ? P.specf[P.espec[e]].dt : P.f_dt;
   float t0 = M.tau[e], t1 = M.tau[ne + e], t2 = M.tau[2 * ne + e];
   float t3 = M.tau[3 * ne + e], t4 = M.tau[4 * ne + e], t5 = M.tau[5 * ne + e];
   {
@@ -362,13 +371,27 @@ __global__ void __launch_bounds__(kElemThreads, 6) k_mix_elements(StepParams P, 
 // ---------------------------------------------------------------------------
 // Block sum in a fixed order (shuffle tree per warp, warps in index order);
 // warps with no nonzero value skip their FP64 shuffles. Valid in thread 0.
-__device__ __forceinline__ double block_sum_sparse(double v, bool nz, double *sh) {
-  const unsigned any = __ballot_sync(0xffffffffu, nz);
+__device__ __forceinline__ double block_sum_sparse(float vf, double *sh) {
+  const unsigned any = __ballot_sync(0xffffffffu, vf != 0.0f);
+  double v = 0.0;
   if (any) {
+    v = (double)vf;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
   }
-  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = any ? v : 0.0;
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (threadIdx.x == 0)
+    for (int i = 0; i < (int)(blockDim.x >> 5); i++) t += sh[i];
+  return t;
+}
+
+// Fixed-order block sum of doubles (all warps reduce). Valid in thread 0.
+__device__ __forceinline__ double block_sum_dense(double v, double *sh) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
   __syncthreads();
   double t = 0.0;
   if (threadIdx.x == 0)
@@ -377,7 +400,7 @@ __device__ __forceinline__ double block_sum_sparse(double v, bool nz, double *sh
 }
 
 template <int NPE>
-__global__ void __launch_bounds__(kNodeThreads) k_mix_nodes(StepParams P, MixState M) {
+__global__ void __launch_bounds__(kNodeThreads, 6) k_mix_nodes(StepParams P, MixState M) {
   __shared__ double sh[kNodeThreads / 32];
   __shared__ bool am_last;
   const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -437,7 +460,19 @@ __global__ void __launch_bounds__(kNodeThreads) k_mix_nodes(StepParams P, MixSta
       cf[2] = M.cf[2 * np + n];
       r = fabsf(cf[2]);
     }
-    if (!P.contact && (fl & NF_REACTION)) r = fi[P.react_dim];
+    if (!P.contact && (fl & NF_REACTION)) {
+      if (P.rnode)
+        P.rnode[n] = fi[P.react_dim];  // summed per specimen by the reaction kernel
+      else
+        r = fi[P.react_dim];
+    }
+    float c_dt = P.f_dt, c_cu_pred = P.f_cu_pred, c_cu_corr = P.f_cu_corr;
+    float c_cv_corr = P.f_cv_corr, c_cv_pred = P.f_cv_pred;
+    if (P.nspec_of) {
+      const SpecF sf = P.specf[P.nspec_of[n]];
+      c_dt = sf.dt; c_cu_pred = sf.cu_pred; c_cu_corr = sf.cu_corr;
+      c_cv_corr = sf.cv_corr; c_cv_pred = sf.cv_pred;
+    }
     const uint32_t code = P.bc[n];
     const double *bvd = &P.bcval[3 * (code >> 3)];
 #pragma unroll
@@ -446,12 +481,12 @@ __global__ void __launch_bounds__(kNodeThreads) k_mix_nodes(StepParams P, MixSta
       float a = (cf[k] - fi[k]) * inv_m;
       if (fixed) a = 0.f;
       a = P.f_fcorr * (a - P.f_alpha * pa[k]);
-      float v = vp[k] + P.f_cv_corr * a;
+      float v = vp[k] + c_cv_corr * a;
       const float bv = fixed ? (float)__ldg(&bvd[k]) : 0.f;
       if (fixed) v = bv;
-      const float udt = P.f_dt * (vold[k] + P.f_cu_pred * pa[k]) + P.f_cu_corr * a;
+      const float udt = c_dt * (vold[k] + c_cu_pred * pa[k]) + c_cu_corr * a;
       x[k] = pair_add(x[k], udt);
-      float vnext = v + P.f_cv_pred * a;
+      float vnext = v + c_cv_pred * a;
       if (fixed) vnext = bv;
       M.xh[k * np + n] = x[k];
       M.v[k * np + n] = v;
@@ -461,7 +496,7 @@ __global__ void __launch_bounds__(kNodeThreads) k_mix_nodes(StepParams P, MixSta
   }
   // reaction: only warps holding a contribution reduce (FP64, fixed order);
   // the last block to finish sums all block partials with the whole block.
-  const double bs = block_sum_sparse((double)r, r != 0.0f, sh);
+  const double bs = block_sum_sparse(r, sh);
   if (threadIdx.x == 0) {
     P.partials[blockIdx.x] = bs;
     __threadfence();
@@ -474,7 +509,7 @@ __global__ void __launch_bounds__(kNodeThreads) k_mix_nodes(StepParams P, MixSta
     double t = 0.0;
     for (unsigned i = threadIdx.x; i < gridDim.x; i += blockDim.x)
       t += ((volatile double *)P.partials)[i];
-    const double tot = block_sum_sparse(t, t != 0.0, sh);
+    const double tot = block_sum_dense(t, sh);
     if (threadIdx.x == 0) {
       const long long s = P.st->step;
       if (s < P.hist_cap) P.hist[s] = tot;
@@ -490,7 +525,8 @@ __global__ void k_mix_predict(StepParams P, MixState M) {
   if (n >= P.nn) return;
   const uint32_t code = P.bc[n];
   for (int k = 0; k < 3; k++) {
-    float v = M.v[k * P.np + n] + P.f_cv_pred * M.pa[k * P.np + n];
+    const float cv = P.nspec_of ? P.specf[P.nspec_of[n]].cv_pred : P.f_cv_pred;
+    float v = M.v[k * P.np + n] + cv * M.pa[k * P.np + n];
     if ((code >> k) & 1u) v = (float)P.bcval[3 * (code >> 3) + k];
     M.vp[k * P.np + n] = v;
   }

@@ -45,7 +45,30 @@ __global__ void k_min_edge(const int32_t *elnod, const double *x, int64_t np, in
 
 __global__ void k_set(unsigned long long *p, unsigned long long v) { *p = v; }
 
+// One block per specimen: sum of its reaction nodes' contributions in list
+// order (each thread a fixed strided subset, then a fixed tree).
+__global__ void k_spec_reaction(StepParams P) {
+  __shared__ double sh[4];
+  const int s = blockIdx.x;
+  const int32_t b = P.rl_off[s], e = P.rl_off[s + 1];
+  double t = 0.0;
+  for (int32_t i = b + threadIdx.x; i < e; i += blockDim.x) t += P.rnode[P.rlist[i]];
+  for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = t;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double tot = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) tot += sh[w];
+    const long long step = P.st->step - 1;  // advanced by this step's node kernel
+    if (step >= 0 && step < P.hist_cap) P.hist_spec[step * P.nspec + s] = tot;
+  }
+}
+
 }  // namespace
+
+void spec_reaction(const StepParams &P, cudaStream_t st) {
+  k_spec_reaction<<<P.nspec, 128, 0, st>>>(P);
+}
 
 void min_edge_length(const int32_t *elnod, const double *x, int64_t np, int64_t ne, int npe,
                      double *out_dev, cudaStream_t st) {

@@ -174,29 +174,28 @@ class Case:
         return self.dt_factor * hmin / np.sqrt(m["E"] / m["rho"])
 
     def bcs(self, x0=None):
-        """Velocity BC list (node, dof, value) in node order."""
-        if x0 is None:
-            x0 = box_coords(self.L, self.r)
+        """Velocity BCs as three arrays (node, dof, value), in node order and,
+        per node, x-symmetry, y-symmetry, z-symmetry, top velocity."""
         nx, ny, nz = (n + 1 for n in self.nel)
-        idx = np.arange(x0.shape[0])
+        idx = np.arange(nx * ny * nz, dtype=np.int64)
         i, j, k = idx % nx, (idx // nx) % ny, idx // (nx * ny)
-        out = []
         if self.bc == "sym_top":
-            for n in idx:
-                if i[n] == 0:
-                    out.append((int(n), 0, 0.0))
-                if j[n] == 0:
-                    out.append((int(n), 1, 0.0))
-                if k[n] == 0:
-                    out.append((int(n), 2, 0.0))
-                if k[n] == nz - 1:
-                    out.append((int(n), 2, float(self.top_vz)))
+            conds = [(i == 0, 0, 0.0), (j == 0, 1, 0.0), (k == 0, 2, 0.0),
+                     (k == nz - 1, 2, float(self.top_vz))]
         elif self.bc == "bottom_z":
-            for n in idx[k == 0]:
-                out.append((int(n), 2, 0.0))
+            conds = [(k == 0, 2, 0.0)]
         else:
             raise ValueError(self.bc)
-        return out
+        nodes, dims, vals, order = [], [], [], []
+        for rank, (mask, dof, val) in enumerate(conds):
+            sel = idx[mask]
+            nodes.append(sel)
+            dims.append(np.full(sel.size, dof, np.int32))
+            vals.append(np.full(sel.size, val))
+            order.append(sel * 4 + rank)
+        perm = np.argsort(np.concatenate(order), kind="stable")
+        return (np.concatenate(nodes)[perm], np.concatenate(dims)[perm],
+                np.concatenate(vals)[perm])
 
     def top_nodes(self) -> np.ndarray:
         nx, ny, nz = (n + 1 for n in self.nel)
@@ -285,3 +284,84 @@ def config(cid: int, steps: Optional[int] = None, scale: Optional[tuple] = None)
     if steps is not None:
         c.steps = steps
     return c
+
+
+@dataclasses.dataclass
+class Batch:
+    """An ensemble of independent specimens run as one batched domain."""
+    name: str
+    cases: list
+    hg: float = 0.1
+
+    def offsets(self):
+        eoff = np.zeros(len(self.cases) + 1, np.int64)
+        noff = np.zeros(len(self.cases) + 1, np.int64)
+        for s, c in enumerate(self.cases):
+            eoff[s + 1] = eoff[s] + c.n_elem
+            noff[s + 1] = noff[s] + c.n_node
+        return eoff, noff
+
+    @property
+    def n_elem(self):
+        return int(sum(c.n_elem for c in self.cases))
+
+    @property
+    def n_node(self):
+        return int(sum(c.n_node for c in self.cases))
+
+    def assemble(self):
+        """Concatenated mesh, per-element specimen ids, BCs and reaction nodes."""
+        eoff, noff = self.offsets()
+        xs, els, bn, bd, bv, tops = [], [], [], [], [], []
+        for s, c in enumerate(self.cases):
+            xs.append(c.coords())
+            els.append(c.elnod() + np.int32(noff[s]))
+            nodes, dims, vals = c.bcs()
+            bn.append(nodes + noff[s])
+            bd.append(dims)
+            bv.append(vals)
+            tops.append(c.top_nodes() + np.int32(noff[s]))
+        x = np.concatenate(xs)
+        el = np.concatenate(els)
+        emat = np.repeat(np.arange(len(self.cases), dtype=np.int32),
+                         [c.n_elem for c in self.cases])
+        bcs = (np.concatenate(bn), np.concatenate(bd), np.concatenate(bv))
+        return x, el, emat, bcs, np.concatenate(tops), eoff, noff
+
+    def dts(self):
+        return np.array([c.time_step() for c in self.cases])
+
+
+def apply_batch(dom, batch: Batch):
+    """Sets up a batched domain (one specimen per material); returns dt per specimen."""
+    x, el, emat, bcs, tops, eoff, noff = batch.assemble()
+    dom.set_mesh(x, el)
+    dom.set_materials([c.materials[0] for c in batch.cases], emat)
+    dom.add_bcs(bcs)
+    dom.set_hourglass(batch.hg)
+    dom.set_reaction_nodes(tops, 2)
+    dts = batch.dts()
+    dom.set_specimens(eoff, noff, dts)
+    return dts
+
+
+def ensemble(n_spec: int = 1024, nmin: int = 6, nmax: int = 40, side: float = 0.01,
+             seed: int = SEED_BASE + 3, steps: int = 2000) -> Batch:
+    """Config 3: n_spec cubes of side `side`, n ~ U{nmin..nmax} elements per edge,
+    E ~ U[70, 210] GPa, sigma_y0 ~ U[200, 500] MPa, H ~ U[0.2, 2] GPa, top velocity
+    ~ U[0.5, 5] m/s, nu = 0.3, rho = 7850; symmetry + top-velocity BCs."""
+    z = splitmix64(seed, 5 * n_spec).reshape(n_spec, 5)
+    u01 = (z >> np.uint64(11)).astype(np.float64) * (2.0 ** -53)
+    cases = []
+    for s in range(n_spec):
+        n = nmin + int(z[s, 0] % np.uint64(nmax - nmin + 1))
+        r = side / (2.0 * n)
+        L = ((n + 0.25) * 2.0 * r,) * 3      # truncates to exactly n cells per edge
+        mat = dict(model=0, E=70e9 + 140e9 * u01[s, 1], nu=0.3, rho=7850.0,
+                   sy0=200e6 + 300e6 * u01[s, 2], H=0.2e9 + 1.8e9 * u01[s, 3])
+        c = Case(f"C3 specimen {s} n={n}", L=L, r=r, hg=0.1, steps=steps,
+                 top_vz=-(0.5 + 4.5 * u01[s, 4]))
+        c.materials = [mat]
+        assert c.nel == (n, n, n)
+        cases.append(c)
+    return Batch(f"C3 ensemble {n_spec} cubes n~U{{{nmin}..{nmax}}}", cases)
