@@ -195,6 +195,8 @@ def run_ours(args):
     ms_phase, nph = dm.phase_times()
     dm.set_phase_timing(False)
     ms_phase = ms_phase / max(nph, 1)
+    tuned = {p: dict(zip(("block", "items_per_thread"), dm.launch_config(i)[:2]))
+             for i, p in enumerate(PHASES[:3])}
 
     # ---- FP64 plain: same steps from the same initial state ----------------------
     df = build_domain(wf, case, wf.WF_FP64, x, device)
@@ -290,6 +292,7 @@ def run_ours(args):
                     "includes": "mesh + BC upload, init, device CFL dt, K steps, "
                                 "displacement + reaction readback"},
             "gpu_launches": int(launches),
+            "autotuned_launch": tuned,
             "roofline": roof,
             "cpu_baseline": cpu,
             "clocks": clk,

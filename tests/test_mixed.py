@@ -95,3 +95,22 @@ def test_mixed_rejects_unsupported_options():
     with pytest.raises(wf.WfError) as e:
         d.init()
     assert e.value.status == 5
+
+
+def test_autotuned_and_default_launch_shapes_agree_bitwise():
+    """The autotuner only changes launch shapes; results are identical."""
+    case = W.config(2, scale=(20, 18, 10))
+    outs = []
+    for tune in (True, False):
+        d = wf.Domain(wf.WF_MIXED)
+        W.apply(d, case)
+        d.set_autotune(tune)
+        d.init()
+        d.run(64)
+        outs.append((d.node_vec("x"), d.reaction(), d.elem_scalar("pl_strain")))
+        if tune:
+            for phase in range(3):
+                bs, ept, ms = d.launch_config(phase)
+                assert bs in (64, 128, 256) and ept in (1, 2, 4) and ms > 0.0
+    for a, b in zip(outs[0], outs[1]):
+        np.testing.assert_array_equal(a, b)

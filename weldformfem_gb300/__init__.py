@@ -104,6 +104,9 @@ _SIGS = {
     "wf_get_phase_times": [C.c_void_p, _dp, C.POINTER(C.c_int64), C.c_int32],
     "wf_get_launch_count": [C.c_void_p, C.POINTER(C.c_int64)],
     "wf_get_stream": [C.c_void_p, C.POINTER(C.c_void_p)],
+    "wf_set_autotune": [C.c_void_p, C.c_int32],
+    "wf_get_launch_config": [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                             C.POINTER(C.c_double)],
     "wf_get_transfer_bytes": [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)],
     # allocation-free nodal volumes: device pointers in, device pointer out
     "wf_nodal_volumes_noalloc": [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_int32,
@@ -325,6 +328,15 @@ class Domain:
         n = C.c_int64()
         self._call("wf_get_phase_times", ms, C.byref(n), int(bool(reset)))
         return ms, n.value
+
+    def set_autotune(self, on=True):
+        self._call("wf_set_autotune", int(bool(on)))
+
+    def launch_config(self, phase):
+        """(block size, items per thread, trial ms) chosen for phase 0/1/2."""
+        b, e, ms = C.c_int32(), C.c_int32(), C.c_double()
+        self._call("wf_get_launch_config", int(phase), C.byref(b), C.byref(e), C.byref(ms))
+        return b.value, e.value, ms.value
 
     def stream_handle(self):
         """The domain's cudaStream_t as an integer (for torch.cuda.ExternalStream)."""

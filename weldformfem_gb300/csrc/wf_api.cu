@@ -73,6 +73,10 @@ struct wf_domain {
   int64_t phase_steps = 0;
   int64_t launches = 0;
   int64_t h2d_bytes = 0, d2h_bytes = 0;
+  // launch shapes of the tunable mixed kernels (geometry, nodal, elements)
+  bool autotune = true;
+  LaunchCfg cfg[3] = {LaunchCfg{128, 1}, LaunchCfg{256, 1}, LaunchCfg{128, 1}};
+  double cfg_ms[3] = {0, 0, 0};
   // batched ensemble
   int32_t nspec = 0;
   std::vector<int64_t> spec_eoff, spec_noff;
@@ -645,6 +649,80 @@ std::vector<T> soa3(const std::vector<double> &aos, int64_t nn, int64_t np) {
 
 }  // namespace
 
+namespace {
+
+// Times each candidate launch shape of the three tunable mixed kernels on the
+// domain's data and keeps the fastest. The element kernel advances the
+// deviatoric stress and plastic strain, the nodal kernel the contact slip:
+// both are saved before the trials and restored after.
+wf_status autotune_launches(wf_domain *d) {
+  const StepParams &P = d->P;
+  MixState &M = d->M;
+  const int64_t ne = d->ne, np = d->np;
+  std::vector<float> tau(6 * ne), pls(ne), ut(2 * np), cf(3 * np);
+  CUDA_TRY(cudaMemcpyAsync(tau.data(), M.tau, 4 * tau.size(), cudaMemcpyDeviceToHost, d->stream));
+  CUDA_TRY(cudaMemcpyAsync(pls.data(), M.pls, 4 * pls.size(), cudaMemcpyDeviceToHost, d->stream));
+  CUDA_TRY(cudaMemcpyAsync(ut.data(), M.ut, 4 * ut.size(), cudaMemcpyDeviceToHost, d->stream));
+  CUDA_TRY(cudaMemcpyAsync(cf.data(), M.cf, 4 * cf.size(), cudaMemcpyDeviceToHost, d->stream));
+  cudaEvent_t a, b;
+  CUDA_TRY(cudaEventCreate(&a));
+  CUDA_TRY(cudaEventCreate(&b));
+  const int sizes[3] = {64, 128, 256}, epts[3] = {1, 2, 4};
+  for (int phase = 0; phase < 3; phase++) {
+    double best = 1e300;
+    LaunchCfg pick = d->cfg[phase];
+    for (int bs : sizes)
+      for (int ept : epts) {
+        const LaunchCfg c{bs, ept};
+        auto launch = [&]() {
+          if (phase == 0) mix_geometry(P, M, d->mvol, d->stream, c);
+          else if (phase == 1) mix_nodal(P, M, d->mvol, d->stream, c);
+          else mix_elements(P, M, d->mvol, d->stream, c);
+        };
+        launch();  // warm-up
+        cudaEventRecord(a, d->stream);
+        for (int r = 0; r < 3; r++) launch();
+        cudaEventRecord(b, d->stream);
+        CUDA_TRY(cudaEventSynchronize(b));
+        CUDA_TRY(cudaGetLastError());
+        float ms = 0.f;
+        CUDA_TRY(cudaEventElapsedTime(&ms, a, b));
+        if (ms / 3.0 < best) {
+          best = ms / 3.0;
+          pick = c;
+        }
+      }
+    d->cfg[phase] = pick;
+    d->cfg_ms[phase] = best;
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  CUDA_TRY(cudaMemcpyAsync(M.tau, tau.data(), 4 * tau.size(), cudaMemcpyHostToDevice, d->stream));
+  CUDA_TRY(cudaMemcpyAsync(M.pls, pls.data(), 4 * pls.size(), cudaMemcpyHostToDevice, d->stream));
+  CUDA_TRY(cudaMemcpyAsync(M.ut, ut.data(), 4 * ut.size(), cudaMemcpyHostToDevice, d->stream));
+  CUDA_TRY(cudaMemcpyAsync(M.cf, cf.data(), 4 * cf.size(), cudaMemcpyHostToDevice, d->stream));
+  CUDA_TRY(cudaStreamSynchronize(d->stream));
+  return WF_OK;
+}
+
+}  // namespace
+
+WF_API wf_status wf_set_autotune(wf_domain *d, int32_t on) {
+  if (!d) return WF_ERR_ARG;
+  if (d->initialized) return fail(d, WF_ERR_STATE, "autotuning is chosen before init");
+  d->autotune = on != 0;
+  return WF_OK;
+}
+
+WF_API wf_status wf_get_launch_config(const wf_domain *d, int32_t phase, int32_t *block,
+                                      int32_t *items_per_thread, double *ms) {
+  if (!d || phase < 0 || phase > 2) return WF_ERR_ARG;
+  if (block) *block = d->cfg[phase].bs;
+  if (items_per_thread) *items_per_thread = d->cfg[phase].ept;
+  if (ms) *ms = d->cfg_ms[phase];
+  return WF_OK;
+}
+
 WF_API wf_status wf_init(wf_domain *d) {
   wf_status s = need_mesh(d);
   if (s) return s;
@@ -898,6 +976,10 @@ WF_API wf_status wf_init(wf_domain *d) {
     mix_init(P, M, S, d->stream);
     CUDA_TRY(cudaGetLastError());
     d->mix_valid_fp64 = true;
+    if (d->autotune) {
+      wf_status ts = autotune_launches(d);
+      if (ts) return ts;
+    }
   }
   CUDA_TRY(cudaStreamSynchronize(d->stream));
   d->initialized = true;
@@ -918,9 +1000,9 @@ void launch_step(wf_domain *d) {
     fp64_elements(P, d->S, d->stream);
     fp64_nodes(P, d->S, d->stream, d->node_grid);
   } else {
-    mix_geometry(P, d->M, d->mvol, d->stream);
-    mix_nodal(P, d->M, d->mvol, d->stream);
-    mix_elements(P, d->M, d->mvol, d->stream);
+    mix_geometry(P, d->M, d->mvol, d->stream, d->cfg[0]);
+    mix_nodal(P, d->M, d->mvol, d->stream, d->cfg[1]);
+    mix_elements(P, d->M, d->mvol, d->stream, d->cfg[2]);
     mix_nodes(P, d->M, d->stream, d->node_grid);
   }
   if (P.nspec) spec_reaction(P, d->stream);
@@ -938,11 +1020,11 @@ void launch_step_timed(wf_domain *d, cudaEvent_t *ev) {
     cudaEventRecord(ev[3], d->stream);
     fp64_nodes(P, d->S, d->stream, d->node_grid);
   } else {
-    mix_geometry(P, d->M, d->mvol, d->stream);
+    mix_geometry(P, d->M, d->mvol, d->stream, d->cfg[0]);
     cudaEventRecord(ev[1], d->stream);
-    mix_nodal(P, d->M, d->mvol, d->stream);
+    mix_nodal(P, d->M, d->mvol, d->stream, d->cfg[1]);
     cudaEventRecord(ev[2], d->stream);
-    mix_elements(P, d->M, d->mvol, d->stream);
+    mix_elements(P, d->M, d->mvol, d->stream, d->cfg[2]);
     cudaEventRecord(ev[3], d->stream);
     mix_nodes(P, d->M, d->stream, d->node_grid);
   }

@@ -132,11 +132,21 @@ void fp64_predict(const StepParams &P, const Fp64State &S, cudaStream_t st);
 void fp64_density(const StepParams &P, const Fp64State &S, const double *rho0, cudaStream_t st);
 int fp64_node_grid(int64_t nn);
 
+// Launch shape of a tunable kernel: block size and items per thread
+// (grid-stride loop; grid = ceil(n / (bs * ept))).
+struct LaunchCfg {
+  int bs = 128;
+  int ept = 1;
+};
+
 // ---- Mixed launchers (wf_mixed.cu) ----------------------------------------
 void mix_init(const StepParams &P, const MixState &M, const Fp64State &S, cudaStream_t st);
-void mix_geometry(const StepParams &P, const MixState &M, float *vol, cudaStream_t st);
-void mix_nodal(const StepParams &P, const MixState &M, const float *vol, cudaStream_t st);
-void mix_elements(const StepParams &P, const MixState &M, const float *vol, cudaStream_t st);
+void mix_geometry(const StepParams &P, const MixState &M, float *vol, cudaStream_t st,
+                  LaunchCfg c);
+void mix_nodal(const StepParams &P, const MixState &M, const float *vol, cudaStream_t st,
+               LaunchCfg c);
+void mix_elements(const StepParams &P, const MixState &M, const float *vol, cudaStream_t st,
+                  LaunchCfg c);
 void mix_nodes(const StepParams &P, const MixState &M, cudaStream_t st, int node_grid);
 void mix_predict(const StepParams &P, const MixState &M, cudaStream_t st);
 void mix_export(const StepParams &P, const MixState &M, const Fp64State &S, const float *vol,

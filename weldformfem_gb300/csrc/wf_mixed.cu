@@ -133,10 +133,8 @@ __device__ __forceinline__ void shape_derivs_f(const float J[3][3], float dH[3][
 
 // ---------------------------------------------------------------------------
 template <int NPE>
-__global__ void __launch_bounds__(kElemThreads) k_mix_geometry(StepParams P, MixState M,
-                                                           float *vol) {
-  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= P.ne) return;
+__device__ __forceinline__ void geometry_one(const StepParams &P, const MixState &M, float *vol,
+                                             int64_t e) {
   float r[NPE][3];
   int32_t nid[NPE];
   rel_coords<NPE>(P, M, e, r, nid);
@@ -145,14 +143,20 @@ __global__ void __launch_bounds__(kElemThreads) k_mix_geometry(StepParams P, Mix
   vol[e] = det3f(J) * weightf<NPE>();
 }
 
+// Launch shapes are chosen at run time by the autotuner (wf_api.cu): block
+// size BS and a grid-stride loop (several elements per thread).
+template <int NPE, int BS>
+__global__ void __launch_bounds__(BS) k_mix_geometry(StepParams P, MixState M, float *vol) {
+  for (int64_t e = (int64_t)blockIdx.x * BS + threadIdx.x; e < P.ne; e += (int64_t)gridDim.x * BS)
+    geometry_one<NPE>(P, M, vol, e);
+}
+
 // Nodal volumes -> J ratio and lumped mass; for contact candidates also the
 // rigid-plane contact force (it needs only x, the predicted velocity and the
 // step's mass, all final here, so it is computed before the element phase).
 template <int NPE>
-__global__ void __launch_bounds__(kNodeThreads) k_mix_nodal(StepParams P, MixState M,
-                                                        const float *vol) {
-  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (n >= P.nn) return;
+__device__ __forceinline__ void nodal_one(const StepParams &P, const MixState &M,
+                                          const float *vol, int64_t n) {
   const int32_t b = __ldg(&P.off[n]), c = __ldg(&P.off[n + 1]) - b;
   float s = 0.0f;
   for (int32_t k0 = 0; k0 < c; k0 += 8) {
@@ -213,10 +217,14 @@ __global__ void __launch_bounds__(kNodeThreads) k_mix_nodal(StepParams P, MixSta
   }
 }
 
+template <int NPE, int BS>
+__global__ void __launch_bounds__(BS) k_mix_nodal(StepParams P, MixState M, const float *vol) {
+  for (int64_t n = (int64_t)blockIdx.x * BS + threadIdx.x; n < P.nn; n += (int64_t)gridDim.x * BS)
+    nodal_one<NPE>(P, M, vol, n);
+}
+
 template <int NPE>
-__global__ void __launch_bounds__(kElemThreads, 6) k_mix_elements(StepParams P, MixState M) {
-  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= P.ne) return;
+__device__ __forceinline__ void element_one(const StepParams &P, const MixState &M, int64_t e) {
   const int64_t ne = P.ne;
   int32_t nid[NPE];
   float dH[3][NPE];
@@ -366,6 +374,16 @@ __global__ void __launch_bounds__(kElemThreads, 6) k_mix_elements(StepParams P, 
   // SoA by (local node, component): fe[(a * 3 + k) * ne + e]
 #pragma unroll
   for (int q = 0; q < NPE * 3; q++) M.fe[q * ne + e] = out[q];
+}
+
+// Registers per thread stay <= 80 (no spills) at 768 resident threads per SM.
+constexpr int elem_min_blocks(int bs) { return 768 / bs; }
+
+template <int NPE, int BS>
+__global__ void __launch_bounds__(BS, elem_min_blocks(BS)) k_mix_elements(StepParams P,
+                                                                          MixState M) {
+  for (int64_t e = (int64_t)blockIdx.x * BS + threadIdx.x; e < P.ne; e += (int64_t)gridDim.x * BS)
+    element_one<NPE>(P, M, e);
 }
 
 // ---------------------------------------------------------------------------
@@ -610,25 +628,58 @@ void mix_init(const StepParams &P, const MixState &M, const Fp64State &S, cudaSt
     k_mix_init_nodes<4><<<grid_for(P.nn, kNodeThreads), kNodeThreads, 0, st>>>(P, M, S);
 }
 
-void mix_geometry(const StepParams &P, const MixState &M, float *vol, cudaStream_t st) {
-  if (P.npe == 8)
-    k_mix_geometry<8><<<grid_for(P.ne, kElemThreads), kElemThreads, 0, st>>>(P, M, vol);
-  else
-    k_mix_geometry<4><<<grid_for(P.ne, kElemThreads), kElemThreads, 0, st>>>(P, M, vol);
+namespace {
+
+template <int NPE>
+void launch_geometry(const StepParams &P, const MixState &M, float *vol, cudaStream_t st,
+                     LaunchCfg c) {
+  const unsigned g = grid_for(P.ne, c.bs * c.ept);
+  switch (c.bs) {
+    case 64: k_mix_geometry<NPE, 64><<<g, 64, 0, st>>>(P, M, vol); break;
+    case 256: k_mix_geometry<NPE, 256><<<g, 256, 0, st>>>(P, M, vol); break;
+    default: k_mix_geometry<NPE, 128><<<g, 128, 0, st>>>(P, M, vol); break;
+  }
 }
 
-void mix_nodal(const StepParams &P, const MixState &M, const float *vol, cudaStream_t st) {
-  if (P.npe == 8)
-    k_mix_nodal<8><<<grid_for(P.nn, kNodeThreads), kNodeThreads, 0, st>>>(P, M, vol);
-  else
-    k_mix_nodal<4><<<grid_for(P.nn, kNodeThreads), kNodeThreads, 0, st>>>(P, M, vol);
+template <int NPE>
+void launch_nodal(const StepParams &P, const MixState &M, const float *vol, cudaStream_t st,
+                  LaunchCfg c) {
+  const unsigned g = grid_for(P.nn, c.bs * c.ept);
+  switch (c.bs) {
+    case 64: k_mix_nodal<NPE, 64><<<g, 64, 0, st>>>(P, M, vol); break;
+    case 128: k_mix_nodal<NPE, 128><<<g, 128, 0, st>>>(P, M, vol); break;
+    default: k_mix_nodal<NPE, 256><<<g, 256, 0, st>>>(P, M, vol); break;
+  }
 }
 
-void mix_elements(const StepParams &P, const MixState &M, const float *, cudaStream_t st) {
-  if (P.npe == 8)
-    k_mix_elements<8><<<grid_for(P.ne, kElemThreads), kElemThreads, 0, st>>>(P, M);
-  else
-    k_mix_elements<4><<<grid_for(P.ne, kElemThreads), kElemThreads, 0, st>>>(P, M);
+template <int NPE>
+void launch_elements(const StepParams &P, const MixState &M, cudaStream_t st, LaunchCfg c) {
+  const unsigned g = grid_for(P.ne, c.bs * c.ept);
+  switch (c.bs) {
+    case 64: k_mix_elements<NPE, 64><<<g, 64, 0, st>>>(P, M); break;
+    case 256: k_mix_elements<NPE, 256><<<g, 256, 0, st>>>(P, M); break;
+    default: k_mix_elements<NPE, 128><<<g, 128, 0, st>>>(P, M); break;
+  }
+}
+
+}  // namespace
+
+void mix_geometry(const StepParams &P, const MixState &M, float *vol, cudaStream_t st,
+                  LaunchCfg c) {
+  if (P.npe == 8) launch_geometry<8>(P, M, vol, st, c);
+  else launch_geometry<4>(P, M, vol, st, c);
+}
+
+void mix_nodal(const StepParams &P, const MixState &M, const float *vol, cudaStream_t st,
+               LaunchCfg c) {
+  if (P.npe == 8) launch_nodal<8>(P, M, vol, st, c);
+  else launch_nodal<4>(P, M, vol, st, c);
+}
+
+void mix_elements(const StepParams &P, const MixState &M, const float *, cudaStream_t st,
+                  LaunchCfg c) {
+  if (P.npe == 8) launch_elements<8>(P, M, st, c);
+  else launch_elements<4>(P, M, st, c);
 }
 
 void mix_nodes(const StepParams &P, const MixState &M, cudaStream_t st, int node_grid) {
