@@ -239,6 +239,29 @@ WF_API wf_status wf_nodal_volumes_noalloc(const double *xyz, const int32_t *elno
                                           const int32_t *nodel_count, const int32_t *nodel,
                                           double *voln, void *stream);
 
+/* ---- adjoint ---------------------------------------------------------------------- */
+/* No counterpart in the reference, which computes no derivatives. Reverse mode
+ * of the FP64 step for material identification: for a loss L(R_0 .. R_{N-1})
+ * of the reaction history over N steps, the gradient with respect to E,
+ * sigma_y0 and H of every material.
+ * wf_adjoint_forward runs nsteps steps from the current state, as wf_run
+ * does, and keeps an in-memory checkpoint of the state (x, v, prev_a, u, tau,
+ * eps, eps_p) every `every` steps (0: about sqrt(nsteps)). Supported: FP64
+ * precision, bilinear materials, pressure algorithm 0 with default
+ * stabilisation, no artificial viscosity, no contact, no specimens.
+ * wf_adjoint_backward takes dL_dR[nsteps] (host) and writes
+ * grad[3 * nmat] = (dL/dE, dL/dsigma_y0, dL/dH) of each material in turn. It
+ * recomputes each segment from its checkpoint, reverses it step by step
+ * (node update, internal-force gather, element stress update with the
+ * consistent derivative of the radial return, hourglass forces, nodal volumes
+ * and masses), and leaves the domain in the state at the end of the forward
+ * run, so it may be called again with another dL_dR. reverse_fp32 != 0 runs
+ * the element reverse arithmetic in FP32 (the recomputed forward stays FP64).
+ * The domain must not step between the two calls. */
+WF_API wf_status wf_adjoint_forward(wf_domain *d, int64_t nsteps, int64_t every);
+WF_API wf_status wf_adjoint_backward(wf_domain *d, const double *dL_dR, int32_t reverse_fp32,
+                                     double *grad);
+
 /* ---- readback (host buffers) -------------------------------------------------- */
 WF_API wf_status wf_get_node_field(wf_domain *d, int32_t field, double *out);   /* 3*nn */
 WF_API wf_status wf_get_node_scalar(wf_domain *d, int32_t field, double *out);  /* nn */

@@ -108,6 +108,8 @@ _SIGS = {
     "wf_get_launch_config": [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                              C.POINTER(C.c_double)],
     "wf_get_transfer_bytes": [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)],
+    "wf_adjoint_forward": [C.c_void_p, C.c_int64, C.c_int64],
+    "wf_adjoint_backward": [C.c_void_p, _dp, C.c_int32, _dp],
     # allocation-free nodal volumes: device pointers in, device pointer out
     "wf_nodal_volumes_noalloc": [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_int32,
                                  C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p],
@@ -160,6 +162,7 @@ class Domain:
             raise WfError(st, "wf_domain_create: no usable CUDA device")
         self.h = h
         self.precision = precision
+        self._nmat = 0
         self._call("wf_set_precision", int(precision))
 
     def _call(self, name, *args):
@@ -229,6 +232,7 @@ class Domain:
                                 float(m["rho"]), float(m.get("sy0", 1e10)), float(m.get("H", 0.0)),
                                 float(m.get("hol_K", 1.0)), float(m.get("hol_m", 1.0)))
         self._call("wf_set_materials", len(mats), arr)
+        self._nmat = len(mats)
         if elem_ids is not None:
             self._call("wf_set_elem_materials", np.ascontiguousarray(elem_ids, np.int32))
 
@@ -298,6 +302,18 @@ class Domain:
 
     def run(self, n):
         self._call("wf_run", int(n))
+
+    # adjoint ----------------------------------------------------------
+    def adjoint_forward(self, n, every=0):
+        """Runs n steps keeping checkpoints every `every` steps (0: ~sqrt(n))."""
+        self._call("wf_adjoint_forward", int(n), int(every))
+
+    def adjoint_backward(self, dL_dR, fp32=False):
+        """dL/dR of each recorded step -> array [nmat, 3] of dL/d(E, sigma_y0, H)."""
+        seed = np.ascontiguousarray(dL_dR, dtype=np.float64)
+        grad = np.zeros(3 * self._nmat)
+        self._call("wf_adjoint_backward", seed, int(bool(fp32)), grad)
+        return grad.reshape(-1, 3)
 
     def solve(self):
         n = C.c_int64()

@@ -29,6 +29,7 @@ UNITS = {
     "wf_mixed.cu": [],
     "wf_reduce.cu": [],
     "wf_noalloc.cu": ["--fmad=false"],
+    "wf_adjoint.cu": [],
 }
 
 
@@ -41,7 +42,8 @@ def nvcc() -> str:
 
 def _sources():
     return [os.path.join(CSRC, u) for u in UNITS] + [
-        os.path.join(CSRC, "wf_internal.cuh"), os.path.join(ROOT, "include", "wf.h")]
+        os.path.join(CSRC, "wf_internal.cuh"), os.path.join(CSRC, "wf_adjoint.cuh"),
+        os.path.join(ROOT, "include", "wf.h")]
 
 
 def up_to_date() -> bool:

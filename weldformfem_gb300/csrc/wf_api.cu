@@ -14,6 +14,7 @@
 #include <tuple>
 #include <vector>
 
+#include "wf_adjoint.cuh"
 #include "wf_internal.cuh"
 
 using namespace wf;
@@ -81,6 +82,16 @@ struct wf_domain {
   int32_t nspec = 0;
   std::vector<int64_t> spec_eoff, spec_noff;
   std::vector<double> spec_dt;
+  // adjoint recording: checkpoints of the forward run and reverse-pass buffers
+  std::vector<void *> adj_allocs;
+  int64_t adj_steps = 0, adj_every = 0, adj_first = 0;
+  int64_t adj_nck = 0;
+  double *ck_node = nullptr;      // [nck][4][3 np]: x, v, prev_a, u
+  double *ck_elem = nullptr;      // [nck][13][ne]: tau, eps, eps_p
+  StepState *ck_st = nullptr;     // [nck]
+  AdjArgs A{};
+  double *adj_seed = nullptr;     // [adj_steps]
+  bool adj_buffers = false;
 };
 
 namespace {
@@ -115,7 +126,19 @@ cudaError_t dalloc(wf_domain *d, T **p, size_t count) {
   return cudaMemsetAsync(q, 0, std::max<size_t>(count, 1) * sizeof(T), d->stream);
 }
 
+void free_adjoint(wf_domain *d) {
+  for (void *p : d->adj_allocs) cudaFree(p);
+  d->adj_allocs.clear();
+  d->adj_steps = d->adj_every = d->adj_nck = 0;
+  d->ck_node = d->ck_elem = nullptr;
+  d->ck_st = nullptr;
+  d->A = AdjArgs{};
+  d->adj_seed = nullptr;
+  d->adj_buffers = false;
+}
+
 void free_device(wf_domain *d) {
+  free_adjoint(d);
   if (d->graph) {
     cudaGraphExecDestroy(d->graph);
     d->graph = nullptr;
@@ -1409,5 +1432,183 @@ WF_API wf_status wf_get_transfer_bytes(const wf_domain *d, int64_t *h2d, int64_t
   if (!d) return WF_ERR_ARG;
   if (h2d) *h2d = d->h2d_bytes;
   if (d2h) *d2h = d->d2h_bytes;
+  return WF_OK;
+}
+
+// ---- adjoint ----------------------------------------------------------------------
+namespace {
+
+template <typename T>
+cudaError_t adj_alloc(wf_domain *d, T **p, size_t count) {
+  void *q = nullptr;
+  cudaError_t e = cudaMalloc(&q, std::max<size_t>(count, 1) * sizeof(T));
+  if (e != cudaSuccess) return e;
+  d->adj_allocs.push_back(q);
+  *p = static_cast<T *>(q);
+  return cudaMemsetAsync(q, 0, std::max<size_t>(count, 1) * sizeof(T), d->stream);
+}
+
+// Checkpoint c holds what the step reads and accumulates: x, v, prev_a, u,
+// tau, eps, eps_p and the device step state (step index and Time).
+wf_status ck_copy(wf_domain *d, int64_t c, bool save) {
+  const size_t nb = sizeof(double) * 3 * d->np, eb = sizeof(double) * d->ne;
+  double *node = d->ck_node + (size_t)c * 12 * d->np;
+  double *elem = d->ck_elem + (size_t)c * 13 * d->ne;
+  Fp64State &S = d->S;
+  double *nf[4] = {S.x, S.v, S.pa, S.u};
+  const auto kind = cudaMemcpyDeviceToDevice;
+  for (int i = 0; i < 4; i++) {
+    double *ck = node + (size_t)i * 3 * d->np;
+    CUDA_TRY(cudaMemcpyAsync(save ? ck : nf[i], save ? nf[i] : ck, nb, kind, d->stream));
+  }
+  CUDA_TRY(cudaMemcpyAsync(save ? elem : S.tau, save ? S.tau : elem, 6 * eb, kind, d->stream));
+  CUDA_TRY(cudaMemcpyAsync(save ? elem + 6 * d->ne : S.eps, save ? S.eps : elem + 6 * d->ne, 6 * eb,
+                           kind, d->stream));
+  CUDA_TRY(cudaMemcpyAsync(save ? elem + 12 * d->ne : S.pls, save ? S.pls : elem + 12 * d->ne, eb,
+                           kind, d->stream));
+  CUDA_TRY(cudaMemcpyAsync(save ? d->ck_st + c : d->P.st, save ? d->P.st : d->ck_st + c,
+                           sizeof(StepState), kind, d->stream));
+  return WF_OK;
+}
+
+wf_status adjoint_buffers(wf_domain *d) {
+  if (d->adj_buffers) return WF_OK;
+  const size_t np = d->np, ne = d->ne, seg = d->adj_every, npe = d->npe;
+  AdjArgs &A = d->A;
+  CUDA_TRY(adj_alloc(d, &A.sx, seg * 3 * np));
+  CUDA_TRY(adj_alloc(d, &A.sv, seg * 3 * np));
+  CUDA_TRY(adj_alloc(d, &A.spa, seg * 3 * np));
+  CUDA_TRY(adj_alloc(d, &A.sjr, seg * np));
+  CUDA_TRY(adj_alloc(d, &A.smass, seg * np));
+  CUDA_TRY(adj_alloc(d, &A.sfi, seg * 3 * np));
+  CUDA_TRY(adj_alloc(d, &A.stau, seg * 6 * ne));
+  CUDA_TRY(adj_alloc(d, &A.spls, seg * ne));
+  CUDA_TRY(adj_alloc(d, &A.X, 3 * np));
+  CUDA_TRY(adj_alloc(d, &A.V, 3 * np));
+  CUDA_TRY(adj_alloc(d, &A.PA, 3 * np));
+  CUDA_TRY(adj_alloc(d, &A.T, 6 * ne));
+  CUDA_TRY(adj_alloc(d, &A.EP, ne));
+  CUDA_TRY(adj_alloc(d, &A.fib, 3 * np));
+  CUDA_TRY(adj_alloc(d, &A.vpb, 3 * np));
+  CUDA_TRY(adj_alloc(d, &A.mb, np));
+  CUDA_TRY(adj_alloc(d, &A.sb, np));
+  CUDA_TRY(adj_alloc(d, &A.cx, npe * 3 * ne));
+  CUDA_TRY(adj_alloc(d, &A.cv, npe * 3 * ne));
+  CUDA_TRY(adj_alloc(d, &A.cgeo, npe * 3 * ne));
+  CUDA_TRY(adj_alloc(d, &A.cj, ne));
+  CUDA_TRY(adj_alloc(d, &A.volb, ne));
+  CUDA_TRY(adj_alloc(d, &A.gth, 3 * ne));
+  CUDA_TRY(adj_alloc(d, &d->adj_seed, d->adj_steps));
+  A.seed = d->adj_seed;
+  A.s0 = d->S.s0;
+  A.rho = d->S.rho;
+  d->adj_buffers = true;
+  return WF_OK;
+}
+
+}  // namespace
+
+WF_API wf_status wf_adjoint_forward(wf_domain *d, int64_t nsteps, int64_t every) {
+  if (!d || nsteps <= 0 || every < 0) return WF_ERR_ARG;
+  if (!d->initialized) return fail(d, WF_ERR_STATE, "wf_init not called");
+  if (d->precision != WF_FP64)
+    return fail(d, WF_ERR_UNSUPPORTED, "the adjoint records the FP64 step");
+  if (d->contact || d->nspec || d->press_alg != 0 || d->av[0] != 0.0 || d->av[1] != 0.0)
+    return fail(d, WF_ERR_UNSUPPORTED, "the adjoint supports pressure algorithm 0 without contact, "
+                                       "artificial viscosity or specimens");
+  const double *sp = &d->stab.alpha_free;
+  for (int i = 0; i < 10; i++)
+    if (sp[i] != 0.0) return fail(d, WF_ERR_UNSUPPORTED, "the adjoint supports default stabilisation");
+  for (const wf_material &m : d->mats)
+    if (m.model != WF_MAT_BILINEAR)
+      return fail(d, WF_ERR_UNSUPPORTED, "the adjoint supports bilinear (linear hardening) materials");
+  if (!(d->dt > 0.0)) return fail(d, WF_ERR_STATE, "time step not set (SetDT)");
+  CUDA_TRY(cudaSetDevice(d->device));
+  if (every == 0) every = std::max<int64_t>(1, (int64_t)std::llround(std::sqrt((double)nsteps)));
+  every = std::min(every, nsteps);
+  free_adjoint(d);
+  const int64_t nck = (nsteps + every - 1) / every;
+  CUDA_TRY(adj_alloc(d, &d->ck_node, (size_t)nck * 12 * d->np));
+  CUDA_TRY(adj_alloc(d, &d->ck_elem, (size_t)nck * 13 * d->ne));
+  CUDA_TRY(adj_alloc(d, &d->ck_st, nck));
+  d->adj_first = d->host_step;
+  for (int64_t c = 0; c < nck; c++) {
+    wf_status s = ck_copy(d, c, true);
+    if (s) return s;
+    s = wf_run(d, std::min(every, nsteps - c * every));
+    if (s) return s;
+  }
+  d->adj_steps = nsteps;
+  d->adj_every = every;
+  d->adj_nck = nck;
+  return WF_OK;
+}
+
+WF_API wf_status wf_adjoint_backward(wf_domain *d, const double *dL_dR, int32_t reverse_fp32,
+                                     double *grad) {
+  if (!d || !dL_dR || !grad) return WF_ERR_ARG;
+  if (d->adj_steps <= 0) return fail(d, WF_ERR_STATE, "wf_adjoint_forward not called");
+  if (d->host_step != d->adj_first + d->adj_steps)
+    return fail(d, WF_ERR_STATE, "the domain stepped after wf_adjoint_forward");
+  CUDA_TRY(cudaSetDevice(d->device));
+  wf_status s = adjoint_buffers(d);
+  if (s) return s;
+  const int64_t N = d->adj_steps, every = d->adj_every;
+  const AdjArgs &A = d->A;
+  const size_t np = d->np, ne = d->ne, npe = d->npe;
+  CUDA_TRY(cudaMemcpyAsync(d->adj_seed, dL_dR, sizeof(double) * N, cudaMemcpyHostToDevice,
+                           d->stream));
+  d->h2d_bytes += (int64_t)(sizeof(double) * N);
+  for (double *p : {A.X, A.V, A.PA})
+    CUDA_TRY(cudaMemsetAsync(p, 0, sizeof(double) * 3 * np, d->stream));
+  CUDA_TRY(cudaMemsetAsync(A.T, 0, sizeof(double) * 6 * ne, d->stream));
+  CUDA_TRY(cudaMemsetAsync(A.EP, 0, sizeof(double) * ne, d->stream));
+  CUDA_TRY(cudaMemsetAsync(A.cgeo, 0, sizeof(double) * npe * 3 * ne, d->stream));
+  CUDA_TRY(cudaMemsetAsync(A.gth, 0, sizeof(double) * 3 * ne, d->stream));
+  StepParams &P = d->P;
+  set_dt_constants(P, d->dt);
+  const Fp64State &S = d->S;
+  for (int64_t c = d->adj_nck - 1; c >= 0; c--) {
+    const int64_t c0 = c * every, L = std::min(every, N - c0);
+    s = ck_copy(d, c, false);
+    if (s) return s;
+    // recompute the segment, stashing each step's inputs
+    fp64_predict(P, S, d->stream);
+    for (int64_t j = 0; j < L; j++) {
+      adj_stash_state(P, S, A, (int)j, d->stream);
+      fp64_geometry(P, S, d->stream, false);
+      fp64_nodal(P, S, d->stream, 0);
+      fp64_elements(P, S, d->stream);
+      fp64_nodes(P, S, d->stream, d->node_grid);
+      adj_stash_step(P, S, A, (int)j, d->stream);
+    }
+    // reverse it
+    for (int64_t j = L - 1; j >= 0; j--)
+      adj_reverse_step(P, A, (int)j, c0 + j, 1, reverse_fp32 != 0, d->stream);
+    CUDA_TRY(cudaGetLastError());
+    d->launches += 1 + 10 * L;
+  }
+  // back to the state at the end of the forward run
+  {
+    const int64_t c = d->adj_nck - 1, L = N - c * every;
+    s = ck_copy(d, c, false);
+    if (s) return s;
+    fp64_predict(P, S, d->stream);
+    for (int64_t j = 0; j < L; j++) launch_step(d);
+    CUDA_TRY(cudaGetLastError());
+    d->launches += 1 + 4 * L;
+  }
+  // per-material sums of the element gradients, in element order
+  std::vector<double> g(3 * ne);
+  CUDA_TRY(cudaMemcpyAsync(g.data(), A.gth, sizeof(double) * 3 * ne, cudaMemcpyDeviceToHost,
+                           d->stream));
+  d->d2h_bytes += (int64_t)(sizeof(double) * 3 * ne);
+  CUDA_TRY(cudaStreamSynchronize(d->stream));
+  const size_t nmat = d->mats.size();
+  for (size_t i = 0; i < 3 * nmat; i++) grad[i] = 0.0;
+  for (size_t e = 0; e < ne; e++) {
+    const size_t m = d->emat.empty() ? 0 : (size_t)d->emat[e];
+    for (int k = 0; k < 3; k++) grad[3 * m + k] += g[k * ne + e];
+  }
   return WF_OK;
 }

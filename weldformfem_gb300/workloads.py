@@ -286,6 +286,35 @@ def config(cid: int, steps: Optional[int] = None, scale: Optional[tuple] = None)
     return c
 
 
+PARAM_KEYS = ("E", "sy0", "H")
+
+
+def material_params(case: Case) -> np.ndarray:
+    """[nmat, 3] array of (E, sigma_y0, H) of the case's materials."""
+    return np.array([[m[k] for k in PARAM_KEYS] for m in case.materials], dtype=np.float64)
+
+
+def with_params(case: Case, theta) -> Case:
+    """Copy of `case` whose materials take (E, sigma_y0, H) from theta[nmat, 3].
+    The time step is frozen at the original case's value first, so that
+    changing material 0's modulus does not change dt."""
+    theta = np.asarray(theta, dtype=np.float64).reshape(-1, 3)
+    c = dataclasses.replace(case, materials=[dict(m) for m in case.materials])
+    if c.dt is None:
+        c.dt = case.time_step()
+    for m, row in zip(c.materials, theta):
+        for k, v in zip(PARAM_KEYS, row):
+            m[k] = float(v)
+    return c
+
+
+def target_factors(case: Case, seed: int = SEED_BASE + 4) -> np.ndarray:
+    """Seeded U[0.8, 1.2) factors, one per material parameter (the target
+    run of the material-identification problem)."""
+    n = len(case.materials) * 3
+    return (1.0 + 0.2 * uniform_pm1(seed, n)).reshape(-1, 3)
+
+
 @dataclasses.dataclass
 class Batch:
     """An ensemble of independent specimens run as one batched domain."""
