@@ -374,6 +374,114 @@ def run_ensemble(args):
     print(json.dumps(line), flush=True)
 
 
+def run_adjoint(args):
+    """Config 4: material identification on the 32^3 octant cube (24
+    parameters), FP64 step with checkpoints every `--every` steps; times the
+    plain forward, the checkpointed forward and the reverse pass (FP64 and
+    FP32 reverse arithmetic), and checks three gradient components against
+    central finite differences of the FP64 forward at full size."""
+    import torch
+
+    import weldformfem_gb300 as wf
+    from weldformfem_gb300 import adjoint as A
+
+    _, _, local = dist_env()
+    device = local
+    torch.cuda.set_device(device)
+    case = W.config(4, steps=args.adj_steps)
+    case.dt = case.time_step()
+    N, every = case.steps, args.every
+    E = case.n_elem
+    th0 = W.material_params(case)
+    Rstar, _ = A.solve_with_adjoint(case, th0 * W.target_factors(case), N, every)
+
+    def timed(dom, fn):
+        st = torch.cuda.ExternalStream(dom.stream_handle(), device=device)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize(device)
+        a.record(st)
+        out = fn()
+        b.record(st)
+        b.synchronize()
+        return a.elapsed_time(b), out
+
+    def fresh(prec=wf.WF_FP64, theta=th0):
+        d = wf.Domain(prec, device=device)
+        W.apply(d, W.with_params(case, theta))
+        d.init()
+        d.sync()
+        return d
+
+    # warm-up of every kernel on a short run
+    dw = fresh()
+    dw.adjoint_forward(2 * every, every)
+    dw.adjoint_backward(np.ones(2 * every))
+    dw.adjoint_backward(np.ones(2 * every), fp32=True)
+    del dw
+    clocks = ClockSampler(device)
+    clocks.start()
+    d = fresh()
+    ms_fwd, _ = timed(d, lambda: d.run(N))
+    R_plain = d.reaction()
+    del d
+    d = fresh(wf.WF_MIXED)
+    ms_mixed, _ = timed(d, lambda: d.run(N))
+    del d
+    d = fresh()
+    l0 = d.launch_count()
+    ms_ck, _ = timed(d, lambda: d.adjoint_forward(N, every))
+    R = d.reaction()
+    seed = 2.0 * (R - Rstar)
+    l1 = d.launch_count()
+    ms_b64, g64 = timed(d, lambda: d.adjoint_backward(seed))
+    l2 = d.launch_count()
+    ms_b32, g32 = timed(d, lambda: d.adjoint_backward(seed, fp32=True))
+    clk = clocks.stop()
+    loss = float(np.sum((R - Rstar) ** 2))
+    assert np.array_equal(R, R_plain)
+
+    # three components against central differences of the FP64 forward
+    fd = []
+    for (i, k) in ((0, 0), (3, 1), (7, 2)):
+        h = 1e-6 * th0[i, k]
+        Ls = []
+        for sgn in (1, -1):
+            t = th0.copy()
+            t[i, k] += sgn * h
+            dd = fresh(theta=t)
+            dd.run(N)
+            Ls.append(float(np.sum((dd.reaction() - Rstar) ** 2)))
+            del dd
+        gfd = (Ls[0] - Ls[1]) / (2 * h)
+        fd.append({"param": f"{W.PARAM_KEYS[k]}[{i}]", "adjoint": float(g64[i, k]),
+                   "fd": gfd, "rel_err": abs(g64[i, k] - gfd) / max(abs(gfd), 1e-300)})
+    lg = lambda g: g * th0
+    err32 = float(np.abs(lg(g32) - lg(g64)).max() / np.abs(lg(g64)).max())
+    line = {
+        "metric": "adjoint/forward time", "value": round(ms_b64 / ms_fwd, 3), "unit": "ratio",
+        "n_gpus": 1, "steps": N, "warmup": 1, "higher_is_better": False,
+        "scaling": "none", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": case.name, "elements": E, "nodes": case.n_node,
+                   "parameters": int(th0.size), "checkpoint_every": every,
+                   "loss": "sum over steps of (F_top - F_target)^2, target = seeded U[0.8,1.2) "
+                           "scaling of the 24 parameters"},
+        "ms": {"forward_fp64": round(ms_fwd, 2), "forward_mixed": round(ms_mixed, 2),
+               "forward_checkpointed": round(ms_ck, 2), "backward_fp64": round(ms_b64, 2),
+               "backward_fp32_reverse": round(ms_b32, 2)},
+        "ratios": {"backward_fp64_over_forward": round(ms_b64 / ms_fwd, 3),
+                   "backward_fp32_over_forward": round(ms_b32 / ms_fwd, 3),
+                   "checkpointed_forward_plus_backward_over_forward":
+                       round((ms_ck + ms_b64) / ms_fwd, 3)},
+        "element_steps_per_s_forward_fp64": round(E * N / (ms_fwd * 1e-3), 1),
+        "loss": loss,
+        "gradient_fd_check": fd,
+        "fp32_reverse_rel_err": err32,
+        "gpu_launches": {"forward_checkpointed": int(l1 - l0), "backward": int(l2 - l1)},
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def cpu_baseline(case, x, steps):
     """The oracle (C restatement of the reference loop) on all host cores."""
     from oracle import orabind
@@ -438,11 +546,15 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--n-spec", type=int, default=1024)
+    ap.add_argument("--adj-steps", type=int, default=4000)
+    ap.add_argument("--every", type=int, default=64)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
     elif args.config == 3:
         run_ensemble(args)
+    elif args.config == 4:
+        run_adjoint(args)
     else:
         run_ours(args)
 

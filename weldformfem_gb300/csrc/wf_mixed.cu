@@ -5,6 +5,10 @@
 // including the reference's Jaumann-term tensor product, with these changes:
 //  * element geometry uses coordinates relative to the element's first node,
 //    formed from (hi, lo) float pairs, so no FP64 instruction is issued;
+//  * for hexahedra, the Jacobian, the velocity gradient, the hourglass modes
+//    and the nodal forces go through a Walsh transform of the nodal values
+//    (the same quantities as the reference's per-node loops, in 24 additions
+//    per component instead of a loop over nodes and derivatives);
 //  * the element force written for assembly is f_elem - f_hourglass;
 //  * the lumped mass is voln * (mean density of the node's elements), the
 //    same quantity as the reference's sum of rho_e * voln / count;
@@ -18,16 +22,6 @@ namespace {
 
 constexpr int kElemThreads = 128;
 constexpr int kNodeThreads = 256;
-
-// Flanagan-Belytschko hourglass base vectors (test_1el_3D.cpp:166-169) as a
-// compile-time sign table: after unrolling, x * sign folds to +x or -x.
-__device__ __forceinline__ constexpr float c_sig_at(int j, int a) {
-  constexpr signed char t[4][8] = {{1, 1, -1, -1, -1, -1, 1, 1},
-                                   {1, -1, -1, 1, -1, 1, 1, -1},
-                                   {1, -1, 1, -1, 1, -1, 1, -1},
-                                   {-1, 1, -1, 1, 1, -1, 1, -1}};
-  return (float)t[j][a];
-}
 
 // (hi, lo) pair helpers ------------------------------------------------------
 __device__ __forceinline__ float2 split_d(double v) {
@@ -223,72 +217,16 @@ __global__ void __launch_bounds__(BS) k_mix_nodal(StepParams P, MixState M, cons
     nodal_one<NPE>(P, M, vol, n);
 }
 
-template <int NPE>
-__device__ __forceinline__ void element_one(const StepParams &P, const MixState &M, int64_t e) {
+// Jaumann rate + radial return, shared by both element types. The
+// reference's tensor3 product (Tensor3.C:290-303) written out for a
+// symmetric tau and the spin W (antisymmetric, zero diagonal): only the six
+// stored components are formed, terms that multiply a zero of W are dropped.
+// In: strain rate sr (xx yy zz xy yz xz), spin (w01, w12, w02), pressure p.
+// Writes the new tau and eps_p; returns sigma = tau - p I in sg.
+__device__ __forceinline__ void stress_update(const StepParams &P, const MixState &M, int64_t e,
+                                              const MatF &m, const float (&sr)[6], float w01,
+                                              float w12, float w02, float p, float (&sg)[6]) {
   const int64_t ne = P.ne;
-  int32_t nid[NPE];
-  float dH[3][NPE];
-  float detJ;
-  {
-    float r[NPE][3];
-    rel_coords<NPE>(P, M, e, r, nid);
-    float J[3][3];
-    jacobian_f<NPE>(r, J);
-    shape_derivs_f<NPE>(J, dH);
-    detJ = det3f(J);
-  }
-  const float vol = detJ * weightf<NPE>();
-  const MatF m = P.matf[P.emat ? __ldg(&P.emat[e]) : 0];
-
-  float s00 = 0.f, s11 = 0.f, s22 = 0.f, s01 = 0.f, s12 = 0.f, s02 = 0.f;
-  float w01 = 0.f, w12 = 0.f, w02 = 0.f;
-  float hm[3][4];
-#pragma unroll
-  for (int k = 0; k < 3; k++)
-#pragma unroll
-    for (int j = 0; j < 4; j++) hm[k][j] = 0.f;
-  float J_avg = 0.f;
-#pragma unroll
-  for (int a = 0; a < NPE; a++) {
-    const float v0 = __ldg(&M.vp[nid[a]]);
-    const float v1 = __ldg(&M.vp[P.np + nid[a]]);
-    const float v2 = __ldg(&M.vp[2 * P.np + nid[a]]);
-    const float d0 = dH[0][a], d1 = dH[1][a], d2 = dH[2][a];
-    s00 += d0 * v0;
-    s11 += d1 * v1;
-    s22 += d2 * v2;
-    s01 += d1 * v0 + d0 * v1;
-    w01 += d1 * v0 - d0 * v1;
-    s12 += d2 * v1 + d1 * v2;
-    s02 += d2 * v0 + d0 * v2;
-    w12 += d2 * v1 - d1 * v2;
-    w02 += d2 * v0 - d0 * v2;
-    J_avg += __ldg(&M.jr[nid[a]]);
-    if constexpr (NPE == 8) {
-      if (P.hg_on) {
-#pragma unroll
-        for (int j = 0; j < 4; j++) {
-          hm[0][j] += v0 * c_sig_at(j, a);
-          hm[1][j] += v1 * c_sig_at(j, a);
-          hm[2][j] += v2 * c_sig_at(j, a);
-        }
-      }
-    }
-  }
-  const float f = 1.0f / detJ;
-  const float fh = 0.5f * f;
-  s00 *= f; s11 *= f; s22 *= f;
-  s01 *= fh; s12 *= fh; s02 *= fh;
-  w01 *= fh; w12 *= fh; w02 *= fh;
-  J_avg *= (1.0f / NPE);
-  float J_bar = J_avg;
-  if (J_bar < 0.0f) J_bar = 0.2f;
-  const float p = -m.K * (J_bar - 1.0f);
-
-  // Jaumann rate + radial return. The reference's tensor3 product
-  // (Tensor3.C:290-303) written out for a symmetric tau and the spin W
-  // (antisymmetric, zero diagonal): only the six stored components are
-  // formed, terms that multiply a zero of W are dropped.
   const float dt = P.espec ? P.specf[P.espec[e]].dt : P.f_dt;
   float t0 = M.tau[e], t1 = M.tau[ne + e], t2 = M.tau[2 * ne + e];
   float t3 = M.tau[3 * ne + e], t4 = M.tau[4 * ne + e], t5 = M.tau[5 * ne + e];
@@ -300,14 +238,14 @@ __device__ __forceinline__ void element_one(const StepParams &P, const MixState 
     const float srt3 = t0 * w01 - t5 * w12, rs3 = w01 * t1 + w02 * t4;    // xy
     const float srt4 = t3 * w02 + t1 * w12, rs4 = w12 * t2 - w01 * t5;    // yz
     const float srt5 = t0 * w02 + t3 * w12, rs5 = w01 * t4 + w02 * t2;    // xz
-    const float c = (1.0f / 3.0f) * (s00 + s11 + s22);
+    const float c = (1.0f / 3.0f) * (sr[0] + sr[1] + sr[2]);
     const float g2 = 2.0f * m.G;
-    t0 += ((s00 - c) * g2 + srt0 + rs0) * dt;
-    t1 += ((s11 - c) * g2 + srt1 + rs1) * dt;
-    t2 += ((s22 - c) * g2 + srt2 + rs2) * dt;
-    t3 += (s01 * g2 + srt3 + rs3) * dt;
-    t4 += (s12 * g2 + srt4 + rs4) * dt;
-    t5 += (s02 * g2 + srt5 + rs5) * dt;
+    t0 += ((sr[0] - c) * g2 + srt0 + rs0) * dt;
+    t1 += ((sr[1] - c) * g2 + srt1 + rs1) * dt;
+    t2 += ((sr[2] - c) * g2 + srt2 + rs2) * dt;
+    t3 += (sr[3] * g2 + srt3 + rs3) * dt;
+    t4 += (sr[4] * g2 + srt4 + rs4) * dt;
+    t5 += (sr[5] * g2 + srt5 + rs5) * dt;
   }
   // deviatoric trial stress of sigma_trial = tau - p I
   const float c2 = (1.0f / 3.0f) * ((t0 - p) + (t1 - p) + (t2 - p));
@@ -336,48 +274,202 @@ __device__ __forceinline__ void element_one(const StepParams &P, const MixState 
   M.pls[e] = pls;
   M.tau[e] = t0; M.tau[ne + e] = t1; M.tau[2 * ne + e] = t2;
   M.tau[3 * ne + e] = t3; M.tau[4 * ne + e] = t4; M.tau[5 * ne + e] = t5;
-  const float sg0 = t0 - p, sg1 = t1 - p, sg2 = t2 - p;
-  const float sg3 = t3, sg4 = t4, sg5 = t5;
-
-  // element force minus hourglass force
-  const float w = weightf<NPE>();
-  float ch = 0.f;
-  if constexpr (NPE == 8) {
-    if (P.hg_on) ch = P.f_hg_coef * powf(vol, 0.6666666f) * m.rho * 0.25f * m.cs0;
-  }
-  float out[NPE * 3];
-#pragma unroll
-  for (int a = 0; a < NPE; a++) {
-    const float d0 = dH[0][a], d1 = dH[1][a], d2 = dH[2][a];
-    float f0 = (d0 * sg0 + d1 * sg3 + d2 * sg5) * w;
-    float f1 = (d1 * sg1 + d0 * sg3 + d2 * sg4) * w;
-    float f2 = (d2 * sg2 + d1 * sg4 + d0 * sg5) * w;
-    if constexpr (NPE == 8) {
-      if (P.hg_on) {
-        float g0 = 0.f, g1 = 0.f, g2 = 0.f;
-#pragma unroll
-        for (int j = 0; j < 4; j++) {
-          g0 += hm[0][j] * c_sig_at(j, a);
-          g1 += hm[1][j] * c_sig_at(j, a);
-          g2 += hm[2][j] * c_sig_at(j, a);
-        }
-        // f_hg = -ch * sum_j h_j Gamma_j; assembly subtracts it
-        f0 += ch * g0;
-        f1 += ch * g1;
-        f2 += ch * g2;
-      }
-    }
-    out[3 * a] = f0;
-    out[3 * a + 1] = f1;
-    out[3 * a + 2] = f2;
-  }
-  // SoA by (local node, component): fe[(a * 3 + k) * ne + e]
-#pragma unroll
-  for (int q = 0; q < NPE * 3; q++) M.fe[q * ne + e] = out[q];
+  sg[0] = t0 - p; sg[1] = t1 - p; sg[2] = t2 - p;
+  sg[3] = t3; sg[4] = t4; sg[5] = t5;
 }
 
-// Registers per thread stay <= 80 (no spills) at 768 resident threads per SM.
-constexpr int elem_min_blocks(int bs) { return 768 / bs; }
+// Walsh transform over the corners of the hexahedron. Node a of the
+// AddBoxLength numbering sits at (xi, eta, zeta) = signs of
+// (-,-,-) (+,-,-) (+,+,-) (-,+,-) (-,-,+) (+,-,+) (+,+,+) (-,+,+).
+// o = sums of v weighted by {1, xi, eta, zeta, eta zeta, xi zeta, xi eta,
+// xi eta zeta}: the first four are the trilinear shape functions' derivative
+// directions at the centre, the last four the Flanagan-Belytschko hourglass
+// base vectors Gamma_0..3 (test_1el_3D.cpp:166-169). 24 additions.
+__device__ __forceinline__ void walsh8(const float (&v)[8], float (&o)[8]) {
+  const float a0 = v[1] + v[0], b0 = v[1] - v[0];  // along xi at (eta-, zeta-)
+  const float a1 = v[2] + v[3], b1 = v[2] - v[3];  // (eta+, zeta-)
+  const float a2 = v[5] + v[4], b2 = v[5] - v[4];  // (eta-, zeta+)
+  const float a3 = v[6] + v[7], b3 = v[6] - v[7];  // (eta+, zeta+)
+  const float c0 = a1 + a0, d0 = a1 - a0, e0 = b1 + b0, f0 = b1 - b0;  // along eta, zeta-
+  const float c1 = a3 + a2, d1 = a3 - a2, e1 = b3 + b2, f1 = b3 - b2;  // zeta+
+  o[0] = c1 + c0;
+  o[3] = c1 - c0;
+  o[2] = d1 + d0;
+  o[4] = d1 - d0;
+  o[1] = e1 + e0;
+  o[5] = e1 - e0;
+  o[6] = f1 + f0;
+  o[7] = f1 - f0;
+}
+
+// Transpose of walsh8 with no constant term: the node values of
+// sum_b o[b] phi_b for b = 1..7.
+__device__ __forceinline__ void walsh8_synth(const float (&o)[8], float (&v)[8]) {
+  const float c1 = o[3], c0 = -o[3];
+  const float d1 = o[2] + o[4], d0 = o[2] - o[4];
+  const float e1 = o[1] + o[5], e0 = o[1] - o[5];
+  const float f1 = o[6] + o[7], f0 = o[6] - o[7];
+  const float a1 = c0 + d0, a0 = c0 - d0, b1 = e0 + f0, b0 = e0 - f0;
+  const float a3 = c1 + d1, a2 = c1 - d1, b3 = e1 + f1, b2 = e1 - f1;
+  v[1] = a0 + b0; v[0] = a0 - b0;
+  v[2] = a1 + b1; v[3] = a1 - b1;
+  v[5] = a2 + b2; v[4] = a2 - b2;
+  v[6] = a3 + b3; v[7] = a3 - b3;
+}
+
+// Hexahedron: with dN_a/dx = (1/8) adj(J)^T-row . s(a) / detJ at the centre,
+// the velocity gradient is adj(J) G / (8 detJ) with G the Walsh sums of the
+// nodal velocities, and the nodal forces are the synthesis of
+// T = adj(J)^T sigma (w / 8 = 1) plus the hourglass coefficients ch h_j.
+// Same quantities as the reference's per-node loops, fewer operations.
+__device__ __forceinline__ void element_hex(const StepParams &P, const MixState &M, int64_t e) {
+  const int64_t ne = P.ne, np = P.np;
+  int32_t nid[8];
+  float A[3][3], detJ;
+  {
+    float r[8][3];
+    rel_coords<8>(P, M, e, r, nid);
+    float J[3][3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      float v[8], o[8];
+#pragma unroll
+      for (int a = 0; a < 8; a++) v[a] = r[a][k];
+      walsh8(v, o);
+      J[0][k] = 0.125f * o[1];
+      J[1][k] = 0.125f * o[2];
+      J[2][k] = 0.125f * o[3];
+    }
+    A[0][0] = (J[1][1] * J[2][2] - J[1][2] * J[2][1]);
+    A[1][0] = -(J[1][0] * J[2][2] - J[1][2] * J[2][0]);
+    A[2][0] = (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+    A[0][1] = -(J[0][1] * J[2][2] - J[0][2] * J[2][1]);
+    A[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]);
+    A[2][1] = -(J[0][0] * J[2][1] - J[0][1] * J[2][0]);
+    A[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]);
+    A[1][2] = -(J[0][0] * J[1][2] - J[0][2] * J[1][0]);
+    A[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]);
+    detJ = J[0][0] * A[0][0] + J[0][1] * A[1][0] + J[0][2] * A[2][0];
+  }
+  const float vol = detJ * 8.0f;
+  const MatF m = P.matf[P.emat ? __ldg(&P.emat[e]) : 0];
+  // velocity Walsh sums: G[m][k] (derivative directions), hm[k][j] (hourglass)
+  float G[3][3], hm[3][4];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    float v[8], o[8];
+#pragma unroll
+    for (int a = 0; a < 8; a++) v[a] = __ldg(&M.vp[k * np + nid[a]]);
+    walsh8(v, o);
+    G[0][k] = o[1];
+    G[1][k] = o[2];
+    G[2][k] = o[3];
+#pragma unroll
+    for (int j = 0; j < 4; j++) hm[k][j] = o[4 + j];
+  }
+  float J_avg = 0.f;
+#pragma unroll
+  for (int a = 0; a < 8; a++) J_avg += __ldg(&M.jr[nid[a]]);
+  // velocity gradient L[i][k] = d v_k / d x_i
+  const float fl = 0.125f / detJ;
+  float L[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int k = 0; k < 3; k++) L[i][k] = fl * (A[i][0] * G[0][k] + A[i][1] * G[1][k] + A[i][2] * G[2][k]);
+  const float sr[6] = {L[0][0], L[1][1], L[2][2], 0.5f * (L[1][0] + L[0][1]),
+                       0.5f * (L[2][1] + L[1][2]), 0.5f * (L[2][0] + L[0][2])};
+  const float w01 = 0.5f * (L[1][0] - L[0][1]);
+  const float w12 = 0.5f * (L[2][1] - L[1][2]);
+  const float w02 = 0.5f * (L[2][0] - L[0][2]);
+  float J_bar = J_avg * 0.125f;
+  if (J_bar < 0.0f) J_bar = 0.2f;
+  const float p = -m.K * (J_bar - 1.0f);
+  float sg[6];
+  stress_update(P, M, e, m, sr, w01, w12, w02, p, sg);
+  // sigma as a symmetric 3x3: S[i][k]
+  const float S[3][3] = {{sg[0], sg[3], sg[5]}, {sg[3], sg[1], sg[4]}, {sg[5], sg[4], sg[2]}};
+  const float ch = P.hg_on ? P.f_hg_coef * powf(vol, 0.6666666f) * m.rho * 0.25f * m.cs0 : 0.f;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    float o[8], f[8];
+    o[0] = 0.f;
+#pragma unroll
+    for (int mm = 0; mm < 3; mm++) o[1 + mm] = A[0][mm] * S[0][k] + A[1][mm] * S[1][k] + A[2][mm] * S[2][k];
+#pragma unroll
+    for (int j = 0; j < 4; j++) o[4 + j] = ch * hm[k][j];
+    walsh8_synth(o, f);
+    // SoA by (local node, component): fe[(a * 3 + k) * ne + e]
+#pragma unroll
+    for (int a = 0; a < 8; a++) M.fe[(a * 3 + k) * ne + e] = f[a];
+  }
+}
+
+// Tetrahedron: per-node shape derivatives (Domain_d.C:1866-1887).
+__device__ __forceinline__ void element_tet(const StepParams &P, const MixState &M, int64_t e) {
+  const int64_t ne = P.ne;
+  int32_t nid[4];
+  float dH[3][4];
+  float detJ;
+  {
+    float r[4][3];
+    rel_coords<4>(P, M, e, r, nid);
+    float J[3][3];
+    jacobian_f<4>(r, J);
+    shape_derivs_f<4>(J, dH);
+    detJ = det3f(J);
+  }
+  const MatF m = P.matf[P.emat ? __ldg(&P.emat[e]) : 0];
+  float s00 = 0.f, s11 = 0.f, s22 = 0.f, s01 = 0.f, s12 = 0.f, s02 = 0.f;
+  float w01 = 0.f, w12 = 0.f, w02 = 0.f;
+  float J_avg = 0.f;
+#pragma unroll
+  for (int a = 0; a < 4; a++) {
+    const float v0 = __ldg(&M.vp[nid[a]]);
+    const float v1 = __ldg(&M.vp[P.np + nid[a]]);
+    const float v2 = __ldg(&M.vp[2 * P.np + nid[a]]);
+    const float d0 = dH[0][a], d1 = dH[1][a], d2 = dH[2][a];
+    s00 += d0 * v0;
+    s11 += d1 * v1;
+    s22 += d2 * v2;
+    s01 += d1 * v0 + d0 * v1;
+    w01 += d1 * v0 - d0 * v1;
+    s12 += d2 * v1 + d1 * v2;
+    s02 += d2 * v0 + d0 * v2;
+    w12 += d2 * v1 - d1 * v2;
+    w02 += d2 * v0 - d0 * v2;
+    J_avg += __ldg(&M.jr[nid[a]]);
+  }
+  const float f = 1.0f / detJ;
+  const float fh = 0.5f * f;
+  const float sr[6] = {s00 * f, s11 * f, s22 * f, s01 * fh, s12 * fh, s02 * fh};
+  w01 *= fh; w12 *= fh; w02 *= fh;
+  J_avg *= 0.25f;
+  float J_bar = J_avg;
+  if (J_bar < 0.0f) J_bar = 0.2f;
+  const float p = -m.K * (J_bar - 1.0f);
+  float sg[6];
+  stress_update(P, M, e, m, sr, w01, w12, w02, p, sg);
+  const float w = weightf<4>();
+#pragma unroll
+  for (int a = 0; a < 4; a++) {
+    const float d0 = dH[0][a], d1 = dH[1][a], d2 = dH[2][a];
+    M.fe[(a * 3) * ne + e] = (d0 * sg[0] + d1 * sg[3] + d2 * sg[5]) * w;
+    M.fe[(a * 3 + 1) * ne + e] = (d1 * sg[1] + d0 * sg[3] + d2 * sg[4]) * w;
+    M.fe[(a * 3 + 2) * ne + e] = (d2 * sg[2] + d1 * sg[4] + d0 * sg[5]) * w;
+  }
+}
+
+template <int NPE>
+__device__ __forceinline__ void element_one(const StepParams &P, const MixState &M, int64_t e) {
+  if constexpr (NPE == 8)
+    element_hex(P, M, e);
+  else
+    element_tet(P, M, e);
+}
+
+// Registers per thread stay <= 64 at 1024 resident threads per SM.
+constexpr int elem_min_blocks(int bs) { return 1024 / bs; }
 
 template <int NPE, int BS>
 __global__ void __launch_bounds__(BS, elem_min_blocks(BS)) k_mix_elements(StepParams P,
