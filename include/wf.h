@@ -148,6 +148,15 @@ WF_API wf_status wf_set_artif_visc(wf_domain *d, double alpha, double beta); /* 
 /* 0: lumped mass recomputed each step from the current volume (reference
  * loop, Solver_explicit.C:605-607); 1: mass kept at its initial value. */
 WF_API wf_status wf_set_mass_mode(wf_domain *d, int32_t mode);
+/* Energy history (before wf_init; off by default): after every step the
+ * kinetic energy sum_n m_n |v_n|^2 / 2 and the internal energy accumulated
+ * as Eint += dt * sum_e (sigma_e . str_rate_e) vol_e over the six stored
+ * Voigt components (Domain_d::computeEnergies, Mechanical.C:2145-2185, called
+ * at Solver_explicit.C:1029-1031). Adds one reduction launch per step. */
+WF_API wf_status wf_set_energy_history(wf_domain *d, int32_t on);
+/* *n = steps recorded; copies min(cap, *n) values into each non-null array. */
+WF_API wf_status wf_get_energy_history(wf_domain *d, double *ekin, double *eint, int64_t cap,
+                                       int64_t *n);
 /* Reaction history: per step, sum over `nodes` of the assembled internal
  * force component `dim` (recorded after assembly). */
 WF_API wf_status wf_set_reaction_nodes(wf_domain *d, int64_t n, const int32_t *nodes, int32_t dim);

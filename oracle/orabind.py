@@ -84,6 +84,7 @@ def lib():
         "wfo_get_derivs": ([vp, _dp], None),
         "wfo_get_elem_forces": ([vp, _dp, _dp], None),
         "wfo_get_reaction": ([vp, _dp, i64], i64),
+        "wfo_get_energies": ([vp, _dp, _dp, i64], i64),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -266,6 +267,13 @@ class OracleDomain:
         fhg = np.zeros(ne * npe * 3)
         lib().wfo_get_elem_forces(self.h, f, fhg)
         return f.reshape(ne, npe, 3), fhg.reshape(ne, npe, 3)
+
+    def energies(self):
+        """(kinetic energy, accumulated internal energy) after each step."""
+        n = lib().wfo_get_energies(self.h, np.zeros(1), np.zeros(1), 0)
+        k, e = np.zeros(max(n, 1)), np.zeros(max(n, 1))
+        lib().wfo_get_energies(self.h, k, e, n)
+        return k[:n], e[:n]
 
     def reaction(self):
         n = lib().wfo_get_reaction(self.h, np.zeros(1), 0)

@@ -61,6 +61,8 @@ class RefDomain : public Domain_d {
   std::vector<int> reaction_nodes;
   int reaction_dim = 2;
   std::vector<double> reaction_hist;
+  std::vector<double> ekin_hist, eint_hist;  // computeEnergies after every step
+  double eint_acc = 0.0;
   long step_count = 0;
 
   void zero_uninitialised() {
@@ -227,6 +229,12 @@ class RefDomain : public Domain_d {
     UpdateCorrectionAccVel();
     ImposeBCVAllDim();
     UpdateCorrectionPos();
+    // end of the loop body (Solver_explicit.C:1029-1031)
+    double ekin = 0.0, deint = 0.0, devisc = 0.0;
+    computeEnergies(dt, ekin, deint, devisc);
+    eint_acc += deint;
+    ekin_hist.push_back(ekin);
+    eint_hist.push_back(eint_acc);
     Time += dt;
     step_count++;
   }
@@ -473,6 +481,17 @@ int wfr_get_reaction(void *h, double *out, int maxn) {
   if (n > maxn) n = maxn;
   for (int i = 0; i < n; i++) out[i] = d->reaction_hist[i];
   return (int)d->reaction_hist.size();
+}
+
+int wfr_get_energies(void *h, double *ekin, double *eint, int maxn) {
+  RefDomain *d = static_cast<RefDomain *>(h);
+  int n = (int)d->ekin_hist.size();
+  if (n > maxn) n = maxn;
+  for (int i = 0; i < n; i++) {
+    ekin[i] = d->ekin_hist[i];
+    eint[i] = d->eint_hist[i];
+  }
+  return (int)d->ekin_hist.size();
 }
 
 }  // extern "C"

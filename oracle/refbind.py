@@ -65,6 +65,7 @@ def lib():
         "wfr_get_derivs": ([vp, _dp], None),
         "wfr_get_elem_forces": ([vp, _dp, _dp], None),
         "wfr_get_reaction": ([vp, _dp, C.c_int], C.c_int),
+        "wfr_get_energies": ([vp, _dp, _dp, C.c_int], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -257,6 +258,13 @@ class RefDomain:
         fhg = np.zeros(n)
         lib().wfr_get_elem_forces(self.h, f, fhg)
         return f.reshape(self.ne, self.npe, 3), fhg.reshape(self.ne, self.npe, 3)
+
+    def energies(self):
+        """(kinetic energy, accumulated internal energy) after each step."""
+        n = lib().wfr_get_energies(self.h, np.zeros(1), np.zeros(1), 0)
+        k, e = np.zeros(max(n, 1)), np.zeros(max(n, 1))
+        lib().wfr_get_energies(self.h, k, e, n)
+        return k[:n], e[:n]
 
     def reaction(self):
         n = lib().wfr_get_reaction(self.h, np.zeros(1), 0)

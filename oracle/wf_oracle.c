@@ -48,6 +48,8 @@ struct wfo_domain {
   int64_t n_react;
   int react_dim;
   double *react_hist;
+  double *ekin_hist, *eint_hist;   /* computeEnergies after every step */
+  double eint;
   int64_t hist_len, hist_cap;
   /* rigid plane contact */
   int contact;
@@ -104,6 +106,8 @@ void wfo_destroy(wfo_domain *d) {
   free(d->mats);
   free(d->react_nodes);
   free(d->react_hist);
+  free(d->ekin_hist);
+  free(d->eint_hist);
   free(d);
 }
 
@@ -979,6 +983,7 @@ int wfo_init(wfo_domain *d) {
   d->time = 0.0;
   d->step_count = 0;
   d->hist_len = 0;
+  d->eint = 0.0;
   return 0;
 }
 
@@ -986,8 +991,31 @@ static void record_reaction(wfo_domain *d, double r) {
   if (d->hist_len == d->hist_cap) {
     d->hist_cap = d->hist_cap ? 2 * d->hist_cap : 1024;
     d->react_hist = realloc(d->react_hist, sizeof(double) * d->hist_cap);
+    d->ekin_hist = realloc(d->ekin_hist, sizeof(double) * d->hist_cap);
+    d->eint_hist = realloc(d->eint_hist, sizeof(double) * d->hist_cap);
   }
   d->react_hist[d->hist_len++] = r;
+}
+
+/* Domain_d::computeEnergies (Mechanical.C:2145-2185): kinetic energy of the
+ * end-of-step velocity with the step's lumped mass, and the internal energy
+ * increment dt * sum_e (sigma . str_rate) vol_e over the six stored Voigt
+ * components (shear terms counted once, as the reference does). Serial sums in
+ * node and element order. */
+static void compute_energies(const wfo_domain *d, double *ekin, double *deint) {
+  double k = 0.0;
+  for (int64_t n = 0; n < d->nn; n++) {
+    const double vx = d->v[3 * n], vy = d->v[3 * n + 1], vz = d->v[3 * n + 2];
+    k += 0.5 * d->mass[n] * (vx * vx + vy * vy + vz * vz);
+  }
+  double ed = 0.0;
+  for (int64_t e = 0; e < d->ne; e++) {
+    const double *s = &d->sigma[6 * e], *r = &d->str_rate[6 * e];
+    const double sdot = s[0] * r[0] + s[1] * r[1] + s[2] * r[2] + s[3] * r[3] + s[4] * r[4] + s[5] * r[5];
+    ed += sdot * d->vol[e];
+  }
+  *ekin = k;
+  *deint = ed * d->dt;
 }
 
 /* One iteration of the loop body of SolveChungHulbert, CPU branch with default
@@ -1025,6 +1053,13 @@ static void one_step(wfo_domain *d) {
   update_correction_acc_vel(d);
   for (int k = 0; k < 3; k++) impose_bcv(d, k);
   update_correction_pos(d);
+  {
+    double ekin, deint;
+    compute_energies(d, &ekin, &deint);
+    d->eint += deint;
+    d->ekin_hist[d->hist_len - 1] = ekin;
+    d->eint_hist[d->hist_len - 1] = d->eint;
+  }
   d->time += d->dt;
   d->step_count++;
 }
@@ -1085,5 +1120,12 @@ void wfo_get_elem_forces(const wfo_domain *d, double *f, double *fhg) {
 int64_t wfo_get_reaction(const wfo_domain *d, double *out, int64_t cap) {
   int64_t n = d->hist_len < cap ? d->hist_len : cap;
   if (out && n > 0) memcpy(out, d->react_hist, sizeof(double) * n);
+  return d->hist_len;
+}
+
+int64_t wfo_get_energies(const wfo_domain *d, double *ekin, double *eint, int64_t cap) {
+  int64_t n = d->hist_len < cap ? d->hist_len : cap;
+  if (ekin && n > 0) memcpy(ekin, d->ekin_hist, sizeof(double) * n);
+  if (eint && n > 0) memcpy(eint, d->eint_hist, sizeof(double) * n);
   return d->hist_len;
 }

@@ -84,6 +84,9 @@ int wfo_get_elem_tensor(const wfo_domain *d, int which, double *out);
 void wfo_get_derivs(const wfo_domain *d, double *out);
 void wfo_get_elem_forces(const wfo_domain *d, double *f, double *fhg);
 int64_t wfo_get_reaction(const wfo_domain *d, double *out, int64_t cap);
+/* Kinetic energy and accumulated internal energy after each step
+ * (Domain_d::computeEnergies, Mechanical.C:2145-2185; Solver_explicit.C:1029-1031). */
+int64_t wfo_get_energies(const wfo_domain *d, double *ekin, double *eint, int64_t cap);
 
 #ifdef __cplusplus
 }

@@ -99,6 +99,7 @@ def run_case(name, case, steps, mode, extra):
     )
     if mode == "step":
         res["reaction"] = d.reaction()
+        res["ekin"], res["eint"] = d.energies()
     np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **res)
     meta = dict(name=name, mode=mode, steps=steps, extra={k: list(v) if isinstance(v, tuple) else v
                                                            for k, v in extra.items()})

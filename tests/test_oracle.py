@@ -52,6 +52,10 @@ def test_oracle_matches_reference_fixture(name, case, steps, mode, extra):
         np.testing.assert_array_equal(val, g[key], err_msg=f"{name}: {key}")
     if "reaction" in g:
         np.testing.assert_array_equal(d.reaction(), g["reaction"])
+    if "ekin" in g:
+        ekin, eint = d.energies()
+        np.testing.assert_array_equal(ekin, g["ekin"])
+        np.testing.assert_array_equal(eint, g["eint"])
 
 
 @pytest.mark.skipif(not R.available(), reason="reference library oracle/_ref not built here")

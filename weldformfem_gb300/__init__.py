@@ -109,6 +109,8 @@ _SIGS = {
                              C.POINTER(C.c_double)],
     "wf_get_transfer_bytes": [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)],
     "wf_adjoint_forward": [C.c_void_p, C.c_int64, C.c_int64],
+    "wf_set_energy_history": [C.c_void_p, C.c_int32],
+    "wf_get_energy_history": [C.c_void_p, _dp, _dp, C.c_int64, C.POINTER(C.c_int64)],
     "wf_adjoint_backward": [C.c_void_p, _dp, C.c_int32, _dp],
     # allocation-free nodal volumes: device pointers in, device pointer out
     "wf_nodal_volumes_noalloc": [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_int32,
@@ -390,6 +392,17 @@ class Domain:
         out = np.zeros(self.ne * 6)
         self._call("wf_get_elem_tensor", ELEM_TENSOR[name], out)
         return out.reshape(-1, 6)
+
+    def set_energy_history(self, on=True):
+        self._call("wf_set_energy_history", int(bool(on)))
+
+    def energies(self):
+        """(kinetic energy, accumulated internal energy) after each step."""
+        n = C.c_int64()
+        self._call("wf_get_energy_history", np.zeros(1), np.zeros(1), 0, C.byref(n))
+        k, e = np.zeros(max(n.value, 1)), np.zeros(max(n.value, 1))
+        self._call("wf_get_energy_history", k, e, n.value, C.byref(n))
+        return k[: n.value], e[: n.value]
 
     def reaction(self):
         n = C.c_int64()

@@ -43,6 +43,7 @@ struct wf_domain {
   int precision = WF_FP64;
   double hg = 0.0;
   int press_alg = 0, mass_mode = 0;
+  bool energy = false;
   wf_stab stab{};
   double av[2] = {0.0, 0.0};
   std::vector<int32_t> react_nodes;
@@ -536,6 +537,13 @@ WF_API wf_status wf_set_mass_mode(wf_domain *d, int32_t mode) {
   return WF_OK;
 }
 
+WF_API wf_status wf_set_energy_history(wf_domain *d, int32_t on) {
+  if (!d) return WF_ERR_ARG;
+  if (d->initialized) return fail(d, WF_ERR_STATE, "the energy history is chosen before init");
+  d->energy = on != 0;
+  return WF_OK;
+}
+
 WF_API wf_status wf_set_reaction_nodes(wf_domain *d, int64_t n, const int32_t *nodes, int32_t dim) {
   wf_status s = need_mesh(d);
   if (s) return s;
@@ -761,6 +769,8 @@ WF_API wf_status wf_init(wf_domain *d) {
   }
   if (d->nspec && d->contact)
     return fail(d, WF_ERR_UNSUPPORTED, "contact is not supported in a batched ensemble");
+  if (d->nspec && d->energy)
+    return fail(d, WF_ERR_UNSUPPORTED, "the energy history is not kept for a batched ensemble");
   CUDA_TRY(cudaSetDevice(d->device));
   free_device(d);
   const int64_t nn = d->nn, ne = d->ne;
@@ -900,6 +910,12 @@ WF_API wf_status wf_init(wf_domain *d) {
   if (d->nspec) CUDA_TRY(dalloc(d, &P.hist_spec, (size_t)d->hist_cap * d->nspec));
   P.hist_cap = d->hist_cap;
   CUDA_TRY(dalloc(d, &P.st, 1));
+  if (d->energy) {
+    P.energy_on = 1;
+    CUDA_TRY(dalloc(d, &P.epart, 2 * (size_t)energy_grid(P)));
+    CUDA_TRY(dalloc(d, &P.ekin_hist, d->hist_cap));
+    CUDA_TRY(dalloc(d, &P.eint_hist, d->hist_cap));
+  }
 
   // FP64 state (also the export target of the mixed state)
   Fp64State &S = d->S;
@@ -972,6 +988,7 @@ WF_API wf_status wf_init(wf_domain *d) {
     CUDA_TRY(dalloc(d, &M.pls, ne));
     CUDA_TRY(dalloc(d, &M.tau, 6 * ne));
     CUDA_TRY(dalloc(d, &M.fe, (size_t)ne * d->npe * 3));
+    if (d->energy) CUDA_TRY(dalloc(d, &M.edot, ne));
     CUDA_TRY(dalloc(d, &d->mvol, ne));
     std::vector<MatF> mf(md.size());
     for (size_t i = 0; i < md.size(); i++) {
@@ -1029,6 +1046,12 @@ void launch_step(wf_domain *d) {
     mix_nodes(P, d->M, d->stream, d->node_grid);
   }
   if (P.nspec) spec_reaction(P, d->stream);
+  if (P.energy_on) {
+    if (d->precision == WF_FP64)
+      energy_fp64(P, d->S, d->stream);
+    else
+      energy_mixed(P, d->M, d->stream);
+  }
 }
 
 void launch_step_timed(wf_domain *d, cudaEvent_t *ev) {
@@ -1052,6 +1075,12 @@ void launch_step_timed(wf_domain *d, cudaEvent_t *ev) {
     mix_nodes(P, d->M, d->stream, d->node_grid);
   }
   if (P.nspec) spec_reaction(P, d->stream);
+  if (P.energy_on) {
+    if (d->precision == WF_FP64)
+      energy_fp64(P, d->S, d->stream);
+    else
+      energy_mixed(P, d->M, d->stream);
+  }
   cudaEventRecord(ev[4], d->stream);
 }
 
@@ -1119,6 +1148,15 @@ WF_API wf_status wf_run(wf_domain *d, int64_t nsteps) {
                                cudaMemcpyDeviceToDevice, d->stream));
       d->P.hist_spec = ns;
     }
+    if (d->P.energy_on) {
+      for (double **h : {&d->P.ekin_hist, &d->P.eint_hist}) {
+        double *nh2 = nullptr;
+        CUDA_TRY(dalloc(d, &nh2, cap));
+        CUDA_TRY(cudaMemcpyAsync(nh2, *h, sizeof(double) * d->hist_cap, cudaMemcpyDeviceToDevice,
+                                 d->stream));
+        *h = nh2;
+      }
+    }
     d->P.hist_cap = cap;
     d->hist_cap = cap;
     if (d->graph) {
@@ -1153,7 +1191,7 @@ WF_API wf_status wf_run(wf_domain *d, int64_t nsteps) {
     }
     left = 0;
   }
-  d->launches += (d->nspec ? 5 : 4) * nsteps;
+  d->launches += (4 + (d->nspec ? 1 : 0) + (d->P.energy_on ? 1 : 0)) * nsteps;
   if (left >= kGraphSteps) {
     wf_status s = ensure_graph(d);
     if (s) return s;
@@ -1368,6 +1406,29 @@ WF_API wf_status wf_get_reaction_history(wf_domain *d, double *out, int64_t cap,
   if (out && m > 0) {
     d->d2h_bytes += (int64_t)(sizeof(double) * m);
     CUDA_TRY(cudaMemcpyAsync(out, d->P.hist, sizeof(double) * m, cudaMemcpyDeviceToHost, d->stream));
+  }
+  CUDA_TRY(cudaStreamSynchronize(d->stream));
+  return WF_OK;
+}
+
+WF_API wf_status wf_get_energy_history(wf_domain *d, double *ekin, double *eint, int64_t cap,
+                                       int64_t *n) {
+  if (!d || !n) return WF_ERR_ARG;
+  if (!d->initialized) return fail(d, WF_ERR_STATE, "wf_init not called");
+  if (!d->P.energy_on) return fail(d, WF_ERR_STATE, "energy history not enabled before init");
+  CUDA_TRY(cudaSetDevice(d->device));
+  *n = d->host_step;
+  const int64_t m = std::min(cap, d->host_step);
+  if (m > 0) {
+    if (ekin) {
+      CUDA_TRY(cudaMemcpyAsync(ekin, d->P.ekin_hist, sizeof(double) * m, cudaMemcpyDeviceToHost,
+                               d->stream));
+    }
+    if (eint) {
+      CUDA_TRY(cudaMemcpyAsync(eint, d->P.eint_hist, sizeof(double) * m, cudaMemcpyDeviceToHost,
+                               d->stream));
+    }
+    d->d2h_bytes += (int64_t)(sizeof(double) * m * ((ekin ? 1 : 0) + (eint ? 1 : 0)));
   }
   CUDA_TRY(cudaStreamSynchronize(d->stream));
   return WF_OK;
@@ -1596,7 +1657,7 @@ WF_API wf_status wf_adjoint_backward(wf_domain *d, const double *dL_dR, int32_t 
     fp64_predict(P, S, d->stream);
     for (int64_t j = 0; j < L; j++) launch_step(d);
     CUDA_TRY(cudaGetLastError());
-    d->launches += 1 + 4 * L;
+    d->launches += 1 + (4 + (P.energy_on ? 1 : 0)) * L;
   }
   // per-material sums of the element gradients, in element order
   std::vector<double> g(3 * ne);

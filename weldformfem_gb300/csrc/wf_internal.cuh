@@ -37,6 +37,9 @@ struct StepState {
   unsigned int done_blocks;  // last-block-done counter of the node kernel
   unsigned int status;       // bit 0: a non-finite internal force was cleared
   long long first_bad_node;
+  double eint;               // accumulated internal energy (energy history)
+  unsigned int energy_blocks;  // last-block-done counter of the energy kernel
+  unsigned int pad;
 };
 
 // Node flags (uint8 per node).
@@ -95,6 +98,10 @@ struct StepParams {
   double *partials;       // [grid of the node kernel]
   double *hist;           // [hist_cap]
   int64_t hist_cap;
+  // energy history (Domain_d::computeEnergies after every step), when on
+  int32_t energy_on;
+  double *epart;          // [2 * grid of the energy kernel]
+  double *ekin_hist, *eint_hist;  // [hist_cap]
   StepState *st;
 };
 
@@ -121,6 +128,7 @@ struct MixState {
   float *tau;                     // [6][ne]
   float *fe;                      // [ne][npe][3] element force minus hourglass force
   double *x0;                     // [3][np] initial positions (export only)
+  float *edot;                    // [ne] sigma . str_rate * vol (energy history only)
 };
 
 // ---- FP64 launchers (wf_fp64.cu) ------------------------------------------
@@ -156,6 +164,11 @@ int mix_node_grid(int64_t nn);
 // ---- reductions (wf_reduce.cu) ---------------------------------------------
 // Per-specimen reaction sums of the step just completed (batched ensemble).
 void spec_reaction(const StepParams &P, cudaStream_t st);
+// Kinetic energy and internal-energy increment of the step just completed,
+// appended to the energy history (fixed-order reduction).
+int energy_grid(const StepParams &P);
+void energy_fp64(const StepParams &P, const Fp64State &S, cudaStream_t st);
+void energy_mixed(const StepParams &P, const MixState &M, cudaStream_t st);
 // Minimum element edge length over the mesh (exact: min is order-free).
 void min_edge_length(const int32_t *elnod, const double *x, int64_t np, int64_t ne, int npe,
                      double *out_dev, cudaStream_t st);

@@ -387,6 +387,9 @@ __device__ __forceinline__ void element_hex(const StepParams &P, const MixState 
   const float p = -m.K * (J_bar - 1.0f);
   float sg[6];
   stress_update(P, M, e, m, sr, w01, w12, w02, p, sg);
+  if (P.energy_on)
+    M.edot[e] = (sg[0] * sr[0] + sg[1] * sr[1] + sg[2] * sr[2] + sg[3] * sr[3] + sg[4] * sr[4] +
+                 sg[5] * sr[5]) * vol;
   // sigma as a symmetric 3x3: S[i][k]
   const float S[3][3] = {{sg[0], sg[3], sg[5]}, {sg[3], sg[1], sg[4]}, {sg[5], sg[4], sg[2]}};
   const float ch = P.hg_on ? P.f_hg_coef * powf(vol, 0.6666666f) * m.rho * 0.25f * m.cs0 : 0.f;
@@ -451,6 +454,9 @@ __device__ __forceinline__ void element_tet(const StepParams &P, const MixState 
   float sg[6];
   stress_update(P, M, e, m, sr, w01, w12, w02, p, sg);
   const float w = weightf<4>();
+  if (P.energy_on)
+    M.edot[e] = (sg[0] * sr[0] + sg[1] * sr[1] + sg[2] * sr[2] + sg[3] * sr[3] + sg[4] * sr[4] +
+                 sg[5] * sr[5]) * (detJ * w);
 #pragma unroll
   for (int a = 0; a < 4; a++) {
     const float d0 = dH[0][a], d1 = dH[1][a], d2 = dH[2][a];

@@ -1,4 +1,5 @@
-// Device reductions: minimum element edge length (CFL time-step rule).
+// Device reductions: minimum element edge length (CFL time-step rule),
+// per-specimen reaction sums and the energy history.
 #include <algorithm>
 #include <cstring>
 
@@ -64,7 +65,101 @@ __global__ void k_spec_reaction(StepParams P) {
   }
 }
 
+// Fixed-order block sum of doubles (shuffle tree per warp, warps in index
+// order); valid in thread 0. Callers separate two calls with __syncthreads.
+__device__ __forceinline__ double block_sum(double v, double *sh) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (threadIdx.x == 0)
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += sh[w];
+  return t;
+}
+
+// Domain_d::computeEnergies (Mechanical.C:2145-2185) at the end of the step
+// (Solver_explicit.C:1029-1031): Ekin = sum_n m_n |v_n|^2 / 2 and
+// dEint = dt * sum_e (sigma_e . str_rate_e) vol_e over the six stored Voigt
+// components, Eint += dEint. Block partials, then the last block to finish
+// sums them in block order: deterministic.
+template <class Item>
+__device__ __forceinline__ void energy_reduce(const StepParams &P, Item item) {
+  __shared__ double sh[kThreads / 32];
+  __shared__ bool am_last;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double k = 0.0, w = 0.0;
+  item(i, k, w);
+  const double kb = block_sum(k, sh);
+  __syncthreads();
+  const double wb = block_sum(w, sh);
+  if (threadIdx.x == 0) {
+    P.epart[2 * blockIdx.x] = kb;
+    P.epart[2 * blockIdx.x + 1] = wb;
+    __threadfence();
+    am_last = atomicAdd(&P.st->energy_blocks, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (am_last) {
+    __threadfence();
+    double tk = 0.0, tw = 0.0;
+    for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
+      tk += ((volatile double *)P.epart)[2 * b];
+      tw += ((volatile double *)P.epart)[2 * b + 1];
+    }
+    const double K = block_sum(tk, sh);
+    __syncthreads();
+    const double Wt = block_sum(tw, sh);
+    if (threadIdx.x == 0) {
+      const long long s = P.st->step - 1;  // advanced by this step's node kernel
+      const double eint = P.st->eint + Wt * P.dt;
+      P.st->eint = eint;
+      if (s >= 0 && s < P.hist_cap) {
+        P.ekin_hist[s] = K;
+        P.eint_hist[s] = eint;
+      }
+      P.st->energy_blocks = 0u;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) k_energy_fp64(StepParams P, Fp64State S) {
+  energy_reduce(P, [&](int64_t i, double &k, double &w) {
+    if (i < P.nn) {
+      const double vx = S.v[i], vy = S.v[P.np + i], vz = S.v[2 * P.np + i];
+      k = 0.5 * S.mass[i] * (vx * vx + vy * vy + vz * vz);
+    }
+    if (i < P.ne) {
+      const int64_t ne = P.ne;
+      double sdot = 0.0;
+      for (int c = 0; c < 6; c++) sdot += S.sig[c * ne + i] * S.sr[c * ne + i];
+      w = sdot * S.vol[i];
+    }
+  });
+}
+
+__global__ void __launch_bounds__(kThreads) k_energy_mixed(StepParams P, MixState M) {
+  energy_reduce(P, [&](int64_t i, double &k, double &w) {
+    if (i < P.nn) {
+      const double vx = M.v[i], vy = M.v[P.np + i], vz = M.v[2 * P.np + i];
+      k = 0.5 * (double)M.mass[i] * (vx * vx + vy * vy + vz * vz);
+    }
+    if (i < P.ne) w = (double)M.edot[i];
+  });
+}
+
 }  // namespace
+
+int energy_grid(const StepParams &P) {
+  return (int)((std::max(P.nn, P.ne) + kThreads - 1) / kThreads);
+}
+
+void energy_fp64(const StepParams &P, const Fp64State &S, cudaStream_t st) {
+  k_energy_fp64<<<energy_grid(P), kThreads, 0, st>>>(P, S);
+}
+
+void energy_mixed(const StepParams &P, const MixState &M, cudaStream_t st) {
+  k_energy_mixed<<<energy_grid(P), kThreads, 0, st>>>(P, M);
+}
 
 void spec_reaction(const StepParams &P, cudaStream_t st) {
   k_spec_reaction<<<P.nspec, 128, 0, st>>>(P);
