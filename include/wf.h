@@ -271,6 +271,58 @@ WF_API wf_status wf_adjoint_forward(wf_domain *d, int64_t nsteps, int64_t every)
 WF_API wf_status wf_adjoint_backward(wf_domain *d, const double *dL_dR, int32_t reverse_fp32,
                                      double *grad);
 
+/* ---- input files and output ------------------------------------------------------- */
+/* JSON deck of the reference's explicit driver (src/explicit/main.C:125-1005),
+ * read on the host into a deck object that wf_deck_apply replays on a domain.
+ * Read: Configuration (simTime, outTime, cflFactor, pressAlgorithm,
+ * artifViscCoeffs, xSymm/ySymm/zSymm, symtol), Stabilization, Materials[0]
+ * (Bilinear: const[0] = tangent modulus Et, H = E Et / (E - Et); Hollomon:
+ * const = [K, n]), DomainBlocks[0] (File: an LS-DYNA .k mesh, path relative to
+ * the deck; Box: a 3-D box of elemLength cells, elemType TriTet for
+ * tetrahedra) and BoundaryConditions (one velocity zone per condition, from
+ * its start/end box or, when it has none, from the DomainZones entry of its
+ * zoneId), then the symmetry-plane BCs, in the reference's order. The time
+ * step is cflFactor * (shortest segment between the first four nodes of each
+ * element) / sqrt(K / rho), the reference's calcMinEdgeLength in 3-D.
+ * Thermal, axisymmetric/plane-strain, Perzyna and rigid-body contact decks
+ * return WF_ERR_UNSUPPORTED. Configuration.hourglass3D (not a reference key,
+ * default 0 as the reference's 3-D no-op) sets the viscous hourglass
+ * coefficient. Errors are written into err (err_len bytes, may be null). */
+typedef struct wf_deck wf_deck;
+typedef struct {
+  int64_t nn, ne;        /* mesh */
+  int32_t npe;
+  int32_t press_alg;
+  int64_t n_bc;          /* AddBCVelNode calls: zone BCs (3 per node) then symmetry */
+  int64_t zone_nodes;    /* nodes inside the velocity zones, summed over zones */
+  int32_t n_zones;
+  int32_t has_stab;
+  double dt, end_time, out_time, cfl, min_length, sound_speed, hourglass;
+  double artif_visc[2];
+  wf_stab stab;
+  wf_material material;
+} wf_deck_info;
+WF_API wf_status wf_deck_read(const char *path, wf_deck **out, char *err, int64_t err_len);
+WF_API wf_status wf_deck_free(wf_deck *k);
+WF_API wf_status wf_deck_get_info(const wf_deck *k, wf_deck_info *info);
+/* xyz[3 nn] interleaved, elnod[ne npe]; either may be null. */
+WF_API wf_status wf_deck_get_mesh(const wf_deck *k, double *xyz, int32_t *elnod);
+/* The n_bc AddBCVelNode calls in order; any array may be null. */
+WF_API wf_status wf_deck_get_bcs(const wf_deck *k, int64_t *node, int32_t *dim, double *val);
+/* Mesh, material, BCs (then AllocateBCs), options, dt and end time onto d. */
+WF_API wf_status wf_deck_apply(const wf_deck *k, wf_domain *d);
+/* wf_deck_read + wf_deck_apply; info may be null. */
+WF_API wf_status wf_load_deck(wf_domain *d, const char *path, wf_deck_info *info, char *err,
+                              int64_t err_len);
+/* Domain_d::CreateFromLSDyna (Domain_d.C:1647-1699): *NODE and *ELEMENT_SOLID
+ * cards (fixed columns or comma-separated), nodes numbered in card order,
+ * elements with n5..n8 equal to n4 read as tetrahedra. */
+WF_API wf_status wf_load_lsdyna(wf_domain *d, const char *path);
+/* Legacy VTK file of the current state (VTKWriter.C field names: DISP,
+ * Velocity, Acceleration, ContForce, nod_mass; pressure, pl_strain, Vol, Rho,
+ * sigy, SIGMA). */
+WF_API wf_status wf_write_vtk(wf_domain *d, const char *path);
+
 /* ---- readback (host buffers) -------------------------------------------------- */
 WF_API wf_status wf_get_node_field(wf_domain *d, int32_t field, double *out);   /* 3*nn */
 WF_API wf_status wf_get_node_scalar(wf_domain *d, int32_t field, double *out);  /* nn */

@@ -48,6 +48,16 @@ class WfStab(C.Structure):
         "av_coeff_bulk", "log_factor", "pspg_scale", "p_pspg_bulkfac", "J_min")]
 
 
+class WfDeckInfo(C.Structure):
+    _fields_ = [("nn", C.c_int64), ("ne", C.c_int64), ("npe", C.c_int32),
+                ("press_alg", C.c_int32), ("n_bc", C.c_int64), ("zone_nodes", C.c_int64),
+                ("n_zones", C.c_int32), ("has_stab", C.c_int32), ("dt", C.c_double),
+                ("end_time", C.c_double), ("out_time", C.c_double), ("cfl", C.c_double),
+                ("min_length", C.c_double), ("sound_speed", C.c_double),
+                ("hourglass", C.c_double), ("artif_visc", C.c_double * 2), ("stab", WfStab),
+                ("material", WfMaterial)]
+
+
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 _ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
 _lp = np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")
@@ -109,6 +119,15 @@ _SIGS = {
                              C.POINTER(C.c_double)],
     "wf_get_transfer_bytes": [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)],
     "wf_adjoint_forward": [C.c_void_p, C.c_int64, C.c_int64],
+    "wf_deck_read": [C.c_char_p, C.POINTER(C.c_void_p), C.c_char_p, C.c_int64],
+    "wf_deck_free": [C.c_void_p],
+    "wf_deck_get_info": [C.c_void_p, C.POINTER(WfDeckInfo)],
+    "wf_deck_get_mesh": [C.c_void_p, _dp, _ip],
+    "wf_deck_get_bcs": [C.c_void_p, _lp, _ip, _dp],
+    "wf_deck_apply": [C.c_void_p, C.c_void_p],
+    "wf_load_deck": [C.c_void_p, C.c_char_p, C.POINTER(WfDeckInfo), C.c_char_p, C.c_int64],
+    "wf_load_lsdyna": [C.c_void_p, C.c_char_p],
+    "wf_write_vtk": [C.c_void_p, C.c_char_p],
     "wf_set_energy_history": [C.c_void_p, C.c_int32],
     "wf_get_energy_history": [C.c_void_p, _dp, _dp, C.c_int64, C.POINTER(C.c_int64)],
     "wf_adjoint_backward": [C.c_void_p, _dp, C.c_int32, _dp],
@@ -393,6 +412,22 @@ class Domain:
         self._call("wf_get_elem_tensor", ELEM_TENSOR[name], out)
         return out.reshape(-1, 6)
 
+    # input files and output ----------------------------------------------
+    def load_deck(self, path):
+        """Reads a JSON deck and sets this domain up from it; returns its info."""
+        info = WfDeckInfo()
+        err = C.create_string_buffer(512)
+        st = lib().wf_load_deck(self.h, os.fsencode(path), C.byref(info), err, 512)
+        if st != 0:
+            raise WfError(st, err.value.decode())
+        return Deck._info_dict(info)
+
+    def load_lsdyna(self, path):
+        self._call("wf_load_lsdyna", os.fsencode(path))
+
+    def write_vtk(self, path):
+        self._call("wf_write_vtk", os.fsencode(path))
+
     def set_energy_history(self, on=True):
         self._call("wf_set_energy_history", int(bool(on)))
 
@@ -410,3 +445,77 @@ class Domain:
         out = np.zeros(max(n.value, 1))
         self._call("wf_get_reaction_history", out, n.value, C.byref(n))
         return out[: n.value]
+
+
+class Deck:
+    """A JSON deck read on the host (wf_deck_read): the mesh, the material,
+    the ordered AddBCVelNode calls and the options, ready to be applied to a
+    GPU domain (apply) or to any backend with the same method names (setup)."""
+
+    def __init__(self, path):
+        h = C.c_void_p()
+        err = C.create_string_buffer(512)
+        st = lib().wf_deck_read(os.fsencode(path), C.byref(h), err, 512)
+        if st != 0:
+            raise WfError(st, err.value.decode())
+        self.h = h
+        info = WfDeckInfo()
+        lib().wf_deck_get_info(self.h, C.byref(info))
+        self.info = self._info_dict(info)
+
+    @staticmethod
+    def _info_dict(info):
+        out = {f: getattr(info, f) for f, _ in WfDeckInfo._fields_
+               if f not in ("artif_visc", "stab", "material")}
+        out["artif_visc"] = (info.artif_visc[0], info.artif_visc[1])
+        out["stab"] = [getattr(info.stab, f) for f, _ in WfStab._fields_]
+        m = info.material
+        out["material"] = {f: getattr(m, f) for f, _ in WfMaterial._fields_}
+        return out
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().wf_deck_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def mesh(self):
+        nn, ne, npe = self.info["nn"], self.info["ne"], self.info["npe"]
+        x = np.zeros(3 * nn)
+        el = np.zeros(ne * npe, np.int32)
+        lib().wf_deck_get_mesh(self.h, x, el)
+        return x.reshape(-1, 3), el.reshape(-1, npe)
+
+    def bcs(self):
+        n = self.info["n_bc"]
+        node, dim, val = np.zeros(max(n, 1), np.int64), np.zeros(max(n, 1), np.int32), np.zeros(max(n, 1))
+        lib().wf_deck_get_bcs(self.h, node, dim, val)
+        return node[:n], dim[:n], val[:n]
+
+    def apply(self, dom):
+        st = lib().wf_deck_apply(self.h, dom.h)
+        if st != 0:
+            raise WfError(st, lib().wf_last_error(dom.h).decode())
+
+    def setup(self, dom):
+        """The same calls as wf_deck_apply, through a backend's Python methods."""
+        x, el = self.mesh()
+        i = self.info
+        dom.set_mesh(x, el)
+        dom.set_materials([i["material"]])
+        dom.add_bcs(self.bcs())
+        if i["has_stab"]:
+            dom.set_stab(np.array(i["stab"]))
+        if i["press_alg"]:
+            dom.set_press_algorithm(i["press_alg"])
+        if any(i["artif_visc"]):
+            dom.set_artif_visc(*i["artif_visc"])
+        if i["hourglass"]:
+            dom.set_hourglass(i["hourglass"])
+        dom.set_dt(i["dt"])
+        dom.set_end_time(i["end_time"])

@@ -30,6 +30,7 @@ UNITS = {
     "wf_reduce.cu": [],
     "wf_noalloc.cu": ["--fmad=false"],
     "wf_adjoint.cu": [],
+    "wf_deck.cpp": [],
 }
 
 
@@ -61,7 +62,7 @@ def build(force: bool = False, verbose: bool = False, extra: list | None = None)
     extra = list(extra or [])
 
     def compile_one(unit):
-        obj = os.path.join(OBJ_DIR, unit.replace(".cu", ".o"))
+        obj = os.path.join(OBJ_DIR, os.path.splitext(unit)[0] + ".o")
         cmd = [nv] + COMMON + UNITS[unit] + extra + ["-c", os.path.join(CSRC, unit), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:

@@ -17,6 +17,74 @@
 #include "wf_adjoint.cuh"
 #include "wf_internal.cuh"
 
+
+namespace wf {
+
+// Structured box of Domain_d::AddBoxLength (Domain_d.C:1136-1504): nel =
+// floor(L / 2r) cells per axis, nodes x-fastest with coordinates formed by
+// repeated addition of 2r (:1215-1235), hexahedra in the same order
+// (:1316-1345) or six tetrahedra per cell (:1383-1388).
+bool box_mesh(const double V[3], const double L[3], double r, bool tritetra,
+              std::vector<double> &x, std::vector<int32_t> &elnod, std::string &err) {
+  int nel[3];
+  for (int k = 0; k < 3; k++) nel[k] = (int)(L[k] / (2.0 * r));
+  if (nel[0] <= 0 || nel[1] <= 0 || nel[2] <= 0) {
+    err = "box smaller than one element";
+    return false;
+  }
+  const int npe = tritetra ? 4 : 8;
+  const int64_t nn = (int64_t)(nel[0] + 1) * (nel[1] + 1) * (nel[2] + 1);
+  const int64_t ne = (int64_t)nel[0] * nel[1] * nel[2] * (tritetra ? 6 : 1);
+  if (ne * npe >= (int64_t)INT32_MAX) {
+    err = "mesh too large";
+    return false;
+  }
+  x.assign(3 * nn, 0.0);
+  int64_t p = 0;
+  double Xz = V[2];
+  for (int k = 0; k <= nel[2]; k++) {
+    double Xy = V[1];
+    for (int j = 0; j <= nel[1]; j++) {
+      double Xx = V[0];
+      for (int i = 0; i <= nel[0]; i++) {
+        x[3 * p] = Xx;
+        x[3 * p + 1] = Xy;
+        x[3 * p + 2] = Xz;
+        p++;
+        Xx = Xx + 2.0 * r;
+      }
+      Xy = Xy + 2.0 * r;
+    }
+    Xz = Xz + 2 * r;
+  }
+  elnod.assign(ne * npe, 0);
+  static const int T[6][4] = {{0, 1, 3, 5}, {1, 2, 3, 5}, {0, 5, 3, 4},
+                              {4, 5, 3, 7}, {5, 6, 3, 7}, {5, 2, 3, 6}};
+  const int64_t nnodz = (int64_t)(nel[0] + 1) * (nel[1] + 1);
+  int64_t ei = 0;
+  for (int ez = 0; ez < nel[2]; ez++)
+    for (int ey = 0; ey < nel[1]; ey++)
+      for (int ex = 0; ex < nel[0]; ex++) {
+        const int64_t nb1 = nnodz * ez + (int64_t)(nel[0] + 1) * ey + ex;
+        const int64_t nb2 = nnodz * ez + (int64_t)(nel[0] + 1) * (ey + 1) + ex;
+        const int32_t h[8] = {(int32_t)nb1, (int32_t)(nb1 + 1), (int32_t)(nb2 + 1),
+                              (int32_t)nb2, (int32_t)(nb1 + nnodz), (int32_t)(nb1 + nnodz + 1),
+                              (int32_t)(nb2 + nnodz + 1), (int32_t)(nb2 + nnodz)};
+        if (!tritetra) {
+          for (int a = 0; a < 8; a++) elnod[ei + a] = h[a];
+          ei += 8;
+        } else {
+          for (int t = 0; t < 6; t++) {
+            for (int a = 0; a < 4; a++) elnod[ei + a] = h[T[t][a]];
+            ei += 4;
+          }
+        }
+      }
+  return true;
+}
+
+}  // namespace wf
+
 using namespace wf;
 
 struct wf_domain {
@@ -208,6 +276,10 @@ wf_status need_mesh(wf_domain *d) {
 
 }  // namespace
 
+wf_status wf::domain_fail(wf_domain *d, wf_status s, const std::string &msg) {
+  return fail(d, s, "%s", msg.c_str());
+}
+
 // Definitions of the functions declared extern "C" in wf.h (C linkage is
 // inherited from those declarations).
 
@@ -266,57 +338,15 @@ WF_API wf_status wf_add_box_length(wf_domain *d, const double V[3], const double
   if (!red_int) return fail(d, WF_ERR_UNSUPPORTED, "only one-point (reduced) integration");
   if (!(L[2] > 0.0)) return fail(d, WF_ERR_UNSUPPORTED, "only 3-D boxes (L.z > 0)");
   if (!(r > 0.0)) return fail(d, WF_ERR_ARG, "r must be positive");
-  int nel[3];
-  for (int k = 0; k < 3; k++) nel[k] = (int)(L[k] / (2.0 * r));
-  if (nel[0] <= 0 || nel[1] <= 0 || nel[2] <= 0)
-    return fail(d, WF_ERR_ARG, "box smaller than one element");
   reset_mesh(d);
-  d->npe = tritetra ? 4 : 8;
-  d->nn = (int64_t)(nel[0] + 1) * (nel[1] + 1) * (nel[2] + 1);
-  d->ne = (int64_t)nel[0] * nel[1] * nel[2] * (tritetra ? 6 : 1);
-  if (d->ne * d->npe >= (int64_t)INT32_MAX) return fail(d, WF_ERR_ARG, "mesh too large");
-  d->x.resize(3 * d->nn);
-  // coordinates by repeated addition of 2r (Domain_d.C:1215-1235)
-  int64_t p = 0;
-  double Xz = V[2];
-  for (int k = 0; k <= nel[2]; k++) {
-    double Xy = V[1];
-    for (int j = 0; j <= nel[1]; j++) {
-      double Xx = V[0];
-      for (int i = 0; i <= nel[0]; i++) {
-        d->x[3 * p] = Xx;
-        d->x[3 * p + 1] = Xy;
-        d->x[3 * p + 2] = Xz;
-        p++;
-        Xx = Xx + 2.0 * r;
-      }
-      Xy = Xy + 2.0 * r;
-    }
-    Xz = Xz + 2 * r;
+  std::string err;
+  if (!wf::box_mesh(V, L, r, tritetra != 0, d->x, d->elnod, err)) {
+    d->nn = d->ne = 0;
+    return fail(d, WF_ERR_ARG, "%s", err.c_str());
   }
-  d->elnod.resize(d->ne * d->npe);
-  static const int T[6][4] = {{0, 1, 3, 5}, {1, 2, 3, 5}, {0, 5, 3, 4},
-                              {4, 5, 3, 7}, {5, 6, 3, 7}, {5, 2, 3, 6}};
-  const int64_t nnodz = (int64_t)(nel[0] + 1) * (nel[1] + 1);
-  int64_t ei = 0;
-  for (int ez = 0; ez < nel[2]; ez++)
-    for (int ey = 0; ey < nel[1]; ey++)
-      for (int ex = 0; ex < nel[0]; ex++) {
-        const int64_t nb1 = nnodz * ez + (int64_t)(nel[0] + 1) * ey + ex;
-        const int64_t nb2 = nnodz * ez + (int64_t)(nel[0] + 1) * (ey + 1) + ex;
-        const int32_t h[8] = {(int32_t)nb1, (int32_t)(nb1 + 1), (int32_t)(nb2 + 1),
-                              (int32_t)nb2, (int32_t)(nb1 + nnodz), (int32_t)(nb1 + nnodz + 1),
-                              (int32_t)(nb2 + nnodz + 1), (int32_t)(nb2 + nnodz)};
-        if (!tritetra) {
-          for (int a = 0; a < 8; a++) d->elnod[ei + a] = h[a];
-          ei += 8;
-        } else {
-          for (int t = 0; t < 6; t++) {
-            for (int a = 0; a < 4; a++) d->elnod[ei + a] = h[T[t][a]];
-            ei += 4;
-          }
-        }
-      }
+  d->npe = tritetra ? 4 : 8;
+  d->nn = (int64_t)(d->x.size() / 3);
+  d->ne = (int64_t)(d->elnod.size() / d->npe);
   build_nodel(d);
   return WF_OK;
 }

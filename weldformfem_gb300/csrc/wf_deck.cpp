@@ -1,0 +1,833 @@
+// Input-file front-end of the reference's explicit driver and its result
+// writer, as host code above the C ABI:
+//  * JSON decks (src/explicit/main.C:125-1005): a deck is read into a host
+//    object (mesh, material, the ordered list of AddBCVelNode calls, options,
+//    time step) that can be inspected and then applied to a domain;
+//  * LS-DYNA keyword meshes, *NODE and *ELEMENT_SOLID
+//    (Domain_d::CreateFromLSDyna, Domain_d.C:1647-1699);
+//  * legacy VTK output (VTKWriter.C) of a domain's current state.
+// Everything reaches the domain through the public wf_* entry points.
+#include <algorithm>
+#include <array>
+#include <cctype>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+#include <string>
+#include <unordered_map>
+#include <utility>
+#include <vector>
+
+#include "wf.h"
+#include "wf_internal.cuh"
+
+namespace {
+
+// ---- JSON ---------------------------------------------------------------------
+struct JVal {
+  enum Kind { Null, Bool, Num, Str, Arr, Obj } kind = Null;
+  bool b = false;
+  double num = 0.0;
+  std::string str;
+  std::vector<JVal> arr;
+  std::vector<std::pair<std::string, JVal>> obj;
+
+  const JVal *get(const char *key) const {
+    if (kind != Obj) return nullptr;
+    for (const auto &kv : obj)
+      if (kv.first == key) return &kv.second;
+    return nullptr;
+  }
+  const JVal *at(size_t i) const { return (kind == Arr && i < arr.size()) ? &arr[i] : nullptr; }
+};
+
+// Recursive-descent parser of RFC 8259 JSON (UTF-8 passed through; \u escapes
+// of the Basic Multilingual Plane encoded as UTF-8). Nesting is limited.
+class JParser {
+ public:
+  explicit JParser(const std::string &s) : s_(s) {}
+  std::string err;
+
+  bool parse(JVal &out) {
+    ws();
+    if (!value(out, 0)) return false;
+    ws();
+    if (i_ != s_.size()) return fail("trailing characters after the top-level value");
+    return true;
+  }
+
+ private:
+  const std::string &s_;
+  size_t i_ = 0;
+  int line_ = 1;
+
+  bool fail(const std::string &m) {
+    err = "line " + std::to_string(line_) + ": " + m;
+    return false;
+  }
+  void ws() {
+    while (i_ < s_.size() && std::isspace((unsigned char)s_[i_])) {
+      if (s_[i_] == '\n') line_++;
+      i_++;
+    }
+  }
+  bool lit(const char *w) {
+    const size_t n = std::strlen(w);
+    if (s_.compare(i_, n, w) != 0) return false;
+    i_ += n;
+    return true;
+  }
+  bool value(JVal &v, int depth) {
+    if (depth > 128) return fail("nesting too deep");
+    if (i_ >= s_.size()) return fail("unexpected end of input");
+    const char c = s_[i_];
+    if (c == '{') return object(v, depth);
+    if (c == '[') return array(v, depth);
+    if (c == '"') {
+      v.kind = JVal::Str;
+      return string(v.str);
+    }
+    if (lit("true")) {
+      v.kind = JVal::Bool;
+      v.b = true;
+      return true;
+    }
+    if (lit("false")) {
+      v.kind = JVal::Bool;
+      v.b = false;
+      return true;
+    }
+    if (lit("null")) {
+      v.kind = JVal::Null;
+      return true;
+    }
+    return number(v);
+  }
+  bool number(JVal &v) {
+    const size_t b = i_;
+    if (i_ < s_.size() && (s_[i_] == '-' || s_[i_] == '+')) i_++;
+    while (i_ < s_.size() &&
+           (std::isdigit((unsigned char)s_[i_]) || s_[i_] == '.' || s_[i_] == 'e' ||
+            s_[i_] == 'E' || s_[i_] == '-' || s_[i_] == '+'))
+      i_++;
+    if (i_ == b) return fail(std::string("unexpected character '") + s_[b] + "'");
+    const std::string t = s_.substr(b, i_ - b);
+    char *end = nullptr;
+    v.num = std::strtod(t.c_str(), &end);
+    if (!end || *end != '\0') return fail("malformed number '" + t + "'");
+    v.kind = JVal::Num;
+    return true;
+  }
+  static void utf8(std::string &o, unsigned cp) {
+    if (cp < 0x80) {
+      o += (char)cp;
+    } else if (cp < 0x800) {
+      o += (char)(0xC0 | (cp >> 6));
+      o += (char)(0x80 | (cp & 0x3F));
+    } else {
+      o += (char)(0xE0 | (cp >> 12));
+      o += (char)(0x80 | ((cp >> 6) & 0x3F));
+      o += (char)(0x80 | (cp & 0x3F));
+    }
+  }
+  bool string(std::string &o) {
+    i_++;  // opening quote
+    o.clear();
+    while (i_ < s_.size()) {
+      const char c = s_[i_++];
+      if (c == '"') return true;
+      if (c == '\n') return fail("newline inside a string");
+      if (c != '\\') {
+        o += c;
+        continue;
+      }
+      if (i_ >= s_.size()) break;
+      const char e = s_[i_++];
+      switch (e) {
+        case '"': o += '"'; break;
+        case '\\': o += '\\'; break;
+        case '/': o += '/'; break;
+        case 'b': o += '\b'; break;
+        case 'f': o += '\f'; break;
+        case 'n': o += '\n'; break;
+        case 'r': o += '\r'; break;
+        case 't': o += '\t'; break;
+        case 'u': {
+          if (i_ + 4 > s_.size()) return fail("short \\u escape");
+          unsigned cp = 0;
+          for (int k = 0; k < 4; k++) {
+            const char h = s_[i_++];
+            cp <<= 4;
+            if (h >= '0' && h <= '9') cp |= (unsigned)(h - '0');
+            else if (h >= 'a' && h <= 'f') cp |= (unsigned)(h - 'a' + 10);
+            else if (h >= 'A' && h <= 'F') cp |= (unsigned)(h - 'A' + 10);
+            else return fail("bad \\u escape");
+          }
+          utf8(o, cp);
+          break;
+        }
+        default: return fail(std::string("bad escape \\") + e);
+      }
+    }
+    return fail("unterminated string");
+  }
+  bool array(JVal &v, int depth) {
+    v.kind = JVal::Arr;
+    i_++;
+    ws();
+    if (i_ < s_.size() && s_[i_] == ']') {
+      i_++;
+      return true;
+    }
+    for (;;) {
+      v.arr.emplace_back();
+      ws();
+      if (!value(v.arr.back(), depth + 1)) return false;
+      ws();
+      if (i_ >= s_.size()) return fail("unterminated array");
+      if (s_[i_] == ',') {
+        i_++;
+        continue;
+      }
+      if (s_[i_] == ']') {
+        i_++;
+        return true;
+      }
+      return fail("expected ',' or ']' in array");
+    }
+  }
+  bool object(JVal &v, int depth) {
+    v.kind = JVal::Obj;
+    i_++;
+    ws();
+    if (i_ < s_.size() && s_[i_] == '}') {
+      i_++;
+      return true;
+    }
+    for (;;) {
+      ws();
+      if (i_ >= s_.size() || s_[i_] != '"') return fail("expected a member name");
+      std::string key;
+      if (!string(key)) return false;
+      ws();
+      if (i_ >= s_.size() || s_[i_] != ':') return fail("expected ':' after \"" + key + "\"");
+      i_++;
+      ws();
+      v.obj.emplace_back(key, JVal());
+      if (!value(v.obj.back().second, depth + 1)) return false;
+      ws();
+      if (i_ >= s_.size()) return fail("unterminated object");
+      if (s_[i_] == ',') {
+        i_++;
+        continue;
+      }
+      if (s_[i_] == '}') {
+        i_++;
+        return true;
+      }
+      return fail("expected ',' or '}' in object");
+    }
+  }
+};
+
+// readValue / readVector of the reference driver: set only when present.
+bool jnum(const JVal *o, const char *k, double &out) {
+  const JVal *v = o ? o->get(k) : nullptr;
+  if (!v) return false;
+  if (v->kind == JVal::Num) out = v->num;
+  else if (v->kind == JVal::Bool) out = v->b ? 1.0 : 0.0;
+  else return false;
+  return true;
+}
+bool jint(const JVal *o, const char *k, int &out) {
+  double t;
+  if (!jnum(o, k, t)) return false;
+  out = (int)t;
+  return true;
+}
+bool jbool(const JVal *o, const char *k, bool &out) {
+  const JVal *v = o ? o->get(k) : nullptr;
+  if (!v) return false;
+  if (v->kind == JVal::Bool) out = v->b;
+  else if (v->kind == JVal::Num) out = v->num != 0.0;
+  else return false;
+  return true;
+}
+bool jstr(const JVal *o, const char *k, std::string &out) {
+  const JVal *v = o ? o->get(k) : nullptr;
+  if (!v || v->kind != JVal::Str) return false;
+  out = v->str;
+  return true;
+}
+// Up to n numbers of an array member (missing entries keep their value).
+bool jvec(const JVal *o, const char *k, double *out, int n) {
+  const JVal *v = o ? o->get(k) : nullptr;
+  if (!v || v->kind != JVal::Arr) return false;
+  for (int i = 0; i < n && i < (int)v->arr.size(); i++)
+    if (v->arr[i].kind == JVal::Num) out[i] = v->arr[i].num;
+  return true;
+}
+
+bool read_file(const std::string &path, std::string &out) {
+  std::ifstream f(path, std::ios::binary);
+  if (!f) return false;
+  std::ostringstream ss;
+  ss << f.rdbuf();
+  out = ss.str();
+  return true;
+}
+
+std::string dir_of(const std::string &p) {
+  const size_t k = p.find_last_of("/\\");
+  return k == std::string::npos ? std::string() : p.substr(0, k + 1);
+}
+
+// ---- LS-DYNA keyword mesh -------------------------------------------------------
+struct KMesh {
+  std::vector<double> x;          // [3 nn]
+  std::vector<int32_t> elnod;     // [ne npe]
+  int npe = 0;
+};
+
+std::string trim(const std::string &s) {
+  size_t a = 0, b = s.size();
+  while (a < b && std::isspace((unsigned char)s[a])) a++;
+  while (b > a && std::isspace((unsigned char)s[b - 1])) b--;
+  return s.substr(a, b - a);
+}
+
+// Fields of a data card: comma-separated (free format) or the fixed columns
+// given by `widths`; a fixed-column card whose fields do not parse falls back
+// to whitespace separation.
+std::vector<std::string> card_fields(const std::string &line, const std::vector<int> &widths) {
+  std::vector<std::string> f;
+  if (line.find(',') != std::string::npos) {
+    std::stringstream ss(line);
+    std::string t;
+    while (std::getline(ss, t, ',')) f.push_back(trim(t));
+    return f;
+  }
+  size_t pos = 0;
+  bool ok = true;
+  for (int w : widths) {
+    if (pos >= line.size()) break;
+    const std::string t = trim(line.substr(pos, w));
+    if (!t.empty() && t.find(' ') != std::string::npos) ok = false;
+    f.push_back(t);
+    pos += w;
+  }
+  if (ok && pos >= line.size()) return f;
+  if (ok && trim(line.substr(std::min(pos, line.size()))).empty()) return f;
+  f.clear();
+  std::stringstream ss(line);
+  std::string t;
+  while (ss >> t) f.push_back(t);
+  return f;
+}
+
+bool to_long(const std::string &t, long long &v) {
+  if (t.empty()) return false;
+  char *end = nullptr;
+  v = std::strtoll(t.c_str(), &end, 10);
+  return end && *end == '\0';
+}
+bool to_double(const std::string &t, double &v) {
+  if (t.empty()) {
+    v = 0.0;
+    return true;
+  }
+  char *end = nullptr;
+  v = std::strtod(t.c_str(), &end);
+  return end && *end == '\0';
+}
+
+// *NODE cards: nid (8), x y z (16 each), tc rc (8); *ELEMENT_SOLID cards:
+// eid pid n1..n8 (8 each). Nodes are numbered in the order of their cards;
+// an element whose n5..n8 are absent or all equal to n4 is a tetrahedron
+// (the keyword format's degenerate-hexahedron convention). All elements must
+// have the same node count.
+bool read_lsdyna(const std::string &path, KMesh &m, std::string &err) {
+  std::string text;
+  if (!read_file(path, text)) {
+    err = "cannot open " + path;
+    return false;
+  }
+  std::stringstream in(text);
+  std::string line, kw;
+  std::vector<long long> nid;
+  std::vector<std::array<long long, 8>> el;
+  std::vector<int> elnpe;
+  int lineno = 0;
+  const std::vector<int> node_w = {8, 16, 16, 16, 8, 8};
+  const std::vector<int> elem_w = {8, 8, 8, 8, 8, 8, 8, 8, 8, 8};
+  while (std::getline(in, line)) {
+    lineno++;
+    if (!line.empty() && line.back() == '\r') line.pop_back();
+    if (line.empty() || line[0] == '$') continue;
+    if (line[0] == '*') {
+      std::string k = trim(line.substr(1));
+      const size_t sp = k.find_first_of(" \t");
+      if (sp != std::string::npos) k = k.substr(0, sp);
+      for (auto &c : k) c = (char)std::toupper((unsigned char)c);
+      kw = k;
+      if (kw.rfind("ELEMENT_SOLID", 0) == 0 && kw != "ELEMENT_SOLID") {
+        err = "unsupported keyword *" + kw + " (line " + std::to_string(lineno) + ")";
+        return false;
+      }
+      continue;
+    }
+    if (trim(line).empty()) continue;
+    if (kw == "NODE") {
+      const auto f = card_fields(line, node_w);
+      long long id;
+      double xyz[3] = {0, 0, 0};
+      if (f.empty() || !to_long(f[0], id)) {
+        err = "bad *NODE card at line " + std::to_string(lineno);
+        return false;
+      }
+      for (int k = 0; k < 3; k++)
+        if (k + 1 < (int)f.size() && !to_double(f[k + 1], xyz[k])) {
+          err = "bad coordinate at line " + std::to_string(lineno);
+          return false;
+        }
+      nid.push_back(id);
+      m.x.insert(m.x.end(), xyz, xyz + 3);
+    } else if (kw == "ELEMENT_SOLID") {
+      const auto f = card_fields(line, elem_w);
+      std::array<long long, 8> n{};
+      int cnt = 0;
+      for (size_t k = 2; k < f.size() && cnt < 8; k++) {
+        long long v;
+        if (f[k].empty()) break;
+        if (!to_long(f[k], v)) {
+          err = "bad *ELEMENT_SOLID card at line " + std::to_string(lineno);
+          return false;
+        }
+        if (v == 0) break;
+        n[cnt++] = v;
+      }
+      if (cnt != 4 && cnt != 8) {
+        err = "element with " + std::to_string(cnt) + " nodes at line " + std::to_string(lineno);
+        return false;
+      }
+      int npe = cnt;
+      if (cnt == 8 && n[4] == n[3] && n[5] == n[3] && n[6] == n[3] && n[7] == n[3]) npe = 4;
+      el.push_back(n);
+      elnpe.push_back(npe);
+    }
+  }
+  if (nid.empty() || el.empty()) {
+    err = path + ": no *NODE or *ELEMENT_SOLID data";
+    return false;
+  }
+  m.npe = elnpe[0];
+  for (int p : elnpe)
+    if (p != m.npe) {
+      err = "mixed tetrahedra and hexahedra are not supported";
+      return false;
+    }
+  std::unordered_map<long long, int32_t> index;
+  index.reserve(nid.size() * 2);
+  for (size_t k = 0; k < nid.size(); k++)
+    if (!index.emplace(nid[k], (int32_t)k).second) {
+      err = "duplicate node id " + std::to_string(nid[k]);
+      return false;
+    }
+  m.elnod.resize(el.size() * m.npe);
+  for (size_t e = 0; e < el.size(); e++)
+    for (int a = 0; a < m.npe; a++) {
+      auto it = index.find(el[e][a]);
+      if (it == index.end()) {
+        err = "element " + std::to_string(e + 1) + " references unknown node " +
+              std::to_string(el[e][a]);
+        return false;
+      }
+      m.elnod[e * m.npe + a] = it->second;
+    }
+  return true;
+}
+
+// Domain_d::calcMinEdgeLength in 3-D (Domain_d.C:2224-2469): every element is
+// read as a tetrahedron of its first four nodes and the six segments between
+// them are measured.
+double ref_min_length(const std::vector<double> &x, const std::vector<int32_t> &elnod, int npe) {
+  double mn = 1.0e6;
+  const size_t ne = elnod.size() / npe;
+  for (size_t e = 0; e < ne; e++) {
+    const int32_t *n = &elnod[e * npe];
+    const int pr[6][2] = {{1, 0}, {2, 0}, {3, 0}, {2, 1}, {3, 1}, {3, 2}};
+    for (const auto &p : pr) {
+      const double dx = x[3 * n[p[0]]] - x[3 * n[p[1]]];
+      const double dy = x[3 * n[p[0]] + 1] - x[3 * n[p[1]] + 1];
+      const double dz = x[3 * n[p[0]] + 2] - x[3 * n[p[1]] + 2];
+      const double len = std::sqrt(dx * dx + dy * dy + dz * dz);
+      if (len < mn) mn = len;
+    }
+  }
+  return mn;
+}
+
+}  // namespace
+
+// ---- deck object ---------------------------------------------------------------------
+struct wf_deck {
+  wf_deck_info info{};
+  std::vector<double> x;
+  std::vector<int32_t> elnod;
+  std::vector<int64_t> bc_node;
+  std::vector<int32_t> bc_dim;
+  std::vector<double> bc_val;
+};
+
+namespace {
+
+wf_status deck_fail(char *err, int64_t len, const std::string &m, wf_status s = WF_ERR_ARG) {
+  if (err && len > 0) {
+    std::strncpy(err, m.c_str(), (size_t)len - 1);
+    err[len - 1] = '\0';
+  }
+  return s;
+}
+
+}  // namespace
+
+WF_API wf_status wf_deck_read(const char *path, wf_deck **out, char *err, int64_t err_len) {
+  if (!path || !out) return WF_ERR_ARG;
+  *out = nullptr;
+  std::string text;
+  if (!read_file(path, text)) return deck_fail(err, err_len, std::string("cannot open ") + path);
+  JVal j;
+  JParser jp(text);
+  if (!jp.parse(j)) return deck_fail(err, err_len, std::string(path) + ": " + jp.err);
+  if (j.kind != JVal::Obj) return deck_fail(err, err_len, "the deck is not a JSON object");
+  wf_deck *k = new wf_deck();
+  wf_deck_info &I = k->info;
+  auto bad = [&](const std::string &m, wf_status s = WF_ERR_ARG) {
+    delete k;
+    return deck_fail(err, err_len, m, s);
+  };
+  const JVal *config = j.get("Configuration");
+  const JVal *stab = j.get("Stabilization");
+  const JVal *mats = j.get("Materials");
+  const JVal *blocks = j.get("DomainBlocks");
+  const JVal *zones = j.get("DomainZones");
+  const JVal *bcs = j.get("BoundaryConditions");
+  const JVal *rig = j.get("RigidBodies");
+
+  // Configuration (main.C:214-330)
+  I.cfl = 0.3;
+  jnum(config, "simTime", I.end_time);
+  jnum(config, "outTime", I.out_time);
+  jnum(config, "cflFactor", I.cfl);
+  jint(config, "pressAlgorithm", I.press_alg);
+  if (I.press_alg < 0) I.press_alg = 0;
+  {
+    double av[3] = {0, 0, 0};
+    jvec(config, "artifViscCoeffs", av, 3);
+    I.artif_visc[0] = av[0];
+    I.artif_visc[1] = av[1];
+  }
+  bool sym[3] = {false, false, false};
+  double symtol = 1.0e-4;
+  jbool(config, "xSymm", sym[0]);
+  jbool(config, "ySymm", sym[1]);
+  jbool(config, "zSymm", sym[2]);
+  jnum(config, "symtol", symtol);
+  bool thermal = false;
+  jbool(config, "thermal", thermal);
+  if (thermal) return bad("thermal coupling is not supported", WF_ERR_UNSUPPORTED);
+  std::string s;
+  if (jstr(config, "plasticType", s) && s != "Hardening")
+    return bad("plasticType " + s + " is not supported", WF_ERR_UNSUPPORTED);
+  if (jstr(config, "domType", s) && s != "3D")
+    return bad("domType " + s + " is not supported (3-D only)", WF_ERR_UNSUPPORTED);
+  jnum(config, "hourglass3D", I.hourglass);
+
+  // Stabilization (loadStabilizationParams, main.C:84-118)
+  if (stab && stab->kind == JVal::Obj) {
+    I.has_stab = 1;
+    jnum(stab, "alpha_free", I.stab.alpha_free);
+    jnum(stab, "alpha_contact", I.stab.alpha_contact);
+    jnum(stab, "hg_coeff_free", I.stab.hg_coeff_free);
+    jnum(stab, "hg_coeff_contact", I.stab.hg_coeff_contact);
+    jnum(stab, "av_coeff_div", I.stab.av_coeff_div);
+    jnum(stab, "av_coeff_bulk", I.stab.av_coeff_bulk);
+    jnum(stab, "log_factor", I.stab.log_factor);
+    jnum(stab, "p_pspg_bulkfac", I.stab.p_pspg_bulkfac);
+    jnum(stab, "J_min", I.stab.J_min);
+  }
+
+  // Materials[0] (main.C:441-575)
+  const JVal *m0 = mats ? mats->at(0) : nullptr;
+  if (!m0) return bad("no Materials entry");
+  wf_material &M = I.material;
+  M = wf_material{};
+  jnum(m0, "density0", M.rho);
+  jnum(m0, "youngsModulus", M.E);
+  jnum(m0, "poissonsRatio", M.nu);
+  jnum(m0, "yieldStress0", M.sy0);
+  double c[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+  jvec(m0, "const", c, 10);
+  std::string mtype = "Bilinear";
+  jstr(m0, "type", mtype);
+  if (!(M.E > 0.0) || !(M.rho > 0.0)) return bad("material needs youngsModulus > 0 and density0 > 0");
+  if (mtype == "Bilinear") {
+    // plastic modulus from the tangent modulus const[0] (main.C:489)
+    M.model = WF_MAT_BILINEAR;
+    M.H = M.E * c[0] / (M.E - c[0]);
+  } else if (mtype == "Hollomon") {
+    M.model = WF_MAT_HOLLOMON;
+    M.hol_K = c[0];
+    M.hol_m = c[1];
+  } else {
+    return bad("material type " + mtype + " is not supported", WF_ERR_UNSUPPORTED);
+  }
+
+  // DomainBlocks[0] (main.C:350-430)
+  const JVal *b0 = blocks ? blocks->at(0) : nullptr;
+  if (!b0) return bad("no DomainBlocks entry");
+  std::string btype = "Box";
+  jstr(b0, "type", btype);
+  if (btype == "File") {
+    std::string fname;
+    if (!jstr(b0, "fileName", fname)) return bad("File block without fileName");
+    const std::string ext = fname.substr(fname.find_last_of('.') + 1);
+    if (ext != "k") return bad("mesh file " + fname + ": only LS-DYNA .k meshes are read",
+                               WF_ERR_UNSUPPORTED);
+    std::string full = dir_of(path) + fname;
+    if (!fname.empty() && fname[0] == '/') full = fname;
+    std::ifstream probe(full);
+    if (!probe) full = fname;
+    KMesh km;
+    std::string e;
+    if (!read_lsdyna(full, km, e)) return bad(e);
+    k->x.swap(km.x);
+    k->elnod.swap(km.elnod);
+    I.npe = km.npe;
+  } else if (btype == "Box") {
+    double L[3] = {0, 0, 0}, V[3] = {0, 0, 0}, dx = 0.06;
+    jvec(b0, "dim", L, 3);
+    jvec(b0, "start", V, 3);
+    jnum(b0, "elemLength", dx);
+    std::string et;
+    jstr(b0, "elemType", et);
+    const bool tet = et == "TriTet";
+    if (!(L[2] > 0.0)) return bad("Box block: only 3-D boxes (dim[2] > 0)", WF_ERR_UNSUPPORTED);
+    std::string e;
+    if (!wf::box_mesh(V, L, dx / 2.0, tet, k->x, k->elnod, e)) return bad(e);
+    I.npe = tet ? 4 : 8;
+  } else {
+    return bad("DomainBlocks type " + btype + " is not supported", WF_ERR_UNSUPPORTED);
+  }
+  I.nn = (int64_t)(k->x.size() / 3);
+  I.ne = (int64_t)(k->elnod.size() / I.npe);
+
+  // Rigid bodies: contact decks need the general triangle-mesh contact
+  std::string rtype;
+  if (rig && rig->at(0) && jstr(rig->at(0), "type", rtype))
+    return bad("rigid-body contact (" + rtype + ") is not supported", WF_ERR_UNSUPPORTED);
+
+  // BoundaryConditions: AddBCVelZone per condition, in order (main.C:578-887)
+  const double *X = k->x.data();
+  auto add = [&](int64_t n, int d, double v) {
+    k->bc_node.push_back(n);
+    k->bc_dim.push_back(d);
+    k->bc_val.push_back(v);
+  };
+  if (bcs && bcs->kind == JVal::Arr) {
+    for (const JVal &bc : bcs->arr) {
+      double st[3] = {0, 0, 0}, en[3] = {0, 0, 0}, val[3] = {0, 0, 0};
+      jvec(&bc, "value", val, 3);
+      bool have = jvec(&bc, "start", st, 3) && jvec(&bc, "end", en, 3);
+      if (!have) {
+        // a condition without its own box takes the DomainZones entry of its zoneId
+        int zid = -1;
+        jint(&bc, "zoneId", zid);
+        if (zones && zones->kind == JVal::Arr)
+          for (const JVal &z : zones->arr) {
+            int id = -2;
+            jint(&z, "id", id);
+            if (id == zid && jvec(&z, "start", st, 3) && jvec(&z, "end", en, 3)) {
+              have = true;
+              break;
+            }
+          }
+        if (!have)
+          return bad("boundary condition for zone " + std::to_string(zid) + " has no box");
+      }
+      I.n_zones++;
+      for (int64_t a = 0; a < I.nn; a++) {
+        const double *p = &X[3 * a];
+        bool inside = true;
+        for (int d = 0; d < 3; d++)
+          if (p[d] < st[d] || p[d] > en[d]) inside = false;
+        if (inside) {
+          for (int d = 0; d < 3; d++) add(a, d, val[d]);
+          I.zone_nodes++;
+        }
+      }
+    }
+  }
+  // symmetry planes (main.C:945-960): coordinate < symtol fixes that dof
+  for (int64_t a = 0; a < I.nn; a++)
+    for (int d = 0; d < 3; d++)
+      if (sym[d] && X[3 * a + d] < symtol) add(a, d, 0.0);
+  I.n_bc = (int64_t)k->bc_node.size();
+
+  // time step (main.C:862-879): dt = cflFactor * min length / sqrt(K / rho)
+  const double K = M.E / (3.0 * (1.0 - 2.0 * M.nu));
+  I.sound_speed = std::sqrt(K / M.rho);
+  I.min_length = ref_min_length(k->x, k->elnod, I.npe);
+  I.dt = I.cfl * I.min_length / I.sound_speed;
+  *out = k;
+  return WF_OK;
+}
+
+WF_API wf_status wf_deck_free(wf_deck *k) {
+  delete k;
+  return WF_OK;
+}
+
+WF_API wf_status wf_deck_get_info(const wf_deck *k, wf_deck_info *info) {
+  if (!k || !info) return WF_ERR_ARG;
+  *info = k->info;
+  return WF_OK;
+}
+
+WF_API wf_status wf_deck_get_mesh(const wf_deck *k, double *xyz, int32_t *elnod) {
+  if (!k) return WF_ERR_ARG;
+  if (xyz) std::memcpy(xyz, k->x.data(), sizeof(double) * k->x.size());
+  if (elnod) std::memcpy(elnod, k->elnod.data(), sizeof(int32_t) * k->elnod.size());
+  return WF_OK;
+}
+
+WF_API wf_status wf_deck_get_bcs(const wf_deck *k, int64_t *node, int32_t *dim, double *val) {
+  if (!k) return WF_ERR_ARG;
+  const size_t n = k->bc_node.size();
+  if (node) std::memcpy(node, k->bc_node.data(), sizeof(int64_t) * n);
+  if (dim) std::memcpy(dim, k->bc_dim.data(), sizeof(int32_t) * n);
+  if (val) std::memcpy(val, k->bc_val.data(), sizeof(double) * n);
+  return WF_OK;
+}
+
+WF_API wf_status wf_deck_apply(const wf_deck *k, wf_domain *d) {
+  if (!k || !d) return WF_ERR_ARG;
+  const wf_deck_info &I = k->info;
+  wf_status s;
+#define WF_DECK_TRY(call) \
+  if ((s = (call)) != WF_OK) return s
+  WF_DECK_TRY(wf_set_mesh(d, I.nn, I.ne, I.npe, k->x.data(), k->elnod.data()));
+  WF_DECK_TRY(wf_set_materials(d, 1, &I.material));
+  WF_DECK_TRY(wf_set_density(d, I.material.rho));
+  if (I.n_bc)
+    WF_DECK_TRY(wf_add_bc_vel_nodes(d, I.n_bc, k->bc_node.data(), k->bc_dim.data(),
+                                    k->bc_val.data()));
+  WF_DECK_TRY(wf_allocate_bcs(d));
+  if (I.has_stab) WF_DECK_TRY(wf_set_stab(d, &I.stab));
+  if (I.press_alg) WF_DECK_TRY(wf_set_press_algorithm(d, I.press_alg));
+  if (I.artif_visc[0] != 0.0 || I.artif_visc[1] != 0.0)
+    WF_DECK_TRY(wf_set_artif_visc(d, I.artif_visc[0], I.artif_visc[1]));
+  if (I.hourglass != 0.0) WF_DECK_TRY(wf_set_hourglass(d, I.hourglass));
+  WF_DECK_TRY(wf_set_dt(d, I.dt));
+  WF_DECK_TRY(wf_set_end_time(d, I.end_time));
+#undef WF_DECK_TRY
+  return WF_OK;
+}
+
+WF_API wf_status wf_load_deck(wf_domain *d, const char *path, wf_deck_info *info, char *err,
+                              int64_t err_len) {
+  if (!d || !path) return WF_ERR_ARG;
+  wf_deck *k = nullptr;
+  wf_status s = wf_deck_read(path, &k, err, err_len);
+  if (s) return s;
+  s = wf_deck_apply(k, d);
+  if (s == WF_OK && info) *info = k->info;
+  if (s && err && err_len > 0) deck_fail(err, err_len, wf_last_error(d), s);
+  wf_deck_free(k);
+  return s;
+}
+
+WF_API wf_status wf_load_lsdyna(wf_domain *d, const char *path) {
+  if (!d || !path) return WF_ERR_ARG;
+  KMesh km;
+  std::string e;
+  if (!read_lsdyna(path, km, e)) return wf::domain_fail(d, WF_ERR_ARG, e);
+  return wf_set_mesh(d, (int64_t)km.x.size() / 3, (int64_t)km.elnod.size() / km.npe, km.npe,
+                     km.x.data(), km.elnod.data());
+}
+
+// ---- VTK -------------------------------------------------------------------------
+// Legacy ASCII unstructured grid of the current state with the field names of
+// the reference's VTKWriter (VTKWriter.C:246-650): point data DISP, Velocity,
+// Acceleration, nod_mass, ContForce; cell data pressure, pl_strain, Vol, Rho,
+// sigy and the stress tensor SIGMA.
+WF_API wf_status wf_write_vtk(wf_domain *d, const char *path) {
+  if (!d || !path) return WF_ERR_ARG;
+  int64_t nn = 0, ne = 0, tot = 0;
+  int32_t npe = 0;
+  wf_status s = wf_get_sizes(d, &nn, &ne, &npe, &tot);
+  if (s) return s;
+  std::vector<double> x(3 * nn), u(3 * nn), v(3 * nn), a(3 * nn), cf(3 * nn), mass(nn);
+  std::vector<double> p(ne), pl(ne), vol(ne), rho(ne), sy(ne), sig(6 * ne);
+  std::vector<int32_t> el(ne * npe);
+  if ((s = wf_get_node_field(d, WF_NODE_X, x.data()))) return s;
+  if ((s = wf_get_node_field(d, WF_NODE_U, u.data()))) return s;
+  if ((s = wf_get_node_field(d, WF_NODE_V, v.data()))) return s;
+  if ((s = wf_get_node_field(d, WF_NODE_A, a.data()))) return s;
+  if ((s = wf_get_node_field(d, WF_NODE_CONTFORCE, cf.data()))) return s;
+  if ((s = wf_get_node_scalar(d, WF_NODE_MASS, mass.data()))) return s;
+  if ((s = wf_get_elem_scalar(d, WF_ELEM_P, p.data()))) return s;
+  if ((s = wf_get_elem_scalar(d, WF_ELEM_PL_STRAIN, pl.data()))) return s;
+  if ((s = wf_get_elem_scalar(d, WF_ELEM_VOL, vol.data()))) return s;
+  if ((s = wf_get_elem_scalar(d, WF_ELEM_RHO, rho.data()))) return s;
+  if ((s = wf_get_elem_scalar(d, WF_ELEM_SIGMA_Y, sy.data()))) return s;
+  if ((s = wf_get_elem_tensor(d, WF_ELEM_SIGMA, sig.data()))) return s;
+  if ((s = wf_get_connectivity(d, el.data(), nullptr, nullptr, nullptr, nullptr))) return s;
+  FILE *f = std::fopen(path, "w");
+  if (!f) return WF_ERR_ARG;
+  std::fprintf(f, "# vtk DataFile Version 3.0\nweldform-gb300 results\nASCII\n"
+                  "DATASET UNSTRUCTURED_GRID\nPOINTS %lld double\n", (long long)nn);
+  for (int64_t n = 0; n < nn; n++)
+    std::fprintf(f, "%.17g %.17g %.17g\n", x[3 * n], x[3 * n + 1], x[3 * n + 2]);
+  std::fprintf(f, "CELLS %lld %lld\n", (long long)ne, (long long)(ne * (npe + 1)));
+  for (int64_t e = 0; e < ne; e++) {
+    std::fprintf(f, "%d", npe);
+    for (int q = 0; q < npe; q++) std::fprintf(f, " %d", el[e * npe + q]);
+    std::fprintf(f, "\n");
+  }
+  std::fprintf(f, "CELL_TYPES %lld\n", (long long)ne);
+  for (int64_t e = 0; e < ne; e++) std::fprintf(f, "%d\n", npe == 8 ? 12 : 10);
+  std::fprintf(f, "POINT_DATA %lld\n", (long long)nn);
+  auto vec = [&](const char *name, const std::vector<double> &w) {
+    std::fprintf(f, "VECTORS %s double\n", name);
+    for (int64_t n = 0; n < nn; n++)
+      std::fprintf(f, "%.9g %.9g %.9g\n", w[3 * n], w[3 * n + 1], w[3 * n + 2]);
+  };
+  vec("DISP", u);
+  vec("Velocity", v);
+  vec("Acceleration", a);
+  vec("ContForce", cf);
+  std::fprintf(f, "SCALARS nod_mass double 1\nLOOKUP_TABLE default\n");
+  for (int64_t n = 0; n < nn; n++) std::fprintf(f, "%.9g\n", mass[n]);
+  std::fprintf(f, "CELL_DATA %lld\n", (long long)ne);
+  auto scal = [&](const char *name, const std::vector<double> &w) {
+    std::fprintf(f, "SCALARS %s double 1\nLOOKUP_TABLE default\n", name);
+    for (int64_t e = 0; e < ne; e++) std::fprintf(f, "%.9g\n", w[e]);
+  };
+  scal("pressure", p);
+  scal("pl_strain", pl);
+  scal("Vol", vol);
+  scal("Rho", rho);
+  scal("sigy", sy);
+  std::fprintf(f, "TENSORS SIGMA double\n");
+  for (int64_t e = 0; e < ne; e++) {
+    const double *t = &sig[6 * e];  // xx yy zz xy yz xz
+    std::fprintf(f, "%.9g %.9g %.9g\n%.9g %.9g %.9g\n%.9g %.9g %.9g\n\n", t[0], t[3], t[5], t[3],
+                 t[1], t[4], t[5], t[4], t[2]);
+  }
+  const bool ok = std::fclose(f) == 0;
+  return ok ? WF_OK : WF_ERR_ARG;
+}

@@ -131,6 +131,13 @@ struct MixState {
   float *edot;                    // [ne] sigma . str_rate * vol (energy history only)
 };
 
+// Records `msg` as the domain's last error and returns s (wf_api.cu).
+wf_status domain_fail(wf_domain *d, wf_status s, const std::string &msg);
+
+// Structured box mesh of Domain_d::AddBoxLength (host; wf_api.cu).
+bool box_mesh(const double V[3], const double L[3], double r, bool tritetra,
+              std::vector<double> &x, std::vector<int32_t> &elnod, std::string &err);
+
 // ---- FP64 launchers (wf_fp64.cu) ------------------------------------------
 void fp64_geometry(const StepParams &P, const Fp64State &S, cudaStream_t st, bool store_detj);
 void fp64_nodal(const StepParams &P, const Fp64State &S, cudaStream_t st, int init_mode);
