@@ -20,6 +20,7 @@ SRC = os.path.join(HERE, "wf_oracle.c")
 
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 _ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_u8 = np.ctypeslib.ndpointer(dtype=np.uint8, flags="C_CONTIGUOUS")
 _lib = None
 
 
@@ -85,6 +86,10 @@ def lib():
         "wfo_get_elem_forces": ([vp, _dp, _dp], None),
         "wfo_get_reaction": ([vp, _dp, i64], i64),
         "wfo_get_energies": ([vp, _dp, _dp, i64], i64),
+        "wfo_set_contact_trimesh": ([vp, i64, _dp, i64, _ip, _dp, C.c_double, C.c_double,
+                                     C.c_double], None),
+        "wfo_get_trimesh_nodes": ([vp, _dp, i64], i64),
+        "wfo_get_surface": ([vp, _u8, _dp, _dp], i64),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -213,6 +218,26 @@ class OracleDomain:
         cand = np.ascontiguousarray(cand_nodes, np.int32)
         lib().wfo_set_contact_plane(self.h, float(z0), float(vz), float(kpen), float(mu),
                                     cand, cand.size)
+
+    def set_contact_trimesh(self, xyz, tri, vel, mu_static=0.0, mu_dynamic=0.0,
+                            penalty_factor=0.1):
+        xyz = np.ascontiguousarray(xyz, np.float64).reshape(-1)
+        tri = np.ascontiguousarray(tri, np.int32).reshape(-1)
+        lib().wfo_set_contact_trimesh(self.h, xyz.size // 3, xyz, tri.size // 3, tri,
+                                      np.ascontiguousarray(vel, np.float64), float(mu_static),
+                                      float(mu_dynamic), float(penalty_factor))
+
+    def trimesh_nodes(self):
+        n = lib().wfo_get_trimesh_nodes(self.h, np.zeros(3), 0)
+        out = np.zeros(3 * max(n, 1))
+        lib().wfo_get_trimesh_nodes(self.h, out, n)
+        return out[:3 * n].reshape(-1, 3)
+
+    def surface(self):
+        nn = self.nn
+        ext, area, nl = np.zeros(nn, np.uint8), np.zeros(nn), np.zeros(nn)
+        lib().wfo_get_surface(self.h, ext, area, nl)
+        return ext, area, nl
 
     def set_dt(self, dt):
         lib().wfo_set_dt(self.h, float(dt))

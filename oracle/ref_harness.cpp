@@ -25,13 +25,16 @@
 //        calcElemHourglassForces is a no-op in 3-D, Mechanical.C:1939-1942);
 //        restated from src/common/test_1el_3D.cpp:159-199 with the current
 //        element volume and density;
-//      - penalty/Coulomb contact against a rigid analytic plane, restated
-//        from src/common/Contact.C:58-323;
 //    and the step records the top reaction force (sum of the internal force
 //    over a node set, after assemblyForces).
+//  A rigid triangle mesh (TriMesh_d) can be attached; the stepwise loop then
+//  calls the reference's own CalcContactForces (Contact.C:31-334), records
+//  its reaction (react_force[0].z) and ramps, moves and re-planes the mesh at
+//  the end of the step as SolveChungHulbert does (Solver_explicit.C:980-1004).
 //  With all switches off, O2 reproduces O1 bit for bit (checked by tests).
 #include "Domain_d.h"
 #include "Material.cuh"
+#include "Mesh.h"
 
 #include <cmath>
 #include <cstdio>
@@ -63,6 +66,47 @@ class RefDomain : public Domain_d {
   std::vector<double> reaction_hist;
   std::vector<double> ekin_hist, eint_hist;  // computeEnergies after every step
   double eint_acc = 0.0;
+  TriMesh_d *tm = nullptr;                  // rigid triangle mesh (contact)
+  std::vector<double3> v_orig;              // its velocity before the ramp
+
+  // A TriMesh_d filled from arrays, one mesh (id 0), uniform velocity; normals,
+  // centroids and plane coefficients as the reference computes them.
+  void set_trimesh(int nn, const double *xyz, int ne, const int *tri, const double *vel,
+                   double mu_s, double mu_d, double pf) {
+    tm = new TriMesh_d();
+    tm->dimension = 3;
+    tm->nodecount = nn;
+    tm->elemcount = ne;
+    tm->mesh_count = 1;
+    malloc_t(tm->node, double3, nn);
+    malloc_t(tm->node_v, double3, nn);
+    malloc_t(tm->elnode, int, 3 * ne);
+    malloc_t(tm->centroid, double3, ne);
+    malloc_t(tm->normal, double3, ne);
+    malloc_t(tm->pplane, double, ne);
+    malloc_t(tm->nfar, int, ne);
+    malloc_t(tm->ele_mesh_id, int, ne);
+    malloc_t(tm->react_force, double3, 1);
+    malloc_t(tm->react_p_force, double, 1);
+    malloc_t(tm->mu_sta, double, 1);
+    malloc_t(tm->mu_dyn, double, 1);
+    for (int n = 0; n < nn; n++) {
+      tm->node[n] = make_double3(xyz[3 * n], xyz[3 * n + 1], xyz[3 * n + 2]);
+      tm->node_v[n] = make_double3(vel[0], vel[1], vel[2]);
+    }
+    for (int e = 0; e < ne; e++) {
+      for (int k = 0; k < 3; k++) tm->elnode[3 * e + k] = tri[3 * e + k];
+      tm->ele_mesh_id[e] = 0;
+    }
+    tm->react_force[0] = make_double3(0., 0., 0.);
+    tm->mu_sta[0] = mu_s;
+    tm->mu_dyn[0] = mu_d;
+    tm->heat_cond = 0.0;
+    tm->CalcCentroids();
+    tm->CalcNormals();
+    tm->CalcSpheres();
+    setContactPF(pf);
+  }
   long step_count = 0;
 
   void zero_uninitialised() {
@@ -106,6 +150,14 @@ class RefDomain : public Domain_d {
     CalcNodalMassFromVol();
     for (int n = 0; n < m_node_count; n++)
       for (int d = 0; d < m_dim; d++) ut_prev[m_dim * n + d] = 0.0;
+    if (tm) {
+      // what main.C does before the solve (main.C:647-650, :862-873)
+      setTriMesh(tm);
+      setContactOn();
+      SearchExtNodes();
+      calcMinEdgeLength();
+      v_orig.assign(tm->node_v, tm->node_v + tm->nodecount);
+    }
     Time = 0.0;
     step_count = 0;
   }
@@ -217,18 +269,32 @@ class RefDomain : public Domain_d {
     calcElemForces();
     calcElemHourglassForces();
     if (hg_coef != 0.0 && m_dim == 3 && m_nodxelem == 8) hourglass_3d();
+    if (tm) CalcContactForces();
     assemblyForces();
     for (int i = 0; i < m_node_count * m_dim; ++i)
       if (!std::isfinite(m_fi[i])) m_fi[i] = 0.0;
     double r = 0.0;
-    for (size_t k = 0; k < reaction_nodes.size(); k++)
-      r += m_fi[m_dim * reaction_nodes[k] + reaction_dim];
+    if (tm)
+      r = tm->react_force[0].z;
+    else
+      for (size_t k = 0; k < reaction_nodes.size(); k++)
+        r += m_fi[m_dim * reaction_nodes[k] + reaction_dim];
     reaction_hist.push_back(r);
     calcAccel();
     ImposeBCAAllDim();
     UpdateCorrectionAccVel();
     ImposeBCVAllDim();
     UpdateCorrectionPos();
+    if (tm) {
+      const double RAMP_FRACTION = 1.0e-2;  // Solver_explicit.C:309, :980-991
+      double f = 1.0;
+      if (Time < RAMP_FRACTION * end_t) f = pow(Time / (RAMP_FRACTION * end_t), 0.5);
+      for (int n = 0; n < tm->nodecount; n++) tm->node_v[n] = f * v_orig[n];
+      tm->Move(dt);
+      tm->CalcCentroids();
+      tm->CalcNormals();
+      tm->UpdatePlaneCoeff();
+    }
     // end of the loop body (Solver_explicit.C:1029-1031)
     double ekin = 0.0, deint = 0.0, devisc = 0.0;
     computeEnergies(dt, ekin, deint, devisc);
@@ -284,6 +350,21 @@ class RefDomain : public Domain_d {
   int dim() const { return m_dim; }
   int npe() const { return m_nodxelem; }
   int nn() const { return m_node_count; }
+  int get_surface(unsigned char *ext, double *area, double *nodlen) const {
+    if (!tm) return 0;
+    for (int i = 0; i < m_node_count; i++) {
+      ext[i] = ext_nodes[i] ? 1 : 0;
+      area[i] = node_area[i];
+      double l = 0.0;
+      for (int e = 0; e < m_nodel_count[i]; e++)
+        l += m_elem_length[m_nodel[m_nodel_offset[i] + e]];
+      nodlen[i] = l / m_nodel_count[i];
+    }
+    return m_node_count;
+  }
+  void get_contforce(double *out) const {
+    std::memcpy(out, contforce, sizeof(double) * m_node_count * m_dim);
+  }
   int ne() const { return m_elem_count; }
   void get_derivs(double *out) {
     // [E][3][npe]
@@ -481,6 +562,30 @@ int wfr_get_reaction(void *h, double *out, int maxn) {
   if (n > maxn) n = maxn;
   for (int i = 0; i < n; i++) out[i] = d->reaction_hist[i];
   return (int)d->reaction_hist.size();
+}
+
+void wfr_set_trimesh(void *h, int nn, const double *xyz, int ne, const int *tri,
+                     const double *vel, double mu_s, double mu_d, double pf) {
+  static_cast<RefDomain *>(h)->set_trimesh(nn, xyz, ne, tri, vel, mu_s, mu_d, pf);
+}
+int wfr_get_trimesh_nodes(void *h, double *out, int cap) {
+  RefDomain *d = static_cast<RefDomain *>(h);
+  if (!d->tm) return 0;
+  for (int n = 0; n < d->tm->nodecount && n < cap; n++) {
+    out[3 * n] = d->tm->node[n].x;
+    out[3 * n + 1] = d->tm->node[n].y;
+    out[3 * n + 2] = d->tm->node[n].z;
+  }
+  return d->tm->nodecount;
+}
+// External-node flags, nodal areas and mean element lengths of the surface
+// search (SearchExtNodes, calcMinEdgeLength) after init.
+int wfr_get_surface(void *h, unsigned char *ext, double *area, double *nodlen) {
+  return static_cast<RefDomain *>(h)->get_surface(ext, area, nodlen);
+}
+int wfr_get_contforce(void *h, double *out) {
+  static_cast<RefDomain *>(h)->get_contforce(out);
+  return 0;
 }
 
 int wfr_get_energies(void *h, double *ekin, double *eint, int maxn) {

@@ -17,6 +17,7 @@ LIB_PATH = os.path.join(HERE, "_ref", "libwfref.so")
 
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 _ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_u8 = np.ctypeslib.ndpointer(dtype=np.uint8, flags="C_CONTIGUOUS")
 _lib = None
 
 
@@ -66,6 +67,11 @@ def lib():
         "wfr_get_elem_forces": ([vp, _dp, _dp], None),
         "wfr_get_reaction": ([vp, _dp, C.c_int], C.c_int),
         "wfr_get_energies": ([vp, _dp, _dp, C.c_int], C.c_int),
+        "wfr_set_trimesh": ([vp, C.c_int, _dp, C.c_int, _ip, _dp, C.c_double, C.c_double,
+                             C.c_double], None),
+        "wfr_get_trimesh_nodes": ([vp, _dp, C.c_int], C.c_int),
+        "wfr_get_surface": ([vp, _u8, _dp, _dp], C.c_int),
+        "wfr_get_contforce": ([vp, _dp], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -197,6 +203,31 @@ class RefDomain:
     def set_reaction_nodes(self, nodes, dim=2):
         nodes = np.ascontiguousarray(nodes, np.int32)
         lib().wfr_set_reaction_nodes(self.h, nodes.size, nodes, int(dim))
+
+    def set_contact_trimesh(self, xyz, tri, vel, mu_static=0.0, mu_dynamic=0.0,
+                            penalty_factor=0.1):
+        xyz = np.ascontiguousarray(xyz, np.float64).reshape(-1)
+        tri = np.ascontiguousarray(tri, np.int32).reshape(-1)
+        lib().wfr_set_trimesh(self.h, xyz.size // 3, xyz, tri.size // 3, tri,
+                              np.ascontiguousarray(vel, np.float64), float(mu_static),
+                              float(mu_dynamic), float(penalty_factor))
+
+    def trimesh_nodes(self):
+        n = lib().wfr_get_trimesh_nodes(self.h, np.zeros(3), 0)
+        out = np.zeros(3 * max(n, 1))
+        lib().wfr_get_trimesh_nodes(self.h, out, n)
+        return out[:3 * n].reshape(-1, 3)
+
+    def surface(self):
+        nn = self.nn
+        ext, area, nl = np.zeros(nn, np.uint8), np.zeros(nn), np.zeros(nn)
+        lib().wfr_get_surface(self.h, ext, area, nl)
+        return ext, area, nl
+
+    def contforce(self):
+        out = np.zeros(3 * self.nn)
+        lib().wfr_get_contforce(self.h, out)
+        return out.reshape(-1, 3)
 
     def set_dt(self, dt):
         lib().wfr_set_dt(self.h, float(dt))

@@ -56,6 +56,15 @@ struct wfo_domain {
   double c_z0, c_vz, c_kpen, c_mu;
   uint8_t *cand;
   double *cfn;
+  /* rigid triangle mesh (TriMesh_d, Mesh.h:69-171) and the part's external
+   * surface (SearchExtNodes / CalcExtFaceAreas, Domain_d.C:110-290) */
+  int tri_on;
+  int64_t tri_nn, tri_ne;
+  double *tri_x, *tri_vorig, *tri_nrm, *tri_pp;
+  int32_t *tri_el;
+  double tri_mu_s, tri_mu_d, tri_pf;
+  uint8_t *ext;
+  double *node_area, *nodlen, *elem_len;
   int64_t step_count;
 };
 
@@ -89,16 +98,30 @@ static void free_mesh(wfo_domain *d) {
                    (void **)&d->sigma_y, (void **)&d->sigma, (void **)&d->tau,
                    (void **)&d->eps, (void **)&d->str_rate, (void **)&d->rot_rate,
                    (void **)&d->pl_incr, (void **)&d->f_elem, (void **)&d->f_hg,
-                   (void **)&d->elem_mat, (void **)&d->cand, (void **)&d->cfn};
+                   (void **)&d->elem_mat, (void **)&d->cand, (void **)&d->cfn,
+                   (void **)&d->ext, (void **)&d->node_area, (void **)&d->nodlen,
+                   (void **)&d->elem_len};
   for (size_t i = 0; i < sizeof(ptrs) / sizeof(ptrs[0]); i++) {
     free(*ptrs[i]);
     *ptrs[i] = NULL;
   }
 }
 
+static void free_trimesh(wfo_domain *d) {
+  free(d->tri_x);
+  free(d->tri_vorig);
+  free(d->tri_nrm);
+  free(d->tri_pp);
+  free(d->tri_el);
+  d->tri_x = d->tri_vorig = d->tri_nrm = d->tri_pp = NULL;
+  d->tri_el = NULL;
+  d->tri_on = 0;
+}
+
 void wfo_destroy(wfo_domain *d) {
   if (!d) return;
   free_mesh(d);
+  free_trimesh(d);
   for (int k = 0; k < 3; k++) {
     free(d->bc_nod[k]);
     free(d->bc_val[k]);
@@ -335,6 +358,65 @@ void wfo_set_press_algorithm(wfo_domain *d, int alg) { d->press_alg = alg; }
 void wfo_set_stab(wfo_domain *d, const double s[10]) { memcpy(d->stab, s, sizeof(d->stab)); }
 void wfo_set_artif_visc(wfo_domain *d, double al, double be) { d->artif[0] = al; d->artif[1] = be; }
 void wfo_set_mass_mode(wfo_domain *d, int mode) { d->mass_mode = mode; }
+
+/* Triangle-mesh normals (TriMesh_d::CalcNormals, Mesh.h:236-262) and plane
+ * coefficients with the far node nfar = 2 (CalcSpheres / UpdatePlaneCoeff,
+ * Mesh.h:275-284, :300-320). */
+static void tri_normals_planes(wfo_domain *d) {
+  for (int64_t e = 0; e < d->tri_ne; e++) {
+    const double *p0 = &d->tri_x[3 * d->tri_el[3 * e]];
+    const double *p1 = &d->tri_x[3 * d->tri_el[3 * e + 1]];
+    const double *p2 = &d->tri_x[3 * d->tri_el[3 * e + 2]];
+    const double u[3] = {p1[0] - p0[0], p1[1] - p0[1], p1[2] - p0[2]};
+    const double v[3] = {p2[0] - p0[0], p2[1] - p0[1], p2[2] - p0[2]};
+    const double w[3] = {u[1] * v[2] - u[2] * v[1], u[2] * v[0] - u[0] * v[2],
+                         u[0] * v[1] - u[1] * v[0]};
+    const double len = sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+    const double inv = 1.0 / len;
+    double *n = &d->tri_nrm[3 * e];
+    n[0] = w[0] * inv;
+    n[1] = w[1] * inv;
+    n[2] = w[2] * inv;
+    d->tri_pp[e] = p2[0] * n[0] + p2[1] * n[1] + p2[2] * n[2];
+  }
+}
+
+void wfo_set_contact_trimesh(wfo_domain *d, int64_t nnodes, const double *xyz, int64_t ntri,
+                             const int32_t *tri, const double vel[3], double mu_static,
+                             double mu_dynamic, double penalty_factor) {
+  free_trimesh(d);
+  d->tri_on = 1;
+  d->contact = 1;
+  d->tri_nn = nnodes;
+  d->tri_ne = ntri;
+  d->tri_x = xcalloc(3 * nnodes, 8);
+  d->tri_vorig = xcalloc(3 * nnodes, 8);
+  d->tri_nrm = xcalloc(3 * ntri, 8);
+  d->tri_pp = xcalloc(ntri, 8);
+  d->tri_el = xcalloc(3 * ntri, 4);
+  memcpy(d->tri_x, xyz, sizeof(double) * 3 * nnodes);
+  memcpy(d->tri_el, tri, sizeof(int32_t) * 3 * ntri);
+  for (int64_t n = 0; n < nnodes; n++)
+    for (int k = 0; k < 3; k++) d->tri_vorig[3 * n + k] = vel[k];
+  d->tri_mu_s = mu_static;
+  d->tri_mu_d = mu_dynamic;
+  d->tri_pf = penalty_factor;
+  tri_normals_planes(d);
+}
+
+int64_t wfo_get_trimesh_nodes(const wfo_domain *d, double *out, int64_t cap) {
+  const int64_t n = d->tri_nn < cap ? d->tri_nn : cap;
+  if (out && d->tri_on && n > 0) memcpy(out, d->tri_x, sizeof(double) * 3 * n);
+  return d->tri_on ? d->tri_nn : 0;
+}
+
+int64_t wfo_get_surface(const wfo_domain *d, uint8_t *ext, double *node_area, double *nodlen) {
+  if (!d->ext) return 0;
+  if (ext) memcpy(ext, d->ext, d->nn);
+  if (node_area) memcpy(node_area, d->node_area, sizeof(double) * d->nn);
+  if (nodlen) memcpy(nodlen, d->nodlen, sizeof(double) * d->nn);
+  return d->nn;
+}
 
 void wfo_set_contact_plane(wfo_domain *d, double z0, double vz, double kpen, double mu,
                            const int32_t *cand, int64_t ncand) {
@@ -955,6 +1037,244 @@ static void update_correction_pos(wfo_domain *d) {
   }
 }
 
+/* ---- triangle-mesh contact ------------------------------------------------ */
+/* Face tables of the reference (Domain_d.h:184-193). */
+static const int TET_FACES[4][3] = {{0, 1, 2}, {0, 1, 3}, {1, 2, 3}, {0, 2, 3}};
+static const int HEX_FACES[6][4] = {{0, 1, 2, 3}, {4, 5, 6, 7}, {0, 1, 5, 4},
+                                    {2, 3, 7, 6}, {0, 3, 7, 4}, {1, 2, 6, 5}};
+
+typedef struct {
+  int32_t k[4];
+  int32_t count;
+  int32_t used;
+} face_slot;
+
+static uint64_t face_hash(const int32_t *k) {
+  uint64_t h = 1469598103934665603ull;
+  for (int i = 0; i < 4; i++) {
+    h ^= (uint64_t)(uint32_t)k[i];
+    h *= 1099511628211ull;
+  }
+  return h;
+}
+
+static void sort_key(const int32_t *in, int n, int32_t *k) {
+  for (int i = 0; i < 4; i++) k[i] = i < n ? in[i] : -1;
+  for (int i = 1; i < n; i++)
+    for (int j = i; j > 0 && k[j - 1] > k[j]; j--) {
+      int32_t t = k[j];
+      k[j] = k[j - 1];
+      k[j - 1] = t;
+    }
+}
+
+static face_slot *face_find(face_slot *tab, uint64_t mask, const int32_t *k) {
+  uint64_t i = face_hash(k) & mask;
+  for (;;) {
+    face_slot *s = &tab[i];
+    if (!s->used || (s->k[0] == k[0] && s->k[1] == k[1] && s->k[2] == k[2] && s->k[3] == k[3]))
+      return s;
+    i = (i + 1) & mask;
+  }
+}
+
+static double tri_area(const double *p0, const double *p1, const double *p2) {
+  const double v1[3] = {p1[0] - p0[0], p1[1] - p0[1], p1[2] - p0[2]};
+  const double v2[3] = {p2[0] - p0[0], p2[1] - p0[1], p2[2] - p0[2]};
+  const double c[3] = {v1[1] * v2[2] - v1[2] * v2[1], v1[2] * v2[0] - v1[0] * v2[2],
+                       v1[0] * v2[1] - v1[1] * v2[0]};
+  return 0.5 * sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+}
+
+/* External nodes and nodal areas (SearchExtNodes + CalcExtFaceAreas): a face
+ * used by one element is external; its area goes in equal shares to its nodes,
+ * faces taken in element order and local face order. Tetrahedra use the
+ * reference's triangular face table; hexahedra the quadrilateral table
+ * (hexa_faces), each quadrilateral's area as the triangles (0,1,2) + (0,2,3).
+ * Element lengths: the 3-D branch of calcMinEdgeLength (Domain_d.C:2236-2262),
+ * the smallest height of the tetrahedron of the element's first four nodes;
+ * nodlen = mean over the node's elements (Contact.C:145-152). */
+static void tri_setup_surface(wfo_domain *d) {
+  const int npe = d->npe, nf = npe == 8 ? 6 : 4, fn = npe == 8 ? 4 : 3;
+  const int64_t nfaces = d->ne * nf;
+  uint64_t cap = 1;
+  while (cap < 2 * (uint64_t)nfaces + 2) cap <<= 1;
+  face_slot *tab = calloc(cap, sizeof(face_slot));
+  int32_t key[4], fnodes[4];
+  for (int64_t e = 0; e < d->ne; e++)
+    for (int f = 0; f < nf; f++) {
+      for (int q = 0; q < fn; q++)
+        fnodes[q] = d->elnod[e * npe + (npe == 8 ? HEX_FACES[f][q] : TET_FACES[f][q])];
+      sort_key(fnodes, fn, key);
+      face_slot *s = face_find(tab, cap - 1, key);
+      if (!s->used) {
+        s->used = 1;
+        memcpy(s->k, key, sizeof(key));
+      }
+      s->count++;
+    }
+  free(d->ext);
+  free(d->node_area);
+  free(d->nodlen);
+  free(d->elem_len);
+  d->ext = xcalloc(d->nn, 1);
+  d->node_area = xcalloc(d->nn, 8);
+  d->nodlen = xcalloc(d->nn, 8);
+  d->elem_len = xcalloc(d->ne, 8);
+  for (int64_t e = 0; e < d->ne; e++)
+    for (int f = 0; f < nf; f++) {
+      for (int q = 0; q < fn; q++)
+        fnodes[q] = d->elnod[e * npe + (npe == 8 ? HEX_FACES[f][q] : TET_FACES[f][q])];
+      sort_key(fnodes, fn, key);
+      if (face_find(tab, cap - 1, key)->count != 1) continue;
+      const double *p0 = &d->x[3 * fnodes[0]], *p1 = &d->x[3 * fnodes[1]], *p2 = &d->x[3 * fnodes[2]];
+      double share;
+      if (fn == 3) {
+        share = tri_area(p0, p1, p2) / 3.0;
+      } else {
+        const double *p3 = &d->x[3 * fnodes[3]];
+        share = (tri_area(p0, p1, p2) + tri_area(p0, p2, p3)) / 4.0;
+      }
+      for (int q = 0; q < fn; q++) {
+        d->ext[fnodes[q]] = 1;
+        d->node_area[fnodes[q]] += share;
+      }
+    }
+  free(tab);
+  for (int64_t e = 0; e < d->ne; e++) {
+    const int32_t *n = &d->elnod[e * npe];
+    const double *A = &d->x[3 * n[0]], *B = &d->x[3 * n[1]], *C = &d->x[3 * n[2]],
+                 *D = &d->x[3 * n[3]];
+    const double *faces[4][3] = {{B, C, D}, {A, C, D}, {A, B, D}, {A, B, C}};
+    double hmin = 1.0e6;
+    for (int i = 0; i < 4; i++) {
+      const double *f0 = faces[i][0], *f1 = faces[i][1], *f2 = faces[i][2];
+      const double x1[3] = {f1[0] - f0[0], f1[1] - f0[1], f1[2] - f0[2]};
+      const double x2[3] = {f2[0] - f0[0], f2[1] - f0[1], f2[2] - f0[2]};
+      double nn[3] = {x1[1] * x2[2] - x1[2] * x2[1], x1[2] * x2[0] - x1[0] * x2[2],
+                      x1[0] * x2[1] - x1[1] * x2[0]};
+      const double area = sqrt(nn[0] * nn[0] + nn[1] * nn[1] + nn[2] * nn[2]);
+      if (area < 1e-12) continue;
+      const double inv = 1.0 / area;
+      nn[0] *= inv;
+      nn[1] *= inv;
+      nn[2] *= inv;
+      const double *P = &d->x[3 * n[i]];
+      const double vec[3] = {P[0] - f0[0], P[1] - f0[1], P[2] - f0[2]};
+      const double h = fabs(vec[0] * nn[0] + vec[1] * nn[1] + vec[2] * nn[2]);
+      if (h < hmin) hmin = h;
+    }
+    d->elem_len[e] = hmin;
+  }
+  for (int64_t i = 0; i < d->nn; i++) {
+    double l = 0.0;
+    const int32_t b = d->nodel_off[i], c = d->nodel_cnt[i];
+    for (int32_t k = 0; k < c; k++) l += d->elem_len[d->nodel[b + k]];
+    d->nodlen[i] = l / c;
+  }
+}
+
+/* Domain_d::CalcContactForces (Contact.C:31-334) against the rigid triangle
+ * mesh: for each external node, the first triangle (in order) it penetrates
+ * (d < 0, projection inside the triangle) gives a penalty normal force with
+ * stiffness min(E A / l, 0.2 m / dt^2) times the penalty factor, a damping
+ * force, and Coulomb friction from the accumulated tangential slip (static
+ * cap, then dynamic force along -v_t). As in the reference, a node that leaves
+ * contact keeps its last contact force. The reaction is the sum of normal-force
+ * magnitudes of the nodes in contact. */
+static void calc_contact_trimesh(wfo_domain *d) {
+  const double dt = d->dt;
+  const double E0 = d->mats[0].E;
+  for (int64_t i = 0; i < d->nn; i++) {
+    d->cfn[i] = 0.0;
+    if (!d->ext[i]) continue;
+    const double *x = &d->x[3 * i];
+    const double *v = &d->v[3 * i];
+    for (int64_t j = 0; j < d->tri_ne; j++) {
+      const double *nr = &d->tri_nrm[3 * j];
+      const double dd = (nr[0] * x[0] + nr[1] * x[1] + nr[2] * x[2]) - d->tri_pp[j];
+      if (!(dd < 0)) continue;
+      const double Q[3] = {x[0] - nr[0] * dd, x[1] - nr[1] * dd, x[2] - nr[2] * dd};
+      int inside = 1;
+      for (int l = 0; l < 3 && inside; l++) {
+        const int nx = l + 1 > 2 ? 0 : l + 1;
+        const double *a = &d->tri_x[3 * d->tri_el[3 * j + l]];
+        const double *b = &d->tri_x[3 * d->tri_el[3 * j + nx]];
+        const double e1[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]};
+        const double e2[3] = {Q[0] - a[0], Q[1] - a[1], Q[2] - a[2]};
+        const double c[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2],
+                             e1[0] * e2[1] - e1[1] * e2[0]};
+        const double crit = c[0] * nr[0] + c[1] * nr[1] + c[2] * nr[2];
+        if (crit < 0.0) inside = 0;
+      }
+      if (!inside) continue;
+      const double m = d->mass[i];
+      const double v_reln = v[0] * nr[0] + v[1] * nr[1] + v[2] * nr[2];
+      const double kgeo = E0 * d->node_area[i] / d->nodlen[i];
+      const double kmass = 0.2 * m / (dt * dt);
+      const double k = (kmass < kgeo) ? kmass : kgeo;  /* std::min(kgeo, kmass) */
+      const double omega = sqrt(k / m);
+      const double ccrit = 2.0 * m * omega;
+      const double F_damp = 0.2 * ccrit * v_reln;
+      const double F_normal = d->tri_pf * k * dd;
+      const double s = -(F_normal + F_damp);
+      double *cf = &d->contforce[3 * i];
+      cf[0] = nr[0] * s;
+      cf[1] = nr[1] * s;
+      cf[2] = nr[2] * s;
+      d->cfn[i] = sqrt(cf[0] * cf[0] + cf[1] * cf[1] + cf[2] * cf[2]);
+      /* friction */
+      const double vn = v[0] * nr[0] + v[1] * nr[1] + v[2] * nr[2];
+      const double vt[3] = {v[0] - nr[0] * vn, v[1] - nr[1] * vn, v[2] - nr[2] * vn};
+      double *ut = &d->ut_prev[3 * i];
+      const double du[3] = {vt[0] * dt, vt[1] * dt, vt[2] * dt};
+      const double ua[3] = {ut[0] + du[0], ut[1] + du[1], ut[2] + du[2]};
+      ut[0] += du[0];
+      ut[1] += du[1];
+      ut[2] += du[2];
+      const double mk = -k;
+      const double ft[3] = {ua[0] * mk, ua[1] * mk, ua[2] * mk};
+      const double ft_mag = sqrt(ft[0] * ft[0] + ft[1] * ft[1] + ft[2] * ft[2]);
+      const double cn = cf[0] * nr[0] + cf[1] * nr[1] + cf[2] * nr[2];
+      const double Fn[3] = {nr[0] * cn, nr[1] * cn, nr[2] * cn};
+      const double fn_norm = sqrt(Fn[0] * Fn[0] + Fn[1] * Fn[1] + Fn[2] * Fn[2]);
+      double F[3];
+      if (ft_mag <= d->tri_mu_s * fn_norm) {
+        F[0] = ft[0];
+        F[1] = ft[1];
+        F[2] = ft[2];
+      } else {
+        const double md = -(d->tri_mu_d * fn_norm);
+        const double vnorm = sqrt(vt[0] * vt[0] + vt[1] * vt[1] + vt[2] * vt[2]);
+        const double inv = 1.0 / vnorm;
+        F[0] = (vt[0] * md) * inv;
+        F[1] = (vt[1] * md) * inv;
+        F[2] = (vt[2] * md) * inv;
+        ut[0] = ut[1] = ut[2] = 0.0;
+      }
+      cf[0] += F[0];
+      cf[1] += F[1];
+      cf[2] += F[2];
+      break;
+    }
+  }
+}
+
+/* End of the loop body (Solver_explicit.C:980-1004): the die velocity ramps
+ * as sqrt(Time / (0.01 end_t)) over the first 1 % of the end time, the mesh
+ * moves by v dt and its normals and planes are recomputed. */
+static void tri_move(wfo_domain *d) {
+  const double rf = 1.0e-2;
+  double f = 1.0;
+  if (d->time < rf * d->end_t) f = pow(d->time / (rf * d->end_t), 0.5);
+  for (int64_t n = 0; n < d->tri_nn; n++)
+    for (int k = 0; k < 3; k++) {
+      const double vk = f * d->tri_vorig[3 * n + k];
+      d->tri_x[3 * n + k] = d->tri_x[3 * n + k] + vk * d->dt;
+    }
+  tri_normals_planes(d);
+}
+
 /* Preamble of Domain_d::SolveChungHulbert (Solver_explicit.C:120-268). */
 int wfo_init(wfo_domain *d) {
   if (!d->mats || !d->nn) return -1;
@@ -984,6 +1304,7 @@ int wfo_init(wfo_domain *d) {
   d->step_count = 0;
   d->hist_len = 0;
   d->eint = 0.0;
+  if (d->tri_on) tri_setup_surface(d);
   return 0;
 }
 
@@ -1039,7 +1360,10 @@ static void one_step(wfo_domain *d) {
   calc_artificial_viscosity(d);
   calc_elem_forces(d);
   calc_hourglass(d);
-  if (d->contact) calc_contact(d);
+  if (d->tri_on)
+    calc_contact_trimesh(d);
+  else if (d->contact)
+    calc_contact(d);
   assembly_forces(d);
   double r = 0.0;
   if (d->contact) {
@@ -1053,6 +1377,7 @@ static void one_step(wfo_domain *d) {
   update_correction_acc_vel(d);
   for (int k = 0; k < 3; k++) impose_bcv(d, k);
   update_correction_pos(d);
+  if (d->tri_on) tri_move(d);
   {
     double ekin, deint;
     compute_energies(d, &ekin, &deint);

@@ -84,6 +84,14 @@ int wfo_get_elem_tensor(const wfo_domain *d, int which, double *out);
 void wfo_get_derivs(const wfo_domain *d, double *out);
 void wfo_get_elem_forces(const wfo_domain *d, double *f, double *fhg);
 int64_t wfo_get_reaction(const wfo_domain *d, double *out, int64_t cap);
+/* Rigid triangle-mesh contact (Domain_d::CalcContactForces, Contact.C:31-334):
+ * mesh nodes xyz[3 nnodes], triangles tri[3 ntri], uniform velocity vel,
+ * static/dynamic friction, penalty factor (m_contPF). */
+void wfo_set_contact_trimesh(wfo_domain *d, int64_t nnodes, const double *xyz, int64_t ntri,
+                             const int32_t *tri, const double vel[3], double mu_static,
+                             double mu_dynamic, double penalty_factor);
+int64_t wfo_get_trimesh_nodes(const wfo_domain *d, double *out, int64_t cap_nodes);
+int64_t wfo_get_surface(const wfo_domain *d, uint8_t *ext, double *node_area, double *nodlen);
 /* Kinetic energy and accumulated internal energy after each step
  * (Domain_d::computeEnergies, Mechanical.C:2145-2185; Solver_explicit.C:1029-1031). */
 int64_t wfo_get_energies(const wfo_domain *d, double *ekin, double *eint, int64_t cap);

@@ -29,6 +29,10 @@ from weldformfem_gb300 import workloads as W  # noqa: E402
 
 HOLLOMON = dict(model=1, E=200e9, nu=0.3, rho=7850.0, sy0=300e6, hol_K=600e6, hol_m=0.2)
 STAB = [0.3, 0.7, 0.2, 0.08, 0.15, 0.15, 0.8, 0.2, 0.05, 0.0]
+# a 2x2-cell plane of triangles just below the top face of the 3x3x4-cell
+# tetrahedral block (top at z = 2 mm), normal -z, moving down at 5 m/s
+DIE = dict(start=[-0.001, -0.001, 0.002 - 1e-5], end=[0.004, 0.004, 0.0], dens=2, flip=True,
+           vel=[0.0, 0.0, -5.0], mu_s=0.1, mu_d=0.08, pf=0.1, end_t=2e-6)
 
 
 def cases():
@@ -68,6 +72,12 @@ def cases():
         mats.append(m)
     c.materials = mats
     out.append(("hex_octants_linear", c, 300, "step", dict(linear=True)))
+    # rigid triangle-mesh die on perturbed tetrahedra (the reference's own
+    # CalcContactForces; its 3-D surface search is the tetrahedron's)
+    c = W.config(1, scale=(3, 3, 4))
+    c.perturb = 0.1
+    c.bc = "bottom_z"
+    out.append(("tet_die_trimesh", c, 300, "step", dict(linear=True, die=DIE)))
     return out
 
 
@@ -80,6 +90,11 @@ def run_case(name, case, steps, mode, extra):
         d.set_stab(np.array(extra["stab"], float))
     if "av" in extra:
         d.set_artif_visc(*extra["av"])
+    if "die" in extra:
+        die = extra["die"]
+        xyz, tri = W.axis_plane_mesh(die["start"], die["end"], die["dens"], die["flip"])
+        d.set_contact_trimesh(xyz, tri, die["vel"], die["mu_s"], die["mu_d"], die["pf"])
+        d.set_end_time(die["end_t"])
     if mode == "verbatim":
         d.set_end_time(steps * dt)
         with tempfile.TemporaryDirectory() as td:
@@ -100,6 +115,10 @@ def run_case(name, case, steps, mode, extra):
     if mode == "step":
         res["reaction"] = d.reaction()
         res["ekin"], res["eint"] = d.energies()
+    if "die" in extra:
+        res["contforce"] = d.contforce()
+        res["die_nodes"] = d.trimesh_nodes()
+        res["ext"], res["node_area"], res["nodlen"] = d.surface()
     np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **res)
     meta = dict(name=name, mode=mode, steps=steps, extra={k: list(v) if isinstance(v, tuple) else v
                                                            for k, v in extra.items()})

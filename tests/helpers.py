@@ -40,6 +40,11 @@ def setup(dom, case, extra=None):
         dom.set_stab(np.array(extra["stab"], float))
     if "av" in extra:
         dom.set_artif_visc(*extra["av"])
+    if "die" in extra:
+        die = extra["die"]
+        xyz, tri = W.axis_plane_mesh(die["start"], die["end"], die["dens"], die["flip"])
+        dom.set_contact_trimesh(xyz, tri, die["vel"], die["mu_s"], die["mu_d"], die["pf"])
+        dom.set_end_time(die["end_t"])
     return dt
 
 

@@ -56,6 +56,13 @@ def test_oracle_matches_reference_fixture(name, case, steps, mode, extra):
         ekin, eint = d.energies()
         np.testing.assert_array_equal(ekin, g["ekin"])
         np.testing.assert_array_equal(eint, g["eint"])
+    if "contforce" in g:
+        np.testing.assert_array_equal(d.node_vec("contforce"), g["contforce"])
+        np.testing.assert_array_equal(d.trimesh_nodes(), g["die_nodes"])
+        ext, area, nodlen = d.surface()
+        np.testing.assert_array_equal(ext, g["ext"])
+        np.testing.assert_array_equal(area, g["node_area"])
+        np.testing.assert_array_equal(nodlen, g["nodlen"])
 
 
 @pytest.mark.skipif(not R.available(), reason="reference library oracle/_ref not built here")

@@ -286,6 +286,35 @@ def config(cid: int, steps: Optional[int] = None, scale: Optional[tuple] = None)
     return c
 
 
+def axis_plane_mesh(start, end, dens, flip_normals=False):
+    """Rigid plane of triangles normal to z (TriMesh_d::AxisPlaneMesh with
+    axis 2, Mesh.C:48-200, as the JSON driver calls it with the block's start
+    and dim): (dens+1)^2 nodes at z = start[2], spacing (end[0] - start[0]) /
+    dens in x and y from start, two triangles per cell; the normal is +z,
+    or -z with flip_normals. Returns (xyz[n, 3], tri[m, 3])."""
+    dl = (float(end[0]) - float(start[0])) / dens
+    nodes = []
+    x2 = float(start[1])
+    for j in range(dens + 1):
+        x1 = float(start[0])
+        for i in range(dens + 1):
+            nodes.append((x1, x2, float(start[2])))
+            x1 += dl
+        x2 += dl
+    tri = []
+    for j in range(dens):
+        for i in range(dens):
+            n0 = (dens + 1) * j + i
+            n1 = n0 + 1
+            n2 = (dens + 1) * (j + 1) + i
+            n3 = n2 + 1
+            if not flip_normals:
+                tri += [(n0, n1, n2), (n1, n3, n2)]
+            else:
+                tri += [(n0, n2, n1), (n1, n2, n3)]
+    return np.array(nodes, dtype=np.float64), np.array(tri, dtype=np.int32)
+
+
 PARAM_KEYS = ("E", "sy0", "H")
 
 
