@@ -168,6 +168,27 @@ WF_API wf_status wf_set_reaction_nodes(wf_domain *d, int64_t n, const int32_t *n
 WF_API wf_status wf_set_contact_plane(wf_domain *d, double z0, double vz, double kpen, double mu,
                                       int64_t ncand, const int32_t *cand_nodes);
 
+/* Rigid triangle-mesh die (Domain_d::setTriMesh / setContactOn / setContactPF,
+ * Domain_d.h:464, :642, :771; CalcContactForces, Contact.C:31-334): mesh nodes
+ * xyz[3 nnodes], triangles tri[3 ntri] (normal (n1-n0)x(n2-n0) pointing toward
+ * the part), uniform velocity vel[3], static and dynamic Coulomb coefficients
+ * and the penalty factor (reference default 0.1). The part's external surface
+ * is found at wf_init (faces used by one element; tetrahedra with the
+ * reference's triangle table, hexahedra with its quadrilateral table) and each
+ * external node contacts the first triangle it penetrates: normal force
+ * pf * min(E A / l, 0.2 m / dt^2) * depth plus damping, then Coulomb friction
+ * from the accumulated slip. As in the reference, a node keeps its last contact
+ * force after it leaves contact, the die velocity ramps as
+ * sqrt(t / (0.01 end time)) over the first 1 % of the end time, and the
+ * reaction history records the sum of normal-force magnitudes. FP64 precision
+ * only. */
+WF_API wf_status wf_set_contact_trimesh(wf_domain *d, int64_t nnodes, const double *xyz,
+                                        int64_t ntri, const int32_t *tri, const double vel[3],
+                                        double mu_static, double mu_dynamic,
+                                        double penalty_factor);
+/* Current die node positions (3 per node): *n = node count, copies min(cap, *n). */
+WF_API wf_status wf_get_trimesh_nodes(wf_domain *d, double *out, int64_t cap, int64_t *n);
+
 /* ---- batched ensemble --------------------------------------------------------- */
 /* Declares the mesh a batch of nspec independent specimens (no counterpart in
  * the reference, which runs one domain per process): specimen s owns elements
@@ -284,8 +305,14 @@ WF_API wf_status wf_adjoint_backward(wf_domain *d, const double *dL_dR, int32_t 
  * zoneId), then the symmetry-plane BCs, in the reference's order. The time
  * step is cflFactor * (shortest segment between the first four nodes of each
  * element) / sqrt(K / rho), the reference's calcMinEdgeLength in 3-D.
- * Thermal, axisymmetric/plane-strain, Perzyna and rigid-body contact decks
- * return WF_ERR_UNSUPPORTED. Configuration.hourglass3D (not a reference key,
+ * RigidBodies[0] of type Plane becomes a rigid triangle-mesh die
+ * (TriMesh_d::AxisPlaneMesh on axis z from start/dim with partSide cells per
+ * side, flipnormals) moving with the velocity of the boundary condition whose
+ * zoneId is the body's, with the Contact block's fricCoeffStatic,
+ * fricCoeffDynamic and penaltyFactor; as in the reference driver, a contact
+ * deck applies no velocity zones to the part (symmetry planes only).
+ * Thermal, axisymmetric/plane-strain, Perzyna, Line/File rigid bodies and
+ * second rigid bodies return WF_ERR_UNSUPPORTED. Configuration.hourglass3D (not a reference key,
  * default 0 as the reference's 3-D no-op) sets the viscous hourglass
  * coefficient. Errors are written into err (err_len bytes, may be null). */
 typedef struct wf_deck wf_deck;
@@ -301,12 +328,19 @@ typedef struct {
   double artif_visc[2];
   wf_stab stab;
   wf_material material;
+  /* rigid-body die (RigidBodies[0] type Plane) */
+  int32_t contact;
+  int32_t die_nodes, die_tris;
+  double die_vel[3];
+  double mu_static, mu_dynamic, penalty_factor;
 } wf_deck_info;
 WF_API wf_status wf_deck_read(const char *path, wf_deck **out, char *err, int64_t err_len);
 WF_API wf_status wf_deck_free(wf_deck *k);
 WF_API wf_status wf_deck_get_info(const wf_deck *k, wf_deck_info *info);
 /* xyz[3 nn] interleaved, elnod[ne npe]; either may be null. */
 WF_API wf_status wf_deck_get_mesh(const wf_deck *k, double *xyz, int32_t *elnod);
+/* Die of a contact deck: xyz[3 die_nodes], tri[3 die_tris]; either may be null. */
+WF_API wf_status wf_deck_get_die(const wf_deck *k, double *xyz, int32_t *tri);
 /* The n_bc AddBCVelNode calls in order; any array may be null. */
 WF_API wf_status wf_deck_get_bcs(const wf_deck *k, int64_t *node, int32_t *dim, double *val);
 /* Mesh, material, BCs (then AllocateBCs), options, dt and end time onto d. */

@@ -159,7 +159,8 @@ def test_deck_errors(tmp_path):
     cases = [
         (dict(Configuration={"thermal": True}), 5),
         (dict(Configuration={"domType": "AxiSymm"}), 5),
-        (dict(RigidBodies=[{"type": "Plane", "start": [0, 0, 0.005], "dim": [1, 1, 0]}]), 5),
+        (dict(RigidBodies=[{"type": "File", "fileName": "die.nas"}]), 5),
+        (dict(RigidBodies=[{"type": "Plane"}, {"type": "Plane"}]), 5),
         (dict(Materials=[dict(STEEL, type="JohnsonCook")]), 5),
         (dict(DomainBlocks=[{"type": "File", "fileName": "missing.k"}]), 1),
         (dict(BoundaryConditions=[{"zoneId": 3, "value": [0, 0, 1.0]}]), 1),
@@ -199,6 +200,38 @@ def test_reference_example_meshes():
         k = wf.Deck(dp)
         assert k.info["npe"] == npe
         assert k.info["nn"] == counts["NODE"] and k.info["ne"] == counts["ELEMENT_SOLID"]
+
+
+CONTACT = dict(
+    Configuration={"simTime": 2.0e-5, "outTime": 1.0e-5, "cflFactor": 0.3, "zSymm": True},
+    RigidBodies=[{"type": "Plane", "zoneId": 10, "start": [-0.0005, -0.0005, 0.005 - 1e-6],
+                  "dim": [0.0045, 0.0045, 0.0], "partSide": 3, "flipnormals": True}],
+    Contact=[{"fricCoeffStatic": 0.2, "fricCoeffDynamic": 0.15, "penaltyFactor": 0.5}],
+    BoundaryConditions=[{"zoneId": 10, "valueType": 0, "value": [0.0, 0.0, -3.0]},
+                        {"zoneId": 2, "start": [-1, -1, -1], "end": [1, 1, 1e-4],
+                         "value": [0.0, 0.0, 0.0]}])
+
+
+def test_contact_deck(tmp_path):
+    p, _ = box_deck(tmp_path, **CONTACT)
+    k = wf.Deck(p)
+    i = k.info
+    assert i["contact"] == 1 and i["die_nodes"] == 16 and i["die_tris"] == 18
+    assert i["die_vel"] == (0.0, 0.0, -3.0)
+    assert (i["mu_static"], i["mu_dynamic"], i["penalty_factor"]) == (0.2, 0.15, 0.5)
+    xyz, tri = k.die()
+    ex, et = W.axis_plane_mesh([-0.0005, -0.0005, 0.005 - 1e-6], [0.0045, 0.0045, 0.0], 3, True)
+    np.testing.assert_array_equal(xyz, ex)
+    np.testing.assert_array_equal(tri, et)
+    # contact decks apply no velocity zone to the part: only the zSymm plane
+    x, _ = k.mesh()
+    node, dim, val = expected_bcs(x, [], (False, False, True))
+    np.testing.assert_array_equal(k.bcs()[0], node)
+    assert i["zone_nodes"] == 0
+    over = dict(CONTACT)
+    over["Contact"] = [{}]
+    p2, _ = box_deck(tmp_path, **over)
+    assert wf.Deck(p2).info["penalty_factor"] == 0.1
 
 
 def build_cli():
@@ -254,6 +287,23 @@ def test_deck_on_gpu_matches_oracle(tmp_path, kind):
     d2.init()
     d2.solve()
     np.testing.assert_array_equal(d2.node_vec("u"), d.node_vec("u"))
+
+
+@pytest.mark.gpu
+def test_contact_deck_on_gpu_matches_oracle(tmp_path):
+    p, _ = box_deck(tmp_path, **CONTACT)
+    k = wf.Deck(p)
+    d = wf.Domain(wf.WF_FP64)
+    k.apply(d)
+    d.init()
+    n = d.solve()
+    o = O.OracleDomain()
+    k.setup(o)
+    o.init()
+    assert o.solve() == n
+    assert o.reaction().max() > 0
+    assert H.rel_err(d.node_vec("u"), o.node_vec("u")) <= 1e-9
+    assert H.rel_err(d.reaction(), o.reaction()) <= 1e-9
 
 
 @pytest.mark.gpu

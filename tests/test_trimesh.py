@@ -1,0 +1,83 @@
+"""Rigid triangle-mesh contact (wf_set_contact_trimesh) on the GPU.
+
+The oracle's restatement of CalcContactForces is pinned bit-for-bit to the
+reference in tests/test_oracle.py (fixture tet_die_trimesh). Here the FP64
+GPU step with a moving die is checked against the oracle on the same inputs:
+displacements, contact forces, the reaction history and the die position,
+1e-9 relative (the reaction sum runs in a different order on the GPU).
+"""
+import numpy as np
+import pytest
+
+import weldformfem_gb300 as wf
+from oracle import orabind as O
+from tests import helpers as H
+from weldformfem_gb300 import workloads as W
+
+DIE_TET = dict(start=[-0.001, -0.001, 0.002 - 1e-5], end=[0.004, 0.004, 0.0], dens=2, flip=True,
+               vel=[0.0, 0.0, -5.0], mu_s=0.1, mu_d=0.08, pf=0.1, end_t=2e-6)
+DIE_HEX = dict(start=[-0.0005, -0.0005, 0.004 - 2e-6], end=[0.0045, 0.0045, 0.0], dens=3,
+               flip=True, vel=[0.0, 0.0, -4.0], mu_s=0.2, mu_d=0.15, pf=0.3, end_t=1e-5)
+
+
+def cases():
+    t = W.config(1, scale=(3, 3, 4))
+    t.perturb = 0.1
+    t.bc = "bottom_z"
+    h = W.config(0, scale=(4, 4, 4))
+    h.perturb = 0.05
+    h.seed = W.SEED_BASE + 11
+    h.bc = "bottom_z"
+    return {"tet": (t, DIE_TET, 300), "hex_hg": (h, DIE_HEX, 400)}
+
+
+def run(dom, case, die, steps):
+    H.setup(dom, case, {"die": die})
+    dom.init()
+    dom.step(steps) if hasattr(dom, "step") else dom.run(steps)
+    return dom
+
+
+def test_axis_plane_mesh_orientation():
+    xyz, tri = W.axis_plane_mesh((0.0, 0.0, 1.0), (2.0, 0.0, 0.0), 2, flip_normals=True)
+    assert xyz.shape == (9, 3) and tri.shape == (8, 3) and np.all(xyz[:, 2] == 1.0)
+    n = np.cross(xyz[tri[:, 1]] - xyz[tri[:, 0]], xyz[tri[:, 2]] - xyz[tri[:, 0]])
+    assert np.all(n[:, 2] < 0)
+    _, tri2 = W.axis_plane_mesh((0.0, 0.0, 1.0), (2.0, 0.0, 0.0), 2)
+    n2 = np.cross(xyz[tri2[:, 1]] - xyz[tri2[:, 0]], xyz[tri2[:, 2]] - xyz[tri2[:, 0]])
+    assert np.all(n2[:, 2] > 0)
+
+
+def test_oracle_die_pushes_the_part():
+    case, die, steps = cases()["hex_hg"]
+    o = run(O.OracleDomain(), case, die, steps)
+    r = o.reaction()
+    assert r.shape == (steps,) and r.max() > 0 and np.all(np.isfinite(o.node_vec("u")))
+    top = case.top_nodes()
+    assert o.node_vec("u")[top, 2].mean() < 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["tet", "hex_hg"])
+def test_trimesh_contact_matches_oracle(name):
+    case, die, steps = cases()[name]
+    o = run(O.OracleDomain(), case, die, steps)
+    d = wf.Domain(wf.WF_FP64)
+    H.setup(d, case, {"die": die})
+    d.init()
+    d.run(steps)
+    assert H.rel_err(d.node_vec("u"), o.node_vec("u")) <= 1e-9
+    assert H.rel_err(d.node_vec("contforce"), o.node_vec("contforce")) <= 1e-9
+    assert H.rel_err(d.reaction(), o.reaction()) <= 1e-9
+    np.testing.assert_allclose(d.trimesh_nodes(), o.trimesh_nodes(), rtol=1e-12, atol=0)
+    assert o.reaction().max() > 0
+
+
+@pytest.mark.gpu
+def test_trimesh_contact_needs_fp64():
+    case, die, _ = cases()["tet"]
+    d = wf.Domain(wf.WF_MIXED)
+    H.setup(d, case, {"die": die})
+    with pytest.raises(wf.WfError) as e:
+        d.init()
+    assert e.value.status == 5

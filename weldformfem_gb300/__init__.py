@@ -55,7 +55,9 @@ class WfDeckInfo(C.Structure):
                 ("end_time", C.c_double), ("out_time", C.c_double), ("cfl", C.c_double),
                 ("min_length", C.c_double), ("sound_speed", C.c_double),
                 ("hourglass", C.c_double), ("artif_visc", C.c_double * 2), ("stab", WfStab),
-                ("material", WfMaterial)]
+                ("material", WfMaterial), ("contact", C.c_int32), ("die_nodes", C.c_int32),
+                ("die_tris", C.c_int32), ("die_vel", C.c_double * 3), ("mu_static", C.c_double),
+                ("mu_dynamic", C.c_double), ("penalty_factor", C.c_double)]
 
 
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
@@ -124,10 +126,14 @@ _SIGS = {
     "wf_deck_get_info": [C.c_void_p, C.POINTER(WfDeckInfo)],
     "wf_deck_get_mesh": [C.c_void_p, _dp, _ip],
     "wf_deck_get_bcs": [C.c_void_p, _lp, _ip, _dp],
+    "wf_deck_get_die": [C.c_void_p, _dp, _ip],
     "wf_deck_apply": [C.c_void_p, C.c_void_p],
     "wf_load_deck": [C.c_void_p, C.c_char_p, C.POINTER(WfDeckInfo), C.c_char_p, C.c_int64],
     "wf_load_lsdyna": [C.c_void_p, C.c_char_p],
     "wf_write_vtk": [C.c_void_p, C.c_char_p],
+    "wf_set_contact_trimesh": [C.c_void_p, C.c_int64, _dp, C.c_int64, _ip, _dp, C.c_double,
+                               C.c_double, C.c_double],
+    "wf_get_trimesh_nodes": [C.c_void_p, _dp, C.c_int64, C.POINTER(C.c_int64)],
     "wf_set_energy_history": [C.c_void_p, C.c_int32],
     "wf_get_energy_history": [C.c_void_p, _dp, _dp, C.c_int64, C.POINTER(C.c_int64)],
     "wf_adjoint_backward": [C.c_void_p, _dp, C.c_int32, _dp],
@@ -412,6 +418,22 @@ class Domain:
         self._call("wf_get_elem_tensor", ELEM_TENSOR[name], out)
         return out.reshape(-1, 6)
 
+    def set_contact_trimesh(self, xyz, tri, vel, mu_static=0.0, mu_dynamic=0.0,
+                            penalty_factor=0.1):
+        """Rigid triangle-mesh die (setTriMesh + setContactOn + setContactPF)."""
+        xyz = np.ascontiguousarray(xyz, np.float64).reshape(-1)
+        tri = np.ascontiguousarray(tri, np.int32).reshape(-1)
+        self._call("wf_set_contact_trimesh", xyz.size // 3, xyz, tri.size // 3, tri,
+                   np.ascontiguousarray(vel, np.float64), float(mu_static), float(mu_dynamic),
+                   float(penalty_factor))
+
+    def trimesh_nodes(self):
+        n = C.c_int64()
+        self._call("wf_get_trimesh_nodes", np.zeros(3), 0, C.byref(n))
+        out = np.zeros(3 * max(n.value, 1))
+        self._call("wf_get_trimesh_nodes", out, n.value, C.byref(n))
+        return out[: 3 * n.value].reshape(-1, 3)
+
     # input files and output ----------------------------------------------
     def load_deck(self, path):
         """Reads a JSON deck and sets this domain up from it; returns its info."""
@@ -466,8 +488,9 @@ class Deck:
     @staticmethod
     def _info_dict(info):
         out = {f: getattr(info, f) for f, _ in WfDeckInfo._fields_
-               if f not in ("artif_visc", "stab", "material")}
+               if f not in ("artif_visc", "stab", "material", "die_vel")}
         out["artif_visc"] = (info.artif_visc[0], info.artif_visc[1])
+        out["die_vel"] = tuple(info.die_vel[k] for k in range(3))
         out["stab"] = [getattr(info.stab, f) for f, _ in WfStab._fields_]
         m = info.material
         out["material"] = {f: getattr(m, f) for f, _ in WfMaterial._fields_}
@@ -497,6 +520,13 @@ class Deck:
         lib().wf_deck_get_bcs(self.h, node, dim, val)
         return node[:n], dim[:n], val[:n]
 
+    def die(self):
+        """(xyz[n, 3], tri[m, 3]) of a contact deck's die."""
+        x = np.zeros(3 * max(self.info["die_nodes"], 1))
+        t = np.zeros(3 * max(self.info["die_tris"], 1), np.int32)
+        lib().wf_deck_get_die(self.h, x, t)
+        return x[: 3 * self.info["die_nodes"]].reshape(-1, 3), t[: 3 * self.info["die_tris"]].reshape(-1, 3)
+
     def apply(self, dom):
         st = lib().wf_deck_apply(self.h, dom.h)
         if st != 0:
@@ -517,5 +547,9 @@ class Deck:
             dom.set_artif_visc(*i["artif_visc"])
         if i["hourglass"]:
             dom.set_hourglass(i["hourglass"])
+        if i["contact"]:
+            xyz, tri = self.die()
+            dom.set_contact_trimesh(xyz, tri, i["die_vel"], i["mu_static"], i["mu_dynamic"],
+                                    i["penalty_factor"])
         dom.set_dt(i["dt"])
         dom.set_end_time(i["end_time"])

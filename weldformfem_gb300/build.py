@@ -24,13 +24,13 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-fvisibility=hidden",
                  f"-I{os.path.join(ROOT, 'include')}", f"-I{CSRC}"]
 UNITS = {
-    "wf_api.cu": [],
+    "wf_api.cu": ["-Xcompiler", "-ffp-contract=off"],
     "wf_fp64.cu": ["--fmad=false"],
     "wf_mixed.cu": [],
     "wf_reduce.cu": [],
     "wf_noalloc.cu": ["--fmad=false"],
     "wf_adjoint.cu": [],
-    "wf_deck.cpp": [],
+    "wf_deck.cpp": ["-Xcompiler", "-ffp-contract=off"],
 }
 
 

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -119,6 +120,12 @@ struct wf_domain {
   bool contact = false;
   double c_z0 = 0, c_vz = 0, c_k = 0, c_mu = 0;
   std::vector<int32_t> cand;
+  // rigid triangle-mesh contact
+  bool tri = false;
+  std::vector<double> tri_x;
+  std::vector<int32_t> tri_el;
+  double tri_vel[3] = {0, 0, 0};
+  double tri_mu_s = 0.0, tri_mu_d = 0.0, tri_pf = 0.1;
   // device
   bool initialized = false;
   std::vector<void *> allocs;
@@ -251,6 +258,117 @@ bool build_nodel(wf_domain *d) {
   return true;
 }
 
+// Triangle normals and plane coefficients (TriMesh_d::CalcNormals,
+// UpdatePlaneCoeff with far node 2; Mesh.h:236-284).
+void tri_normals_planes(const std::vector<double> &x, const std::vector<int32_t> &el,
+                        std::vector<double> &nrm, std::vector<double> &pp) {
+  const size_t ne = el.size() / 3;
+  nrm.assign(3 * ne, 0.0);
+  pp.assign(ne, 0.0);
+  for (size_t e = 0; e < ne; e++) {
+    const double *p0 = &x[3 * el[3 * e]], *p1 = &x[3 * el[3 * e + 1]], *p2 = &x[3 * el[3 * e + 2]];
+    const double u[3] = {p1[0] - p0[0], p1[1] - p0[1], p1[2] - p0[2]};
+    const double v[3] = {p2[0] - p0[0], p2[1] - p0[1], p2[2] - p0[2]};
+    const double w[3] = {u[1] * v[2] - u[2] * v[1], u[2] * v[0] - u[0] * v[2],
+                         u[0] * v[1] - u[1] * v[0]};
+    const double len = std::sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+    const double inv = 1.0 / len;
+    double *n = &nrm[3 * e];
+    n[0] = w[0] * inv;
+    n[1] = w[1] * inv;
+    n[2] = w[2] * inv;
+    pp[e] = p2[0] * n[0] + p2[1] * n[1] + p2[2] * n[2];
+  }
+}
+
+double tri_area(const double *p0, const double *p1, const double *p2) {
+  const double v1[3] = {p1[0] - p0[0], p1[1] - p0[1], p1[2] - p0[2]};
+  const double v2[3] = {p2[0] - p0[0], p2[1] - p0[1], p2[2] - p0[2]};
+  const double c[3] = {v1[1] * v2[2] - v1[2] * v2[1], v1[2] * v2[0] - v1[0] * v2[2],
+                       v1[0] * v2[1] - v1[1] * v2[0]};
+  return 0.5 * std::sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+}
+
+// External surface of the part (SearchExtNodes + CalcExtFaceAreas,
+// Domain_d.C:110-290): faces used by one element are external, their area goes
+// in equal shares to their nodes (faces in element order and local order;
+// tetrahedra with the reference's triangle table, hexahedra with its
+// quadrilateral table, a quadrilateral's area as triangles (0,1,2) + (0,2,3)).
+// Element length: the smallest height of the tetrahedron of the element's
+// first four nodes (calcMinEdgeLength, Domain_d.C:2236-2262); nodlen is its
+// mean over the node's elements (Contact.C:145-152).
+void part_surface(const wf_domain *d, std::vector<uint8_t> &ext, std::vector<double> &area,
+                  std::vector<double> &nodlen) {
+  static const int TF[4][3] = {{0, 1, 2}, {0, 1, 3}, {1, 2, 3}, {0, 2, 3}};
+  static const int HF[6][4] = {{0, 1, 2, 3}, {4, 5, 6, 7}, {0, 1, 5, 4},
+                               {2, 3, 7, 6}, {0, 3, 7, 4}, {1, 2, 6, 5}};
+  const int npe = d->npe, nf = npe == 8 ? 6 : 4, fn = npe == 8 ? 4 : 3;
+  std::map<std::array<int32_t, 4>, int> count;
+  auto face = [&](int64_t e, int f, int32_t *fnodes) {
+    std::array<int32_t, 4> k{-1, -1, -1, -1};
+    for (int q = 0; q < fn; q++) {
+      fnodes[q] = d->elnod[e * npe + (npe == 8 ? HF[f][q] : TF[f][q])];
+      k[q] = fnodes[q];
+    }
+    std::sort(k.begin(), k.begin() + fn);
+    return k;
+  };
+  int32_t fnodes[4];
+  for (int64_t e = 0; e < d->ne; e++)
+    for (int f = 0; f < nf; f++) count[face(e, f, fnodes)]++;
+  ext.assign(d->nn, 0);
+  area.assign(d->nn, 0.0);
+  nodlen.assign(d->nn, 0.0);
+  const double *X = d->x.data();
+  for (int64_t e = 0; e < d->ne; e++)
+    for (int f = 0; f < nf; f++) {
+      if (count[face(e, f, fnodes)] != 1) continue;
+      const double *p0 = &X[3 * fnodes[0]], *p1 = &X[3 * fnodes[1]], *p2 = &X[3 * fnodes[2]];
+      double share;
+      if (fn == 3) {
+        share = tri_area(p0, p1, p2) / 3.0;
+      } else {
+        const double *p3 = &X[3 * fnodes[3]];
+        share = (tri_area(p0, p1, p2) + tri_area(p0, p2, p3)) / 4.0;
+      }
+      for (int q = 0; q < fn; q++) {
+        ext[fnodes[q]] = 1;
+        area[fnodes[q]] += share;
+      }
+    }
+  std::vector<double> elen(d->ne);
+  for (int64_t e = 0; e < d->ne; e++) {
+    const int32_t *n = &d->elnod[e * npe];
+    const double *A = &X[3 * n[0]], *B = &X[3 * n[1]], *C = &X[3 * n[2]], *D = &X[3 * n[3]];
+    const double *faces[4][3] = {{B, C, D}, {A, C, D}, {A, B, D}, {A, B, C}};
+    double hmin = 1.0e6;
+    for (int i = 0; i < 4; i++) {
+      const double *f0 = faces[i][0], *f1 = faces[i][1], *f2 = faces[i][2];
+      const double x1[3] = {f1[0] - f0[0], f1[1] - f0[1], f1[2] - f0[2]};
+      const double x2[3] = {f2[0] - f0[0], f2[1] - f0[1], f2[2] - f0[2]};
+      double nn[3] = {x1[1] * x2[2] - x1[2] * x2[1], x1[2] * x2[0] - x1[0] * x2[2],
+                      x1[0] * x2[1] - x1[1] * x2[0]};
+      const double ar = std::sqrt(nn[0] * nn[0] + nn[1] * nn[1] + nn[2] * nn[2]);
+      if (ar < 1e-12) continue;
+      const double inv = 1.0 / ar;
+      nn[0] *= inv;
+      nn[1] *= inv;
+      nn[2] *= inv;
+      const double *P = &X[3 * n[i]];
+      const double vec[3] = {P[0] - f0[0], P[1] - f0[1], P[2] - f0[2]};
+      const double h = std::fabs(vec[0] * nn[0] + vec[1] * nn[1] + vec[2] * nn[2]);
+      if (h < hmin) hmin = h;
+    }
+    elen[e] = hmin;
+  }
+  for (int64_t i = 0; i < d->nn; i++) {
+    double l = 0.0;
+    const int32_t b = d->nodel_off[i], c = d->nodel_cnt[i];
+    for (int32_t k = 0; k < c; k++) l += elen[d->nodel[b + k]];
+    nodlen[i] = l / c;
+  }
+}
+
 void reset_mesh(wf_domain *d) {
   free_device(d);
   for (int k = 0; k < 3; k++) {
@@ -261,6 +379,9 @@ void reset_mesh(wf_domain *d) {
   d->react_nodes.clear();
   d->cand.clear();
   d->contact = false;
+  d->tri = false;
+  d->tri_x.clear();
+  d->tri_el.clear();
   d->bcs_allocated = false;
   d->nspec = 0;
   d->spec_eoff.clear();
@@ -521,6 +642,14 @@ WF_API wf_status wf_set_dt(wf_domain *d, double dt) {
 WF_API wf_status wf_set_end_time(wf_domain *d, double t) {
   if (!d) return WF_ERR_ARG;
   d->end_t = t;
+  if (d->initialized && d->P.end_t != t) {
+    // the die ramp of triangle-mesh contact reads the end time
+    d->P.end_t = t;
+    if (d->graph) {
+      cudaGraphExecDestroy(d->graph);
+      d->graph = nullptr;
+    }
+  }
   return WF_OK;
 }
 
@@ -604,6 +733,42 @@ WF_API wf_status wf_set_contact_plane(wf_domain *d, double z0, double vz, double
 }
 
 // ---- batched ensemble ------------------------------------------------------------
+WF_API wf_status wf_set_contact_trimesh(wf_domain *d, int64_t nnodes, const double *xyz,
+                                        int64_t ntri, const int32_t *tri, const double vel[3],
+                                        double mu_static, double mu_dynamic,
+                                        double penalty_factor) {
+  wf_status s = need_mesh(d);
+  if (s) return s;
+  if (!xyz || !tri || !vel || nnodes < 3 || ntri < 1) return WF_ERR_ARG;
+  if (d->initialized) return fail(d, WF_ERR_STATE, "the contact mesh is set before init");
+  for (int64_t i = 0; i < 3 * ntri; i++)
+    if (tri[i] < 0 || tri[i] >= nnodes)
+      return fail(d, WF_ERR_ARG, "triangle %lld references node %d", (long long)(i / 3), tri[i]);
+  d->tri = true;
+  d->tri_x.assign(xyz, xyz + 3 * nnodes);
+  d->tri_el.assign(tri, tri + 3 * ntri);
+  for (int k = 0; k < 3; k++) d->tri_vel[k] = vel[k];
+  d->tri_mu_s = mu_static;
+  d->tri_mu_d = mu_dynamic;
+  d->tri_pf = penalty_factor;
+  d->contact = true;
+  return WF_OK;
+}
+
+WF_API wf_status wf_get_trimesh_nodes(wf_domain *d, double *out, int64_t cap, int64_t *n) {
+  if (!d || !n) return WF_ERR_ARG;
+  if (!d->initialized || !d->P.tri_on) return fail(d, WF_ERR_STATE, "no contact mesh on the device");
+  CUDA_TRY(cudaSetDevice(d->device));
+  *n = d->P.tri_nn;
+  const int64_t m = std::min<int64_t>(cap, d->P.tri_nn);
+  if (out && m > 0) {
+    CUDA_TRY(cudaMemcpyAsync(out, d->P.tri_x, sizeof(double) * 3 * m, cudaMemcpyDeviceToHost,
+                             d->stream));
+    CUDA_TRY(cudaStreamSynchronize(d->stream));
+  }
+  return WF_OK;
+}
+
 WF_API wf_status wf_set_specimens(wf_domain *d, int32_t nspec, const int64_t *elem_off,
                                   const int64_t *node_off, const double *dt) {
   wf_status s = need_mesh(d);
@@ -799,6 +964,8 @@ WF_API wf_status wf_init(wf_domain *d) {
   }
   if (d->nspec && d->contact)
     return fail(d, WF_ERR_UNSUPPORTED, "contact is not supported in a batched ensemble");
+  if (d->tri && d->precision != WF_FP64)
+    return fail(d, WF_ERR_UNSUPPORTED, "triangle-mesh contact runs in the FP64 step");
   if (d->nspec && d->energy)
     return fail(d, WF_ERR_UNSUPPORTED, "the energy history is not kept for a batched ensemble");
   CUDA_TRY(cudaSetDevice(d->device));
@@ -862,6 +1029,41 @@ WF_API wf_status wf_init(wf_domain *d) {
   std::vector<uint8_t> flags(nn, 0);
   for (int32_t n : d->react_nodes) flags[n] |= NF_REACTION;
   for (int32_t n : d->cand) flags[n] |= NF_CONTACT;
+  P.end_t = d->end_t;
+  if (d->tri) {
+    std::vector<uint8_t> ext;
+    std::vector<double> area, nodlen, nrm, pp;
+    part_surface(d, ext, area, nodlen);
+    for (int64_t n = 0; n < nn; n++)
+      if (ext[n]) flags[n] |= NF_CONTACT;
+    tri_normals_planes(d->tri_x, d->tri_el, nrm, pp);
+    std::vector<double> tv(d->tri_x.size());
+    for (size_t i = 0; i < tv.size(); i++) tv[i] = d->tri_vel[i % 3];
+    double *tx = nullptr, *tvd = nullptr, *tn = nullptr, *tp = nullptr, *na = nullptr,
+           *nl = nullptr;
+    int32_t *te = nullptr;
+    CUDA_TRY(upload(d, &tx, d->tri_x));
+    CUDA_TRY(upload(d, &tvd, tv));
+    CUDA_TRY(upload(d, &tn, nrm));
+    CUDA_TRY(upload(d, &tp, pp));
+    CUDA_TRY(upload(d, &te, d->tri_el));
+    CUDA_TRY(upload(d, &na, area));
+    CUDA_TRY(upload(d, &nl, nodlen));
+    P.tri_on = 1;
+    P.tri_nn = (int32_t)(d->tri_x.size() / 3);
+    P.tri_ne = (int32_t)(d->tri_el.size() / 3);
+    P.tri_x = tx;
+    P.tri_v = tvd;
+    P.tri_nrm = tn;
+    P.tri_pp = tp;
+    P.tri_el = te;
+    P.node_area = na;
+    P.nodlen = nl;
+    P.tri_mu_s = d->tri_mu_s;
+    P.tri_mu_d = d->tri_mu_d;
+    P.tri_pf = d->tri_pf;
+    P.tri_E0 = d->mats[0].E;
+  }
   uint8_t *fl = nullptr;
   CUDA_TRY(upload(d, &fl, flags));
   P.nflag = fl;

@@ -475,6 +475,8 @@ double ref_min_length(const std::vector<double> &x, const std::vector<int32_t> &
 // ---- deck object ---------------------------------------------------------------------
 struct wf_deck {
   wf_deck_info info{};
+  std::vector<double> die_x;
+  std::vector<int32_t> die_tri;
   std::vector<double> x;
   std::vector<int32_t> elnod;
   std::vector<int64_t> bc_node;
@@ -625,10 +627,56 @@ WF_API wf_status wf_deck_read(const char *path, wf_deck **out, char *err, int64_
   I.nn = (int64_t)(k->x.size() / 3);
   I.ne = (int64_t)(k->elnod.size() / I.npe);
 
-  // Rigid bodies: contact decks need the general triangle-mesh contact
+  // Rigid bodies (main.C:633-750): one Plane body becomes a triangle-mesh die
   std::string rtype;
-  if (rig && rig->at(0) && jstr(rig->at(0), "type", rtype))
-    return bad("rigid-body contact (" + rtype + ") is not supported", WF_ERR_UNSUPPORTED);
+  int die_zone = 0;
+  const JVal *r0 = rig ? rig->at(0) : nullptr;
+  if (r0 && jstr(r0, "type", rtype)) {
+    if (rtype != "Plane")
+      return bad("rigid body type " + rtype + " is not supported", WF_ERR_UNSUPPORTED);
+    if (rig->arr.size() > 1) return bad("a second rigid body is not supported", WF_ERR_UNSUPPORTED);
+    double st[3] = {0, 0, 0}, dm[3] = {0, 0, 0};
+    jvec(r0, "start", st, 3);
+    jvec(r0, "dim", dm, 3);
+    bool flip = false;
+    jbool(r0, "flipnormals", flip);
+    int dens = 1;
+    jint(r0, "partSide", dens);
+    jint(r0, "zoneId", die_zone);
+    if (dens < 1) return bad("RigidBodies partSide must be >= 1");
+    // TriMesh_d::AxisPlaneMesh(id, axis 2, !flipnormals, start, dim, partSide)
+    // (Mesh.C:48-200): (dens+1)^2 nodes at z = start.z spaced (dim.x - start.x) / dens
+    const double dl = (dm[0] - st[0]) / dens;
+    double x2 = st[1];
+    for (int jj = 0; jj <= dens; jj++) {
+      double x1 = st[0];
+      for (int ii = 0; ii <= dens; ii++) {
+        k->die_x.push_back(x1);
+        k->die_x.push_back(x2);
+        k->die_x.push_back(st[2]);
+        x1 += dl;
+      }
+      x2 += dl;
+    }
+    for (int jj = 0; jj < dens; jj++)
+      for (int ii = 0; ii < dens; ii++) {
+        const int32_t n0 = (dens + 1) * jj + ii, n1 = n0 + 1, n2 = (dens + 1) * (jj + 1) + ii,
+                      n3 = n2 + 1;
+        const int32_t t[2][3] = {{n0, n1, n2}, {n1, n3, n2}};
+        const int32_t tf[2][3] = {{n0, n2, n1}, {n1, n2, n3}};
+        for (int q = 0; q < 2; q++)
+          for (int c = 0; c < 3; c++) k->die_tri.push_back(flip ? tf[q][c] : t[q][c]);
+      }
+    I.contact = 1;
+    I.die_nodes = (int32_t)(k->die_x.size() / 3);
+    I.die_tris = (int32_t)(k->die_tri.size() / 3);
+    I.penalty_factor = 0.1;  // Domain_d constructor (Domain_d.h:256)
+    const JVal *c0 = j.get("Contact") ? j.get("Contact")->at(0) : nullptr;
+    jnum(c0, "fricCoeffStatic", I.mu_static);
+    jnum(c0, "fricCoeffDynamic", I.mu_dynamic);
+    double pf = -1.0;
+    if (jnum(c0, "penaltyFactor", pf) && pf > -1.0) I.penalty_factor = pf;
+  }
 
   // BoundaryConditions: AddBCVelZone per condition, in order (main.C:578-887)
   const double *X = k->x.data();
@@ -641,6 +689,15 @@ WF_API wf_status wf_deck_read(const char *path, wf_deck **out, char *err, int64_
     for (const JVal &bc : bcs->arr) {
       double st[3] = {0, 0, 0}, en[3] = {0, 0, 0}, val[3] = {0, 0, 0};
       jvec(&bc, "value", val, 3);
+      if (I.contact) {
+        // contact decks: the body's zone gives the die velocity and no zone
+        // condition acts on the part (main.C:690-700, :737-750)
+        int zid = -1;
+        jint(&bc, "zoneId", zid);
+        if (zid == die_zone)
+          for (int q = 0; q < 3; q++) I.die_vel[q] = val[q];
+        continue;
+      }
       bool have = jvec(&bc, "start", st, 3) && jvec(&bc, "end", en, 3);
       if (!have) {
         // a condition without its own box takes the DomainZones entry of its zoneId
@@ -704,6 +761,13 @@ WF_API wf_status wf_deck_get_mesh(const wf_deck *k, double *xyz, int32_t *elnod)
   return WF_OK;
 }
 
+WF_API wf_status wf_deck_get_die(const wf_deck *k, double *xyz, int32_t *tri) {
+  if (!k) return WF_ERR_ARG;
+  if (xyz) std::memcpy(xyz, k->die_x.data(), sizeof(double) * k->die_x.size());
+  if (tri) std::memcpy(tri, k->die_tri.data(), sizeof(int32_t) * k->die_tri.size());
+  return WF_OK;
+}
+
 WF_API wf_status wf_deck_get_bcs(const wf_deck *k, int64_t *node, int32_t *dim, double *val) {
   if (!k) return WF_ERR_ARG;
   const size_t n = k->bc_node.size();
@@ -731,6 +795,10 @@ WF_API wf_status wf_deck_apply(const wf_deck *k, wf_domain *d) {
   if (I.artif_visc[0] != 0.0 || I.artif_visc[1] != 0.0)
     WF_DECK_TRY(wf_set_artif_visc(d, I.artif_visc[0], I.artif_visc[1]));
   if (I.hourglass != 0.0) WF_DECK_TRY(wf_set_hourglass(d, I.hourglass));
+  if (I.contact)
+    WF_DECK_TRY(wf_set_contact_trimesh(d, I.die_nodes, k->die_x.data(), I.die_tris,
+                                       k->die_tri.data(), I.die_vel, I.mu_static, I.mu_dynamic,
+                                       I.penalty_factor));
   WF_DECK_TRY(wf_set_dt(d, I.dt));
   WF_DECK_TRY(wf_set_end_time(d, I.end_time));
 #undef WF_DECK_TRY

@@ -443,6 +443,128 @@ __device__ __forceinline__ double block_sum(double v, double *sh) {
   return t;
 }
 
+// Rigid triangle-mesh contact of one external node (Domain_d::CalcContactForces,
+// Contact.C:31-334): the first triangle, in order, that the node penetrates
+// (d < 0 with its projection inside the triangle) gives the penalty normal
+// force pf * min(E A / l, 0.2 m / dt^2) * d plus damping, then Coulomb
+// friction from the accumulated tangential slip (static cap, else dynamic
+// force along -v_t, slip reset). A node out of contact keeps its last contact
+// force, as in the reference. Returns the normal-force magnitude (reaction).
+__device__ __forceinline__ double tri_contact(const StepParams &P, const Fp64State &S, int64_t n,
+                                              const double (&x)[3], const double (&v)[3],
+                                              double m, double (&cf)[3]) {
+  const int64_t np = P.np;
+  cf[0] = S.cf[n];
+  cf[1] = S.cf[np + n];
+  cf[2] = S.cf[2 * np + n];
+  double cfn = 0.0;
+  for (int32_t j = 0; j < P.tri_ne; j++) {
+    const double n0 = P.tri_nrm[3 * j], n1 = P.tri_nrm[3 * j + 1], n2 = P.tri_nrm[3 * j + 2];
+    const double dd = (n0 * x[0] + n1 * x[1] + n2 * x[2]) - P.tri_pp[j];
+    if (!(dd < 0)) continue;
+    const double Q[3] = {x[0] - n0 * dd, x[1] - n1 * dd, x[2] - n2 * dd};
+    bool inside = true;
+    for (int l = 0; l < 3 && inside; l++) {
+      const int nx = l + 1 > 2 ? 0 : l + 1;
+      const double *a = &P.tri_x[3 * P.tri_el[3 * j + l]];
+      const double *b = &P.tri_x[3 * P.tri_el[3 * j + nx]];
+      const double e1[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]};
+      const double e2[3] = {Q[0] - a[0], Q[1] - a[1], Q[2] - a[2]};
+      const double c0 = e1[1] * e2[2] - e1[2] * e2[1];
+      const double c1 = e1[2] * e2[0] - e1[0] * e2[2];
+      const double c2 = e1[0] * e2[1] - e1[1] * e2[0];
+      const double crit = c0 * n0 + c1 * n1 + c2 * n2;
+      if (crit < 0.0) inside = false;
+    }
+    if (!inside) continue;
+    const double dt = P.dt;
+    const double v_reln = v[0] * n0 + v[1] * n1 + v[2] * n2;
+    const double kgeo = P.tri_E0 * P.node_area[n] / P.nodlen[n];
+    const double kmass = 0.2 * m / (dt * dt);
+    const double k = (kmass < kgeo) ? kmass : kgeo;
+    const double omega = sqrt(k / m);
+    const double ccrit = 2.0 * m * omega;
+    const double F_damp = 0.2 * ccrit * v_reln;
+    const double F_normal = P.tri_pf * k * dd;
+    const double sc = -(F_normal + F_damp);
+    cf[0] = n0 * sc;
+    cf[1] = n1 * sc;
+    cf[2] = n2 * sc;
+    cfn = sqrt(cf[0] * cf[0] + cf[1] * cf[1] + cf[2] * cf[2]);
+    // friction
+    const double vn = v[0] * n0 + v[1] * n1 + v[2] * n2;
+    const double vt[3] = {v[0] - n0 * vn, v[1] - n1 * vn, v[2] - n2 * vn};
+    double ut[3] = {S.ut[n], S.ut[np + n], S.ut[2 * np + n]};
+    const double du[3] = {vt[0] * dt, vt[1] * dt, vt[2] * dt};
+    const double ua[3] = {ut[0] + du[0], ut[1] + du[1], ut[2] + du[2]};
+    ut[0] += du[0];
+    ut[1] += du[1];
+    ut[2] += du[2];
+    const double mk = -k;
+    const double ft[3] = {ua[0] * mk, ua[1] * mk, ua[2] * mk};
+    const double ft_mag = sqrt(ft[0] * ft[0] + ft[1] * ft[1] + ft[2] * ft[2]);
+    const double cn = cf[0] * n0 + cf[1] * n1 + cf[2] * n2;
+    const double Fn[3] = {n0 * cn, n1 * cn, n2 * cn};
+    const double fn_norm = sqrt(Fn[0] * Fn[0] + Fn[1] * Fn[1] + Fn[2] * Fn[2]);
+    double F[3];
+    if (ft_mag <= P.tri_mu_s * fn_norm) {
+      F[0] = ft[0];
+      F[1] = ft[1];
+      F[2] = ft[2];
+    } else {
+      const double md = -(P.tri_mu_d * fn_norm);
+      const double vnorm = sqrt(vt[0] * vt[0] + vt[1] * vt[1] + vt[2] * vt[2]);
+      const double inv = 1.0 / vnorm;
+      F[0] = (vt[0] * md) * inv;
+      F[1] = (vt[1] * md) * inv;
+      F[2] = (vt[2] * md) * inv;
+      ut[0] = ut[1] = ut[2] = 0.0;
+    }
+    S.ut[n] = ut[0];
+    S.ut[np + n] = ut[1];
+    S.ut[2 * np + n] = ut[2];
+    cf[0] += F[0];
+    cf[1] += F[1];
+    cf[2] += F[2];
+    break;
+  }
+  S.cf[n] = cf[0];
+  S.cf[np + n] = cf[1];
+  S.cf[2 * np + n] = cf[2];
+  return cfn;
+}
+
+// End of the loop body (Solver_explicit.C:980-1004), run by the last block of
+// the node kernel once every node has been updated: the die velocity ramps as
+// sqrt(Time / (0.01 end_t)) over the first 1 % of the end time, the mesh moves
+// by v dt, and normals and plane coefficients are recomputed (far node 2).
+__device__ void tri_move(const StepParams &P, double time) {
+  const double rf = 1.0e-2;
+  double f = 1.0;
+  if (time < rf * P.end_t) f = pow(time / (rf * P.end_t), 0.5);
+  for (int32_t i = threadIdx.x; i < 3 * P.tri_nn; i += blockDim.x) {
+    const double vk = f * P.tri_v[i];
+    P.tri_x[i] = P.tri_x[i] + vk * P.dt;
+  }
+  __syncthreads();
+  for (int32_t e = threadIdx.x; e < P.tri_ne; e += blockDim.x) {
+    const double *p0 = &P.tri_x[3 * P.tri_el[3 * e]];
+    const double *p1 = &P.tri_x[3 * P.tri_el[3 * e + 1]];
+    const double *p2 = &P.tri_x[3 * P.tri_el[3 * e + 2]];
+    const double u[3] = {p1[0] - p0[0], p1[1] - p0[1], p1[2] - p0[2]};
+    const double w0[3] = {p2[0] - p0[0], p2[1] - p0[1], p2[2] - p0[2]};
+    const double w[3] = {u[1] * w0[2] - u[2] * w0[1], u[2] * w0[0] - u[0] * w0[2],
+                         u[0] * w0[1] - u[1] * w0[0]};
+    const double len = sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+    const double inv = 1.0 / len;
+    const double nn0 = w[0] * inv, nn1 = w[1] * inv, nn2 = w[2] * inv;
+    P.tri_nrm[3 * e] = nn0;
+    P.tri_nrm[3 * e + 1] = nn1;
+    P.tri_nrm[3 * e + 2] = nn2;
+    P.tri_pp[e] = p2[0] * nn0 + p2[1] * nn1 + p2[2] * nn2;
+  }
+}
+
 // nodes: assemblyForces (Matrices.C:42-87) as a gather over the node's
 // element list, the non-finite clamp (Solver_explicit.C:777-785), plane
 // contact (Contact.C:58-323), calcAccel (Mechanical.C:321-341), ImposeBCA,
@@ -494,7 +616,9 @@ __global__ void __launch_bounds__(kNodeThreads) k_fp64_nodes(StepParams P, Fp64S
       u[k] = S.u[k * np + n];
     }
     double cf[3] = {0.0, 0.0, 0.0};
-    if (P.contact && (fl & NF_CONTACT)) {
+    if (P.tri_on) {
+      if (fl & NF_CONTACT) r = tri_contact(P, S, n, x, vp, mass, cf);
+    } else if (P.contact && (fl & NF_CONTACT)) {
       // rigid plane, outward normal (0, 0, -1), at z0 + vz * Time
       const double zd = P.c_z0 + P.c_vz * time;
       const double gap = zd - x[2];
@@ -587,6 +711,7 @@ __global__ void __launch_bounds__(kNodeThreads) k_fp64_nodes(StepParams P, Fp64S
       P.st->time = time + P.dt;
       P.st->done_blocks = 0u;
     }
+    if (P.tri_on) tri_move(P, time);
   }
 }
 

@@ -98,6 +98,17 @@ struct StepParams {
   double *partials;       // [grid of the node kernel]
   double *hist;           // [hist_cap]
   int64_t hist_cap;
+  // rigid triangle-mesh contact (FP64 path; one mesh with a uniform velocity)
+  int32_t tri_on;
+  int32_t tri_nn, tri_ne;
+  double *tri_x;            // [3 tri_nn] node positions, moved every step
+  const double *tri_v;      // [3 tri_nn] velocity before the start-up ramp
+  double *tri_nrm;          // [3 tri_ne] unit normals
+  double *tri_pp;           // [tri_ne] plane coefficients
+  const int32_t *tri_el;    // [3 tri_ne]
+  const double *node_area;  // [nn] external-surface area share of each node
+  const double *nodlen;     // [nn] mean element length at each node
+  double tri_mu_s, tri_mu_d, tri_pf, tri_E0, end_t;
   // energy history (Domain_d::computeEnergies after every step), when on
   int32_t energy_on;
   double *epart;          // [2 * grid of the energy kernel]
