@@ -44,7 +44,7 @@ typedef enum {
 
 typedef enum { WF_FP64 = 0, WF_MIXED = 1 } wf_precision;
 
-typedef enum { WF_MAT_BILINEAR = 0, WF_MAT_HOLLOMON = 1 } wf_material_model;
+typedef enum { WF_MAT_BILINEAR = 0, WF_MAT_HOLLOMON = 1, WF_MAT_JOHNSON_COOK = 2 } wf_material_model;
 
 /* Material_ + Elastic_ (include/common/Material.cuh:15-156). BILINEAR is
  * linear isotropic hardening sigma_y = sy0 + H eps_p. HOLLOMON is the
@@ -119,6 +119,20 @@ WF_API wf_status wf_set_density(wf_domain *d, double rho);
 /* Domain_d::AssignMaterial (Domain_d.C:903): material table; entry 0 is the
  * default of every element. Sets the density of every element to mats[0].rho. */
 WF_API wf_status wf_set_materials(wf_domain *d, int32_t nmat, const wf_material *mats);
+/* Material_::Init_JohnsonCook (Material.cuh:105-114) for a material of model
+ * WF_MAT_JOHNSON_COOK: sigma_y = (sy0 + B eps_p^n) (1 + C ln(edot / eps0_dot))
+ * (1 - T_h^m), T_h = (T - T_transition) / (T_melt - T_transition), and the
+ * tangent modulus n B eps_p^(n-1) (1 + C ln(edot' / eps0_dot)) (1 - T_h^m)
+ * (E / 10 at eps_p = 0) of the radial return (CalcJohnsonCookYieldStress,
+ * CalcJohnsonCookTangentModulus, Material.cuh:377-410; CalcStressStrain,
+ * Mechanical.C:1701-1770). edot is the element's effective strain rate
+ * sqrt(((Dxx-Dyy)^2 + (Dyy-Dzz)^2 + (Dzz-Dxx)^2) / 2 + 3 (Dxy^2 + Dyz^2 + Dxz^2))
+ * (1e-5 where it is exactly 0) and edot' = min(edot, 1e6). T is the
+ * (uniform) temperature of the material's elements: thermal coupling is not
+ * built. Call after wf_set_materials and before wf_init. */
+WF_API wf_status wf_set_johnson_cook(wf_domain *d, int32_t mat, double B, double n, double C,
+                                     double eps0_dot, double m, double T_melt,
+                                     double T_transition, double T);
 /* Per-element material index (the reference's mat[e] pointers). */
 WF_API wf_status wf_set_elem_materials(wf_domain *d, const int32_t *ids);
 
@@ -298,7 +312,9 @@ WF_API wf_status wf_adjoint_backward(wf_domain *d, const double *dL_dR, int32_t 
  * Read: Configuration (simTime, outTime, cflFactor, pressAlgorithm,
  * artifViscCoeffs, xSymm/ySymm/zSymm, symtol), Stabilization, Materials[0]
  * (Bilinear: const[0] = tangent modulus Et, H = E Et / (E - Et); Hollomon:
- * const = [K, n]), DomainBlocks[0] (File: an LS-DYNA .k mesh, path relative to
+ * const = [K, n]; JohnsonCook: A = yieldStress0, const = [B, n, C, eps0_dot]
+ * with m = 1, T_melt = 1e10, T_transition = 0 as the non-thermal driver sets
+ * them, temperature 0), DomainBlocks[0] (File: an LS-DYNA .k mesh, path relative to
  * the deck; Box: a 3-D box of elemLength cells, elemType TriTet for
  * tetrahedra) and BoundaryConditions (one velocity zone per condition, from
  * its start/end box or, when it has none, from the DomainZones entry of its
@@ -333,6 +349,8 @@ typedef struct {
   int32_t die_nodes, die_tris;
   double die_vel[3];
   double mu_static, mu_dynamic, penalty_factor;
+  /* Johnson-Cook material: B, n, C, eps0_dot, m, T_melt, T_transition, T */
+  double johnson_cook[8];
 } wf_deck_info;
 WF_API wf_status wf_deck_read(const char *path, wf_deck **out, char *err, int64_t err_len);
 WF_API wf_status wf_deck_free(wf_deck *k);

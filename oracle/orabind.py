@@ -63,6 +63,7 @@ def lib():
         "wfo_get_connectivity": ([vp, _ip, _ip, _ip, _ip, _ip], None),
         "wfo_set_materials": ([vp, C.c_int, C.POINTER(WfoMaterial)], C.c_int),
         "wfo_set_elem_materials": ([vp, _ip], C.c_int),
+        "wfo_set_johnson_cook": ([vp, C.c_int] + [C.c_double] * 8, C.c_int),
         "wfo_add_bc_vel_node": ([vp, i64, C.c_int, C.c_double], C.c_int),
         "wfo_allocate_bcs": ([vp], C.c_int),
         "wfo_set_reaction_nodes": ([vp, i64, _ip, C.c_int], C.c_int),
@@ -183,6 +184,11 @@ class OracleDomain:
         if elem_ids is not None:
             self._check(lib().wfo_set_elem_materials(self.h, np.ascontiguousarray(elem_ids, np.int32)),
                         "set_elem_materials")
+
+    def set_johnson_cook(self, mat, B, n, C, eps0, m, Tm, Tt, T=0.0):
+        self._check(lib().wfo_set_johnson_cook(self.h, int(mat), float(B), float(n), float(C),
+                                               float(eps0), float(m), float(Tm), float(Tt),
+                                               float(T)), "set_johnson_cook")
 
     def set_hourglass(self, coef):
         lib().wfo_set_hourglass(self.h, float(coef))

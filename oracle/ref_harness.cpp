@@ -67,6 +67,7 @@ class RefDomain : public Domain_d {
   std::vector<double> ekin_hist, eint_hist;  // computeEnergies after every step
   double eint_acc = 0.0;
   TriMesh_d *tm = nullptr;                  // rigid triangle mesh (contact)
+  double temp = 0.0;                        // uniform temperature T[]
   std::vector<double3> v_orig;              // its velocity before the ramp
 
   // A TriMesh_d filled from arrays, one mesh (id 0), uniform velocity; normals,
@@ -150,6 +151,7 @@ class RefDomain : public Domain_d {
     CalcNodalMassFromVol();
     for (int n = 0; n < m_node_count; n++)
       for (int d = 0; d < m_dim; d++) ut_prev[m_dim * n + d] = 0.0;
+    for (int n = 0; n < m_node_count; n++) T[n] = temp;
     if (tm) {
       // what main.C does before the solve (main.C:647-650, :862-873)
       setTriMesh(tm);
@@ -477,6 +479,19 @@ void wfr_set_materials(void *h, int nmat, const double *E, const double *nu,
   }
   d->setDensity(rho[0]);
   d->AssignMaterial(&d->mats[0]);
+}
+
+// Material_::Init_JohnsonCook (Material.cuh:105-114) on material `mat`; the
+// reference's CalcStressStrain reads the temperature T[e], set uniform here.
+void wfr_set_johnson_cook(void *h, int mat, double B, double n, double C, double eps0, double m,
+                          double Tm, double Tt, double T) {
+  RefDomain *d = static_cast<RefDomain *>(h);
+  Material_ &M = d->mats[mat];
+  Elastic_ el = M.Elastic();
+  M.Init_JohnsonCook(el, M.sy0, B, n, C, eps0, m, Tm, Tt);
+  d->temp = T;
+  // AssignMaterial copies material 0 into the domain (Domain_d.C:903-907)
+  if (mat == 0) d->AssignMaterial(&d->mats[0]);
 }
 
 void wfr_set_elem_materials(void *h, const int *ids) {

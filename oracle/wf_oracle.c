@@ -20,6 +20,9 @@ typedef struct {
   double E, nu, rho, sy0, H, hol_K, hol_m;
   double K, G, cs0;          /* Elastic_ (Material.cuh:24-27) */
   double eps0, eps1;         /* Hollomon (Material.cuh:90-104) */
+  /* Johnson-Cook (Material_::Init_JohnsonCook, Material.cuh:105-114) and the
+   * element temperature it reads (uniform here) */
+  double jc_B, jc_n, jc_C, jc_eps0, jc_m, jc_Tm, jc_Tt, jc_T;
 } mat_t;
 
 struct wfo_domain {
@@ -312,6 +315,21 @@ int wfo_set_materials(wfo_domain *d, int nmat, const wfo_material *m) {
   }
   /* Domain_d::setDensity (Domain_d.C:952): rho_0 of every element. */
   for (int64_t e = 0; e < d->ne; e++) d->rho0[e] = d->mats[0].rho;
+  return 0;
+}
+
+int wfo_set_johnson_cook(wfo_domain *d, int mat, double B, double n, double C, double eps0,
+                         double m, double Tm, double Tt, double T) {
+  if (mat < 0 || mat >= d->nmat) return -1;
+  mat_t *t = &d->mats[mat];
+  t->jc_B = B;
+  t->jc_n = n;
+  t->jc_C = C;
+  t->jc_eps0 = eps0;
+  t->jc_m = m;
+  t->jc_Tm = Tm;
+  t->jc_Tt = Tt;
+  t->jc_T = T;
   return 0;
 }
 
@@ -754,6 +772,27 @@ static void t3_scaled_identity(double s, double *r) {
 }
 
 /* CalcHollomonYieldStress / CalcHollomonTangentModulus (Material.cuh:353-395). */
+/* CalcJohnsonCookYieldStress (Material.cuh:377-392). */
+static double jc_sy(double strain, double strain_rate, const mat_t *m) {
+  double T_h = (m->jc_T - m->jc_Tt) / (m->jc_Tm - m->jc_Tt);
+  double sr = strain_rate;
+  if (strain_rate == 0.0) sr = 1.e-5;
+  return (m->sy0 + m->jc_B * pow(strain, m->jc_n)) * (1.0 + m->jc_C * log(sr / m->jc_eps0)) *
+         (1.0 - pow(T_h, m->jc_m));
+}
+
+/* CalcJohnsonCookTangentModulus (Material.cuh:397-410). */
+static double jc_et(double plstrain, double strain_rate, const mat_t *m) {
+  double T_h = (m->jc_T - m->jc_Tt) / (m->jc_Tm - m->jc_Tt);
+  double Et = 0.;
+  if (plstrain > 0.)
+    Et = m->jc_n * m->jc_B * pow(plstrain, m->jc_n - 1.) *
+         (1.0 + m->jc_C * log(strain_rate / m->jc_eps0)) * (1.0 - pow(T_h, m->jc_m));
+  else
+    Et = m->E * 0.1;
+  return Et;
+}
+
 static double hollomon_sy(double strain, const mat_t *m) {
   if (strain + m->eps0 > m->eps1) return m->hol_K * pow(strain + m->eps0, m->hol_m);
   return m->sy0;
@@ -800,14 +839,25 @@ static void calc_stress_strain(wfo_domain *d) {
                        S[YY] * S[YY] + 2.0 * S[YZ] * S[YZ] + S[ZZ] * S[ZZ]);
     double sig_trial = sqrt(3.0 * J2);
     double H;
-    if (m->model == 1) {
+    /* effective strain rate (Mechanical.C:1701-1705) */
+    double eff = sqrt(0.5 * ((SR[XX] - SR[YY]) * (SR[XX] - SR[YY]) +
+                             (SR[YY] - SR[ZZ]) * (SR[YY] - SR[ZZ]) +
+                             (SR[ZZ] - SR[XX]) * (SR[ZZ] - SR[XX])) +
+                      3.0 * (SR[XY] * SR[XY] + SR[YZ] * SR[YZ] + SR[XZ] * SR[XZ]));
+    if (m->model == 2) {
+      d->sigma_y[e] = jc_sy(d->pl_strain[e], eff, m);
+    } else if (m->model == 1) {
       d->sigma_y[e] = hollomon_sy(d->pl_strain[e], m);
     } else {
       d->sigma_y[e] = m->sy0 + m->H * d->pl_strain[e];
     }
+    eff = (1.0e6 < eff) ? 1.0e6 : eff;  /* min(eff, m_max_edot) */
     double dep = 0.0;
     if (d->sigma_y[e] < sig_trial) {
-      H = (m->model == 1) ? hollomon_et(d->pl_strain[e], m) : m->H;
+      if (m->model == 2)
+        H = jc_et(d->pl_strain[e], eff, m);
+      else
+        H = (m->model == 1) ? hollomon_et(d->pl_strain[e], m) : m->H;
       double G = m->G;
       double dgamma = (sig_trial - d->sigma_y[e]) / (3.0 * G + H);
       double factor = 1.0 - (3.0 * G * dgamma) / sig_trial;

@@ -23,7 +23,7 @@ typedef struct wfo_domain wfo_domain;
 
 /* Material_ / Elastic_ (include/common/Material.cuh:15-156). */
 typedef struct {
-  int model;      /* 0 = bilinear (linear isotropic hardening), 1 = Hollomon */
+  int model;      /* 0 = bilinear (linear isotropic hardening), 1 = Hollomon, 2 = Johnson-Cook */
   double E, nu, rho;
   double sy0;     /* initial yield stress */
   double H;       /* hardening modulus d(sigma_y)/d(eps_p), model 0 */
@@ -47,6 +47,9 @@ void wfo_get_connectivity(const wfo_domain *d, int32_t *elnod, int32_t *nodel,
 
 int wfo_set_materials(wfo_domain *d, int nmat, const wfo_material *m);
 int wfo_set_elem_materials(wfo_domain *d, const int32_t *ids);
+/* Johnson-Cook constants of material `mat` (model 2) and its temperature. */
+int wfo_set_johnson_cook(wfo_domain *d, int mat, double B, double n, double C, double eps0,
+                         double m, double Tm, double Tt, double T);
 int wfo_add_bc_vel_node(wfo_domain *d, int64_t node, int dim, double val);
 int wfo_allocate_bcs(wfo_domain *d);
 int wfo_set_reaction_nodes(wfo_domain *d, int64_t n, const int32_t *nodes, int dim);

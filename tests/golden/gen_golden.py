@@ -29,6 +29,8 @@ from weldformfem_gb300 import workloads as W  # noqa: E402
 
 HOLLOMON = dict(model=1, E=200e9, nu=0.3, rho=7850.0, sy0=300e6, hol_K=600e6, hol_m=0.2)
 STAB = [0.3, 0.7, 0.2, 0.08, 0.15, 0.15, 0.8, 0.2, 0.05, 0.0]
+# Johnson-Cook B, n, C, eps0_dot, m, T_melt, T_transition, T
+JC = [400e6, 0.35, 0.02, 1.0, 1.0, 1500.0, 20.0, 300.0]
 # a 2x2-cell plane of triangles just below the top face of the 3x3x4-cell
 # tetrahedral block (top at z = 2 mm), normal -z, moving down at 5 m/s
 DIE = dict(start=[-0.001, -0.001, 0.002 - 1e-5], end=[0.004, 0.004, 0.0], dens=2, flip=True,
@@ -78,6 +80,15 @@ def cases():
     c.perturb = 0.1
     c.bc = "bottom_z"
     out.append(("tet_die_trimesh", c, 300, "step", dict(linear=True, die=DIE)))
+    # Johnson-Cook through Material_::Init_JohnsonCook and the reference's own
+    # CalcStressStrain (hexahedra: the reference reads the temperature T[e] of a
+    # node-sized array by element index)
+    c = W.config(0, scale=(3, 3, 4))
+    c.perturb = 0.1
+    c.seed = W.SEED_BASE + 9
+    c.top_vz = -5.0
+    c.materials = [dict(model=2, E=200e9, nu=0.3, rho=7850.0, sy0=250e6)]
+    out.append(("hex_johnson_cook", c, 400, "step", dict(jc=JC)))
     return out
 
 
@@ -90,6 +101,8 @@ def run_case(name, case, steps, mode, extra):
         d.set_stab(np.array(extra["stab"], float))
     if "av" in extra:
         d.set_artif_visc(*extra["av"])
+    if "jc" in extra:
+        d.set_johnson_cook(0, *extra["jc"])
     if "die" in extra:
         die = extra["die"]
         xyz, tri = W.axis_plane_mesh(die["start"], die["end"], die["dens"], die["flip"])

@@ -40,6 +40,8 @@ def setup(dom, case, extra=None):
         dom.set_stab(np.array(extra["stab"], float))
     if "av" in extra:
         dom.set_artif_visc(*extra["av"])
+    if "jc" in extra:
+        dom.set_johnson_cook(0, *extra["jc"])
     if "die" in extra:
         die = extra["die"]
         xyz, tri = W.axis_plane_mesh(die["start"], die["end"], die["dens"], die["flip"])

@@ -161,7 +161,7 @@ def test_deck_errors(tmp_path):
         (dict(Configuration={"domType": "AxiSymm"}), 5),
         (dict(RigidBodies=[{"type": "File", "fileName": "die.nas"}]), 5),
         (dict(RigidBodies=[{"type": "Plane"}, {"type": "Plane"}]), 5),
-        (dict(Materials=[dict(STEEL, type="JohnsonCook")]), 5),
+        (dict(Materials=[dict(STEEL, type="GMT")]), 5),
         (dict(DomainBlocks=[{"type": "File", "fileName": "missing.k"}]), 1),
         (dict(BoundaryConditions=[{"zoneId": 3, "value": [0, 0, 1.0]}]), 1),
     ]

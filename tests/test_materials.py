@@ -1,0 +1,100 @@
+"""Material laws beyond linear hardening on the GPU: Johnson-Cook.
+
+The oracle's Johnson-Cook restatement is pinned bit-for-bit to the
+reference's own CalcStressStrain (Material_::Init_JohnsonCook) by the
+hex_johnson_cook fixture in tests/test_oracle.py. Here the GPU paths are
+checked against the oracle on the same inputs: FP64 within 1e-9 relative
+(log and pow of the device and the host libm can differ by an ulp), mixed
+precision within the mixed-path bounds.
+"""
+import numpy as np
+import pytest
+
+import weldformfem_gb300 as wf
+from oracle import orabind as O
+from tests import helpers as H
+from weldformfem_gb300 import workloads as W
+
+JC_MAT = dict(model=2, E=200e9, nu=0.3, rho=7850.0, sy0=250e6)
+JC = [400e6, 0.35, 0.02, 1.0, 1.0, 1500.0, 20.0, 300.0]
+
+
+def cases():
+    h = W.config(0, scale=(3, 3, 4))
+    h.perturb = 0.1
+    h.seed = W.SEED_BASE + 9
+    h.top_vz = -5.0
+    h.materials = [dict(JC_MAT)]
+    t = W.config(1, scale=(3, 3, 4))
+    t.top_vz = -3.0
+    t.materials = [dict(JC_MAT)]
+    return {"hex": (h, 400), "tet": (t, 300)}
+
+
+def oracle(case, steps):
+    o = O.OracleDomain()
+    H.setup(o, case, {"jc": JC})
+    o.init()
+    o.step(steps)
+    return o
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["hex", "tet"])
+def test_johnson_cook_fp64_matches_oracle(name):
+    case, steps = cases()[name]
+    o = oracle(case, steps)
+    assert o.elem_scalar("pl_strain").max() > 0.005   # the runs are well into yield
+    d = wf.Domain(wf.WF_FP64)
+    H.setup(d, case, {"jc": JC})
+    d.init()
+    d.run(steps)
+    for kind, f in [("node_vec", "u"), ("elem_scalar", "pl_strain"), ("elem_scalar", "sigma_y"),
+                    ("elem_tensor", "sigma")]:
+        assert H.rel_err(getattr(d, kind)(f), getattr(o, kind)(f)) <= 1e-9, f
+    assert H.rel_err(d.reaction(), o.reaction()) <= 1e-9
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["hex", "tet"])
+def test_johnson_cook_mixed(name):
+    case, steps = cases()[name]
+    o = oracle(case, steps)
+    d = wf.Domain(wf.WF_MIXED)
+    H.setup(d, case, {"jc": JC})
+    d.init()
+    d.run(steps)
+    assert H.rel_err(d.node_vec("u"), o.node_vec("u")) <= 1e-4
+    assert H.rel_err(d.elem_scalar("pl_strain"), o.elem_scalar("pl_strain")) <= 1e-2
+    assert H.rel_err(d.reaction(), o.reaction()) <= 1e-3
+
+
+@pytest.mark.gpu
+def test_johnson_cook_needs_its_constants():
+    case, _ = cases()["hex"]
+    d = wf.Domain(wf.WF_FP64)
+    W.apply(d, case)
+    with pytest.raises(wf.WfError) as e:
+        d.init()
+    assert e.value.status == 2
+    d2 = wf.Domain(wf.WF_FP64)
+    c2 = W.config(0, scale=(2, 2, 2))
+    W.apply(d2, c2)
+    with pytest.raises(wf.WfError) as e:
+        d2.set_johnson_cook(0, *JC)
+    assert e.value.status == 2
+
+
+def test_johnson_cook_deck(tmp_path):
+    import json
+    deck = {"Configuration": {"simTime": 1e-6, "cflFactor": 0.3},
+            "Materials": [{"type": "JohnsonCook", "const": [400e6, 0.35, 0.02, 1.0],
+                           "density0": 7850.0, "youngsModulus": 200e9, "poissonsRatio": 0.3,
+                           "yieldStress0": 250e6}],
+            "DomainBlocks": [{"type": "Box", "dim": [0.002, 0.002, 0.002],
+                              "elemLength": 0.001}]}
+    p = tmp_path / "jc.json"
+    p.write_text(json.dumps(deck))
+    k = wf.Deck(str(p))
+    assert k.info["material"]["model"] == 2 and k.info["material"]["sy0"] == 250e6
+    assert k.info["johnson_cook"] == [400e6, 0.35, 0.02, 1.0, 1.0, 1.0e10, 0.0, 0.0]

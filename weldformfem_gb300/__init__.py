@@ -57,7 +57,8 @@ class WfDeckInfo(C.Structure):
                 ("hourglass", C.c_double), ("artif_visc", C.c_double * 2), ("stab", WfStab),
                 ("material", WfMaterial), ("contact", C.c_int32), ("die_nodes", C.c_int32),
                 ("die_tris", C.c_int32), ("die_vel", C.c_double * 3), ("mu_static", C.c_double),
-                ("mu_dynamic", C.c_double), ("penalty_factor", C.c_double)]
+                ("mu_dynamic", C.c_double), ("penalty_factor", C.c_double),
+                ("johnson_cook", C.c_double * 8)]
 
 
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
@@ -135,6 +136,7 @@ _SIGS = {
                                C.c_double, C.c_double],
     "wf_get_trimesh_nodes": [C.c_void_p, _dp, C.c_int64, C.POINTER(C.c_int64)],
     "wf_set_energy_history": [C.c_void_p, C.c_int32],
+    "wf_set_johnson_cook": [C.c_void_p, C.c_int32] + [C.c_double] * 8,
     "wf_get_energy_history": [C.c_void_p, _dp, _dp, C.c_int64, C.POINTER(C.c_int64)],
     "wf_adjoint_backward": [C.c_void_p, _dp, C.c_int32, _dp],
     # allocation-free nodal volumes: device pointers in, device pointer out
@@ -262,6 +264,11 @@ class Domain:
         self._nmat = len(mats)
         if elem_ids is not None:
             self._call("wf_set_elem_materials", np.ascontiguousarray(elem_ids, np.int32))
+
+    def set_johnson_cook(self, mat, B, n, C, eps0, m, Tm, Tt, T=0.0):
+        """Material_::Init_JohnsonCook constants of material `mat` (model 2)."""
+        self._call("wf_set_johnson_cook", int(mat), float(B), float(n), float(C), float(eps0),
+                   float(m), float(Tm), float(Tt), float(T))
 
     def set_hourglass(self, coef):
         self._call("wf_set_hourglass", float(coef))
@@ -488,7 +495,8 @@ class Deck:
     @staticmethod
     def _info_dict(info):
         out = {f: getattr(info, f) for f, _ in WfDeckInfo._fields_
-               if f not in ("artif_visc", "stab", "material", "die_vel")}
+               if f not in ("artif_visc", "stab", "material", "die_vel", "johnson_cook")}
+        out["johnson_cook"] = [info.johnson_cook[k] for k in range(8)]
         out["artif_visc"] = (info.artif_visc[0], info.artif_visc[1])
         out["die_vel"] = tuple(info.die_vel[k] for k in range(3))
         out["stab"] = [getattr(info.stab, f) for f, _ in WfStab._fields_]
@@ -538,6 +546,8 @@ class Deck:
         i = self.info
         dom.set_mesh(x, el)
         dom.set_materials([i["material"]])
+        if i["material"]["model"] == 2:
+            dom.set_johnson_cook(0, *i["johnson_cook"])
         dom.add_bcs(self.bcs())
         if i["has_stab"]:
             dom.set_stab(np.array(i["stab"]))

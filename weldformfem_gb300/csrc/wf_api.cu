@@ -100,6 +100,7 @@ struct wf_domain {
   std::vector<int32_t> nodel, nodel_loc, nodel_off, nodel_cnt;
   // materials
   std::vector<wf_material> mats;
+  std::vector<std::array<double, 8>> jc;  // Johnson-Cook B, n, C, eps0_dot, m, T_melt, T_t, T
   std::vector<int32_t> emat;
   double rho_all = 0.0;
   bool rho_set = false;
@@ -547,14 +548,31 @@ WF_API wf_status wf_set_materials(wf_domain *d, int32_t nmat, const wf_material 
     const wf_material &m = mats[i];
     if (!(m.E > 0) || !(m.rho > 0) || !(m.nu > -1.0 && m.nu < 0.5))
       return fail(d, WF_ERR_ARG, "material %d: need E > 0, rho > 0, -1 < nu < 0.5", i);
-    if (m.model != WF_MAT_BILINEAR && m.model != WF_MAT_HOLLOMON)
+    if (m.model != WF_MAT_BILINEAR && m.model != WF_MAT_HOLLOMON &&
+        m.model != WF_MAT_JOHNSON_COOK)
       return fail(d, WF_ERR_UNSUPPORTED, "material %d: model %d", i, m.model);
     if (m.model == WF_MAT_HOLLOMON && !(m.hol_K > 0 && m.hol_m > 0))
       return fail(d, WF_ERR_ARG, "material %d: Hollomon needs K > 0, m > 0", i);
   }
   d->mats.assign(mats, mats + nmat);
+  d->jc.assign(nmat, std::array<double, 8>{0, 0, 0, 0, 0, 0, 0, 0});
   d->rho_all = mats[0].rho;
   d->rho_set = true;
+  return WF_OK;
+}
+
+WF_API wf_status wf_set_johnson_cook(wf_domain *d, int32_t mat, double B, double n, double C,
+                                     double eps0_dot, double m, double T_melt,
+                                     double T_transition, double T) {
+  if (!d) return WF_ERR_ARG;
+  if (d->initialized) return fail(d, WF_ERR_STATE, "materials are set before init");
+  if (mat < 0 || mat >= (int32_t)d->mats.size())
+    return fail(d, WF_ERR_ARG, "material %d out of range", mat);
+  if (d->mats[mat].model != WF_MAT_JOHNSON_COOK)
+    return fail(d, WF_ERR_STATE, "material %d is not of model WF_MAT_JOHNSON_COOK", mat);
+  if (!(eps0_dot > 0) || !(T_melt != T_transition))
+    return fail(d, WF_ERR_ARG, "Johnson-Cook needs eps0_dot > 0 and T_melt != T_transition");
+  d->jc[mat] = {B, n, C, eps0_dot, m, T_melt, T_transition, T};
   return WF_OK;
 }
 
@@ -1086,6 +1104,16 @@ WF_API wf_status wf_init(wf_domain *d) {
       t.eps0 = m.sy0 / m.E;
       t.eps1 = std::pow(m.sy0 / m.hol_K, 1. / m.hol_m);
     }
+    if (m.model == WF_MAT_JOHNSON_COOK) {
+      const std::array<double, 8> &j = d->jc[i];
+      if (!(j[3] > 0)) return fail(d, WF_ERR_STATE, "material %zu: wf_set_johnson_cook not called", i);
+      t.jc_B = j[0];
+      t.jc_n = j[1];
+      t.jc_C = j[2];
+      t.jc_eps0 = j[3];
+      const double T_h = (j[7] - j[6]) / (j[5] - j[6]);
+      t.jc_Th = 1.0 - std::pow(T_h, j[4]);
+    }
   }
   MatDev *mdev = nullptr;
   CUDA_TRY(upload(d, &mdev, md));
@@ -1235,6 +1263,12 @@ WF_API wf_status wf_init(wf_domain *d) {
       mf[i].hol_m = (float)md[i].hol_m;
       mf[i].eps0 = (float)md[i].eps0;
       mf[i].eps1 = (float)md[i].eps1;
+      mf[i].jc_B = (float)md[i].jc_B;
+      mf[i].jc_n = (float)md[i].jc_n;
+      mf[i].jc_C = (float)md[i].jc_C;
+      mf[i].jc_eps0 = (float)md[i].jc_eps0;
+      mf[i].jc_Th = (float)md[i].jc_Th;
+      mf[i].E = (float)md[i].E;
       mf[i].model = md[i].model;
     }
     MatF *mfd = nullptr;

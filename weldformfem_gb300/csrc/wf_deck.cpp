@@ -584,6 +584,11 @@ WF_API wf_status wf_deck_read(const char *path, wf_deck **out, char *err, int64_
     M.model = WF_MAT_HOLLOMON;
     M.hol_K = c[0];
     M.hol_m = c[1];
+  } else if (mtype == "JohnsonCook") {
+    // JohnsonCook(el, Fy, c[0], c[1], c[2], c[3], 1.0, 1.0e10, 0.0) (main.C:527)
+    M.model = WF_MAT_JOHNSON_COOK;
+    const double jc[8] = {c[0], c[1], c[2], c[3], 1.0, 1.0e10, 0.0, 0.0};
+    for (int q = 0; q < 8; q++) I.johnson_cook[q] = jc[q];
   } else {
     return bad("material type " + mtype + " is not supported", WF_ERR_UNSUPPORTED);
   }
@@ -785,6 +790,10 @@ WF_API wf_status wf_deck_apply(const wf_deck *k, wf_domain *d) {
   if ((s = (call)) != WF_OK) return s
   WF_DECK_TRY(wf_set_mesh(d, I.nn, I.ne, I.npe, k->x.data(), k->elnod.data()));
   WF_DECK_TRY(wf_set_materials(d, 1, &I.material));
+  if (I.material.model == WF_MAT_JOHNSON_COOK) {
+    const double *j = I.johnson_cook;
+    WF_DECK_TRY(wf_set_johnson_cook(d, 0, j[0], j[1], j[2], j[3], j[4], j[5], j[6], j[7]));
+  }
   WF_DECK_TRY(wf_set_density(d, I.material.rho));
   if (I.n_bc)
     WF_DECK_TRY(wf_add_bc_vel_nodes(d, I.n_bc, k->bc_node.data(), k->bc_dim.data(),

@@ -334,12 +334,31 @@ __global__ void __launch_bounds__(kElemThreads) k_fp64_elements(StepParams P, Fp
   const double sig_trial = sqrt(3.0 * J2);
   double pls = S.pls[e];
   double sy;
-  if (m.model == WF_MAT_HOLLOMON)
+  double eff = 0.0;
+  if (m.model == WF_MAT_JOHNSON_COOK) {
+    // effective strain rate (Mechanical.C:1701-1705) and the Johnson-Cook yield
+    // stress (CalcJohnsonCookYieldStress, Material.cuh:377-392)
+    eff = sqrt(0.5 * ((s00 - s11) * (s00 - s11) + (s11 - s22) * (s11 - s22) +
+                      (s22 - s00) * (s22 - s00)) +
+               3.0 * (s01 * s01 + s12 * s12 + s02 * s02));
+    const double sr = (eff == 0.0) ? 1.e-5 : eff;
+    sy = (m.sy0 + m.jc_B * pow(pls, m.jc_n)) * (1.0 + m.jc_C * log(sr / m.jc_eps0)) * m.jc_Th;
+  } else if (m.model == WF_MAT_HOLLOMON) {
     sy = hollomon_sy(pls, m);
-  else
+  } else {
     sy = m.sy0 + m.H * pls;
+  }
   if (sy < sig_trial) {
-    const double H = (m.model == WF_MAT_HOLLOMON) ? hollomon_et(pls, m) : m.H;
+    double H;
+    if (m.model == WF_MAT_JOHNSON_COOK) {
+      // CalcJohnsonCookTangentModulus (Material.cuh:397-410) at min(edot, 1e6)
+      const double er = (1.0e6 < eff) ? 1.0e6 : eff;
+      H = (pls > 0.) ? m.jc_n * m.jc_B * pow(pls, m.jc_n - 1.) *
+                           (1.0 + m.jc_C * log(er / m.jc_eps0)) * m.jc_Th
+                     : m.E * 0.1;
+    } else {
+      H = (m.model == WF_MAT_HOLLOMON) ? hollomon_et(pls, m) : m.H;
+    }
     const double G = m.G;
     const double dgamma = (sig_trial - sy) / (3.0 * G + H);
     const double factor = 1.0 - (3.0 * G * dgamma) / sig_trial;

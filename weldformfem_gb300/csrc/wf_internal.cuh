@@ -14,6 +14,7 @@ namespace wf {
 // Per-material constants on the device (Elastic_ / Material_, Material.cuh).
 struct MatDev {
   double K, G, sy0, H, cs0, hol_K, hol_m, eps0, eps1, E;
+  double jc_B, jc_n, jc_C, jc_eps0, jc_Th;  // Johnson-Cook; jc_Th = 1 - T_h^m (host-computed)
   int32_t model;
   int32_t pad;
 };
@@ -21,6 +22,7 @@ struct MatDev {
 // FP32 material constants of the mixed kernels.
 struct MatF {
   float K, G, sy0, H, cs0, rho, hol_K, hol_m, eps0, eps1;
+  float jc_B, jc_n, jc_C, jc_eps0, jc_Th, E;
   int32_t model;
   int32_t pad;
 };

@@ -255,16 +255,33 @@ __device__ __forceinline__ void stress_update(const StepParams &P, const MixStat
   const float sig_trial = sqrtf(3.0f * J2);
   float pls = M.pls[e];
   float sy;
-  if (m.model == WF_MAT_HOLLOMON)
+  float eff = 0.f;
+  if (m.model == WF_MAT_JOHNSON_COOK) {
+    eff = sqrtf(0.5f * ((sr[0] - sr[1]) * (sr[0] - sr[1]) + (sr[1] - sr[2]) * (sr[1] - sr[2]) +
+                        (sr[2] - sr[0]) * (sr[2] - sr[0])) +
+                3.0f * (sr[3] * sr[3] + sr[4] * sr[4] + sr[5] * sr[5]));
+    const float srate = (eff == 0.f) ? 1.e-5f : eff;
+    sy = (m.sy0 + m.jc_B * powf(pls, m.jc_n)) * (1.0f + m.jc_C * logf(srate / m.jc_eps0)) *
+         m.jc_Th;
+  } else if (m.model == WF_MAT_HOLLOMON) {
     sy = (pls + m.eps0 > m.eps1) ? m.hol_K * powf(pls + m.eps0, m.hol_m) : m.sy0;
-  else
+  } else {
     sy = m.sy0 + m.H * pls;
+  }
   if (sy < sig_trial) {
-    const float H = (m.model == WF_MAT_HOLLOMON)
-                        ? ((pls + m.eps0 > m.eps1)
-                               ? m.hol_K * m.hol_m * powf(pls + m.eps0, m.hol_m - 1.0f)
-                               : 0.f)
-                        : m.H;
+    float H;
+    if (m.model == WF_MAT_JOHNSON_COOK) {
+      const float er = (1.0e6f < eff) ? 1.0e6f : eff;
+      H = (pls > 0.f) ? m.jc_n * m.jc_B * powf(pls, m.jc_n - 1.f) *
+                            (1.0f + m.jc_C * logf(er / m.jc_eps0)) * m.jc_Th
+                      : m.E * 0.1f;
+    } else {
+      H = (m.model == WF_MAT_HOLLOMON)
+              ? ((pls + m.eps0 > m.eps1)
+                     ? m.hol_K * m.hol_m * powf(pls + m.eps0, m.hol_m - 1.0f)
+                     : 0.f)
+              : m.H;
+    }
     const float dgamma = (sig_trial - sy) / (3.0f * m.G + H);
     const float factor = 1.0f - (3.0f * m.G * dgamma) / sig_trial;
     t0 = d0s * factor; t1 = d1s * factor; t2 = d2s * factor;
@@ -701,9 +718,11 @@ __global__ void k_mix_export_elems(StepParams P, MixState M, Fp64State S, const 
   S.vol[e] = vol[e];
   const float pls = M.pls[e];
   S.pls[e] = pls;
+  // exported yield stress; for Johnson-Cook its rate-independent part
   S.sy[e] = (m.model == WF_MAT_HOLLOMON)
                 ? ((pls + m.eps0 > m.eps1) ? m.hol_K * powf(pls + m.eps0, m.hol_m) : m.sy0)
-                : m.sy0 + m.H * pls;
+                : (m.model == WF_MAT_JOHNSON_COOK) ? (m.sy0 + m.jc_B * powf(pls, m.jc_n)) * m.jc_Th
+                                                   : m.sy0 + m.H * pls;
   for (int c = 0; c < 6; c++) {
     const double t = M.tau[c * ne + e];
     S.tau[c * ne + e] = t;
