@@ -38,7 +38,7 @@ class Elastic_ {
   double E_m, nu_m;
 };
 
-enum { BILINEAR = 0, HOLLOMON = 1 };
+enum { BILINEAR = 0, HOLLOMON = 1, JOHNSON_COOK = 2 };
 
 // Material_ (Material.cuh:36-156): the fields the explicit step reads.
 class Material_ {
@@ -53,8 +53,25 @@ class Material_ {
     K = k_;
     m = m_;
   }
+  // Material_::Init_JohnsonCook (Material.cuh:105-114); T is the (uniform)
+  // element temperature the yield function reads (thermal coupling not built)
+  void Init_JohnsonCook(const Elastic_ &el, double a, double b, double n_, double c,
+                        double eps_0_, double m_, double T_m_, double T_t_, double T_ = 0.0) {
+    elastic_m = el;
+    Material_model = JOHNSON_COOK;
+    sy0 = a;
+    B = b;
+    n = n_;
+    C = c;
+    eps_0 = eps_0_;
+    m = m_;
+    T_m = T_m_;
+    T_t = T_t_;
+    T = T_;
+  }
   int Material_model = BILINEAR;
   double sy0 = 1.0e10;  // as the reference constructor
+  double B = 0.0, n = 1.0, C = 0.0, eps_0 = 1.0, T_m = 1.0e10, T_t = 0.0, T = 0.0;
   double Ep = 0.0;      // hardening modulus of the bilinear law
   double K = 1.0, m = 1.0;
   double cs0 = 0.0;     // informational; the library uses sqrt(K_bulk / rho)
@@ -104,6 +121,12 @@ class Domain_d {
                          m.sy0, m.Ep, m.K, m.m};
     }
     check(wf_set_materials(d_, (int32_t)t.size(), t.data()), "AssignMaterial");
+    for (size_t i = 0; i < ms.size(); i++) {
+      const Material_ &m = *ms[i];
+      if (m.Material_model == JOHNSON_COOK)
+        check(wf_set_johnson_cook(d_, (int32_t)i, m.B, m.n, m.C, m.eps_0, m.m, m.T_m, m.T_t, m.T),
+              "Init_JohnsonCook");
+    }
   }
   void setElemMaterials(const std::vector<int32_t> &ids) {
     check(wf_set_elem_materials(d_, ids.data()), "setElemMaterials");
@@ -132,6 +155,34 @@ class Domain_d {
                        const std::vector<int32_t> &cand) {
     check(wf_set_contact_plane(d_, z0, vz, kpen, mu, (int64_t)cand.size(), cand.data()),
           "setContactPlane");
+  }
+  // setTriMesh + setContactOn + setContactPF (Domain_d.h:464, :642, :771) for
+  // one rigid triangle mesh with a uniform velocity
+  void setTriMesh(const std::vector<double> &xyz, const std::vector<int32_t> &tri,
+                  const vector_t &vel, double mu_static = 0.0, double mu_dynamic = 0.0,
+                  double penalty_factor = 0.1) {
+    const double v[3] = {vel.x, vel.y, vel.z};
+    check(wf_set_contact_trimesh(d_, (int64_t)xyz.size() / 3, xyz.data(),
+                                 (int64_t)tri.size() / 3, tri.data(), v, mu_static, mu_dynamic,
+                                 penalty_factor),
+          "setTriMesh");
+  }
+  // CreateFromLSDyna (Domain_d.C:1647-1699) from a keyword file
+  void CreateFromLSDyna(const std::string &path) {
+    check(wf_load_lsdyna(d_, path.c_str()), "CreateFromLSDyna");
+  }
+  // The JSON driver's setup (src/explicit/main.C:125-1005): mesh, material,
+  // BCs, options, dt and end time from a deck
+  wf_deck_info LoadDeck(const std::string &path) {
+    wf_deck_info info{};
+    char err[512] = {0};
+    const wf_status s = wf_load_deck(d_, path.c_str(), &info, err, sizeof(err));
+    if (s != WF_OK) throw std::runtime_error(path + ": " + err);
+    return info;
+  }
+  void setEnergyHistory(bool on) { check(wf_set_energy_history(d_, on ? 1 : 0), "energies"); }
+  void WriteVTK(const std::string &path) {
+    check(wf_write_vtk(d_, path.c_str()), "VTKWriter");
   }
   void setReactionNodes(const std::vector<int32_t> &nodes, int dim = 2) {
     check(wf_set_reaction_nodes(d_, (int64_t)nodes.size(), nodes.data(), dim), "reaction");
