@@ -299,6 +299,7 @@ def run_ours(args):
                                 "displacement + reaction readback"},
             "gpu_launches": int(launches),
             "autotuned_launch": tuned,
+            "launch_note": "items_per_thread 0 = persistent grid (SMs x resident blocks)",
             "roofline": roof,
             "cpu_baseline": cpu,
             "clocks": clk,
@@ -343,6 +344,8 @@ def run_ensemble(args):
     d.run(max(10, min(K, 50)))
     ph, nph = d.phase_times()
     d.set_phase_timing(False)
+    tuned = {p: dict(zip(("block", "items_per_thread"), d.launch_config(i)[:2]))
+             for i, p in enumerate(PHASES[:3])}
     del d
     # looping the solver: one domain per specimen, same steps, same precision
     loop_ms = 0.0
@@ -374,6 +377,8 @@ def run_ensemble(args):
                    "how": "one domain per specimen, 32 graph-launched steps each, summed"},
         "batched_over_looped": round(value / loop_value, 2),
         "gpu_launches": int(launches),
+        "autotuned_launch": tuned,
+        "launch_note": "items_per_thread 0 = persistent grid (SMs x resident blocks)",
         "phases_ms": {p: round(float(m) / max(nph, 1), 4) for p, m in zip(PHASES, ph)},
         "clocks": clk,
     }

@@ -242,13 +242,19 @@ WF_API wf_status wf_get_phase_times(wf_domain *d, double ms[4], int64_t *steps, 
 /* Launch-shape autotuning of the mixed-precision geometry, nodal and element
  * kernels (on by default): at wf_init the library times each kernel on the
  * domain's own data for block sizes {64, 128, 256} x {1, 2, 4} items per
- * thread (grid-stride) and keeps the fastest; the kernels' results do not
+ * thread or a persistent grid of (SMs x resident blocks) (items_per_thread
+ * reported as 0), all grid-stride, and keeps the fastest; the kernels' results do not
  * depend on the shape, and the state the element kernel advances is restored
  * after the trials. wf_get_launch_config reports the choice for phase 0
  * (geometry), 1 (nodal) or 2 (element). */
 WF_API wf_status wf_set_autotune(wf_domain *d, int32_t on);
 WF_API wf_status wf_get_launch_config(const wf_domain *d, int32_t phase, int32_t *block,
                                       int32_t *items_per_thread, double *ms);
+/* Sets a launch shape by hand (block 64, 128 or 256; items_per_thread >= 1, or
+ * 0 for a persistent grid); with autotuning off before wf_init, or any time
+ * after it (the choice replaces the tuned one). */
+WF_API wf_status wf_set_launch_config(wf_domain *d, int32_t phase, int32_t block,
+                                      int32_t items_per_thread);
 /* Number of kernels this domain has launched since wf_init (graph nodes
  * included). */
 WF_API wf_status wf_get_launch_count(const wf_domain *d, int64_t *n);

@@ -111,6 +111,17 @@ def test_autotuned_and_default_launch_shapes_agree_bitwise():
         if tune:
             for phase in range(3):
                 bs, ept, ms = d.launch_config(phase)
-                assert bs in (64, 128, 256) and ept in (1, 2, 4) and ms > 0.0
-    for a, b in zip(outs[0], outs[1]):
-        np.testing.assert_array_equal(a, b)
+                assert bs in (64, 128, 256) and ept in (0, 1, 2, 4) and ms > 0.0
+    # every shape by hand, persistent grids (items per thread 0) included
+    for bs, ept in ((64, 0), (256, 0), (128, 4)):
+        d = wf.Domain(wf.WF_MIXED)
+        W.apply(d, case)
+        d.set_autotune(False)
+        d.init()
+        for phase in range(3):
+            d.set_launch_config(phase, bs, ept)
+        d.run(64)
+        outs.append((d.node_vec("x"), d.reaction(), d.elem_scalar("pl_strain")))
+    for o in outs[1:]:
+        for a, b in zip(outs[0], o):
+            np.testing.assert_array_equal(a, b)

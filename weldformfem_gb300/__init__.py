@@ -121,6 +121,7 @@ _SIGS = {
     "wf_get_launch_config": [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                              C.POINTER(C.c_double)],
     "wf_get_transfer_bytes": [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)],
+    "wf_set_launch_config": [C.c_void_p, C.c_int32, C.c_int32, C.c_int32],
     "wf_adjoint_forward": [C.c_void_p, C.c_int64, C.c_int64],
     "wf_deck_read": [C.c_char_p, C.POINTER(C.c_void_p), C.c_char_p, C.c_int64],
     "wf_deck_free": [C.c_void_p],
@@ -381,6 +382,10 @@ class Domain:
 
     def set_autotune(self, on=True):
         self._call("wf_set_autotune", int(bool(on)))
+
+    def set_launch_config(self, phase, block, items_per_thread):
+        """Launch shape of phase 0/1/2 (items_per_thread 0: persistent grid)."""
+        self._call("wf_set_launch_config", int(phase), int(block), int(items_per_thread))
 
     def launch_config(self, phase):
         """(block size, items per thread, trial ms) chosen for phase 0/1/2."""

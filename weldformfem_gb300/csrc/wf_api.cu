@@ -911,7 +911,8 @@ wf_status autotune_launches(wf_domain *d) {
   cudaEvent_t a, b;
   CUDA_TRY(cudaEventCreate(&a));
   CUDA_TRY(cudaEventCreate(&b));
-  const int sizes[3] = {64, 128, 256}, epts[3] = {1, 2, 4};
+  // items per thread 1, 2, 4, or 0: a persistent grid (SMs x resident blocks)
+  const int sizes[3] = {64, 128, 256}, epts[4] = {1, 2, 4, 0};
   for (int phase = 0; phase < 3; phase++) {
     double best = 1e300;
     LaunchCfg pick = d->cfg[phase];
@@ -955,6 +956,21 @@ WF_API wf_status wf_set_autotune(wf_domain *d, int32_t on) {
   if (!d) return WF_ERR_ARG;
   if (d->initialized) return fail(d, WF_ERR_STATE, "autotuning is chosen before init");
   d->autotune = on != 0;
+  return WF_OK;
+}
+
+WF_API wf_status wf_set_launch_config(wf_domain *d, int32_t phase, int32_t block,
+                                      int32_t items_per_thread) {
+  if (!d || phase < 0 || phase > 2) return WF_ERR_ARG;
+  if (block != 64 && block != 128 && block != 256)
+    return fail(d, WF_ERR_ARG, "block size must be 64, 128 or 256");
+  if (items_per_thread < 0) return fail(d, WF_ERR_ARG, "items per thread must be >= 0");
+  d->cfg[phase] = LaunchCfg{block, items_per_thread};
+  d->cfg_ms[phase] = 0.0;
+  if (d->graph) {
+    cudaGraphExecDestroy(d->graph);
+    d->graph = nullptr;
+  }
   return WF_OK;
 }
 
@@ -1118,6 +1134,8 @@ WF_API wf_status wf_init(wf_domain *d) {
   MatDev *mdev = nullptr;
   CUDA_TRY(upload(d, &mdev, md));
   P.mats = mdev;
+  for (const MatDev &t : md)
+    if (t.model != WF_MAT_BILINEAR) P.mat_general = 1;
   P.k0 = md[0].K;
   if (!d->emat.empty()) {
     int32_t *em = nullptr;

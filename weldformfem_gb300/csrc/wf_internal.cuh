@@ -77,6 +77,7 @@ struct StepParams {
   const uint8_t *nflag;   // [nn]
   const MatDev *mats;
   const int32_t *emat;    // [ne] or null
+  int32_t mat_general;    // 1 when a material is not bilinear (mixed kernels' general law)
   double k0;              // bulk modulus of material 0 (pressure algorithm 1)
   // FP32 constants of the mixed kernels (host-rounded once)
   float f_dt, f_alpha, f_fcorr;

@@ -15,6 +15,10 @@
 //  * with default options the pressure is -K (J_avg - 1) (pressure
 //    algorithm 0 with zero stabilisation, as the reference defaults);
 //  * displacements are x - x0 (exported in FP64), total strain is not kept.
+#include <map>
+#include <mutex>
+#include <utility>
+
 #include "wf_internal.cuh"
 
 namespace wf {
@@ -223,9 +227,13 @@ __global__ void __launch_bounds__(BS) k_mix_nodal(StepParams P, MixState M, cons
 // stored components are formed, terms that multiply a zero of W are dropped.
 // In: strain rate sr (xx yy zz xy yz xz), spin (w01, w12, w02), pressure p.
 // Writes the new tau and eps_p; returns sigma = tau - p I in sg.
+// LAW = 0: linear hardening only (the common case, fewer registers); LAW = 1:
+// every material model.
+template <int LAW>
 __device__ __forceinline__ void stress_update(const StepParams &P, const MixState &M, int64_t e,
                                               const MatF &m, const float (&sr)[6], float w01,
-                                              float w12, float w02, float p, float (&sg)[6]) {
+                                              float w12, float w02, float p, float (&sg)[6],
+                                              float &sdot) {
   const int64_t ne = P.ne;
   const float dt = P.espec ? P.specf[P.espec[e]].dt : P.f_dt;
   float t0 = M.tau[e], t1 = M.tau[ne + e], t2 = M.tau[2 * ne + e];
@@ -256,7 +264,9 @@ __device__ __forceinline__ void stress_update(const StepParams &P, const MixStat
   float pls = M.pls[e];
   float sy;
   float eff = 0.f;
-  if (m.model == WF_MAT_JOHNSON_COOK) {
+  if (LAW == 0) {
+    sy = m.sy0 + m.H * pls;
+  } else if (m.model == WF_MAT_JOHNSON_COOK) {
     eff = sqrtf(0.5f * ((sr[0] - sr[1]) * (sr[0] - sr[1]) + (sr[1] - sr[2]) * (sr[1] - sr[2]) +
                         (sr[2] - sr[0]) * (sr[2] - sr[0])) +
                 3.0f * (sr[3] * sr[3] + sr[4] * sr[4] + sr[5] * sr[5]));
@@ -270,7 +280,9 @@ __device__ __forceinline__ void stress_update(const StepParams &P, const MixStat
   }
   if (sy < sig_trial) {
     float H;
-    if (m.model == WF_MAT_JOHNSON_COOK) {
+    if (LAW == 0) {
+      H = m.H;
+    } else if (m.model == WF_MAT_JOHNSON_COOK) {
       const float er = (1.0e6f < eff) ? 1.0e6f : eff;
       H = (pls > 0.f) ? m.jc_n * m.jc_B * powf(pls, m.jc_n - 1.f) *
                             (1.0f + m.jc_C * logf(er / m.jc_eps0)) * m.jc_Th
@@ -293,6 +305,10 @@ __device__ __forceinline__ void stress_update(const StepParams &P, const MixStat
   M.tau[3 * ne + e] = t3; M.tau[4 * ne + e] = t4; M.tau[5 * ne + e] = t5;
   sg[0] = t0 - p; sg[1] = t1 - p; sg[2] = t2 - p;
   sg[3] = t3; sg[4] = t4; sg[5] = t5;
+  // sigma . str_rate over the six stored components (energy history)
+  if (P.energy_on)
+    sdot = sg[0] * sr[0] + sg[1] * sr[1] + sg[2] * sr[2] + sg[3] * sr[3] + sg[4] * sr[4] +
+           sg[5] * sr[5];
 }
 
 // Walsh transform over the corners of the hexahedron. Node a of the
@@ -339,7 +355,9 @@ __device__ __forceinline__ void walsh8_synth(const float (&o)[8], float (&v)[8])
 // nodal velocities, and the nodal forces are the synthesis of
 // T = adj(J)^T sigma (w / 8 = 1) plus the hourglass coefficients ch h_j.
 // Same quantities as the reference's per-node loops, fewer operations.
-__device__ __forceinline__ void element_hex(const StepParams &P, const MixState &M, int64_t e) {
+template <int LAW>
+__device__ __forceinline__ void element_hex(const StepParams &P, const MixState &M, int64_t e,
+                                            float *stash, int stride) {
   const int64_t ne = P.ne, np = P.np;
   int32_t nid[8];
   float A[3][3], detJ;
@@ -369,7 +387,7 @@ __device__ __forceinline__ void element_hex(const StepParams &P, const MixState 
     detJ = J[0][0] * A[0][0] + J[0][1] * A[1][0] + J[0][2] * A[2][0];
   }
   const float vol = detJ * 8.0f;
-  const MatF m = P.matf[P.emat ? __ldg(&P.emat[e]) : 0];
+  const MatF &m = P.matf[P.emat ? __ldg(&P.emat[e]) : 0];
   // velocity Walsh sums: G[m][k] (derivative directions), hm[k][j] (hourglass)
   float G[3][3], hm[3][4];
 #pragma unroll
@@ -383,6 +401,15 @@ __device__ __forceinline__ void element_hex(const StepParams &P, const MixState 
     G[2][k] = o[3];
 #pragma unroll
     for (int j = 0; j < 4; j++) hm[k][j] = o[4 + j];
+  }
+  // hourglass forces' coefficients ch h_j, kept in shared memory (one column
+  // per thread) across the stress update to free registers
+  {
+    const float ch = P.hg_on ? P.f_hg_coef * powf(vol, 0.6666666f) * m.rho * 0.25f * m.cs0 : 0.f;
+#pragma unroll
+    for (int k = 0; k < 3; k++)
+#pragma unroll
+      for (int j = 0; j < 4; j++) stash[(k * 4 + j) * stride] = ch * hm[k][j];
   }
   float J_avg = 0.f;
 #pragma unroll
@@ -402,14 +429,11 @@ __device__ __forceinline__ void element_hex(const StepParams &P, const MixState 
   float J_bar = J_avg * 0.125f;
   if (J_bar < 0.0f) J_bar = 0.2f;
   const float p = -m.K * (J_bar - 1.0f);
-  float sg[6];
-  stress_update(P, M, e, m, sr, w01, w12, w02, p, sg);
-  if (P.energy_on)
-    M.edot[e] = (sg[0] * sr[0] + sg[1] * sr[1] + sg[2] * sr[2] + sg[3] * sr[3] + sg[4] * sr[4] +
-                 sg[5] * sr[5]) * vol;
+  float sg[6], sdot = 0.f;
+  stress_update<LAW>(P, M, e, m, sr, w01, w12, w02, p, sg, sdot);
+  if (P.energy_on) M.edot[e] = sdot * vol;
   // sigma as a symmetric 3x3: S[i][k]
   const float S[3][3] = {{sg[0], sg[3], sg[5]}, {sg[3], sg[1], sg[4]}, {sg[5], sg[4], sg[2]}};
-  const float ch = P.hg_on ? P.f_hg_coef * powf(vol, 0.6666666f) * m.rho * 0.25f * m.cs0 : 0.f;
 #pragma unroll
   for (int k = 0; k < 3; k++) {
     float o[8], f[8];
@@ -417,7 +441,7 @@ __device__ __forceinline__ void element_hex(const StepParams &P, const MixState 
 #pragma unroll
     for (int mm = 0; mm < 3; mm++) o[1 + mm] = A[0][mm] * S[0][k] + A[1][mm] * S[1][k] + A[2][mm] * S[2][k];
 #pragma unroll
-    for (int j = 0; j < 4; j++) o[4 + j] = ch * hm[k][j];
+    for (int j = 0; j < 4; j++) o[4 + j] = stash[(k * 4 + j) * stride];
     walsh8_synth(o, f);
     // SoA by (local node, component): fe[(a * 3 + k) * ne + e]
 #pragma unroll
@@ -426,6 +450,7 @@ __device__ __forceinline__ void element_hex(const StepParams &P, const MixState 
 }
 
 // Tetrahedron: per-node shape derivatives (Domain_d.C:1866-1887).
+template <int LAW>
 __device__ __forceinline__ void element_tet(const StepParams &P, const MixState &M, int64_t e) {
   const int64_t ne = P.ne;
   int32_t nid[4];
@@ -439,7 +464,7 @@ __device__ __forceinline__ void element_tet(const StepParams &P, const MixState 
     shape_derivs_f<4>(J, dH);
     detJ = det3f(J);
   }
-  const MatF m = P.matf[P.emat ? __ldg(&P.emat[e]) : 0];
+  const MatF &m = P.matf[P.emat ? __ldg(&P.emat[e]) : 0];
   float s00 = 0.f, s11 = 0.f, s22 = 0.f, s01 = 0.f, s12 = 0.f, s02 = 0.f;
   float w01 = 0.f, w12 = 0.f, w02 = 0.f;
   float J_avg = 0.f;
@@ -468,12 +493,10 @@ __device__ __forceinline__ void element_tet(const StepParams &P, const MixState 
   float J_bar = J_avg;
   if (J_bar < 0.0f) J_bar = 0.2f;
   const float p = -m.K * (J_bar - 1.0f);
-  float sg[6];
-  stress_update(P, M, e, m, sr, w01, w12, w02, p, sg);
+  float sg[6], sdot = 0.f;
+  stress_update<LAW>(P, M, e, m, sr, w01, w12, w02, p, sg, sdot);
   const float w = weightf<4>();
-  if (P.energy_on)
-    M.edot[e] = (sg[0] * sr[0] + sg[1] * sr[1] + sg[2] * sr[2] + sg[3] * sr[3] + sg[4] * sr[4] +
-                 sg[5] * sr[5]) * (detJ * w);
+  if (P.energy_on) M.edot[e] = sdot * (detJ * w);
 #pragma unroll
   for (int a = 0; a < 4; a++) {
     const float d0 = dH[0][a], d1 = dH[1][a], d2 = dH[2][a];
@@ -483,22 +506,24 @@ __device__ __forceinline__ void element_tet(const StepParams &P, const MixState 
   }
 }
 
-template <int NPE>
-__device__ __forceinline__ void element_one(const StepParams &P, const MixState &M, int64_t e) {
+template <int NPE, int LAW>
+__device__ __forceinline__ void element_one(const StepParams &P, const MixState &M, int64_t e,
+                                            float *stash, int stride) {
   if constexpr (NPE == 8)
-    element_hex(P, M, e);
+    element_hex<LAW>(P, M, e, stash, stride);
   else
-    element_tet(P, M, e);
+    element_tet<LAW>(P, M, e);
 }
 
 // Registers per thread stay <= 64 at 1024 resident threads per SM.
 constexpr int elem_min_blocks(int bs) { return 1024 / bs; }
 
-template <int NPE, int BS>
+template <int NPE, int BS, int LAW>
 __global__ void __launch_bounds__(BS, elem_min_blocks(BS)) k_mix_elements(StepParams P,
                                                                           MixState M) {
+  __shared__ float stash[NPE == 8 ? 12 * BS : 1];
   for (int64_t e = (int64_t)blockIdx.x * BS + threadIdx.x; e < P.ne; e += (int64_t)gridDim.x * BS)
-    element_one<NPE>(P, M, e);
+    element_one<NPE, LAW>(P, M, e, &stash[threadIdx.x], BS);
 }
 
 // ---------------------------------------------------------------------------
@@ -747,36 +772,104 @@ void mix_init(const StepParams &P, const MixState &M, const Fp64State &S, cudaSt
 
 namespace {
 
+// Grid of a tunable launch: ceil(n / (bs * ept)) blocks, or with ept = 0 a
+// persistent grid of (SMs x resident blocks per SM) that strides over the
+// whole range. Occupancy and SM count are looked up once per instantiation.
+template <typename Kernel>
+unsigned tuned_grid(Kernel kernel, int bs, int ept, int64_t n) {
+  const unsigned full = grid_for(n, bs);
+  if (ept > 0) return grid_for(n, bs * ept);
+  static std::mutex mu;
+  static std::map<std::pair<const void *, int>, unsigned> cache;  // (kernel, device)
+  int dev = 0;
+  cudaGetDevice(&dev);
+  unsigned g;
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    auto key = std::make_pair((const void *)kernel, dev);
+    auto it = cache.find(key);
+    if (it == cache.end()) {
+      int sms = 0, per_sm = 0;
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, bs, 0);
+      it = cache.emplace(key, (unsigned)(sms * (per_sm < 1 ? 1 : per_sm))).first;
+    }
+    g = it->second;
+  }
+  return g < full ? g : full;
+}
+
 template <int NPE>
 void launch_geometry(const StepParams &P, const MixState &M, float *vol, cudaStream_t st,
                      LaunchCfg c) {
-  const unsigned g = grid_for(P.ne, c.bs * c.ept);
   switch (c.bs) {
-    case 64: k_mix_geometry<NPE, 64><<<g, 64, 0, st>>>(P, M, vol); break;
-    case 256: k_mix_geometry<NPE, 256><<<g, 256, 0, st>>>(P, M, vol); break;
-    default: k_mix_geometry<NPE, 128><<<g, 128, 0, st>>>(P, M, vol); break;
+    case 64: {
+      const unsigned g = tuned_grid(k_mix_geometry<NPE, 64>, 64, c.ept, P.ne);
+      k_mix_geometry<NPE, 64><<<g, 64, 0, st>>>(P, M, vol);
+      break;
+    }
+    case 256: {
+      const unsigned g = tuned_grid(k_mix_geometry<NPE, 256>, 256, c.ept, P.ne);
+      k_mix_geometry<NPE, 256><<<g, 256, 0, st>>>(P, M, vol);
+      break;
+    }
+    default: {
+      const unsigned g = tuned_grid(k_mix_geometry<NPE, 128>, 128, c.ept, P.ne);
+      k_mix_geometry<NPE, 128><<<g, 128, 0, st>>>(P, M, vol);
+      break;
+    }
   }
 }
 
 template <int NPE>
 void launch_nodal(const StepParams &P, const MixState &M, const float *vol, cudaStream_t st,
                   LaunchCfg c) {
-  const unsigned g = grid_for(P.nn, c.bs * c.ept);
   switch (c.bs) {
-    case 64: k_mix_nodal<NPE, 64><<<g, 64, 0, st>>>(P, M, vol); break;
-    case 128: k_mix_nodal<NPE, 128><<<g, 128, 0, st>>>(P, M, vol); break;
-    default: k_mix_nodal<NPE, 256><<<g, 256, 0, st>>>(P, M, vol); break;
+    case 64: {
+      const unsigned g = tuned_grid(k_mix_nodal<NPE, 64>, 64, c.ept, P.nn);
+      k_mix_nodal<NPE, 64><<<g, 64, 0, st>>>(P, M, vol);
+      break;
+    }
+    case 128: {
+      const unsigned g = tuned_grid(k_mix_nodal<NPE, 128>, 128, c.ept, P.nn);
+      k_mix_nodal<NPE, 128><<<g, 128, 0, st>>>(P, M, vol);
+      break;
+    }
+    default: {
+      const unsigned g = tuned_grid(k_mix_nodal<NPE, 256>, 256, c.ept, P.nn);
+      k_mix_nodal<NPE, 256><<<g, 256, 0, st>>>(P, M, vol);
+      break;
+    }
+  }
+}
+
+template <int NPE, int LAW>
+void launch_elements_law(const StepParams &P, const MixState &M, cudaStream_t st, LaunchCfg c) {
+  switch (c.bs) {
+    case 64: {
+      const unsigned g = tuned_grid(k_mix_elements<NPE, 64, LAW>, 64, c.ept, P.ne);
+      k_mix_elements<NPE, 64, LAW><<<g, 64, 0, st>>>(P, M);
+      break;
+    }
+    case 256: {
+      const unsigned g = tuned_grid(k_mix_elements<NPE, 256, LAW>, 256, c.ept, P.ne);
+      k_mix_elements<NPE, 256, LAW><<<g, 256, 0, st>>>(P, M);
+      break;
+    }
+    default: {
+      const unsigned g = tuned_grid(k_mix_elements<NPE, 128, LAW>, 128, c.ept, P.ne);
+      k_mix_elements<NPE, 128, LAW><<<g, 128, 0, st>>>(P, M);
+      break;
+    }
   }
 }
 
 template <int NPE>
 void launch_elements(const StepParams &P, const MixState &M, cudaStream_t st, LaunchCfg c) {
-  const unsigned g = grid_for(P.ne, c.bs * c.ept);
-  switch (c.bs) {
-    case 64: k_mix_elements<NPE, 64><<<g, 64, 0, st>>>(P, M); break;
-    case 256: k_mix_elements<NPE, 256><<<g, 256, 0, st>>>(P, M); break;
-    default: k_mix_elements<NPE, 128><<<g, 128, 0, st>>>(P, M); break;
-  }
+  if (P.mat_general)
+    launch_elements_law<NPE, 1>(P, M, st, c);
+  else
+    launch_elements_law<NPE, 0>(P, M, st, c);
 }
 
 }  // namespace
