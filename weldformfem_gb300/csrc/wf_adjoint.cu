@@ -139,6 +139,7 @@ __global__ void k_adj_nodes(StepParams P, AdjArgs A, int s, long long gstep, int
   }
   const double dt = P.dt;
   const double m = A.smass[(int64_t)s * np + n];
+  const double inv_m = 1.0 / m;
   const uint32_t code = P.bc[n];
   double mb = 0.0;
   for (int k = 0; k < 3; k++) {
@@ -147,8 +148,8 @@ __global__ void k_adj_nodes(StepParams P, AdjArgs A, int s, long long gstep, int
     const double fi = A.sfi[((int64_t)s * 3 + k) * np + n];
     const double abar = pabn + (fixed ? 0.0 : P.gamma * dt * vbn) + P.beta * dt * dt * xb[k];
     const double araw = fixed ? 0.0 : P.fcorr * abar;
-    double fib = -araw / m;
-    mb += araw * fi / (m * m);
+    double fib = -araw * inv_m;
+    mb += araw * fi * (inv_m * inv_m);
     if ((P.nflag[n] & NF_REACTION) && k == P.react_dim) fib += A.seed[gstep];
     A.fib[k * np + n] = fib;
     A.vpb[k * np + n] = fixed ? 0.0 : vbn;
@@ -432,6 +433,270 @@ __global__ void __launch_bounds__(kThreads) k_adj_elements(StepParams P, AdjArgs
   A.gth[2 * ne + e] += (double)Hb;
 }
 
+// Walsh transform over the hexahedron's corners and its transpose (node a at
+// the signs of (xi, eta, zeta) of the AddBoxLength numbering): o = sums of v
+// weighted by {1, xi, eta, zeta, eta zeta, xi zeta, xi eta, xi eta zeta};
+// the synthesis returns the node values of sum_b o[b] phi_b for b = 1..7.
+template <typename T>
+__device__ __forceinline__ void walsh8t(const T (&v)[8], T (&o)[8]) {
+  const T a0 = v[1] + v[0], b0 = v[1] - v[0], a1 = v[2] + v[3], b1 = v[2] - v[3];
+  const T a2 = v[5] + v[4], b2 = v[5] - v[4], a3 = v[6] + v[7], b3 = v[6] - v[7];
+  const T c0 = a1 + a0, d0 = a1 - a0, e0 = b1 + b0, f0 = b1 - b0;
+  const T c1 = a3 + a2, d1 = a3 - a2, e1 = b3 + b2, f1 = b3 - b2;
+  o[0] = c1 + c0; o[3] = c1 - c0; o[2] = d1 + d0; o[4] = d1 - d0;
+  o[1] = e1 + e0; o[5] = e1 - e0; o[6] = f1 + f0; o[7] = f1 - f0;
+}
+template <typename T>
+__device__ __forceinline__ void walsh8t_synth(const T (&o)[8], T (&v)[8]) {
+  const T c1 = o[3], c0 = -o[3];
+  const T d1 = o[2] + o[4], d0 = o[2] - o[4], e1 = o[1] + o[5], e0 = o[1] - o[5];
+  const T f1 = o[6] + o[7], f0 = o[6] - o[7];
+  const T a1 = c0 + d0, a0 = c0 - d0, b1 = e0 + f0, b0 = e0 - f0;
+  const T a3 = c1 + d1, a2 = c1 - d1, b3 = e1 + f1, b2 = e1 - f1;
+  v[1] = a0 + b0; v[0] = a0 - b0; v[2] = a1 + b1; v[3] = a1 - b1;
+  v[5] = a2 + b2; v[4] = a2 - b2; v[6] = a3 + b3; v[7] = a3 - b3;
+}
+
+// Reverse of the element phase of step s for hexahedra, in the Walsh form:
+// J = W(x)/8, the velocity gradient adj(J) W(v) / (8 detJ), the forces the
+// synthesis of adj(J)^T sigma and of the hourglass terms ch h_j (the same
+// quantities as the per-node formulation of the forward kernel). Outputs as
+// k_adj_elements. Coordinates enter relative to the element's first node.
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_adj_hex(StepParams P, AdjArgs A, int s) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= P.ne) return;
+  const int64_t np = P.np, ne = P.ne;
+  const double *sx = A.sx + (int64_t)s * 3 * np, *sv = A.sv + (int64_t)s * 3 * np;
+  const double *spa = A.spa + (int64_t)s * 3 * np, *sjr = A.sjr + (int64_t)s * np;
+  const double *stau = A.stau + (int64_t)s * 6 * ne, *spls = A.spls + (int64_t)s * ne;
+  const double dt_d = P.dt;
+  const T dt = (T)dt_d;
+  int32_t nid[8];
+  for (int a = 0; a < 8; a++) nid[a] = P.elnod[a * ne + e];
+  // Jacobian from relative coordinates
+  T J[3][3];
+  for (int k = 0; k < 3; k++) {
+    const double x0 = sx[k * np + nid[0]];
+    T v[8], o[8];
+    for (int a = 0; a < 8; a++) v[a] = (T)(sx[k * np + nid[a]] - x0);
+    walsh8t(v, o);
+    for (int mm = 0; mm < 3; mm++) J[mm][k] = (T)0.125 * o[1 + mm];
+  }
+  T Am[3][3];  // adj(J): Am[k][m] = cofactor[m][k]
+  Am[0][0] = (J[1][1] * J[2][2] - J[1][2] * J[2][1]);
+  Am[1][0] = -(J[1][0] * J[2][2] - J[1][2] * J[2][0]);
+  Am[2][0] = (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+  Am[0][1] = -(J[0][1] * J[2][2] - J[0][2] * J[2][1]);
+  Am[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]);
+  Am[2][1] = -(J[0][0] * J[2][1] - J[0][1] * J[2][0]);
+  Am[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]);
+  Am[1][2] = -(J[0][0] * J[1][2] - J[0][2] * J[1][0]);
+  Am[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]);
+  const T detJ = J[0][0] * Am[0][0] + J[0][1] * Am[1][0] + J[0][2] * Am[2][0];
+  const T vol = detJ * (T)8;
+  // predicted velocities: Walsh sums G (derivative directions) and hm (hourglass)
+  T G[3][3], hm[3][4];
+  for (int k = 0; k < 3; k++) {
+    T v[8], o[8];
+    for (int a = 0; a < 8; a++) {
+      const uint32_t code = P.bc[nid[a]];
+      double vv = sv[k * np + nid[a]] + (1.0 - P.gamma) * dt_d * spa[k * np + nid[a]];
+      if ((code >> k) & 1u) vv = P.bcval[3 * (code >> 3) + k];
+      v[a] = (T)vv;
+    }
+    walsh8t(v, o);
+    for (int mm = 0; mm < 3; mm++) G[mm][k] = o[1 + mm];
+    for (int j = 0; j < 4; j++) hm[k][j] = o[4 + j];
+  }
+  const MatDev m = P.mats[P.emat ? P.emat[e] : 0];
+  const T K = (T)m.K, Gm = (T)m.G, H = (T)m.H, sy0 = (T)m.sy0;
+  const T fl = (T)0.125 / detJ;
+  T L[3][3];
+  for (int i = 0; i < 3; i++)
+    for (int k = 0; k < 3; k++)
+      L[i][k] = fl * (Am[i][0] * G[0][k] + Am[i][1] * G[1][k] + Am[i][2] * G[2][k]);
+  const T D[6] = {L[0][0], L[1][1], L[2][2], (T)0.5 * (L[1][0] + L[0][1]),
+                  (T)0.5 * (L[2][1] + L[1][2]), (T)0.5 * (L[2][0] + L[0][2])};
+  const T w01 = (T)0.5 * (L[1][0] - L[0][1]);
+  const T w12 = (T)0.5 * (L[2][1] - L[1][2]);
+  const T w02 = (T)0.5 * (L[2][0] - L[0][2]);
+  T Javg = 0;
+  for (int a = 0; a < 8; a++) Javg += (T)sjr[nid[a]];
+  Javg /= (T)8;
+  const T p = -K * (Javg - (T)1);
+  T t[6];
+  for (int c = 0; c < 6; c++) t[c] = (T)stau[c * ne + e];
+  const T epl = (T)spls[e];
+  T Q[6];
+  Q[0] = (T)2 * (t[3] * w01 + t[5] * w02);
+  Q[1] = 0;
+  Q[2] = 0;
+  Q[3] = w01 * (t[0] + t[1]) - t[5] * w12 + w02 * t[4];
+  Q[4] = t[3] * w02 + w12 * (t[1] + t[2]) - w01 * t[5];
+  Q[5] = w02 * (t[0] + t[2]) + t[3] * w12 + w01 * t[4];
+  const T c3 = (D[0] + D[1] + D[2]) / (T)3;
+  const T Dd[6] = {D[0] - c3, D[1] - c3, D[2] - c3, D[3], D[4], D[5]};
+  T ts[6];
+  for (int c = 0; c < 6; c++) ts[c] = t[c] + dt * ((T)2 * Gm * Dd[c] + Q[c]);
+  const T tr3 = (ts[0] + ts[1] + ts[2]) / (T)3;
+  const T sdev[6] = {ts[0] - tr3, ts[1] - tr3, ts[2] - tr3, ts[3], ts[4], ts[5]};
+  const T J2 = (T)0.5 * (sdev[0] * sdev[0] + sdev[1] * sdev[1] + sdev[2] * sdev[2] +
+                         (T)2 * (sdev[3] * sdev[3] + sdev[4] * sdev[4] + sdev[5] * sdev[5]));
+  const T seq = sqrt((T)3 * J2);
+  const T sy = sy0 + H * epl;
+  const bool plastic = sy < seq;
+  T tn[6], dgam = 0, fac = 1;
+  if (plastic) {
+    dgam = (seq - sy) / ((T)3 * Gm + H);
+    fac = (T)1 - (T)3 * Gm * dgam / seq;
+    for (int c = 0; c < 6; c++) tn[c] = sdev[c] * fac;
+  } else {
+    for (int c = 0; c < 6; c++) tn[c] = ts[c];
+  }
+  const T S[3][3] = {{tn[0] - p, tn[3], tn[5]}, {tn[3], tn[1] - p, tn[4]}, {tn[5], tn[4], tn[2] - p}};
+  const T ch = P.hg_on ? (T)P.hg_coef * pow(vol, (T)0.6666666) * (T)A.rho[e] * (T)0.25 * (T)m.cs0
+                       : (T)0;
+
+  // ---- reverse ------------------------------------------------------------
+  // forces: f = synth(T, ch hm) with T = adj(J)^T S; the transpose is W(fb)
+  T Tb[3][3], hmb[3][4];
+  T chb = 0;
+  for (int k = 0; k < 3; k++) {
+    T v[8], o[8];
+    for (int a = 0; a < 8; a++) v[a] = (T)A.fib[k * np + nid[a]];
+    walsh8t(v, o);
+    for (int mm = 0; mm < 3; mm++) Tb[mm][k] = o[1 + mm];
+    for (int j = 0; j < 4; j++) {
+      chb += o[4 + j] * hm[k][j];
+      hmb[k][j] = ch * o[4 + j];
+    }
+  }
+  T Ab[3][3];
+  T Sb[3][3];
+  for (int i = 0; i < 3; i++)
+    for (int mm = 0; mm < 3; mm++) {
+      T acc = 0;
+      for (int k = 0; k < 3; k++) acc += S[i][k] * Tb[mm][k];
+      Ab[i][mm] = acc;
+    }
+  for (int i = 0; i < 3; i++)
+    for (int k = 0; k < 3; k++)
+      Sb[i][k] = Am[i][0] * Tb[0][k] + Am[i][1] * Tb[1][k] + Am[i][2] * Tb[2][k];
+  T sigb[6] = {Sb[0][0], Sb[1][1], Sb[2][2], Sb[0][1] + Sb[1][0], Sb[1][2] + Sb[2][1],
+               Sb[0][2] + Sb[2][0]};
+  T volb = 0, Kb = 0, Gb = 0, Hb = 0, sy0b = 0;
+  if (P.hg_on) {
+    volb += chb * ch * (T)0.6666666 / vol;
+    Kb += chb * ch * (T)0.5 / K;  // cs0 = sqrt(K / rho)
+  }
+  // sigma = tau_new - p I
+  T tnb[6];
+  for (int c = 0; c < 6; c++) tnb[c] = sigb[c] + (T)A.T[c * ne + e];
+  const T pb = -(sigb[0] + sigb[1] + sigb[2]);
+  T eplb = (T)A.EP[e];
+  T tsb[6];
+  if (plastic) {
+    T facb = 0;
+    T sdb[6];
+    for (int c = 0; c < 6; c++) {
+      facb += tnb[c] * sdev[c];
+      sdb[c] = tnb[c] * fac;
+    }
+    const T den = (T)3 * Gm + H;
+    const T dgb = eplb + facb * (-(T)3 * Gm / seq);
+    const T seqb = facb * ((T)3 * Gm * dgam / (seq * seq)) + dgb / den;
+    const T syb = -dgb / den;
+    Gb += facb * (-(T)3 * dgam / seq) + dgb * (-(T)3 * (seq - sy) / (den * den));
+    Hb += dgb * (-(seq - sy) / (den * den)) + syb * epl;
+    sy0b += syb;
+    eplb = eplb + syb * H;
+    const T q = (T)1.5 / seq * seqb;
+    for (int c = 0; c < 3; c++) sdb[c] += q * sdev[c];
+    for (int c = 3; c < 6; c++) sdb[c] += q * (T)2 * sdev[c];
+    const T mean = (sdb[0] + sdb[1] + sdb[2]) / (T)3;
+    for (int c = 0; c < 3; c++) tsb[c] = sdb[c] - mean;
+    for (int c = 3; c < 6; c++) tsb[c] = sdb[c];
+  } else {
+    for (int c = 0; c < 6; c++) tsb[c] = tnb[c];
+  }
+  const T Javgb = -K * pb;
+  Kb += -(Javg - (T)1) * pb;
+  T tb[6], Qb[6], Ddb[6];
+  for (int c = 0; c < 6; c++) {
+    tb[c] = tsb[c];
+    Qb[c] = dt * tsb[c];
+    Ddb[c] = dt * (T)2 * Gm * tsb[c];
+    Gb += dt * (T)2 * Dd[c] * tsb[c];
+  }
+  T w01b = 0, w12b = 0, w02b = 0;
+  tb[3] += Qb[0] * (T)2 * w01; tb[5] += Qb[0] * (T)2 * w02;
+  w01b += Qb[0] * (T)2 * t[3]; w02b += Qb[0] * (T)2 * t[5];
+  tb[0] += Qb[3] * w01; tb[1] += Qb[3] * w01; tb[5] -= Qb[3] * w12; tb[4] += Qb[3] * w02;
+  w01b += Qb[3] * (t[0] + t[1]); w12b -= Qb[3] * t[5]; w02b += Qb[3] * t[4];
+  tb[3] += Qb[4] * w02; tb[1] += Qb[4] * w12; tb[2] += Qb[4] * w12; tb[5] -= Qb[4] * w01;
+  w02b += Qb[4] * t[3]; w12b += Qb[4] * (t[1] + t[2]); w01b -= Qb[4] * t[5];
+  tb[0] += Qb[5] * w02; tb[2] += Qb[5] * w02; tb[3] += Qb[5] * w12; tb[4] += Qb[5] * w01;
+  w02b += Qb[5] * (t[0] + t[2]); w12b += Qb[5] * t[3]; w01b += Qb[5] * t[4];
+  T Db[6];
+  {
+    const T mean = (Ddb[0] + Ddb[1] + Ddb[2]) / (T)3;
+    for (int c = 0; c < 3; c++) Db[c] = Ddb[c] - mean;
+    for (int c = 3; c < 6; c++) Db[c] = Ddb[c];
+  }
+  // D, W from the velocity gradient L
+  T Lb[3][3] = {{Db[0], 0, 0}, {0, Db[1], 0}, {0, 0, Db[2]}};
+  Lb[1][0] += (T)0.5 * (Db[3] + w01b);
+  Lb[0][1] += (T)0.5 * (Db[3] - w01b);
+  Lb[2][1] += (T)0.5 * (Db[4] + w12b);
+  Lb[1][2] += (T)0.5 * (Db[4] - w12b);
+  Lb[2][0] += (T)0.5 * (Db[5] + w02b);
+  Lb[0][2] += (T)0.5 * (Db[5] - w02b);
+  // L = fl adj(J) G
+  T flb = 0;
+  for (int i = 0; i < 3; i++)
+    for (int k = 0; k < 3; k++) flb += Lb[i][k] * L[i][k];
+  flb /= fl;
+  T Gbar[3][3];
+  for (int mm = 0; mm < 3; mm++)
+    for (int k = 0; k < 3; k++)
+      Gbar[mm][k] = fl * (Am[0][mm] * Lb[0][k] + Am[1][mm] * Lb[1][k] + Am[2][mm] * Lb[2][k]);
+  for (int i = 0; i < 3; i++)
+    for (int mm = 0; mm < 3; mm++)
+      Ab[i][mm] += fl * (Lb[i][0] * G[mm][0] + Lb[i][1] * G[mm][1] + Lb[i][2] * G[mm][2]);
+  const T detJb = -flb * fl / detJ;
+  // predicted velocities: the transpose of the Walsh analysis
+  for (int k = 0; k < 3; k++) {
+    T o[8], v[8];
+    o[0] = 0;
+    for (int mm = 0; mm < 3; mm++) o[1 + mm] = Gbar[mm][k];
+    for (int j = 0; j < 4; j++) o[4 + j] = hmb[k][j];
+    walsh8t_synth(o, v);
+    for (int a = 0; a < 8; a++) A.cv[(a * 3 + k) * ne + e] = (double)v[a];
+  }
+  // adj(J) and detJ back to J, then to the coordinates
+  T Jb[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+  adj_reverse<T>(J, Ab, Jb);
+  for (int mm = 0; mm < 3; mm++)
+    for (int k = 0; k < 3; k++) Jb[mm][k] += detJb * Am[k][mm];
+  for (int k = 0; k < 3; k++) {
+    T o[8], v[8];
+    o[0] = 0;
+    for (int mm = 0; mm < 3; mm++) o[1 + mm] = (T)0.125 * Jb[mm][k];
+    for (int j = 4; j < 8; j++) o[j] = 0;
+    walsh8t_synth(o, v);
+    for (int a = 0; a < 8; a++) A.cx[(a * 3 + k) * ne + e] = (double)v[a];
+  }
+  A.cj[e] = (double)(Javgb / (T)8);
+  A.volb[e] = (double)volb;
+  for (int c = 0; c < 6; c++) A.T[c * ne + e] = (double)tb[c];
+  A.EP[e] = (double)eplb;
+  const double Eb = (double)Kb * (m.K / m.E) + (double)Gb * (m.G / m.E);
+  A.gth[e] += Eb;
+  A.gth[ne + e] += (double)sy0b;
+  A.gth[2 * ne + e] += (double)Hb;
+}
+
 // Node gather of the element contributions; predictor and nodal-volume reverse.
 __global__ void k_adj_gather(StepParams P, AdjArgs A) {
   const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -441,7 +706,7 @@ __global__ void k_adj_gather(StepParams P, AdjArgs A) {
   const int32_t b = P.off[n], c = P.off[n + 1] - b;
   double vpb[3] = {A.vpb[n], A.vpb[np + n], A.vpb[2 * np + n]};
   double xb[3] = {0, 0, 0};
-  double jrb = 0.0, rho_sum = 0.0;
+  double jrb = 0.0;
   for (int32_t q = 0; q < c; q++) {
     const int32_t sl = P.slot[b + q];
     const int64_t e = sl / npe, loc = sl % npe;
@@ -450,7 +715,6 @@ __global__ void k_adj_gather(StepParams P, AdjArgs A) {
       xb[k] += A.cx[(loc * 3 + k) * ne + e];
     }
     jrb += A.cj[e];
-    rho_sum += A.rho[e];
   }
   const uint32_t code = P.bc[n];
   const double dt = P.dt;
@@ -462,8 +726,8 @@ __global__ void k_adj_gather(StepParams P, AdjArgs A) {
     }
   }
   // jr = s / s0; mass = sum_e rho_e (s / npe) / c, recomputed each step
-  double sb = jrb / A.s0[n];
-  if (P.mass_mode == 0) sb += A.mb[n] * rho_sum / ((double)c * npe);
+  double sb = jrb * A.inv_s0[n];
+  if (P.mass_mode == 0) sb += A.mb[n] * A.dmds[n];
   A.sb[n] = sb;
 }
 
@@ -481,16 +745,45 @@ __global__ void k_adj_volume(StepParams P, AdjArgs A, int s) {
     volb += A.sb[n];
     for (int k = 0; k < 3; k++) x[a][k] = sx[k * np + n];
   }
-  ElemGeom<double, NPE> g;
-  geom_forward<double, NPE>(x, g);
   const double w = (NPE == 8) ? 8.0 : 1.0 / 6.0;
   const double detJb = w * volb;
-  for (int a = 0; a < NPE; a++)
+  if constexpr (NPE == 8) {
+    // d detJ / d J = cofactors; J = W(x) / 8 relative to node 0, x-bar its transpose
+    double J[3][3];
     for (int k = 0; k < 3; k++) {
-      double xb = 0;
-      for (int mm = 0; mm < 3; mm++) xb += detJb * g.A[k][mm] * tj<NPE>(mm, a);
-      A.cgeo[(a * 3 + k) * ne + e] = xb;
+      double v[8], o[8];
+      for (int a = 0; a < 8; a++) v[a] = x[a][k] - x[0][k];
+      walsh8t(v, o);
+      for (int mm = 0; mm < 3; mm++) J[mm][k] = 0.125 * o[1 + mm];
     }
+    double C[3][3];  // cofactors C[m][k] = d detJ / d J[m][k]
+    C[0][0] = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+    C[0][1] = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+    C[0][2] = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+    C[1][0] = J[0][2] * J[2][1] - J[0][1] * J[2][2];
+    C[1][1] = J[0][0] * J[2][2] - J[0][2] * J[2][0];
+    C[1][2] = J[0][1] * J[2][0] - J[0][0] * J[2][1];
+    C[2][0] = J[0][1] * J[1][2] - J[0][2] * J[1][1];
+    C[2][1] = J[0][2] * J[1][0] - J[0][0] * J[1][2];
+    C[2][2] = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+    for (int k = 0; k < 3; k++) {
+      double o[8], v[8];
+      o[0] = 0.0;
+      for (int mm = 0; mm < 3; mm++) o[1 + mm] = 0.125 * detJb * C[mm][k];
+      for (int j = 4; j < 8; j++) o[j] = 0.0;
+      walsh8t_synth(o, v);
+      for (int a = 0; a < 8; a++) A.cgeo[(a * 3 + k) * ne + e] = v[a];
+    }
+  } else {
+    ElemGeom<double, NPE> g;
+    geom_forward<double, NPE>(x, g);
+    for (int a = 0; a < NPE; a++)
+      for (int k = 0; k < 3; k++) {
+        double xb = 0;
+        for (int mm = 0; mm < 3; mm++) xb += detJb * g.A[k][mm] * tj<NPE>(mm, a);
+        A.cgeo[(a * 3 + k) * ne + e] = xb;
+      }
+  }
 }
 
 // Copies the start-of-step state into the stash slot s.
@@ -517,9 +810,25 @@ __global__ void k_adj_stash_step(StepParams P, Fp64State S, AdjArgs A, int s) {
   if (i < 3 * np) A.sfi[(int64_t)s * 3 * np + i] = S.fi[i];
 }
 
+// Per-node constants of the reverse: 1 / s0 and d(mass)/d(sum of element
+// volumes) = sum_e rho_e / (count npe) (CalcNodalMassFromVol, Mechanical.C:1576-1601).
+__global__ void k_adj_node_constants(StepParams P, AdjArgs A) {
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= P.nn) return;
+  const int32_t b = P.off[n], c = P.off[n + 1] - b;
+  double rho_sum = 0.0;
+  for (int32_t q = 0; q < c; q++) rho_sum += A.rho[P.slot[b + q] / P.npe];
+  A.inv_s0[n] = 1.0 / A.s0[n];
+  A.dmds[n] = rho_sum / ((double)c * P.npe);
+}
+
 inline unsigned grid_for(int64_t n) { return (unsigned)((n + kThreads - 1) / kThreads); }
 
 }  // namespace
+
+void adj_node_constants(const StepParams &P, const AdjArgs &A, cudaStream_t st) {
+  k_adj_node_constants<<<grid_for(P.nn), kThreads, 0, st>>>(P, A);
+}
 
 void adj_stash_state(const StepParams &P, const Fp64State &S, const AdjArgs &A, int s,
                      cudaStream_t st) {
@@ -537,9 +846,9 @@ void adj_reverse_step(const StepParams &P, const AdjArgs &A, int s, long long gs
   k_adj_nodes<<<grid_for(P.nn), kThreads, 0, st>>>(P, A, s, gstep, have_geo);
   if (P.npe == 8) {
     if (fp32)
-      k_adj_elements<float, 8><<<grid_for(P.ne), kThreads, 0, st>>>(P, A, s);
+      k_adj_hex<float><<<grid_for(P.ne), kThreads, 0, st>>>(P, A, s);
     else
-      k_adj_elements<double, 8><<<grid_for(P.ne), kThreads, 0, st>>>(P, A, s);
+      k_adj_hex<double><<<grid_for(P.ne), kThreads, 0, st>>>(P, A, s);
   } else {
     if (fp32)
       k_adj_elements<float, 4><<<grid_for(P.ne), kThreads, 0, st>>>(P, A, s);

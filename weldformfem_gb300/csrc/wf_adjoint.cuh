@@ -23,6 +23,7 @@ struct AdjArgs {
   // per-step scratch
   double *fib, *vpb;        // [3][np] adjoint of internal force / predicted velocity
   double *mb, *sb;          // [np]    adjoint of lumped mass / nodal volume sum
+  double *inv_s0, *dmds;    // [np]    1 / s0 and d(mass)/d(volume sum)
   double *cx, *cv, *cgeo;   // [npe][3][ne] per element-node contributions
   double *cj, *volb;        // [ne]
   double *gth;              // [3][ne] per-element dL/d(E, sigma_y0, H), summed over steps
@@ -32,6 +33,7 @@ struct AdjArgs {
   const double *rho;        // [ne] element density (constant during the run)
 };
 
+void adj_node_constants(const StepParams &P, const AdjArgs &A, cudaStream_t st);
 void adj_stash_state(const StepParams &P, const Fp64State &S, const AdjArgs &A, int slot,
                      cudaStream_t st);
 void adj_stash_step(const StepParams &P, const Fp64State &S, const AdjArgs &A, int slot,

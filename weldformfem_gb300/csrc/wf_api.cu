@@ -1843,10 +1843,14 @@ wf_status adjoint_buffers(wf_domain *d) {
   CUDA_TRY(adj_alloc(d, &A.cj, ne));
   CUDA_TRY(adj_alloc(d, &A.volb, ne));
   CUDA_TRY(adj_alloc(d, &A.gth, 3 * ne));
+  CUDA_TRY(adj_alloc(d, &A.inv_s0, np));
+  CUDA_TRY(adj_alloc(d, &A.dmds, np));
   CUDA_TRY(adj_alloc(d, &d->adj_seed, d->adj_steps));
   A.seed = d->adj_seed;
   A.s0 = d->S.s0;
   A.rho = d->S.rho;
+  adj_node_constants(d->P, A, d->stream);
+  CUDA_TRY(cudaGetLastError());
   d->adj_buffers = true;
   return WF_OK;
 }
