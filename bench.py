@@ -447,6 +447,13 @@ def run_adjoint(args):
     ms_b64, g64 = timed(d, lambda: d.adjoint_backward(seed))
     l2 = d.launch_count()
     ms_b32, g32 = timed(d, lambda: d.adjoint_backward(seed, fp32=True))
+    del d
+    # every step kept in HBM instead of checkpoints: no recompute
+    d = fresh()
+    ms_ka, _ = timed(d, lambda: d.adjoint_forward(N, -1))
+    ms_kb, gk = timed(d, lambda: d.adjoint_backward(seed))
+    ms_kb32, _ = timed(d, lambda: d.adjoint_backward(seed, fp32=True))
+    assert np.array_equal(gk, g64)
     clk = clocks.stop()
     loss = float(np.sum((R - Rstar) ** 2))
     assert np.array_equal(R, R_plain)
@@ -482,7 +489,12 @@ def run_adjoint(args):
         "ratios": {"backward_fp64_over_forward": round(ms_b64 / ms_fwd, 3),
                    "backward_fp32_over_forward": round(ms_b32 / ms_fwd, 3),
                    "checkpointed_forward_plus_backward_over_forward":
-                       round((ms_ck + ms_b64) / ms_fwd, 3)},
+                       round((ms_ck + ms_b64) / ms_fwd, 3),
+                   "all_steps_kept": {
+                       "forward_over_forward": round(ms_ka / ms_fwd, 3),
+                       "backward_fp64_over_forward": round(ms_kb / ms_fwd, 3),
+                       "backward_fp32_over_forward": round(ms_kb32 / ms_fwd, 3),
+                       "stash_gb": round(N * (14 * case.n_node + 7 * E) * 8 / 1e9, 2)}},
         "element_steps_per_s_forward_fp64": round(E * N / (ms_fwd * 1e-3), 1),
         "loss": loss,
         "gradient_fd_check": fd,

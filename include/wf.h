@@ -296,7 +296,9 @@ WF_API wf_status wf_nodal_volumes_noalloc(const double *xyz, const int32_t *elno
  * sigma_y0 and H of every material.
  * wf_adjoint_forward runs nsteps steps from the current state, as wf_run
  * does, and keeps an in-memory checkpoint of the state (x, v, prev_a, u, tau,
- * eps, eps_p) every `every` steps (0: about sqrt(nsteps)). Supported: FP64
+ * eps, eps_p) every `every` steps (0: about sqrt(nsteps); -1: keep every
+ * step's inputs instead, no checkpoints and no recompute in the reverse pass,
+ * when the device has room: nsteps (14 nn + 7 ne) doubles). Supported: FP64
  * precision, bilinear materials, pressure algorithm 0 with default
  * stabilisation, no artificial viscosity, no contact, no specimens.
  * wf_adjoint_backward takes dL_dR[nsteps] (host) and writes

@@ -109,7 +109,7 @@ def test_fp32_reverse_against_fp64(problem):
 def test_checkpoint_interval_does_not_change_gradient(problem):
     c, th0, Rstar = problem
     grads = []
-    for every in (1, 7, 0, STEPS):
+    for every in (1, 7, 0, STEPS, -1):   # -1: every step kept, no recompute
         R, d = A.solve_with_adjoint(c, th0, STEPS, every=every)
         grads.append(d.adjoint_backward(2.0 * (R - Rstar)))
     for g in grads[1:]:
@@ -117,9 +117,10 @@ def test_checkpoint_interval_does_not_change_gradient(problem):
 
 
 @pytest.mark.gpu
-def test_backward_restores_final_state_and_repeats(problem):
+@pytest.mark.parametrize("every", [32, -1])
+def test_backward_restores_final_state_and_repeats(problem, every):
     c, th0, Rstar = problem
-    R, d = A.solve_with_adjoint(c, th0, STEPS, every=32)
+    R, d = A.solve_with_adjoint(c, th0, STEPS, every=every)
     u = d.node_vec("u")
     pl = d.elem_scalar("pl_strain")
     seed = np.random.default_rng(7).standard_normal(STEPS)

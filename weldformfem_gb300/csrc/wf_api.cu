@@ -162,6 +162,7 @@ struct wf_domain {
   // adjoint recording: checkpoints of the forward run and reverse-pass buffers
   std::vector<void *> adj_allocs;
   int64_t adj_steps = 0, adj_every = 0, adj_first = 0;
+  bool adj_store_all = false;     // every step stashed in the forward, no recompute
   int64_t adj_nck = 0;
   double *ck_node = nullptr;      // [nck][4][3 np]: x, v, prev_a, u
   double *ck_elem = nullptr;      // [nck][13][ne]: tau, eps, eps_p
@@ -207,6 +208,7 @@ void free_adjoint(wf_domain *d) {
   for (void *p : d->adj_allocs) cudaFree(p);
   d->adj_allocs.clear();
   d->adj_steps = d->adj_every = d->adj_nck = 0;
+  d->adj_store_all = false;
   d->ck_node = d->ck_elem = nullptr;
   d->ck_st = nullptr;
   d->A = AdjArgs{};
@@ -1409,17 +1411,13 @@ wf_status ensure_graph(wf_domain *d) {
   return WF_OK;
 }
 
-}  // namespace
-
-WF_API wf_status wf_run(wf_domain *d, int64_t nsteps) {
-  if (!d || nsteps < 0) return WF_ERR_ARG;
-  if (!d->initialized) return fail(d, WF_ERR_STATE, "wf_init not called");
-  if (nsteps == 0) return WF_OK;
-  CUDA_TRY(cudaSetDevice(d->device));
-  if (d->host_step + nsteps > d->hist_cap) {
+// Grows the device histories (reaction, per-specimen reactions, energies) to
+// hold `total` steps, keeping what is recorded so far.
+wf_status grow_history(wf_domain *d, int64_t total) {
+  if (total > d->hist_cap) {
     // grow the reaction history (device copy of what is recorded so far)
     int64_t cap = d->hist_cap;
-    while (cap < d->host_step + nsteps) cap *= 2;
+    while (cap < total) cap *= 2;
     double *nh = nullptr;
     CUDA_TRY(dalloc(d, &nh, cap));
     CUDA_TRY(cudaMemcpyAsync(nh, d->P.hist, sizeof(double) * d->hist_cap, cudaMemcpyDeviceToDevice,
@@ -1447,6 +1445,20 @@ WF_API wf_status wf_run(wf_domain *d, int64_t nsteps) {
       cudaGraphExecDestroy(d->graph);
       d->graph = nullptr;
     }
+  }
+  return WF_OK;
+}
+
+}  // namespace
+
+WF_API wf_status wf_run(wf_domain *d, int64_t nsteps) {
+  if (!d || nsteps < 0) return WF_ERR_ARG;
+  if (!d->initialized) return fail(d, WF_ERR_STATE, "wf_init not called");
+  if (nsteps == 0) return WF_OK;
+  CUDA_TRY(cudaSetDevice(d->device));
+  {
+    const wf_status gs = grow_history(d, d->host_step + nsteps);
+    if (gs) return gs;
   }
   if (!(d->dt > 0.0) && !d->nspec) return fail(d, WF_ERR_STATE, "time step not set (SetDT)");
   set_dt_constants(d->P, d->dt);
@@ -1857,8 +1869,32 @@ wf_status adjoint_buffers(wf_domain *d) {
 
 }  // namespace
 
+namespace {
+
+// FP64 steps from the current state with each step's inputs stashed in slots
+// first..first+L-1 (the recompute of a segment, or the whole forward run when
+// every step is kept).
+void run_stashed(wf_domain *d, int64_t first, int64_t L) {
+  const StepParams &P = d->P;
+  const Fp64State &S = d->S;
+  const AdjArgs &A = d->A;
+  fp64_predict(P, S, d->stream);
+  for (int64_t j = 0; j < L; j++) {
+    adj_stash_state(P, S, A, (int)(first + j), d->stream);
+    fp64_geometry(P, S, d->stream, false);
+    fp64_nodal(P, S, d->stream, 0);
+    fp64_elements(P, S, d->stream);
+    fp64_nodes(P, S, d->stream, d->node_grid);
+    if (P.energy_on) energy_fp64(P, S, d->stream);
+    adj_stash_step(P, S, A, (int)(first + j), d->stream);
+  }
+  d->launches += 1 + (6 + (P.energy_on ? 1 : 0)) * L;
+}
+
+}  // namespace
+
 WF_API wf_status wf_adjoint_forward(wf_domain *d, int64_t nsteps, int64_t every) {
-  if (!d || nsteps <= 0 || every < 0) return WF_ERR_ARG;
+  if (!d || nsteps <= 0 || every < -1) return WF_ERR_ARG;
   if (!d->initialized) return fail(d, WF_ERR_STATE, "wf_init not called");
   if (d->precision != WF_FP64)
     return fail(d, WF_ERR_UNSUPPORTED, "the adjoint records the FP64 step");
@@ -1873,6 +1909,31 @@ WF_API wf_status wf_adjoint_forward(wf_domain *d, int64_t nsteps, int64_t every)
       return fail(d, WF_ERR_UNSUPPORTED, "the adjoint supports bilinear (linear hardening) materials");
   if (!(d->dt > 0.0)) return fail(d, WF_ERR_STATE, "time step not set (SetDT)");
   CUDA_TRY(cudaSetDevice(d->device));
+  if (every == -1) {
+    // keep every step's inputs: no checkpoints, no recompute in the reverse pass
+    free_adjoint(d);
+    const double need = (double)nsteps * (14.0 * d->np + 7.0 * d->ne) * sizeof(double);
+    size_t free_b = 0, total_b = 0;
+    CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
+    if (need > 0.9 * (double)free_b)
+      return fail(d, WF_ERR_NOMEM, "keeping %lld steps needs %.1f GB, %.1f GB free: use checkpoints",
+                  (long long)nsteps, need / 1e9, free_b / 1e9);
+    d->adj_steps = nsteps;
+    d->adj_every = nsteps;
+    d->adj_nck = 0;
+    d->adj_store_all = true;
+    d->adj_first = d->host_step;
+    wf_status s = adjoint_buffers(d);
+    if (s) return s;
+    s = grow_history(d, d->host_step + nsteps);
+    if (s) return s;
+    set_dt_constants(d->P, d->dt);
+    run_stashed(d, 0, nsteps);
+    CUDA_TRY(cudaGetLastError());
+    for (int64_t i = 0; i < nsteps; i++) d->host_time += d->dt;
+    d->host_step += nsteps;
+    return WF_OK;
+  }
   if (every == 0) every = std::max<int64_t>(1, (int64_t)std::llround(std::sqrt((double)nsteps)));
   every = std::min(every, nsteps);
   free_adjoint(d);
@@ -1916,33 +1977,30 @@ WF_API wf_status wf_adjoint_backward(wf_domain *d, const double *dL_dR, int32_t 
   CUDA_TRY(cudaMemsetAsync(A.gth, 0, sizeof(double) * 3 * ne, d->stream));
   StepParams &P = d->P;
   set_dt_constants(P, d->dt);
-  const Fp64State &S = d->S;
+  if (d->adj_store_all) {
+    // every step's inputs are in the stash: reverse straight away
+    for (int64_t j = N - 1; j >= 0; j--)
+      adj_reverse_step(P, A, (int)j, j, 1, reverse_fp32 != 0, d->stream);
+    CUDA_TRY(cudaGetLastError());
+    d->launches += 4 * N;
+  }
   for (int64_t c = d->adj_nck - 1; c >= 0; c--) {
     const int64_t c0 = c * every, L = std::min(every, N - c0);
     s = ck_copy(d, c, false);
     if (s) return s;
-    // recompute the segment, stashing each step's inputs
-    fp64_predict(P, S, d->stream);
-    for (int64_t j = 0; j < L; j++) {
-      adj_stash_state(P, S, A, (int)j, d->stream);
-      fp64_geometry(P, S, d->stream, false);
-      fp64_nodal(P, S, d->stream, 0);
-      fp64_elements(P, S, d->stream);
-      fp64_nodes(P, S, d->stream, d->node_grid);
-      adj_stash_step(P, S, A, (int)j, d->stream);
-    }
-    // reverse it
+    // recompute the segment, stashing each step's inputs, then reverse it
+    run_stashed(d, 0, L);
     for (int64_t j = L - 1; j >= 0; j--)
       adj_reverse_step(P, A, (int)j, c0 + j, 1, reverse_fp32 != 0, d->stream);
     CUDA_TRY(cudaGetLastError());
-    d->launches += 1 + 10 * L;
+    d->launches += 4 * L;
   }
   // back to the state at the end of the forward run
-  {
+  if (!d->adj_store_all) {
     const int64_t c = d->adj_nck - 1, L = N - c * every;
     s = ck_copy(d, c, false);
     if (s) return s;
-    fp64_predict(P, S, d->stream);
+    fp64_predict(P, d->S, d->stream);
     for (int64_t j = 0; j < L; j++) launch_step(d);
     CUDA_TRY(cudaGetLastError());
     d->launches += 1 + (4 + (P.energy_on ? 1 : 0)) * L;
