@@ -167,6 +167,34 @@ class Domain_d {
                                  penalty_factor),
           "setTriMesh");
   }
+  // addMeshData (Domain_d.C:2780, TriMesh_d::AddMesh): another rigid body with
+  // its own uniform velocity; only body 0 (setTriMesh) feeds the reaction
+  void addMeshData(const std::vector<double> &xyz, const std::vector<int32_t> &tri,
+                   const vector_t &vel) {
+    const double v[3] = {vel.x, vel.y, vel.z};
+    check(wf_add_contact_trimesh(d_, (int64_t)xyz.size() / 3, xyz.data(),
+                                 (int64_t)tri.size() / 3, tri.data(), v),
+          "addMeshData");
+  }
+  // TriMesh_d(NastranReader(path), flipnormals, orientNormals, orient_pt)
+  // (Mesh.C:560-760): die nodes and triangles from a Nastran file
+  static void ReadNastranMesh(const std::string &path, bool flipnormals, bool orientNormals,
+                              const vector_t &orient_pt, std::vector<double> &xyz,
+                              std::vector<int32_t> &tri) {
+    const double p[3] = {orient_pt.x, orient_pt.y, orient_pt.z};
+    const double *pp = orientNormals ? p : nullptr;
+    int64_t nn = 0, nt = 0;
+    char err[512] = {0};
+    wf_status s = wf_read_nastran(path.c_str(), flipnormals, pp, nullptr, 0, nullptr, 0, &nn,
+                                  &nt, err, sizeof(err));
+    if (s == WF_OK) {
+      xyz.resize(3 * nn);
+      tri.resize(3 * nt);
+      s = wf_read_nastran(path.c_str(), flipnormals, pp, xyz.data(), nn, tri.data(), nt, &nn,
+                          &nt, err, sizeof(err));
+    }
+    if (s != WF_OK) throw std::runtime_error(path + ": " + err);
+  }
   // CreateFromLSDyna (Domain_d.C:1647-1699) from a keyword file
   void CreateFromLSDyna(const std::string &path) {
     check(wf_load_lsdyna(d_, path.c_str()), "CreateFromLSDyna");

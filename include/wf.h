@@ -194,13 +194,24 @@ WF_API wf_status wf_set_contact_plane(wf_domain *d, double z0, double vz, double
  * from the accumulated slip. As in the reference, a node keeps its last contact
  * force after it leaves contact, the die velocity ramps as
  * sqrt(t / (0.01 end time)) over the first 1 % of the end time, and the
- * reaction history records the sum of normal-force magnitudes. FP64 precision
- * only. */
+ * reaction history records the sum of normal-force magnitudes. This mesh is
+ * rigid body 0; wf_add_contact_trimesh appends more. FP64 precision only. */
 WF_API wf_status wf_set_contact_trimesh(wf_domain *d, int64_t nnodes, const double *xyz,
                                         int64_t ntri, const int32_t *tri, const double vel[3],
                                         double mu_static, double mu_dynamic,
                                         double penalty_factor);
-/* Current die node positions (3 per node): *n = node count, copies min(cap, *n). */
+/* Appends another rigid body to the contact mesh (TriMesh_d::AddMesh,
+ * Mesh.C:445-545; Domain_d::addMeshData, Domain_d.C:2780): its nodes xyz[3 nnodes]
+ * and triangles tri[3 ntri] (indices into this body's own nodes) with uniform
+ * velocity vel[3]. Bodies take the indices 1, 2, ... in the order added; a
+ * node contacts the first triangle it penetrates over all bodies in that
+ * order, friction and penalty factor are those of wf_set_contact_trimesh, and
+ * the reaction history sums only the contacts with body 0 (Contact.C:326-329).
+ * Called after wf_set_contact_trimesh and before wf_init. */
+WF_API wf_status wf_add_contact_trimesh(wf_domain *d, int64_t nnodes, const double *xyz,
+                                        int64_t ntri, const int32_t *tri, const double vel[3]);
+/* Current die node positions (3 per node, all bodies in order): *n = node
+ * count, copies min(cap, *n). */
 WF_API wf_status wf_get_trimesh_nodes(wf_domain *d, double *out, int64_t cap, int64_t *n);
 
 /* ---- batched ensemble --------------------------------------------------------- */
@@ -255,6 +266,20 @@ WF_API wf_status wf_get_launch_config(const wf_domain *d, int32_t phase, int32_t
  * after it (the choice replaces the tuned one). */
 WF_API wf_status wf_set_launch_config(wf_domain *d, int32_t phase, int32_t block,
                                       int32_t items_per_thread);
+/* Step scheduling of the mixed-precision path. Mode 1: each step is the four
+ * phase kernels (geometry, nodal, element, node), replayed as a CUDA graph.
+ * Mode 2: a whole wf_run is one launch of one thread-block cluster (up to 16
+ * blocks, sized at wf_init for meshes of at most 65536 elements) whose blocks
+ * own fixed element and node ranges and meet at cluster barriers between the
+ * phases: same per-element and per-node arithmetic, so the state is bitwise
+ * that of mode 1; the reaction sum runs in another order. Not with specimens,
+ * the energy history or phase timing. Mode 0 (default) picks mode 2 for
+ * meshes of at most 8192 elements, else mode 1. wf_get_step_mode reports the
+ * mode the next wf_run uses and, for mode 2, the cluster's blocks and block
+ * size (0 otherwise). */
+WF_API wf_status wf_set_step_mode(wf_domain *d, int32_t mode);
+WF_API wf_status wf_get_step_mode(const wf_domain *d, int32_t *mode, int32_t *blocks,
+                                  int32_t *block_size);
 /* Number of kernels this domain has launched since wf_init (graph nodes
  * included). */
 WF_API wf_status wf_get_launch_count(const wf_domain *d, int64_t *n);
@@ -329,14 +354,19 @@ WF_API wf_status wf_adjoint_backward(wf_domain *d, const double *dL_dR, int32_t 
  * zoneId), then the symmetry-plane BCs, in the reference's order. The time
  * step is cflFactor * (shortest segment between the first four nodes of each
  * element) / sqrt(K / rho), the reference's calcMinEdgeLength in 3-D.
- * RigidBodies[0] of type Plane becomes a rigid triangle-mesh die
- * (TriMesh_d::AxisPlaneMesh on axis z from start/dim with partSide cells per
- * side, flipnormals) moving with the velocity of the boundary condition whose
- * zoneId is the body's, with the Contact block's fricCoeffStatic,
- * fricCoeffDynamic and penaltyFactor; as in the reference driver, a contact
- * deck applies no velocity zones to the part (symmetry planes only).
- * Thermal, axisymmetric/plane-strain, Perzyna, Line/File rigid bodies and
- * second rigid bodies return WF_ERR_UNSUPPORTED. Configuration.hourglass3D (not a reference key,
+ * RigidBodies[0] and RigidBodies[1] (the reference driver reads no further
+ * entries) become rigid triangle meshes, body 0 through
+ * wf_set_contact_trimesh and body 1 through wf_add_contact_trimesh: type
+ * Plane is TriMesh_d::AxisPlaneMesh on axis z from start/dim with partSide
+ * cells per side and flipnormals; type File is a Nastran mesh (fileName,
+ * relative to the deck; see wf_read_nastran) with flipnormals, orientNormals
+ * (default true) and orientPoint (default the mean of the part's nodes). Each
+ * body moves with the velocity of the boundary condition whose zoneId is the
+ * body's; the Contact block gives fricCoeffStatic, fricCoeffDynamic and
+ * penaltyFactor; as in the reference driver, a contact deck applies no
+ * velocity zones to the part (symmetry planes only). Thermal,
+ * axisymmetric/plane-strain, Perzyna and Line (2-D) rigid bodies return
+ * WF_ERR_UNSUPPORTED. Configuration.hourglass3D (not a reference key,
  * default 0 as the reference's 3-D no-op) sets the viscous hourglass
  * coefficient. Errors are written into err (err_len bytes, may be null). */
 typedef struct wf_deck wf_deck;
@@ -352,21 +382,41 @@ typedef struct {
   double artif_visc[2];
   wf_stab stab;
   wf_material material;
-  /* rigid-body die (RigidBodies[0] type Plane) */
+  /* rigid body 0 (RigidBodies[0]): its mesh sizes and velocity */
   int32_t contact;
   int32_t die_nodes, die_tris;
   double die_vel[3];
   double mu_static, mu_dynamic, penalty_factor;
   /* Johnson-Cook material: B, n, C, eps0_dot, m, T_melt, T_transition, T */
   double johnson_cook[8];
+  int32_t rigid_bodies;  /* number of rigid bodies read (0, 1 or 2) */
 } wf_deck_info;
 WF_API wf_status wf_deck_read(const char *path, wf_deck **out, char *err, int64_t err_len);
 WF_API wf_status wf_deck_free(wf_deck *k);
 WF_API wf_status wf_deck_get_info(const wf_deck *k, wf_deck_info *info);
 /* xyz[3 nn] interleaved, elnod[ne npe]; either may be null. */
 WF_API wf_status wf_deck_get_mesh(const wf_deck *k, double *xyz, int32_t *elnod);
-/* Die of a contact deck: xyz[3 die_nodes], tri[3 die_tris]; either may be null. */
+/* Rigid body 0 of a contact deck: xyz[3 die_nodes], tri[3 die_tris]; either may be null. */
 WF_API wf_status wf_deck_get_die(const wf_deck *k, double *xyz, int32_t *tri);
+/* Rigid body `body` (0 .. rigid_bodies-1): sizes, velocity, xyz[3 nnodes] and
+ * tri[3 ntris] (indices into the body's own nodes); any output may be null. */
+WF_API wf_status wf_deck_get_body(const wf_deck *k, int32_t body, int64_t *nnodes, int64_t *ntris,
+                                  double vel[3], double *xyz, int32_t *tri);
+/* Nastran bulk-data die mesh (NastranReader::read, NastranReader.cpp:34-180, and
+ * TriMesh_d(NastranReader&, ...), Mesh.C:560-760): GRID cards give the nodes
+ * (fixed 8-column fields: id in columns 8-15, x y z from column 24; a D
+ * exponent reads as E and a field without an exponent letter takes one before
+ * its first sign after the first column, "1.5-3" = 1.5E-3), CTRIA cards the
+ * triangles (node ids from column 24), each kind read as consecutive lines
+ * from its first card. flip_normals swaps every triangle's first two nodes;
+ * with orient_pt non-null, a triangle whose normal points away from the
+ * interior point C + 2 (C - P) (C the mean node, P = orient_pt) is turned too,
+ * so normals face P. Writes min(cap, count) nodes and triangles (either buffer
+ * may be null) and the counts. CBEAM/CBAR line meshes return
+ * WF_ERR_UNSUPPORTED. */
+WF_API wf_status wf_read_nastran(const char *path, int32_t flip_normals, const double *orient_pt,
+                                 double *xyz, int64_t cap_nodes, int32_t *tri, int64_t cap_tris,
+                                 int64_t *nnodes, int64_t *ntris, char *err, int64_t err_len);
 /* The n_bc AddBCVelNode calls in order; any array may be null. */
 WF_API wf_status wf_deck_get_bcs(const wf_deck *k, int64_t *node, int32_t *dim, double *val);
 /* Mesh, material, BCs (then AllocateBCs), options, dt and end time onto d. */

@@ -89,6 +89,7 @@ def lib():
         "wfo_get_energies": ([vp, _dp, _dp, i64], i64),
         "wfo_set_contact_trimesh": ([vp, i64, _dp, i64, _ip, _dp, C.c_double, C.c_double,
                                      C.c_double], None),
+        "wfo_add_contact_trimesh": ([vp, i64, _dp, i64, _ip, _dp], C.c_int),
         "wfo_get_trimesh_nodes": ([vp, _dp, i64], i64),
         "wfo_get_surface": ([vp, _u8, _dp, _dp], i64),
     }
@@ -232,6 +233,13 @@ class OracleDomain:
         lib().wfo_set_contact_trimesh(self.h, xyz.size // 3, xyz, tri.size // 3, tri,
                                       np.ascontiguousarray(vel, np.float64), float(mu_static),
                                       float(mu_dynamic), float(penalty_factor))
+
+    def add_contact_trimesh(self, xyz, tri, vel):
+        xyz = np.ascontiguousarray(xyz, np.float64).reshape(-1)
+        tri = np.ascontiguousarray(tri, np.int32).reshape(-1)
+        if lib().wfo_add_contact_trimesh(self.h, xyz.size // 3, xyz, tri.size // 3, tri,
+                                         np.ascontiguousarray(vel, np.float64)) != 0:
+            raise RuntimeError("add_contact_trimesh needs set_contact_trimesh first")
 
     def trimesh_nodes(self):
         n = lib().wfo_get_trimesh_nodes(self.h, np.zeros(3), 0)

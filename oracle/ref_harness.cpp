@@ -35,6 +35,9 @@
 #include "Domain_d.h"
 #include "Material.cuh"
 #include "Mesh.h"
+// NastranReader::read is an inline member defined in this source file, so it
+// is compiled here, where the harness constructs a reader.
+#include "NastranReader.cpp"
 
 #include <cmath>
 #include <cstdio>
@@ -70,43 +73,58 @@ class RefDomain : public Domain_d {
   double temp = 0.0;                        // uniform temperature T[]
   std::vector<double3> v_orig;              // its velocity before the ramp
 
-  // A TriMesh_d filled from arrays, one mesh (id 0), uniform velocity; normals,
-  // centroids and plane coefficients as the reference computes them.
-  void set_trimesh(int nn, const double *xyz, int ne, const int *tri, const double *vel,
-                   double mu_s, double mu_d, double pf) {
-    tm = new TriMesh_d();
-    tm->dimension = 3;
-    tm->nodecount = nn;
-    tm->elemcount = ne;
-    tm->mesh_count = 1;
-    malloc_t(tm->node, double3, nn);
-    malloc_t(tm->node_v, double3, nn);
-    malloc_t(tm->elnode, int, 3 * ne);
-    malloc_t(tm->centroid, double3, ne);
-    malloc_t(tm->normal, double3, ne);
-    malloc_t(tm->pplane, double, ne);
-    malloc_t(tm->nfar, int, ne);
-    malloc_t(tm->ele_mesh_id, int, ne);
-    malloc_t(tm->react_force, double3, 1);
-    malloc_t(tm->react_p_force, double, 1);
-    malloc_t(tm->mu_sta, double, 1);
-    malloc_t(tm->mu_dyn, double, 1);
+  // A TriMesh_d filled from arrays: one mesh with the given id, uniform
+  // velocity (node_v and m_v); normals, centroids and plane coefficients as
+  // the reference computes them.
+  static TriMesh_d *mesh_from_arrays(int nn, const double *xyz, int ne, const int *tri,
+                                     const double *vel, int id) {
+    TriMesh_d *m = new TriMesh_d();
+    m->dimension = 3;
+    m->nodecount = nn;
+    m->elemcount = ne;
+    m->mesh_count = 1;
+    malloc_t(m->node, double3, nn);
+    malloc_t(m->node_v, double3, nn);
+    malloc_t(m->elnode, int, 3 * ne);
+    malloc_t(m->centroid, double3, ne);
+    malloc_t(m->normal, double3, ne);
+    malloc_t(m->pplane, double, ne);
+    malloc_t(m->nfar, int, ne);
+    malloc_t(m->ele_mesh_id, int, ne);
+    malloc_t(m->react_force, double3, 1);
+    malloc_t(m->react_p_force, double, 1);
+    malloc_t(m->mu_sta, double, 1);
+    malloc_t(m->mu_dyn, double, 1);
     for (int n = 0; n < nn; n++) {
-      tm->node[n] = make_double3(xyz[3 * n], xyz[3 * n + 1], xyz[3 * n + 2]);
-      tm->node_v[n] = make_double3(vel[0], vel[1], vel[2]);
+      m->node[n] = make_double3(xyz[3 * n], xyz[3 * n + 1], xyz[3 * n + 2]);
+      m->node_v[n] = make_double3(vel[0], vel[1], vel[2]);
     }
     for (int e = 0; e < ne; e++) {
-      for (int k = 0; k < 3; k++) tm->elnode[3 * e + k] = tri[3 * e + k];
-      tm->ele_mesh_id[e] = 0;
+      for (int k = 0; k < 3; k++) m->elnode[3 * e + k] = tri[3 * e + k];
+      m->ele_mesh_id[e] = id;
     }
-    tm->react_force[0] = make_double3(0., 0., 0.);
+    m->m_v = make_double3(vel[0], vel[1], vel[2]);
+    m->react_force[0] = make_double3(0., 0., 0.);
+    m->heat_cond = 0.0;
+    m->CalcCentroids();
+    m->CalcNormals();
+    m->CalcSpheres();
+    return m;
+  }
+  void set_trimesh(int nn, const double *xyz, int ne, const int *tri, const double *vel,
+                   double mu_s, double mu_d, double pf) {
+    tm = mesh_from_arrays(nn, xyz, ne, tri, vel, 0);
     tm->mu_sta[0] = mu_s;
     tm->mu_dyn[0] = mu_d;
-    tm->heat_cond = 0.0;
-    tm->CalcCentroids();
-    tm->CalcNormals();
-    tm->CalcSpheres();
     setContactPF(pf);
+  }
+  // The driver's second rigid body (main.C:756-830): SetMeshVel, addMeshData
+  // (whose body is TriMesh_d::AddMesh, called here on the mesh that init
+  // attaches with setTriMesh), then CalcSpheres over the whole mesh.
+  void add_trimesh(int nn, const double *xyz, int ne, const int *tri, const double *vel) {
+    TriMesh_d *m = mesh_from_arrays(nn, xyz, ne, tri, vel, tm->mesh_count);
+    tm->AddMesh(*m);
+    tm->CalcSpheres();
   }
   long step_count = 0;
 
@@ -582,6 +600,29 @@ int wfr_get_reaction(void *h, double *out, int maxn) {
 void wfr_set_trimesh(void *h, int nn, const double *xyz, int ne, const int *tri,
                      const double *vel, double mu_s, double mu_d, double pf) {
   static_cast<RefDomain *>(h)->set_trimesh(nn, xyz, ne, tri, vel, mu_s, mu_d, pf);
+}
+void wfr_add_trimesh(void *h, int nn, const double *xyz, int ne, const int *tri,
+                     const double *vel) {
+  static_cast<RefDomain *>(h)->add_trimesh(nn, xyz, ne, tri, vel);
+}
+// The reference's Nastran die: NastranReader(path) and
+// TriMesh_d(reader, flipnormals, orientNormals, orient_pt) (Mesh.C:560-760).
+// Writes up to cap nodes and triangles; returns the node count, *ntri the
+// triangle count.
+int wfr_nastran_trimesh(const char *path, int flip, int orient, const double *pt, double *xyz,
+                        int cap_nodes, int *tri, int cap_tris, int *ntri) {
+  NastranReader reader(path);
+  const double3 op = make_double3(pt[0], pt[1], pt[2]);
+  TriMesh_d m(reader, flip != 0, orient != 0, op);
+  for (int n = 0; n < m.nodecount && n < cap_nodes; n++) {
+    xyz[3 * n] = m.node[n].x;
+    xyz[3 * n + 1] = m.node[n].y;
+    xyz[3 * n + 2] = m.node[n].z;
+  }
+  for (int e = 0; e < m.elemcount && e < cap_tris; e++)
+    for (int k = 0; k < 3; k++) tri[3 * e + k] = m.elnode[3 * e + k];
+  *ntri = m.elemcount;
+  return m.nodecount;
 }
 int wfr_get_trimesh_nodes(void *h, double *out, int cap) {
   RefDomain *d = static_cast<RefDomain *>(h);

@@ -70,6 +70,9 @@ def lib():
         "wfr_get_energies": ([vp, _dp, _dp, C.c_int], C.c_int),
         "wfr_set_trimesh": ([vp, C.c_int, _dp, C.c_int, _ip, _dp, C.c_double, C.c_double,
                              C.c_double], None),
+        "wfr_add_trimesh": ([vp, C.c_int, _dp, C.c_int, _ip, _dp], None),
+        "wfr_nastran_trimesh": ([C.c_char_p, C.c_int, C.c_int, _dp, _dp, C.c_int, _ip, C.c_int,
+                                 C.POINTER(C.c_int)], C.c_int),
         "wfr_get_trimesh_nodes": ([vp, _dp, C.c_int], C.c_int),
         "wfr_get_surface": ([vp, _u8, _dp, _dp], C.c_int),
         "wfr_get_contforce": ([vp, _dp], C.c_int),
@@ -105,6 +108,21 @@ NODE_VEC = {"x": 0, "v": 1, "a": 2, "u": 3, "prev_a": 4, "fi": 5, "u_dt": 6}
 NODE_SCALAR = {"mass": 0, "voln": 1, "p_node": 2}
 ELEM_SCALAR = {"vol": 0, "vol0": 1, "detJ": 2, "p": 3, "pl_strain": 4, "sigma_y": 5, "rho": 6}
 ELEM_TENSOR = {"sigma": 0, "tau": 1, "eps": 2, "str_rate": 3, "rot_rate": 4}
+
+
+def nastran_trimesh(path, flip_normals=False, orient_point=None):
+    """The reference's Nastran die (NastranReader + TriMesh_d constructor):
+    (xyz[n, 3], tri[m, 3]); orient_point None disables orientNormals."""
+    pt = np.zeros(3) if orient_point is None else np.asarray(orient_point, np.float64)
+    nt = C.c_int()
+    args = (os.fsencode(path), int(bool(flip_normals)), int(orient_point is not None), pt)
+    with _Silence():
+        nn = lib().wfr_nastran_trimesh(*args, np.zeros(3), 0, np.zeros(3, np.int32), 0,
+                                       C.byref(nt))
+        x = np.zeros(3 * max(nn, 1))
+        t = np.zeros(3 * max(nt.value, 1), np.int32)
+        lib().wfr_nastran_trimesh(*args, x, nn, t, nt.value, C.byref(nt))
+    return x[: 3 * nn].reshape(-1, 3), t[: 3 * nt.value].reshape(-1, 3)
 
 
 class RefDomain:
@@ -216,6 +234,13 @@ class RefDomain:
         lib().wfr_set_trimesh(self.h, xyz.size // 3, xyz, tri.size // 3, tri,
                               np.ascontiguousarray(vel, np.float64), float(mu_static),
                               float(mu_dynamic), float(penalty_factor))
+
+    def add_contact_trimesh(self, xyz, tri, vel):
+        xyz = np.ascontiguousarray(xyz, np.float64).reshape(-1)
+        tri = np.ascontiguousarray(tri, np.int32).reshape(-1)
+        with _Silence():
+            lib().wfr_add_trimesh(self.h, xyz.size // 3, xyz, tri.size // 3, tri,
+                                  np.ascontiguousarray(vel, np.float64))
 
     def trimesh_nodes(self):
         n = lib().wfr_get_trimesh_nodes(self.h, np.zeros(3), 0)

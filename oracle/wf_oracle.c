@@ -9,6 +9,7 @@
 #include "wf_oracle.h"
 
 #include <math.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 #ifdef _OPENMP
@@ -64,7 +65,8 @@ struct wfo_domain {
   int tri_on;
   int64_t tri_nn, tri_ne;
   double *tri_x, *tri_vorig, *tri_nrm, *tri_pp;
-  int32_t *tri_el;
+  int32_t *tri_el, *tri_mid; /* tri_mid: rigid-body index of each triangle */
+  int32_t tri_meshes;
   double tri_mu_s, tri_mu_d, tri_pf;
   uint8_t *ext;
   double *node_area, *nodlen, *elem_len;
@@ -116,9 +118,11 @@ static void free_trimesh(wfo_domain *d) {
   free(d->tri_nrm);
   free(d->tri_pp);
   free(d->tri_el);
+  free(d->tri_mid);
   d->tri_x = d->tri_vorig = d->tri_nrm = d->tri_pp = NULL;
-  d->tri_el = NULL;
+  d->tri_el = d->tri_mid = NULL;
   d->tri_on = 0;
+  d->tri_meshes = 0;
 }
 
 void wfo_destroy(wfo_domain *d) {
@@ -412,6 +416,8 @@ void wfo_set_contact_trimesh(wfo_domain *d, int64_t nnodes, const double *xyz, i
   d->tri_nrm = xcalloc(3 * ntri, 8);
   d->tri_pp = xcalloc(ntri, 8);
   d->tri_el = xcalloc(3 * ntri, 4);
+  d->tri_mid = xcalloc(ntri, 4);
+  d->tri_meshes = 1;
   memcpy(d->tri_x, xyz, sizeof(double) * 3 * nnodes);
   memcpy(d->tri_el, tri, sizeof(int32_t) * 3 * ntri);
   for (int64_t n = 0; n < nnodes; n++)
@@ -420,6 +426,36 @@ void wfo_set_contact_trimesh(wfo_domain *d, int64_t nnodes, const double *xyz, i
   d->tri_mu_d = mu_dynamic;
   d->tri_pf = penalty_factor;
   tri_normals_planes(d);
+}
+
+/* TriMesh_d::AddMesh (Mesh.C:445-545): the body's nodes and triangles are
+ * appended, triangle node indices offset by the node count so far; its nodes
+ * take its velocity, its triangles the next mesh index. */
+int wfo_add_contact_trimesh(wfo_domain *d, int64_t nnodes, const double *xyz, int64_t ntri,
+                            const int32_t *tri, const double vel[3]) {
+  if (!d->tri_on) return -1;
+  const int64_t nn0 = d->tri_nn, ne0 = d->tri_ne;
+  const int64_t nn = nn0 + nnodes, ne = ne0 + ntri;
+  d->tri_x = realloc(d->tri_x, sizeof(double) * 3 * nn);
+  d->tri_vorig = realloc(d->tri_vorig, sizeof(double) * 3 * nn);
+  d->tri_nrm = realloc(d->tri_nrm, sizeof(double) * 3 * ne);
+  d->tri_pp = realloc(d->tri_pp, sizeof(double) * ne);
+  d->tri_el = realloc(d->tri_el, sizeof(int32_t) * 3 * ne);
+  d->tri_mid = realloc(d->tri_mid, sizeof(int32_t) * ne);
+  if (!d->tri_x || !d->tri_vorig || !d->tri_nrm || !d->tri_pp || !d->tri_el || !d->tri_mid) {
+    fprintf(stderr, "wf_oracle: out of memory\n");
+    abort();
+  }
+  memcpy(&d->tri_x[3 * nn0], xyz, sizeof(double) * 3 * nnodes);
+  for (int64_t n = 0; n < nnodes; n++)
+    for (int k = 0; k < 3; k++) d->tri_vorig[3 * (nn0 + n) + k] = vel[k];
+  for (int64_t i = 0; i < 3 * ntri; i++) d->tri_el[3 * ne0 + i] = (int32_t)(tri[i] + nn0);
+  for (int64_t e = 0; e < ntri; e++) d->tri_mid[ne0 + e] = d->tri_meshes;
+  d->tri_meshes++;
+  d->tri_nn = nn;
+  d->tri_ne = ne;
+  tri_normals_planes(d);
+  return 0;
 }
 
 int64_t wfo_get_trimesh_nodes(const wfo_domain *d, double *out, int64_t cap) {
@@ -1231,7 +1267,7 @@ static void tri_setup_surface(wfo_domain *d) {
  * force, and Coulomb friction from the accumulated tangential slip (static
  * cap, then dynamic force along -v_t). As in the reference, a node that leaves
  * contact keeps its last contact force. The reaction is the sum of normal-force
- * magnitudes of the nodes in contact. */
+ * magnitudes of the nodes in contact with rigid body 0. */
 static void calc_contact_trimesh(wfo_domain *d) {
   const double dt = d->dt;
   const double E0 = d->mats[0].E;
@@ -1272,7 +1308,8 @@ static void calc_contact_trimesh(wfo_domain *d) {
       cf[0] = nr[0] * s;
       cf[1] = nr[1] * s;
       cf[2] = nr[2] * s;
-      d->cfn[i] = sqrt(cf[0] * cf[0] + cf[1] * cf[1] + cf[2] * cf[2]);
+      /* only contacts with rigid body 0 feed the reaction (Contact.C:326-329) */
+      if (d->tri_mid[j] == 0) d->cfn[i] = sqrt(cf[0] * cf[0] + cf[1] * cf[1] + cf[2] * cf[2]);
       /* friction */
       const double vn = v[0] * nr[0] + v[1] * nr[1] + v[2] * nr[2];
       const double vt[3] = {v[0] - nr[0] * vn, v[1] - nr[1] * vn, v[2] - nr[2] * vn};

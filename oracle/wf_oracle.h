@@ -93,6 +93,10 @@ int64_t wfo_get_reaction(const wfo_domain *d, double *out, int64_t cap);
 void wfo_set_contact_trimesh(wfo_domain *d, int64_t nnodes, const double *xyz, int64_t ntri,
                              const int32_t *tri, const double vel[3], double mu_static,
                              double mu_dynamic, double penalty_factor);
+/* Appends rigid body 1, 2, ... (TriMesh_d::AddMesh); only contacts with body 0
+ * feed the reaction. Returns -1 without a first body. */
+int wfo_add_contact_trimesh(wfo_domain *d, int64_t nnodes, const double *xyz, int64_t ntri,
+                            const int32_t *tri, const double vel[3]);
 int64_t wfo_get_trimesh_nodes(const wfo_domain *d, double *out, int64_t cap_nodes);
 int64_t wfo_get_surface(const wfo_domain *d, uint8_t *ext, double *node_area, double *nodlen);
 /* Kinetic energy and accumulated internal energy after each step

@@ -37,6 +37,12 @@ DIE = dict(start=[-0.001, -0.001, 0.002 - 1e-5], end=[0.004, 0.004, 0.0], dens=2
            vel=[0.0, 0.0, -5.0], mu_s=0.1, mu_d=0.08, pf=0.1, end_t=2e-6)
 
 
+# a second, fixed-velocity body: a plane 1e-5 above the bottom face (z = 0),
+# normal +z, moving up at 2 m/s; the part keeps only its x/y symmetry planes
+DIE_BOTTOM = dict(start=[-0.001, -0.001, 1e-5], end=[0.004, 0.004, 0.0], dens=3, flip=False,
+                  vel=[0.0, 0.0, 2.0])
+
+
 def cases():
     """(name, Case, steps, mode, extra) with mode 'step' (harness loop) or 'verbatim'."""
     out = []
@@ -80,6 +86,13 @@ def cases():
     c.perturb = 0.1
     c.bc = "bottom_z"
     out.append(("tet_die_trimesh", c, 300, "step", dict(linear=True, die=DIE)))
+    # two rigid bodies (TriMesh_d::AddMesh): only the contacts with body 0
+    # (the top die) feed the reaction
+    c = W.config(1, scale=(3, 3, 4))
+    c.perturb = 0.1
+    c.seed = W.SEED_BASE + 13
+    c.bc = "sym_xy"
+    out.append(("tet_two_dies", c, 300, "step", dict(linear=True, die=DIE, die2=DIE_BOTTOM)))
     # Johnson-Cook through Material_::Init_JohnsonCook and the reference's own
     # CalcStressStrain (hexahedra: the reference reads the temperature T[e] of a
     # node-sized array by element index)
@@ -108,6 +121,10 @@ def run_case(name, case, steps, mode, extra):
         xyz, tri = W.axis_plane_mesh(die["start"], die["end"], die["dens"], die["flip"])
         d.set_contact_trimesh(xyz, tri, die["vel"], die["mu_s"], die["mu_d"], die["pf"])
         d.set_end_time(die["end_t"])
+    if "die2" in extra:
+        b = extra["die2"]
+        xyz, tri = W.axis_plane_mesh(b["start"], b["end"], b["dens"], b["flip"])
+        d.add_contact_trimesh(xyz, tri, b["vel"])
     if mode == "verbatim":
         d.set_end_time(steps * dt)
         with tempfile.TemporaryDirectory() as td:

@@ -47,6 +47,10 @@ def setup(dom, case, extra=None):
         xyz, tri = W.axis_plane_mesh(die["start"], die["end"], die["dens"], die["flip"])
         dom.set_contact_trimesh(xyz, tri, die["vel"], die["mu_s"], die["mu_d"], die["pf"])
         dom.set_end_time(die["end_t"])
+    if "die2" in extra:
+        b = extra["die2"]
+        xyz, tri = W.axis_plane_mesh(b["start"], b["end"], b["dens"], b["flip"])
+        dom.add_contact_trimesh(xyz, tri, b["vel"])
     return dt
 
 

@@ -159,8 +159,10 @@ def test_deck_errors(tmp_path):
     cases = [
         (dict(Configuration={"thermal": True}), 5),
         (dict(Configuration={"domType": "AxiSymm"}), 5),
-        (dict(RigidBodies=[{"type": "File", "fileName": "die.nas"}]), 5),
-        (dict(RigidBodies=[{"type": "Plane"}, {"type": "Plane"}]), 5),
+        (dict(RigidBodies=[{"type": "File", "fileName": "missing.nas"}]), 1),
+        (dict(RigidBodies=[{"type": "Line", "dim": [1.0, 0.0, 0.0]}]), 5),
+        (dict(RigidBodies=[{"type": "Plane"}, {"type": "Sphere"}]), 5),
+        (dict(RigidBodies=[{"zoneId": 1}, {"type": "Plane"}]), 1),
         (dict(Materials=[dict(STEEL, type="GMT")]), 5),
         (dict(DomainBlocks=[{"type": "File", "fileName": "missing.k"}]), 1),
         (dict(BoundaryConditions=[{"zoneId": 3, "value": [0, 0, 1.0]}]), 1),

@@ -48,6 +48,12 @@ def test_axis_plane_mesh_orientation():
     assert np.all(n2[:, 2] > 0)
 
 
+def test_add_body_needs_a_first_body():
+    o = O.OracleDomain()
+    with pytest.raises(RuntimeError):
+        o.add_contact_trimesh(np.zeros((3, 3)), np.array([[0, 1, 2]]), [0.0, 0.0, 0.0])
+
+
 def test_oracle_die_pushes_the_part():
     case, die, steps = cases()["hex_hg"]
     o = run(O.OracleDomain(), case, die, steps)
@@ -71,6 +77,39 @@ def test_trimesh_contact_matches_oracle(name):
     assert H.rel_err(d.reaction(), o.reaction()) <= 1e-9
     np.testing.assert_allclose(d.trimesh_nodes(), o.trimesh_nodes(), rtol=1e-12, atol=0)
     assert o.reaction().max() > 0
+
+
+DIE_BOTTOM = dict(start=[-0.001, -0.001, 1e-5], end=[0.004, 0.004, 0.0], dens=3, flip=False,
+                  vel=[0.0, 0.0, 2.0])
+
+
+@pytest.mark.gpu
+def test_two_rigid_bodies_match_oracle():
+    """Top die (body 0) and a rising bottom plate (body 1, wf_add_contact_trimesh)
+    squeezing a block held only by x/y symmetry planes: only the top die's
+    contacts feed the reaction."""
+    case = W.config(1, scale=(3, 3, 4))
+    case.perturb = 0.1
+    case.seed = W.SEED_BASE + 13
+    case.bc = "sym_xy"
+    extra = {"die": DIE_TET, "die2": DIE_BOTTOM}
+    steps = 300
+    o = O.OracleDomain()
+    H.setup(o, case, extra)
+    o.init()
+    o.step(steps)
+    d = wf.Domain(wf.WF_FP64)
+    H.setup(d, case, extra)
+    d.init()
+    d.run(steps)
+    assert H.rel_err(d.node_vec("u"), o.node_vec("u")) <= 1e-9
+    cf = d.node_vec("contforce")
+    assert H.rel_err(cf, o.node_vec("contforce")) <= 1e-9
+    assert H.rel_err(d.reaction(), o.reaction()) <= 1e-9
+    np.testing.assert_allclose(d.trimesh_nodes(), o.trimesh_nodes(), rtol=1e-12, atol=0)
+    x0 = case.coords()
+    assert cf[x0[:, 2] < 1e-12, 2].max() > 0      # the plate pushes up
+    assert d.trimesh_nodes().shape == (9 + 16, 3)
 
 
 @pytest.mark.gpu

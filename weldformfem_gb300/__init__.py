@@ -20,6 +20,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_lib", "libwf_gb300.so")
 
 WF_FP64, WF_MIXED = 0, 1
+# wf_status codes (include/wf.h)
+WF_OK, WF_ERR_ARG, WF_ERR_STATE, WF_ERR_CUDA, WF_ERR_NOMEM = 0, 1, 2, 3, 4
+WF_ERR_UNSUPPORTED, WF_ERR_NONFINITE, WF_ERR_TIMEOUT = 5, 6, 7
 STATUS = {0: "ok", 1: "invalid argument", 2: "call out of order", 3: "CUDA error",
           4: "out of memory", 5: "unsupported option", 6: "non-finite state",
           7: "device wait timed out"}
@@ -58,7 +61,7 @@ class WfDeckInfo(C.Structure):
                 ("material", WfMaterial), ("contact", C.c_int32), ("die_nodes", C.c_int32),
                 ("die_tris", C.c_int32), ("die_vel", C.c_double * 3), ("mu_static", C.c_double),
                 ("mu_dynamic", C.c_double), ("penalty_factor", C.c_double),
-                ("johnson_cook", C.c_double * 8)]
+                ("johnson_cook", C.c_double * 8), ("rigid_bodies", C.c_int32)]
 
 
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
@@ -122,6 +125,9 @@ _SIGS = {
                              C.POINTER(C.c_double)],
     "wf_get_transfer_bytes": [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)],
     "wf_set_launch_config": [C.c_void_p, C.c_int32, C.c_int32, C.c_int32],
+    "wf_set_step_mode": [C.c_void_p, C.c_int32],
+    "wf_get_step_mode": [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                         C.POINTER(C.c_int32)],
     "wf_adjoint_forward": [C.c_void_p, C.c_int64, C.c_int64],
     "wf_deck_read": [C.c_char_p, C.POINTER(C.c_void_p), C.c_char_p, C.c_int64],
     "wf_deck_free": [C.c_void_p],
@@ -136,6 +142,12 @@ _SIGS = {
     "wf_set_contact_trimesh": [C.c_void_p, C.c_int64, _dp, C.c_int64, _ip, _dp, C.c_double,
                                C.c_double, C.c_double],
     "wf_get_trimesh_nodes": [C.c_void_p, _dp, C.c_int64, C.POINTER(C.c_int64)],
+    "wf_add_contact_trimesh": [C.c_void_p, C.c_int64, _dp, C.c_int64, _ip, _dp],
+    "wf_deck_get_body": [C.c_void_p, C.c_int32, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                         C.POINTER(C.c_double), C.c_void_p, C.c_void_p],
+    "wf_read_nastran": [C.c_char_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p,
+                        C.c_int64, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.c_char_p,
+                        C.c_int64],
     "wf_set_energy_history": [C.c_void_p, C.c_int32],
     "wf_set_johnson_cook": [C.c_void_p, C.c_int32] + [C.c_double] * 8,
     "wf_get_energy_history": [C.c_void_p, _dp, _dp, C.c_int64, C.POINTER(C.c_int64)],
@@ -383,6 +395,16 @@ class Domain:
     def set_autotune(self, on=True):
         self._call("wf_set_autotune", int(bool(on)))
 
+    def set_step_mode(self, mode):
+        """0 automatic, 1 per-phase kernels (graph), 2 one cluster launch per run."""
+        self._call("wf_set_step_mode", int(mode))
+
+    def step_mode(self):
+        """(mode the next run uses, cluster blocks, block size)."""
+        m, b, t = C.c_int32(), C.c_int32(), C.c_int32()
+        self._call("wf_get_step_mode", C.byref(m), C.byref(b), C.byref(t))
+        return m.value, b.value, t.value
+
     def set_launch_config(self, phase, block, items_per_thread):
         """Launch shape of phase 0/1/2 (items_per_thread 0: persistent grid)."""
         self._call("wf_set_launch_config", int(phase), int(block), int(items_per_thread))
@@ -439,6 +461,13 @@ class Domain:
                    np.ascontiguousarray(vel, np.float64), float(mu_static), float(mu_dynamic),
                    float(penalty_factor))
 
+    def add_contact_trimesh(self, xyz, tri, vel):
+        """Another rigid body (TriMesh_d::AddMesh); only body 0 feeds the reaction."""
+        xyz = np.ascontiguousarray(xyz, np.float64).reshape(-1)
+        tri = np.ascontiguousarray(tri, np.int32).reshape(-1)
+        self._call("wf_add_contact_trimesh", xyz.size // 3, xyz, tri.size // 3, tri,
+                   np.ascontiguousarray(vel, np.float64))
+
     def trimesh_nodes(self):
         n = C.c_int64()
         self._call("wf_get_trimesh_nodes", np.zeros(3), 0, C.byref(n))
@@ -479,6 +508,26 @@ class Domain:
         out = np.zeros(max(n.value, 1))
         self._call("wf_get_reaction_history", out, n.value, C.byref(n))
         return out[: n.value]
+
+
+def read_nastran(path, flip_normals=False, orient_point=None):
+    """Nastran die mesh (wf_read_nastran): (xyz[n, 3], tri[m, 3]) with the
+    reference's flipnormals and orientNormals rules (orient_point None: no
+    orientation)."""
+    nn, nt = C.c_int64(), C.c_int64()
+    err = C.create_string_buffer(512)
+    pt = None if orient_point is None else (C.c_double * 3)(*[float(v) for v in orient_point])
+    args = (os.fsencode(path), int(bool(flip_normals)), pt)
+    st = lib().wf_read_nastran(*args, None, 0, None, 0, C.byref(nn), C.byref(nt), err, 512)
+    if st != 0:
+        raise WfError(st, err.value.decode())
+    x = np.zeros(3 * nn.value)
+    t = np.zeros(3 * nt.value, np.int32)
+    st = lib().wf_read_nastran(*args, x.ctypes.data, nn.value, t.ctypes.data, nt.value,
+                               C.byref(nn), C.byref(nt), err, 512)
+    if st != 0:
+        raise WfError(st, err.value.decode())
+    return x.reshape(-1, 3), t.reshape(-1, 3)
 
 
 class Deck:
@@ -533,8 +582,21 @@ class Deck:
         lib().wf_deck_get_bcs(self.h, node, dim, val)
         return node[:n], dim[:n], val[:n]
 
+    def body(self, b):
+        """(xyz[n, 3], tri[m, 3], vel[3]) of rigid body b of a contact deck."""
+        nn, nt = C.c_int64(), C.c_int64()
+        vel = (C.c_double * 3)()
+        st = lib().wf_deck_get_body(self.h, int(b), C.byref(nn), C.byref(nt), vel, None, None)
+        if st != 0:
+            raise WfError(st, f"no rigid body {b}")
+        x = np.zeros(3 * max(nn.value, 1))
+        t = np.zeros(3 * max(nt.value, 1), np.int32)
+        lib().wf_deck_get_body(self.h, int(b), None, None, None, x.ctypes.data, t.ctypes.data)
+        return (x[: 3 * nn.value].reshape(-1, 3), t[: 3 * nt.value].reshape(-1, 3),
+                np.array(vel[:]))
+
     def die(self):
-        """(xyz[n, 3], tri[m, 3]) of a contact deck's die."""
+        """(xyz[n, 3], tri[m, 3]) of a contact deck's die (rigid body 0)."""
         x = np.zeros(3 * max(self.info["die_nodes"], 1))
         t = np.zeros(3 * max(self.info["die_tris"], 1), np.int32)
         lib().wf_deck_get_die(self.h, x, t)
@@ -566,5 +628,7 @@ class Deck:
             xyz, tri = self.die()
             dom.set_contact_trimesh(xyz, tri, i["die_vel"], i["mu_static"], i["mu_dynamic"],
                                     i["penalty_factor"])
+            for b in range(1, i["rigid_bodies"]):
+                dom.add_contact_trimesh(*self.body(b))
         dom.set_dt(i["dt"])
         dom.set_end_time(i["end_time"])

@@ -7,6 +7,7 @@
 #include <array>
 #include <cmath>
 #include <cstdarg>
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -125,7 +126,9 @@ struct wf_domain {
   bool tri = false;
   std::vector<double> tri_x;
   std::vector<int32_t> tri_el;
-  double tri_vel[3] = {0, 0, 0};
+  std::vector<double> tri_v;      // [3 per node] velocity before the start-up ramp
+  std::vector<int32_t> tri_mid;   // [per triangle] rigid-body (mesh) index
+  int32_t tri_meshes = 0;
   double tri_mu_s = 0.0, tri_mu_d = 0.0, tri_pf = 0.1;
   // device
   bool initialized = false;
@@ -155,6 +158,10 @@ struct wf_domain {
   bool autotune = true;
   LaunchCfg cfg[3] = {LaunchCfg{128, 1}, LaunchCfg{256, 1}, LaunchCfg{128, 1}};
   double cfg_ms[3] = {0, 0, 0};
+  // step scheduling (mixed): 0 automatic, 1 per-phase kernels, 2 one cluster
+  // launch per run; the cluster shape is found at init for small meshes
+  int32_t step_mode = 0;
+  int cl_blocks = 0, cl_bs = 0;
   // batched ensemble
   int32_t nspec = 0;
   std::vector<int64_t> spec_eoff, spec_noff;
@@ -385,6 +392,9 @@ void reset_mesh(wf_domain *d) {
   d->tri = false;
   d->tri_x.clear();
   d->tri_el.clear();
+  d->tri_v.clear();
+  d->tri_mid.clear();
+  d->tri_meshes = 0;
   d->bcs_allocated = false;
   d->nspec = 0;
   d->spec_eoff.clear();
@@ -767,11 +777,38 @@ WF_API wf_status wf_set_contact_trimesh(wf_domain *d, int64_t nnodes, const doub
   d->tri = true;
   d->tri_x.assign(xyz, xyz + 3 * nnodes);
   d->tri_el.assign(tri, tri + 3 * ntri);
-  for (int k = 0; k < 3; k++) d->tri_vel[k] = vel[k];
+  d->tri_v.resize(3 * nnodes);
+  for (int64_t i = 0; i < 3 * nnodes; i++) d->tri_v[i] = vel[i % 3];
+  d->tri_mid.assign(ntri, 0);
+  d->tri_meshes = 1;
   d->tri_mu_s = mu_static;
   d->tri_mu_d = mu_dynamic;
   d->tri_pf = penalty_factor;
   d->contact = true;
+  return WF_OK;
+}
+
+// TriMesh_d::AddMesh (Mesh.C:445-545): the new body's nodes and triangles are
+// appended (triangle node indices offset by the current node count), its nodes
+// take its velocity and its triangles its mesh index.
+WF_API wf_status wf_add_contact_trimesh(wf_domain *d, int64_t nnodes, const double *xyz,
+                                        int64_t ntri, const int32_t *tri, const double vel[3]) {
+  wf_status s = need_mesh(d);
+  if (s) return s;
+  if (!xyz || !tri || !vel || nnodes < 3 || ntri < 1) return WF_ERR_ARG;
+  if (d->initialized) return fail(d, WF_ERR_STATE, "the contact mesh is set before init");
+  if (!d->tri) return fail(d, WF_ERR_STATE, "wf_set_contact_trimesh sets the first rigid body");
+  const int64_t base = (int64_t)d->tri_x.size() / 3;
+  if (base + nnodes > INT32_MAX || (int64_t)d->tri_mid.size() + ntri > INT32_MAX)
+    return fail(d, WF_ERR_ARG, "contact mesh too large");
+  for (int64_t i = 0; i < 3 * ntri; i++)
+    if (tri[i] < 0 || tri[i] >= nnodes)
+      return fail(d, WF_ERR_ARG, "triangle %lld references node %d", (long long)(i / 3), tri[i]);
+  d->tri_x.insert(d->tri_x.end(), xyz, xyz + 3 * nnodes);
+  for (int64_t i = 0; i < 3 * ntri; i++) d->tri_el.push_back((int32_t)(tri[i] + base));
+  for (int64_t i = 0; i < 3 * nnodes; i++) d->tri_v.push_back(vel[i % 3]);
+  d->tri_mid.insert(d->tri_mid.end(), ntri, d->tri_meshes);
+  d->tri_meshes++;
   return WF_OK;
 }
 
@@ -976,6 +1013,37 @@ WF_API wf_status wf_set_launch_config(wf_domain *d, int32_t phase, int32_t block
   return WF_OK;
 }
 
+// Meshes up to kClusterMaxElems elements get a cluster shape at init (the
+// cluster run can then be chosen by hand); up to kClusterAutoElems the
+// automatic mode uses it.
+constexpr int64_t kClusterMaxElems = 65536;
+constexpr int64_t kClusterAutoElems = 8192;
+
+namespace {
+// Whether the next wf_run of d runs as one cluster launch.
+bool cluster_mode(const wf_domain *d) {
+  if (d->precision != WF_MIXED || d->nspec || d->P.energy_on || d->phase_timing || !d->cl_blocks)
+    return false;
+  return d->step_mode == 2 || (d->step_mode == 0 && d->ne <= kClusterAutoElems);
+}
+}  // namespace
+
+WF_API wf_status wf_set_step_mode(wf_domain *d, int32_t mode) {
+  if (!d || mode < 0 || mode > 2) return WF_ERR_ARG;
+  d->step_mode = mode;
+  return WF_OK;
+}
+
+WF_API wf_status wf_get_step_mode(const wf_domain *d, int32_t *mode, int32_t *blocks,
+                                  int32_t *block_size) {
+  if (!d) return WF_ERR_ARG;
+  const bool c = d->initialized && cluster_mode(d);
+  if (mode) *mode = c ? 2 : 1;
+  if (blocks) *blocks = c ? d->cl_blocks : 0;
+  if (block_size) *block_size = c ? d->cl_bs : 0;
+  return WF_OK;
+}
+
 WF_API wf_status wf_get_launch_config(const wf_domain *d, int32_t phase, int32_t *block,
                                       int32_t *items_per_thread, double *ms) {
   if (!d || phase < 0 || phase > 2) return WF_ERR_ARG;
@@ -1073,13 +1141,12 @@ WF_API wf_status wf_init(wf_domain *d) {
     for (int64_t n = 0; n < nn; n++)
       if (ext[n]) flags[n] |= NF_CONTACT;
     tri_normals_planes(d->tri_x, d->tri_el, nrm, pp);
-    std::vector<double> tv(d->tri_x.size());
-    for (size_t i = 0; i < tv.size(); i++) tv[i] = d->tri_vel[i % 3];
     double *tx = nullptr, *tvd = nullptr, *tn = nullptr, *tp = nullptr, *na = nullptr,
            *nl = nullptr;
-    int32_t *te = nullptr;
+    int32_t *te = nullptr, *tm = nullptr;
     CUDA_TRY(upload(d, &tx, d->tri_x));
-    CUDA_TRY(upload(d, &tvd, tv));
+    CUDA_TRY(upload(d, &tvd, d->tri_v));
+    CUDA_TRY(upload(d, &tm, d->tri_mid));
     CUDA_TRY(upload(d, &tn, nrm));
     CUDA_TRY(upload(d, &tp, pp));
     CUDA_TRY(upload(d, &te, d->tri_el));
@@ -1093,6 +1160,7 @@ WF_API wf_status wf_init(wf_domain *d) {
     P.tri_nrm = tn;
     P.tri_pp = tp;
     P.tri_el = te;
+    P.tri_mid = tm;
     P.node_area = na;
     P.nodlen = nl;
     P.tri_mu_s = d->tri_mu_s;
@@ -1184,7 +1252,7 @@ WF_API wf_status wf_init(wf_domain *d) {
   }
   // reaction history and step state
   d->node_grid = (d->precision == WF_MIXED) ? mix_node_grid(nn) : fp64_node_grid(nn);
-  CUDA_TRY(dalloc(d, &P.partials, d->node_grid));
+  CUDA_TRY(dalloc(d, &P.partials, std::max(d->node_grid, 32)));
   d->hist_cap = 1 << 16;
   CUDA_TRY(dalloc(d, &P.hist, d->hist_cap));
   if (d->nspec) CUDA_TRY(dalloc(d, &P.hist_spec, (size_t)d->hist_cap * d->nspec));
@@ -1305,6 +1373,21 @@ WF_API wf_status wf_init(wf_domain *d) {
     if (d->autotune) {
       wf_status ts = autotune_launches(d);
       if (ts) return ts;
+    }
+    d->cl_blocks = d->cl_bs = 0;
+    if (d->ne <= kClusterMaxElems && !d->nspec) {
+      // the largest cluster (16 blocks needs the non-portable size) that
+      // can be resident, at most one block per 32 elements
+      for (int blocks : {16, 8, 4, 2, 1}) {
+        if (blocks > 1 && (int64_t)blocks * 32 > d->ne) continue;
+        const int64_t per = std::max((d->ne + blocks - 1) / blocks, (d->nn + blocks - 1) / blocks);
+        const int bs = per <= 64 ? 64 : (per <= 128 ? 128 : 256);
+        if (mix_cluster_fits(P, M, d->mvol, blocks, bs) >= 1) {
+          d->cl_blocks = blocks;
+          d->cl_bs = bs;
+          break;
+        }
+      }
     }
   }
   CUDA_TRY(cudaStreamSynchronize(d->stream));
@@ -1487,7 +1570,20 @@ WF_API wf_status wf_run(wf_domain *d, int64_t nsteps) {
     }
     left = 0;
   }
-  d->launches += (4 + (d->nspec ? 1 : 0) + (d->P.energy_on ? 1 : 0)) * nsteps;
+  if (d->step_mode == 2 && !cluster_mode(d))
+    return fail(d, WF_ERR_UNSUPPORTED,
+                "the cluster run needs mixed precision, a mesh of at most %lld elements, and no "
+                "specimens, energy history or phase timing", (long long)kClusterMaxElems);
+  if (cluster_mode(d)) {
+    // one launch per chunk of steps (kernels stay short)
+    while (left > 0) {
+      const int64_t chunk = std::min<int64_t>(left, 4096);
+      CUDA_TRY(mix_cluster_run(d->P, d->M, d->mvol, chunk, d->cl_blocks, d->cl_bs, d->stream));
+      d->launches += 1;
+      left -= chunk;
+    }
+  }
+  d->launches += (4 + (d->nspec ? 1 : 0) + (d->P.energy_on ? 1 : 0)) * left;
   if (left >= kGraphSteps) {
     wf_status s = ensure_graph(d);
     if (s) return s;

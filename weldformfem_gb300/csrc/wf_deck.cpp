@@ -5,6 +5,7 @@
 //    time step) that can be inspected and then applied to a domain;
 //  * LS-DYNA keyword meshes, *NODE and *ELEMENT_SOLID
 //    (Domain_d::CreateFromLSDyna, Domain_d.C:1647-1699);
+//  * Nastran GRID/CTRIA die meshes (NastranReader.cpp, Mesh.C:560-760);
 //  * legacy VTK output (VTKWriter.C) of a domain's current state.
 // Everything reaches the domain through the public wf_* entry points.
 #include <algorithm>
@@ -15,6 +16,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
+#include <map>
 #include <sstream>
 #include <string>
 #include <unordered_map>
@@ -450,6 +452,195 @@ bool read_lsdyna(const std::string &path, KMesh &m, std::string &err) {
   return true;
 }
 
+// ---- Nastran bulk data (rigid die meshes) -----------------------------------------
+// NastranReader::read (NastranReader.cpp:34-180): lines starting GRID are
+// nodes and lines starting CTRIA elements, each read as a run of consecutive
+// lines from the first one of its kind; fixed 8-column fields, the id in the
+// second field and the values from the fourth (column 24) on.
+struct NasMesh {
+  std::vector<double> x;     // [3 nn]
+  std::vector<int32_t> tri;  // [3 ne] node positions, file order
+};
+
+// The 8-column field at `pos` (shorter at the end of the line); false when the
+// line ends before the field starts.
+bool nas_field(const std::string &line, size_t pos, std::string &f) {
+  if (pos > line.size()) return false;
+  f = line.substr(pos, 8);
+  return true;
+}
+
+// A real field: a Fortran D exponent reads as E, and a field with no exponent
+// letter takes one before its first sign past the first column ("1.5-3").
+double nas_real(std::string f) {
+  for (char &c : f)
+    if (c == 'D' || c == 'd') c = 'E';
+  if (f.find('E') == std::string::npos && f.find('e') == std::string::npos)
+    for (size_t k = 1; k < f.size(); k++)
+      if (f[k] == '+' || f[k] == '-') {
+        f.insert(k, "E");
+        break;
+      }
+  return std::strtod(f.c_str(), nullptr);
+}
+
+wf_status read_nastran(const std::string &path, NasMesh &m, std::string &err) {
+  std::ifstream in(path);
+  if (!in) {
+    err = "cannot open " + path;
+    return WF_ERR_ARG;
+  }
+  std::vector<std::string> lines;
+  std::string ln;
+  long long first_node = -1, first_elem = -1, nnode = 0, nelem = 0;
+  bool lines2d = false;
+  while (std::getline(in, ln)) {
+    if (ln.compare(0, 4, "GRID") == 0) {
+      if (first_node < 0) first_node = (long long)lines.size();
+      nnode++;
+    } else if (ln.compare(0, 5, "CTRIA") == 0 || ln.compare(0, 5, "CBEAM") == 0 ||
+               ln.compare(0, 4, "CBAR") == 0) {
+      if (first_elem < 0) first_elem = (long long)lines.size();
+      if (ln[1] == 'B') lines2d = true;
+      nelem++;
+    }
+    lines.push_back(ln);
+  }
+  if (lines2d) {
+    err = path + ": CBEAM/CBAR line meshes are 2-D rigid bodies (3-D only)";
+    return WF_ERR_UNSUPPORTED;
+  }
+  if (nnode < 3 || nelem < 1) {
+    err = path + ": no GRID nodes or CTRIA triangles";
+    return WF_ERR_ARG;
+  }
+  if (first_node + nnode > (long long)lines.size() || first_elem + nelem > (long long)lines.size()) {
+    err = path + ": GRID and CTRIA cards must each be consecutive lines";
+    return WF_ERR_ARG;
+  }
+  std::map<int, int32_t> pos;  // node id -> position (the first card of an id wins)
+  m.x.assign(3 * nnode, 0.0);
+  std::string f;
+  for (long long n = 0; n < nnode; n++) {
+    const std::string &L = lines[first_node + n];
+    if (!nas_field(L, 8, f)) {
+      err = path + ": short GRID card: " + L;
+      return WF_ERR_ARG;
+    }
+    pos.emplace(std::atoi(f.c_str()), (int32_t)n);
+    for (int i = 0; i < 3; i++) {
+      if (!nas_field(L, 24 + 8 * i, f)) {
+        err = path + ": short GRID card: " + L;
+        return WF_ERR_ARG;
+      }
+      m.x[3 * n + i] = nas_real(f);
+    }
+  }
+  m.tri.assign(3 * nelem, 0);
+  for (long long e = 0; e < nelem; e++) {
+    const std::string &L = lines[first_elem + e];
+    for (int a = 0; a < 3; a++) {
+      if (!nas_field(L, 24 + 8 * a, f)) {
+        err = path + ": short CTRIA card: " + L;
+        return WF_ERR_ARG;
+      }
+      const int id = std::atoi(f.c_str());
+      auto it = pos.find(id);
+      if (it == pos.end()) {
+        err = path + ": triangle " + std::to_string(e + 1) + " references unknown node " +
+              std::to_string(id);
+        return WF_ERR_ARG;
+      }
+      m.tri[3 * e + a] = it->second;
+    }
+  }
+  return WF_OK;
+}
+
+// TriMesh_d(NastranReader&, flipnormals, orientNormals, orient_pt) (Mesh.C:560-760):
+// flipnormals swaps each triangle's first two nodes. With an orientation point
+// P, a triangle turns (first two nodes swapped again) when its normal points
+// away from the interior point C + 2 |C - P| (C - P) / |C - P|, C the mean
+// of the die's nodes: the normals end up facing P, the part's side.
+void nas_orient(const NasMesh &m, bool flip, const double *P, std::vector<int32_t> &tri) {
+  const size_t nn = m.x.size() / 3, ne = m.tri.size() / 3;
+  const double *X = m.x.data();
+  double C[3] = {0.0, 0.0, 0.0};
+  for (size_t n = 0; n < nn; n++)
+    for (int k = 0; k < 3; k++) C[k] = C[k] + X[3 * n + k];
+  const double inv_nn = 1.0 / (double)nn;
+  for (int k = 0; k < 3; k++) C[k] = C[k] * inv_nn;
+  tri.resize(3 * ne);
+  double S[3] = {0.0, 0.0, 0.0};
+  if (P) {
+    double dir[3] = {C[0] - P[0], C[1] - P[1], C[2] - P[2]};
+    const double dist = std::sqrt(dir[0] * dir[0] + dir[1] * dir[1] + dir[2] * dir[2]);
+    const double inv = 1.0 / dist;
+    for (int k = 0; k < 3; k++) dir[k] = dir[k] * inv;
+    for (int k = 0; k < 3; k++) S[k] = C[k] + dir[k] * (2.0 * dist);
+  }
+  const double third = 1.0 / 3.;
+  for (size_t e = 0; e < ne; e++) {
+    const int32_t c0 = m.tri[3 * e], c1 = m.tri[3 * e + 1], c2 = m.tri[3 * e + 2];
+    const double *p0 = &X[3 * c0], *p1 = &X[3 * c1], *p2 = &X[3 * c2];
+    int32_t *t = &tri[3 * e];
+    t[0] = flip ? c1 : c0;
+    t[1] = flip ? c0 : c1;
+    t[2] = c2;
+    if (!P) continue;
+    const double u[3] = {p1[0] - p0[0], p1[1] - p0[1], p1[2] - p0[2]};
+    const double v[3] = {p2[0] - p0[0], p2[1] - p0[1], p2[2] - p0[2]};
+    double w[3] = {u[1] * v[2] - u[2] * v[1], u[2] * v[0] - u[0] * v[2],
+                   u[0] * v[1] - u[1] * v[0]};
+    for (int pass = 0; pass < 2; pass++) {
+      const double inv = 1.0 / std::sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+      for (int k = 0; k < 3; k++) w[k] = w[k] * inv;
+    }
+    if (flip)
+      for (int k = 0; k < 3; k++) w[k] = -w[k];
+    double g[3];
+    for (int k = 0; k < 3; k++) g[k] = ((p0[k] + p1[k]) + p2[k]) * third - S[k];
+    if (w[0] * g[0] + w[1] * g[1] + w[2] * g[2] < 0.0) std::swap(t[0], t[1]);
+  }
+}
+
+// A file named in a deck: relative to the deck's folder when it exists there,
+// else as given (relative to the working directory) or absolute.
+std::string resolve(const std::string &deck, const std::string &fname) {
+  if (!fname.empty() && fname[0] == '/') return fname;
+  const std::string full = dir_of(deck) + fname;
+  std::ifstream probe(full);
+  return probe ? full : fname;
+}
+
+// TriMesh_d::AxisPlaneMesh for axis 2 (Mesh.C:48-200), the Plane rigid body:
+// (dens+1)^2 nodes at z = start.z spaced (dim.x - start.x) / dens in x and y,
+// two triangles per cell with normal +z, or -z with flipnormals.
+void plane_mesh(const double *st, const double *dm, int dens, bool flip, std::vector<double> &x,
+                std::vector<int32_t> &tri) {
+  const double dl = (dm[0] - st[0]) / dens;
+  double x2 = st[1];
+  for (int jj = 0; jj <= dens; jj++) {
+    double x1 = st[0];
+    for (int ii = 0; ii <= dens; ii++) {
+      x.push_back(x1);
+      x.push_back(x2);
+      x.push_back(st[2]);
+      x1 += dl;
+    }
+    x2 += dl;
+  }
+  for (int jj = 0; jj < dens; jj++)
+    for (int ii = 0; ii < dens; ii++) {
+      const int32_t n0 = (dens + 1) * jj + ii, n1 = n0 + 1, n2 = (dens + 1) * (jj + 1) + ii,
+                    n3 = n2 + 1;
+      const int32_t t[2][3] = {{n0, n1, n2}, {n1, n3, n2}};
+      const int32_t tf[2][3] = {{n0, n2, n1}, {n1, n2, n3}};
+      for (int q = 0; q < 2; q++)
+        for (int c = 0; c < 3; c++) tri.push_back(flip ? tf[q][c] : t[q][c]);
+    }
+}
+
 // Domain_d::calcMinEdgeLength in 3-D (Domain_d.C:2224-2469): every element is
 // read as a tetrahedron of its first four nodes and the six segments between
 // them are measured.
@@ -473,10 +664,18 @@ double ref_min_length(const std::vector<double> &x, const std::vector<int32_t> &
 }  // namespace
 
 // ---- deck object ---------------------------------------------------------------------
+// A rigid body of a contact deck: triangle mesh, zone id and the velocity the
+// boundary condition of that zone gives it.
+struct DeckBody {
+  std::vector<double> x;
+  std::vector<int32_t> tri;
+  int zone = 0;
+  double vel[3] = {0.0, 0.0, 0.0};
+};
+
 struct wf_deck {
   wf_deck_info info{};
-  std::vector<double> die_x;
-  std::vector<int32_t> die_tri;
+  std::vector<DeckBody> bodies;
   std::vector<double> x;
   std::vector<int32_t> elnod;
   std::vector<int64_t> bc_node;
@@ -604,10 +803,7 @@ WF_API wf_status wf_deck_read(const char *path, wf_deck **out, char *err, int64_
     const std::string ext = fname.substr(fname.find_last_of('.') + 1);
     if (ext != "k") return bad("mesh file " + fname + ": only LS-DYNA .k meshes are read",
                                WF_ERR_UNSUPPORTED);
-    std::string full = dir_of(path) + fname;
-    if (!fname.empty() && fname[0] == '/') full = fname;
-    std::ifstream probe(full);
-    if (!probe) full = fname;
+    const std::string full = resolve(path, fname);
     KMesh km;
     std::string e;
     if (!read_lsdyna(full, km, e)) return bad(e);
@@ -632,55 +828,66 @@ WF_API wf_status wf_deck_read(const char *path, wf_deck **out, char *err, int64_
   I.nn = (int64_t)(k->x.size() / 3);
   I.ne = (int64_t)(k->elnod.size() / I.npe);
 
-  // Rigid bodies (main.C:633-750): one Plane body becomes a triangle-mesh die
-  std::string rtype;
-  int die_zone = 0;
+  // Rigid bodies (main.C:633-830): entry 0 and, when present, entry 1 (the
+  // reference reads no further entries) become rigid triangle meshes
   const JVal *r0 = rig ? rig->at(0) : nullptr;
+  std::string rtype;
   if (r0 && jstr(r0, "type", rtype)) {
-    if (rtype != "Plane")
-      return bad("rigid body type " + rtype + " is not supported", WF_ERR_UNSUPPORTED);
-    if (rig->arr.size() > 1) return bad("a second rigid body is not supported", WF_ERR_UNSUPPORTED);
-    double st[3] = {0, 0, 0}, dm[3] = {0, 0, 0};
-    jvec(r0, "start", st, 3);
-    jvec(r0, "dim", dm, 3);
-    bool flip = false;
-    jbool(r0, "flipnormals", flip);
-    int dens = 1;
-    jint(r0, "partSide", dens);
-    jint(r0, "zoneId", die_zone);
-    if (dens < 1) return bad("RigidBodies partSide must be >= 1");
-    // TriMesh_d::AxisPlaneMesh(id, axis 2, !flipnormals, start, dim, partSide)
-    // (Mesh.C:48-200): (dens+1)^2 nodes at z = start.z spaced (dim.x - start.x) / dens
-    const double dl = (dm[0] - st[0]) / dens;
-    double x2 = st[1];
-    for (int jj = 0; jj <= dens; jj++) {
-      double x1 = st[0];
-      for (int ii = 0; ii <= dens; ii++) {
-        k->die_x.push_back(x1);
-        k->die_x.push_back(x2);
-        k->die_x.push_back(st[2]);
-        x1 += dl;
+    // Domain_d::ComputeCentroid (Domain_d.C:2733-2755): default orientation point
+    double cen[3] = {0.0, 0.0, 0.0};
+    for (int64_t a = 0; a < I.nn; a++)
+      for (int q = 0; q < 3; q++) cen[q] += k->x[3 * a + q];
+    for (int q = 0; q < 3; q++) cen[q] /= (double)I.nn;
+    const size_t nb = std::min<size_t>(rig->arr.size(), 2);
+    for (size_t b = 0; b < nb; b++) {
+      const JVal *r = rig->at(b);
+      DeckBody body;
+      std::string bt;
+      jstr(r, "type", bt);
+      jint(r, "zoneId", body.zone);
+      bool flip = false;
+      jbool(r, "flipnormals", flip);
+      if (bt == "Plane") {
+        double st[3] = {0, 0, 0}, dm[3] = {0, 0, 0};
+        jvec(r, "start", st, 3);
+        jvec(r, "dim", dm, 3);
+        int dens = 1;
+        jint(r, "partSide", dens);
+        if (dens < 1) return bad("RigidBodies partSide must be >= 1");
+        plane_mesh(st, dm, dens, flip, body.x, body.tri);
+      } else if (bt == "File") {
+        std::string fname;
+        if (!jstr(r, "fileName", fname)) return bad("File rigid body without fileName");
+        bool orient = true;
+        jbool(r, "orientNormals", orient);
+        double opt[3] = {cen[0], cen[1], cen[2]};
+        jvec(r, "orientPoint", opt, 3);
+        NasMesh nm;
+        std::string e;
+        const wf_status rs = read_nastran(resolve(path, fname), nm, e);
+        if (rs) return bad(e, rs);
+        nas_orient(nm, flip, orient ? opt : nullptr, body.tri);
+        body.x.swap(nm.x);
+      } else if (bt == "Line") {
+        return bad("rigid body type Line is 2-D (3-D only)", WF_ERR_UNSUPPORTED);
+      } else {
+        return bad("rigid body " + std::to_string(b) + ": type " + bt + " is not supported",
+                   WF_ERR_UNSUPPORTED);
       }
-      x2 += dl;
+      k->bodies.push_back(std::move(body));
     }
-    for (int jj = 0; jj < dens; jj++)
-      for (int ii = 0; ii < dens; ii++) {
-        const int32_t n0 = (dens + 1) * jj + ii, n1 = n0 + 1, n2 = (dens + 1) * (jj + 1) + ii,
-                      n3 = n2 + 1;
-        const int32_t t[2][3] = {{n0, n1, n2}, {n1, n3, n2}};
-        const int32_t tf[2][3] = {{n0, n2, n1}, {n1, n2, n3}};
-        for (int q = 0; q < 2; q++)
-          for (int c = 0; c < 3; c++) k->die_tri.push_back(flip ? tf[q][c] : t[q][c]);
-      }
     I.contact = 1;
-    I.die_nodes = (int32_t)(k->die_x.size() / 3);
-    I.die_tris = (int32_t)(k->die_tri.size() / 3);
+    I.rigid_bodies = (int32_t)k->bodies.size();
+    I.die_nodes = (int32_t)(k->bodies[0].x.size() / 3);
+    I.die_tris = (int32_t)(k->bodies[0].tri.size() / 3);
     I.penalty_factor = 0.1;  // Domain_d constructor (Domain_d.h:256)
     const JVal *c0 = j.get("Contact") ? j.get("Contact")->at(0) : nullptr;
     jnum(c0, "fricCoeffStatic", I.mu_static);
     jnum(c0, "fricCoeffDynamic", I.mu_dynamic);
     double pf = -1.0;
     if (jnum(c0, "penaltyFactor", pf) && pf > -1.0) I.penalty_factor = pf;
+  } else if (rig && rig->kind == JVal::Arr && rig->arr.size() > 1) {
+    return bad("a second rigid body needs a first one with a type");
   }
 
   // BoundaryConditions: AddBCVelZone per condition, in order (main.C:578-887)
@@ -699,8 +906,9 @@ WF_API wf_status wf_deck_read(const char *path, wf_deck **out, char *err, int64_
         // condition acts on the part (main.C:690-700, :737-750)
         int zid = -1;
         jint(&bc, "zoneId", zid);
-        if (zid == die_zone)
-          for (int q = 0; q < 3; q++) I.die_vel[q] = val[q];
+        for (DeckBody &body : k->bodies)
+          if (zid == body.zone)
+            for (int q = 0; q < 3; q++) body.vel[q] = val[q];
         continue;
       }
       bool have = jvec(&bc, "start", st, 3) && jvec(&bc, "end", en, 3);
@@ -733,6 +941,8 @@ WF_API wf_status wf_deck_read(const char *path, wf_deck **out, char *err, int64_
       }
     }
   }
+  if (I.contact)
+    for (int q = 0; q < 3; q++) I.die_vel[q] = k->bodies[0].vel[q];
   // symmetry planes (main.C:945-960): coordinate < symtol fixes that dof
   for (int64_t a = 0; a < I.nn; a++)
     for (int d = 0; d < 3; d++)
@@ -768,8 +978,43 @@ WF_API wf_status wf_deck_get_mesh(const wf_deck *k, double *xyz, int32_t *elnod)
 
 WF_API wf_status wf_deck_get_die(const wf_deck *k, double *xyz, int32_t *tri) {
   if (!k) return WF_ERR_ARG;
-  if (xyz) std::memcpy(xyz, k->die_x.data(), sizeof(double) * k->die_x.size());
-  if (tri) std::memcpy(tri, k->die_tri.data(), sizeof(int32_t) * k->die_tri.size());
+  if (k->bodies.empty()) return WF_OK;
+  const DeckBody &b = k->bodies[0];
+  if (xyz) std::memcpy(xyz, b.x.data(), sizeof(double) * b.x.size());
+  if (tri) std::memcpy(tri, b.tri.data(), sizeof(int32_t) * b.tri.size());
+  return WF_OK;
+}
+
+WF_API wf_status wf_deck_get_body(const wf_deck *k, int32_t body, int64_t *nnodes, int64_t *ntris,
+                                  double vel[3], double *xyz, int32_t *tri) {
+  if (!k || body < 0 || body >= (int32_t)k->bodies.size()) return WF_ERR_ARG;
+  const DeckBody &b = k->bodies[body];
+  if (nnodes) *nnodes = (int64_t)(b.x.size() / 3);
+  if (ntris) *ntris = (int64_t)(b.tri.size() / 3);
+  if (vel)
+    for (int q = 0; q < 3; q++) vel[q] = b.vel[q];
+  if (xyz) std::memcpy(xyz, b.x.data(), sizeof(double) * b.x.size());
+  if (tri) std::memcpy(tri, b.tri.data(), sizeof(int32_t) * b.tri.size());
+  return WF_OK;
+}
+
+WF_API wf_status wf_read_nastran(const char *path, int32_t flip_normals, const double *orient_pt,
+                                 double *xyz, int64_t cap_nodes, int32_t *tri, int64_t cap_tris,
+                                 int64_t *nnodes, int64_t *ntris, char *err, int64_t err_len) {
+  if (!path) return WF_ERR_ARG;
+  NasMesh m;
+  std::string e;
+  const wf_status s = read_nastran(path, m, e);
+  if (s) return deck_fail(err, err_len, e, s);
+  std::vector<int32_t> t;
+  nas_orient(m, flip_normals != 0, orient_pt, t);
+  const int64_t nn = (int64_t)(m.x.size() / 3), ne = (int64_t)(t.size() / 3);
+  if (nnodes) *nnodes = nn;
+  if (ntris) *ntris = ne;
+  if (xyz && cap_nodes > 0)
+    std::memcpy(xyz, m.x.data(), sizeof(double) * 3 * (size_t)std::min(nn, cap_nodes));
+  if (tri && cap_tris > 0)
+    std::memcpy(tri, t.data(), sizeof(int32_t) * 3 * (size_t)std::min(ne, cap_tris));
   return WF_OK;
 }
 
@@ -804,10 +1049,16 @@ WF_API wf_status wf_deck_apply(const wf_deck *k, wf_domain *d) {
   if (I.artif_visc[0] != 0.0 || I.artif_visc[1] != 0.0)
     WF_DECK_TRY(wf_set_artif_visc(d, I.artif_visc[0], I.artif_visc[1]));
   if (I.hourglass != 0.0) WF_DECK_TRY(wf_set_hourglass(d, I.hourglass));
-  if (I.contact)
-    WF_DECK_TRY(wf_set_contact_trimesh(d, I.die_nodes, k->die_x.data(), I.die_tris,
-                                       k->die_tri.data(), I.die_vel, I.mu_static, I.mu_dynamic,
-                                       I.penalty_factor));
+  if (I.contact) {
+    const DeckBody &b0 = k->bodies[0];
+    WF_DECK_TRY(wf_set_contact_trimesh(d, I.die_nodes, b0.x.data(), I.die_tris, b0.tri.data(),
+                                       b0.vel, I.mu_static, I.mu_dynamic, I.penalty_factor));
+    for (size_t b = 1; b < k->bodies.size(); b++) {
+      const DeckBody &bb = k->bodies[b];
+      WF_DECK_TRY(wf_add_contact_trimesh(d, (int64_t)(bb.x.size() / 3), bb.x.data(),
+                                         (int64_t)(bb.tri.size() / 3), bb.tri.data(), bb.vel));
+    }
+  }
   WF_DECK_TRY(wf_set_dt(d, I.dt));
   WF_DECK_TRY(wf_set_end_time(d, I.end_time));
 #undef WF_DECK_TRY

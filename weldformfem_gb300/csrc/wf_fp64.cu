@@ -468,7 +468,9 @@ __device__ __forceinline__ double block_sum(double v, double *sh) {
 // force pf * min(E A / l, 0.2 m / dt^2) * d plus damping, then Coulomb
 // friction from the accumulated tangential slip (static cap, else dynamic
 // force along -v_t, slip reset). A node out of contact keeps its last contact
-// force, as in the reference. Returns the normal-force magnitude (reaction).
+// force, as in the reference. Returns the normal-force magnitude when the
+// triangle belongs to rigid body 0, the only body the reaction sums
+// (Contact.C:229, :326-329), else 0.
 __device__ __forceinline__ double tri_contact(const StepParams &P, const Fp64State &S, int64_t n,
                                               const double (&x)[3], const double (&v)[3],
                                               double m, double (&cf)[3]) {
@@ -545,6 +547,7 @@ __device__ __forceinline__ double tri_contact(const StepParams &P, const Fp64Sta
     cf[0] += F[0];
     cf[1] += F[1];
     cf[2] += F[2];
+    if (P.tri_mid[j] != 0) cfn = 0.0;
     break;
   }
   S.cf[n] = cf[0];

@@ -109,6 +109,7 @@ struct StepParams {
   double *tri_nrm;          // [3 tri_ne] unit normals
   double *tri_pp;           // [tri_ne] plane coefficients
   const int32_t *tri_el;    // [3 tri_ne]
+  const int32_t *tri_mid;   // [tri_ne] rigid-body index; body 0 feeds the reaction
   const double *node_area;  // [nn] external-surface area share of each node
   const double *nodlen;     // [nn] mean element length at each node
   double tri_mu_s, tri_mu_d, tri_pf, tri_E0, end_t;
@@ -178,6 +179,12 @@ void mix_elements(const StepParams &P, const MixState &M, const float *vol, cuda
                   LaunchCfg c);
 void mix_nodes(const StepParams &P, const MixState &M, cudaStream_t st, int node_grid);
 void mix_predict(const StepParams &P, const MixState &M, cudaStream_t st);
+// Whole runs of steps in one launch of one cluster of `blocks` blocks of `bs`
+// threads (64, 128 or 256), for small meshes; mix_cluster_fits returns how
+// many such clusters can be resident (0: the shape cannot launch).
+int mix_cluster_fits(const StepParams &P, const MixState &M, float *vol, int blocks, int bs);
+cudaError_t mix_cluster_run(const StepParams &P, const MixState &M, float *vol, int64_t nsteps,
+                            int blocks, int bs, cudaStream_t st);
 void mix_export(const StepParams &P, const MixState &M, const Fp64State &S, const float *vol,
                 cudaStream_t st);
 int mix_node_grid(int64_t nn);

@@ -47,25 +47,37 @@ __device__ __forceinline__ float pair_rel(float2 a, float2 b) {
   return __fadd_rn(__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y));
 }
 
+// Loads of data that other threads write during the run: through the
+// read-only path (__ldg) in the per-phase kernels, where it is constant for
+// the launch, and through L2 (__ldcg) in the persistent cluster kernel, whose
+// phases share one launch.
+template <bool CG, typename T>
+__device__ __forceinline__ T ldx(const T *p) {
+  if constexpr (CG)
+    return __ldcg(p);
+  else
+    return __ldg(p);
+}
+
 template <int NPE>
 __device__ __forceinline__ float weightf() {
   return NPE == 8 ? 8.0f : 1.0f / 6.0f;
 }
 
-template <int NPE>
+template <int NPE, bool CG>
 __device__ __forceinline__ void rel_coords(const StepParams &P, const MixState &M, int64_t e,
                                            float (&r)[NPE][3], int32_t (&nid)[NPE]) {
 #pragma unroll
   for (int a = 0; a < NPE; a++) nid[a] = __ldg(&P.elnod[a * P.ne + e]);
   float2 o[3];
 #pragma unroll
-  for (int k = 0; k < 3; k++) o[k] = __ldg(&M.xh[k * P.np + nid[0]]);
+  for (int k = 0; k < 3; k++) o[k] = ldx<CG>(&M.xh[k * P.np + nid[0]]);
 #pragma unroll
   for (int k = 0; k < 3; k++) r[0][k] = 0.0f;
 #pragma unroll
   for (int a = 1; a < NPE; a++)
 #pragma unroll
-    for (int k = 0; k < 3; k++) r[a][k] = pair_rel(__ldg(&M.xh[k * P.np + nid[a]]), o[k]);
+    for (int k = 0; k < 3; k++) r[a][k] = pair_rel(ldx<CG>(&M.xh[k * P.np + nid[a]]), o[k]);
 }
 
 template <int NPE>
@@ -130,12 +142,12 @@ __device__ __forceinline__ void shape_derivs_f(const float J[3][3], float dH[3][
 }
 
 // ---------------------------------------------------------------------------
-template <int NPE>
+template <int NPE, bool CG>
 __device__ __forceinline__ void geometry_one(const StepParams &P, const MixState &M, float *vol,
                                              int64_t e) {
   float r[NPE][3];
   int32_t nid[NPE];
-  rel_coords<NPE>(P, M, e, r, nid);
+  rel_coords<NPE, CG>(P, M, e, r, nid);
   float J[3][3];
   jacobian_f<NPE>(r, J);
   vol[e] = det3f(J) * weightf<NPE>();
@@ -146,15 +158,15 @@ __device__ __forceinline__ void geometry_one(const StepParams &P, const MixState
 template <int NPE, int BS>
 __global__ void __launch_bounds__(BS) k_mix_geometry(StepParams P, MixState M, float *vol) {
   for (int64_t e = (int64_t)blockIdx.x * BS + threadIdx.x; e < P.ne; e += (int64_t)gridDim.x * BS)
-    geometry_one<NPE>(P, M, vol, e);
+    geometry_one<NPE, false>(P, M, vol, e);
 }
 
 // Nodal volumes -> J ratio and lumped mass; for contact candidates also the
 // rigid-plane contact force (it needs only x, the predicted velocity and the
 // step's mass, all final here, so it is computed before the element phase).
-template <int NPE>
+template <int NPE, bool CG>
 __device__ __forceinline__ void nodal_one(const StepParams &P, const MixState &M,
-                                          const float *vol, int64_t n) {
+                                          const float *vol, int64_t n, double time) {
   const int32_t b = __ldg(&P.off[n]), c = __ldg(&P.off[n + 1]) - b;
   float s = 0.0f;
   for (int32_t k0 = 0; k0 < c; k0 += 8) {
@@ -163,7 +175,7 @@ __device__ __forceinline__ void nodal_one(const StepParams &P, const MixState &M
     for (int j = 0; j < 8; j++) sl[j] = (k0 + j < c) ? __ldg(&P.slot[b + k0 + j]) : -1;
     float g[8];
 #pragma unroll
-    for (int j = 0; j < 8; j++) g[j] = (sl[j] >= 0) ? __ldg(&vol[sl[j] / NPE]) : 0.0f;
+    for (int j = 0; j < 8; j++) g[j] = (sl[j] >= 0) ? ldx<CG>(&vol[sl[j] / NPE]) : 0.0f;
 #pragma unroll
     for (int j = 0; j < 8; j++) s += g[j];
   }
@@ -182,7 +194,7 @@ __device__ __forceinline__ void nodal_one(const StepParams &P, const MixState &M
     const int64_t np = P.np;
     const float2 xz = M.xh[2 * np + n];
     const float vp0 = M.vp[n], vp1 = M.vp[np + n], vp2 = M.vp[2 * np + n];
-    const double zd = P.c_z0 + P.c_vz * P.st->time;
+    const double zd = P.c_z0 + P.c_vz * time;
     const float gap = (float)(zd - ((double)xz.x + (double)xz.y));
     float cf0 = 0.f, cf1 = 0.f, cf2 = 0.f;
     if (gap < 0.f) {
@@ -218,7 +230,7 @@ __device__ __forceinline__ void nodal_one(const StepParams &P, const MixState &M
 template <int NPE, int BS>
 __global__ void __launch_bounds__(BS) k_mix_nodal(StepParams P, MixState M, const float *vol) {
   for (int64_t n = (int64_t)blockIdx.x * BS + threadIdx.x; n < P.nn; n += (int64_t)gridDim.x * BS)
-    nodal_one<NPE>(P, M, vol, n);
+    nodal_one<NPE, false>(P, M, vol, n, P.st->time);
 }
 
 // Jaumann rate + radial return, shared by both element types. The
@@ -355,7 +367,7 @@ __device__ __forceinline__ void walsh8_synth(const float (&o)[8], float (&v)[8])
 // nodal velocities, and the nodal forces are the synthesis of
 // T = adj(J)^T sigma (w / 8 = 1) plus the hourglass coefficients ch h_j.
 // Same quantities as the reference's per-node loops, fewer operations.
-template <int LAW>
+template <int LAW, bool CG>
 __device__ __forceinline__ void element_hex(const StepParams &P, const MixState &M, int64_t e,
                                             float *stash, int stride) {
   const int64_t ne = P.ne, np = P.np;
@@ -363,7 +375,7 @@ __device__ __forceinline__ void element_hex(const StepParams &P, const MixState 
   float A[3][3], detJ;
   {
     float r[8][3];
-    rel_coords<8>(P, M, e, r, nid);
+    rel_coords<8, CG>(P, M, e, r, nid);
     float J[3][3];
 #pragma unroll
     for (int k = 0; k < 3; k++) {
@@ -394,7 +406,7 @@ __device__ __forceinline__ void element_hex(const StepParams &P, const MixState 
   for (int k = 0; k < 3; k++) {
     float v[8], o[8];
 #pragma unroll
-    for (int a = 0; a < 8; a++) v[a] = __ldg(&M.vp[k * np + nid[a]]);
+    for (int a = 0; a < 8; a++) v[a] = ldx<CG>(&M.vp[k * np + nid[a]]);
     walsh8(v, o);
     G[0][k] = o[1];
     G[1][k] = o[2];
@@ -413,7 +425,7 @@ __device__ __forceinline__ void element_hex(const StepParams &P, const MixState 
   }
   float J_avg = 0.f;
 #pragma unroll
-  for (int a = 0; a < 8; a++) J_avg += __ldg(&M.jr[nid[a]]);
+  for (int a = 0; a < 8; a++) J_avg += ldx<CG>(&M.jr[nid[a]]);
   // velocity gradient L[i][k] = d v_k / d x_i
   const float fl = 0.125f / detJ;
   float L[3][3];
@@ -450,7 +462,7 @@ __device__ __forceinline__ void element_hex(const StepParams &P, const MixState 
 }
 
 // Tetrahedron: per-node shape derivatives (Domain_d.C:1866-1887).
-template <int LAW>
+template <int LAW, bool CG>
 __device__ __forceinline__ void element_tet(const StepParams &P, const MixState &M, int64_t e) {
   const int64_t ne = P.ne;
   int32_t nid[4];
@@ -458,7 +470,7 @@ __device__ __forceinline__ void element_tet(const StepParams &P, const MixState 
   float detJ;
   {
     float r[4][3];
-    rel_coords<4>(P, M, e, r, nid);
+    rel_coords<4, CG>(P, M, e, r, nid);
     float J[3][3];
     jacobian_f<4>(r, J);
     shape_derivs_f<4>(J, dH);
@@ -470,9 +482,9 @@ __device__ __forceinline__ void element_tet(const StepParams &P, const MixState 
   float J_avg = 0.f;
 #pragma unroll
   for (int a = 0; a < 4; a++) {
-    const float v0 = __ldg(&M.vp[nid[a]]);
-    const float v1 = __ldg(&M.vp[P.np + nid[a]]);
-    const float v2 = __ldg(&M.vp[2 * P.np + nid[a]]);
+    const float v0 = ldx<CG>(&M.vp[nid[a]]);
+    const float v1 = ldx<CG>(&M.vp[P.np + nid[a]]);
+    const float v2 = ldx<CG>(&M.vp[2 * P.np + nid[a]]);
     const float d0 = dH[0][a], d1 = dH[1][a], d2 = dH[2][a];
     s00 += d0 * v0;
     s11 += d1 * v1;
@@ -483,7 +495,7 @@ __device__ __forceinline__ void element_tet(const StepParams &P, const MixState 
     s02 += d2 * v0 + d0 * v2;
     w12 += d2 * v1 - d1 * v2;
     w02 += d2 * v0 - d0 * v2;
-    J_avg += __ldg(&M.jr[nid[a]]);
+    J_avg += ldx<CG>(&M.jr[nid[a]]);
   }
   const float f = 1.0f / detJ;
   const float fh = 0.5f * f;
@@ -506,13 +518,13 @@ __device__ __forceinline__ void element_tet(const StepParams &P, const MixState 
   }
 }
 
-template <int NPE, int LAW>
+template <int NPE, int LAW, bool CG>
 __device__ __forceinline__ void element_one(const StepParams &P, const MixState &M, int64_t e,
                                             float *stash, int stride) {
   if constexpr (NPE == 8)
-    element_hex<LAW>(P, M, e, stash, stride);
+    element_hex<LAW, CG>(P, M, e, stash, stride);
   else
-    element_tet<LAW>(P, M, e);
+    element_tet<LAW, CG>(P, M, e);
 }
 
 // Registers per thread stay <= 64 at 1024 resident threads per SM.
@@ -523,7 +535,7 @@ __global__ void __launch_bounds__(BS, elem_min_blocks(BS)) k_mix_elements(StepPa
                                                                           MixState M) {
   __shared__ float stash[NPE == 8 ? 12 * BS : 1];
   for (int64_t e = (int64_t)blockIdx.x * BS + threadIdx.x; e < P.ne; e += (int64_t)gridDim.x * BS)
-    element_one<NPE, LAW>(P, M, e, &stash[threadIdx.x], BS);
+    element_one<NPE, LAW, false>(P, M, e, &stash[threadIdx.x], BS);
 }
 
 // ---------------------------------------------------------------------------
@@ -557,101 +569,108 @@ __device__ __forceinline__ double block_sum_dense(double v, double *sh) {
   return t;
 }
 
+// Node update of one node: gather of the element forces in list order,
+// accelerations, velocity BCs, Chung-Hulbert corrector and the next
+// predictor. Returns the node's reaction contribution.
+template <int NPE, bool CG>
+__device__ __forceinline__ float node_one(const StepParams &P, const MixState &M, int64_t n) {
+  float r = 0.0f;
+  const int64_t np = P.np;
+  const int32_t b = __ldg(&P.off[n]), c = __ldg(&P.off[n + 1]) - b;
+  const int64_t ne = P.ne;
+  // gather over the node's element list in list order, eight entries at a
+  // time so that the slot and force loads of a chunk are all in flight
+  float fi0 = 0.f, fi1 = 0.f, fi2 = 0.f;
+  for (int32_t k0 = 0; k0 < c; k0 += 8) {
+    int32_t sl[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) sl[j] = (k0 + j < c) ? __ldg(&P.slot[b + k0 + j]) : -1;
+    float g0[8], g1[8], g2[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      g0[j] = g1[j] = g2[j] = 0.f;
+      if (sl[j] >= 0) {
+        const int64_t base = (int64_t)(sl[j] % NPE) * 3 * ne + sl[j] / NPE;
+        g0[j] = ldx<CG>(&M.fe[base]);
+        g1[j] = ldx<CG>(&M.fe[base + ne]);
+        g2[j] = ldx<CG>(&M.fe[base + 2 * ne]);
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      fi0 += g0[j];
+      fi1 += g1[j];
+      fi2 += g2[j];
+    }
+  }
+  float fi[3] = {fi0, fi1, fi2};
+#pragma unroll
+  for (int k = 0; k < 3; k++)
+    if (!isfinite(fi[k])) {
+      fi[k] = 0.f;
+      atomicOr(&P.st->status, 1u);
+    }
+  const uint8_t fl = P.nflag[n];
+  const float mass = M.mass[n];
+  const float inv_m = 1.0f / mass;
+  float2 x[3];
+  float vold[3], vp[3], pa[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    x[k] = M.xh[k * np + n];
+    vold[k] = M.v[k * np + n];
+    vp[k] = M.vp[k * np + n];
+    pa[k] = M.pa[k * np + n];
+  }
+  float cf[3] = {0.f, 0.f, 0.f};
+  if (P.contact && (fl & NF_CONTACT)) {
+    cf[0] = M.cf[n];
+    cf[1] = M.cf[np + n];
+    cf[2] = M.cf[2 * np + n];
+    r = fabsf(cf[2]);
+  }
+  if (!P.contact && (fl & NF_REACTION)) {
+    if (P.rnode)
+      P.rnode[n] = fi[P.react_dim];  // summed per specimen by the reaction kernel
+    else
+      r = fi[P.react_dim];
+  }
+  float c_dt = P.f_dt, c_cu_pred = P.f_cu_pred, c_cu_corr = P.f_cu_corr;
+  float c_cv_corr = P.f_cv_corr, c_cv_pred = P.f_cv_pred;
+  if (P.nspec_of) {
+    const SpecF sf = P.specf[P.nspec_of[n]];
+    c_dt = sf.dt; c_cu_pred = sf.cu_pred; c_cu_corr = sf.cu_corr;
+    c_cv_corr = sf.cv_corr; c_cv_pred = sf.cv_pred;
+  }
+  const uint32_t code = P.bc[n];
+  const double *bvd = &P.bcval[3 * (code >> 3)];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const bool fixed = (code >> k) & 1u;
+    float a = (cf[k] - fi[k]) * inv_m;
+    if (fixed) a = 0.f;
+    a = P.f_fcorr * (a - P.f_alpha * pa[k]);
+    float v = vp[k] + c_cv_corr * a;
+    const float bv = fixed ? (float)__ldg(&bvd[k]) : 0.f;
+    if (fixed) v = bv;
+    const float udt = c_dt * (vold[k] + c_cu_pred * pa[k]) + c_cu_corr * a;
+    x[k] = pair_add(x[k], udt);
+    float vnext = v + c_cv_pred * a;
+    if (fixed) vnext = bv;
+    M.xh[k * np + n] = x[k];
+    M.v[k * np + n] = v;
+    M.pa[k * np + n] = a;
+    M.vp[k * np + n] = vnext;
+  }
+  return r;
+}
+
 template <int NPE>
 __global__ void __launch_bounds__(kNodeThreads, 6) k_mix_nodes(StepParams P, MixState M) {
   __shared__ double sh[kNodeThreads / 32];
   __shared__ bool am_last;
   const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  float r = 0.0f;
-  if (n < P.nn) {
-    const int64_t np = P.np;
-    const int32_t b = __ldg(&P.off[n]), c = __ldg(&P.off[n + 1]) - b;
-    const int64_t ne = P.ne;
-    // gather over the node's element list in list order, eight entries at a
-    // time so that the slot and force loads of a chunk are all in flight
-    float fi0 = 0.f, fi1 = 0.f, fi2 = 0.f;
-    for (int32_t k0 = 0; k0 < c; k0 += 8) {
-      int32_t sl[8];
-#pragma unroll
-      for (int j = 0; j < 8; j++) sl[j] = (k0 + j < c) ? __ldg(&P.slot[b + k0 + j]) : -1;
-      float g0[8], g1[8], g2[8];
-#pragma unroll
-      for (int j = 0; j < 8; j++) {
-        g0[j] = g1[j] = g2[j] = 0.f;
-        if (sl[j] >= 0) {
-          const int64_t base = (int64_t)(sl[j] % NPE) * 3 * ne + sl[j] / NPE;
-          g0[j] = __ldg(&M.fe[base]);
-          g1[j] = __ldg(&M.fe[base + ne]);
-          g2[j] = __ldg(&M.fe[base + 2 * ne]);
-        }
-      }
-#pragma unroll
-      for (int j = 0; j < 8; j++) {
-        fi0 += g0[j];
-        fi1 += g1[j];
-        fi2 += g2[j];
-      }
-    }
-    float fi[3] = {fi0, fi1, fi2};
-#pragma unroll
-    for (int k = 0; k < 3; k++)
-      if (!isfinite(fi[k])) {
-        fi[k] = 0.f;
-        atomicOr(&P.st->status, 1u);
-      }
-    const uint8_t fl = P.nflag[n];
-    const float mass = M.mass[n];
-    const float inv_m = 1.0f / mass;
-    float2 x[3];
-    float vold[3], vp[3], pa[3];
-#pragma unroll
-    for (int k = 0; k < 3; k++) {
-      x[k] = M.xh[k * np + n];
-      vold[k] = M.v[k * np + n];
-      vp[k] = M.vp[k * np + n];
-      pa[k] = M.pa[k * np + n];
-    }
-    float cf[3] = {0.f, 0.f, 0.f};
-    if (P.contact && (fl & NF_CONTACT)) {
-      cf[0] = M.cf[n];
-      cf[1] = M.cf[np + n];
-      cf[2] = M.cf[2 * np + n];
-      r = fabsf(cf[2]);
-    }
-    if (!P.contact && (fl & NF_REACTION)) {
-      if (P.rnode)
-        P.rnode[n] = fi[P.react_dim];  // summed per specimen by the reaction kernel
-      else
-        r = fi[P.react_dim];
-    }
-    float c_dt = P.f_dt, c_cu_pred = P.f_cu_pred, c_cu_corr = P.f_cu_corr;
-    float c_cv_corr = P.f_cv_corr, c_cv_pred = P.f_cv_pred;
-    if (P.nspec_of) {
-      const SpecF sf = P.specf[P.nspec_of[n]];
-      c_dt = sf.dt; c_cu_pred = sf.cu_pred; c_cu_corr = sf.cu_corr;
-      c_cv_corr = sf.cv_corr; c_cv_pred = sf.cv_pred;
-    }
-    const uint32_t code = P.bc[n];
-    const double *bvd = &P.bcval[3 * (code >> 3)];
-#pragma unroll
-    for (int k = 0; k < 3; k++) {
-      const bool fixed = (code >> k) & 1u;
-      float a = (cf[k] - fi[k]) * inv_m;
-      if (fixed) a = 0.f;
-      a = P.f_fcorr * (a - P.f_alpha * pa[k]);
-      float v = vp[k] + c_cv_corr * a;
-      const float bv = fixed ? (float)__ldg(&bvd[k]) : 0.f;
-      if (fixed) v = bv;
-      const float udt = c_dt * (vold[k] + c_cu_pred * pa[k]) + c_cu_corr * a;
-      x[k] = pair_add(x[k], udt);
-      float vnext = v + c_cv_pred * a;
-      if (fixed) vnext = bv;
-      M.xh[k * np + n] = x[k];
-      M.v[k * np + n] = v;
-      M.pa[k * np + n] = a;
-      M.vp[k * np + n] = vnext;
-    }
-  }
+  const float r = (n < P.nn) ? node_one<NPE, false>(P, M, n) : 0.0f;
   // reaction: only warps holding a contribution reduce (FP64, fixed order);
   // the last block to finish sums all block partials with the whole block.
   const double bs = block_sum_sparse(r, sh);
@@ -675,6 +694,60 @@ __global__ void __launch_bounds__(kNodeThreads, 6) k_mix_nodes(StepParams P, Mix
       P.st->time = P.st->time + P.dt;
       P.st->done_blocks = 0u;
     }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Small meshes: a whole run of steps in one launch of one thread-block
+// cluster. The four phases of a step are separated by cluster barriers
+// (release / acquire at cluster scope). Each block owns fixed element and
+// node ranges, so per-element and per-node state is read back by the thread
+// that wrote it, and what other blocks wrote (positions, predicted
+// velocities, volumes, volume ratios, element forces) is loaded through L2.
+// Each element and node is updated with the same arithmetic as in the
+// per-phase kernels; the reaction is summed per thread and per block (FP64)
+// and block 0 adds the block partials after the step's last barrier, so its
+// summation order differs from the per-phase node kernel's.
+__device__ __forceinline__ void cluster_barrier() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n" ::: "memory");
+  asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory");
+}
+
+template <int NPE, int BS, int LAW>
+__global__ void __launch_bounds__(BS) k_mix_cluster_run(StepParams P, MixState M, float *vol,
+                                                        int64_t nsteps) {
+  __shared__ float stash[NPE == 8 ? 12 * BS : 1];
+  __shared__ double sh[BS / 32];
+  const int64_t nb = gridDim.x, b = blockIdx.x;
+  const int t = threadIdx.x;
+  const int64_t e0 = P.ne * b / nb, e1 = P.ne * (b + 1) / nb;
+  const int64_t n0 = P.nn * b / nb, n1 = P.nn * (b + 1) / nb;
+  double time = __ldcg(&P.st->time);
+  long long step = __ldcg(&P.st->step);
+  for (int64_t it = 0; it < nsteps; it++) {
+    for (int64_t e = e0 + t; e < e1; e += BS) geometry_one<NPE, true>(P, M, vol, e);
+    cluster_barrier();
+    for (int64_t n = n0 + t; n < n1; n += BS) nodal_one<NPE, true>(P, M, vol, n, time);
+    cluster_barrier();
+    for (int64_t e = e0 + t; e < e1; e += BS)
+      element_one<NPE, LAW, true>(P, M, e, &stash[t], BS);
+    cluster_barrier();
+    double r = 0.0;
+    for (int64_t n = n0 + t; n < n1; n += BS) r += (double)node_one<NPE, true>(P, M, n);
+    const double part = block_sum_dense(r, sh);
+    if (t == 0) P.partials[b] = part;
+    cluster_barrier();
+    if (b == 0 && t == 0) {
+      double tot = 0.0;
+      for (int64_t i = 0; i < nb; i++) tot += __ldcg(&P.partials[i]);
+      if (step < P.hist_cap) P.hist[step] = tot;
+    }
+    step++;
+    time = time + P.dt;
+  }
+  if (b == 0 && t == 0) {
+    P.st->step = step;
+    P.st->time = time;
   }
 }
 
@@ -872,6 +945,55 @@ void launch_elements(const StepParams &P, const MixState &M, cudaStream_t st, La
     launch_elements_law<NPE, 0>(P, M, st, c);
 }
 
+template <int NPE, int BS, int LAW>
+cudaError_t cluster_launch(const StepParams &P, const MixState &M, float *vol, int64_t nsteps,
+                           int blocks, cudaStream_t st, bool query, int *fits) {
+  auto kern = k_mix_cluster_run<NPE, BS, LAW>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  if (e != cudaSuccess) return e;
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = (unsigned)blocks;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.gridDim = dim3((unsigned)blocks);
+  cfg.blockDim = dim3(BS);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  if (query) {
+    int n = 0;
+    e = cudaOccupancyMaxActiveClusters(&n, kern, &cfg);
+    *fits = (e == cudaSuccess) ? n : 0;
+    return e;
+  }
+  return cudaLaunchKernelEx(&cfg, kern, P, M, vol, nsteps);
+}
+
+template <int NPE, int LAW>
+cudaError_t cluster_dispatch_bs(const StepParams &P, const MixState &M, float *vol,
+                                int64_t nsteps, int blocks, int bs, cudaStream_t st, bool query,
+                                int *fits) {
+  switch (bs) {
+    case 64: return cluster_launch<NPE, 64, LAW>(P, M, vol, nsteps, blocks, st, query, fits);
+    case 128: return cluster_launch<NPE, 128, LAW>(P, M, vol, nsteps, blocks, st, query, fits);
+    default: return cluster_launch<NPE, 256, LAW>(P, M, vol, nsteps, blocks, st, query, fits);
+  }
+}
+
+cudaError_t cluster_dispatch(const StepParams &P, const MixState &M, float *vol, int64_t nsteps,
+                             int blocks, int bs, cudaStream_t st, bool query, int *fits) {
+  if (P.npe == 8)
+    return P.mat_general
+               ? cluster_dispatch_bs<8, 1>(P, M, vol, nsteps, blocks, bs, st, query, fits)
+               : cluster_dispatch_bs<8, 0>(P, M, vol, nsteps, blocks, bs, st, query, fits);
+  return P.mat_general
+             ? cluster_dispatch_bs<4, 1>(P, M, vol, nsteps, blocks, bs, st, query, fits)
+             : cluster_dispatch_bs<4, 0>(P, M, vol, nsteps, blocks, bs, st, query, fits);
+}
+
 }  // namespace
 
 void mix_geometry(const StepParams &P, const MixState &M, float *vol, cudaStream_t st,
@@ -897,6 +1019,20 @@ void mix_nodes(const StepParams &P, const MixState &M, cudaStream_t st, int node
     k_mix_nodes<8><<<node_grid, kNodeThreads, 0, st>>>(P, M);
   else
     k_mix_nodes<4><<<node_grid, kNodeThreads, 0, st>>>(P, M);
+}
+
+int mix_cluster_fits(const StepParams &P, const MixState &M, float *vol, int blocks, int bs) {
+  int fits = 0;
+  if (cluster_dispatch(P, M, vol, 0, blocks, bs, nullptr, true, &fits) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return fits;
+}
+
+cudaError_t mix_cluster_run(const StepParams &P, const MixState &M, float *vol, int64_t nsteps,
+                            int blocks, int bs, cudaStream_t st) {
+  return cluster_dispatch(P, M, vol, nsteps, blocks, bs, st, false, nullptr);
 }
 
 void mix_predict(const StepParams &P, const MixState &M, cudaStream_t st) {

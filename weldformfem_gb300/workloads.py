@@ -126,7 +126,8 @@ class Case:
     seed: int = SEED_BASE
     materials: list = dataclasses.field(default_factory=lambda: [dict(STEEL)])
     elem_mat: Optional[np.ndarray] = None
-    bc: str = "sym_top"          # "sym_top": symmetry + top vz; "bottom_z": bottom fixed in z
+    bc: str = "sym_top"          # "sym_top": symmetry + top vz; "bottom_z": bottom fixed in z;
+    #                              "sym_xy": x and y symmetry planes only
     top_vz: float = -1.0
     hg: float = 0.0
     dt: Optional[float] = None   # None: 0.3 h_min / sqrt(E / rho)
@@ -184,6 +185,8 @@ class Case:
                      (k == nz - 1, 2, float(self.top_vz))]
         elif self.bc == "bottom_z":
             conds = [(k == 0, 2, 0.0)]
+        elif self.bc == "sym_xy":
+            conds = [(i == 0, 0, 0.0), (j == 0, 1, 0.0)]
         else:
             raise ValueError(self.bc)
         nodes, dims, vals, order = [], [], [], []
