@@ -126,8 +126,11 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
-def kernel_traffic(phase):
-    """DRAM bytes per launch from the committed ncu summary, if present."""
+def kernel_traffic(phase, workload, elements):
+    """DRAM bytes per launch of the full C2 mesh from the committed ncu summary,
+    if present; None for other workloads (no capture covers them)."""
+    if not (workload.startswith("C2") and elements == 256 * 256 * 128):
+        return None
     p = os.path.join(ROOT, "profiles", "kernel_traffic.txt")
     try:
         for ln in open(p):
@@ -178,6 +181,7 @@ def run_ours(args):
     stream = torch.cuda.ExternalStream(dm.stream_handle(), device=device)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     clocks = ClockSampler(device)
+    mode, cl_blocks, cl_bs = dm.step_mode()
     barrier()
     torch.cuda.synchronize(device)
     launches0 = dm.launch_count()
@@ -267,7 +271,7 @@ def run_ours(args):
     achieved = alg_bytes / (ms_phase[dom] * 1e-3) / 1e9
     roof = {"bound": "hbm", "kernel": KERNEL_NAMES[ph], "achieved": round(achieved, 1),
             "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
-            "frac": round(achieved / peak, 4), "traffic": kernel_traffic(ph),
+            "frac": round(achieved / peak, 4), "traffic": kernel_traffic(ph, case.name, E),
             "alg_bytes_per_launch": alg_bytes, "ms_per_launch": round(float(ms_phase[dom]), 4),
             "phases_ms": {p: round(float(m), 4) for p, m in zip(PHASES, ms_phase)}}
     step_alg = sum(alg_table[p][0] * E + alg_table[p][1] * case.n_node
@@ -298,6 +302,10 @@ def run_ours(args):
                     "includes": "mesh + BC upload, init, device CFL dt, K steps, "
                                 "displacement + reaction readback"},
             "gpu_launches": int(launches),
+            "step_mode": ({"mode": "one cluster launch per run", "cluster_blocks": cl_blocks,
+                           "block_size": cl_bs,
+                           "note": "roofline phases are the per-phase kernels, timed apart"}
+                          if mode == 2 else {"mode": "per-phase kernels, CUDA graph"}),
             "autotuned_launch": tuned,
             "launch_note": "items_per_thread 0 = persistent grid (SMs x resident blocks)",
             "roofline": roof,

@@ -195,7 +195,9 @@ WF_API wf_status wf_set_contact_plane(wf_domain *d, double z0, double vz, double
  * force after it leaves contact, the die velocity ramps as
  * sqrt(t / (0.01 end time)) over the first 1 % of the end time, and the
  * reaction history records the sum of normal-force magnitudes. This mesh is
- * rigid body 0; wf_add_contact_trimesh appends more. FP64 precision only. */
+ * rigid body 0; wf_add_contact_trimesh appends more. Both precisions: the
+ * mixed step evaluates the contact in FP32 with coordinates relative to the
+ * centre of the part's bounding box, the die kept in FP64. */
 WF_API wf_status wf_set_contact_trimesh(wf_domain *d, int64_t nnodes, const double *xyz,
                                         int64_t ntri, const int32_t *tri, const double vel[3],
                                         double mu_static, double mu_dynamic,
@@ -274,7 +276,7 @@ WF_API wf_status wf_set_launch_config(wf_domain *d, int32_t phase, int32_t block
  * phases: same per-element and per-node arithmetic, so the state is bitwise
  * that of mode 1; the reaction sum runs in another order. Not with specimens,
  * the energy history or phase timing. Mode 0 (default) picks mode 2 for
- * meshes of at most 8192 elements, else mode 1. wf_get_step_mode reports the
+ * meshes of at most 3000 elements, else mode 1. wf_get_step_mode reports the
  * mode the next wf_run uses and, for mode 2, the cluster's blocks and block
  * size (0 otherwise). */
 WF_API wf_status wf_set_step_mode(wf_domain *d, int32_t mode);

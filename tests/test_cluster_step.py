@@ -75,7 +75,7 @@ def test_automatic_mode_and_fallbacks():
     W.apply(d, case)
     d.init()
     assert d.step_mode()[0] == 1            # FP64 always runs per phase
-    big = W.config(0, scale=(24, 24, 16))   # 9216 elements: above the automatic limit
+    big = W.config(0, scale=(16, 16, 16))   # 4096 elements: above the automatic limit
     d = wf.Domain(wf.WF_MIXED)
     W.apply(d, big)
     d.init()

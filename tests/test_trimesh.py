@@ -4,7 +4,8 @@ The oracle's restatement of CalcContactForces is pinned bit-for-bit to the
 reference in tests/test_oracle.py (fixture tet_die_trimesh). Here the FP64
 GPU step with a moving die is checked against the oracle on the same inputs:
 displacements, contact forces, the reaction history and the die position,
-1e-9 relative (the reaction sum runs in a different order on the GPU).
+1e-9 relative (the reaction sum runs in a different order on the GPU). The
+mixed-precision contact is checked against the FP64 step.
 """
 import numpy as np
 import pytest
@@ -112,11 +113,68 @@ def test_two_rigid_bodies_match_oracle():
     assert d.trimesh_nodes().shape == (9 + 16, 3)
 
 
-@pytest.mark.gpu
-def test_trimesh_contact_needs_fp64():
-    case, die, _ = cases()["tet"]
-    d = wf.Domain(wf.WF_MIXED)
-    H.setup(d, case, {"die": die})
-    with pytest.raises(wf.WfError) as e:
+def off_grid(die, dx=1.1e-4, dy=7e-5):
+    """The die shifted so that no part node lies on a die edge. The
+    reference's inside test (crit < 0 rejects) decides a node that lies exactly
+    on an edge shared by two triangles by the sign of a rounding error: in
+    either precision it may find both triangles or neither, so runs that differ
+    by rounding are compared on dies whose edges avoid the part's nodes."""
+    d = dict(die)
+    d["start"] = [die["start"][0] + dx, die["start"][1] + dy, die["start"][2]]
+    return d
+
+
+def mixed_vs_fp64(case, extra, steps, mode=0):
+    out = []
+    for prec in (wf.WF_FP64, wf.WF_MIXED):
+        d = wf.Domain(prec)
+        H.setup(d, case, extra)
+        if prec == wf.WF_MIXED:
+            d.set_step_mode(mode)
         d.init()
-    assert e.value.status == 5
+        d.run(steps)
+        out.append(d)
+    return out
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["tet", "hex_hg"])
+def test_mixed_trimesh_contact_against_fp64(name):
+    """FP32 contact (coordinates relative to the part's centre, die kept in
+    FP64 and copied to FP32 after every move) against the FP64 step."""
+    case, die, steps = cases()[name]
+    f, m = mixed_vs_fp64(case, {"die": off_grid(die)}, steps)
+    eu = H.rel_err(m.node_vec("u"), f.node_vec("u"))
+    er = H.rel_err(m.reaction(), f.reaction())
+    print(f"{name}: mixed vs FP64 displacement {eu:.2e}, reaction {er:.2e}")
+    assert eu <= 1e-4 and er <= 1e-3
+    np.testing.assert_allclose(m.trimesh_nodes(), f.trimesh_nodes(), rtol=1e-12, atol=0)
+
+
+@pytest.mark.gpu
+def test_mixed_two_bodies_cluster_run_is_bitwise_the_graph_run():
+    """Two rigid bodies in mixed precision: the single-cluster run (die moved
+    by block 0) and the per-phase kernels give the same state bit for bit."""
+    case = W.config(1, scale=(3, 3, 4))
+    case.perturb = 0.1
+    case.seed = W.SEED_BASE + 13
+    case.bc = "sym_xy"
+    extra = {"die": off_grid(DIE_TET), "die2": off_grid(DIE_BOTTOM, 1.3e-4, -1.9e-4)}
+    runs = []
+    for mode in (1, 2):
+        d = wf.Domain(wf.WF_MIXED)
+        H.setup(d, case, extra)
+        d.set_step_mode(mode)
+        d.init()
+        assert d.step_mode()[0] == mode
+        d.run(150)
+        d.run(150)
+        runs.append(d)
+    a, b = runs
+    for f in ("u", "v", "contforce"):
+        np.testing.assert_array_equal(b.node_vec(f), a.node_vec(f), err_msg=f)
+    np.testing.assert_array_equal(b.trimesh_nodes(), a.trimesh_nodes())
+    assert H.rel_err(b.reaction(), a.reaction()) <= 1e-12
+    f, _ = mixed_vs_fp64(case, extra, 300)
+    assert H.rel_err(a.node_vec("u"), f.node_vec("u")) <= 1e-4
+    assert H.rel_err(a.reaction(), f.reaction()) <= 1e-3

@@ -44,6 +44,7 @@ def nvcc() -> str:
 def _sources():
     return [os.path.join(CSRC, u) for u in UNITS] + [
         os.path.join(CSRC, "wf_internal.cuh"), os.path.join(CSRC, "wf_adjoint.cuh"),
+        os.path.join(CSRC, "wf_trimesh.cuh"),
         os.path.join(ROOT, "include", "wf.h")]
 
 

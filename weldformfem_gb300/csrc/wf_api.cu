@@ -162,6 +162,7 @@ struct wf_domain {
   // launch per run; the cluster shape is found at init for small meshes
   int32_t step_mode = 0;
   int cl_blocks = 0, cl_bs = 0;
+  double *cl_part = nullptr;      // [kClusterChunk][cl_blocks] reaction partials
   // batched ensemble
   int32_t nspec = 0;
   std::vector<int64_t> spec_eoff, spec_noff;
@@ -942,7 +943,7 @@ wf_status autotune_launches(wf_domain *d) {
   const StepParams &P = d->P;
   MixState &M = d->M;
   const int64_t ne = d->ne, np = d->np;
-  std::vector<float> tau(6 * ne), pls(ne), ut(2 * np), cf(3 * np);
+  std::vector<float> tau(6 * ne), pls(ne), ut(3 * np), cf(3 * np);
   CUDA_TRY(cudaMemcpyAsync(tau.data(), M.tau, 4 * tau.size(), cudaMemcpyDeviceToHost, d->stream));
   CUDA_TRY(cudaMemcpyAsync(pls.data(), M.pls, 4 * pls.size(), cudaMemcpyDeviceToHost, d->stream));
   CUDA_TRY(cudaMemcpyAsync(ut.data(), M.ut, 4 * ut.size(), cudaMemcpyDeviceToHost, d->stream));
@@ -1017,7 +1018,8 @@ WF_API wf_status wf_set_launch_config(wf_domain *d, int32_t phase, int32_t block
 // cluster run can then be chosen by hand); up to kClusterAutoElems the
 // automatic mode uses it.
 constexpr int64_t kClusterMaxElems = 65536;
-constexpr int64_t kClusterAutoElems = 8192;
+constexpr int64_t kClusterAutoElems = 3000;
+constexpr int64_t kClusterChunk = 4096;   // steps per cluster launch
 
 namespace {
 // Whether the next wf_run of d runs as one cluster launch.
@@ -1068,8 +1070,6 @@ WF_API wf_status wf_init(wf_domain *d) {
   }
   if (d->nspec && d->contact)
     return fail(d, WF_ERR_UNSUPPORTED, "contact is not supported in a batched ensemble");
-  if (d->tri && d->precision != WF_FP64)
-    return fail(d, WF_ERR_UNSUPPORTED, "triangle-mesh contact runs in the FP64 step");
   if (d->nspec && d->energy)
     return fail(d, WF_ERR_UNSUPPORTED, "the energy history is not kept for a batched ensemble");
   CUDA_TRY(cudaSetDevice(d->device));
@@ -1329,7 +1329,35 @@ WF_API wf_status wf_init(wf_domain *d) {
     CUDA_TRY(dalloc(d, &M.vp, 3 * np));
     CUDA_TRY(dalloc(d, &M.pa, 3 * np));
     CUDA_TRY(dalloc(d, &M.cf, 3 * np));
-    CUDA_TRY(dalloc(d, &M.ut, 2 * np));
+    CUDA_TRY(dalloc(d, &M.ut, 3 * np));
+    CUDA_TRY(dalloc(d, &M.cfn, d->tri ? np : 1));
+    if (d->tri) {
+      // FP32 die copies relative to the centre of the part's bounding box
+      double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+      for (int64_t n = 0; n < nn; n++)
+        for (int k = 0; k < 3; k++) {
+          lo[k] = std::min(lo[k], d->x[3 * n + k]);
+          hi[k] = std::max(hi[k], d->x[3 * n + k]);
+        }
+      for (int k = 0; k < 3; k++) P.tri_ref[k] = 0.5 * (lo[k] + hi[k]);
+      std::vector<double> nrm, pp;
+      tri_normals_planes(d->tri_x, d->tri_el, nrm, pp);
+      const size_t tn = d->tri_x.size() / 3, te = d->tri_el.size() / 3;
+      std::vector<float> xf(3 * tn), nf(3 * te), ppf(te);
+      for (size_t i = 0; i < 3 * tn; i++) xf[i] = (float)(d->tri_x[i] - P.tri_ref[i % 3]);
+      for (size_t e = 0; e < te; e++) {
+        const double *p2 = &d->tri_x[3 * d->tri_el[3 * e + 2]];
+        double q = 0.0;
+        for (int k = 0; k < 3; k++) {
+          nf[3 * e + k] = (float)nrm[3 * e + k];
+          q += (p2[k] - P.tri_ref[k]) * nrm[3 * e + k];
+        }
+        ppf[e] = (float)q;
+      }
+      CUDA_TRY(upload(d, &P.tri_xf, xf));
+      CUDA_TRY(upload(d, &P.tri_nf, nf));
+      CUDA_TRY(upload(d, &P.tri_ppf, ppf));
+    }
     CUDA_TRY(dalloc(d, &M.mass, np));
     CUDA_TRY(dalloc(d, &M.jr, np));
     CUDA_TRY(dalloc(d, &M.nc, np));
@@ -1385,6 +1413,7 @@ WF_API wf_status wf_init(wf_domain *d) {
         if (mix_cluster_fits(P, M, d->mvol, blocks, bs) >= 1) {
           d->cl_blocks = blocks;
           d->cl_bs = bs;
+          CUDA_TRY(dalloc(d, &d->cl_part, (size_t)kClusterChunk * blocks));
           break;
         }
       }
@@ -1577,8 +1606,9 @@ WF_API wf_status wf_run(wf_domain *d, int64_t nsteps) {
   if (cluster_mode(d)) {
     // one launch per chunk of steps (kernels stay short)
     while (left > 0) {
-      const int64_t chunk = std::min<int64_t>(left, 4096);
-      CUDA_TRY(mix_cluster_run(d->P, d->M, d->mvol, chunk, d->cl_blocks, d->cl_bs, d->stream));
+      const int64_t chunk = std::min<int64_t>(left, kClusterChunk);
+      CUDA_TRY(mix_cluster_run(d->P, d->M, d->mvol, d->cl_part, chunk, d->cl_blocks, d->cl_bs,
+                               d->stream));
       d->launches += 1;
       left -= chunk;
     }

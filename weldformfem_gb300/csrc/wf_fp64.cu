@@ -13,6 +13,7 @@
 //                        Chung-Hulbert corrector, position update and the
 //                        next step's predictor; reaction sum (last block).
 #include "wf_internal.cuh"
+#include "wf_trimesh.cuh"
 
 namespace wf {
 namespace {
@@ -556,37 +557,6 @@ __device__ __forceinline__ double tri_contact(const StepParams &P, const Fp64Sta
   return cfn;
 }
 
-// End of the loop body (Solver_explicit.C:980-1004), run by the last block of
-// the node kernel once every node has been updated: the die velocity ramps as
-// sqrt(Time / (0.01 end_t)) over the first 1 % of the end time, the mesh moves
-// by v dt, and normals and plane coefficients are recomputed (far node 2).
-__device__ void tri_move(const StepParams &P, double time) {
-  const double rf = 1.0e-2;
-  double f = 1.0;
-  if (time < rf * P.end_t) f = pow(time / (rf * P.end_t), 0.5);
-  for (int32_t i = threadIdx.x; i < 3 * P.tri_nn; i += blockDim.x) {
-    const double vk = f * P.tri_v[i];
-    P.tri_x[i] = P.tri_x[i] + vk * P.dt;
-  }
-  __syncthreads();
-  for (int32_t e = threadIdx.x; e < P.tri_ne; e += blockDim.x) {
-    const double *p0 = &P.tri_x[3 * P.tri_el[3 * e]];
-    const double *p1 = &P.tri_x[3 * P.tri_el[3 * e + 1]];
-    const double *p2 = &P.tri_x[3 * P.tri_el[3 * e + 2]];
-    const double u[3] = {p1[0] - p0[0], p1[1] - p0[1], p1[2] - p0[2]};
-    const double w0[3] = {p2[0] - p0[0], p2[1] - p0[1], p2[2] - p0[2]};
-    const double w[3] = {u[1] * w0[2] - u[2] * w0[1], u[2] * w0[0] - u[0] * w0[2],
-                         u[0] * w0[1] - u[1] * w0[0]};
-    const double len = sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
-    const double inv = 1.0 / len;
-    const double nn0 = w[0] * inv, nn1 = w[1] * inv, nn2 = w[2] * inv;
-    P.tri_nrm[3 * e] = nn0;
-    P.tri_nrm[3 * e + 1] = nn1;
-    P.tri_nrm[3 * e + 2] = nn2;
-    P.tri_pp[e] = p2[0] * nn0 + p2[1] * nn1 + p2[2] * nn2;
-  }
-}
-
 // nodes: assemblyForces (Matrices.C:42-87) as a gather over the node's
 // element list, the non-finite clamp (Solver_explicit.C:777-785), plane
 // contact (Contact.C:58-323), calcAccel (Mechanical.C:321-341), ImposeBCA,
@@ -733,7 +703,7 @@ __global__ void __launch_bounds__(kNodeThreads) k_fp64_nodes(StepParams P, Fp64S
       P.st->time = time + P.dt;
       P.st->done_blocks = 0u;
     }
-    if (P.tri_on) tri_move(P, time);
+    if (P.tri_on) tri_move<false>(P, time);
   }
 }
 

@@ -101,7 +101,7 @@ struct StepParams {
   double *partials;       // [grid of the node kernel]
   double *hist;           // [hist_cap]
   int64_t hist_cap;
-  // rigid triangle-mesh contact (FP64 path; one mesh with a uniform velocity)
+  // rigid triangle-mesh contact (bodies concatenated; velocity per die node)
   int32_t tri_on;
   int32_t tri_nn, tri_ne;
   double *tri_x;            // [3 tri_nn] node positions, moved every step
@@ -113,6 +113,11 @@ struct StepParams {
   const double *node_area;  // [nn] external-surface area share of each node
   const double *nodlen;     // [nn] mean element length at each node
   double tri_mu_s, tri_mu_d, tri_pf, tri_E0, end_t;
+  // FP32 copies for the mixed-precision contact, relative to tri_ref
+  float *tri_xf;            // [3 tri_nn]
+  float *tri_nf;            // [3 tri_ne]
+  float *tri_ppf;           // [tri_ne] n . (p2 - tri_ref)
+  double tri_ref[3];
   // energy history (Domain_d::computeEnergies after every step), when on
   int32_t energy_on;
   double *epart;          // [2 * grid of the energy kernel]
@@ -136,7 +141,8 @@ struct Fp64State {
 struct MixState {
   float2 *xh;                     // [3][np] (hi, lo)
   float *v, *vp, *pa;             // [3][np]
-  float *cf, *ut;                 // [3][np], [2][np] contact force / slip
+  float *cf, *ut;                 // [3][np], [3][np] contact force / slip
+  float *cfn;                     // [np] reaction share of the step (triangle-mesh contact)
   float *mass, *jr;               // [np]
   float2 *nc;                     // [np] (1 / sum of initial volumes, mean density)
   float *pls;                     // [ne]
@@ -183,8 +189,9 @@ void mix_predict(const StepParams &P, const MixState &M, cudaStream_t st);
 // threads (64, 128 or 256), for small meshes; mix_cluster_fits returns how
 // many such clusters can be resident (0: the shape cannot launch).
 int mix_cluster_fits(const StepParams &P, const MixState &M, float *vol, int blocks, int bs);
-cudaError_t mix_cluster_run(const StepParams &P, const MixState &M, float *vol, int64_t nsteps,
-                            int blocks, int bs, cudaStream_t st);
+// part: [nsteps][blocks] staging for the reaction's block partials.
+cudaError_t mix_cluster_run(const StepParams &P, const MixState &M, float *vol, double *part,
+                            int64_t nsteps, int blocks, int bs, cudaStream_t st);
 void mix_export(const StepParams &P, const MixState &M, const Fp64State &S, const float *vol,
                 cudaStream_t st);
 int mix_node_grid(int64_t nn);

@@ -20,6 +20,7 @@
 #include <utility>
 
 #include "wf_internal.cuh"
+#include "wf_trimesh.cuh"
 
 namespace wf {
 namespace {
@@ -161,6 +162,86 @@ __global__ void __launch_bounds__(BS) k_mix_geometry(StepParams P, MixState M, f
     geometry_one<NPE, false>(P, M, vol, e);
 }
 
+// Rigid triangle-mesh contact of one external node in FP32 (the FP64 step's
+// CalcContactForces restatement, Contact.C:31-334): coordinates relative to
+// P.tri_ref; the first triangle, in order, that the node penetrates with its
+// projection inside gives the penalty normal force
+// pf * min(E A / l, 0.2 m / dt^2) * d, 20 % critical damping and Coulomb
+// friction from the accumulated slip. A node out of contact keeps its last
+// contact force. The node's reaction share (normal-force magnitude, rigid
+// body 0 only) goes to M.cfn.
+template <bool CG>
+__device__ __forceinline__ void tri_contact_mixed(const StepParams &P, const MixState &M,
+                                                  int64_t n, float mass) {
+  const int64_t np = P.np;
+  float x[3], v[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const float2 h = M.xh[k * np + n];
+    x[k] = (float)(((double)h.x + (double)h.y) - P.tri_ref[k]);
+    v[k] = M.vp[k * np + n];
+  }
+  float cfn = 0.f;
+  for (int32_t j = 0; j < P.tri_ne; j++) {
+    const float n0 = ldx<CG>(&P.tri_nf[3 * j]), n1 = ldx<CG>(&P.tri_nf[3 * j + 1]),
+                n2 = ldx<CG>(&P.tri_nf[3 * j + 2]);
+    const float dd = (n0 * x[0] + n1 * x[1] + n2 * x[2]) - ldx<CG>(&P.tri_ppf[j]);
+    if (!(dd < 0.f)) continue;
+    const float Q[3] = {x[0] - n0 * dd, x[1] - n1 * dd, x[2] - n2 * dd};
+    bool inside = true;
+    for (int l = 0; l < 3 && inside; l++) {
+      const int nx = l + 1 > 2 ? 0 : l + 1;
+      const int32_t ia = 3 * __ldg(&P.tri_el[3 * j + l]), ib = 3 * __ldg(&P.tri_el[3 * j + nx]);
+      const float a0 = ldx<CG>(&P.tri_xf[ia]), a1 = ldx<CG>(&P.tri_xf[ia + 1]),
+                  a2 = ldx<CG>(&P.tri_xf[ia + 2]);
+      const float e1[3] = {ldx<CG>(&P.tri_xf[ib]) - a0, ldx<CG>(&P.tri_xf[ib + 1]) - a1,
+                           ldx<CG>(&P.tri_xf[ib + 2]) - a2};
+      const float e2[3] = {Q[0] - a0, Q[1] - a1, Q[2] - a2};
+      const float crit = (e1[1] * e2[2] - e1[2] * e2[1]) * n0 +
+                         (e1[2] * e2[0] - e1[0] * e2[2]) * n1 +
+                         (e1[0] * e2[1] - e1[1] * e2[0]) * n2;
+      if (crit < 0.f) inside = false;
+    }
+    if (!inside) continue;
+    const float dt = P.f_dt;
+    const float v_reln = v[0] * n0 + v[1] * n1 + v[2] * n2;
+    const float kgeo = (float)(P.tri_E0 * P.node_area[n] / P.nodlen[n]);
+    const float kmass = 0.2f * mass / (dt * dt);
+    const float k = (kmass < kgeo) ? kmass : kgeo;
+    const float ccrit = 2.0f * mass * sqrtf(k / mass);
+    const float sc = -((float)P.tri_pf * k * dd + 0.2f * ccrit * v_reln);
+    float cf[3] = {n0 * sc, n1 * sc, n2 * sc};
+    const float cfn_j = sqrtf(cf[0] * cf[0] + cf[1] * cf[1] + cf[2] * cf[2]);
+    // friction from the accumulated tangential slip
+    const float vt[3] = {v[0] - n0 * v_reln, v[1] - n1 * v_reln, v[2] - n2 * v_reln};
+    float ut[3];
+#pragma unroll
+    for (int q = 0; q < 3; q++) ut[q] = M.ut[q * np + n] + vt[q] * dt;
+    const float ft[3] = {-k * ut[0], -k * ut[1], -k * ut[2]};
+    const float ft_mag = sqrtf(ft[0] * ft[0] + ft[1] * ft[1] + ft[2] * ft[2]);
+    const float fn_norm = fabsf(cf[0] * n0 + cf[1] * n1 + cf[2] * n2);
+    float F[3] = {ft[0], ft[1], ft[2]};
+    if (!(ft_mag <= (float)P.tri_mu_s * fn_norm)) {
+      // sliding: dynamic friction along -v_t (none when v_t vanishes)
+      const float vtn = sqrtf(vt[0] * vt[0] + vt[1] * vt[1] + vt[2] * vt[2]);
+      const float md = vtn > 0.f ? -((float)P.tri_mu_d * fn_norm) / vtn : 0.f;
+#pragma unroll
+      for (int q = 0; q < 3; q++) {
+        F[q] = vt[q] * md;
+        ut[q] = 0.f;
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+      M.ut[q * np + n] = ut[q];
+      M.cf[q * np + n] = cf[q] + F[q];
+    }
+    if (__ldg(&P.tri_mid[j]) == 0) cfn = cfn_j;
+    break;
+  }
+  M.cfn[n] = cfn;
+}
+
 // Nodal volumes -> J ratio and lumped mass; for contact candidates also the
 // rigid-plane contact force (it needs only x, the predicted velocity and the
 // step's mass, all final here, so it is computed before the element phase).
@@ -188,7 +269,9 @@ __device__ __forceinline__ void nodal_one(const StepParams &P, const MixState &M
   } else {
     mass = M.mass[n];
   }
-  if (P.contact && (P.nflag[n] & NF_CONTACT)) {
+  if (P.tri_on) {
+    if (P.nflag[n] & NF_CONTACT) tri_contact_mixed<CG>(P, M, n, mass);
+  } else if (P.contact && (P.nflag[n] & NF_CONTACT)) {
     // rigid plane, outward normal (0, 0, -1), at z0 + vz * Time
     // (Domain_d::CalcContactForces, Contact.C:58-323, one plane)
     const int64_t np = P.np;
@@ -627,7 +710,7 @@ __device__ __forceinline__ float node_one(const StepParams &P, const MixState &M
     cf[0] = M.cf[n];
     cf[1] = M.cf[np + n];
     cf[2] = M.cf[2 * np + n];
-    r = fabsf(cf[2]);
+    r = P.tri_on ? M.cfn[n] : fabsf(cf[2]);
   }
   if (!P.contact && (fl & NF_REACTION)) {
     if (P.rnode)
@@ -683,6 +766,7 @@ __global__ void __launch_bounds__(kNodeThreads, 6) k_mix_nodes(StepParams P, Mix
   __syncthreads();
   if (am_last) {
     __threadfence();
+    const double time = P.st->time;
     double t = 0.0;
     for (unsigned i = threadIdx.x; i < gridDim.x; i += blockDim.x)
       t += ((volatile double *)P.partials)[i];
@@ -691,9 +775,10 @@ __global__ void __launch_bounds__(kNodeThreads, 6) k_mix_nodes(StepParams P, Mix
       const long long s = P.st->step;
       if (s < P.hist_cap) P.hist[s] = tot;
       P.st->step = s + 1;
-      P.st->time = P.st->time + P.dt;
+      P.st->time = time + P.dt;
       P.st->done_blocks = 0u;
     }
+    if (P.tri_on) tri_move<true>(P, time);
   }
 }
 
@@ -706,8 +791,9 @@ __global__ void __launch_bounds__(kNodeThreads, 6) k_mix_nodes(StepParams P, Mix
 // velocities, volumes, volume ratios, element forces) is loaded through L2.
 // Each element and node is updated with the same arithmetic as in the
 // per-phase kernels; the reaction is summed per thread and per block (FP64)
-// and block 0 adds the block partials after the step's last barrier, so its
-// summation order differs from the per-phase node kernel's.
+// into a [steps][blocks] staging array whose rows block 0 adds in block order
+// at the end of the launch, so its summation order differs from the
+// per-phase node kernel's.
 __device__ __forceinline__ void cluster_barrier() {
   asm volatile("barrier.cluster.arrive.release.aligned;\n" ::: "memory");
   asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory");
@@ -715,7 +801,7 @@ __device__ __forceinline__ void cluster_barrier() {
 
 template <int NPE, int BS, int LAW>
 __global__ void __launch_bounds__(BS) k_mix_cluster_run(StepParams P, MixState M, float *vol,
-                                                        int64_t nsteps) {
+                                                        double *part, int64_t nsteps) {
   __shared__ float stash[NPE == 8 ? 12 * BS : 1];
   __shared__ double sh[BS / 32];
   const int64_t nb = gridDim.x, b = blockIdx.x;
@@ -723,7 +809,7 @@ __global__ void __launch_bounds__(BS) k_mix_cluster_run(StepParams P, MixState M
   const int64_t e0 = P.ne * b / nb, e1 = P.ne * (b + 1) / nb;
   const int64_t n0 = P.nn * b / nb, n1 = P.nn * (b + 1) / nb;
   double time = __ldcg(&P.st->time);
-  long long step = __ldcg(&P.st->step);
+  const long long step0 = __ldcg(&P.st->step);
   for (int64_t it = 0; it < nsteps; it++) {
     for (int64_t e = e0 + t; e < e1; e += BS) geometry_one<NPE, true>(P, M, vol, e);
     cluster_barrier();
@@ -734,20 +820,23 @@ __global__ void __launch_bounds__(BS) k_mix_cluster_run(StepParams P, MixState M
     cluster_barrier();
     double r = 0.0;
     for (int64_t n = n0 + t; n < n1; n += BS) r += (double)node_one<NPE, true>(P, M, n);
-    const double part = block_sum_dense(r, sh);
-    if (t == 0) P.partials[b] = part;
+    const double bsum = block_sum_dense(r, sh);
+    if (t == 0) part[it * nb + b] = bsum;   // step it, block b
     cluster_barrier();
-    if (b == 0 && t == 0) {
-      double tot = 0.0;
-      for (int64_t i = 0; i < nb; i++) tot += __ldcg(&P.partials[i]);
-      if (step < P.hist_cap) P.hist[step] = tot;
-    }
-    step++;
+    if (b == 0 && P.tri_on) tri_move<true>(P, time);
     time = time + P.dt;
   }
-  if (b == 0 && t == 0) {
-    P.st->step = step;
-    P.st->time = time;
+  // reaction history: block partials of each step added in block order
+  if (b == 0) {
+    for (int64_t it = t; it < nsteps; it += BS) {
+      double tot = 0.0;
+      for (int64_t i = 0; i < nb; i++) tot += __ldcg(&part[it * nb + i]);
+      if (step0 + it < P.hist_cap) P.hist[step0 + it] = tot;
+    }
+    if (t == 0) {
+      P.st->step = step0 + nsteps;
+      P.st->time = time;
+    }
   }
 }
 
@@ -946,8 +1035,8 @@ void launch_elements(const StepParams &P, const MixState &M, cudaStream_t st, La
 }
 
 template <int NPE, int BS, int LAW>
-cudaError_t cluster_launch(const StepParams &P, const MixState &M, float *vol, int64_t nsteps,
-                           int blocks, cudaStream_t st, bool query, int *fits) {
+cudaError_t cluster_launch(const StepParams &P, const MixState &M, float *vol, double *part,
+                           int64_t nsteps, int blocks, cudaStream_t st, bool query, int *fits) {
   auto kern = k_mix_cluster_run<NPE, BS, LAW>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
   if (e != cudaSuccess) return e;
@@ -969,29 +1058,33 @@ cudaError_t cluster_launch(const StepParams &P, const MixState &M, float *vol, i
     *fits = (e == cudaSuccess) ? n : 0;
     return e;
   }
-  return cudaLaunchKernelEx(&cfg, kern, P, M, vol, nsteps);
+  return cudaLaunchKernelEx(&cfg, kern, P, M, vol, part, nsteps);
 }
 
 template <int NPE, int LAW>
-cudaError_t cluster_dispatch_bs(const StepParams &P, const MixState &M, float *vol,
+cudaError_t cluster_dispatch_bs(const StepParams &P, const MixState &M, float *vol, double *part,
                                 int64_t nsteps, int blocks, int bs, cudaStream_t st, bool query,
                                 int *fits) {
   switch (bs) {
-    case 64: return cluster_launch<NPE, 64, LAW>(P, M, vol, nsteps, blocks, st, query, fits);
-    case 128: return cluster_launch<NPE, 128, LAW>(P, M, vol, nsteps, blocks, st, query, fits);
-    default: return cluster_launch<NPE, 256, LAW>(P, M, vol, nsteps, blocks, st, query, fits);
+    case 64:
+      return cluster_launch<NPE, 64, LAW>(P, M, vol, part, nsteps, blocks, st, query, fits);
+    case 128:
+      return cluster_launch<NPE, 128, LAW>(P, M, vol, part, nsteps, blocks, st, query, fits);
+    default:
+      return cluster_launch<NPE, 256, LAW>(P, M, vol, part, nsteps, blocks, st, query, fits);
   }
 }
 
-cudaError_t cluster_dispatch(const StepParams &P, const MixState &M, float *vol, int64_t nsteps,
-                             int blocks, int bs, cudaStream_t st, bool query, int *fits) {
+cudaError_t cluster_dispatch(const StepParams &P, const MixState &M, float *vol, double *part,
+                             int64_t nsteps, int blocks, int bs, cudaStream_t st, bool query,
+                             int *fits) {
   if (P.npe == 8)
     return P.mat_general
-               ? cluster_dispatch_bs<8, 1>(P, M, vol, nsteps, blocks, bs, st, query, fits)
-               : cluster_dispatch_bs<8, 0>(P, M, vol, nsteps, blocks, bs, st, query, fits);
+               ? cluster_dispatch_bs<8, 1>(P, M, vol, part, nsteps, blocks, bs, st, query, fits)
+               : cluster_dispatch_bs<8, 0>(P, M, vol, part, nsteps, blocks, bs, st, query, fits);
   return P.mat_general
-             ? cluster_dispatch_bs<4, 1>(P, M, vol, nsteps, blocks, bs, st, query, fits)
-             : cluster_dispatch_bs<4, 0>(P, M, vol, nsteps, blocks, bs, st, query, fits);
+             ? cluster_dispatch_bs<4, 1>(P, M, vol, part, nsteps, blocks, bs, st, query, fits)
+             : cluster_dispatch_bs<4, 0>(P, M, vol, part, nsteps, blocks, bs, st, query, fits);
 }
 
 }  // namespace
@@ -1023,16 +1116,16 @@ void mix_nodes(const StepParams &P, const MixState &M, cudaStream_t st, int node
 
 int mix_cluster_fits(const StepParams &P, const MixState &M, float *vol, int blocks, int bs) {
   int fits = 0;
-  if (cluster_dispatch(P, M, vol, 0, blocks, bs, nullptr, true, &fits) != cudaSuccess) {
+  if (cluster_dispatch(P, M, vol, nullptr, 0, blocks, bs, nullptr, true, &fits) != cudaSuccess) {
     cudaGetLastError();
     return 0;
   }
   return fits;
 }
 
-cudaError_t mix_cluster_run(const StepParams &P, const MixState &M, float *vol, int64_t nsteps,
-                            int blocks, int bs, cudaStream_t st) {
-  return cluster_dispatch(P, M, vol, nsteps, blocks, bs, st, false, nullptr);
+cudaError_t mix_cluster_run(const StepParams &P, const MixState &M, float *vol, double *part,
+                            int64_t nsteps, int blocks, int bs, cudaStream_t st) {
+  return cluster_dispatch(P, M, vol, part, nsteps, blocks, bs, st, false, nullptr);
 }
 
 void mix_predict(const StepParams &P, const MixState &M, cudaStream_t st) {
