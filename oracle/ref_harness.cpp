@@ -71,6 +71,7 @@ class RefDomain : public Domain_d {
   double eint_acc = 0.0;
   TriMesh_d *tm = nullptr;                  // rigid triangle mesh (contact)
   double temp = 0.0;                        // uniform temperature T[]
+  bool thermal_on = false;
   std::vector<double3> v_orig;              // its velocity before the ramp
 
   // A TriMesh_d filled from arrays: one mesh with the given id, uniform
@@ -106,6 +107,7 @@ class RefDomain : public Domain_d {
     m->m_v = make_double3(vel[0], vel[1], vel[2]);
     m->react_force[0] = make_double3(0., 0., 0.);
     m->heat_cond = 0.0;
+    m->T_const = 20.;  // main.C:714
     m->CalcCentroids();
     m->CalcNormals();
     m->CalcSpheres();
@@ -146,6 +148,10 @@ class RefDomain : public Domain_d {
     for (int e = 0; e < m_elem_count; e++) { p[e] = 0.0; pl_strain[e] = 0.0; }
     m_artifvisc[0] = 0.0;
     m_artifvisc[1] = 0.0;
+    // thermal arrays, also read before they are first written
+    for (int i = 0; i < m_elem_count * m_nodxelem; i++) m_dTedt[i] = 0.0;
+    for (int e = 0; e < m_elem_count * m_gp_count; e++) m_q_plheat[e] = 0.0;
+    for (int n = 0; n < m_node_count; n++) q_cont_conv[n] = 0.0;
   }
 
   // Preamble of SolveChungHulbert (Solver_explicit.C:120-268), CPU branch.
@@ -170,6 +176,7 @@ class RefDomain : public Domain_d {
     for (int n = 0; n < m_node_count; n++)
       for (int d = 0; d < m_dim; d++) ut_prev[m_dim * n + d] = 0.0;
     for (int n = 0; n < m_node_count; n++) T[n] = temp;
+    if (thermal_on) setThermalOn();  // main.C:435-441 (setTemp is the loop above)
     if (tm) {
       // what main.C does before the solve (main.C:647-650, :862-873)
       setTriMesh(tm);
@@ -225,6 +232,7 @@ class RefDomain : public Domain_d {
         dep = dgamma;
       }
       Sigma = -p[offset_s] * Identity() + ShearStress;
+      if (m_thermal) m_q_plheat[e] = 0.0;
       if (dep > 0.0) {
         double f = dep / sigma_y[e];
         Strain_pl_incr.xx = f * (Sigma.xx - 0.5 * (Sigma.yy + Sigma.zz));
@@ -233,6 +241,13 @@ class RefDomain : public Domain_d {
         Strain_pl_incr.xy = Strain_pl_incr.yx = 1.5 * f * (Sigma.xy);
         Strain_pl_incr.xz = Strain_pl_incr.zx = 1.5 * f * (Sigma.xz);
         Strain_pl_incr.yz = Strain_pl_incr.zy = 1.5 * f * (Sigma.yz);
+        if (m_thermal) {  // Mechanical.C:1797-1810
+          tensor3 depdt = 1. / dt_ * Strain_pl_incr;
+          m_q_plheat[e] = m_plheatfraction *
+                          (Sigma.xx * depdt.xx + 2.0 * Sigma.xy * depdt.yx +
+                           2.0 * Sigma.xz * depdt.zx + Sigma.yy * depdt.yy +
+                           2.0 * Sigma.yz * depdt.yz + Sigma.zz * depdt.zz);
+        }
       }
       Strain = Strain + dt_ * StrRate;
       ToFlatSymPtr(Sigma, m_sigma, offset_t);
@@ -276,6 +291,7 @@ class RefDomain : public Domain_d {
     CalcNodalVol();
     CalcNodalMassFromVol();
     calcElemStrainRates();
+    if (m_thermal) calcThermalExpansion();  // Solver_explicit.C:719-720
     if (m_press_algorithm == 0)
       calcElemPressure();
     else if (m_press_algorithm == 1)
@@ -315,6 +331,7 @@ class RefDomain : public Domain_d {
       tm->CalcNormals();
       tm->UpdatePlaneCoeff();
     }
+    if (m_thermal) ThermalCalcs();  // Solver_explicit.C:1008-1011
     // end of the loop body (Solver_explicit.C:1029-1031)
     double ekin = 0.0, deint = 0.0, devisc = 0.0;
     computeEnergies(dt, ekin, deint, devisc);
@@ -342,6 +359,7 @@ class RefDomain : public Domain_d {
       case 0: return m_mdiag;
       case 1: return m_voln;
       case 2: return p_node;
+      case 3: return T;
       default: return nullptr;
     }
   }
@@ -510,6 +528,30 @@ void wfr_set_johnson_cook(void *h, int mat, double B, double n, double C, double
   d->temp = T;
   // AssignMaterial copies material 0 into the domain (Domain_d.C:903-907)
   if (mat == 0) d->AssignMaterial(&d->mats[0]);
+}
+
+// Thermal coupling as the JSON driver sets it (main.C:424-441): every node at T0.
+void wfr_set_thermal(void *h, int on, double T0) {
+  RefDomain *d = static_cast<RefDomain *>(h);
+  d->thermal_on = on != 0;
+  d->temp = T0;
+}
+// Material thermal constants (main.C:575-577) on material `mat`, re-assigned
+// because AssignMaterial copies material 0.
+void wfr_set_material_thermal(void *h, int mat, double k_T, double cp_T, double exp_T) {
+  RefDomain *d = static_cast<RefDomain *>(h);
+  d->mats[mat].k_T = k_T;
+  d->mats[mat].cp_T = cp_T;
+  d->mats[mat].exp_T = exp_T;
+  if (mat == 0) d->AssignMaterial(&d->mats[0]);
+}
+// Die heat transfer (main.C:714-719): TriMesh_d heat_cond and T_const.
+void wfr_set_contact_heat(void *h, double heat_cond, double T_die) {
+  RefDomain *d = static_cast<RefDomain *>(h);
+  if (d->tm) {
+    d->tm->heat_cond = heat_cond;
+    d->tm->T_const = T_die;
+  }
 }
 
 void wfr_set_elem_materials(void *h, const int *ids) {

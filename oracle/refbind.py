@@ -61,6 +61,9 @@ def lib():
         "wfr_time": ([vp], C.c_double),
         "wfr_solve_verbatim": ([vp], None),
         "wfr_get_node_vec": ([vp, C.c_int, _dp], C.c_int),
+        "wfr_set_thermal": ([vp, C.c_int, C.c_double], None),
+        "wfr_set_material_thermal": ([vp, C.c_int, C.c_double, C.c_double, C.c_double], None),
+        "wfr_set_contact_heat": ([vp, C.c_double, C.c_double], None),
         "wfr_get_node_scalar": ([vp, C.c_int, _dp], C.c_int),
         "wfr_get_elem_scalar": ([vp, C.c_int, _dp], C.c_int),
         "wfr_get_elem_tensor": ([vp, C.c_int, _dp], C.c_int),
@@ -105,7 +108,7 @@ class _Silence:
 
 
 NODE_VEC = {"x": 0, "v": 1, "a": 2, "u": 3, "prev_a": 4, "fi": 5, "u_dt": 6}
-NODE_SCALAR = {"mass": 0, "voln": 1, "p_node": 2}
+NODE_SCALAR = {"mass": 0, "voln": 1, "p_node": 2, "T": 3}
 ELEM_SCALAR = {"vol": 0, "vol0": 1, "detJ": 2, "p": 3, "pl_strain": 4, "sigma_y": 5, "rho": 6}
 ELEM_TENSOR = {"sigma": 0, "tau": 1, "eps": 2, "str_rate": 3, "rot_rate": 4}
 
@@ -292,6 +295,15 @@ class RefDomain:
         out = np.zeros(self.nn * 3)
         lib().wfr_get_node_vec(self.h, NODE_VEC[name], out)
         return out.reshape(-1, 3)
+
+    def set_thermal(self, on=True, T0=20.0):
+        lib().wfr_set_thermal(self.h, int(bool(on)), float(T0))
+
+    def set_material_thermal(self, mat, k_T, cp_T, exp_T=0.0):
+        lib().wfr_set_material_thermal(self.h, int(mat), float(k_T), float(cp_T), float(exp_T))
+
+    def set_contact_heat(self, heat_cond, T_die=20.0):
+        lib().wfr_set_contact_heat(self.h, float(heat_cond), float(T_die))
 
     def node_scalar(self, name):
         out = np.zeros(self.nn)

@@ -24,6 +24,8 @@ typedef struct {
   /* Johnson-Cook (Material_::Init_JohnsonCook, Material.cuh:105-114) and the
    * element temperature it reads (uniform here) */
   double jc_B, jc_n, jc_C, jc_eps0, jc_m, jc_Tm, jc_Tt, jc_T;
+  /* thermal constants (Material_ k_T, cp_T, exp_T, Material.cuh:81-83) */
+  double k_T, cp_T, exp_T;
 } mat_t;
 
 struct wfo_domain {
@@ -70,6 +72,12 @@ struct wfo_domain {
   double tri_mu_s, tri_mu_d, tri_pf;
   uint8_t *ext;
   double *node_area, *nodlen, *elem_len;
+  /* thermal coupling (Thermal.C): nodal temperature, plastic heat per element,
+   * element-node temperature rates, contact heat per node */
+  int thermal;
+  double T0;
+  double *T, *q_plheat, *dTedt, *q_cont;
+  double heat_cond, T_die;
   int64_t step_count;
 };
 
@@ -87,6 +95,7 @@ wfo_domain *wfo_create(void) {
   d->react_dim = 2;
   d->c_mu = 0.0;
   d->nthreads = 0;
+  d->T_die = 20.0;  /* TriMesh_d T_const as the driver sets it (main.C:714) */
   return d;
 }
 
@@ -105,7 +114,8 @@ static void free_mesh(wfo_domain *d) {
                    (void **)&d->pl_incr, (void **)&d->f_elem, (void **)&d->f_hg,
                    (void **)&d->elem_mat, (void **)&d->cand, (void **)&d->cfn,
                    (void **)&d->ext, (void **)&d->node_area, (void **)&d->nodlen,
-                   (void **)&d->elem_len};
+                   (void **)&d->elem_len, (void **)&d->T, (void **)&d->q_plheat,
+                   (void **)&d->dTedt, (void **)&d->q_cont};
   for (size_t i = 0; i < sizeof(ptrs) / sizeof(ptrs[0]); i++) {
     free(*ptrs[i]);
     *ptrs[i] = NULL;
@@ -172,6 +182,8 @@ static int alloc_mesh(wfo_domain *d, int64_t nn, int64_t ne, int npe) {
   d->str_rate = xcalloc(e6, 8); d->rot_rate = xcalloc(e6, 8); d->pl_incr = xcalloc(e6, 8);
   d->f_elem = xcalloc(ea * 3, 8); d->f_hg = xcalloc(ea * 3, 8);
   d->cand = xcalloc(nn, 1); d->cfn = xcalloc(nn, 8);
+  d->T = xcalloc(nn, 8); d->q_plheat = xcalloc(ne, 8); d->dTedt = xcalloc(ea, 8);
+  d->q_cont = xcalloc(nn, 8);
   return 0;
 }
 
@@ -809,8 +821,8 @@ static void t3_scaled_identity(double s, double *r) {
 
 /* CalcHollomonYieldStress / CalcHollomonTangentModulus (Material.cuh:353-395). */
 /* CalcJohnsonCookYieldStress (Material.cuh:377-392). */
-static double jc_sy(double strain, double strain_rate, const mat_t *m) {
-  double T_h = (m->jc_T - m->jc_Tt) / (m->jc_Tm - m->jc_Tt);
+static double jc_sy(double strain, double strain_rate, const mat_t *m, double temp) {
+  double T_h = (temp - m->jc_Tt) / (m->jc_Tm - m->jc_Tt);
   double sr = strain_rate;
   if (strain_rate == 0.0) sr = 1.e-5;
   return (m->sy0 + m->jc_B * pow(strain, m->jc_n)) * (1.0 + m->jc_C * log(sr / m->jc_eps0)) *
@@ -818,8 +830,8 @@ static double jc_sy(double strain, double strain_rate, const mat_t *m) {
 }
 
 /* CalcJohnsonCookTangentModulus (Material.cuh:397-410). */
-static double jc_et(double plstrain, double strain_rate, const mat_t *m) {
-  double T_h = (m->jc_T - m->jc_Tt) / (m->jc_Tm - m->jc_Tt);
+static double jc_et(double plstrain, double strain_rate, const mat_t *m, double temp) {
+  double T_h = (temp - m->jc_Tt) / (m->jc_Tm - m->jc_Tt);
   double Et = 0.;
   if (plstrain > 0.)
     Et = m->jc_n * m->jc_B * pow(plstrain, m->jc_n - 1.) *
@@ -880,8 +892,17 @@ static void calc_stress_strain(wfo_domain *d) {
                              (SR[YY] - SR[ZZ]) * (SR[YY] - SR[ZZ]) +
                              (SR[ZZ] - SR[XX]) * (SR[ZZ] - SR[XX])) +
                       3.0 * (SR[XY] * SR[XY] + SR[YZ] * SR[YZ] + SR[XZ] * SR[XZ]));
+    /* Johnson-Cook temperature: the material's (uniform) temperature, or
+     * with thermal coupling the mean of the element's node temperatures (the
+     * reference reads T[e], a node array indexed by element) */
+    double temp = m->jc_T;
+    if (d->thermal && m->model == 2) {
+      double ts = 0.0;
+      for (int a = 0; a < d->npe; a++) ts += d->T[d->elnod[e * d->npe + a]];
+      temp = ts / d->npe;
+    }
     if (m->model == 2) {
-      d->sigma_y[e] = jc_sy(d->pl_strain[e], eff, m);
+      d->sigma_y[e] = jc_sy(d->pl_strain[e], eff, m, temp);
     } else if (m->model == 1) {
       d->sigma_y[e] = hollomon_sy(d->pl_strain[e], m);
     } else {
@@ -891,7 +912,7 @@ static void calc_stress_strain(wfo_domain *d) {
     double dep = 0.0;
     if (d->sigma_y[e] < sig_trial) {
       if (m->model == 2)
-        H = jc_et(d->pl_strain[e], eff, m);
+        H = jc_et(d->pl_strain[e], eff, m, temp);
       else
         H = (m->model == 1) ? hollomon_et(d->pl_strain[e], m) : m->H;
       double G = m->G;
@@ -914,6 +935,18 @@ static void calc_stress_strain(wfo_domain *d) {
       pi[5] = 1.5 * f * (SG[XZ]);
     } else {
       for (int i = 0; i < 6; i++) pi[i] = 0.0;
+    }
+    /* plastic heat (Mechanical.C:1783-1810): 0.9 sigma : (incr / dt) with the
+     * shear terms doubled */
+    if (d->thermal) {
+      d->q_plheat[e] = 0.0;
+      if (dep > 0.0) {
+        const double idt = 1. / dt;
+        const double dxx = pi[0] * idt, dyy = pi[1] * idt, dzz = pi[2] * idt;
+        const double dxy = pi[3] * idt, dyz = pi[4] * idt, dxz = pi[5] * idt;
+        d->q_plheat[e] = 0.9 * (SG[XX] * dxx + 2.0 * SG[XY] * dxy + 2.0 * SG[XZ] * dxz +
+                                SG[YY] * dyy + 2.0 * SG[YZ] * dyz + SG[ZZ] * dzz);
+      }
     }
     for (int i = 0; i < 9; i++) EPS[i] = EPS[i] + SR[i] * dt;
     t3_to_sym(SG, &d->sigma[6 * e]);
@@ -1342,6 +1375,8 @@ static void calc_contact_trimesh(wfo_domain *d) {
       cf[0] += F[0];
       cf[1] += F[1];
       cf[2] += F[2];
+      /* heat from the die (Contact.C:309); kept after contact ends */
+      d->q_cont[i] = d->heat_cond * d->node_area[i] * (d->T_die - d->T[i]);
       break;
     }
   }
@@ -1360,6 +1395,89 @@ static void tri_move(wfo_domain *d) {
       d->tri_x[3 * n + k] = d->tri_x[3 * n + k] + vk * d->dt;
     }
   tri_normals_planes(d);
+}
+
+/* Domain_d::calcThermalExpansion (Thermal.C:163-178): the strain rate's
+ * diagonal loses exp_T * mean of m_dTedt at the element's node ids. As in the
+ * reference, the element-node array of the previous step's temperature rates
+ * is indexed by node id. */
+static void calc_thermal_expansion(wfo_domain *d) {
+  const int npe = d->npe;
+  OMP_FOR
+  for (int64_t e = 0; e < d->ne; e++) {
+    const mat_t *m = mat_of(d, e);
+    double g = 0.0;
+    for (int i = 0; i < npe; i++) g += 1.0 / npe * d->dTedt[d->elnod[e * npe + i]];
+    const double c = m->exp_T * g;
+    double *sr = &d->str_rate[6 * e];
+    sr[0] = sr[0] - c;
+    sr[1] = sr[1] - c;
+    sr[2] = sr[2] - c;
+  }
+}
+
+/* Domain_d::ThermalCalcs (Thermal.C:27-126): per element the conduction
+ * matrix K_ij = (sum_d dN_i detJ dN_j detJ) k_T / detJ w times the element's
+ * node temperatures, and the plastic heat 0.9 q vol split evenly over the
+ * nodes: dT_e,i = -(1 / m_i) (K T)_i + (q_e vol / n) / (m_i cp_T). Then per
+ * node, in node-to-element list order, T += (sum dT_e,i + q_cont / (m cp_T of
+ * material 0)) dt. */
+static void thermal_calcs(wfo_domain *d) {
+  const int npe = d->npe;
+  const double w = (npe == 8) ? 8.0 : 1.0 / 6.0;
+  OMP_FOR
+  for (int64_t e = 0; e < d->ne; e++) {
+    const mat_t *m = mat_of(d, e);
+    const double *dH = &d->dH[e * 3 * npe];
+    const int32_t *en = &d->elnod[e * npe];
+    double Kt[8][8], Te[8];
+    for (int i = 0; i < npe; i++)
+      for (int j = 0; j < npe; j++) {
+        double k = 0.0;
+        for (int dd = 0; dd < 3; dd++) k += dH[dd * npe + i] * dH[dd * npe + j];
+        Kt[i][j] = k * m->k_T / d->detJ[e] * w;
+      }
+    for (int i = 0; i < npe; i++) Te[i] = d->T[en[i]];
+    const double heat = 0.9 * d->q_plheat[e];
+    const double elem_pow = heat * d->vol[e];
+    const double pow_per_node = elem_pow / npe;
+    for (int i = 0; i < npe; i++) {
+      double dT = 0.0;
+      for (int k = 0; k < npe; k++) dT += Kt[i][k] * Te[k];
+      const double m_inv = 1.0 / d->mass[en[i]];
+      double r = -m_inv * dT;
+      r += pow_per_node / (d->mass[en[i]] * m->cp_T);
+      d->dTedt[e * npe + i] = r;
+    }
+  }
+  const double cp0 = d->mats[0].cp_T;
+  OMP_FOR
+  for (int64_t n = 0; n < d->nn; n++) {
+    double s = 0.0;
+    for (int32_t k = 0; k < d->nodel_cnt[n]; k++) {
+      const int64_t i = d->nodel_off[n] + k;
+      s += d->dTedt[(int64_t)d->nodel[i] * npe + d->nodel_loc[i]];
+    }
+    d->T[n] += (s + d->q_cont[n] * 1.0 / (d->mass[n] * cp0)) * d->dt;
+  }
+}
+
+void wfo_set_thermal(wfo_domain *d, int on, double T0) {
+  d->thermal = on;
+  d->T0 = T0;
+}
+
+int wfo_set_material_thermal(wfo_domain *d, int mat, double k_T, double cp_T, double exp_T) {
+  if (mat < 0 || mat >= d->nmat) return -1;
+  d->mats[mat].k_T = k_T;
+  d->mats[mat].cp_T = cp_T;
+  d->mats[mat].exp_T = exp_T;
+  return 0;
+}
+
+void wfo_set_contact_heat(wfo_domain *d, double heat_cond, double T_die) {
+  d->heat_cond = heat_cond;
+  d->T_die = T_die;
 }
 
 /* Preamble of Domain_d::SolveChungHulbert (Solver_explicit.C:120-268). */
@@ -1387,6 +1505,13 @@ int wfo_init(wfo_domain *d) {
   calc_nodal_mass(d);
   memcpy(d->mass0, d->mass, sizeof(double) * d->nn);
   memset(d->ut_prev, 0, sizeof(double) * 3 * d->nn);
+  /* setTemp (Domain_d.h:678-684) and zero thermal rates */
+  if (d->thermal) {
+    for (int64_t n = 0; n < d->nn; n++) d->T[n] = d->T0;
+    memset(d->q_plheat, 0, sizeof(double) * d->ne);
+    memset(d->dTedt, 0, sizeof(double) * d->ne * d->npe);
+    memset(d->q_cont, 0, sizeof(double) * d->nn);
+  }
   d->time = 0.0;
   d->step_count = 0;
   d->hist_len = 0;
@@ -1438,6 +1563,7 @@ static void one_step(wfo_domain *d) {
     calc_nodal_mass(d);
   }
   calc_strain_rates(d);
+  if (d->thermal) calc_thermal_expansion(d);
   if (d->press_alg == 1)
     calc_pressure_anp(d);
   else
@@ -1465,6 +1591,7 @@ static void one_step(wfo_domain *d) {
   for (int k = 0; k < 3; k++) impose_bcv(d, k);
   update_correction_pos(d);
   if (d->tri_on) tri_move(d);
+  if (d->thermal) thermal_calcs(d);
   {
     double ekin, deint;
     compute_energies(d, &ekin, &deint);
@@ -1500,8 +1627,8 @@ int wfo_get_node_vec(const wfo_domain *d, int which, double *out) {
 }
 
 int wfo_get_node_scalar(wfo_domain *d, int which, double *out) {
-  const double *src[] = {d->mass, d->voln, d->p_node};
-  if (which < 0 || which > 2) return -1;
+  const double *src[] = {d->mass, d->voln, d->p_node, d->T};
+  if (which < 0 || which > 3) return -1;
   memcpy(out, src[which], sizeof(double) * d->nn);
   return 0;
 }

@@ -50,6 +50,12 @@ int wfo_set_elem_materials(wfo_domain *d, const int32_t *ids);
 /* Johnson-Cook constants of material `mat` (model 2) and its temperature. */
 int wfo_set_johnson_cook(wfo_domain *d, int mat, double B, double n, double C, double eps0,
                          double m, double Tm, double Tt, double T);
+/* Thermal coupling (Domain_d::setThermalOn / setTemp): every node at T0 at init. */
+void wfo_set_thermal(wfo_domain *d, int on, double T0);
+/* Conductivity, heat capacity and expansion coefficient of material `mat`. */
+int wfo_set_material_thermal(wfo_domain *d, int mat, double k_T, double cp_T, double exp_T);
+/* Die heat transfer coefficient and temperature (TriMesh_d heat_cond, T_const). */
+void wfo_set_contact_heat(wfo_domain *d, double heat_cond, double T_die);
 int wfo_add_bc_vel_node(wfo_domain *d, int64_t node, int dim, double val);
 int wfo_allocate_bcs(wfo_domain *d);
 int wfo_set_reaction_nodes(wfo_domain *d, int64_t n, const int32_t *nodes, int dim);

@@ -43,6 +43,12 @@ DIE_BOTTOM = dict(start=[-0.001, -0.001, 1e-5], end=[0.004, 0.004, 0.0], dens=3,
                   vel=[0.0, 0.0, 2.0])
 
 
+# thermal coupling: T0, conductivity, heat capacity, expansion coefficient and
+# (with a die) the die's heat transfer coefficient and temperature
+THERMAL_DIE = dict(T0=20.0, k=50.0, cp=460.0, exp=1.2e-5, hc=2.0e6, T_die=600.0)
+THERMAL = dict(T0=25.0, k=45.0, cp=480.0, exp=1.0e-5)
+
+
 def cases():
     """(name, Case, steps, mode, extra) with mode 'step' (harness loop) or 'verbatim'."""
     out = []
@@ -93,6 +99,20 @@ def cases():
     c.seed = W.SEED_BASE + 13
     c.bc = "sym_xy"
     out.append(("tet_two_dies", c, 300, "step", dict(linear=True, die=DIE, die2=DIE_BOTTOM)))
+    # thermal coupling (ThermalCalcs, calcThermalExpansion, plastic heat, die
+    # heat transfer) with the die, and with Hollomon through the reference's
+    # own CalcStressStrain
+    c = W.config(1, scale=(3, 3, 4))
+    c.perturb = 0.1
+    c.bc = "bottom_z"
+    out.append(("tet_die_thermal", c, 300, "step",
+                dict(linear=True, die=DIE, thermal=THERMAL_DIE)))
+    c = W.config(1, scale=(2, 3, 3))
+    c.perturb = 0.1
+    c.seed = W.SEED_BASE + 17
+    c.top_vz = -20.0
+    c.materials = [dict(HOLLOMON)]
+    out.append(("tet_hollomon_thermal", c, 300, "step", dict(thermal=THERMAL)))
     # Johnson-Cook through Material_::Init_JohnsonCook and the reference's own
     # CalcStressStrain (hexahedra: the reference reads the temperature T[e] of a
     # node-sized array by element index)
@@ -125,6 +145,12 @@ def run_case(name, case, steps, mode, extra):
         b = extra["die2"]
         xyz, tri = W.axis_plane_mesh(b["start"], b["end"], b["dens"], b["flip"])
         d.add_contact_trimesh(xyz, tri, b["vel"])
+    if "thermal" in extra:
+        t = extra["thermal"]
+        d.set_thermal(True, t["T0"])
+        d.set_material_thermal(0, t["k"], t["cp"], t.get("exp", 0.0))
+        if "hc" in t:
+            d.set_contact_heat(t["hc"], t["T_die"])
     if mode == "verbatim":
         d.set_end_time(steps * dt)
         with tempfile.TemporaryDirectory() as td:
@@ -145,6 +171,8 @@ def run_case(name, case, steps, mode, extra):
     if mode == "step":
         res["reaction"] = d.reaction()
         res["ekin"], res["eint"] = d.energies()
+    if "thermal" in extra:
+        res["T"] = d.node_scalar("T")
     if "die" in extra:
         res["contforce"] = d.contforce()
         res["die_nodes"] = d.trimesh_nodes()

@@ -47,6 +47,12 @@ def setup(dom, case, extra=None):
         xyz, tri = W.axis_plane_mesh(die["start"], die["end"], die["dens"], die["flip"])
         dom.set_contact_trimesh(xyz, tri, die["vel"], die["mu_s"], die["mu_d"], die["pf"])
         dom.set_end_time(die["end_t"])
+    if "thermal" in extra:
+        t = extra["thermal"]
+        dom.set_thermal(True, t["T0"])
+        dom.set_material_thermal(0, t["k"], t["cp"], t.get("exp", 0.0))
+        if "hc" in t:
+            dom.set_contact_heat(t["hc"], t["T_die"])
     if "die2" in extra:
         b = extra["die2"]
         xyz, tri = W.axis_plane_mesh(b["start"], b["end"], b["dens"], b["flip"])

@@ -56,6 +56,9 @@ def test_oracle_matches_reference_fixture(name, case, steps, mode, extra):
         ekin, eint = d.energies()
         np.testing.assert_array_equal(ekin, g["ekin"])
         np.testing.assert_array_equal(eint, g["eint"])
+    if "T" in g:
+        np.testing.assert_array_equal(d.node_scalar("T"), g["T"])
+        assert g["T"].max() > g["T"].min()       # the temperature field evolved
     if "contforce" in g:
         np.testing.assert_array_equal(d.node_vec("contforce"), g["contforce"])
         np.testing.assert_array_equal(d.trimesh_nodes(), g["die_nodes"])
