@@ -53,8 +53,9 @@ class Material_ {
     K = k_;
     m = m_;
   }
-  // Material_::Init_JohnsonCook (Material.cuh:105-114); T is the (uniform)
-  // element temperature the yield function reads (thermal coupling not built)
+  // Material_::Init_JohnsonCook (Material.cuh:105-114); T is the uniform
+  // element temperature the yield function reads without thermal coupling
+  // (with it, each element takes the mean of its node temperatures)
   void Init_JohnsonCook(const Elastic_ &el, double a, double b, double n_, double c,
                         double eps_0_, double m_, double T_m_, double T_t_, double T_ = 0.0) {
     elastic_m = el;
@@ -75,6 +76,7 @@ class Material_ {
   double Ep = 0.0;      // hardening modulus of the bilinear law
   double K = 1.0, m = 1.0;
   double cs0 = 0.0;     // informational; the library uses sqrt(K_bulk / rho)
+  double k_T = 0.0, cp_T = 0.0, exp_T = 0.0;  // thermal (Material.cuh:81-83)
 
  private:
   Elastic_ elastic_m;
@@ -126,7 +128,22 @@ class Domain_d {
       if (m.Material_model == JOHNSON_COOK)
         check(wf_set_johnson_cook(d_, (int32_t)i, m.B, m.n, m.C, m.eps_0, m.m, m.T_m, m.T_t, m.T),
               "Init_JohnsonCook");
+      if (m.cp_T > 0.0)
+        check(wf_set_material_thermal(d_, (int32_t)i, m.k_T, m.cp_T, m.exp_T), "thermal");
     }
+  }
+  // thermal coupling (Domain_d.h:676-684): setThermalOn, setTemp(T0)
+  void setThermalOn() {
+    thermal_ = true;
+    check(wf_set_thermal(d_, 1, T0_), "setThermalOn");
+  }
+  void setTemp(const double &val) {
+    T0_ = val;
+    check(wf_set_thermal(d_, thermal_ ? 1 : 0, T0_), "setTemp");
+  }
+  // TriMesh_d heat_cond and T_const of the rigid bodies
+  void setContactHeat(double heat_cond, double T_die) {
+    check(wf_set_contact_heat(d_, heat_cond, T_die), "contact heat");
   }
   void setElemMaterials(const std::vector<int32_t> &ids) {
     check(wf_set_elem_materials(d_, ids.data()), "setElemMaterials");
@@ -292,6 +309,8 @@ class Domain_d {
   wf_domain *d_ = nullptr;
   bool initialized_ = false;
   double rho_ = 0.0;
+  bool thermal_ = false;
+  double T0_ = 20.0;
   std::vector<double> x_, u_, v_, fi_, pl_;
 };
 

@@ -71,7 +71,7 @@ enum {
   WF_NODE_FI = 5, WF_NODE_CONTFORCE = 7
 };
 /* Node scalar fields. */
-enum { WF_NODE_MASS = 0, WF_NODE_VOLN = 1, WF_NODE_PRESSURE = 2 };
+enum { WF_NODE_MASS = 0, WF_NODE_VOLN = 1, WF_NODE_PRESSURE = 2, WF_NODE_TEMP = 3 };
 /* Element scalar fields. */
 enum {
   WF_ELEM_VOL = 0, WF_ELEM_VOL0 = 1, WF_ELEM_DETJ = 2, WF_ELEM_P = 3,
@@ -181,6 +181,32 @@ WF_API wf_status wf_set_reaction_nodes(wf_domain *d, int64_t n, const int32_t *n
  * sum of normal contact forces. */
 WF_API wf_status wf_set_contact_plane(wf_domain *d, double z0, double vz, double kpen, double mu,
                                       int64_t ncand, const int32_t *cand_nodes);
+
+/* Thermal coupling of the FP64 step (Domain_d::setThermalOn / setTemp,
+ * ThermalCalcs, Thermal.C:27-126; calcThermalExpansion, :163-178): every node
+ * starts at T0; each element adds to its nodes' temperature rates the
+ * conduction term -(1/m_i) (K T)_i with K_ij = (sum_d dN_i detJ dN_j detJ)
+ * k_T / detJ w, and the plastic heat 0.9 q vol / n / (m_i cp_T), where
+ * q = 0.9 sigma : (d eps_p / dt) is formed in the radial return
+ * (Mechanical.C:1783-1810; the reference applies the 0.9 plastic-work fraction
+ * twice); nodes in contact with a rigid body receive heat_cond * A *
+ * (T_die - T), kept after the contact ends (Contact.C:309); then
+ * T += (sum of rates + die heat / (m cp_T of material 0)) dt. The strain
+ * rate's diagonal loses exp_T times the mean of the previous step's
+ * element-node rates read at the element's node ids, as the reference indexes
+ * them. A Johnson-Cook element takes the mean of its node temperatures (the
+ * reference reads T[e], a node array indexed by element). Readback:
+ * wf_get_node_scalar(WF_NODE_TEMP). Before wf_init; FP64, one domain. */
+WF_API wf_status wf_set_thermal(wf_domain *d, int32_t on, double T0);
+/* Conductivity k_T, heat capacity cp_T (> 0) and expansion coefficient of
+ * material `mat` (Material_ k_T, cp_T, exp_T; deck keys thermalCond,
+ * thermalHeatCap, thermalExp). */
+WF_API wf_status wf_set_material_thermal(wf_domain *d, int32_t mat, double k_T, double cp_T,
+                                         double exp_T);
+/* Heat transfer coefficient and temperature of the rigid bodies (TriMesh_d
+ * heat_cond, T_const; deck Contact keys heatCondCoeff, dieTemp; defaults 0 and
+ * 20). */
+WF_API wf_status wf_set_contact_heat(wf_domain *d, double heat_cond, double T_die);
 
 /* Rigid triangle-mesh die (Domain_d::setTriMesh / setContactOn / setContactPF,
  * Domain_d.h:464, :642, :771; CalcContactForces, Contact.C:31-334): mesh nodes
@@ -366,9 +392,11 @@ WF_API wf_status wf_adjoint_backward(wf_domain *d, const double *dL_dR, int32_t 
  * body moves with the velocity of the boundary condition whose zoneId is the
  * body's; the Contact block gives fricCoeffStatic, fricCoeffDynamic and
  * penaltyFactor; as in the reference driver, a contact deck applies no
- * velocity zones to the part (symmetry planes only). Thermal,
- * axisymmetric/plane-strain, Perzyna and Line (2-D) rigid bodies return
- * WF_ERR_UNSUPPORTED. Configuration.hourglass3D (not a reference key,
+ * velocity zones to the part (symmetry planes only). Configuration.thermal
+ * turns on the thermal coupling (wf_set_thermal) with the keys listed in
+ * wf_deck_info; a JohnsonCook material then takes m, T_melt, T_transition
+ * from const[4..6]. Axisymmetric/plane-strain, Perzyna and Line (2-D) rigid
+ * bodies return WF_ERR_UNSUPPORTED. Configuration.hourglass3D (not a reference key,
  * default 0 as the reference's 3-D no-op) sets the viscous hourglass
  * coefficient. Errors are written into err (err_len bytes, may be null). */
 typedef struct wf_deck wf_deck;
@@ -392,6 +420,11 @@ typedef struct {
   /* Johnson-Cook material: B, n, C, eps0_dot, m, T_melt, T_transition, T */
   double johnson_cook[8];
   int32_t rigid_bodies;  /* number of rigid bodies read (0, 1 or 2) */
+  /* thermal coupling: Configuration.thermal, InitialConditions Temp (default
+   * 20), Materials[0] thermalCond / thermalHeatCap / thermalExp, Contact
+   * heatCondCoeff / dieTemp (default 20) */
+  int32_t thermal;
+  double T0, thermal_k, thermal_cp, thermal_exp, heat_cond, die_temp;
 } wf_deck_info;
 WF_API wf_status wf_deck_read(const char *path, wf_deck **out, char *err, int64_t err_len);
 WF_API wf_status wf_deck_free(wf_deck *k);

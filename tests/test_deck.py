@@ -157,7 +157,7 @@ def test_lsdyna_reader(tmp_path, comma, tet):
 
 def test_deck_errors(tmp_path):
     cases = [
-        (dict(Configuration={"thermal": True}), 5),
+        (dict(Configuration={"thermal": True}), 1),    # no thermalHeatCap
         (dict(Configuration={"domType": "AxiSymm"}), 5),
         (dict(RigidBodies=[{"type": "File", "fileName": "missing.nas"}]), 1),
         (dict(RigidBodies=[{"type": "Line", "dim": [1.0, 0.0, 0.0]}]), 5),

@@ -156,7 +156,7 @@ STEEL = {"type": "Bilinear", "const": [2.0e9], "density0": 7850.0, "youngsModulu
          "poissonsRatio": 0.3, "yieldStress0": 300e6}
 
 
-def two_body_deck(tmp_path, top="File", third=False, tet=False):
+def two_body_deck(tmp_path, top="File", third=False, tet=False, thermal=False):
     """A 4 x 4 x 5 mm block (hexahedra, or tetrahedra) with x/y symmetry,
     pressed by a die (File: a Nastran plane, flipnormals, oriented toward the
     part; or Plane) moving down and a fixed Plane body under it."""
@@ -181,6 +181,12 @@ def two_body_deck(tmp_path, top="File", third=False, tet=False):
                                {"zoneId": 1, "valueType": 0, "value": [0.0, 0.0, 0.0]},
                                {"zoneId": 5, "valueType": 0, "value": [1.0, 0.0, 0.0]}],
     }
+    if thermal:
+        # the reference's thermal contact decks: hot die, plastic heat
+        deck["Configuration"]["thermal"] = True
+        deck["InitialConditions"] = [{"Temp": 30.0}]
+        deck["Materials"][0].update(thermalCond=50.0, thermalHeatCap=460.0, thermalExp=1.2e-5)
+        deck["Contact"][0].update(heatConductance=True, heatCondCoeff=2.0e6, dieTemp=500.0)
     p = tmp_path / "two_body.json"
     p.write_text(json.dumps(deck, indent=1))
     return str(p)
@@ -220,12 +226,21 @@ def test_two_body_deck_drives_the_oracle(tmp_path):
     assert o.reaction().max() > 0
 
 
+def test_thermal_deck(tmp_path):
+    i = wf.Deck(two_body_deck(tmp_path, thermal=True)).info
+    assert i["thermal"] == 1 and i["T0"] == 30.0
+    assert (i["thermal_k"], i["thermal_cp"], i["thermal_exp"]) == (50.0, 460.0, 1.2e-5)
+    assert (i["heat_cond"], i["die_temp"]) == (2.0e6, 500.0)
+    assert wf.Deck(two_body_deck(tmp_path)).info["thermal"] == 0
+
+
 @NEEDS_REF
-def test_two_plane_bodies_match_reference(tmp_path):
+@pytest.mark.parametrize("thermal", [False, True])
+def test_two_plane_bodies_match_reference(tmp_path, thermal):
     """Two Plane bodies from a deck, oracle against the reference harness
     (tetrahedra: the reference's 3-D surface search is compiled for 4-node
     elements)."""
-    k = wf.Deck(two_body_deck(tmp_path, top="Plane", tet=True))
+    k = wf.Deck(two_body_deck(tmp_path, top="Plane", tet=True, thermal=thermal))
     res = []
     for dom in (O.OracleDomain(), R.RefDomain()):
         k.setup(dom)
@@ -235,16 +250,20 @@ def test_two_plane_bodies_match_reference(tmp_path):
             dom.set_linear_hardening(True)
         dom.init()
         dom.step(150)
-        res.append((dom.node_vec("u"), dom.reaction(), dom.trimesh_nodes()))
+        res.append((dom.node_vec("u"), dom.reaction(), dom.trimesh_nodes(),
+                    dom.node_scalar("T") if thermal else None))
     for a, b in zip(*res):
         np.testing.assert_array_equal(a, b)
+    if thermal:
+        assert res[0][3].max() > 30.0
 
 
 # ---- GPU -------------------------------------------------------------------------
 @pytest.mark.gpu
-@pytest.mark.parametrize("top,tet", [("File", False), ("Plane", True)])
-def test_two_body_deck_on_gpu_matches_oracle(tmp_path, top, tet):
-    k = wf.Deck(two_body_deck(tmp_path, top=top, tet=tet))
+@pytest.mark.parametrize("top,tet,thermal", [("File", False, False), ("Plane", True, False),
+                                             ("File", True, True)])
+def test_two_body_deck_on_gpu_matches_oracle(tmp_path, top, tet, thermal):
+    k = wf.Deck(two_body_deck(tmp_path, top=top, tet=tet, thermal=thermal))
     d = wf.Domain(wf.WF_FP64)
     k.apply(d)
     d.init()
@@ -258,3 +277,5 @@ def test_two_body_deck_on_gpu_matches_oracle(tmp_path, top, tet):
     assert H.rel_err(d.node_vec("contforce"), o.node_vec("contforce")) <= 1e-9
     assert H.rel_err(d.reaction(), o.reaction()) <= 1e-9
     np.testing.assert_allclose(d.trimesh_nodes(), o.trimesh_nodes(), rtol=1e-12, atol=0)
+    if thermal:
+        assert H.rel_err(d.node_scalar("T"), o.node_scalar("T")) <= 1e-9

@@ -1,0 +1,103 @@
+"""Thermal coupling of the FP64 step (wf_set_thermal).
+
+The oracle's restatement of ThermalCalcs, calcThermalExpansion, the plastic
+heat of the radial return and the die heat transfer is pinned bit-for-bit to
+the reference by the fixtures tet_die_thermal and tet_hollomon_thermal
+(tests/test_oracle.py). Here the GPU step runs the same cases, a hexahedral
+one with hourglass control and a Johnson-Cook one (whose element temperature
+is the mean of its node temperatures), against the oracle: displacements,
+temperatures and the reaction history within 1e-9 relative.
+"""
+import numpy as np
+import pytest
+
+import weldformfem_gb300 as wf
+from oracle import orabind as O
+from tests import helpers as H
+from weldformfem_gb300 import workloads as W
+
+DIE = dict(start=[-0.001, -0.001, 0.002 - 1e-5], end=[0.004, 0.004, 0.0], dens=2, flip=True,
+           vel=[0.0, 0.0, -5.0], mu_s=0.1, mu_d=0.08, pf=0.1, end_t=2e-6)
+THERMAL_DIE = dict(T0=20.0, k=50.0, cp=460.0, exp=1.2e-5, hc=2.0e6, T_die=600.0)
+THERMAL = dict(T0=25.0, k=45.0, cp=480.0, exp=1.0e-5)
+HOLLOMON = dict(model=1, E=200e9, nu=0.3, rho=7850.0, sy0=300e6, hol_K=600e6, hol_m=0.2)
+JC = [400e6, 0.35, 0.02, 1.0, 1.0, 1500.0, 20.0, 300.0]
+
+
+def cases():
+    out = {}
+    c = W.config(1, scale=(3, 3, 4))
+    c.perturb = 0.1
+    c.bc = "bottom_z"
+    out["tet_die"] = (c, dict(die=DIE, thermal=THERMAL_DIE), 300)
+    c = W.config(1, scale=(2, 3, 3))
+    c.perturb = 0.1
+    c.seed = W.SEED_BASE + 17
+    c.top_vz = -20.0
+    c.materials = [dict(HOLLOMON)]
+    out["tet_hollomon"] = (c, dict(thermal=THERMAL), 300)
+    c = W.config(0, scale=(4, 4, 5))
+    c.perturb = 0.05
+    c.seed = W.SEED_BASE + 19
+    c.top_vz = -15.0
+    out["hex_hg"] = (c, dict(thermal=THERMAL), 400)
+    c = W.config(0, scale=(3, 3, 4))
+    c.perturb = 0.1
+    c.seed = W.SEED_BASE + 9
+    c.top_vz = -15.0
+    c.materials = [dict(model=2, E=200e9, nu=0.3, rho=7850.0, sy0=250e6)]
+    out["hex_jc"] = (c, dict(jc=JC, thermal=dict(T0=300.0, k=40.0, cp=450.0, exp=1.1e-5)), 400)
+    return out
+
+
+def run(dom, case, extra, steps):
+    H.setup(dom, case, extra)
+    dom.init()
+    dom.step(steps) if hasattr(dom, "step") else dom.run(steps)
+    return dom
+
+
+def test_oracle_heats_the_part():
+    case, extra, steps = cases()["tet_die"]
+    o = run(O.OracleDomain(), case, extra, steps)
+    T = o.node_scalar("T")
+    assert T.min() >= 20.0 - 1e-9 and T.max() > 30.0          # die at 600 C heats the top
+    top = case.top_nodes()
+    assert T[top].mean() > T.mean()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["tet_die", "tet_hollomon", "hex_hg", "hex_jc"])
+def test_thermal_step_matches_oracle(name):
+    case, extra, steps = cases()[name]
+    o = run(O.OracleDomain(), case, extra, steps)
+    d = run(wf.Domain(wf.WF_FP64), case, extra, steps)
+    T, To = d.node_scalar("T"), o.node_scalar("T")
+    assert To.max() > To.min()
+    assert H.rel_err(T, To) <= 1e-9
+    assert H.rel_err(d.node_vec("u"), o.node_vec("u")) <= 1e-9
+    assert H.rel_err(d.elem_scalar("pl_strain"), o.elem_scalar("pl_strain")) <= 1e-9
+    assert H.rel_err(d.reaction(), o.reaction()) <= 1e-9
+
+
+@pytest.mark.gpu
+def test_thermal_options():
+    case, extra, _ = cases()["tet_hollomon"]
+    d = wf.Domain(wf.WF_MIXED)
+    H.setup(d, case, extra)
+    with pytest.raises(wf.WfError) as e:
+        d.init()
+    assert e.value.status == wf.WF_ERR_UNSUPPORTED
+    d = wf.Domain(wf.WF_FP64)
+    W.apply(d, case)
+    d.set_thermal(True, 20.0)
+    with pytest.raises(wf.WfError) as e:
+        d.init()                                   # no material thermal constants
+    assert e.value.status == wf.WF_ERR_STATE
+    d = wf.Domain(wf.WF_FP64)
+    W.apply(d, case)
+    d.init()
+    with pytest.raises(wf.WfError):
+        d.node_scalar("T")                          # thermal coupling off
+    with pytest.raises(wf.WfError):
+        d.set_thermal(True, 20.0)                   # after init

@@ -28,7 +28,7 @@ STATUS = {0: "ok", 1: "invalid argument", 2: "call out of order", 3: "CUDA error
           7: "device wait timed out"}
 
 NODE_VEC = {"x": 0, "v": 1, "a": 2, "u": 3, "prev_a": 4, "fi": 5, "contforce": 7}
-NODE_SCALAR = {"mass": 0, "voln": 1, "p_node": 2}
+NODE_SCALAR = {"mass": 0, "voln": 1, "p_node": 2, "T": 3}
 ELEM_SCALAR = {"vol": 0, "vol0": 1, "detJ": 2, "p": 3, "pl_strain": 4, "sigma_y": 5, "rho": 6}
 ELEM_TENSOR = {"sigma": 0, "tau": 1, "eps": 2, "str_rate": 3, "rot_rate": 4}
 
@@ -61,7 +61,10 @@ class WfDeckInfo(C.Structure):
                 ("material", WfMaterial), ("contact", C.c_int32), ("die_nodes", C.c_int32),
                 ("die_tris", C.c_int32), ("die_vel", C.c_double * 3), ("mu_static", C.c_double),
                 ("mu_dynamic", C.c_double), ("penalty_factor", C.c_double),
-                ("johnson_cook", C.c_double * 8), ("rigid_bodies", C.c_int32)]
+                ("johnson_cook", C.c_double * 8), ("rigid_bodies", C.c_int32),
+                ("thermal", C.c_int32), ("T0", C.c_double), ("thermal_k", C.c_double),
+                ("thermal_cp", C.c_double), ("thermal_exp", C.c_double),
+                ("heat_cond", C.c_double), ("die_temp", C.c_double)]
 
 
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
@@ -143,6 +146,9 @@ _SIGS = {
                                C.c_double, C.c_double],
     "wf_get_trimesh_nodes": [C.c_void_p, _dp, C.c_int64, C.POINTER(C.c_int64)],
     "wf_add_contact_trimesh": [C.c_void_p, C.c_int64, _dp, C.c_int64, _ip, _dp],
+    "wf_set_thermal": [C.c_void_p, C.c_int32, C.c_double],
+    "wf_set_material_thermal": [C.c_void_p, C.c_int32, C.c_double, C.c_double, C.c_double],
+    "wf_set_contact_heat": [C.c_void_p, C.c_double, C.c_double],
     "wf_deck_get_body": [C.c_void_p, C.c_int32, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
                          C.POINTER(C.c_double), C.c_void_p, C.c_void_p],
     "wf_read_nastran": [C.c_char_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p,
@@ -461,6 +467,16 @@ class Domain:
                    np.ascontiguousarray(vel, np.float64), float(mu_static), float(mu_dynamic),
                    float(penalty_factor))
 
+    def set_thermal(self, on=True, T0=20.0):
+        """Thermal coupling (setThermalOn + setTemp), FP64 step."""
+        self._call("wf_set_thermal", int(bool(on)), float(T0))
+
+    def set_material_thermal(self, mat, k_T, cp_T, exp_T=0.0):
+        self._call("wf_set_material_thermal", int(mat), float(k_T), float(cp_T), float(exp_T))
+
+    def set_contact_heat(self, heat_cond, T_die=20.0):
+        self._call("wf_set_contact_heat", float(heat_cond), float(T_die))
+
     def add_contact_trimesh(self, xyz, tri, vel):
         """Another rigid body (TriMesh_d::AddMesh); only body 0 feeds the reaction."""
         xyz = np.ascontiguousarray(xyz, np.float64).reshape(-1)
@@ -624,11 +640,16 @@ class Deck:
             dom.set_artif_visc(*i["artif_visc"])
         if i["hourglass"]:
             dom.set_hourglass(i["hourglass"])
+        if i["thermal"]:
+            dom.set_thermal(True, i["T0"])
+            dom.set_material_thermal(0, i["thermal_k"], i["thermal_cp"], i["thermal_exp"])
         if i["contact"]:
             xyz, tri = self.die()
             dom.set_contact_trimesh(xyz, tri, i["die_vel"], i["mu_static"], i["mu_dynamic"],
                                     i["penalty_factor"])
             for b in range(1, i["rigid_bodies"]):
                 dom.add_contact_trimesh(*self.body(b))
+            if i["thermal"]:
+                dom.set_contact_heat(i["heat_cond"], i["die_temp"])
         dom.set_dt(i["dt"])
         dom.set_end_time(i["end_time"])

@@ -102,6 +102,10 @@ struct wf_domain {
   // materials
   std::vector<wf_material> mats;
   std::vector<std::array<double, 8>> jc;  // Johnson-Cook B, n, C, eps0_dot, m, T_melt, T_t, T
+  std::vector<std::array<double, 3>> mat_thermal;  // k_T, cp_T, exp_T per material
+  bool thermal = false;
+  double T0 = 20.0;
+  double tri_hc = 0.0, tri_Tdie = 20.0;             // die heat transfer
   std::vector<int32_t> emat;
   double rho_all = 0.0;
   bool rho_set = false;
@@ -569,6 +573,7 @@ WF_API wf_status wf_set_materials(wf_domain *d, int32_t nmat, const wf_material 
   }
   d->mats.assign(mats, mats + nmat);
   d->jc.assign(nmat, std::array<double, 8>{0, 0, 0, 0, 0, 0, 0, 0});
+  d->mat_thermal.assign(nmat, std::array<double, 3>{0, 0, 0});
   d->rho_all = mats[0].rho;
   d->rho_set = true;
   return WF_OK;
@@ -586,6 +591,34 @@ WF_API wf_status wf_set_johnson_cook(wf_domain *d, int32_t mat, double B, double
   if (!(eps0_dot > 0) || !(T_melt != T_transition))
     return fail(d, WF_ERR_ARG, "Johnson-Cook needs eps0_dot > 0 and T_melt != T_transition");
   d->jc[mat] = {B, n, C, eps0_dot, m, T_melt, T_transition, T};
+  return WF_OK;
+}
+
+// ---- thermal coupling (Thermal.C) ---------------------------------------------------
+WF_API wf_status wf_set_thermal(wf_domain *d, int32_t on, double T0) {
+  if (!d) return WF_ERR_ARG;
+  if (d->initialized) return fail(d, WF_ERR_STATE, "thermal coupling is set before init");
+  d->thermal = on != 0;
+  d->T0 = T0;
+  return WF_OK;
+}
+
+WF_API wf_status wf_set_material_thermal(wf_domain *d, int32_t mat, double k_T, double cp_T,
+                                         double exp_T) {
+  if (!d) return WF_ERR_ARG;
+  if (d->initialized) return fail(d, WF_ERR_STATE, "materials are set before init");
+  if (mat < 0 || mat >= (int32_t)d->mats.size())
+    return fail(d, WF_ERR_ARG, "material %d out of range", mat);
+  if (!(k_T >= 0) || !(cp_T > 0)) return fail(d, WF_ERR_ARG, "need k_T >= 0 and cp_T > 0");
+  d->mat_thermal[mat] = {k_T, cp_T, exp_T};
+  return WF_OK;
+}
+
+WF_API wf_status wf_set_contact_heat(wf_domain *d, double heat_cond, double T_die) {
+  if (!d) return WF_ERR_ARG;
+  if (d->initialized) return fail(d, WF_ERR_STATE, "contact heat is set before init");
+  d->tri_hc = heat_cond;
+  d->tri_Tdie = T_die;
   return WF_OK;
 }
 
@@ -1072,6 +1105,12 @@ WF_API wf_status wf_init(wf_domain *d) {
     return fail(d, WF_ERR_UNSUPPORTED, "contact is not supported in a batched ensemble");
   if (d->nspec && d->energy)
     return fail(d, WF_ERR_UNSUPPORTED, "the energy history is not kept for a batched ensemble");
+  if (d->thermal && (d->precision != WF_FP64 || d->nspec))
+    return fail(d, WF_ERR_UNSUPPORTED, "thermal coupling runs in the FP64 step of one domain");
+  if (d->thermal)
+    for (size_t i = 0; i < d->mats.size(); i++)
+      if (!(d->mat_thermal[i][1] > 0))
+        return fail(d, WF_ERR_STATE, "material %zu: wf_set_material_thermal not called", i);
   CUDA_TRY(cudaSetDevice(d->device));
   free_device(d);
   const int64_t nn = d->nn, ne = d->ne;
@@ -1079,6 +1118,11 @@ WF_API wf_status wf_init(wf_domain *d) {
   d->np = np;
   StepParams &P = d->P;
   P = StepParams{};
+  {
+    int sms = 0;
+    CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, d->device));
+    P.sms = sms;
+  }
   P.nn = nn;
   P.ne = ne;
   P.np = np;
@@ -1199,7 +1243,13 @@ WF_API wf_status wf_init(wf_domain *d) {
       t.jc_eps0 = j[3];
       const double T_h = (j[7] - j[6]) / (j[5] - j[6]);
       t.jc_Th = 1.0 - std::pow(T_h, j[4]);
+      t.jc_m = j[4];
+      t.jc_Tm = j[5];
+      t.jc_Tt = j[6];
     }
+    t.k_T = d->mat_thermal[i][0];
+    t.cp_T = d->mat_thermal[i][1];
+    t.exp_T = d->mat_thermal[i][2];
   }
   MatDev *mdev = nullptr;
   CUDA_TRY(upload(d, &mdev, md));
@@ -1292,6 +1342,15 @@ WF_API wf_status wf_init(wf_domain *d) {
   if (fp64) {
     CUDA_TRY(dalloc(d, &S.vp, 3 * np));
     CUDA_TRY(dalloc(d, &S.ut, 3 * np));
+    if (d->thermal) {
+      CUDA_TRY(upload(d, &S.T, std::vector<double>(np, d->T0)));
+      CUDA_TRY(dalloc(d, &S.qc, np));
+      CUDA_TRY(dalloc(d, &S.dte, 2 * ne * d->npe));
+      P.thermal = 1;
+      P.cp0 = d->mat_thermal[0][1];
+      P.tri_hc = d->tri_hc;
+      P.tri_Tdie = d->tri_Tdie;
+    }
     CUDA_TRY(dalloc(d, &S.sr, 6 * ne));
     CUDA_TRY(dalloc(d, &S.rr, 6 * ne));
     CUDA_TRY(dalloc(d, &S.fe, (size_t)ne * d->npe * 3));
@@ -1743,6 +1802,13 @@ WF_API wf_status wf_get_node_scalar(wf_domain *d, int32_t field, double *out) {
     std::copy(tmp.begin(), tmp.begin() + d->nn, out);
     return WF_OK;
   }
+  if (field == WF_NODE_TEMP) {
+    if (!d->thermal) return fail(d, WF_ERR_STATE, "thermal coupling is off");
+    s = copy_plain(d, d->S.T, tmp.data(), d->np);
+    if (s) return s;
+    std::copy(tmp.begin(), tmp.begin() + d->nn, out);
+    return WF_OK;
+  }
   if (field == WF_NODE_PRESSURE) {
     // calcNodalPressureFromElemental (Mechanical.C:1187-1213), serial order
     std::vector<double> p(d->ne), vol(d->ne);
@@ -2024,9 +2090,10 @@ WF_API wf_status wf_adjoint_forward(wf_domain *d, int64_t nsteps, int64_t every)
   if (!d->initialized) return fail(d, WF_ERR_STATE, "wf_init not called");
   if (d->precision != WF_FP64)
     return fail(d, WF_ERR_UNSUPPORTED, "the adjoint records the FP64 step");
-  if (d->contact || d->nspec || d->press_alg != 0 || d->av[0] != 0.0 || d->av[1] != 0.0)
+  if (d->contact || d->nspec || d->thermal || d->press_alg != 0 || d->av[0] != 0.0 ||
+      d->av[1] != 0.0)
     return fail(d, WF_ERR_UNSUPPORTED, "the adjoint supports pressure algorithm 0 without contact, "
-                                       "artificial viscosity or specimens");
+                                       "thermal coupling, artificial viscosity or specimens");
   const double *sp = &d->stab.alpha_free;
   for (int i = 0; i < 10; i++)
     if (sp[i] != 0.0) return fail(d, WF_ERR_UNSUPPORTED, "the adjoint supports default stabilisation");

@@ -737,9 +737,14 @@ WF_API wf_status wf_deck_read(const char *path, wf_deck **out, char *err, int64_
   jbool(config, "ySymm", sym[1]);
   jbool(config, "zSymm", sym[2]);
   jnum(config, "symtol", symtol);
+  // thermal coupling (main.C:424-441): InitialConditions Temp (last entry wins)
   bool thermal = false;
   jbool(config, "thermal", thermal);
-  if (thermal) return bad("thermal coupling is not supported", WF_ERR_UNSUPPORTED);
+  I.thermal = thermal ? 1 : 0;
+  I.T0 = 20.0;
+  if (const JVal *ics = j.get("InitialConditions"))
+    if (ics->kind == JVal::Arr)
+      for (const JVal &ic : ics->arr) jnum(&ic, "Temp", I.T0);
   std::string s;
   if (jstr(config, "plasticType", s) && s != "Hardening")
     return bad("plasticType " + s + " is not supported", WF_ERR_UNSUPPORTED);
@@ -784,13 +789,22 @@ WF_API wf_status wf_deck_read(const char *path, wf_deck **out, char *err, int64_
     M.hol_K = c[0];
     M.hol_m = c[1];
   } else if (mtype == "JohnsonCook") {
-    // JohnsonCook(el, Fy, c[0], c[1], c[2], c[3], 1.0, 1.0e10, 0.0) (main.C:527)
+    // JohnsonCook(el, Fy, B, n, C, eps0_dot, m, T_m, T_t) from const (main.C:538-541):
+    // m, T_m, T_t are const[4..6] with thermal coupling, else 1, 1e10, 0
     M.model = WF_MAT_JOHNSON_COOK;
-    const double jc[8] = {c[0], c[1], c[2], c[3], 1.0, 1.0e10, 0.0, 0.0};
+    const double jc[8] = {c[0], c[1], c[2], c[3], thermal ? c[4] : 1.0, thermal ? c[5] : 1.0e10,
+                          thermal ? c[6] : 0.0, thermal ? I.T0 : 0.0};
     for (int q = 0; q < 8; q++) I.johnson_cook[q] = jc[q];
   } else {
     return bad("material type " + mtype + " is not supported", WF_ERR_UNSUPPORTED);
   }
+
+  // thermal constants (main.C:575-577)
+  jnum(m0, "thermalCond", I.thermal_k);
+  jnum(m0, "thermalHeatCap", I.thermal_cp);
+  jnum(m0, "thermalExp", I.thermal_exp);
+  if (thermal && !(I.thermal_cp > 0.0))
+    return bad("thermal coupling needs Materials[0].thermalHeatCap > 0");
 
   // DomainBlocks[0] (main.C:350-430)
   const JVal *b0 = blocks ? blocks->at(0) : nullptr;
@@ -886,6 +900,10 @@ WF_API wf_status wf_deck_read(const char *path, wf_deck **out, char *err, int64_
     jnum(c0, "fricCoeffDynamic", I.mu_dynamic);
     double pf = -1.0;
     if (jnum(c0, "penaltyFactor", pf) && pf > -1.0) I.penalty_factor = pf;
+    // die heat transfer (main.C:714-719)
+    I.die_temp = 20.0;
+    jnum(c0, "heatCondCoeff", I.heat_cond);
+    jnum(c0, "dieTemp", I.die_temp);
   } else if (rig && rig->kind == JVal::Arr && rig->arr.size() > 1) {
     return bad("a second rigid body needs a first one with a type");
   }
@@ -1049,6 +1067,11 @@ WF_API wf_status wf_deck_apply(const wf_deck *k, wf_domain *d) {
   if (I.artif_visc[0] != 0.0 || I.artif_visc[1] != 0.0)
     WF_DECK_TRY(wf_set_artif_visc(d, I.artif_visc[0], I.artif_visc[1]));
   if (I.hourglass != 0.0) WF_DECK_TRY(wf_set_hourglass(d, I.hourglass));
+  if (I.thermal) {
+    WF_DECK_TRY(wf_set_thermal(d, 1, I.T0));
+    WF_DECK_TRY(wf_set_material_thermal(d, 0, I.thermal_k, I.thermal_cp, I.thermal_exp));
+    if (I.contact) WF_DECK_TRY(wf_set_contact_heat(d, I.heat_cond, I.die_temp));
+  }
   if (I.contact) {
     const DeckBody &b0 = k->bodies[0];
     WF_DECK_TRY(wf_set_contact_trimesh(d, I.die_nodes, b0.x.data(), I.die_tris, b0.tri.data(),

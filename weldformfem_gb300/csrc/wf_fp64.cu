@@ -181,7 +181,9 @@ __device__ __forceinline__ double hollomon_et(double strain, const MatDev &m) {
 // calcElemPressure (:691-819) or calcElemPressureANP (:1220-1250),
 // CalcStressStrain (:1664-1839), calcArtificialViscosity (:1948-1977),
 // calcElemForces (:375-481) and the 3-D viscous hourglass forces.
-template <int NPE>
+// TH: thermal coupling (a separate instantiation keeps the common case's
+// register allocation).
+template <int NPE, bool TH>
 __global__ void __launch_bounds__(kElemThreads) k_fp64_elements(StepParams P, Fp64State S) {
   int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= P.ne) return;
@@ -243,6 +245,20 @@ __global__ void __launch_bounds__(kElemThreads) k_fp64_elements(StepParams P, Fp
   }
   s01 = s01 * 0.5; s02 = s02 * 0.5; s12 = s12 * 0.5;
   w01 = w01 * 0.5; w02 = w02 * 0.5; w12 = w12 * 0.5;
+  const long long step = TH ? P.st->step : 0;
+  if constexpr (TH) {
+    // calcThermalExpansion (Thermal.C:163-178): the previous step's
+    // element-node temperature rates read at the element's node ids, as the
+    // reference indexes them
+    const double *prev = S.dte + ((step + 1) & 1) * ne * NPE;
+    double g = 0.0;
+#pragma unroll
+    for (int a = 0; a < NPE; a++) g += 1.0 / NPE * prev[nid[a]];
+    const double c = m.exp_T * g;
+    s00 = s00 - c;
+    s11 = s11 - c;
+    s22 = s22 - c;
+  }
 
   // pressure
   double p;
@@ -336,6 +352,7 @@ __global__ void __launch_bounds__(kElemThreads) k_fp64_elements(StepParams P, Fp
   double pls = S.pls[e];
   double sy;
   double eff = 0.0;
+  double jTh = m.jc_Th;
   if (m.model == WF_MAT_JOHNSON_COOK) {
     // effective strain rate (Mechanical.C:1701-1705) and the Johnson-Cook yield
     // stress (CalcJohnsonCookYieldStress, Material.cuh:377-392)
@@ -343,19 +360,29 @@ __global__ void __launch_bounds__(kElemThreads) k_fp64_elements(StepParams P, Fp
                       (s22 - s00) * (s22 - s00)) +
                3.0 * (s01 * s01 + s12 * s12 + s02 * s02));
     const double sr = (eff == 0.0) ? 1.e-5 : eff;
-    sy = (m.sy0 + m.jc_B * pow(pls, m.jc_n)) * (1.0 + m.jc_C * log(sr / m.jc_eps0)) * m.jc_Th;
+    if constexpr (TH) {
+      // element temperature: mean of its node temperatures (the reference
+      // reads T[e], a node array indexed by element)
+      double ts = 0.0;
+#pragma unroll
+      for (int a = 0; a < NPE; a++) ts += S.T[nid[a]];
+      const double th = (ts / NPE - m.jc_Tt) / (m.jc_Tm - m.jc_Tt);
+      jTh = 1.0 - pow(th, m.jc_m);
+    }
+    sy = (m.sy0 + m.jc_B * pow(pls, m.jc_n)) * (1.0 + m.jc_C * log(sr / m.jc_eps0)) * jTh;
   } else if (m.model == WF_MAT_HOLLOMON) {
     sy = hollomon_sy(pls, m);
   } else {
     sy = m.sy0 + m.H * pls;
   }
+  double dep = 0.0;
   if (sy < sig_trial) {
     double H;
     if (m.model == WF_MAT_JOHNSON_COOK) {
       // CalcJohnsonCookTangentModulus (Material.cuh:397-410) at min(edot, 1e6)
       const double er = (1.0e6 < eff) ? 1.0e6 : eff;
       H = (pls > 0.) ? m.jc_n * m.jc_B * pow(pls, m.jc_n - 1.) *
-                           (1.0 + m.jc_C * log(er / m.jc_eps0)) * m.jc_Th
+                           (1.0 + m.jc_C * log(er / m.jc_eps0)) * jTh
                      : m.E * 0.1;
     } else {
       H = (m.model == WF_MAT_HOLLOMON) ? hollomon_et(pls, m) : m.H;
@@ -366,8 +393,22 @@ __global__ void __launch_bounds__(kElemThreads) k_fp64_elements(StepParams P, Fp
     t0 = d0s * factor; t1 = d1s * factor; t2 = d2s * factor;
     t3 = t3 * factor; t4 = t4 * factor; t5 = t5 * factor;
     pls += dgamma;
+    dep = dgamma;
   }
   double SG[6] = {t0 - p, t1 - p, t2 - p, t3, t4, t5};
+  // plastic heat (Mechanical.C:1783-1810): 0.9 sigma : (d eps_p / dt), the
+  // plastic strain increment along the returned stress, shear terms doubled
+  double q_pl = 0.0;
+  if (TH && dep > 0.0) {
+    const double f = dep / sy;
+    const double idt = 1. / dt;
+    const double ixx = f * (SG[0] - 0.5 * (SG[1] + SG[2]));
+    const double iyy = f * (SG[1] - 0.5 * (SG[0] + SG[2]));
+    const double izz = f * (SG[2] - 0.5 * (SG[0] + SG[1]));
+    const double ixy = 1.5 * f * (SG[3]), ixz = 1.5 * f * (SG[5]), iyz = 1.5 * f * (SG[4]);
+    q_pl = 0.9 * (SG[0] * (ixx * idt) + 2.0 * SG[3] * (ixy * idt) + 2.0 * SG[5] * (ixz * idt) +
+                  SG[1] * (iyy * idt) + 2.0 * SG[4] * (iyz * idt) + SG[2] * (izz * idt));
+  }
   // total strain: eps = eps + dt * D
   {
     double e0 = S.eps[e], e1 = S.eps[ne + e], e2 = S.eps[2 * ne + e];
@@ -444,6 +485,33 @@ __global__ void __launch_bounds__(kElemThreads) k_fp64_elements(StepParams P, Fp
           fh[3 * i + k] = acc;
         }
       }
+    }
+  }
+  if constexpr (TH) {
+    // Domain_d::ThermalCalcs (Thermal.C:27-106), element part: conduction
+    // K_ij = (sum_d dN_i detJ dN_j detJ) k_T / detJ w against the node
+    // temperatures, and the plastic heat 0.9 q vol split evenly over the nodes
+    double Te[NPE];
+#pragma unroll
+    for (int a = 0; a < NPE; a++) Te[a] = S.T[nid[a]];
+    const double heat = 0.9 * q_pl;
+    const double elem_pow = heat * vol;
+    const double pow_per_node = elem_pow / NPE;
+    double *cur = S.dte + (step & 1) * ne * NPE + e * NPE;
+    const double wt = weight<NPE>();
+    for (int i = 0; i < NPE; i++) {
+      double dT = 0.0;
+      for (int k = 0; k < NPE; k++) {
+        double kk = 0.0;
+#pragma unroll
+        for (int dd = 0; dd < 3; dd++) kk += dH[dd][i] * dH[dd][k];
+        dT += kk * m.k_T / detJ * wt * Te[k];
+      }
+      const double mi = S.mass[nid[i]];
+      const double m_inv = 1.0 / mi;
+      double r = -m_inv * dT;
+      r += pow_per_node / (mi * m.cp_T);
+      cur[i] = r;
     }
   }
 }
@@ -549,6 +617,8 @@ __device__ __forceinline__ double tri_contact(const StepParams &P, const Fp64Sta
     cf[1] += F[1];
     cf[2] += F[2];
     if (P.tri_mid[j] != 0) cfn = 0.0;
+    // heat from the die (Contact.C:309), kept after the contact ends
+    if (P.thermal) S.qc[n] = P.tri_hc * P.node_area[n] * (P.tri_Tdie - S.T[n]);
     break;
   }
   S.cf[n] = cf[0];
@@ -679,6 +749,14 @@ __global__ void __launch_bounds__(kNodeThreads) k_fp64_nodes(StepParams P, Fp64S
       S.pa[k * np + n] = a;
       S.vp[k * np + n] = vnext;
     }
+    if (P.thermal) {
+      // ThermalCalcs node part (Thermal.C:108-126): element-node rates of the
+      // step gathered in list order, plus the die heat over m cp of material 0
+      const double *cur = S.dte + (P.st->step & 1) * P.ne * NPE;
+      double sT = 0.0;
+      for (int32_t k = 0; k < c; k++) sT += cur[__ldg(&P.slot[b + k])];
+      S.T[n] = S.T[n] + (sT + S.qc[n] * 1.0 / (mass * P.cp0)) * P.dt;
+    }
   }
   // reaction: block partial, then the last block to finish sums all partials
   // (each thread a fixed strided subset, then a fixed tree): deterministic.
@@ -736,25 +814,45 @@ inline unsigned grid_for(int64_t n, int threads) {
 
 int fp64_node_grid(int64_t nn) { return (int)grid_for(nn, kNodeThreads); }
 
+// Block size of the FP64 per-element and per-node kernels. GB300's FP64 rate
+// per SM is low, so a small mesh is spread over more SMs with smaller blocks
+// (down to one warp) until there are two blocks per SM; large meshes keep
+// max_threads.
+static int spread(int64_t n, int max_threads, int sms) {
+  int t = max_threads;
+  while (t > 32 && grid_for(n, t) < 2 * (int64_t)sms) t /= 2;
+  return t;
+}
+
 void fp64_geometry(const StepParams &P, const Fp64State &S, cudaStream_t st, bool store_detj) {
+  const int t = spread(P.ne, kElemThreads, P.sms);
   if (P.npe == 8)
-    k_fp64_geometry<8><<<grid_for(P.ne, kElemThreads), kElemThreads, 0, st>>>(P, S, store_detj);
+    k_fp64_geometry<8><<<grid_for(P.ne, t), t, 0, st>>>(P, S, store_detj);
   else
-    k_fp64_geometry<4><<<grid_for(P.ne, kElemThreads), kElemThreads, 0, st>>>(P, S, store_detj);
+    k_fp64_geometry<4><<<grid_for(P.ne, t), t, 0, st>>>(P, S, store_detj);
 }
 
 void fp64_nodal(const StepParams &P, const Fp64State &S, cudaStream_t st, int init_mode) {
+  const int t = spread(P.nn, kNodeThreads, P.sms);
   if (P.npe == 8)
-    k_fp64_nodal<8><<<grid_for(P.nn, kNodeThreads), kNodeThreads, 0, st>>>(P, S, init_mode);
+    k_fp64_nodal<8><<<grid_for(P.nn, t), t, 0, st>>>(P, S, init_mode);
   else
-    k_fp64_nodal<4><<<grid_for(P.nn, kNodeThreads), kNodeThreads, 0, st>>>(P, S, init_mode);
+    k_fp64_nodal<4><<<grid_for(P.nn, t), t, 0, st>>>(P, S, init_mode);
 }
 
 void fp64_elements(const StepParams &P, const Fp64State &S, cudaStream_t st) {
+  const int t = spread(P.ne, kElemThreads, P.sms);
+  const unsigned g = (unsigned)grid_for(P.ne, t);
   if (P.npe == 8)
-    k_fp64_elements<8><<<grid_for(P.ne, kElemThreads), kElemThreads, 0, st>>>(P, S);
+    if (P.thermal)
+      k_fp64_elements<8, true><<<g, t, 0, st>>>(P, S);
+    else
+      k_fp64_elements<8, false><<<g, t, 0, st>>>(P, S);
   else
-    k_fp64_elements<4><<<grid_for(P.ne, kElemThreads), kElemThreads, 0, st>>>(P, S);
+    if (P.thermal)
+      k_fp64_elements<4, true><<<g, t, 0, st>>>(P, S);
+    else
+      k_fp64_elements<4, false><<<g, t, 0, st>>>(P, S);
 }
 
 void fp64_nodes(const StepParams &P, const Fp64State &S, cudaStream_t st, int node_grid) {

@@ -15,6 +15,8 @@ namespace wf {
 struct MatDev {
   double K, G, sy0, H, cs0, hol_K, hol_m, eps0, eps1, E;
   double jc_B, jc_n, jc_C, jc_eps0, jc_Th;  // Johnson-Cook; jc_Th = 1 - T_h^m (host-computed)
+  double jc_m, jc_Tm, jc_Tt;                 // its temperature terms (thermal coupling)
+  double k_T, cp_T, exp_T;                   // conductivity, heat capacity, expansion
   int32_t model;
   int32_t pad;
 };
@@ -118,6 +120,11 @@ struct StepParams {
   float *tri_nf;            // [3 tri_ne]
   float *tri_ppf;           // [tri_ne] n . (p2 - tri_ref)
   double tri_ref[3];
+  int32_t sms;              // multiprocessors of the device (launch shapes)
+  // thermal coupling (Domain_d::ThermalCalcs), FP64 step
+  int32_t thermal;
+  double cp0;               // heat capacity of material 0 (die heat term)
+  double tri_hc, tri_Tdie;  // die heat transfer coefficient and temperature
   // energy history (Domain_d::computeEnergies after every step), when on
   int32_t energy_on;
   double *epart;          // [2 * grid of the energy kernel]
@@ -132,6 +139,11 @@ struct Fp64State {
   double *vol, *vol0, *rho, *p, *pls, *sy, *detJ;  // [ne]
   double *tau, *sig, *eps, *sr, *rr;             // [6][ne]
   double *fe, *fhg;                              // [ne][npe][3]
+  // thermal coupling: nodal temperature, die heat per node (kept after the
+  // contact ends), and the element-node temperature rates of the step in two
+  // buffers [2][ne][npe] chosen by step parity (the thermal expansion of a
+  // step reads the previous step's)
+  double *T, *qc, *dte;
 };
 
 // Mixed state. Positions are compensated float pairs (hi + lo, ~48-bit
