@@ -24,7 +24,7 @@ from weldformfem_gb300 import workloads as W
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 CLI_SRC = os.path.join(ROOT, "weldformfem_gb300", "examples", "wf_deck_solve.cpp")
 CLI_EXE = os.path.join(ROOT, "weldformfem_gb300", "_lib", "wf_deck_solve")
-REF_INPUT = "/root/reference/examples/input"
+REF_INPUT = os.path.join(H.REFERENCE_ROOT, "examples", "input")
 
 STEEL = {"type": "Bilinear", "const": [2.0e9], "density0": 7850.0, "youngsModulus": 200e9,
          "poissonsRatio": 0.3, "yieldStress0": 300e6}
