@@ -182,7 +182,7 @@ WF_API wf_status wf_set_reaction_nodes(wf_domain *d, int64_t n, const int32_t *n
 WF_API wf_status wf_set_contact_plane(wf_domain *d, double z0, double vz, double kpen, double mu,
                                       int64_t ncand, const int32_t *cand_nodes);
 
-/* Thermal coupling of the FP64 step (Domain_d::setThermalOn / setTemp,
+/* Thermal coupling (Domain_d::setThermalOn / setTemp,
  * ThermalCalcs, Thermal.C:27-126; calcThermalExpansion, :163-178): every node
  * starts at T0; each element adds to its nodes' temperature rates the
  * conduction term -(1/m_i) (K T)_i with K_ij = (sum_d dN_i detJ dN_j detJ)
@@ -196,7 +196,9 @@ WF_API wf_status wf_set_contact_plane(wf_domain *d, double z0, double vz, double
  * element-node rates read at the element's node ids, as the reference indexes
  * them. A Johnson-Cook element takes the mean of its node temperatures (the
  * reference reads T[e], a node array indexed by element). Readback:
- * wf_get_node_scalar(WF_NODE_TEMP). Before wf_init; FP64, one domain. */
+ * wf_get_node_scalar(WF_NODE_TEMP). Before wf_init; one domain (no
+ * specimens, no adjoint). The mixed-precision step evaluates the same terms
+ * in FP32 with the temperature kept as a compensated float pair. */
 WF_API wf_status wf_set_thermal(wf_domain *d, int32_t on, double T0);
 /* Conductivity k_T, heat capacity cp_T (> 0) and expansion coefficient of
  * material `mat` (Material_ k_T, cp_T, exp_T; deck keys thermalCond,

@@ -984,34 +984,39 @@ wf_status autotune_launches(wf_domain *d) {
   cudaEvent_t a, b;
   CUDA_TRY(cudaEventCreate(&a));
   CUDA_TRY(cudaEventCreate(&b));
-  // items per thread 1, 2, 4, or 0: a persistent grid (SMs x resident blocks)
+  // items per thread 1, 2, 4, or 0: a persistent grid (SMs x resident blocks).
+  // The candidates are timed in interleaved rounds so that a drift of the
+  // clocks while the GPU warms up does not favour the ones timed last.
   const int sizes[3] = {64, 128, 256}, epts[4] = {1, 2, 4, 0};
+  constexpr int kRounds = 4, kReps = 3;
   for (int phase = 0; phase < 3; phase++) {
-    double best = 1e300;
-    LaunchCfg pick = d->cfg[phase];
+    std::vector<LaunchCfg> cands;
     for (int bs : sizes)
-      for (int ept : epts) {
-        const LaunchCfg c{bs, ept};
+      for (int ept : epts) cands.push_back(LaunchCfg{bs, ept});
+    std::vector<double> total(cands.size(), 0.0);
+    for (int round = 0; round < kRounds; round++)
+      for (size_t i = 0; i < cands.size(); i++) {
+        const LaunchCfg c = cands[i];
         auto launch = [&]() {
           if (phase == 0) mix_geometry(P, M, d->mvol, d->stream, c);
           else if (phase == 1) mix_nodal(P, M, d->mvol, d->stream, c);
           else mix_elements(P, M, d->mvol, d->stream, c);
         };
-        launch();  // warm-up
+        if (round == 0) launch();  // warm-up
         cudaEventRecord(a, d->stream);
-        for (int r = 0; r < 3; r++) launch();
+        for (int r = 0; r < kReps; r++) launch();
         cudaEventRecord(b, d->stream);
         CUDA_TRY(cudaEventSynchronize(b));
         CUDA_TRY(cudaGetLastError());
         float ms = 0.f;
         CUDA_TRY(cudaEventElapsedTime(&ms, a, b));
-        if (ms / 3.0 < best) {
-          best = ms / 3.0;
-          pick = c;
-        }
+        total[i] += ms;
       }
-    d->cfg[phase] = pick;
-    d->cfg_ms[phase] = best;
+    size_t best = 0;
+    for (size_t i = 1; i < cands.size(); i++)
+      if (total[i] < total[best]) best = i;
+    d->cfg[phase] = cands[best];
+    d->cfg_ms[phase] = total[best] / (kRounds * kReps);
   }
   cudaEventDestroy(a);
   cudaEventDestroy(b);
@@ -1105,8 +1110,8 @@ WF_API wf_status wf_init(wf_domain *d) {
     return fail(d, WF_ERR_UNSUPPORTED, "contact is not supported in a batched ensemble");
   if (d->nspec && d->energy)
     return fail(d, WF_ERR_UNSUPPORTED, "the energy history is not kept for a batched ensemble");
-  if (d->thermal && (d->precision != WF_FP64 || d->nspec))
-    return fail(d, WF_ERR_UNSUPPORTED, "thermal coupling runs in the FP64 step of one domain");
+  if (d->thermal && d->nspec)
+    return fail(d, WF_ERR_UNSUPPORTED, "thermal coupling is not kept for a batched ensemble");
   if (d->thermal)
     for (size_t i = 0; i < d->mats.size(); i++)
       if (!(d->mat_thermal[i][1] > 0))
@@ -1301,7 +1306,7 @@ WF_API wf_status wf_init(wf_domain *d) {
     CUDA_TRY(dalloc(d, &P.rnode, np));
   }
   // reaction history and step state
-  d->node_grid = (d->precision == WF_MIXED) ? mix_node_grid(nn) : fp64_node_grid(nn);
+  d->node_grid = (d->precision == WF_MIXED) ? mix_node_grid(nn) : fp64_node_grid(nn, P.sms);
   CUDA_TRY(dalloc(d, &P.partials, std::max(d->node_grid, 32)));
   d->hist_cap = 1 << 16;
   CUDA_TRY(dalloc(d, &P.hist, d->hist_cap));
@@ -1339,17 +1344,20 @@ WF_API wf_status wf_init(wf_domain *d) {
   CUDA_TRY(dalloc(d, &S.eps, 6 * ne));
   CUDA_TRY(dalloc(d, &S.jr, np));
   CUDA_TRY(dalloc(d, &S.s0, np));
+  if (d->thermal) {
+    // temperature (both precisions: the mixed state exports into S.T)
+    CUDA_TRY(upload(d, &S.T, std::vector<double>(np, d->T0)));
+    P.thermal = 1;
+    P.cp0 = d->mat_thermal[0][1];
+    P.tri_hc = d->tri_hc;
+    P.tri_Tdie = d->tri_Tdie;
+  }
   if (fp64) {
     CUDA_TRY(dalloc(d, &S.vp, 3 * np));
     CUDA_TRY(dalloc(d, &S.ut, 3 * np));
     if (d->thermal) {
-      CUDA_TRY(upload(d, &S.T, std::vector<double>(np, d->T0)));
       CUDA_TRY(dalloc(d, &S.qc, np));
       CUDA_TRY(dalloc(d, &S.dte, 2 * ne * d->npe));
-      P.thermal = 1;
-      P.cp0 = d->mat_thermal[0][1];
-      P.tri_hc = d->tri_hc;
-      P.tri_Tdie = d->tri_Tdie;
     }
     CUDA_TRY(dalloc(d, &S.sr, 6 * ne));
     CUDA_TRY(dalloc(d, &S.rr, 6 * ne));
@@ -1390,6 +1398,14 @@ WF_API wf_status wf_init(wf_domain *d) {
     CUDA_TRY(dalloc(d, &M.cf, 3 * np));
     CUDA_TRY(dalloc(d, &M.ut, 3 * np));
     CUDA_TRY(dalloc(d, &M.cfn, d->tri ? np : 1));
+    if (d->thermal) {
+      // temperature as a compensated pair (T0 split into hi + lo)
+      const float hi = (float)d->T0;
+      CUDA_TRY(upload(d, &M.T, std::vector<float2>(np, make_float2(hi, (float)(d->T0 - hi)))));
+      CUDA_TRY(dalloc(d, &M.qc, np));
+      CUDA_TRY(dalloc(d, &M.dte, 2 * ne * d->npe));
+      P.f_cp0 = (float)P.cp0;
+    }
     if (d->tri) {
       // FP32 die copies relative to the centre of the part's bounding box
       double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
@@ -1444,6 +1460,12 @@ WF_API wf_status wf_init(wf_domain *d) {
       mf[i].jc_eps0 = (float)md[i].jc_eps0;
       mf[i].jc_Th = (float)md[i].jc_Th;
       mf[i].E = (float)md[i].E;
+      mf[i].jc_m = (float)md[i].jc_m;
+      mf[i].jc_Tm = (float)md[i].jc_Tm;
+      mf[i].jc_Tt = (float)md[i].jc_Tt;
+      mf[i].k_T = (float)md[i].k_T;
+      mf[i].cp_T = (float)md[i].cp_T;
+      mf[i].exp_T = (float)md[i].exp_T;
       mf[i].model = md[i].model;
     }
     MatF *mfd = nullptr;

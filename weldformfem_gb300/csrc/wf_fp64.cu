@@ -812,8 +812,6 @@ inline unsigned grid_for(int64_t n, int threads) {
 
 }  // namespace
 
-int fp64_node_grid(int64_t nn) { return (int)grid_for(nn, kNodeThreads); }
-
 // Block size of the FP64 per-element and per-node kernels. GB300's FP64 rate
 // per SM is low, so a small mesh is spread over more SMs with smaller blocks
 // (down to one warp) until there are two blocks per SM; large meshes keep
@@ -822,6 +820,10 @@ static int spread(int64_t n, int max_threads, int sms) {
   int t = max_threads;
   while (t > 32 && grid_for(n, t) < 2 * (int64_t)sms) t /= 2;
   return t;
+}
+
+int fp64_node_grid(int64_t nn, int sms) {
+  return (int)grid_for(nn, spread(nn, kNodeThreads, sms));
 }
 
 void fp64_geometry(const StepParams &P, const Fp64State &S, cudaStream_t st, bool store_detj) {
@@ -856,10 +858,12 @@ void fp64_elements(const StepParams &P, const Fp64State &S, cudaStream_t st) {
 }
 
 void fp64_nodes(const StepParams &P, const Fp64State &S, cudaStream_t st, int node_grid) {
+  // node_grid = fp64_node_grid(P.nn, P.sms): blocks of the spread size
+  const int t = spread(P.nn, kNodeThreads, P.sms);
   if (P.npe == 8)
-    k_fp64_nodes<8><<<node_grid, kNodeThreads, 0, st>>>(P, S);
+    k_fp64_nodes<8><<<node_grid, t, 0, st>>>(P, S);
   else
-    k_fp64_nodes<4><<<node_grid, kNodeThreads, 0, st>>>(P, S);
+    k_fp64_nodes<4><<<node_grid, t, 0, st>>>(P, S);
 }
 
 void fp64_predict(const StepParams &P, const Fp64State &S, cudaStream_t st) {

@@ -25,6 +25,7 @@ struct MatDev {
 struct MatF {
   float K, G, sy0, H, cs0, rho, hol_K, hol_m, eps0, eps1;
   float jc_B, jc_n, jc_C, jc_eps0, jc_Th, E;
+  float jc_m, jc_Tm, jc_Tt, k_T, cp_T, exp_T;
   int32_t model;
   int32_t pad;
 };
@@ -121,6 +122,7 @@ struct StepParams {
   float *tri_ppf;           // [tri_ne] n . (p2 - tri_ref)
   double tri_ref[3];
   int32_t sms;              // multiprocessors of the device (launch shapes)
+  float f_cp0;              // FP32 heat capacity of material 0 (mixed thermal)
   // thermal coupling (Domain_d::ThermalCalcs), FP64 step
   int32_t thermal;
   double cp0;               // heat capacity of material 0 (die heat term)
@@ -162,6 +164,10 @@ struct MixState {
   float *fe;                      // [ne][npe][3] element force minus hourglass force
   double *x0;                     // [3][np] initial positions (export only)
   float *edot;                    // [ne] sigma . str_rate * vol (energy history only)
+  // thermal coupling: temperature as a compensated pair, die heat per node,
+  // element-node temperature rates [2][ne][npe] chosen by step parity
+  float2 *T;
+  float *qc, *dte;
 };
 
 // Records `msg` as the domain's last error and returns s (wf_api.cu).
@@ -178,7 +184,7 @@ void fp64_elements(const StepParams &P, const Fp64State &S, cudaStream_t st);
 void fp64_nodes(const StepParams &P, const Fp64State &S, cudaStream_t st, int node_grid);
 void fp64_predict(const StepParams &P, const Fp64State &S, cudaStream_t st);
 void fp64_density(const StepParams &P, const Fp64State &S, const double *rho0, cudaStream_t st);
-int fp64_node_grid(int64_t nn);
+int fp64_node_grid(int64_t nn, int sms);
 
 // Launch shape of a tunable kernel: block size and items per thread
 // (grid-stride loop; grid = ceil(n / (bs * ept))).

@@ -237,6 +237,9 @@ __device__ __forceinline__ void tri_contact_mixed(const StepParams &P, const Mix
       M.cf[q * np + n] = cf[q] + F[q];
     }
     if (__ldg(&P.tri_mid[j]) == 0) cfn = cfn_j;
+    // heat from the die (Contact.C:309), kept after the contact ends
+    if (P.thermal)
+      M.qc[n] = (float)(P.tri_hc * P.node_area[n]) * ((float)P.tri_Tdie - M.T[n].x);
     break;
   }
   M.cfn[n] = cfn;
@@ -324,11 +327,11 @@ __global__ void __launch_bounds__(BS) k_mix_nodal(StepParams P, MixState M, cons
 // Writes the new tau and eps_p; returns sigma = tau - p I in sg.
 // LAW = 0: linear hardening only (the common case, fewer registers); LAW = 1:
 // every material model.
-template <int LAW>
+template <int LAW, bool TH>
 __device__ __forceinline__ void stress_update(const StepParams &P, const MixState &M, int64_t e,
                                               const MatF &m, const float (&sr)[6], float w01,
-                                              float w12, float w02, float p, float (&sg)[6],
-                                              float &sdot) {
+                                              float w12, float w02, float p, float jTh,
+                                              float (&sg)[6], float &sdot, float &qpl) {
   const int64_t ne = P.ne;
   const float dt = P.espec ? P.specf[P.espec[e]].dt : P.f_dt;
   float t0 = M.tau[e], t1 = M.tau[ne + e], t2 = M.tau[2 * ne + e];
@@ -359,6 +362,7 @@ __device__ __forceinline__ void stress_update(const StepParams &P, const MixStat
   float pls = M.pls[e];
   float sy;
   float eff = 0.f;
+  float dep = 0.f;
   if (LAW == 0) {
     sy = m.sy0 + m.H * pls;
   } else if (m.model == WF_MAT_JOHNSON_COOK) {
@@ -367,7 +371,7 @@ __device__ __forceinline__ void stress_update(const StepParams &P, const MixStat
                 3.0f * (sr[3] * sr[3] + sr[4] * sr[4] + sr[5] * sr[5]));
     const float srate = (eff == 0.f) ? 1.e-5f : eff;
     sy = (m.sy0 + m.jc_B * powf(pls, m.jc_n)) * (1.0f + m.jc_C * logf(srate / m.jc_eps0)) *
-         m.jc_Th;
+         jTh;
   } else if (m.model == WF_MAT_HOLLOMON) {
     sy = (pls + m.eps0 > m.eps1) ? m.hol_K * powf(pls + m.eps0, m.hol_m) : m.sy0;
   } else {
@@ -380,7 +384,7 @@ __device__ __forceinline__ void stress_update(const StepParams &P, const MixStat
     } else if (m.model == WF_MAT_JOHNSON_COOK) {
       const float er = (1.0e6f < eff) ? 1.0e6f : eff;
       H = (pls > 0.f) ? m.jc_n * m.jc_B * powf(pls, m.jc_n - 1.f) *
-                            (1.0f + m.jc_C * logf(er / m.jc_eps0)) * m.jc_Th
+                            (1.0f + m.jc_C * logf(er / m.jc_eps0)) * jTh
                       : m.E * 0.1f;
     } else {
       H = (m.model == WF_MAT_HOLLOMON)
@@ -394,12 +398,23 @@ __device__ __forceinline__ void stress_update(const StepParams &P, const MixStat
     t0 = d0s * factor; t1 = d1s * factor; t2 = d2s * factor;
     t3 *= factor; t4 *= factor; t5 *= factor;
     pls += dgamma;
+    dep = dgamma;
   }
   M.pls[e] = pls;
   M.tau[e] = t0; M.tau[ne + e] = t1; M.tau[2 * ne + e] = t2;
   M.tau[3 * ne + e] = t3; M.tau[4 * ne + e] = t4; M.tau[5 * ne + e] = t5;
   sg[0] = t0 - p; sg[1] = t1 - p; sg[2] = t2 - p;
   sg[3] = t3; sg[4] = t4; sg[5] = t5;
+  // plastic heat 0.9 sigma : (d eps_p / dt) (Mechanical.C:1783-1810)
+  if (TH && dep > 0.f) {
+    const float f = dep / sy;
+    const float ixx = f * (sg[0] - 0.5f * (sg[1] + sg[2]));
+    const float iyy = f * (sg[1] - 0.5f * (sg[0] + sg[2]));
+    const float izz = f * (sg[2] - 0.5f * (sg[0] + sg[1]));
+    const float ixy = 1.5f * f * sg[3], iyz = 1.5f * f * sg[4], ixz = 1.5f * f * sg[5];
+    qpl = 0.9f * (sg[0] * ixx + 2.0f * sg[3] * ixy + 2.0f * sg[5] * ixz + sg[1] * iyy +
+                  2.0f * sg[4] * iyz + sg[2] * izz) / dt;
+  }
   // sigma . str_rate over the six stored components (energy history)
   if (P.energy_on)
     sdot = sg[0] * sr[0] + sg[1] * sr[1] + sg[2] * sr[2] + sg[3] * sr[3] + sg[4] * sr[4] +
@@ -445,14 +460,55 @@ __device__ __forceinline__ void walsh8_synth(const float (&o)[8], float (&v)[8])
   v[6] = a3 + b3; v[7] = a3 - b3;
 }
 
+// Thermal coupling, element side (the FP64 step's restatement of
+// calcThermalExpansion and ThermalCalcs in FP32). Before the stress update:
+// the strain rate's diagonal loses exp_T times the mean of the previous step's
+// element-node rates read at the element's node ids, and a Johnson-Cook
+// element's temperature factor uses the mean of its node temperatures.
+template <int NPE, bool CG>
+__device__ __forceinline__ void thermal_pre(const StepParams &P, const MixState &M,
+                                            const MatF &m, const int32_t (&nid)[NPE],
+                                            long long step, float (&sr)[6], float &jTh) {
+  const float *prev = M.dte + ((step + 1) & 1) * P.ne * NPE;
+  float g = 0.f, ts = 0.f;
+#pragma unroll
+  for (int a = 0; a < NPE; a++) {
+    g += ldx<CG>(&prev[nid[a]]);
+    ts += ldx<CG>(&M.T[nid[a]]).x;
+  }
+  const float c = m.exp_T * (g * (1.0f / NPE));
+  sr[0] -= c;
+  sr[1] -= c;
+  sr[2] -= c;
+  if (m.model == WF_MAT_JOHNSON_COOK)
+    jTh = 1.0f - powf((ts * (1.0f / NPE) - m.jc_Tt) / (m.jc_Tm - m.jc_Tt), m.jc_m);
+}
+
+// After the forces: the element-node temperature rates -(K T)_a / m_a plus the
+// plastic heat 0.9 q vol / n / (m_a cp_T), written to the step's buffer.
+// KT holds (K T)_a / kf; qvol = q vol.
+template <int NPE, bool CG>
+__device__ __forceinline__ void thermal_rates(const StepParams &P, const MixState &M,
+                                              const MatF &m, int64_t e,
+                                              const int32_t (&nid)[NPE], long long step,
+                                              const float (&KT)[NPE], float kf, float qvol) {
+  float *cur = M.dte + (step & 1) * P.ne * NPE + e * NPE;
+  const float ppn = 0.9f * qvol * (1.0f / NPE);
+#pragma unroll
+  for (int a = 0; a < NPE; a++) {
+    const float mi = ldx<CG>(&M.mass[nid[a]]);
+    cur[a] = -(kf * KT[a]) / mi + ppn / (mi * m.cp_T);
+  }
+}
+
 // Hexahedron: with dN_a/dx = (1/8) adj(J)^T-row . s(a) / detJ at the centre,
 // the velocity gradient is adj(J) G / (8 detJ) with G the Walsh sums of the
 // nodal velocities, and the nodal forces are the synthesis of
 // T = adj(J)^T sigma (w / 8 = 1) plus the hourglass coefficients ch h_j.
 // Same quantities as the reference's per-node loops, fewer operations.
-template <int LAW, bool CG>
+template <int LAW, bool CG, bool TH>
 __device__ __forceinline__ void element_hex(const StepParams &P, const MixState &M, int64_t e,
-                                            float *stash, int stride) {
+                                            float *stash, int stride, long long step) {
   const int64_t ne = P.ne, np = P.np;
   int32_t nid[8];
   float A[3][3], detJ;
@@ -516,16 +572,18 @@ __device__ __forceinline__ void element_hex(const StepParams &P, const MixState 
   for (int i = 0; i < 3; i++)
 #pragma unroll
     for (int k = 0; k < 3; k++) L[i][k] = fl * (A[i][0] * G[0][k] + A[i][1] * G[1][k] + A[i][2] * G[2][k]);
-  const float sr[6] = {L[0][0], L[1][1], L[2][2], 0.5f * (L[1][0] + L[0][1]),
-                       0.5f * (L[2][1] + L[1][2]), 0.5f * (L[2][0] + L[0][2])};
+  float sr[6] = {L[0][0], L[1][1], L[2][2], 0.5f * (L[1][0] + L[0][1]),
+                 0.5f * (L[2][1] + L[1][2]), 0.5f * (L[2][0] + L[0][2])};
   const float w01 = 0.5f * (L[1][0] - L[0][1]);
   const float w12 = 0.5f * (L[2][1] - L[1][2]);
   const float w02 = 0.5f * (L[2][0] - L[0][2]);
+  float jTh = m.jc_Th;
+  if constexpr (TH) thermal_pre<8, CG>(P, M, m, nid, step, sr, jTh);
   float J_bar = J_avg * 0.125f;
   if (J_bar < 0.0f) J_bar = 0.2f;
   const float p = -m.K * (J_bar - 1.0f);
-  float sg[6], sdot = 0.f;
-  stress_update<LAW>(P, M, e, m, sr, w01, w12, w02, p, sg, sdot);
+  float sg[6], sdot = 0.f, qpl = 0.f;
+  stress_update<LAW, TH>(P, M, e, m, sr, w01, w12, w02, p, jTh, sg, sdot, qpl);
   if (P.energy_on) M.edot[e] = sdot * vol;
   // sigma as a symmetric 3x3: S[i][k]
   const float S[3][3] = {{sg[0], sg[3], sg[5]}, {sg[3], sg[1], sg[4]}, {sg[5], sg[4], sg[2]}};
@@ -542,11 +600,29 @@ __device__ __forceinline__ void element_hex(const StepParams &P, const MixState 
 #pragma unroll
     for (int a = 0; a < 8; a++) M.fe[(a * 3 + k) * ne + e] = f[a];
   }
+  if constexpr (TH) {
+    // conduction in the same Walsh form: grad T detJ = A (Walsh sums of T) / 8,
+    // (K T)_a = k_T / detJ * synthesis of A^T grad T detJ (w = 8 cancels 1/8)
+    float tv[8], oT[8], KT[8];
+#pragma unroll
+    for (int a = 0; a < 8; a++) tv[a] = ldx<CG>(&M.T[nid[a]]).x;
+    walsh8(tv, oT);
+    float BT[3];
+#pragma unroll
+    for (int d = 0; d < 3; d++)
+      BT[d] = 0.125f * (A[d][0] * oT[1] + A[d][1] * oT[2] + A[d][2] * oT[3]);
+    float o[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+    for (int mm = 0; mm < 3; mm++) o[1 + mm] = A[0][mm] * BT[0] + A[1][mm] * BT[1] + A[2][mm] * BT[2];
+    walsh8_synth(o, KT);
+    thermal_rates<8, CG>(P, M, m, e, nid, step, KT, m.k_T / detJ, qpl * vol);
+  }
 }
 
 // Tetrahedron: per-node shape derivatives (Domain_d.C:1866-1887).
-template <int LAW, bool CG>
-__device__ __forceinline__ void element_tet(const StepParams &P, const MixState &M, int64_t e) {
+template <int LAW, bool CG, bool TH>
+__device__ __forceinline__ void element_tet(const StepParams &P, const MixState &M, int64_t e,
+                                            long long step) {
   const int64_t ne = P.ne;
   int32_t nid[4];
   float dH[3][4];
@@ -582,14 +658,16 @@ __device__ __forceinline__ void element_tet(const StepParams &P, const MixState 
   }
   const float f = 1.0f / detJ;
   const float fh = 0.5f * f;
-  const float sr[6] = {s00 * f, s11 * f, s22 * f, s01 * fh, s12 * fh, s02 * fh};
+  float sr[6] = {s00 * f, s11 * f, s22 * f, s01 * fh, s12 * fh, s02 * fh};
   w01 *= fh; w12 *= fh; w02 *= fh;
+  float jTh = m.jc_Th;
+  if constexpr (TH) thermal_pre<4, CG>(P, M, m, nid, step, sr, jTh);
   J_avg *= 0.25f;
   float J_bar = J_avg;
   if (J_bar < 0.0f) J_bar = 0.2f;
   const float p = -m.K * (J_bar - 1.0f);
-  float sg[6], sdot = 0.f;
-  stress_update<LAW>(P, M, e, m, sr, w01, w12, w02, p, sg, sdot);
+  float sg[6], sdot = 0.f, qpl = 0.f;
+  stress_update<LAW, TH>(P, M, e, m, sr, w01, w12, w02, p, jTh, sg, sdot, qpl);
   const float w = weightf<4>();
   if (P.energy_on) M.edot[e] = sdot * (detJ * w);
 #pragma unroll
@@ -599,26 +677,46 @@ __device__ __forceinline__ void element_tet(const StepParams &P, const MixState 
     M.fe[(a * 3 + 1) * ne + e] = (d1 * sg[1] + d0 * sg[3] + d2 * sg[4]) * w;
     M.fe[(a * 3 + 2) * ne + e] = (d2 * sg[2] + d1 * sg[4] + d0 * sg[5]) * w;
   }
+  if constexpr (TH) {
+    // conduction K_ij = (sum_d dN_i detJ dN_j detJ) k_T / detJ w against the
+    // temperatures relative to node 0's (K's rows sum to zero): no FP32
+    // cancellation between the absolute temperatures
+    float Te[4], KT[4];
+    const float T0n = ldx<CG>(&M.T[nid[0]]).x;
+    Te[0] = 0.f;
+#pragma unroll
+    for (int a = 1; a < 4; a++) Te[a] = ldx<CG>(&M.T[nid[a]]).x - T0n;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+      float t = 0.f;
+#pragma unroll
+      for (int k = 0; k < 4; k++)
+        t += (dH[0][i] * dH[0][k] + dH[1][i] * dH[1][k] + dH[2][i] * dH[2][k]) * Te[k];
+      KT[i] = t;
+    }
+    thermal_rates<4, CG>(P, M, m, e, nid, step, KT, m.k_T / detJ * w, qpl * (detJ * w));
+  }
 }
 
-template <int NPE, int LAW, bool CG>
+template <int NPE, int LAW, bool CG, bool TH>
 __device__ __forceinline__ void element_one(const StepParams &P, const MixState &M, int64_t e,
-                                            float *stash, int stride) {
+                                            float *stash, int stride, long long step) {
   if constexpr (NPE == 8)
-    element_hex<LAW, CG>(P, M, e, stash, stride);
+    element_hex<LAW, CG, TH>(P, M, e, stash, stride, step);
   else
-    element_tet<LAW, CG>(P, M, e);
+    element_tet<LAW, CG, TH>(P, M, e, step);
 }
 
 // Registers per thread stay <= 64 at 1024 resident threads per SM.
 constexpr int elem_min_blocks(int bs) { return 1024 / bs; }
 
-template <int NPE, int BS, int LAW>
+template <int NPE, int BS, int LAW, bool TH>
 __global__ void __launch_bounds__(BS, elem_min_blocks(BS)) k_mix_elements(StepParams P,
                                                                           MixState M) {
   __shared__ float stash[NPE == 8 ? 12 * BS : 1];
+  const long long step = TH ? P.st->step : 0;
   for (int64_t e = (int64_t)blockIdx.x * BS + threadIdx.x; e < P.ne; e += (int64_t)gridDim.x * BS)
-    element_one<NPE, LAW, false>(P, M, e, &stash[threadIdx.x], BS);
+    element_one<NPE, LAW, false, TH>(P, M, e, &stash[threadIdx.x], BS, step);
 }
 
 // ---------------------------------------------------------------------------
@@ -656,7 +754,8 @@ __device__ __forceinline__ double block_sum_dense(double v, double *sh) {
 // accelerations, velocity BCs, Chung-Hulbert corrector and the next
 // predictor. Returns the node's reaction contribution.
 template <int NPE, bool CG>
-__device__ __forceinline__ float node_one(const StepParams &P, const MixState &M, int64_t n) {
+__device__ __forceinline__ float node_one(const StepParams &P, const MixState &M, int64_t n,
+                                          long long step) {
   float r = 0.0f;
   const int64_t np = P.np;
   const int32_t b = __ldg(&P.off[n]), c = __ldg(&P.off[n + 1]) - b;
@@ -745,6 +844,14 @@ __device__ __forceinline__ float node_one(const StepParams &P, const MixState &M
     M.pa[k * np + n] = a;
     M.vp[k * np + n] = vnext;
   }
+  if (P.thermal) {
+    // ThermalCalcs node part: the step's element-node rates in list order and
+    // the die heat over m cp of material 0
+    const float *cur = M.dte + (step & 1) * ne * NPE;
+    float sT = 0.f;
+    for (int32_t k = 0; k < c; k++) sT += ldx<CG>(&cur[__ldg(&P.slot[b + k])]);
+    M.T[n] = pair_add(M.T[n], (sT + M.qc[n] / (mass * P.f_cp0)) * c_dt);
+  }
   return r;
 }
 
@@ -753,7 +860,7 @@ __global__ void __launch_bounds__(kNodeThreads, 6) k_mix_nodes(StepParams P, Mix
   __shared__ double sh[kNodeThreads / 32];
   __shared__ bool am_last;
   const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const float r = (n < P.nn) ? node_one<NPE, false>(P, M, n) : 0.0f;
+  const float r = (n < P.nn) ? node_one<NPE, false>(P, M, n, P.st->step) : 0.0f;
   // reaction: only warps holding a contribution reduce (FP64, fixed order);
   // the last block to finish sums all block partials with the whole block.
   const double bs = block_sum_sparse(r, sh);
@@ -799,7 +906,7 @@ __device__ __forceinline__ void cluster_barrier() {
   asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory");
 }
 
-template <int NPE, int BS, int LAW>
+template <int NPE, int BS, int LAW, bool TH>
 __global__ void __launch_bounds__(BS) k_mix_cluster_run(StepParams P, MixState M, float *vol,
                                                         double *part, int64_t nsteps) {
   __shared__ float stash[NPE == 8 ? 12 * BS : 1];
@@ -816,10 +923,11 @@ __global__ void __launch_bounds__(BS) k_mix_cluster_run(StepParams P, MixState M
     for (int64_t n = n0 + t; n < n1; n += BS) nodal_one<NPE, true>(P, M, vol, n, time);
     cluster_barrier();
     for (int64_t e = e0 + t; e < e1; e += BS)
-      element_one<NPE, LAW, true>(P, M, e, &stash[t], BS);
+      element_one<NPE, LAW, true, TH>(P, M, e, &stash[t], BS, step0 + it);
     cluster_barrier();
     double r = 0.0;
-    for (int64_t n = n0 + t; n < n1; n += BS) r += (double)node_one<NPE, true>(P, M, n);
+    for (int64_t n = n0 + t; n < n1; n += BS)
+      r += (double)node_one<NPE, true>(P, M, n, step0 + it);
     const double bsum = block_sum_dense(r, sh);
     if (t == 0) part[it * nb + b] = bsum;   // step it, block b
     cluster_barrier();
@@ -889,6 +997,7 @@ __global__ void k_mix_export_nodes(StepParams P, MixState M, Fp64State S) {
   }
   S.mass[n] = M.mass[n];
   S.jr[n] = M.jr[n];
+  if (P.thermal) S.T[n] = (double)M.T[n].x + (double)M.T[n].y;
 }
 
 template <int NPE>
@@ -1005,22 +1114,22 @@ void launch_nodal(const StepParams &P, const MixState &M, const float *vol, cuda
   }
 }
 
-template <int NPE, int LAW>
+template <int NPE, int LAW, bool TH>
 void launch_elements_law(const StepParams &P, const MixState &M, cudaStream_t st, LaunchCfg c) {
   switch (c.bs) {
     case 64: {
-      const unsigned g = tuned_grid(k_mix_elements<NPE, 64, LAW>, 64, c.ept, P.ne);
-      k_mix_elements<NPE, 64, LAW><<<g, 64, 0, st>>>(P, M);
+      const unsigned g = tuned_grid(k_mix_elements<NPE, 64, LAW, TH>, 64, c.ept, P.ne);
+      k_mix_elements<NPE, 64, LAW, TH><<<g, 64, 0, st>>>(P, M);
       break;
     }
     case 256: {
-      const unsigned g = tuned_grid(k_mix_elements<NPE, 256, LAW>, 256, c.ept, P.ne);
-      k_mix_elements<NPE, 256, LAW><<<g, 256, 0, st>>>(P, M);
+      const unsigned g = tuned_grid(k_mix_elements<NPE, 256, LAW, TH>, 256, c.ept, P.ne);
+      k_mix_elements<NPE, 256, LAW, TH><<<g, 256, 0, st>>>(P, M);
       break;
     }
     default: {
-      const unsigned g = tuned_grid(k_mix_elements<NPE, 128, LAW>, 128, c.ept, P.ne);
-      k_mix_elements<NPE, 128, LAW><<<g, 128, 0, st>>>(P, M);
+      const unsigned g = tuned_grid(k_mix_elements<NPE, 128, LAW, TH>, 128, c.ept, P.ne);
+      k_mix_elements<NPE, 128, LAW, TH><<<g, 128, 0, st>>>(P, M);
       break;
     }
   }
@@ -1028,16 +1137,23 @@ void launch_elements_law(const StepParams &P, const MixState &M, cudaStream_t st
 
 template <int NPE>
 void launch_elements(const StepParams &P, const MixState &M, cudaStream_t st, LaunchCfg c) {
-  if (P.mat_general)
-    launch_elements_law<NPE, 1>(P, M, st, c);
-  else
-    launch_elements_law<NPE, 0>(P, M, st, c);
+  if (P.thermal) {
+    if (P.mat_general)
+      launch_elements_law<NPE, 1, true>(P, M, st, c);
+    else
+      launch_elements_law<NPE, 0, true>(P, M, st, c);
+  } else if (P.mat_general) {
+    launch_elements_law<NPE, 1, false>(P, M, st, c);
+  } else {
+    launch_elements_law<NPE, 0, false>(P, M, st, c);
+  }
 }
 
 template <int NPE, int BS, int LAW>
 cudaError_t cluster_launch(const StepParams &P, const MixState &M, float *vol, double *part,
                            int64_t nsteps, int blocks, cudaStream_t st, bool query, int *fits) {
-  auto kern = k_mix_cluster_run<NPE, BS, LAW>;
+  auto kern = P.thermal ? k_mix_cluster_run<NPE, BS, LAW, true>
+                        : k_mix_cluster_run<NPE, BS, LAW, false>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
   if (e != cudaSuccess) return e;
   cudaLaunchConfig_t cfg = {};
