@@ -156,3 +156,15 @@ def test_thermal_options():
         d.node_scalar("T")                          # thermal coupling off
     with pytest.raises(wf.WfError):
         d.set_thermal(True, 20.0)                   # after init
+
+
+@pytest.mark.gpu
+def test_vtk_writes_temperature(tmp_path):
+    case, extra, steps = cases()["tet_hollomon"]
+    d = run(wf.Domain(wf.WF_FP64), case, extra, 50)
+    out = tmp_path / "t.vtk"
+    d.write_vtk(str(out))
+    text = out.read_text().splitlines()
+    i = text.index("SCALARS Temp double 1")
+    T = np.array([float(v) for v in text[i + 2:i + 2 + case.n_node]])
+    np.testing.assert_allclose(T, d.node_scalar("T"), rtol=1e-8, atol=0)

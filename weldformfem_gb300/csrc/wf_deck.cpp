@@ -1113,8 +1113,8 @@ WF_API wf_status wf_load_lsdyna(wf_domain *d, const char *path) {
 // ---- VTK -------------------------------------------------------------------------
 // Legacy ASCII unstructured grid of the current state with the field names of
 // the reference's VTKWriter (VTKWriter.C:246-650): point data DISP, Velocity,
-// Acceleration, nod_mass, ContForce; cell data pressure, pl_strain, Vol, Rho,
-// sigy and the stress tensor SIGMA.
+// Acceleration, nod_mass, ContForce and, with thermal coupling, Temp; cell data
+// pressure, pl_strain, Vol, Rho, sigy and the stress tensor SIGMA.
 WF_API wf_status wf_write_vtk(wf_domain *d, const char *path) {
   if (!d || !path) return WF_ERR_ARG;
   int64_t nn = 0, ne = 0, tot = 0;
@@ -1163,6 +1163,14 @@ WF_API wf_status wf_write_vtk(wf_domain *d, const char *path) {
   vec("ContForce", cf);
   std::fprintf(f, "SCALARS nod_mass double 1\nLOOKUP_TABLE default\n");
   for (int64_t n = 0; n < nn; n++) std::fprintf(f, "%.9g\n", mass[n]);
+  {
+    // temperature (VTKWriter.C:434-441), when the thermal coupling is on
+    std::vector<double> T(nn);
+    if (wf_get_node_scalar(d, WF_NODE_TEMP, T.data()) == WF_OK) {
+      std::fprintf(f, "SCALARS Temp double 1\nLOOKUP_TABLE default\n");
+      for (int64_t n = 0; n < nn; n++) std::fprintf(f, "%.9g\n", T[n]);
+    }
+  }
   std::fprintf(f, "CELL_DATA %lld\n", (long long)ne);
   auto scal = [&](const char *name, const std::vector<double> &w) {
     std::fprintf(f, "SCALARS %s double 1\nLOOKUP_TABLE default\n", name);
