@@ -282,9 +282,10 @@ WF_API wf_status wf_set_phase_timing(wf_domain *d, int32_t on);
 WF_API wf_status wf_get_phase_times(wf_domain *d, double ms[4], int64_t *steps, int32_t reset);
 /* Launch-shape autotuning of the mixed-precision geometry, nodal and element
  * kernels (on by default): at wf_init the library times each kernel on the
- * domain's own data for block sizes {64, 128, 256} x {1, 2, 4} items per
+ * domain's own data for block sizes {64, 128, 256} x {1, 2} items per
  * thread or a persistent grid of (SMs x resident blocks) (items_per_thread
- * reported as 0), all grid-stride, and keeps the fastest; the kernels' results do not
+ * reported as 0), all grid-stride, timed in interleaved rounds, and keeps the
+ * fastest; the kernels' results do not
  * depend on the shape, and the state the element kernel advances is restored
  * after the trials. wf_get_launch_config reports the choice for phase 0
  * (geometry), 1 (nodal) or 2 (element). */

@@ -13,6 +13,8 @@
 #include <map>
 #include <new>
 #include <string>
+#include <thread>
+#include <atomic>
 #include <tuple>
 #include <vector>
 
@@ -245,31 +247,137 @@ void free_device(wf_domain *d) {
   d->initialized = false;
 }
 
-// Node -> element lists, element-ascending per node (setNodElem,
-// Domain_d.C:1508-1611; tail of AddBoxLength, :1436-1481).
-bool build_nodel(wf_domain *d) {
-  d->nodel_cnt.assign(d->nn, 0);
-  for (int32_t n : d->elnod) {
-    if (n < 0 || n >= d->nn) return false;
-    d->nodel_cnt[n]++;
+// Host threads for the setup loops over large meshes: f(begin, end) on
+// contiguous chunks of [0, n); small ranges run inline.
+template <typename F>
+void host_parallel(int64_t n, F f) {
+  constexpr int64_t kMinChunk = int64_t(1) << 20;
+  int64_t T = (int64_t)std::min(32u, std::max(1u, std::thread::hardware_concurrency()));
+  T = std::min<int64_t>(T, (n + kMinChunk - 1) / kMinChunk);
+  if (T <= 1) {
+    f((int64_t)0, n);
+    return;
   }
-  d->nodel_off.assign(d->nn + 1, 0);
+  std::vector<std::thread> th;
+  for (int64_t t = 0; t < T; t++) th.emplace_back(f, n * t / T, n * (t + 1) / T);
+  for (std::thread &x : th) x.join();
+}
+
+// Node -> element lists, element-ascending per node (setNodElem,
+// Domain_d.C:1508-1611; tail of AddBoxLength, :1436-1481), built by host
+// threads over contiguous element chunks: (1) each chunk counts its entries
+// per node (8-bit counters, one array per chunk); (2) per node, the chunks'
+// counts become their starting ranks (chunk order = element order) and the
+// totals give the offsets; (3) each chunk places its entries in element order
+// from those ranks. Every list comes out element-ascending, exactly as one
+// thread would build it; a node with 255 or more entries in one chunk falls
+// back to the single-threaded build.
+bool build_nodel_serial(wf_domain *d) {
+  const int64_t nn = d->nn, ent = d->ne * d->npe;
+  const int32_t *el = d->elnod.data();
+  d->nodel_cnt.assign(nn, 0);
+  for (int64_t i = 0; i < ent; i++) d->nodel_cnt[el[i]]++;
+  d->nodel_off.assign(nn + 1, 0);
   int64_t tot = 0;
-  for (int64_t n = 0; n < d->nn; n++) {
+  for (int64_t n = 0; n < nn; n++) {
     d->nodel_off[n] = (int32_t)tot;
     tot += d->nodel_cnt[n];
   }
-  d->nodel_off[d->nn] = (int32_t)tot;
+  d->nodel_off[nn] = (int32_t)tot;
   d->nodel.assign(tot, 0);
   d->nodel_loc.assign(tot, 0);
-  std::vector<int32_t> fill(d->nn, 0);
-  for (int64_t e = 0; e < d->ne; e++)
-    for (int a = 0; a < d->npe; a++) {
-      int32_t n = d->elnod[e * d->npe + a];
-      int64_t k = d->nodel_off[n] + fill[n]++;
-      d->nodel[k] = (int32_t)e;
-      d->nodel_loc[k] = a;
+  std::vector<int32_t> fill(nn, 0);
+  for (int64_t i = 0; i < ent; i++) {
+    const int32_t n = el[i];
+    const int64_t k = d->nodel_off[n] + fill[n]++;
+    d->nodel[k] = (int32_t)(i / d->npe);
+    d->nodel_loc[k] = (int32_t)(i % d->npe);
+  }
+  return true;
+}
+
+bool build_nodel(wf_domain *d) {
+  const int64_t nn = d->nn, ne = d->ne, ent = ne * d->npe;
+  const int npe = d->npe;
+  const int32_t *el = d->elnod.data();
+  // validation, in parallel
+  std::atomic<bool> bad{false};
+  host_parallel(ent, [&](int64_t i0, int64_t i1) {
+    for (int64_t i = i0; i < i1; i++)
+      if (el[i] < 0 || el[i] >= nn) {
+        bad = true;
+        return;
+      }
+  });
+  if (bad) return false;
+  const int64_t T = std::min<int64_t>(
+      std::min(32u, std::max(1u, std::thread::hardware_concurrency())),
+      std::max<int64_t>(1, ent / (int64_t(1) << 20)));
+  if (T <= 1) return build_nodel_serial(d);
+  std::vector<std::vector<uint8_t>> rank(T);
+  std::atomic<bool> overflow{false};
+  auto chunk = [&](int64_t t, int64_t &e0, int64_t &e1) {
+    e0 = ne * t / T;
+    e1 = ne * (t + 1) / T;
+  };
+  {  // (1) per-chunk counts
+    std::vector<std::thread> th;
+    for (int64_t t = 0; t < T; t++)
+      th.emplace_back([&, t]() {
+        rank[t].assign(nn, 0);
+        uint8_t *c = rank[t].data();
+        int64_t e0, e1;
+        chunk(t, e0, e1);
+        for (int64_t i = e0 * npe; i < e1 * npe; i++)
+          if (++c[el[i]] == 255) overflow = true;
+      });
+    for (std::thread &x : th) x.join();
+  }
+  if (overflow) return build_nodel_serial(d);
+  // (2) per node: totals, and each chunk's starting rank within the node's list
+  d->nodel_cnt.assign(nn, 0);
+  int32_t *cnt = d->nodel_cnt.data();
+  host_parallel(nn, [&](int64_t n0, int64_t n1) {
+    for (int64_t n = n0; n < n1; n++) {
+      int32_t r = 0;
+      for (int64_t t = 0; t < T; t++) {
+        const uint8_t c = rank[t][n];
+        rank[t][n] = (uint8_t)r;
+        r += c;
+      }
+      cnt[n] = r;
     }
+  });
+  bool big = false;
+  for (int64_t n = 0; n < nn && !big; n++) big = cnt[n] > 255;
+  if (big) return build_nodel_serial(d);
+  d->nodel_off.assign(nn + 1, 0);
+  int64_t tot = 0;
+  for (int64_t n = 0; n < nn; n++) {
+    d->nodel_off[n] = (int32_t)tot;
+    tot += cnt[n];
+  }
+  d->nodel_off[nn] = (int32_t)tot;
+  d->nodel.assign(tot, 0);
+  d->nodel_loc.assign(tot, 0);
+  const int32_t *off = d->nodel_off.data();
+  int32_t *lst = d->nodel.data(), *loc = d->nodel_loc.data();
+  {  // (3) placement in element order from each chunk's ranks
+    std::vector<std::thread> th;
+    for (int64_t t = 0; t < T; t++)
+      th.emplace_back([&, t]() {
+        uint8_t *r = rank[t].data();
+        int64_t e0, e1;
+        chunk(t, e0, e1);
+        for (int64_t i = e0 * npe; i < e1 * npe; i++) {
+          const int32_t n = el[i];
+          const int64_t k = off[n] + r[n]++;
+          lst[k] = (int32_t)(i / npe);
+          loc[k] = (int32_t)(i % npe);
+        }
+      });
+    for (std::thread &x : th) x.join();
+  }
   return true;
 }
 
@@ -501,8 +609,16 @@ WF_API wf_status wf_set_mesh(wf_domain *d, int64_t nn, int64_t ne, int32_t npe, 
   d->npe = npe;
   d->nn = nn;
   d->ne = ne;
-  d->x.assign(xyz, xyz + 3 * nn);
-  d->elnod.assign(elnod, elnod + ne * npe);
+  d->x.resize(3 * nn);
+  d->elnod.resize(ne * npe);
+  double *xd = d->x.data();
+  int32_t *ed = d->elnod.data();
+  host_parallel(3 * nn, [&](int64_t i0, int64_t i1) {
+    std::memcpy(xd + i0, xyz + i0, sizeof(double) * (i1 - i0));
+  });
+  host_parallel(ne * npe, [&](int64_t i0, int64_t i1) {
+    std::memcpy(ed + i0, elnod + i0, sizeof(int32_t) * (i1 - i0));
+  });
   if (!build_nodel(d)) {
     d->nn = d->ne = 0;
     return fail(d, WF_ERR_ARG, "connectivity references a node outside [0, nn)");
@@ -926,41 +1042,56 @@ cudaError_t upload(wf_domain *d, T **dst, const std::vector<T> &src) {
 // node's value triple; for repeated entries the later one wins, as the serial
 // BC loops of the reference (Domain_d.C:1109-1134) leave it.
 void bc_tables(wf_domain *d, std::vector<uint32_t> &code, std::vector<double> &vals) {
-  std::vector<uint8_t> mask(d->nn, 0);
-  std::vector<double> v3(3 * d->nn, 0.0);
+  // compact per-BC-node records (mask, value triple), later entries winning
+  std::vector<int32_t> slot(d->nn, -1);
+  std::vector<int64_t> nodes;
+  std::vector<std::array<double, 3>> v3;
+  std::vector<uint8_t> mask;
   for (int k = 0; k < 3; k++)
     for (size_t i = 0; i < d->bc_nod[k].size(); i++) {
       const int64_t n = d->bc_nod[k][i];
-      mask[n] |= (uint8_t)(1u << k);
-      v3[3 * n + k] = d->bc_val[k][i];
+      int32_t &sl = slot[n];
+      if (sl < 0) {
+        sl = (int32_t)nodes.size();
+        nodes.push_back(n);
+        v3.push_back({0.0, 0.0, 0.0});
+        mask.push_back(0);
+      }
+      mask[sl] |= (uint8_t)(1u << k);
+      v3[sl][k] = d->bc_val[k][i];
     }
+  // value sets numbered in ascending node order
+  std::vector<int32_t> order(nodes.size());
+  for (size_t i = 0; i < order.size(); i++) order[i] = (int32_t)i;
+  std::sort(order.begin(), order.end(), [&](int32_t a, int32_t b) { return nodes[a] < nodes[b]; });
   std::map<std::tuple<double, double, double>, uint32_t> sets;
   vals.assign(3, 0.0);
   sets[std::make_tuple(0.0, 0.0, 0.0)] = 0;
   code.assign(d->nn, 0u);
-  for (int64_t n = 0; n < d->nn; n++) {
-    if (!mask[n]) continue;
-    auto key = std::make_tuple(v3[3 * n], v3[3 * n + 1], v3[3 * n + 2]);
+  for (int32_t i : order) {
+    auto key = std::make_tuple(v3[i][0], v3[i][1], v3[i][2]);
     uint32_t id;
     auto it = sets.find(key);
     if (it == sets.end()) {
       id = (uint32_t)(vals.size() / 3);
       sets[key] = id;
-      vals.push_back(v3[3 * n]);
-      vals.push_back(v3[3 * n + 1]);
-      vals.push_back(v3[3 * n + 2]);
+      vals.push_back(v3[i][0]);
+      vals.push_back(v3[i][1]);
+      vals.push_back(v3[i][2]);
     } else {
       id = it->second;
     }
-    code[n] = (id << 3) | mask[n];
+    code[nodes[i]] = (id << 3) | mask[i];
   }
 }
 
 template <typename T>
 std::vector<T> soa3(const std::vector<double> &aos, int64_t nn, int64_t np) {
   std::vector<T> out(3 * np, T(0));
-  for (int64_t n = 0; n < nn; n++)
-    for (int k = 0; k < 3; k++) out[k * np + n] = (T)aos[3 * n + k];
+  host_parallel(nn, [&](int64_t n0, int64_t n1) {
+    for (int64_t n = n0; n < n1; n++)
+      for (int k = 0; k < 3; k++) out[k * np + n] = (T)aos[3 * n + k];
+  });
   return out;
 }
 
@@ -984,11 +1115,11 @@ wf_status autotune_launches(wf_domain *d) {
   cudaEvent_t a, b;
   CUDA_TRY(cudaEventCreate(&a));
   CUDA_TRY(cudaEventCreate(&b));
-  // items per thread 1, 2, 4, or 0: a persistent grid (SMs x resident blocks).
+  // items per thread 1, 2, or 0: a persistent grid (SMs x resident blocks).
   // The candidates are timed in interleaved rounds so that a drift of the
   // clocks while the GPU warms up does not favour the ones timed last.
-  const int sizes[3] = {64, 128, 256}, epts[4] = {1, 2, 4, 0};
-  constexpr int kRounds = 4, kReps = 3;
+  const int sizes[3] = {64, 128, 256}, epts[3] = {1, 2, 0};
+  constexpr int kRounds = 2, kReps = 2;
   for (int phase = 0; phase < 3; phase++) {
     std::vector<LaunchCfg> cands;
     for (int bs : sizes)
@@ -1159,10 +1290,14 @@ WF_API wf_status wf_init(wf_domain *d) {
 
   // connectivity (SoA elnod), node lists as slots e*npe + local
   std::vector<int32_t> elsoa(ne * d->npe);
-  for (int64_t e = 0; e < ne; e++)
-    for (int a = 0; a < d->npe; a++) elsoa[a * ne + e] = d->elnod[e * d->npe + a];
+  host_parallel(ne, [&](int64_t e0, int64_t e1) {
+    for (int64_t e = e0; e < e1; e++)
+      for (int a = 0; a < d->npe; a++) elsoa[a * ne + e] = d->elnod[e * d->npe + a];
+  });
   std::vector<int32_t> slots(d->nodel.size());
-  for (size_t k = 0; k < slots.size(); k++) slots[k] = d->nodel[k] * d->npe + d->nodel_loc[k];
+  host_parallel((int64_t)slots.size(), [&](int64_t k0, int64_t k1) {
+    for (int64_t k = k0; k < k1; k++) slots[k] = d->nodel[k] * d->npe + d->nodel_loc[k];
+  });
   int32_t *el = nullptr, *off = nullptr, *sl = nullptr;
   CUDA_TRY(upload(d, &el, elsoa));
   CUDA_TRY(upload(d, &off, d->nodel_off));
