@@ -1107,11 +1107,15 @@ wf_status autotune_launches(wf_domain *d) {
   const StepParams &P = d->P;
   MixState &M = d->M;
   const int64_t ne = d->ne, np = d->np;
-  std::vector<float> tau(6 * ne), pls(ne), ut(3 * np), cf(3 * np);
-  CUDA_TRY(cudaMemcpyAsync(tau.data(), M.tau, 4 * tau.size(), cudaMemcpyDeviceToHost, d->stream));
-  CUDA_TRY(cudaMemcpyAsync(pls.data(), M.pls, 4 * pls.size(), cudaMemcpyDeviceToHost, d->stream));
-  CUDA_TRY(cudaMemcpyAsync(ut.data(), M.ut, 4 * ut.size(), cudaMemcpyDeviceToHost, d->stream));
-  CUDA_TRY(cudaMemcpyAsync(cf.data(), M.cf, 4 * cf.size(), cudaMemcpyDeviceToHost, d->stream));
+  // the state the trials advance, saved in a device scratch buffer
+  const size_t n_tau = 6 * ne, n_pls = ne, n_ut = 3 * np, n_cf = 3 * np;
+  float *save = nullptr;
+  CUDA_TRY(cudaMalloc(&save, 4 * (n_tau + n_pls + n_ut + n_cf)));
+  float *s_tau = save, *s_pls = s_tau + n_tau, *s_ut = s_pls + n_pls, *s_cf = s_ut + n_ut;
+  CUDA_TRY(cudaMemcpyAsync(s_tau, M.tau, 4 * n_tau, cudaMemcpyDeviceToDevice, d->stream));
+  CUDA_TRY(cudaMemcpyAsync(s_pls, M.pls, 4 * n_pls, cudaMemcpyDeviceToDevice, d->stream));
+  CUDA_TRY(cudaMemcpyAsync(s_ut, M.ut, 4 * n_ut, cudaMemcpyDeviceToDevice, d->stream));
+  CUDA_TRY(cudaMemcpyAsync(s_cf, M.cf, 4 * n_cf, cudaMemcpyDeviceToDevice, d->stream));
   cudaEvent_t a, b;
   CUDA_TRY(cudaEventCreate(&a));
   CUDA_TRY(cudaEventCreate(&b));
@@ -1151,11 +1155,12 @@ wf_status autotune_launches(wf_domain *d) {
   }
   cudaEventDestroy(a);
   cudaEventDestroy(b);
-  CUDA_TRY(cudaMemcpyAsync(M.tau, tau.data(), 4 * tau.size(), cudaMemcpyHostToDevice, d->stream));
-  CUDA_TRY(cudaMemcpyAsync(M.pls, pls.data(), 4 * pls.size(), cudaMemcpyHostToDevice, d->stream));
-  CUDA_TRY(cudaMemcpyAsync(M.ut, ut.data(), 4 * ut.size(), cudaMemcpyHostToDevice, d->stream));
-  CUDA_TRY(cudaMemcpyAsync(M.cf, cf.data(), 4 * cf.size(), cudaMemcpyHostToDevice, d->stream));
+  CUDA_TRY(cudaMemcpyAsync(M.tau, s_tau, 4 * n_tau, cudaMemcpyDeviceToDevice, d->stream));
+  CUDA_TRY(cudaMemcpyAsync(M.pls, s_pls, 4 * n_pls, cudaMemcpyDeviceToDevice, d->stream));
+  CUDA_TRY(cudaMemcpyAsync(M.ut, s_ut, 4 * n_ut, cudaMemcpyDeviceToDevice, d->stream));
+  CUDA_TRY(cudaMemcpyAsync(M.cf, s_cf, 4 * n_cf, cudaMemcpyDeviceToDevice, d->stream));
   CUDA_TRY(cudaStreamSynchronize(d->stream));
+  CUDA_TRY(cudaFree(save));
   return WF_OK;
 }
 
