@@ -27,6 +27,11 @@ namespace {
 
 constexpr int kElemThreads = 128;
 constexpr int kNodeThreads = 256;
+// Resident blocks per SM the node kernel is compiled for (registers per
+// thread = 65536 / (256 * this)); a build-time tunable.
+#ifndef WF_NODE_MIN_BLOCKS
+#define WF_NODE_MIN_BLOCKS 6
+#endif
 
 // (hi, lo) pair helpers ------------------------------------------------------
 __device__ __forceinline__ float2 split_d(double v) {
@@ -856,7 +861,8 @@ __device__ __forceinline__ float node_one(const StepParams &P, const MixState &M
 }
 
 template <int NPE>
-__global__ void __launch_bounds__(kNodeThreads, 6) k_mix_nodes(StepParams P, MixState M) {
+__global__ void __launch_bounds__(kNodeThreads, WF_NODE_MIN_BLOCKS) k_mix_nodes(StepParams P,
+                                                                             MixState M) {
   __shared__ double sh[kNodeThreads / 32];
   __shared__ bool am_last;
   const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
