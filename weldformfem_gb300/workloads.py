@@ -282,6 +282,7 @@ def config(cid: int, steps: Optional[int] = None, scale: Optional[tuple] = None)
     if scale is not None:
         h = c.h
         c.L = tuple(float(n) * h for n in scale)
+        c.name = f"{c.name.split()[0]} scaled to {scale[0]}x{scale[1]}x{scale[2]} cells"
         if c.elem_mat is not None:
             c.elem_mat = octant_ids(c)
     if steps is not None:
