@@ -28,6 +28,7 @@ UNITS = {
     "wf_fp64.cu": ["--fmad=false"],
     "wf_mixed.cu": [],
     "wf_reduce.cu": [],
+    "wf_setup.cu": [],
     "wf_noalloc.cu": ["--fmad=false"],
     "wf_adjoint.cu": [],
     "wf_deck.cpp": ["-Xcompiler", "-ffp-contract=off"],

@@ -11,11 +11,13 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <memory>
 #include <new>
 #include <string>
 #include <thread>
 #include <atomic>
 #include <tuple>
+#include <utility>
 #include <vector>
 
 #include "wf_adjoint.cuh"
@@ -87,6 +89,29 @@ bool box_mesh(const double V[3], const double L[3], double r, bool tritetra,
   return true;
 }
 
+// Allocator whose resize() leaves trivial elements uninitialised: the large
+// host copies of the mesh are overwritten right after they are sized.
+template <typename T>
+struct NoInitAlloc : std::allocator<T> {
+  template <typename U>
+  struct rebind {
+    using other = NoInitAlloc<U>;
+  };
+  NoInitAlloc() = default;
+  template <typename U>
+  NoInitAlloc(const NoInitAlloc<U> &) {}
+  template <typename U>
+  void construct(U *p) noexcept {
+    ::new (static_cast<void *>(p)) U;
+  }
+  template <typename U, typename... Args>
+  void construct(U *p, Args &&...args) {
+    ::new (static_cast<void *>(p)) U(std::forward<Args>(args)...);
+  }
+};
+template <typename T>
+using hvec = std::vector<T, NoInitAlloc<T>>;
+
 }  // namespace wf
 
 using namespace wf;
@@ -98,8 +123,11 @@ struct wf_domain {
   // host mesh
   int32_t npe = 0;
   int64_t nn = 0, ne = 0, np = 0;
-  std::vector<double> x;          // interleaved [3 nn]
-  std::vector<int32_t> elnod;     // [ne npe]
+  hvec<double> x;                 // interleaved [3 nn]
+  hvec<int32_t> elnod;            // [ne npe]
+  // node -> element lists on the host, built when a host caller needs them
+  // (wf_get_connectivity, the part's surface search); wf_init builds the
+  // device copy itself
   std::vector<int32_t> nodel, nodel_loc, nodel_off, nodel_cnt;
   // materials
   std::vector<wf_material> mats;
@@ -139,6 +167,8 @@ struct wf_domain {
   // device
   bool initialized = false;
   std::vector<void *> allocs;
+  void *init_stage = nullptr;     // AoS uploads and scratch of wf_init, freed at its end
+  double *readback = nullptr;     // [3 nn] AoS staging of node-field readbacks
   StepParams P{};
   Fp64State S{};
   MixState M{};
@@ -208,6 +238,18 @@ wf_status fail(wf_domain *d, wf_status s, const char *fmt, ...) {
                   "%s: %s", #call, cudaGetErrorString(e_));                              \
   } while (0)
 
+// Device allocation freed with the domain, left uninitialised (the caller
+// writes every element).
+template <typename T>
+cudaError_t dalloc_raw(wf_domain *d, T **p, size_t count) {
+  void *q = nullptr;
+  cudaError_t e = cudaMalloc(&q, std::max<size_t>(count, 1) * sizeof(T));
+  if (e != cudaSuccess) return e;
+  d->allocs.push_back(q);
+  *p = static_cast<T *>(q);
+  return cudaSuccess;
+}
+
 template <typename T>
 cudaError_t dalloc(wf_domain *d, T **p, size_t count) {
   void *q = nullptr;
@@ -238,11 +280,14 @@ void free_device(wf_domain *d) {
   }
   for (void *p : d->allocs) cudaFree(p);
   d->allocs.clear();
+  if (d->init_stage) cudaFree(d->init_stage);
+  d->init_stage = nullptr;
   for (cudaEvent_t ev : d->ev_pool) cudaEventDestroy(ev);
   d->ev_pool.clear();
   d->ev_used = 0;
   d->S = Fp64State{};
   d->M = MixState{};
+  d->readback = nullptr;
   d->mvol = nullptr;
   d->initialized = false;
 }
@@ -272,7 +317,7 @@ void host_parallel(int64_t n, F f) {
 // from those ranks. Every list comes out element-ascending, exactly as one
 // thread would build it; a node with 255 or more entries in one chunk falls
 // back to the single-threaded build.
-bool build_nodel_serial(wf_domain *d) {
+void build_nodel_serial(wf_domain *d) {
   const int64_t nn = d->nn, ent = d->ne * d->npe;
   const int32_t *el = d->elnod.data();
   d->nodel_cnt.assign(nn, 0);
@@ -293,14 +338,12 @@ bool build_nodel_serial(wf_domain *d) {
     d->nodel[k] = (int32_t)(i / d->npe);
     d->nodel_loc[k] = (int32_t)(i % d->npe);
   }
-  return true;
 }
 
-bool build_nodel(wf_domain *d) {
-  const int64_t nn = d->nn, ne = d->ne, ent = ne * d->npe;
-  const int npe = d->npe;
+// Every connectivity entry names a node in [0, nn) (checked by host threads).
+bool valid_connectivity(const wf_domain *d) {
+  const int64_t nn = d->nn, ent = d->ne * d->npe;
   const int32_t *el = d->elnod.data();
-  // validation, in parallel
   std::atomic<bool> bad{false};
   host_parallel(ent, [&](int64_t i0, int64_t i1) {
     for (int64_t i = i0; i < i1; i++)
@@ -309,11 +352,20 @@ bool build_nodel(wf_domain *d) {
         return;
       }
   });
-  if (bad) return false;
+  return !bad;
+}
+
+void build_nodel(wf_domain *d) {
+  const int64_t nn = d->nn, ne = d->ne, ent = ne * d->npe;
+  const int npe = d->npe;
+  const int32_t *el = d->elnod.data();
   const int64_t T = std::min<int64_t>(
       std::min(32u, std::max(1u, std::thread::hardware_concurrency())),
       std::max<int64_t>(1, ent / (int64_t(1) << 20)));
-  if (T <= 1) return build_nodel_serial(d);
+  if (T <= 1) {
+    build_nodel_serial(d);
+    return;
+  }
   std::vector<std::vector<uint8_t>> rank(T);
   std::atomic<bool> overflow{false};
   auto chunk = [&](int64_t t, int64_t &e0, int64_t &e1) {
@@ -333,7 +385,10 @@ bool build_nodel(wf_domain *d) {
       });
     for (std::thread &x : th) x.join();
   }
-  if (overflow) return build_nodel_serial(d);
+  if (overflow) {
+    build_nodel_serial(d);
+    return;
+  }
   // (2) per node: totals, and each chunk's starting rank within the node's list
   d->nodel_cnt.assign(nn, 0);
   int32_t *cnt = d->nodel_cnt.data();
@@ -350,7 +405,10 @@ bool build_nodel(wf_domain *d) {
   });
   bool big = false;
   for (int64_t n = 0; n < nn && !big; n++) big = cnt[n] > 255;
-  if (big) return build_nodel_serial(d);
+  if (big) {
+    build_nodel_serial(d);
+    return;
+  }
   d->nodel_off.assign(nn + 1, 0);
   int64_t tot = 0;
   for (int64_t n = 0; n < nn; n++) {
@@ -378,7 +436,40 @@ bool build_nodel(wf_domain *d) {
       });
     for (std::thread &x : th) x.join();
   }
+}
+
+// The device tables of an initialised domain read back as host lists.
+bool download_lists(wf_domain *d) {
+  const int64_t nn = d->nn, ent = d->ne * d->npe;
+  std::vector<int32_t> off(nn + 1), slot(ent);
+  if (cudaSetDevice(d->device) != cudaSuccess ||
+      cudaMemcpyAsync(off.data(), d->P.off, sizeof(int32_t) * (nn + 1), cudaMemcpyDeviceToHost,
+                      d->stream) != cudaSuccess ||
+      cudaMemcpyAsync(slot.data(), d->P.slot, sizeof(int32_t) * ent, cudaMemcpyDeviceToHost,
+                      d->stream) != cudaSuccess ||
+      cudaStreamSynchronize(d->stream) != cudaSuccess)
+    return false;
+  d->nodel.resize(ent);
+  d->nodel_loc.resize(ent);
+  d->nodel_cnt.resize(nn);
+  host_parallel(ent, [&](int64_t k0, int64_t k1) {
+    for (int64_t k = k0; k < k1; k++) {
+      d->nodel[k] = slot[k] / d->npe;
+      d->nodel_loc[k] = slot[k] % d->npe;
+    }
+  });
+  for (int64_t n = 0; n < nn; n++) d->nodel_cnt[n] = off[n + 1] - off[n];
+  d->nodel_off = std::move(off);
   return true;
+}
+
+// The host lists, built on first use after the mesh was set: from the
+// device tables once wf_init has built them, else by host threads.
+void ensure_host_lists(const wf_domain *cd) {
+  wf_domain *d = const_cast<wf_domain *>(cd);
+  if (d->nodel_off.size() == (size_t)d->nn + 1) return;
+  if (d->initialized && d->P.slot && download_lists(d)) return;
+  build_nodel(d);
 }
 
 // Triangle normals and plane coefficients (TriMesh_d::CalcNormals,
@@ -513,6 +604,10 @@ void reset_mesh(wf_domain *d) {
   d->spec_eoff.clear();
   d->spec_noff.clear();
   d->spec_dt.clear();
+  d->nodel.clear();
+  d->nodel_loc.clear();
+  d->nodel_off.clear();
+  d->nodel_cnt.clear();
 }
 
 wf_status need_mesh(wf_domain *d) {
@@ -587,14 +682,17 @@ WF_API wf_status wf_add_box_length(wf_domain *d, const double V[3], const double
   if (!(r > 0.0)) return fail(d, WF_ERR_ARG, "r must be positive");
   reset_mesh(d);
   std::string err;
-  if (!wf::box_mesh(V, L, r, tritetra != 0, d->x, d->elnod, err)) {
+  std::vector<double> bx;
+  std::vector<int32_t> be;
+  if (!wf::box_mesh(V, L, r, tritetra != 0, bx, be, err)) {
     d->nn = d->ne = 0;
     return fail(d, WF_ERR_ARG, "%s", err.c_str());
   }
+  d->x.assign(bx.begin(), bx.end());
+  d->elnod.assign(be.begin(), be.end());
   d->npe = tritetra ? 4 : 8;
   d->nn = (int64_t)(d->x.size() / 3);
   d->ne = (int64_t)(d->elnod.size() / d->npe);
-  build_nodel(d);
   return WF_OK;
 }
 
@@ -619,7 +717,7 @@ WF_API wf_status wf_set_mesh(wf_domain *d, int64_t nn, int64_t ne, int32_t npe, 
   host_parallel(ne * npe, [&](int64_t i0, int64_t i1) {
     std::memcpy(ed + i0, elnod + i0, sizeof(int32_t) * (i1 - i0));
   });
-  if (!build_nodel(d)) {
+  if (!valid_connectivity(d)) {
     d->nn = d->ne = 0;
     return fail(d, WF_ERR_ARG, "connectivity references a node outside [0, nn)");
   }
@@ -652,13 +750,14 @@ WF_API wf_status wf_get_sizes(const wf_domain *d, int64_t *nn, int64_t *ne, int3
   if (nn) *nn = d->nn;
   if (ne) *ne = d->ne;
   if (npe) *npe = d->npe;
-  if (tot) *tot = (int64_t)d->nodel.size();
+  if (tot) *tot = d->ne * d->npe;   // every entry is on one node's list
   return WF_OK;
 }
 
 WF_API wf_status wf_get_connectivity(const wf_domain *d, int32_t *elnod, int32_t *nodel,
                                      int32_t *nodel_loc, int32_t *offset, int32_t *count) {
   if (!d) return WF_ERR_ARG;
+  if (nodel || nodel_loc || offset || count) ensure_host_lists(d);
   if (elnod) std::copy(d->elnod.begin(), d->elnod.end(), elnod);
   if (nodel) std::copy(d->nodel.begin(), d->nodel.end(), nodel);
   if (nodel_loc) std::copy(d->nodel_loc.begin(), d->nodel_loc.end(), nodel_loc);
@@ -1028,8 +1127,8 @@ WF_API wf_status wf_get_specimen_reaction(wf_domain *d, int32_t spec, double *ou
 // ---- init -------------------------------------------------------------------------
 namespace {
 
-template <typename T>
-cudaError_t upload(wf_domain *d, T **dst, const std::vector<T> &src) {
+template <typename T, typename A>
+cudaError_t upload(wf_domain *d, T **dst, const std::vector<T, A> &src) {
   cudaError_t e = dalloc(d, dst, src.size());
   if (e != cudaSuccess) return e;
   if (src.empty()) return cudaSuccess;
@@ -1083,16 +1182,6 @@ void bc_tables(wf_domain *d, std::vector<uint32_t> &code, std::vector<double> &v
     }
     code[nodes[i]] = (id << 3) | mask[i];
   }
-}
-
-template <typename T>
-std::vector<T> soa3(const std::vector<double> &aos, int64_t nn, int64_t np) {
-  std::vector<T> out(3 * np, T(0));
-  host_parallel(nn, [&](int64_t n0, int64_t n1) {
-    for (int64_t n = n0; n < n1; n++)
-      for (int k = 0; k < 3; k++) out[k * np + n] = (T)aos[3 * n + k];
-  });
-  return out;
 }
 
 }  // namespace
@@ -1293,23 +1382,36 @@ WF_API wf_status wf_init(wf_domain *d) {
   P.c_k = d->c_k;
   P.c_mu = d->c_mu;
 
-  // connectivity (SoA elnod), node lists as slots e*npe + local
-  std::vector<int32_t> elsoa(ne * d->npe);
-  host_parallel(ne, [&](int64_t e0, int64_t e1) {
-    for (int64_t e = e0; e < e1; e++)
-      for (int a = 0; a < d->npe; a++) elsoa[a * ne + e] = d->elnod[e * d->npe + a];
-  });
-  std::vector<int32_t> slots(d->nodel.size());
-  host_parallel((int64_t)slots.size(), [&](int64_t k0, int64_t k1) {
-    for (int64_t k = k0; k < k1; k++) slots[k] = d->nodel[k] * d->npe + d->nodel_loc[k];
-  });
+  // connectivity (SoA elnod), node lists as slots e*npe + local, built on
+  // the device from one upload of the AoS connectivity and the AoS
+  // coordinates (transposed into S.x below); the staging buffer is freed at
+  // the end of init
+  const int64_t ent = ne * d->npe;
   int32_t *el = nullptr, *off = nullptr, *sl = nullptr;
-  CUDA_TRY(upload(d, &el, elsoa));
-  CUDA_TRY(upload(d, &off, d->nodel_off));
-  CUDA_TRY(upload(d, &sl, slots));
+  CUDA_TRY(dalloc_raw(d, &el, ent));
+  CUDA_TRY(dalloc_raw(d, &off, nn + 1));
+  CUDA_TRY(dalloc_raw(d, &sl, ent));
   P.elnod = el;
   P.off = off;
   P.slot = sl;
+  double *x_aos = nullptr;
+  {
+    const size_t el_bytes = sizeof(int32_t) * ent, x_bytes = sizeof(double) * 3 * nn;
+    const size_t scratch_bytes = sizeof(int32_t) * connectivity_scratch_ints(nn);
+    const size_t x_at = (el_bytes + 255) / 256 * 256, sc_at = x_at + (x_bytes + 255) / 256 * 256;
+    void *stage = nullptr;
+    CUDA_TRY(cudaMalloc(&stage, sc_at + scratch_bytes));
+    d->init_stage = stage;
+    char *base = static_cast<char *>(stage);
+    int32_t *el_aos = reinterpret_cast<int32_t *>(base);
+    x_aos = reinterpret_cast<double *>(base + x_at);
+    CUDA_TRY(cudaMemcpyAsync(el_aos, d->elnod.data(), el_bytes, cudaMemcpyHostToDevice,
+                             d->stream));
+    CUDA_TRY(cudaMemcpyAsync(x_aos, d->x.data(), x_bytes, cudaMemcpyHostToDevice, d->stream));
+    d->h2d_bytes += (int64_t)(el_bytes + x_bytes);
+    CUDA_TRY(build_connectivity(el_aos, ne, d->npe, nn, el, off, sl,
+                                reinterpret_cast<int32_t *>(base + sc_at), d->stream));
+  }
   std::vector<uint32_t> code;
   std::vector<double> vals;
   bc_tables(d, code, vals);
@@ -1326,6 +1428,7 @@ WF_API wf_status wf_init(wf_domain *d) {
   if (d->tri) {
     std::vector<uint8_t> ext;
     std::vector<double> area, nodlen, nrm, pp;
+    ensure_host_lists(d);
     part_surface(d, ext, area, nodlen);
     for (int64_t n = 0; n < nn; n++)
       if (ext[n]) flags[n] |= NF_CONTACT;
@@ -1462,8 +1565,8 @@ WF_API wf_status wf_init(wf_domain *d) {
 
   // FP64 state (also the export target of the mixed state)
   Fp64State &S = d->S;
-  std::vector<double> xs = soa3<double>(d->x, nn, np);
-  CUDA_TRY(upload(d, &S.x, xs));
+  CUDA_TRY(dalloc_raw(d, &S.x, 3 * np));
+  coords_soa(x_aos, nn, np, S.x, d->stream);
   const bool fp64 = d->precision == WF_FP64;
   CUDA_TRY(dalloc(d, &S.v, 3 * np));
   CUDA_TRY(dalloc(d, &S.pa, 3 * np));
@@ -1504,24 +1607,14 @@ WF_API wf_status wf_init(wf_domain *d) {
     CUDA_TRY(dalloc(d, &S.fe, (size_t)ne * d->npe * 3));
     if (P.hg_on) CUDA_TRY(dalloc(d, &S.fhg, (size_t)ne * d->npe * 3));
   }
-  std::vector<double> rho0(ne, d->rho_all);
-  CUDA_TRY(upload(d, &d->rho0_dev, rho0));
+  CUDA_TRY(dalloc_raw(d, &d->rho0_dev, ne));
+  fill_values(d->rho0_dev, d->rho_all, ne, d->stream);
 
   // preamble (Solver_explicit.C:120-268): sigma_y = sy0, eps_p = 0; v = a = u
   // = 0 then ImposeBCV per dimension -- the zeroing sits inside the dimension
   // loop, so only the last dimension's BC values survive into step 1.
-  {
-    std::vector<double> sy(ne);
-    for (int64_t e = 0; e < ne; e++) sy[e] = d->mats[d->emat.empty() ? 0 : d->emat[e]].sy0;
-    CUDA_TRY(cudaMemcpyAsync(S.sy, sy.data(), sizeof(double) * ne, cudaMemcpyHostToDevice,
-                             d->stream));
-    d->h2d_bytes += (int64_t)(sizeof(double) * (ne + 3 * np));
-    std::vector<double> v0(3 * np, 0.0);
-    for (size_t i = 0; i < d->bc_nod[2].size(); i++)
-      v0[2 * np + d->bc_nod[2][i]] = d->bc_val[2][i];
-    CUDA_TRY(cudaMemcpyAsync(S.v, v0.data(), sizeof(double) * 3 * np, cudaMemcpyHostToDevice,
-                             d->stream));
-  }
+  initial_yield(P, S.sy, d->stream);
+  initial_velocity(P, S.v, d->stream);
   fp64_geometry(P, S, d->stream, true);
   CUDA_TRY(cudaMemcpyAsync(S.vol0, S.vol, sizeof(double) * ne, cudaMemcpyDeviceToDevice,
                            d->stream));
@@ -1641,6 +1734,8 @@ WF_API wf_status wf_init(wf_domain *d) {
     }
   }
   CUDA_TRY(cudaStreamSynchronize(d->stream));
+  CUDA_TRY(cudaFree(d->init_stage));
+  d->init_stage = nullptr;
   d->initialized = true;
   d->host_step = 0;
   d->host_time = 0.0;
@@ -1916,14 +2011,16 @@ wf_status ready_for_readback(wf_domain *d) {
   return WF_OK;
 }
 
+// SoA [3][np] field -> caller's AoS [nn][3]: transposed on the device into
+// a readback buffer kept with the domain, then one copy to the host.
 wf_status copy_node3(wf_domain *d, const double *src, double *out) {
-  std::vector<double> tmp(3 * d->np);
-  d->d2h_bytes += (int64_t)(sizeof(double) * 3 * d->np);
-  CUDA_TRY(cudaMemcpyAsync(tmp.data(), src, sizeof(double) * 3 * d->np, cudaMemcpyDeviceToHost,
-                           d->stream));
+  if (!d->readback) CUDA_TRY(dalloc_raw(d, &d->readback, 3 * d->np));
+  coords_aos(src, d->nn, d->np, d->readback, d->stream);
+  CUDA_TRY(cudaGetLastError());
+  const size_t bytes = sizeof(double) * 3 * d->nn;
+  d->d2h_bytes += (int64_t)bytes;
+  CUDA_TRY(cudaMemcpyAsync(out, d->readback, bytes, cudaMemcpyDeviceToHost, d->stream));
   CUDA_TRY(cudaStreamSynchronize(d->stream));
-  for (int64_t n = 0; n < d->nn; n++)
-    for (int k = 0; k < 3; k++) out[3 * n + k] = tmp[k * d->np + n];
   return WF_OK;
 }
 
@@ -1957,19 +2054,12 @@ WF_API wf_status wf_get_node_scalar(wf_domain *d, int32_t field, double *out) {
   wf_status s = ready_for_readback(d);
   if (s) return s;
   if (!out) return WF_ERR_ARG;
-  std::vector<double> tmp(d->np);
-  if (field == WF_NODE_MASS || field == WF_NODE_VOLN) {
-    s = copy_plain(d, field == WF_NODE_MASS ? d->S.mass : d->S.voln, tmp.data(), d->np);
-    if (s) return s;
-    std::copy(tmp.begin(), tmp.begin() + d->nn, out);
-    return WF_OK;
-  }
+  // per-node arrays are padded to np entries: the first nn are the nodes
+  if (field == WF_NODE_MASS || field == WF_NODE_VOLN)
+    return copy_plain(d, field == WF_NODE_MASS ? d->S.mass : d->S.voln, out, d->nn);
   if (field == WF_NODE_TEMP) {
     if (!d->thermal) return fail(d, WF_ERR_STATE, "thermal coupling is off");
-    s = copy_plain(d, d->S.T, tmp.data(), d->np);
-    if (s) return s;
-    std::copy(tmp.begin(), tmp.begin() + d->nn, out);
-    return WF_OK;
+    return copy_plain(d, d->S.T, out, d->nn);
   }
   if (field == WF_NODE_PRESSURE) {
     // calcNodalPressureFromElemental (Mechanical.C:1187-1213), serial order

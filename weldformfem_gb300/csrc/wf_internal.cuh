@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <string>
 #include <vector>
 
@@ -225,5 +226,24 @@ void energy_mixed(const StepParams &P, const MixState &M, cudaStream_t st);
 // Minimum element edge length over the mesh (exact: min is order-free).
 void min_edge_length(const int32_t *elnod, const double *x, int64_t np, int64_t ne, int npe,
                      double *out_dev, cudaStream_t st);
+
+// ---- device setup (wf_setup.cu) ------------------------------------------------
+// Node -> element lists from the AoS connectivity on the device: SoA element
+// nodes, CSR offsets [nn + 1] and slots e * npe + a, ascending within each
+// node's list (the host build's order). scratch holds
+// connectivity_scratch_ints(nn) ints.
+int64_t connectivity_scratch_ints(int64_t nn);
+cudaError_t build_connectivity(const int32_t *el_aos, int64_t ne, int npe, int64_t nn,
+                               int32_t *el_soa, int32_t *off, int32_t *slot, int32_t *scratch,
+                               cudaStream_t st);
+// AoS [nn][3] -> SoA [3][np], zero padded
+void coords_soa(const double *x_aos, int64_t nn, int64_t np, double *out, cudaStream_t st);
+// SoA [3][np] -> AoS [nn][3]
+void coords_aos(const double *soa, int64_t nn, int64_t np, double *out, cudaStream_t st);
+void fill_values(double *p, double v, int64_t n, cudaStream_t st);
+// sigma_y = sy0 of each element's material
+void initial_yield(const StepParams &P, double *sy, cudaStream_t st);
+// v after the preamble's BC loop: zero but the z velocity BCs
+void initial_velocity(const StepParams &P, double *v, cudaStream_t st);
 
 }  // namespace wf

@@ -211,13 +211,14 @@ class Case:
                     mu=float(c["mu"]))
 
 
-def apply_options(dom, case: Case, with_bcs=True, x=None, set_dt=True):
+def apply_options(dom, case: Case, with_bcs=True, x=None, set_dt=True, bcs=None):
     """Everything after the mesh: materials, BCs, options, dt. Returns dt
     (None when set_dt is False: the caller sets it, e.g. from the device
-    min-edge reduction after init)."""
+    min-edge reduction after init). `bcs` = case.bcs() when the caller has
+    built them already."""
     dom.set_materials(case.materials, case.elem_mat)
     if with_bcs:
-        dom.add_bcs(case.bcs())
+        dom.add_bcs(case.bcs() if bcs is None else bcs)
     if case.hg:
         dom.set_hourglass(case.hg)
     if case.press_alg:
