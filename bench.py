@@ -19,6 +19,7 @@ independent replica on its own GPU and the value is the total over ranks.
 from __future__ import annotations
 
 import argparse
+import datetime
 import json
 import os
 import subprocess
@@ -62,58 +63,87 @@ def dist_env():
 
 
 class ClockSampler:
-    """Samples nvidia-smi clocks and throttle reasons during the timed region."""
+    """Samples nvidia-smi clocks and throttle reasons during the timed region.
 
-    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+    nvidia-smi is started before the region (it takes a moment to print its
+    first line) and sampled every 50 ms; start() returns once it is live and
+    opens the window, stop() closes it and keeps the samples whose timestamps
+    fall inside (or the nearest one when the region is shorter than a
+    sampling period)."""
+
+    FIELDS = ("timestamp,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
               "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
               "clocks_event_reasons.sw_power_cap")
+    PERIOD_MS = 50
 
     def __init__(self, gpu: int):
         self.gpu = gpu
         self.proc = None
         self.lines = []
+        self.t0 = self.t1 = None
 
     def start(self):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", str(self.PERIOD_MS)],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
         except (OSError, FileNotFoundError):
             self.proc = None
+            return
+        deadline = time.time() + 5.0
+        while not self.lines and time.time() < deadline and self.proc.poll() is None:
+            time.sleep(0.01)
+        self.t0 = datetime.datetime.now()
+
+    def begin(self):
+        """Opens the window (when the sampler was started ahead of it)."""
+        self.t0 = datetime.datetime.now()
 
     def _read(self):
         for ln in self.proc.stdout:
-            self.lines.append(ln.strip())
+            self.lines.append((datetime.datetime.now(), ln.strip()))
 
     def stop(self):
         if not self.proc:
             return None
+        self.t1 = datetime.datetime.now()
+        time.sleep(self.PERIOD_MS * 1.5e-3)        # the sample that covers the region's end
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
         except subprocess.TimeoutExpired:
             self.proc.kill()
-        sm, mx, reasons = [], None, set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        rows = []
+        for seen, ln in self.lines:
             parts = [p.strip() for p in ln.split(",")]
-            if len(parts) < 7:
+            if len(parts) < 8:
                 continue
             try:
-                sm.append(float(parts[0]))
-                mx = float(parts[1])
+                ts = datetime.datetime.strptime(parts[0], "%Y/%m/%d %H:%M:%S.%f")
+            except ValueError:
+                ts = seen                           # arrival time of the line instead
+            try:
+                rows.append((ts, float(parts[1]), float(parts[2]), parts[4:8]))
             except ValueError:
                 continue
-            for nm, val in zip(names, parts[3:7]):
+        if not rows:
+            return None
+        inside = [r for r in rows if self.t0 <= r[0] <= self.t1]
+        if not inside:   # region shorter than a period: the sample nearest to its middle
+            mid = self.t0 + (self.t1 - self.t0) / 2
+            inside = [min(rows, key=lambda r: abs((r[0] - mid).total_seconds()))]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in inside:
+            for nm, val in zip(names, r[3]):
                 if val.lower() in ("active", "1"):
                     reasons.add(nm)
-        if not sm:
-            return None
-        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons),
-                "samples": len(sm)}
+        return {"sm_mhz": float(np.median([r[1] for r in inside])), "sm_max_mhz": inside[-1][2],
+                "reasons": sorted(reasons), "samples": len(inside),
+                "window_s": round((self.t1 - self.t0).total_seconds(), 3)}
 
 
 def measured_peak():
@@ -201,16 +231,17 @@ def run_ours(args):
 
     # ---- mixed precision, graph launches: the headline -------------------------
     dm = build_domain(wf, case, wf.WF_MIXED, x, device)
+    clocks = ClockSampler(device)
+    clocks.start()                   # live before the timed region
     dm.run(Wm)
     dm.sync()
     stream = torch.cuda.ExternalStream(dm.stream_handle(), device=device)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    clocks = ClockSampler(device)
     mode, cl_blocks, cl_bs = dm.step_mode()
     barrier()
     torch.cuda.synchronize(device)
     launches0 = dm.launch_count()
-    clocks.start()
+    clocks.begin()
     ev0.record(stream)
     dm.run(K)
     ev1.record(stream)
@@ -361,13 +392,14 @@ def run_ensemble(args):
     d = wf.Domain(wf.WF_MIXED, device=device)
     W.apply_batch(d, batch)
     d.init()
+    clocks = ClockSampler(device)
+    clocks.start()                   # live before the timed region
     d.run(Wm)
     d.sync()
     stream = torch.cuda.ExternalStream(d.stream_handle(), device=device)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    clocks = ClockSampler(device)
     launches0 = d.launch_count()
-    clocks.start()
+    clocks.begin()
     ev0.record(stream)
     d.run(K)
     ev1.record(stream)

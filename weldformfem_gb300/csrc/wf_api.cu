@@ -1210,16 +1210,30 @@ wf_status autotune_launches(wf_domain *d) {
   CUDA_TRY(cudaEventCreate(&b));
   // items per thread 1, 2, or 0: a persistent grid (SMs x resident blocks).
   // The candidates are timed in interleaved rounds so that a drift of the
-  // clocks while the GPU warms up does not favour the ones timed last.
+  // clocks while the GPU warms up does not favour the ones timed last; the
+  // second round times only those within kKeep of the first round's best.
+  // Each timing covers two launches, or one on meshes of a million elements
+  // and more (a launch there lasts tens of microseconds or more, well above
+  // the events' resolution).
   const int sizes[3] = {64, 128, 256}, epts[3] = {1, 2, 0};
-  constexpr int kRounds = 2, kReps = 2;
+  constexpr int kRounds = 2;
+  const int reps = ne >= (int64_t(1) << 20) ? 1 : 2;
+  constexpr double kKeep = 1.25;
   for (int phase = 0; phase < 3; phase++) {
     std::vector<LaunchCfg> cands;
     for (int bs : sizes)
       for (int ept : epts) cands.push_back(LaunchCfg{bs, ept});
     std::vector<double> total(cands.size(), 0.0);
-    for (int round = 0; round < kRounds; round++)
+    std::vector<int> timed(cands.size(), 0);
+    std::vector<bool> alive(cands.size(), true);
+    for (int round = 0; round < kRounds; round++) {
+      if (round == 1) {
+        // all candidates have one timing after the first round
+        const double best0 = *std::min_element(total.begin(), total.end());
+        for (size_t i = 0; i < cands.size(); i++) alive[i] = total[i] <= kKeep * best0;
+      }
       for (size_t i = 0; i < cands.size(); i++) {
+        if (!alive[i]) continue;
         const LaunchCfg c = cands[i];
         auto launch = [&]() {
           if (phase == 0) mix_geometry(P, M, d->mvol, d->stream, c);
@@ -1228,19 +1242,22 @@ wf_status autotune_launches(wf_domain *d) {
         };
         if (round == 0) launch();  // warm-up
         cudaEventRecord(a, d->stream);
-        for (int r = 0; r < kReps; r++) launch();
+        for (int r = 0; r < reps; r++) launch();
         cudaEventRecord(b, d->stream);
         CUDA_TRY(cudaEventSynchronize(b));
         CUDA_TRY(cudaGetLastError());
         float ms = 0.f;
         CUDA_TRY(cudaEventElapsedTime(&ms, a, b));
         total[i] += ms;
+        timed[i] += reps;
       }
+    }
     size_t best = 0;
-    for (size_t i = 1; i < cands.size(); i++)
-      if (total[i] < total[best]) best = i;
+    while (!alive[best]) best++;
+    for (size_t i = best + 1; i < cands.size(); i++)
+      if (alive[i] && total[i] < total[best]) best = i;
     d->cfg[phase] = cands[best];
-    d->cfg_ms[phase] = total[best] / (kRounds * kReps);
+    d->cfg_ms[phase] = total[best] / timed[best];
   }
   cudaEventDestroy(a);
   cudaEventDestroy(b);
