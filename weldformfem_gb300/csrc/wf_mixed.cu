@@ -712,8 +712,12 @@ __device__ __forceinline__ void element_one(const StepParams &P, const MixState 
     element_tet<LAW, CG, TH>(P, M, e, step);
 }
 
-// Registers per thread stay <= 64 at 1024 resident threads per SM.
-constexpr int elem_min_blocks(int bs) { return 1024 / bs; }
+// Resident threads per SM the element kernel is compiled for (1024: at most
+// 64 registers per thread), a build-time constant.
+#ifndef WF_ELEM_THREADS_PER_SM
+#define WF_ELEM_THREADS_PER_SM 1024
+#endif
+constexpr int elem_min_blocks(int bs) { return WF_ELEM_THREADS_PER_SM / bs; }
 
 template <int NPE, int BS, int LAW, bool TH>
 __global__ void __launch_bounds__(BS, elem_min_blocks(BS)) k_mix_elements(StepParams P,
