@@ -464,12 +464,14 @@ bool download_lists(wf_domain *d) {
 }
 
 // The host lists, built on first use after the mesh was set: from the
-// device tables once wf_init has built them, else by host threads.
-void ensure_host_lists(const wf_domain *cd) {
+// device tables once wf_init has built them, else by host threads. False
+// when the device tables could not be read back.
+bool ensure_host_lists(const wf_domain *cd) {
   wf_domain *d = const_cast<wf_domain *>(cd);
-  if (d->nodel_off.size() == (size_t)d->nn + 1) return;
-  if (d->initialized && d->P.slot && download_lists(d)) return;
+  if (d->nodel_off.size() == (size_t)d->nn + 1) return true;
+  if (d->initialized && d->P.slot) return download_lists(d);
   build_nodel(d);
+  return true;
 }
 
 // Triangle normals and plane coefficients (TriMesh_d::CalcNormals,
@@ -757,7 +759,8 @@ WF_API wf_status wf_get_sizes(const wf_domain *d, int64_t *nn, int64_t *ne, int3
 WF_API wf_status wf_get_connectivity(const wf_domain *d, int32_t *elnod, int32_t *nodel,
                                      int32_t *nodel_loc, int32_t *offset, int32_t *count) {
   if (!d) return WF_ERR_ARG;
-  if (nodel || nodel_loc || offset || count) ensure_host_lists(d);
+  if ((nodel || nodel_loc || offset || count) && !ensure_host_lists(d))
+    return fail(const_cast<wf_domain *>(d), WF_ERR_CUDA, "reading back the node lists failed");
   if (elnod) std::copy(d->elnod.begin(), d->elnod.end(), elnod);
   if (nodel) std::copy(d->nodel.begin(), d->nodel.end(), nodel);
   if (nodel_loc) std::copy(d->nodel_loc.begin(), d->nodel_loc.end(), nodel_loc);
@@ -1445,7 +1448,7 @@ WF_API wf_status wf_init(wf_domain *d) {
   if (d->tri) {
     std::vector<uint8_t> ext;
     std::vector<double> area, nodlen, nrm, pp;
-    ensure_host_lists(d);
+    if (!ensure_host_lists(d)) return fail(d, WF_ERR_CUDA, "reading back the node lists failed");
     part_surface(d, ext, area, nodlen);
     for (int64_t n = 0; n < nn; n++)
       if (ext[n]) flags[n] |= NF_CONTACT;
