@@ -109,7 +109,10 @@ WF_API wf_status wf_set_nodes(wf_domain *d, const double *xyz);
 /* getNodeCount / getElemCount (Domain_d.h:561-563). */
 WF_API wf_status wf_get_sizes(const wf_domain *d, int64_t *nn, int64_t *ne, int32_t *npe,
                               int64_t *nodel_total);
-/* m_elnod, m_nodel, m_nodel_loc, m_nodel_offset, m_nodel_count (Domain_d.h:961-965). */
+/* m_elnod, m_nodel, m_nodel_loc, m_nodel_offset, m_nodel_count (Domain_d.h:961-965).
+ * The lists are element-ascending per node; before wf_init they are built on
+ * the host on first request, after it read back from the device tables the
+ * step uses. Any output pointer may be NULL. */
 WF_API wf_status wf_get_connectivity(const wf_domain *d, int32_t *elnod, int32_t *nodel,
                                      int32_t *nodel_loc, int32_t *offset, int32_t *count);
 
