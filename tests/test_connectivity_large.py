@@ -80,3 +80,21 @@ def test_device_lists_of_a_renumbered_mesh():
     # the reaction is a reduction over the node set (the device adds block
     # partials, the oracle adds in list order): equal to rounding
     np.testing.assert_allclose(d.reaction(), o.reaction(), rtol=1e-13, atol=0)
+
+
+@pytest.mark.gpu
+def test_set_mesh_rejects_unknown_nodes_and_lists_follow_a_new_mesh():
+    c = W.config(0, scale=(3, 3, 3))
+    x, el = c.coords(), c.elnod()
+    d = wf.Domain(wf.WF_MIXED)
+    for v in (c.n_node, -1):
+        bad = el.copy()
+        bad[5, 2] = v
+        with pytest.raises(wf.WfError) as e:
+            d.set_mesh(x, bad)
+        assert e.value.status == wf.WF_ERR_ARG
+    d.set_mesh(x, el)
+    check(d, el.reshape(-1), 8, c.n_node)
+    el2 = np.ascontiguousarray(el[::-1])          # same node count, other lists
+    d.set_mesh(x, el2)
+    check(d, el2.reshape(-1), 8, c.n_node)

@@ -632,9 +632,19 @@ __device__ __forceinline__ void element_tet(const StepParams &P, const MixState 
   int32_t nid[4];
   float dH[3][4];
   float detJ;
+  float vpn[4][3], jrn[4];
   {
     float r[4][3];
     rel_coords<4, CG>(P, M, e, r, nid);
+    // the nodes' predicted velocities and volume ratios, gathered before the
+    // Jacobian arithmetic so that their loads are in flight during it
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+      vpn[a][0] = ldx<CG>(&M.vp[nid[a]]);
+      vpn[a][1] = ldx<CG>(&M.vp[P.np + nid[a]]);
+      vpn[a][2] = ldx<CG>(&M.vp[2 * P.np + nid[a]]);
+      jrn[a] = ldx<CG>(&M.jr[nid[a]]);
+    }
     float J[3][3];
     jacobian_f<4>(r, J);
     shape_derivs_f<4>(J, dH);
@@ -646,9 +656,7 @@ __device__ __forceinline__ void element_tet(const StepParams &P, const MixState 
   float J_avg = 0.f;
 #pragma unroll
   for (int a = 0; a < 4; a++) {
-    const float v0 = ldx<CG>(&M.vp[nid[a]]);
-    const float v1 = ldx<CG>(&M.vp[P.np + nid[a]]);
-    const float v2 = ldx<CG>(&M.vp[2 * P.np + nid[a]]);
+    const float v0 = vpn[a][0], v1 = vpn[a][1], v2 = vpn[a][2];
     const float d0 = dH[0][a], d1 = dH[1][a], d2 = dH[2][a];
     s00 += d0 * v0;
     s11 += d1 * v1;
@@ -659,7 +667,7 @@ __device__ __forceinline__ void element_tet(const StepParams &P, const MixState 
     s02 += d2 * v0 + d0 * v2;
     w12 += d2 * v1 - d1 * v2;
     w02 += d2 * v0 - d0 * v2;
-    J_avg += ldx<CG>(&M.jr[nid[a]]);
+    J_avg += jrn[a];
   }
   const float f = 1.0f / detJ;
   const float fh = 0.5f * f;
