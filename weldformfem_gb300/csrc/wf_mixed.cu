@@ -517,14 +517,18 @@ __device__ __forceinline__ void element_hex(const StepParams &P, const MixState 
   const int64_t ne = P.ne, np = P.np;
   int32_t nid[8];
   float A[3][3], detJ;
-  // mean volume ratio of the nodes, gathered with the positions so that its
-  // loads are in flight during the Jacobian arithmetic
+  // mean volume ratio of the nodes; the per-phase kernel gathers it with the
+  // positions so that its loads are in flight during the Jacobian arithmetic
+  // (the cluster run, one element per thread, gathers it later: early it
+  // spills there)
   float J_avg = 0.f;
   {
     float r[8][3];
     rel_coords<8, CG>(P, M, e, r, nid);
+    if constexpr (!CG) {
 #pragma unroll
-    for (int a = 0; a < 8; a++) J_avg += ldx<CG>(&M.jr[nid[a]]);
+      for (int a = 0; a < 8; a++) J_avg += ldx<CG>(&M.jr[nid[a]]);
+    }
     float J[3][3];
 #pragma unroll
     for (int k = 0; k < 3; k++) {
@@ -571,6 +575,10 @@ __device__ __forceinline__ void element_hex(const StepParams &P, const MixState 
     for (int k = 0; k < 3; k++)
 #pragma unroll
       for (int j = 0; j < 4; j++) stash[(k * 4 + j) * stride] = ch * hm[k][j];
+  }
+  if constexpr (CG) {
+#pragma unroll
+    for (int a = 0; a < 8; a++) J_avg += ldx<CG>(&M.jr[nid[a]]);
   }
   // velocity gradient L[i][k] = d v_k / d x_i
   const float fl = 0.125f / detJ;
