@@ -340,21 +340,6 @@ void build_nodel_serial(wf_domain *d) {
   }
 }
 
-// Every connectivity entry names a node in [0, nn) (checked by host threads).
-bool valid_connectivity(const wf_domain *d) {
-  const int64_t nn = d->nn, ent = d->ne * d->npe;
-  const int32_t *el = d->elnod.data();
-  std::atomic<bool> bad{false};
-  host_parallel(ent, [&](int64_t i0, int64_t i1) {
-    for (int64_t i = i0; i < i1; i++)
-      if (el[i] < 0 || el[i] >= nn) {
-        bad = true;
-        return;
-      }
-  });
-  return !bad;
-}
-
 void build_nodel(wf_domain *d) {
   const int64_t nn = d->nn, ne = d->ne, ent = ne * d->npe;
   const int npe = d->npe;
@@ -716,10 +701,18 @@ WF_API wf_status wf_set_mesh(wf_domain *d, int64_t nn, int64_t ne, int32_t npe, 
   host_parallel(3 * nn, [&](int64_t i0, int64_t i1) {
     std::memcpy(xd + i0, xyz + i0, sizeof(double) * (i1 - i0));
   });
+  // copied and checked in one pass: every entry names a node in [0, nn)
+  std::atomic<bool> bad{false};
   host_parallel(ne * npe, [&](int64_t i0, int64_t i1) {
-    std::memcpy(ed + i0, elnod + i0, sizeof(int32_t) * (i1 - i0));
+    bool b = false;
+    for (int64_t i = i0; i < i1; i++) {
+      const int32_t v = elnod[i];
+      ed[i] = v;
+      b |= (v < 0) | (v >= nn);
+    }
+    if (b) bad = true;
   });
-  if (!valid_connectivity(d)) {
+  if (bad) {
     d->nn = d->ne = 0;
     return fail(d, WF_ERR_ARG, "connectivity references a node outside [0, nn)");
   }
