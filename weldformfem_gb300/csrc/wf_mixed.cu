@@ -257,6 +257,7 @@ template <int NPE, bool CG>
 __device__ __forceinline__ void nodal_one(const StepParams &P, const MixState &M,
                                           const float *vol, int64_t n, double time) {
   const int32_t b = __ldg(&P.off[n]), c = __ldg(&P.off[n + 1]) - b;
+  const float2 nc = __ldg(&M.nc[n]);   // issued before the gather, used after it
   float s = 0.0f;
   for (int32_t k0 = 0; k0 < c; k0 += 8) {
     int32_t sl[8];
@@ -268,7 +269,6 @@ __device__ __forceinline__ void nodal_one(const StepParams &P, const MixState &M
 #pragma unroll
     for (int j = 0; j < 8; j++) s += g[j];
   }
-  const float2 nc = __ldg(&M.nc[n]);
   M.jr[n] = s * nc.x;
   float mass;
   if (P.mass_mode == 0) {
