@@ -52,7 +52,29 @@ ALG_BYTES_HEX_MIXED = {"geometry": (36, 24), "nodal": (36, 20), "elements": (184
 ALG_BYTES_TET_MIXED = {"geometry": (20, 24), "nodal": (20, 20), "elements": (120, 40),
                        "nodes": (64, 121)}
 KERNEL_NAMES = {"geometry": "k_mix_geometry", "nodal": "k_mix_nodal",
-                "elements": "k_mix_elements", "nodes": "k_mix_nodes"}
+                "elements": "k_mix_elements", "nodes": "k_mix_nodes",
+                "tile": "k_mix_tile", "shared": "k_mix_shared"}
+TILED_PHASES = ["geometry", "nodal", "tile", "shared"]
+
+
+def tiled_alg_bytes(E, N, stats):
+    """Algorithmic bytes per launch of the tiled kernels, from the tile counts
+    the library reports (tiles, shared nodes, sum of tile nodes, shared-node
+    list entries):
+      tile  : per tile node 4 (id) + 40 (positions 24, predicted velocity 12,
+              volume ratio 4, staged once); per element 4 (id) + 16 (local
+              corners) + 48 (deviatoric stress RW) + 8 (plastic strain RW);
+              per shared incidence 12 (corner force to HBM); per interior node
+              93 (velocity, acceleration, mass, BC code, flags read 33;
+              positions, velocity, acceleration, predicted velocity written 60)
+      shared: per shared node 4 (id) + 8 (list bounds) + 129 (node update 93,
+              positions 24, predicted velocity 12); per list entry 4 + 12
+              (slot, corner force)"""
+    ntiles, nshared, tile_nodes, shared_slots = stats[:4]
+    n_int = N - nshared
+    tile = 44 * tile_nodes + 76 * E + 12 * (tile_nodes - n_int) + 93 * n_int
+    shared = 141 * nshared + 16 * shared_slots
+    return tile, shared
 
 
 def dist_env():
@@ -232,25 +254,29 @@ def run_ours(args):
     # ---- mixed precision, graph launches: the headline -------------------------
     dm = build_domain(wf, case, wf.WF_MIXED, x, device)
     clocks = ClockSampler(device)
-    clocks.start()                   # live before the timed region
+    clocks.start()                   # live before the warm-up
+    clocks.begin()                   # window: warm-up, timed steps, phase steps, FP64 steps
     dm.run(Wm)
     dm.sync()
+    dm.prepare_run(K)                # the graphs the timed run replays, built untimed
     stream = torch.cuda.ExternalStream(dm.stream_handle(), device=device)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     mode, cl_blocks, cl_bs = dm.step_mode()
+    tile_stats = dm.tile_stats()
     barrier()
     torch.cuda.synchronize(device)
     launches0 = dm.launch_count()
-    clocks.begin()
+    graphs0 = dm.graph_launches()
     ev0.record(stream)
     dm.run(K)
     ev1.record(stream)
     ev1.synchronize()
     torch.cuda.synchronize(device)
-    clk = clocks.stop()
     barrier()
     ms_total = ev0.elapsed_time(ev1)
     launches = dm.launch_count() - launches0
+    graph_replays = dm.graph_launches() - graphs0
+    dm.sync()                        # raises if a non-finite force was cleared
     # per-phase breakdown (direct launches, CUDA events around each kernel)
     dm.set_phase_timing(True)
     kp = max(10, min(K, 100))
@@ -265,26 +291,26 @@ def run_ours(args):
     df = build_domain(wf, case, wf.WF_FP64, x, device)
     df.run(Wm)
     df.sync()
+    df.prepare_run(K)
     fstream = torch.cuda.ExternalStream(df.stream_handle(), device=device)
     f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     f0.record(fstream)
     df.run(K)
     f1.record(fstream)
     f1.synchronize()
+    clk = clocks.stop()
     ms_fp64 = f0.elapsed_time(f1)
+    df.sync()
 
-    # errors of mixed vs FP64 over the first W + K steps (same inputs)
-    nrun = Wm + K
-    rm, rf = dm.reaction()[:nrun], df.reaction()[:nrun]
-    um, uf = None, None
+    # errors of mixed vs FP64 over the configuration's whole run (outside any
+    # timed region): a fresh mixed domain and the FP64 one, same inputs
+    nrun = max(Wm + K, case.steps) if not args.short_error else Wm + K
+    df.run(nrun - (Wm + K))
     dm2 = build_domain(wf, case, wf.WF_MIXED, x, device)
     dm2.run(nrun)
-    um, uf = dm2.node_vec("u"), df.node_vec("u")
-    plm, plf = dm2.elem_scalar("pl_strain"), df.elem_scalar("pl_strain")
-    rel = lambda a, b: float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
-    err = {"reaction": rel(rm, rf), "displacement": rel(um, uf),
-           "pl_strain": rel(plm, plf) if np.max(np.abs(plf)) > 0 else 0.0,
-           "steps": nrun}
+    dm2.sync()
+    df.sync()
+    err = mixed_errors(dm2, df, nrun)
     del dm2, df
 
     # ---- end to end through the C ABI from host buffers ------------------------------
@@ -299,6 +325,7 @@ def run_ours(args):
     W.apply_options(de, case, x=x, set_dt=False, bcs=bcs)
     de.init()
     de.set_dt(W.cfl_dt(case, de.min_edge_length()))   # CFL step from the device reduction
+    t_setup = time.perf_counter() - t0
     de.run(K)
     u_host = de.node_vec("u")
     r_host = de.reaction()
@@ -316,20 +343,35 @@ def run_ours(args):
 
     # ---- roofline of the dominant kernel -------------------------------------------------
     peak, peak_kind = measured_peak()
-    dom = int(np.argmax(ms_phase))
-    ph = PHASES[dom]
     alg_table = ALG_BYTES_TET_MIXED if case.tritetra else ALG_BYTES_HEX_MIXED
-    be, bn = alg_table[ph]
-    alg_bytes = be * E + bn * case.n_node
+    phase_bytes = {p: alg_table[p][0] * E + alg_table[p][1] * case.n_node for p in PHASES}
+    phases = PHASES
+    if mode == 3:
+        phases = TILED_PHASES
+        phase_bytes["tile"], phase_bytes["shared"] = tiled_alg_bytes(E, case.n_node, tile_stats)
+    dom = int(np.argmax(ms_phase))
+    ph = phases[dom]
+    alg_bytes = phase_bytes[ph]
     achieved = alg_bytes / (ms_phase[dom] * 1e-3) / 1e9
     roof = {"bound": "hbm", "kernel": KERNEL_NAMES[ph], "achieved": round(achieved, 1),
             "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
             "frac": round(achieved / peak, 4), "traffic": kernel_traffic(ph, case.name, E),
-            "alg_bytes_per_launch": alg_bytes, "ms_per_launch": round(float(ms_phase[dom]), 4),
-            "phases_ms": {p: round(float(m), 4) for p, m in zip(PHASES, ms_phase)}}
-    step_alg = sum(alg_table[p][0] * E + alg_table[p][1] * case.n_node
-                   for p in PHASES)
+            "alg_bytes_per_launch": int(alg_bytes),
+            "ms_per_launch": round(float(ms_phase[dom]), 4),
+            "phases_ms": {p: round(float(m), 4) for p, m in zip(phases, ms_phase)},
+            "phases_gbs": {p: round(phase_bytes[p] / (float(m) * 1e-3) / 1e9, 1)
+                           for p, m in zip(phases, ms_phase)}}
+    step_alg = sum(phase_bytes[p] for p in phases)
     roof["step_achieved_gbs"] = round(step_alg / (ms_step * 1e-3) / 1e9, 1)
+    # the path's roofline: compulsory bytes of one pass over the state per
+    # element-step (mixed: hex 92 + 144 r, tet 76 + 144 r, r = nodes / elements)
+    r_ne = case.n_node / E
+    b_alg = (76.0 if case.tritetra else 92.0) + 144.0 * r_ne
+    path_gbs = b_alg * E / (ms_step * 1e-3) / 1e9
+    roof["path"] = {"b_alg_per_element_step": round(b_alg, 1), "achieved": round(path_gbs, 1),
+                    "frac": round(path_gbs / peak, 4),
+                    "note": "compulsory bytes per element-step x element-steps/s over the "
+                            "peak; 'frac' above is the dominant kernel's own bytes"}
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -346,19 +388,22 @@ def run_ours(args):
                        "l2": f"~{step_alg / 1e9:.2f} GB touched per step per replica, "
                              f"{'larger' if step_alg > 129e6 else 'smaller'} than the 129 MB L2; "
                              "no flush"},
-            "fp64": {"value": round(fp64_value, 1), "ms_per_step": round(ms_fp64 / K, 4)},
+            "fp64": {"value": round(fp64_value, 1), "ms_per_step": round(ms_fp64 / K, 4),
+                     "over_cpu_baseline": (round(fp64_value / cpu["value"], 2) if cpu
+                                           else None)},
             "mixed_over_fp64": round(value / world / fp64_value, 3),
             "error_vs_fp64": err,
             "e2e": {"value": round(E * K / t_e2e, 1), "unit": UNIT,
                     "h2d_bytes_per_step": int(h2d / K), "d2h_bytes_per_step": int(d2h / K),
-                    "seconds": round(t_e2e, 3),
-                    "includes": "mesh + BC upload, init, device CFL dt, K steps, "
-                                "displacement + reaction readback"},
+                    "seconds": round(t_e2e, 3), "setup_seconds": round(t_setup, 3),
+                    "setup_share": round(t_setup / t_e2e, 3),
+                    "includes": "mesh + BC upload, init (launch shapes from the library's "
+                                "per-process autotune cache: an earlier domain of this size "
+                                "was tuned), device CFL dt, K steps (graphs captured in the "
+                                "run), displacement + reaction readback"},
             "gpu_launches": int(launches),
-            "step_mode": ({"mode": "one cluster launch per run", "cluster_blocks": cl_blocks,
-                           "block_size": cl_bs,
-                           "note": "roofline phases are the per-phase kernels, timed apart"}
-                          if mode == 2 else {"mode": "per-phase kernels, CUDA graph"}),
+            "step_mode": step_mode_label(mode, cl_blocks, cl_bs, K, graph_replays, launches,
+                                         tile_stats),
             "autotuned_launch": tuned,
             "launch_note": "items_per_thread 0 = persistent grid (SMs x resident blocks)",
             "roofline": roof,
@@ -370,6 +415,53 @@ def run_ours(args):
         import torch.distributed as dist
 
         dist.destroy_process_group()
+
+
+def step_mode_label(mode, cl_blocks, cl_bs, K, graph_replays, launches, tile_stats=None):
+    """What the timed wf_run(K) launched, as counted by the library."""
+    if mode == 2:
+        return {"mode": "one cluster launch per run", "cluster_blocks": cl_blocks,
+                "block_size": cl_bs, "kernel_launches": int(launches),
+                "note": "roofline phases are the per-phase kernels, timed apart"}
+    full, rem = divmod(K, 32)
+    kernels = ("geometry, nodal, tiled element+assembly, shared-node kernels" if mode == 3
+               else "per-phase kernels")
+    extra = {}
+    if mode == 3 and tile_stats:
+        extra = {"tiles": tile_stats[0], "shared_nodes": tile_stats[1],
+                 "threads_per_tile": cl_bs}
+    return {**extra, "mode": f"{kernels} replayed from CUDA graphs" if graph_replays
+            else f"{kernels}, direct launches",
+            "graph_replays": int(graph_replays),
+            "graphs": f"{full} x 32 steps" + (f" + 1 x {rem} steps" if rem > 1 else "")
+            + (" + 1 direct step" if rem == 1 else ""),
+            "graphs_built": "before the timed region (wf_prepare_run)"}
+
+
+def mixed_errors(dm, df, nrun):
+    """Mixed-precision run against the FP64 run of the same inputs: max-norm
+    and RMS relative errors of the displacement, the plastic strain and the
+    reaction history."""
+    rm, rf = dm.reaction()[:nrun], df.reaction()[:nrun]
+    um, uf = dm.node_vec("u"), df.node_vec("u")
+    plm, plf = dm.elem_scalar("pl_strain"), df.elem_scalar("pl_strain")
+
+    def rel(a, b):
+        return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+    def rms(a, b):
+        return float(np.sqrt(np.mean((a - b) ** 2)) / max(np.sqrt(np.mean(b ** 2)), 1e-300))
+
+    has_pl = np.max(np.abs(plf)) > 0
+    return {"reaction": rel(rm, rf), "reaction_rms": rms(rm, rf),
+            "displacement": rel(um, uf), "displacement_rms": rms(um, uf),
+            "pl_strain": rel(plm, plf) if has_pl else 0.0,
+            "pl_strain_rms": rms(plm, plf) if has_pl else 0.0,
+            "pl_strain_max_fp64": float(np.max(plf)),
+            "plastic_elements_fp64": int(np.count_nonzero(plf)),
+            "steps": nrun,
+            "how": "fresh mixed run vs the FP64 run of the same inputs; max-norm: "
+                   "max|a-b|/max|b|, rms: ||a-b||_2/||b||_2"}
 
 
 def run_ensemble(args):
@@ -612,12 +704,14 @@ def run_reference(args):
     d = orabind.OracleDomain(threads=threads)
     W.apply(d, case, x=x)
     d.init()
-    d.step(max(1, min(args.warmup, 1)))
-    # each step is one full time step of the workload; the count is bounded so
-    # that the run ends within a few minutes on the host cores
+    # the same warm-up count as the GPU arm, bounded to ~30 s on slow hosts
     t0 = time.perf_counter()
     d.step(1)
     per = time.perf_counter() - t0
+    wn = int(max(0, min(args.warmup - 1, 30.0 / max(per, 1e-9))))
+    d.step(wn)
+    # each step is one full time step of the workload; the count is bounded so
+    # that the run ends within a few minutes on the host cores
     n = int(max(1, min(args.steps, 60.0 / max(per, 1e-9))))
     t0 = time.perf_counter()
     d.step(n)
@@ -625,9 +719,9 @@ def run_reference(args):
     value = case.n_elem * n / t
     line = {
         "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": 0, "steps": n,
-        "warmup": 2, "ms_per_step": round(t / n * 1e3, 3), "higher_is_better": True,
+        "warmup": args.warmup, "ms_per_step": round(t / n * 1e3, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "impl": "reference",
+        "impl": "reference", "warmup_steps_run": 1 + wn,
         "config": {"workload": case.name, "elements": case.n_elem, "nodes": case.n_node,
                    "precision": "fp64"},
         "cpu_baseline": {"value": round(value, 1), "unit": UNIT, "cores": threads, "kind": "port",
@@ -636,6 +730,38 @@ def run_reference(args):
                 "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def run_profile_case(args):
+    """A bare run for kernel profiles: one domain of the configuration (FP64 or
+    mixed), W + K steps in the library's default step mode, no other work, so
+    that the launch sequence under a profiler is init, then the steps. With
+    --no-autotune the mixed kernels keep their default launch shapes (no
+    tuning launches before the steps)."""
+    import torch
+
+    import weldformfem_gb300 as wf
+
+    torch.cuda.set_device(0)
+    case = W.config(args.config, scale=tuple(args.scale) if args.scale else None)
+    prec = wf.WF_FP64 if args.profile == "fp64" else wf.WF_MIXED
+    d = wf.Domain(prec, device=0)
+    W.apply(d, case)
+    if args.no_autotune:
+        d.set_autotune(False)
+    d.init()
+    d.run(args.warmup)
+    d.sync()
+    st = torch.cuda.ExternalStream(d.stream_handle(), device=0)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(st)
+    d.run(args.steps)
+    b.record(st)
+    b.synchronize()
+    d.sync()
+    print(json.dumps({"profile_case": case.name, "precision": args.profile,
+                      "elements": case.n_elem, "step_mode": d.step_mode()[0],
+                      "ms_per_step": round(a.elapsed_time(b) / args.steps, 4)}), flush=True)
 
 
 def main():
@@ -648,11 +774,18 @@ def main():
     ap.add_argument("--scale", type=int, nargs=3, default=None)
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--profile", choices=["mixed", "fp64"], default=None,
+                    help="bare run of one domain for kernel profiles (no other measurement)")
+    ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--short-error", action="store_true",
+                    help="mixed-vs-FP64 errors over W + K steps instead of the whole run")
     ap.add_argument("--n-spec", type=int, default=1024)
     ap.add_argument("--adj-steps", type=int, default=4000)
     ap.add_argument("--every", type=int, default=64)
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.profile:
+        run_profile_case(args)
+    elif args.impl == "reference":
         run_reference(args)
     elif args.config == 3:
         run_ensemble(args)

@@ -267,12 +267,27 @@ WF_API wf_status wf_get_specimen_reaction(wf_domain *d, int32_t spec, double *ou
  * The time step may be set before or after (wf_min_edge_length works once
  * the mesh is on the device); it must be set before wf_run. */
 WF_API wf_status wf_init(wf_domain *d);
-/* nsteps iterations of the loop body (Solver_explicit.C:346-1167). */
+/* nsteps iterations of the loop body (Solver_explicit.C:346-1167). The
+ * per-phase kernels of the steps are replayed from CUDA graphs: graphs of 32
+ * steps, then one graph of the remaining steps (a single remaining step is
+ * launched directly). A graph is captured and instantiated the first time a
+ * run needs it and kept until a launch parameter changes (time step, end
+ * time, launch shapes, history growth). */
 WF_API wf_status wf_run(wf_domain *d, int64_t nsteps);
+/* No counterpart in the reference. Captures and instantiates now the graphs
+ * a following wf_run(d, nsteps) replays (and grows the histories it fills),
+ * so that the run itself does no capture. Runs nothing. */
+WF_API wf_status wf_prepare_run(wf_domain *d, int64_t nsteps);
 /* Domain_d::SolveChungHulbert: steps while Time < end time; *nsteps = count. */
 WF_API wf_status wf_solve(wf_domain *d, int64_t *nsteps);
 WF_API wf_status wf_get_time(const wf_domain *d, double *t, int64_t *step);
-/* Waits for the domain's stream and reports any device-side error status. */
+/* Waits for the domain's stream and reports any device-side error status.
+ * As the reference loop does (Solver_explicit.C:777-785), a non-finite
+ * assembled internal force is cleared to zero and the run goes on; the node
+ * kernels also raise a flag, which the first wf_sync (or wf_solve) after the
+ * wf_run that raised it reports as WF_ERR_NONFINITE, with the smallest
+ * offending node id in wf_last_error(). The flag is then cleared, so a
+ * later wf_sync reports only new occurrences. Readbacks do not check it. */
 WF_API wf_status wf_sync(wf_domain *d);
 /* Minimum element edge length of the current mesh (device reduction). */
 WF_API wf_status wf_min_edge_length(wf_domain *d, double *hmin);
@@ -290,8 +305,12 @@ WF_API wf_status wf_get_phase_times(wf_domain *d, double ms[4], int64_t *steps, 
  * reported as 0), all grid-stride, timed in interleaved rounds, and keeps the
  * fastest; the kernels' results do not
  * depend on the shape, and the state the element kernel advances is restored
- * after the trials. wf_get_launch_config reports the choice for phase 0
- * (geometry), 1 (nodal) or 2 (element). */
+ * after the trials. The choice is kept for the life of the process, keyed by
+ * the device, the element type, the mesh sizes and the kernel variant
+ * (material law, contact, thermal coupling, energy history, specimens): a
+ * later domain with the same key takes it without timing again.
+ * wf_get_launch_config reports the choice for phase 0 (geometry), 1 (nodal)
+ * or 2 (element). */
 WF_API wf_status wf_set_autotune(wf_domain *d, int32_t on);
 WF_API wf_status wf_get_launch_config(const wf_domain *d, int32_t phase, int32_t *block,
                                       int32_t *items_per_thread, double *ms);
@@ -307,16 +326,38 @@ WF_API wf_status wf_set_launch_config(wf_domain *d, int32_t phase, int32_t block
  * own fixed element and node ranges and meet at cluster barriers between the
  * phases: same per-element and per-node arithmetic, so the state is bitwise
  * that of mode 1; the reaction sum runs in another order. Not with specimens,
- * the energy history or phase timing. Mode 0 (default) picks mode 2 for
- * meshes of at most 3000 elements, else mode 1. wf_get_step_mode reports the
- * mode the next wf_run uses and, for mode 2, the cluster's blocks and block
- * size (0 otherwise). */
+ * the energy history or phase timing. Mode 3 (hexahedra): the element and
+ * node phases become a tiled kernel and a shared-node kernel. At wf_init the
+ * elements are binned by centroid into cubes of about 8 element sizes and cut
+ * into tiles of at most 512 elements; one block per tile stages the tile's
+ * nodes in shared memory, computes its elements' forces (same arithmetic as
+ * mode 1), sums them per node in shared memory and updates the nodes all of
+ * whose elements are in the tile; the other ("shared") nodes gather their
+ * forces from HBM in list order, as in mode 1. On meshes numbered like
+ * AddBoxLength's, every node's force is summed in mode 1's order, so the
+ * state is bitwise that of mode 1; the reaction sum runs in another order.
+ * Not with specimens, thermal coupling, the energy history or triangle-mesh
+ * contact; wf_get_tiles tells whether the mesh was tiled. Mode 0 (default)
+ * picks mode 2 for meshes of at most 3000 elements, else mode 1. wf_get_step_mode reports the mode the next
+ * wf_run uses and, for mode 2, the cluster's blocks and block size, for mode
+ * 3 the tiles and threads per tile (0 otherwise). */
 WF_API wf_status wf_set_step_mode(wf_domain *d, int32_t mode);
+/* No counterpart in the reference. The tiles built at wf_init for step mode
+ * 3: their number, the number of shared nodes, the sum over tiles of their
+ * distinct nodes and the node-list entries of the shared nodes (the counts
+ * the tiled kernels' memory traffic follows), or zeros and, in why (a
+ * NUL-terminated string of at most why_cap bytes), the reason the mesh was
+ * not tiled. Any output may be NULL. */
+WF_API wf_status wf_get_tiles(const wf_domain *d, int32_t *ntiles, int32_t *nshared,
+                              int64_t *tile_nodes, int64_t *shared_slots, char *why,
+                              int64_t why_cap);
 WF_API wf_status wf_get_step_mode(const wf_domain *d, int32_t *mode, int32_t *blocks,
                                   int32_t *block_size);
 /* Number of kernels this domain has launched since wf_init (graph nodes
  * included). */
 WF_API wf_status wf_get_launch_count(const wf_domain *d, int64_t *n);
+/* Number of step graphs this domain has replayed since wf_init. */
+WF_API wf_status wf_get_graph_launches(const wf_domain *d, int64_t *n);
 /* The domain's CUDA stream (a cudaStream_t), for callers that order their
  * own work or CUDA events after the domain's kernels. */
 WF_API wf_status wf_get_stream(const wf_domain *d, void **stream);
@@ -327,9 +368,11 @@ WF_API wf_status wf_get_transfer_bytes(const wf_domain *d, int64_t *h2d, int64_t
 /* No counterpart in the reference. For callers that cannot allocate device
  * memory (code inside another framework's memory pool, loops that must not
  * risk the synchronisation cudaMalloc/cudaFree can cause, hosts with a device
- * budget fixed up front): the element volumes and per-node volume sums of
- * the step's geometry and nodal phases (CalcElemVol, Mechanical.C:264-293;
- * CalcNodalVol, :1555-1572), computed without any allocation. The caller
+ * budget fixed up front): each element's volume (determinant of its Jacobian
+ * times the integration weight: 8 at the centre of a hexahedron, 1/6 for a
+ * tetrahedron), then each node's volume (the sum of its elements' volumes in
+ * list order, divided by the nodes per element), computed without any
+ * allocation. The caller
  * passes device pointers: xyz[3*nn] interleaved coordinates, elnod[ne*npe]
  * (npe 8 or 4), the node->element lists as wf_get_connectivity returns them
  * (nodel_offset[nn], nodel_count[nn], nodel[total]) and voln[nn] for the
@@ -340,8 +383,11 @@ WF_API wf_status wf_get_transfer_bytes(const wf_domain *d, int64_t *h2d, int64_t
  * doubles (8 MiB) that every GPU which loads the library holds until exit;
  * ne above that returns WF_ERR_UNSUPPORTED. The array is shared by all calls
  * and keeps the last call's contents; calls that overlap on the GPU race.
- * The first call on a device looks up the array's device address; make that
- * first call before any stream capture. */
+ * The first call on a device looks up the array's device address (again
+ * after the device's context has been replaced, e.g. by cudaDeviceReset);
+ * make that first call before any stream capture. A launch error of the call
+ * returns WF_ERR_CUDA and is cleared; a CUDA error already pending on the
+ * calling thread is left pending and not reported here. */
 #define WF_NOALLOC_MAX_ELEMS 1048576
 WF_API wf_status wf_nodal_volumes_noalloc(const double *xyz, const int32_t *elnod, int64_t nn,
                                           int64_t ne, int32_t npe, const int32_t *nodel_offset,

@@ -11,9 +11,12 @@ from weldformfem_gb300 import workloads as W
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 HOLLOMON = dict(model=1, E=200e9, nu=0.3, rho=7850.0, sy0=300e6, hol_K=600e6, hol_m=0.2)
 STAB = [0.3, 0.7, 0.2, 0.08, 0.15, 0.15, 0.8, 0.2, 0.05, 0.0]
-# The reference checkout read by the CPU parity tests that need it (absent on
-# machines without it; those tests skip).
-REFERENCE_ROOT = os.environ.get("WF_REFERENCE_ROOT", "/root/reference")
+# The reference checkout read by the CPU parity tests that need it: the
+# WF_REFERENCE_ROOT environment variable, else a "reference" directory beside
+# the repository (absent on machines without it; those tests skip).
+REFERENCE_ROOT = os.environ.get("WF_REFERENCE_ROOT") or os.path.normpath(
+    os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), os.pardir,
+                 "reference"))
 
 
 def golden_cases():

@@ -88,6 +88,33 @@ def test_batched_fp64_matches_oracle():
 
 
 @pytest.mark.gpu
+def test_batched_fp64_config3_slice_matches_oracle():
+    """The first 32 specimens of the config-3 ensemble itself (n ~ U{6..40},
+    per-specimen materials and top velocities), 400 steps, FP64 against the
+    oracle run of each specimen on its own."""
+    full = W.ensemble(n_spec=1024)
+    b = W.Batch(full.name, full.cases[:32], full.hg)
+    steps = 400
+    d = wf.Domain(wf.WF_FP64)
+    dts = W.apply_batch(d, b)
+    d.init()
+    d.run(steps)
+    u = d.node_vec("u")
+    pl = d.elem_scalar("pl_strain")
+    eoff, noff = b.offsets()
+    assert eoff[-1] > 200000
+    for s, c in enumerate(b.cases):
+        c.dt = float(dts[s])
+        o = O.OracleDomain()
+        W.apply(o, c)
+        o.init()
+        o.step(steps)
+        assert H.rel_err(u[noff[s]:noff[s + 1]], o.node_vec("u")) <= 1e-9, s
+        assert H.rel_err(pl[eoff[s]:eoff[s + 1]], o.elem_scalar("pl_strain")) <= 1e-9, s
+        assert H.rel_err(d.specimen_reaction(s), o.reaction()) <= 1e-9, s
+
+
+@pytest.mark.gpu
 def test_batched_rejects_bad_tables():
     b = small_ensemble()
     x, el, emat, bcs, tops, eoff, noff = b.assemble()

@@ -98,12 +98,14 @@ def test_mixed_rejects_unsupported_options():
 
 
 def test_autotuned_and_default_launch_shapes_agree_bitwise():
-    """The autotuner only changes launch shapes; results are identical."""
+    """The autotuner only changes launch shapes; results are identical (the
+    per-phase step, whose three kernels are all tuned)."""
     case = W.config(2, scale=(20, 18, 10))
     outs = []
     for tune in (True, False):
         d = wf.Domain(wf.WF_MIXED)
         W.apply(d, case)
+        d.set_step_mode(1)
         d.set_autotune(tune)
         d.init()
         d.run(64)
@@ -116,6 +118,7 @@ def test_autotuned_and_default_launch_shapes_agree_bitwise():
     for bs, ept in ((64, 0), (256, 0), (128, 4)):
         d = wf.Domain(wf.WF_MIXED)
         W.apply(d, case)
+        d.set_step_mode(1)
         d.set_autotune(False)
         d.init()
         for phase in range(3):

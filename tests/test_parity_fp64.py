@@ -108,17 +108,68 @@ def test_fp64_tets_perturbed_matches_oracle():
     check(errs)
 
 
+def test_fp64_config1_full_size_matches_oracle():
+    """Config 1 as specified: 576,000 perturbed tetrahedra, 2000 steps."""
+    case = W.config(1)
+    assert case.n_elem == 576000
+    d, _ = gpu_run(case, case.steps)
+    o = O.OracleDomain()
+    W.apply(o, case)
+    o.init()
+    o.step(case.steps)
+    errs = H.compare_state(d, o)
+    check(errs)
+    assert H.rel_err(d.reaction(), o.reaction()) <= TOL
+    assert d.elem_scalar("pl_strain").max() > 0.0   # the run is plastic
+
+
+def test_fp64_config2_full_size_matches_oracle():
+    """Config 2 at full size (8,388,608 hexahedra, rigid die, friction) for
+    a bounded 20 steps: the oracle takes about 0.4 s per step on 16 cores."""
+    case = W.config(2)
+    steps = 20
+    x = case.coords()
+    d = wf.Domain(wf.WF_FP64)
+    W.apply(d, case, x=x)
+    d.init()
+    d.run(steps)
+    d.sync()
+    o = O.OracleDomain()
+    W.apply(o, case, x=x)
+    o.init()
+    o.step(steps)
+    errs = H.compare_state(d, o)
+    check(errs)
+    assert H.rel_err(d.node_vec("contforce"), o.node_vec("contforce")) <= TOL
+    r = d.reaction()
+    assert r.shape == (steps,) and r.max() > 0.0
+    assert H.rel_err(r, o.reaction()) <= TOL
+
+
 def test_graph_and_direct_launches_agree_bitwise():
     case = W.config(0, scale=(5, 5, 5))
-    a, _ = gpu_run(case, 70)       # 2 graph launches of 32 steps + 6 direct steps
+    a, _ = gpu_run(case, 70)       # 2 graph launches of 32 steps + a graph of 6 steps
+    assert a.graph_launches() == 3
     b = wf.Domain()
     W.apply(b, case)
     b.init()
     for _ in range(70):
         b.run(1)                   # direct launches only
+    assert b.graph_launches() == 0
+    c = wf.Domain()
+    W.apply(c, case)
+    c.init()
+    c.prepare_run(20)              # graphs built ahead, nothing run
+    assert c.graph_launches() == 0 and c.reaction().shape == (0,)
+    for _ in range(3):
+        c.run(20)                  # one 20-step graph per call
+    c.run(10)
+    assert c.graph_launches() == 4
     for f in ("x", "v", "u"):
         np.testing.assert_array_equal(a.node_vec(f), b.node_vec(f))
+        np.testing.assert_array_equal(a.node_vec(f), c.node_vec(f))
     np.testing.assert_array_equal(a.reaction(), b.reaction())
+    np.testing.assert_array_equal(a.reaction(), c.reaction())
 
 
 def test_min_edge_length_reduction():

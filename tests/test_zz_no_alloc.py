@@ -28,7 +28,7 @@ def domain_voln(case):
     return d, d.node_scalar("voln")
 
 
-def noalloc_voln(torch, case, d):
+def noalloc_voln(torch, case, d, stream=None):
     elnod, nodel, _loc, off, cnt = d.conn()
     nn, ne, npe = d.nn, d.ne, d.npe
     dev = torch.device("cuda:0")
@@ -38,12 +38,23 @@ def noalloc_voln(torch, case, d):
     t_cnt = torch.from_numpy(cnt).to(dev)
     t_nodel = torch.from_numpy(nodel).to(dev)
     out = torch.full((nn,), float("nan"), dtype=torch.float64, device=dev)
-    stream = torch.cuda.current_stream(dev).cuda_stream
+    if stream is None:
+        st = wf.lib().wf_nodal_volumes_noalloc(xyz.data_ptr(), el.data_ptr(), nn, ne, npe,
+                                               t_off.data_ptr(), t_cnt.data_ptr(),
+                                               t_nodel.data_ptr(), out.data_ptr(),
+                                               torch.cuda.current_stream(dev).cuda_stream)
+        assert st == 0, wf.STATUS.get(st, st)
+        torch.cuda.synchronize(dev)
+        return out.cpu().numpy()
+    # on the caller's own stream: the inputs were made on the current stream,
+    # so the side stream waits for it; only that stream is synchronised after
+    stream.wait_stream(torch.cuda.current_stream(dev))
     st = wf.lib().wf_nodal_volumes_noalloc(xyz.data_ptr(), el.data_ptr(), nn, ne, npe,
                                            t_off.data_ptr(), t_cnt.data_ptr(),
-                                           t_nodel.data_ptr(), out.data_ptr(), stream)
+                                           t_nodel.data_ptr(), out.data_ptr(),
+                                           stream.cuda_stream)
     assert st == 0, wf.STATUS.get(st, st)
-    torch.cuda.synchronize(dev)
+    stream.synchronize()
     return out.cpu().numpy()
 
 
@@ -63,6 +74,10 @@ def test_noalloc_matches_domain_path_on_two_calls_in_a_row():
     assert rel_err(got2, ref2) <= TOL
     again = noalloc_voln(torch, second, d2)
     np.testing.assert_array_equal(again, got2)
+    # queued on a non-default stream of the caller: same bits
+    side = torch.cuda.Stream(device=torch.device("cuda:0"))
+    on_side = noalloc_voln(torch, second, d2, stream=side)
+    np.testing.assert_array_equal(on_side, got2)
 
 
 def test_noalloc_rejects_too_many_elements():
@@ -71,3 +86,7 @@ def test_noalloc_rejects_too_many_elements():
     st = L.wf_nodal_volumes_noalloc(8, 8, 8, 1048577, 8, 8, 8, 8, 8, None)
     assert st == 5   # WF_ERR_UNSUPPORTED
     assert L.wf_nodal_volumes_noalloc(None, 8, 8, 8, 8, 8, 8, 8, 8, None) == 1
+    # invalid element type and empty meshes: WF_ERR_ARG before any pointer is used
+    assert L.wf_nodal_volumes_noalloc(8, 8, 8, 8, 6, 8, 8, 8, 8, None) == 1
+    assert L.wf_nodal_volumes_noalloc(8, 8, 8, 0, 8, 8, 8, 8, 8, None) == 1
+    assert L.wf_nodal_volumes_noalloc(8, 8, 0, 8, 8, 8, 8, 8, 8, None) == 1

@@ -122,6 +122,8 @@ _SIGS = {
     "wf_set_phase_timing": [C.c_void_p, C.c_int32],
     "wf_get_phase_times": [C.c_void_p, _dp, C.POINTER(C.c_int64), C.c_int32],
     "wf_get_launch_count": [C.c_void_p, C.POINTER(C.c_int64)],
+    "wf_get_graph_launches": [C.c_void_p, C.POINTER(C.c_int64)],
+    "wf_prepare_run": [C.c_void_p, C.c_int64],
     "wf_get_stream": [C.c_void_p, C.POINTER(C.c_void_p)],
     "wf_set_autotune": [C.c_void_p, C.c_int32],
     "wf_get_launch_config": [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
@@ -131,6 +133,8 @@ _SIGS = {
     "wf_set_step_mode": [C.c_void_p, C.c_int32],
     "wf_get_step_mode": [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                          C.POINTER(C.c_int32)],
+    "wf_get_tiles": [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                     C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.c_char_p, C.c_int64],
     "wf_adjoint_forward": [C.c_void_p, C.c_int64, C.c_int64],
     "wf_deck_read": [C.c_char_p, C.POINTER(C.c_void_p), C.c_char_p, C.c_int64],
     "wf_deck_free": [C.c_void_p],
@@ -402,11 +406,23 @@ class Domain:
         self._call("wf_set_autotune", int(bool(on)))
 
     def set_step_mode(self, mode):
-        """0 automatic, 1 per-phase kernels (graph), 2 one cluster launch per run."""
+        """0 automatic, 1 per-phase kernels, 2 one cluster launch per run, 3 tiled."""
         self._call("wf_set_step_mode", int(mode))
 
+    def tiles(self):
+        """(tiles, shared nodes, why the mesh was not tiled) of step mode 3."""
+        return self.tile_stats()[:2] + (self.tile_stats()[4],)
+
+    def tile_stats(self):
+        """(tiles, shared nodes, sum of tile nodes, shared-node list entries, why)."""
+        nt, ns = C.c_int32(), C.c_int32()
+        tn, ss = C.c_int64(), C.c_int64()
+        buf = C.create_string_buffer(256)
+        self._call("wf_get_tiles", C.byref(nt), C.byref(ns), C.byref(tn), C.byref(ss), buf, 256)
+        return nt.value, ns.value, tn.value, ss.value, buf.value.decode()
+
     def step_mode(self):
-        """(mode the next run uses, cluster blocks, block size)."""
+        """(mode the next run uses, cluster blocks or tiles, block size)."""
         m, b, t = C.c_int32(), C.c_int32(), C.c_int32()
         self._call("wf_get_step_mode", C.byref(m), C.byref(b), C.byref(t))
         return m.value, b.value, t.value
@@ -436,6 +452,16 @@ class Domain:
         n = C.c_int64()
         self._call("wf_get_launch_count", C.byref(n))
         return n.value
+
+    def graph_launches(self):
+        """Step graphs replayed since init."""
+        n = C.c_int64()
+        self._call("wf_get_graph_launches", C.byref(n))
+        return n.value
+
+    def prepare_run(self, n):
+        """Builds now the step graphs a following run(n) replays (runs nothing)."""
+        self._call("wf_prepare_run", int(n))
 
     # readback ---------------------------------------------------------
     def node_vec(self, name):

@@ -7,11 +7,14 @@
 #include <array>
 #include <cmath>
 #include <cstdarg>
+#include <cstddef>
+#include <climits>
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <new>
 #include <string>
 #include <thread>
@@ -179,9 +182,10 @@ struct wf_domain {
   int64_t host_step = 0;          // steps launched since init
   double host_time = 0.0;         // Time accumulated on the host (mirror)
   bool mix_valid_fp64 = false;    // FP64 export of the mixed state is current
-  // graphs
-  cudaGraphExec_t graph = nullptr;
-  int graph_steps = 0;
+  // step graphs keyed by their number of steps: kGraphSteps for long runs and
+  // one per remainder length wf_run has met (built on first use, or ahead of
+  // time by wf_prepare_run)
+  std::map<int64_t, cudaGraphExec_t> graphs;
   // per-phase timing
   bool phase_timing = false;
   std::vector<cudaEvent_t> ev_pool;   // 5 events per timed step
@@ -189,14 +193,25 @@ struct wf_domain {
   double phase_ms[4] = {0, 0, 0, 0};
   int64_t phase_steps = 0;
   int64_t launches = 0;
+  int64_t graph_launches = 0;     // step graphs replayed since wf_init
   int64_t h2d_bytes = 0, d2h_bytes = 0;
+  // pinned copy of the device step state, queued after every wf_run and
+  // read by the next wf_sync (the non-finite force check)
+  StepState *st_host = nullptr;
+  bool st_pending = false;
   // launch shapes of the tunable mixed kernels (geometry, nodal, elements)
   bool autotune = true;
+  bool tune_cached = false;       // the last init took its shapes from the process cache
   LaunchCfg cfg[3] = {LaunchCfg{128, 1}, LaunchCfg{256, 1}, LaunchCfg{128, 1}};
   double cfg_ms[3] = {0, 0, 0};
   // step scheduling (mixed): 0 automatic, 1 per-phase kernels, 2 one cluster
-  // launch per run; the cluster shape is found at init for small meshes
+  // launch per run, 3 tiled element + assembly kernels; the cluster shape is
+  // found at init for small meshes, the tiles are built at init for meshes of
+  // hexahedra that the tiled kernels cover
   int32_t step_mode = 0;
+  bool tiled = false;             // tiles built (TileParams T valid)
+  TileParams T{};
+  std::string tile_why;           // why the mesh was not tiled
   int cl_blocks = 0, cl_bs = 0;
   double *cl_part = nullptr;      // [kClusterChunk][cl_blocks] reaction partials
   // batched ensemble
@@ -217,6 +232,12 @@ struct wf_domain {
 };
 
 namespace {
+
+// Destroys the domain's step graphs (they hold launch parameters by value).
+void drop_graphs(wf_domain *d) {
+  for (auto &g : d->graphs) cudaGraphExecDestroy(g.second);
+  d->graphs.clear();
+}
 
 wf_status fail(wf_domain *d, wf_status s, const char *fmt, ...) {
   if (d) {
@@ -274,12 +295,12 @@ void free_adjoint(wf_domain *d) {
 
 void free_device(wf_domain *d) {
   free_adjoint(d);
-  if (d->graph) {
-    cudaGraphExecDestroy(d->graph);
-    d->graph = nullptr;
-  }
+  drop_graphs(d);
   for (void *p : d->allocs) cudaFree(p);
   d->allocs.clear();
+  if (d->st_host) cudaFreeHost(d->st_host);
+  d->st_host = nullptr;
+  d->st_pending = false;
   if (d->init_stage) cudaFree(d->init_stage);
   d->init_stage = nullptr;
   for (cudaEvent_t ev : d->ev_pool) cudaEventDestroy(ev);
@@ -289,6 +310,8 @@ void free_device(wf_domain *d) {
   d->M = MixState{};
   d->readback = nullptr;
   d->mvol = nullptr;
+  d->tiled = false;
+  d->T = TileParams{};
   d->initialized = false;
 }
 
@@ -907,10 +930,7 @@ WF_API wf_status wf_allocate_bcs(wf_domain *d) {
 WF_API wf_status wf_set_dt(wf_domain *d, double dt) {
   if (!d || !(dt > 0.0) || !std::isfinite(dt)) return WF_ERR_ARG;
   d->dt = dt;
-  if (d->graph) {
-    cudaGraphExecDestroy(d->graph);
-    d->graph = nullptr;
-  }
+  drop_graphs(d);
   return WF_OK;
 }
 
@@ -920,10 +940,7 @@ WF_API wf_status wf_set_end_time(wf_domain *d, double t) {
   if (d->initialized && d->P.end_t != t) {
     // the die ramp of triangle-mesh contact reads the end time
     d->P.end_t = t;
-    if (d->graph) {
-      cudaGraphExecDestroy(d->graph);
-      d->graph = nullptr;
-    }
+    drop_graphs(d);
   }
   return WF_OK;
 }
@@ -1159,12 +1176,19 @@ void bc_tables(wf_domain *d, std::vector<uint32_t> &code, std::vector<double> &v
   std::vector<int32_t> order(nodes.size());
   for (size_t i = 0; i < order.size(); i++) order[i] = (int32_t)i;
   std::sort(order.begin(), order.end(), [&](int32_t a, int32_t b) { return nodes[a] < nodes[b]; });
-  std::map<std::tuple<double, double, double>, uint32_t> sets;
+  // keyed on the values' bit patterns: every value keeps its own set, NaN
+  // included (double comparisons would merge a NaN into another set)
+  auto bits = [](double v) {
+    uint64_t u;
+    std::memcpy(&u, &v, sizeof u);
+    return u;
+  };
+  std::map<std::tuple<uint64_t, uint64_t, uint64_t>, uint32_t> sets;
   vals.assign(3, 0.0);
-  sets[std::make_tuple(0.0, 0.0, 0.0)] = 0;
+  sets[std::make_tuple(bits(0.0), bits(0.0), bits(0.0))] = 0;
   code.assign(d->nn, 0u);
   for (int32_t i : order) {
-    auto key = std::make_tuple(v3[i][0], v3[i][1], v3[i][2]);
+    auto key = std::make_tuple(bits(v3[i][0]), bits(v3[i][1]), bits(v3[i][2]));
     uint32_t id;
     auto it = sets.find(key);
     if (it == sets.end()) {
@@ -1184,11 +1208,81 @@ void bc_tables(wf_domain *d, std::vector<uint32_t> &code, std::vector<double> &v
 
 namespace {
 
+// Bounding box of the host coordinates {min x, y, z, max x, y, z}.
+void host_bbox(const wf_domain *d, double bb[6]) {
+  const int64_t nn = d->nn;
+  const double *x = d->x.data();
+  std::mutex mu;
+  for (int k = 0; k < 3; k++) {
+    bb[k] = INFINITY;
+    bb[3 + k] = -INFINITY;
+  }
+  host_parallel(nn, [&](int64_t i0, int64_t i1) {
+    double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int64_t n = i0; n < i1; n++)
+      for (int k = 0; k < 3; k++) {
+        lo[k] = std::min(lo[k], x[3 * n + k]);
+        hi[k] = std::max(hi[k], x[3 * n + k]);
+      }
+    std::lock_guard<std::mutex> lock(mu);
+    for (int k = 0; k < 3; k++) {
+      bb[k] = std::min(bb[k], lo[k]);
+      bb[3 + k] = std::max(bb[3 + k], hi[k]);
+    }
+  });
+}
+
+// Device allocation kept with the domain (build_tiles' tables).
+cudaError_t keep_alloc(void *ctx, void **p, size_t bytes) {
+  return dalloc_raw(static_cast<wf_domain *>(ctx), reinterpret_cast<char **>(p), bytes);
+}
+
 // Times each candidate launch shape of the three tunable mixed kernels on the
 // domain's data and keeps the fastest. The element kernel advances the
 // deviatoric stress and plastic strain, the nodal kernel the contact slip:
 // both are saved before the trials and restored after.
+// Launch shapes chosen by the autotuner, kept for the life of the process and
+// keyed by everything the tuned kernels' speed depends on (device, element
+// type, mesh sizes, material-law and coupling variants): a later domain of
+// the same mesh shape takes them instead of timing the candidates again.
+struct TuneKey {
+  int device;
+  int32_t npe, mat_general, thermal, contact, tri_on, energy_on, specimens, tiled;
+  int64_t ne, nn;
+  bool operator<(const TuneKey &o) const {
+    return std::tie(device, npe, mat_general, thermal, contact, tri_on, energy_on, specimens,
+                    tiled, ne, nn) < std::tie(o.device, o.npe, o.mat_general, o.thermal,
+                                              o.contact, o.tri_on, o.energy_on, o.specimens,
+                                              o.tiled, o.ne, o.nn);
+  }
+};
+struct TuneResult {
+  LaunchCfg cfg[3];
+  double ms[3];
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, TuneResult> g_tune_cache;
+
+TuneKey tune_key(const wf_domain *d) {
+  const StepParams &P = d->P;
+  return TuneKey{d->device, P.npe, P.mat_general, P.thermal, P.contact, P.tri_on, P.energy_on,
+                 P.nspec ? 1 : 0, (d->tiled && d->step_mode != 1) ? 1 : 0, d->ne, d->nn};
+}
+
 wf_status autotune_launches(wf_domain *d) {
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    auto it = g_tune_cache.find(tune_key(d));
+    if (it != g_tune_cache.end()) {
+      for (int k = 0; k < 3; k++) {
+        d->cfg[k] = it->second.cfg[k];
+        d->cfg_ms[k] = it->second.ms[k];
+      }
+      d->tune_cached = true;
+      return WF_OK;
+    }
+  }
+  d->tune_cached = false;
   const StepParams &P = d->P;
   MixState &M = d->M;
   const int64_t ne = d->ne, np = d->np;
@@ -1215,7 +1309,9 @@ wf_status autotune_launches(wf_domain *d) {
   constexpr int kRounds = 2;
   const int reps = ne >= (int64_t(1) << 20) ? 1 : 2;
   constexpr double kKeep = 1.25;
-  for (int phase = 0; phase < 3; phase++) {
+  // the per-phase element kernel is not run by tiled steps: not tuned then
+  const int nphase = (d->tiled && d->step_mode != 1) ? 2 : 3;
+  for (int phase = 0; phase < nphase; phase++) {
     std::vector<LaunchCfg> cands;
     for (int bs : sizes)
       for (int ept : epts) cands.push_back(LaunchCfg{bs, ept});
@@ -1263,6 +1359,15 @@ wf_status autotune_launches(wf_domain *d) {
   CUDA_TRY(cudaMemcpyAsync(M.cf, s_cf, 4 * n_cf, cudaMemcpyDeviceToDevice, d->stream));
   CUDA_TRY(cudaStreamSynchronize(d->stream));
   CUDA_TRY(cudaFree(save));
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    TuneResult r;
+    for (int k = 0; k < 3; k++) {
+      r.cfg[k] = d->cfg[k];
+      r.ms[k] = d->cfg_ms[k];
+    }
+    g_tune_cache[tune_key(d)] = r;
+  }
   return WF_OK;
 }
 
@@ -1283,10 +1388,7 @@ WF_API wf_status wf_set_launch_config(wf_domain *d, int32_t phase, int32_t block
   if (items_per_thread < 0) return fail(d, WF_ERR_ARG, "items per thread must be >= 0");
   d->cfg[phase] = LaunchCfg{block, items_per_thread};
   d->cfg_ms[phase] = 0.0;
-  if (d->graph) {
-    cudaGraphExecDestroy(d->graph);
-    d->graph = nullptr;
-  }
+  drop_graphs(d);
   return WF_OK;
 }
 
@@ -1304,10 +1406,18 @@ bool cluster_mode(const wf_domain *d) {
     return false;
   return d->step_mode == 2 || (d->step_mode == 0 && d->ne <= kClusterAutoElems);
 }
+// Whether the automatic mode picks the tiled kernels for tiled meshes.
+constexpr bool kTiledAuto = false;
+// Whether the steps of d run as tiled element + assembly kernels.
+bool tiled_mode(const wf_domain *d) {
+  if (d->precision != WF_MIXED || !d->tiled) return false;
+  return d->step_mode == 3 || (kTiledAuto && d->step_mode == 0 && !cluster_mode(d));
+}
 }  // namespace
 
 WF_API wf_status wf_set_step_mode(wf_domain *d, int32_t mode) {
-  if (!d || mode < 0 || mode > 2) return WF_ERR_ARG;
+  if (!d || mode < 0 || mode > 3) return WF_ERR_ARG;
+  if (mode != d->step_mode) drop_graphs(d);   // the graphs hold the other kernels
   d->step_mode = mode;
   return WF_OK;
 }
@@ -1316,9 +1426,28 @@ WF_API wf_status wf_get_step_mode(const wf_domain *d, int32_t *mode, int32_t *bl
                                   int32_t *block_size) {
   if (!d) return WF_ERR_ARG;
   const bool c = d->initialized && cluster_mode(d);
-  if (mode) *mode = c ? 2 : 1;
-  if (blocks) *blocks = c ? d->cl_blocks : 0;
-  if (block_size) *block_size = c ? d->cl_bs : 0;
+  const bool t = d->initialized && !c && tiled_mode(d);
+  if (mode) *mode = c ? 2 : (t ? 3 : 1);
+  if (blocks) *blocks = c ? d->cl_blocks : (t ? d->T.ntiles : 0);
+  if (block_size) *block_size = c ? d->cl_bs : (t ? kTileElems : 0);
+  return WF_OK;
+}
+
+WF_API wf_status wf_get_tiles(const wf_domain *d, int32_t *ntiles, int32_t *nshared,
+                              int64_t *tile_nodes, int64_t *shared_slots, char *why,
+                              int64_t why_cap) {
+  if (!d) return WF_ERR_ARG;
+  if (!d->initialized) return fail(const_cast<wf_domain *>(d), WF_ERR_STATE, "wf_init not called");
+  if (ntiles) *ntiles = d->tiled ? d->T.ntiles : 0;
+  if (nshared) *nshared = d->tiled ? d->T.nshared : 0;
+  if (tile_nodes) *tile_nodes = d->tiled ? d->T.tile_nodes : 0;
+  if (shared_slots) *shared_slots = d->tiled ? d->T.shared_slots : 0;
+  if (why && why_cap > 0) {
+    const std::string &w = d->tiled ? std::string() : d->tile_why;
+    const size_t n = std::min<size_t>(w.size(), (size_t)why_cap - 1);
+    std::memcpy(why, w.data(), n);
+    why[n] = '\0';
+  }
   return WF_OK;
 }
 
@@ -1569,6 +1698,11 @@ WF_API wf_status wf_init(wf_domain *d) {
   if (d->nspec) CUDA_TRY(dalloc(d, &P.hist_spec, (size_t)d->hist_cap * d->nspec));
   P.hist_cap = d->hist_cap;
   CUDA_TRY(dalloc(d, &P.st, 1));
+  CUDA_TRY(cudaMallocHost(&d->st_host, sizeof(StepState)));
+  *d->st_host = StepState{};
+  d->st_host->first_bad_node = LLONG_MAX;
+  CUDA_TRY(cudaMemcpyAsync(&P.st->first_bad_node, &d->st_host->first_bad_node, sizeof(long long),
+                           cudaMemcpyHostToDevice, d->stream));
   if (d->energy) {
     P.energy_on = 1;
     CUDA_TRY(dalloc(d, &P.epart, 2 * (size_t)energy_grid(P)));
@@ -1725,6 +1859,22 @@ WF_API wf_status wf_init(wf_domain *d) {
     mix_init(P, M, S, d->stream);
     CUDA_TRY(cudaGetLastError());
     d->mix_valid_fp64 = true;
+    // element tiles of the tiled step (hexahedra; the kernels leave out
+    // specimens, thermal coupling, the energy history and triangle-mesh dies)
+    d->tiled = false;
+    d->tile_why.clear();
+    if (d->npe != 8) d->tile_why = "tetrahedra";
+    else if (d->nspec) d->tile_why = "specimens";
+    else if (P.thermal) d->tile_why = "thermal coupling";
+    else if (P.energy_on) d->tile_why = "energy history";
+    else if (P.tri_on) d->tile_why = "triangle-mesh contact";
+    if (d->tile_why.empty()) {
+      double bb[6];
+      host_bbox(d, bb);
+      CUDA_TRY(build_tiles(P.elnod, S.x, np, ne, nn, P.off, bb, kSharedThreads, keep_alloc, d,
+                           d->stream, d->T, d->tile_why));
+      d->tiled = d->tile_why.empty();
+    }
     if (d->autotune) {
       wf_status ts = autotune_launches(d);
       if (ts) return ts;
@@ -1753,6 +1903,7 @@ WF_API wf_status wf_init(wf_domain *d) {
   d->host_step = 0;
   d->host_time = 0.0;
   d->launches = 0;
+  d->graph_launches = 0;
   return WF_OK;
 }
 
@@ -1766,6 +1917,11 @@ void launch_step(wf_domain *d) {
     fp64_nodal(P, d->S, d->stream, 0);
     fp64_elements(P, d->S, d->stream);
     fp64_nodes(P, d->S, d->stream, d->node_grid);
+  } else if (tiled_mode(d)) {
+    mix_geometry(P, d->M, d->mvol, d->stream, d->cfg[0]);
+    mix_nodal(P, d->M, d->mvol, d->stream, d->cfg[1]);
+    mix_tile(P, d->M, d->T, d->stream);
+    mix_shared(P, d->M, d->T, d->stream);
   } else {
     mix_geometry(P, d->M, d->mvol, d->stream, d->cfg[0]);
     mix_nodal(P, d->M, d->mvol, d->stream, d->cfg[1]);
@@ -1793,13 +1949,16 @@ void launch_step_timed(wf_domain *d, cudaEvent_t *ev) {
     cudaEventRecord(ev[3], d->stream);
     fp64_nodes(P, d->S, d->stream, d->node_grid);
   } else {
+    const bool tl = tiled_mode(d);
     mix_geometry(P, d->M, d->mvol, d->stream, d->cfg[0]);
     cudaEventRecord(ev[1], d->stream);
     mix_nodal(P, d->M, d->mvol, d->stream, d->cfg[1]);
     cudaEventRecord(ev[2], d->stream);
-    mix_elements(P, d->M, d->mvol, d->stream, d->cfg[2]);
+    if (tl) mix_tile(P, d->M, d->T, d->stream);
+    else mix_elements(P, d->M, d->mvol, d->stream, d->cfg[2]);
     cudaEventRecord(ev[3], d->stream);
-    mix_nodes(P, d->M, d->stream, d->node_grid);
+    if (tl) mix_shared(P, d->M, d->T, d->stream);
+    else mix_nodes(P, d->M, d->stream, d->node_grid);
   }
   if (P.nspec) spec_reaction(P, d->stream);
   if (P.energy_on) {
@@ -1838,17 +1997,25 @@ void set_dt_constants(StepParams &P, double dt) {
 
 constexpr int kGraphSteps = 32;
 
-wf_status ensure_graph(wf_domain *d) {
-  if (d->graph) return WF_OK;
+// The graph of `steps` consecutive steps (captured and instantiated on first
+// use; kept until the launch parameters change).
+wf_status ensure_graph(wf_domain *d, int64_t steps, cudaGraphExec_t *out) {
+  auto it = d->graphs.find(steps);
+  if (it != d->graphs.end()) {
+    *out = it->second;
+    return WF_OK;
+  }
   cudaGraph_t g = nullptr;
   CUDA_TRY(cudaStreamBeginCapture(d->stream, cudaStreamCaptureModeThreadLocal));
-  for (int i = 0; i < kGraphSteps; i++) launch_step(d);
+  for (int64_t i = 0; i < steps; i++) launch_step(d);
   cudaError_t e = cudaStreamEndCapture(d->stream, &g);
   if (e != cudaSuccess) return fail(d, WF_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
-  e = cudaGraphInstantiate(&d->graph, g, 0);
+  cudaGraphExec_t x = nullptr;
+  e = cudaGraphInstantiate(&x, g, 0);
   cudaGraphDestroy(g);
   if (e != cudaSuccess) return fail(d, WF_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
-  d->graph_steps = kGraphSteps;
+  d->graphs[steps] = x;
+  *out = x;
   return WF_OK;
 }
 
@@ -1882,10 +2049,7 @@ wf_status grow_history(wf_domain *d, int64_t total) {
     }
     d->P.hist_cap = cap;
     d->hist_cap = cap;
-    if (d->graph) {
-      cudaGraphExecDestroy(d->graph);
-      d->graph = nullptr;
-    }
+    drop_graphs(d);
   }
   return WF_OK;
 }
@@ -1928,6 +2092,9 @@ WF_API wf_status wf_run(wf_domain *d, int64_t nsteps) {
     }
     left = 0;
   }
+  if (d->step_mode == 3 && !tiled_mode(d))
+    return fail(d, WF_ERR_UNSUPPORTED, "tiled steps need mixed precision and a mesh the tiles "
+                                       "cover (%s)", d->tile_why.c_str());
   if (d->step_mode == 2 && !cluster_mode(d))
     return fail(d, WF_ERR_UNSUPPORTED,
                 "the cluster run needs mixed precision, a mesh of at most %lld elements, and no "
@@ -1943,19 +2110,58 @@ WF_API wf_status wf_run(wf_domain *d, int64_t nsteps) {
     }
   }
   d->launches += (4 + (d->nspec ? 1 : 0) + (d->P.energy_on ? 1 : 0)) * left;
+  // graph replays: kGraphSteps at a time, then one graph of the remainder
   if (left >= kGraphSteps) {
-    wf_status s = ensure_graph(d);
+    cudaGraphExec_t g = nullptr;
+    wf_status s = ensure_graph(d, kGraphSteps, &g);
     if (s) return s;
     while (left >= kGraphSteps) {
-      CUDA_TRY(cudaGraphLaunch(d->graph, d->stream));
+      CUDA_TRY(cudaGraphLaunch(g, d->stream));
       left -= kGraphSteps;
+      d->graph_launches++;
     }
+  }
+  if (left > 1) {
+    cudaGraphExec_t g = nullptr;
+    wf_status s = ensure_graph(d, left, &g);
+    if (s) return s;
+    CUDA_TRY(cudaGraphLaunch(g, d->stream));
+    d->graph_launches++;
+    left = 0;
   }
   for (int64_t i = 0; i < left; i++) launch_step(d);
   CUDA_TRY(cudaGetLastError());
+  // the step state (its non-finite flag) for the next wf_sync to check
+  CUDA_TRY(cudaMemcpyAsync(d->st_host, d->P.st, sizeof(StepState), cudaMemcpyDeviceToHost,
+                           d->stream));
+  d->st_pending = true;
   for (int64_t i = 0; i < nsteps; i++) d->host_time += d->dt;
   d->host_step += nsteps;
   d->mix_valid_fp64 = false;
+  return WF_OK;
+}
+
+WF_API wf_status wf_prepare_run(wf_domain *d, int64_t nsteps) {
+  if (!d || nsteps < 0) return WF_ERR_ARG;
+  if (!d->initialized) return fail(d, WF_ERR_STATE, "wf_init not called");
+  if (!(d->dt > 0.0) && !d->nspec) return fail(d, WF_ERR_STATE, "time step not set (SetDT)");
+  if (d->phase_timing || cluster_mode(d)) return WF_OK;   // these runs replay no graph
+  CUDA_TRY(cudaSetDevice(d->device));
+  {
+    const wf_status gs = grow_history(d, d->host_step + nsteps);
+    if (gs) return gs;
+  }
+  set_dt_constants(d->P, d->dt);
+  cudaGraphExec_t g = nullptr;
+  if (nsteps >= kGraphSteps) {
+    const wf_status s = ensure_graph(d, kGraphSteps, &g);
+    if (s) return s;
+  }
+  const int64_t rem = nsteps % kGraphSteps;
+  if (rem > 1) {
+    const wf_status s = ensure_graph(d, rem, &g);
+    if (s) return s;
+  }
   return WF_OK;
 }
 
@@ -1980,6 +2186,25 @@ WF_API wf_status wf_sync(wf_domain *d) {
   if (!d) return WF_ERR_ARG;
   CUDA_TRY(cudaSetDevice(d->device));
   CUDA_TRY(cudaStreamSynchronize(d->stream));
+  if (d->st_pending && d->st_host) {
+    // Solver_explicit.C:777-785 clears a non-finite internal force and
+    // prints it; here the node kernels clear it the same way and raise a
+    // flag, reported once by this call and then reset on the device
+    d->st_pending = false;
+    const StepState st = *d->st_host;
+    if (st.status & 1u) {
+      d->st_host->status = 0u;
+      d->st_host->first_bad_node = LLONG_MAX;
+      CUDA_TRY(cudaMemcpy(&d->P.st->status, &d->st_host->status,
+                          offsetof(StepState, first_bad_node) + sizeof(long long) -
+                              offsetof(StepState, status),
+                          cudaMemcpyHostToDevice));
+      return fail(d, WF_ERR_NONFINITE,
+                  "non-finite internal force cleared to zero (first at node %lld), in the "
+                  "steps up to step %lld",
+                  (long long)st.first_bad_node, (long long)st.step);
+    }
+  }
   return WF_OK;
 }
 
@@ -2233,6 +2458,12 @@ WF_API wf_status wf_get_phase_times(wf_domain *d, double ms[4], int64_t *steps, 
 WF_API wf_status wf_get_launch_count(const wf_domain *d, int64_t *n) {
   if (!d || !n) return WF_ERR_ARG;
   *n = d->launches;
+  return WF_OK;
+}
+
+WF_API wf_status wf_get_graph_launches(const wf_domain *d, int64_t *n) {
+  if (!d || !n) return WF_ERR_ARG;
+  *n = d->graph_launches;
   return WF_OK;
 }
 

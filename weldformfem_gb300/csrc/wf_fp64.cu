@@ -663,6 +663,7 @@ __global__ void __launch_bounds__(kNodeThreads) k_fp64_nodes(StepParams P, Fp64S
       if (!isfinite(fi[k])) {
         fi[k] = 0.0;
         atomicOr(&P.st->status, 1u);
+        atomicMin(&P.st->first_bad_node, (long long)n);
       }
       S.fi[k * np + n] = fi[k];
     }

@@ -42,7 +42,7 @@ struct StepState {
   long long step;     // steps completed since wf_init
   unsigned int done_blocks;  // last-block-done counter of the node kernel
   unsigned int status;       // bit 0: a non-finite internal force was cleared
-  long long first_bad_node;
+  long long first_bad_node;  // smallest node id whose force was cleared (LLONG_MAX: none)
   double eint;               // accumulated internal energy (energy history)
   unsigned int energy_blocks;  // last-block-done counter of the energy kernel
   unsigned int pad;
@@ -171,6 +171,30 @@ struct MixState {
   float *qc, *dte;
 };
 
+// Element tiles of the fused element + assembly step (mixed hexahedra). The
+// elements are binned by centroid into cubes of about 8 element sizes; each
+// bin is split into tiles of at most kTileElems elements in ascending element
+// order. A tile's nodes are staged in shared memory; a node is "interior" to
+// a tile when every element that holds it is in that tile, "shared" when it
+// is interior to no tile.
+constexpr int kTileElems = 512;    // elements per tile, one thread each
+constexpr int kTileNodes = 1024;   // distinct nodes per tile at most
+constexpr int kTileBinMax = 4096;  // elements per bin at most
+constexpr int kSharedThreads = 256;  // block size of the shared-node kernel
+struct TileParams {
+  int32_t ntiles;
+  int32_t nshared;
+  const int32_t *eoff;     // [ntiles + 1] tile boundaries in elems
+  const int32_t *elems;    // [ne] element ids, tile by tile, ascending within a tile
+  const uint16_t *lel;     // [8][ne] tile-local node index of corner a of elems[i]
+  const int32_t *ncount;   // [ntiles] distinct nodes of each tile
+  const int32_t *nodes;    // [ntiles][kTileNodes] node ids ascending; bit 31: shared
+  const int32_t *shared;   // [nshared] the shared nodes, ascending
+  double *partials;        // [ntiles + blocks of the shared-node kernel] reaction partials
+  int64_t tile_nodes;      // sum of ncount (host-side statistic)
+  int64_t shared_slots;    // node-list entries of the shared nodes (host-side statistic)
+};
+
 // Records `msg` as the domain's last error and returns s (wf_api.cu).
 wf_status domain_fail(wf_domain *d, wf_status s, const std::string &msg);
 
@@ -204,6 +228,11 @@ void mix_elements(const StepParams &P, const MixState &M, const float *vol, cuda
                   LaunchCfg c);
 void mix_nodes(const StepParams &P, const MixState &M, cudaStream_t st, int node_grid);
 void mix_predict(const StepParams &P, const MixState &M, cudaStream_t st);
+// Tiled step of hexahedra (replaces mix_elements + mix_nodes): the element
+// phase and interior-node assembly and update per tile, then the shared nodes.
+void mix_tile(const StepParams &P, const MixState &M, const TileParams &T, cudaStream_t st);
+void mix_shared(const StepParams &P, const MixState &M, const TileParams &T, cudaStream_t st);
+int mix_shared_grid(const TileParams &T);
 // Whole runs of steps in one launch of one cluster of `blocks` blocks of `bs`
 // threads (64, 128 or 256), for small meshes; mix_cluster_fits returns how
 // many such clusters can be resident (0: the shape cannot launch).
@@ -236,6 +265,19 @@ int64_t connectivity_scratch_ints(int64_t nn);
 cudaError_t build_connectivity(const int32_t *el_aos, int64_t ne, int npe, int64_t nn,
                                int32_t *el_soa, int32_t *off, int32_t *slot, int32_t *scratch,
                                cudaStream_t st);
+// Element tiles (TileParams) of a hexahedral mesh from the SoA connectivity,
+// the SoA FP64 coordinates and the node-list offsets, built on the device.
+// bbox = {min x, min y, min z, max x, max y, max z}. Device arrays that stay
+// with the domain come from `keep` (freed with it); temporaries are freed
+// before returning. Returns cudaSuccess and sets `why` (non-empty) when the
+// mesh does not tile (a bin or tile over its limits, or two elements of a
+// tile holding one node at the same corner).
+using DeviceAlloc = cudaError_t (*)(void *ctx, void **p, size_t bytes);
+cudaError_t build_tiles(const int32_t *el_soa, const double *x_soa, int64_t np, int64_t ne,
+                        int64_t nn, const int32_t *off, const double bbox[6], int shared_threads,
+                        DeviceAlloc keep, void *keep_ctx, cudaStream_t st, TileParams &T,
+                        std::string &why);
+
 // AoS [nn][3] -> SoA [3][np], zero padded
 void coords_soa(const double *x_aos, int64_t nn, int64_t np, double *out, cudaStream_t st);
 // SoA [3][np] -> AoS [nn][3]

@@ -506,39 +506,74 @@ __device__ __forceinline__ void thermal_rates(const StepParams &P, const MixStat
   }
 }
 
+// Where an element's node values come from. GlobalNodes: the node arrays in
+// HBM through the element's connectivity (per-phase kernels, cluster run);
+// TileNodes (below): a tile's node arrays staged in shared memory through
+// tile-local indices. Both return the same values, so an element computes
+// the same forces bit for bit from either.
+template <bool CG>
+struct GlobalNodes {
+  const float2 *xh;
+  const float *vp, *jr;
+  int64_t np;
+  int32_t nid[8];
+  __device__ __forceinline__ GlobalNodes(const StepParams &P, const MixState &M, int64_t e)
+      : xh(M.xh), vp(M.vp), jr(M.jr), np(P.np) {
+#pragma unroll
+    for (int a = 0; a < 8; a++) nid[a] = __ldg(&P.elnod[a * P.ne + e]);
+  }
+  __device__ __forceinline__ float2 x(int a, int k) const { return ldx<CG>(&xh[k * np + nid[a]]); }
+  __device__ __forceinline__ float v(int a, int k) const { return ldx<CG>(&vp[k * np + nid[a]]); }
+  __device__ __forceinline__ float j(int a) const { return ldx<CG>(&jr[nid[a]]); }
+};
+
+// Element forces to HBM, SoA by (local node, component): fe[(a * 3 + k) * ne + e].
+struct ForcesToHbm {
+  float *fe;
+  int64_t ne, e;
+  __device__ __forceinline__ void put(int a, int k, float f) { fe[(a * 3 + k) * ne + e] = f; }
+};
+
 // Hexahedron: with dN_a/dx = (1/8) adj(J)^T-row . s(a) / detJ at the centre,
 // the velocity gradient is adj(J) G / (8 detJ) with G the Walsh sums of the
 // nodal velocities, and the nodal forces are the synthesis of
 // T = adj(J)^T sigma (w / 8 = 1) plus the hourglass coefficients ch h_j.
 // Same quantities as the reference's per-node loops, fewer operations.
-template <int LAW, bool CG, bool TH>
-__device__ __forceinline__ void element_hex(const StepParams &P, const MixState &M, int64_t e,
-                                            float *stash, int stride, long long step) {
-  const int64_t ne = P.ne, np = P.np;
-  int32_t nid[8];
+// EARLY_JR: gather the nodes' volume ratios with the positions, so that their
+// loads are in flight during the Jacobian arithmetic (the cluster run, one
+// element per thread, gathers them later: early it spills there).
+template <int LAW, bool EARLY_JR, bool TH, class Nodes, class Out>
+__device__ __forceinline__ void element_hex_core(const StepParams &P, const MixState &M,
+                                                 int64_t e, const Nodes &nd, float *stash,
+                                                 int stride, long long step, Out &out) {
   float A[3][3], detJ;
-  // mean volume ratio of the nodes; the per-phase kernel gathers it with the
-  // positions so that its loads are in flight during the Jacobian arithmetic
-  // (the cluster run, one element per thread, gathers it later: early it
-  // spills there)
   float J_avg = 0.f;
   {
+    // coordinates relative to node 0, from the (hi, lo) pairs
     float r[8][3];
-    rel_coords<8, CG>(P, M, e, r, nid);
-    if constexpr (!CG) {
+    float2 o[3];
 #pragma unroll
-      for (int a = 0; a < 8; a++) J_avg += ldx<CG>(&M.jr[nid[a]]);
+    for (int k = 0; k < 3; k++) o[k] = nd.x(0, k);
+#pragma unroll
+    for (int k = 0; k < 3; k++) r[0][k] = 0.0f;
+#pragma unroll
+    for (int a = 1; a < 8; a++)
+#pragma unroll
+      for (int k = 0; k < 3; k++) r[a][k] = pair_rel(nd.x(a, k), o[k]);
+    if constexpr (EARLY_JR) {
+#pragma unroll
+      for (int a = 0; a < 8; a++) J_avg += nd.j(a);
     }
     float J[3][3];
 #pragma unroll
     for (int k = 0; k < 3; k++) {
-      float v[8], o[8];
+      float v[8], o8[8];
 #pragma unroll
       for (int a = 0; a < 8; a++) v[a] = r[a][k];
-      walsh8(v, o);
-      J[0][k] = 0.125f * o[1];
-      J[1][k] = 0.125f * o[2];
-      J[2][k] = 0.125f * o[3];
+      walsh8(v, o8);
+      J[0][k] = 0.125f * o8[1];
+      J[1][k] = 0.125f * o8[2];
+      J[2][k] = 0.125f * o8[3];
     }
     A[0][0] = (J[1][1] * J[2][2] - J[1][2] * J[2][1]);
     A[1][0] = -(J[1][0] * J[2][2] - J[1][2] * J[2][0]);
@@ -559,7 +594,7 @@ __device__ __forceinline__ void element_hex(const StepParams &P, const MixState 
   for (int k = 0; k < 3; k++) {
     float v[8], o[8];
 #pragma unroll
-    for (int a = 0; a < 8; a++) v[a] = ldx<CG>(&M.vp[k * np + nid[a]]);
+    for (int a = 0; a < 8; a++) v[a] = nd.v(a, k);
     walsh8(v, o);
     G[0][k] = o[1];
     G[1][k] = o[2];
@@ -576,9 +611,9 @@ __device__ __forceinline__ void element_hex(const StepParams &P, const MixState 
 #pragma unroll
       for (int j = 0; j < 4; j++) stash[(k * 4 + j) * stride] = ch * hm[k][j];
   }
-  if constexpr (CG) {
+  if constexpr (!EARLY_JR) {
 #pragma unroll
-    for (int a = 0; a < 8; a++) J_avg += ldx<CG>(&M.jr[nid[a]]);
+    for (int a = 0; a < 8; a++) J_avg += nd.j(a);
   }
   // velocity gradient L[i][k] = d v_k / d x_i
   const float fl = 0.125f / detJ;
@@ -593,7 +628,7 @@ __device__ __forceinline__ void element_hex(const StepParams &P, const MixState 
   const float w12 = 0.5f * (L[2][1] - L[1][2]);
   const float w02 = 0.5f * (L[2][0] - L[0][2]);
   float jTh = m.jc_Th;
-  if constexpr (TH) thermal_pre<8, CG>(P, M, m, nid, step, sr, jTh);
+  if constexpr (TH) thermal_pre<8, !EARLY_JR>(P, M, m, nd.nid, step, sr, jTh);
   float J_bar = J_avg * 0.125f;
   if (J_bar < 0.0f) J_bar = 0.2f;
   const float p = -m.K * (J_bar - 1.0f);
@@ -611,16 +646,16 @@ __device__ __forceinline__ void element_hex(const StepParams &P, const MixState 
 #pragma unroll
     for (int j = 0; j < 4; j++) o[4 + j] = stash[(k * 4 + j) * stride];
     walsh8_synth(o, f);
-    // SoA by (local node, component): fe[(a * 3 + k) * ne + e]
 #pragma unroll
-    for (int a = 0; a < 8; a++) M.fe[(a * 3 + k) * ne + e] = f[a];
+    for (int a = 0; a < 8; a++) out.put(a, k, f[a]);
   }
   if constexpr (TH) {
     // conduction in the same Walsh form: grad T detJ = A (Walsh sums of T) / 8,
     // (K T)_a = k_T / detJ * synthesis of A^T grad T detJ (w = 8 cancels 1/8)
+    constexpr bool CG = !EARLY_JR;
     float tv[8], oT[8], KT[8];
 #pragma unroll
-    for (int a = 0; a < 8; a++) tv[a] = ldx<CG>(&M.T[nid[a]]).x;
+    for (int a = 0; a < 8; a++) tv[a] = ldx<CG>(&M.T[nd.nid[a]]).x;
     walsh8(tv, oT);
     float BT[3];
 #pragma unroll
@@ -630,8 +665,17 @@ __device__ __forceinline__ void element_hex(const StepParams &P, const MixState 
 #pragma unroll
     for (int mm = 0; mm < 3; mm++) o[1 + mm] = A[0][mm] * BT[0] + A[1][mm] * BT[1] + A[2][mm] * BT[2];
     walsh8_synth(o, KT);
-    thermal_rates<8, CG>(P, M, m, e, nid, step, KT, m.k_T / detJ, qpl * vol);
+    thermal_rates<8, CG>(P, M, m, e, nd.nid, step, KT, m.k_T / detJ, qpl * vol);
   }
+}
+
+// Per-phase kernels and the cluster run: node values from HBM, forces to HBM.
+template <int LAW, bool CG, bool TH>
+__device__ __forceinline__ void element_hex(const StepParams &P, const MixState &M, int64_t e,
+                                            float *stash, int stride, long long step) {
+  const GlobalNodes<CG> nd(P, M, e);
+  ForcesToHbm out{M.fe, P.ne, e};
+  element_hex_core<LAW, !CG, TH>(P, M, e, nd, stash, stride, step, out);
 }
 
 // Tetrahedron: per-node shape derivatives (Domain_d.C:1866-1887).
@@ -777,58 +821,33 @@ __device__ __forceinline__ double block_sum_dense(double v, double *sh) {
   return t;
 }
 
-// Node update of one node: gather of the element forces in list order,
-// accelerations, velocity BCs, Chung-Hulbert corrector and the next
-// predictor. Returns the node's reaction contribution.
+// Update of one node from its assembled internal force fi (the element forces
+// summed in list order): non-finite check, accelerations, velocity BCs,
+// Chung-Hulbert corrector and the next predictor. x and vp are the node's
+// position pair and predicted velocity (read by the caller from HBM or from
+// a tile's staged copy). Returns the node's reaction contribution.
 template <int NPE, bool CG>
-__device__ __forceinline__ float node_one(const StepParams &P, const MixState &M, int64_t n,
-                                          long long step) {
+__device__ __forceinline__ float node_finish(const StepParams &P, const MixState &M, int64_t n,
+                                             long long step, float fi0, float fi1, float fi2,
+                                             float2 (&x)[3], const float (&vp)[3]) {
   float r = 0.0f;
   const int64_t np = P.np;
-  const int32_t b = __ldg(&P.off[n]), c = __ldg(&P.off[n + 1]) - b;
   const int64_t ne = P.ne;
-  // gather over the node's element list in list order, eight entries at a
-  // time so that the slot and force loads of a chunk are all in flight
-  float fi0 = 0.f, fi1 = 0.f, fi2 = 0.f;
-  for (int32_t k0 = 0; k0 < c; k0 += 8) {
-    int32_t sl[8];
-#pragma unroll
-    for (int j = 0; j < 8; j++) sl[j] = (k0 + j < c) ? __ldg(&P.slot[b + k0 + j]) : -1;
-    float g0[8], g1[8], g2[8];
-#pragma unroll
-    for (int j = 0; j < 8; j++) {
-      g0[j] = g1[j] = g2[j] = 0.f;
-      if (sl[j] >= 0) {
-        const int64_t base = (int64_t)(sl[j] % NPE) * 3 * ne + sl[j] / NPE;
-        g0[j] = ldx<CG>(&M.fe[base]);
-        g1[j] = ldx<CG>(&M.fe[base + ne]);
-        g2[j] = ldx<CG>(&M.fe[base + 2 * ne]);
-      }
-    }
-#pragma unroll
-    for (int j = 0; j < 8; j++) {
-      fi0 += g0[j];
-      fi1 += g1[j];
-      fi2 += g2[j];
-    }
-  }
   float fi[3] = {fi0, fi1, fi2};
 #pragma unroll
   for (int k = 0; k < 3; k++)
     if (!isfinite(fi[k])) {
       fi[k] = 0.f;
       atomicOr(&P.st->status, 1u);
+      atomicMin(&P.st->first_bad_node, (long long)n);
     }
   const uint8_t fl = P.nflag[n];
   const float mass = M.mass[n];
   const float inv_m = 1.0f / mass;
-  float2 x[3];
-  float vold[3], vp[3], pa[3];
+  float vold[3], pa[3];
 #pragma unroll
   for (int k = 0; k < 3; k++) {
-    x[k] = M.xh[k * np + n];
     vold[k] = M.v[k * np + n];
-    vp[k] = M.vp[k * np + n];
     pa[k] = M.pa[k * np + n];
   }
   float cf[3] = {0.f, 0.f, 0.f};
@@ -876,10 +895,54 @@ __device__ __forceinline__ float node_one(const StepParams &P, const MixState &M
     // the die heat over m cp of material 0
     const float *cur = M.dte + (step & 1) * ne * NPE;
     float sT = 0.f;
+    const int32_t b = __ldg(&P.off[n]), c = __ldg(&P.off[n + 1]) - b;
     for (int32_t k = 0; k < c; k++) sT += ldx<CG>(&cur[__ldg(&P.slot[b + k])]);
     M.T[n] = pair_add(M.T[n], (sT + M.qc[n] / (mass * P.f_cp0)) * c_dt);
   }
   return r;
+}
+
+// Node update of one node: gather of the element forces in list order, then
+// node_finish. Returns the node's reaction contribution.
+template <int NPE, bool CG>
+__device__ __forceinline__ float node_one(const StepParams &P, const MixState &M, int64_t n,
+                                          long long step) {
+  const int32_t b = __ldg(&P.off[n]), c = __ldg(&P.off[n + 1]) - b;
+  const int64_t ne = P.ne;
+  // gather over the node's element list in list order, eight entries at a
+  // time so that the slot and force loads of a chunk are all in flight
+  float fi0 = 0.f, fi1 = 0.f, fi2 = 0.f;
+  for (int32_t k0 = 0; k0 < c; k0 += 8) {
+    int32_t sl[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) sl[j] = (k0 + j < c) ? __ldg(&P.slot[b + k0 + j]) : -1;
+    float g0[8], g1[8], g2[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      g0[j] = g1[j] = g2[j] = 0.f;
+      if (sl[j] >= 0) {
+        const int64_t base = (int64_t)(sl[j] % NPE) * 3 * ne + sl[j] / NPE;
+        g0[j] = ldx<CG>(&M.fe[base]);
+        g1[j] = ldx<CG>(&M.fe[base + ne]);
+        g2[j] = ldx<CG>(&M.fe[base + 2 * ne]);
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      fi0 += g0[j];
+      fi1 += g1[j];
+      fi2 += g2[j];
+    }
+  }
+  const int64_t np = P.np;
+  float2 x[3];
+  float vp[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    x[k] = M.xh[k * np + n];
+    vp[k] = M.vp[k * np + n];
+  }
+  return node_finish<NPE, CG>(P, M, n, step, fi0, fi1, fi2, x, vp);
 }
 
 template <int NPE>
@@ -914,6 +977,165 @@ __global__ void __launch_bounds__(kNodeThreads, WF_NODE_MIN_BLOCKS) k_mix_nodes(
       P.st->done_blocks = 0u;
     }
     if (P.tri_on) tri_move<true>(P, time);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Tiled step for hexahedra: element phase and assembly of a tile in one block.
+//
+// One block per tile (TileParams, built at init), one thread per element. The
+// tile's node positions, predicted velocities and volume ratios are staged in
+// shared memory once; each element computes its forces from the staged copy
+// (the per-phase element arithmetic, so the same forces bit for bit) and
+// keeps them in registers. The block then sums them into per-node
+// accumulators in shared memory in eight passes, one per corner, in the
+// corner order 6, 7, 5, 4, 2, 3, 1, 0: for the AddBoxLength numbering that is
+// the element-ascending order of every node's list, so an interior node's
+// force is the per-phase gather's sum bit for bit (two elements of a tile
+// never hold one node at the same corner: checked at init). Interior nodes
+// (all their elements in the tile) are then updated by the block; a corner
+// force whose node is shared goes to HBM for the shared-node kernel, which
+// gathers it in list order. The element-force round trip through HBM is left
+// only for shared nodes.
+
+// A tile's staged node values through tile-local indices.
+struct TileNodes {
+  const float2 *sx;
+  const float *svp, *sjr;
+  int32_t loc[8];
+  __device__ __forceinline__ float2 x(int a, int k) const { return sx[k * kTileNodes + loc[a]]; }
+  __device__ __forceinline__ float v(int a, int k) const { return svp[k * kTileNodes + loc[a]]; }
+  __device__ __forceinline__ float j(int a) const { return sjr[loc[a]]; }
+};
+
+// Element forces kept in registers (all indices compile-time after unrolling).
+struct ForcesToRegs {
+  float (&f)[8][3];
+  __device__ __forceinline__ void put(int a, int k, float v) { f[a][k] = v; }
+};
+
+// Dynamic shared memory of the tile kernel: staged positions (hi, lo),
+// predicted velocities, volume ratios, force accumulators, node ids, and the
+// hourglass stash of each thread.
+constexpr size_t kTileSmem = sizeof(float2) * 3 * kTileNodes + sizeof(float) * 3 * kTileNodes +
+                             sizeof(float) * kTileNodes + sizeof(float) * 3 * kTileNodes +
+                             sizeof(int32_t) * kTileNodes + sizeof(float) * 12 * kTileElems;
+
+template <int LAW>
+__global__ void __launch_bounds__(kTileElems, 2) k_mix_tile(StepParams P, MixState M,
+                                                            TileParams T) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  float2 *sx = reinterpret_cast<float2 *>(smem);
+  float *svp = reinterpret_cast<float *>(sx + 3 * kTileNodes);
+  float *sjr = svp + 3 * kTileNodes;
+  float *acc = sjr + kTileNodes;
+  int32_t *sid = reinterpret_cast<int32_t *>(acc + 3 * kTileNodes);
+  float *stash = reinterpret_cast<float *>(sid + kTileNodes);
+  __shared__ double sh[kTileElems / 32];
+  const int t = blockIdx.x, tid = threadIdx.x;
+  const int64_t np = P.np, ne = P.ne;
+  const int nt = __ldg(&T.ncount[t]);
+  const int32_t *tn = T.nodes + (int64_t)t * kTileNodes;
+  const long long step = P.st->step;
+  for (int i = tid; i < nt; i += kTileElems) {
+    const int32_t id = __ldg(&tn[i]);
+    const int64_t n = id & 0x7fffffff;
+    sid[i] = id;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      sx[k * kTileNodes + i] = __ldg(&M.xh[k * np + n]);
+      svp[k * kTileNodes + i] = __ldg(&M.vp[k * np + n]);
+      acc[k * kTileNodes + i] = 0.0f;
+    }
+    sjr[i] = __ldg(&M.jr[n]);
+  }
+  __syncthreads();
+  const int32_t e0 = __ldg(&T.eoff[t]);
+  const bool act = tid < __ldg(&T.eoff[t + 1]) - e0;
+  float f[8][3];
+  TileNodes nd{sx, svp, sjr, {0, 0, 0, 0, 0, 0, 0, 0}};
+  if (act) {
+    const int64_t pos = e0 + tid;
+    const int64_t e = __ldg(&T.elems[pos]);
+#pragma unroll
+    for (int a = 0; a < 8; a++) nd.loc[a] = __ldg(&T.lel[a * ne + pos]);
+    ForcesToRegs out{f};
+    element_hex_core<LAW, true, false>(P, M, e, nd, &stash[tid], kTileElems, step, out);
+    // corner forces of shared nodes: to HBM, for the shared-node gather
+#pragma unroll
+    for (int a = 0; a < 8; a++)
+      if (sid[nd.loc[a]] < 0) {
+#pragma unroll
+        for (int k = 0; k < 3; k++) M.fe[(a * 3 + k) * ne + e] = f[a][k];
+      }
+  }
+  // corner passes: no two elements of the tile write one accumulator in a pass
+  constexpr int kOrder[8] = {6, 7, 5, 4, 2, 3, 1, 0};
+#pragma unroll
+  for (int q = 0; q < 8; q++) {
+    __syncthreads();
+    if (act) {
+      const int a = kOrder[q];
+      const int l = nd.loc[a];
+#pragma unroll
+      for (int k = 0; k < 3; k++) acc[k * kTileNodes + l] += f[a][k];
+    }
+  }
+  __syncthreads();
+  // interior nodes: the node update with the tile's sums
+  double r = 0.0;
+  for (int i = tid; i < nt; i += kTileElems) {
+    const int32_t id = sid[i];
+    if (id >= 0) {
+      float2 x[3];
+      float vp[3];
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        x[k] = sx[k * kTileNodes + i];
+        vp[k] = svp[k * kTileNodes + i];
+      }
+      r += (double)node_finish<8, false>(P, M, id, step, acc[i], acc[kTileNodes + i],
+                                         acc[2 * kTileNodes + i], x, vp);
+    }
+  }
+  const double bsum = block_sum_dense(r, sh);
+  if (tid == 0) T.partials[t] = bsum;
+}
+
+// The shared nodes: list-order gather from HBM and node update; the last
+// block adds the reaction partials of the tiles and of its own blocks in a
+// fixed order and advances the step state.
+__global__ void __launch_bounds__(kNodeThreads, WF_NODE_MIN_BLOCKS) k_mix_shared(StepParams P,
+                                                                              MixState M,
+                                                                              TileParams T) {
+  __shared__ double sh[kNodeThreads / 32];
+  __shared__ bool am_last;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const float r = (i < T.nshared) ? node_one<8, false>(P, M, __ldg(&T.shared[i]), P.st->step)
+                                  : 0.0f;
+  const double bs = block_sum_sparse(r, sh);
+  if (threadIdx.x == 0) {
+    T.partials[T.ntiles + blockIdx.x] = bs;
+    __threadfence();
+    const unsigned prev = atomicAdd(&P.st->done_blocks, 1u);
+    am_last = (prev == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (am_last) {
+    __threadfence();
+    const double time = P.st->time;
+    double t = 0.0;
+    const int64_t np_all = (int64_t)T.ntiles + gridDim.x;
+    for (int64_t j = threadIdx.x; j < np_all; j += blockDim.x)
+      t += ((volatile double *)T.partials)[j];
+    const double tot = block_sum_dense(t, sh);
+    if (threadIdx.x == 0) {
+      const long long s = P.st->step;
+      if (s < P.hist_cap) P.hist[s] = tot;
+      P.st->step = s + 1;
+      P.st->time = time + P.dt;
+      P.st->done_blocks = 0u;
+    }
   }
 }
 
@@ -1256,6 +1478,32 @@ void mix_nodes(const StepParams &P, const MixState &M, cudaStream_t st, int node
     k_mix_nodes<8><<<node_grid, kNodeThreads, 0, st>>>(P, M);
   else
     k_mix_nodes<4><<<node_grid, kNodeThreads, 0, st>>>(P, M);
+}
+
+static_assert(kSharedThreads == kNodeThreads, "the shared-node kernel runs node-kernel blocks");
+int mix_shared_grid(const TileParams &T) {
+  return std::max(1, (int)grid_for(T.nshared, kNodeThreads));
+}
+
+void mix_tile(const StepParams &P, const MixState &M, const TileParams &T, cudaStream_t st) {
+  auto kern = P.mat_general ? k_mix_tile<1> : k_mix_tile<0>;
+  static std::mutex mu;
+  static std::map<std::pair<const void *, int>, bool> set;   // (kernel, device)
+  int dev = 0;
+  cudaGetDevice(&dev);
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    bool &done = set[std::make_pair((const void *)kern, dev)];
+    if (!done) {
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmem);
+      done = true;
+    }
+  }
+  kern<<<(unsigned)T.ntiles, kTileElems, kTileSmem, st>>>(P, M, T);
+}
+
+void mix_shared(const StepParams &P, const MixState &M, const TileParams &T, cudaStream_t st) {
+  k_mix_shared<<<(unsigned)mix_shared_grid(T), kNodeThreads, 0, st>>>(P, M, T);
 }
 
 int mix_cluster_fits(const StepParams &P, const MixState &M, float *vol, int blocks, int bs) {

@@ -17,6 +17,7 @@
 // every element slot a call reads is written by that same call first, so
 // nothing needs clearing. Calls whose kernels overlap on the GPU (different
 // streams, or host threads without ordering) race on the array.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -30,10 +31,44 @@ constexpr int kThreads = 256;
 // Element volumes of the most recent call (file-scope: no allocation).
 static __device__ __align__(256) double g_vol_scratch[WF_NOALLOC_MAX_ELEMS];
 
-// Device address of g_vol_scratch per device, resolved once per device.
+// Device address of g_vol_scratch per device, with the id of the CUDA context
+// it was resolved in: resolved once per device, and again only when the
+// device's context has changed (after a cudaDeviceReset the old address
+// belongs to a destroyed context).
 constexpr int kMaxDevices = 64;
-double *g_scratch_addr[kMaxDevices] = {nullptr};
+struct ScratchAddr {
+  double *ptr = nullptr;
+  unsigned long long ctx_id = 0;
+};
+ScratchAddr g_scratch_addr[kMaxDevices];
 std::mutex g_scratch_mu;
+
+// cuCtxGetCurrent / cuCtxGetId through the runtime's driver entry points (no
+// link against the driver library).
+using CtxGetCurrentFn = CUresult(CUDAAPI *)(CUcontext *);
+using CtxGetIdFn = CUresult(CUDAAPI *)(CUcontext, unsigned long long *);
+
+// Id of the calling thread's current context; 0 when there is none yet.
+cudaError_t current_context_id(unsigned long long *id) {
+  static CtxGetCurrentFn get_current = nullptr;
+  static CtxGetIdFn get_id = nullptr;
+  if (!get_current || !get_id) {
+    void *f1 = nullptr, *f2 = nullptr;
+    cudaDriverEntryPointQueryResult q1, q2;
+    cudaError_t e = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000,
+                                                     cudaEnableDefault, &q1);
+    if (e != cudaSuccess || q1 != cudaDriverEntryPointSuccess) return cudaErrorNotSupported;
+    e = cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2);
+    if (e != cudaSuccess || q2 != cudaDriverEntryPointSuccess) return cudaErrorNotSupported;
+    get_current = reinterpret_cast<CtxGetCurrentFn>(f1);
+    get_id = reinterpret_cast<CtxGetIdFn>(f2);
+  }
+  CUcontext ctx = nullptr;
+  if (get_current(&ctx) != CUDA_SUCCESS) return cudaErrorDeviceUninitialized;
+  *id = 0;
+  if (ctx && get_id(ctx, id) != CUDA_SUCCESS) return cudaErrorDeviceUninitialized;
+  return cudaSuccess;
+}
 
 __device__ __forceinline__ double det3(const double J[3][3]) {
   return J[0][0] * J[1][1] * J[2][2] - J[0][0] * J[1][2] * J[2][1] -
@@ -94,21 +129,29 @@ __global__ void k_noalloc_nodal_vol(const int32_t *offset, const int32_t *count,
   voln[n] = s;
 }
 
-// Resolves the device address of the scratch array for the current device,
-// once per device.
+// Resolves the device address of the scratch array for the current device:
+// once per device, again when that device's context has changed.
 cudaError_t scratch_for_current_device(double **out) {
   int dev = -1;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
   std::lock_guard<std::mutex> lock(g_scratch_mu);
-  if (!g_scratch_addr[dev]) {
+  unsigned long long ctx = 0;
+  e = current_context_id(&ctx);
+  if (e != cudaSuccess) return e;
+  ScratchAddr &a = g_scratch_addr[dev];
+  if (!a.ptr || ctx == 0 || ctx != a.ctx_id) {
     void *p = nullptr;
+    // also makes the device's primary context current when none was yet
     e = cudaGetSymbolAddress(&p, g_vol_scratch);
     if (e != cudaSuccess) return e;
-    g_scratch_addr[dev] = static_cast<double *>(p);
+    e = current_context_id(&ctx);
+    if (e != cudaSuccess) return e;
+    a.ptr = static_cast<double *>(p);
+    a.ctx_id = ctx;
   }
-  *out = g_scratch_addr[dev];
+  *out = a.ptr;
   return cudaSuccess;
 }
 
@@ -124,9 +167,17 @@ WF_API wf_status wf_nodal_volumes_noalloc(const double *xyz, const int32_t *elno
   double *scratch = nullptr;
   if (scratch_for_current_device(&scratch) != cudaSuccess) return WF_ERR_CUDA;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
+  // a launch error of this call is reported and cleared; an error the
+  // calling thread already had pending is left pending for its owner
+  const cudaError_t before = cudaPeekAtLastError();
   k_noalloc_elem_vol<<<(unsigned)((ne + kThreads - 1) / kThreads), kThreads, 0, st>>>(
       xyz, elnod, ne, npe, scratch);
-  k_noalloc_nodal_vol<<<(unsigned)((nn + kThreads - 1) / kThreads), kThreads, 0, st>>>(
-      nodel_offset, nodel_count, nodel, nn, npe, scratch, voln);
-  return cudaGetLastError() == cudaSuccess ? WF_OK : WF_ERR_CUDA;
+  cudaError_t after = cudaPeekAtLastError();
+  if (after == before)
+    k_noalloc_nodal_vol<<<(unsigned)((nn + kThreads - 1) / kThreads), kThreads, 0, st>>>(
+        nodel_offset, nodel_count, nodel, nn, npe, scratch, voln);
+  after = cudaPeekAtLastError();
+  if (after == before) return WF_OK;
+  if (before == cudaSuccess) cudaGetLastError();
+  return WF_ERR_CUDA;
 }
