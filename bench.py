@@ -51,6 +51,10 @@ ALG_BYTES_HEX_MIXED = {"geometry": (36, 24), "nodal": (36, 20), "elements": (184
 # tetrahedra: 4 nodes per element (elnod 16, slots 16, forces 48 B per element)
 ALG_BYTES_TET_MIXED = {"geometry": (20, 24), "nodal": (20, 20), "elements": (120, 40),
                        "nodes": (64, 121)}
+# box meshes: corners and node lists computed in the kernels (no elnod, slots
+# or offsets read)
+ALG_BYTES_HEX_MIXED_BOX = {"geometry": (4, 24), "nodal": (4, 16), "elements": (152, 40),
+                           "nodes": (96, 117)}
 KERNEL_NAMES = {"geometry": "k_mix_geometry", "nodal": "k_mix_nodal",
                 "elements": "k_mix_elements", "nodes": "k_mix_nodes",
                 "tile": "k_mix_tile", "shared": "k_mix_shared"}
@@ -343,7 +347,9 @@ def run_ours(args):
 
     # ---- roofline of the dominant kernel -------------------------------------------------
     peak, peak_kind = measured_peak()
-    alg_table = ALG_BYTES_TET_MIXED if case.tritetra else ALG_BYTES_HEX_MIXED
+    box = dm.box() != (0, 0, 0)
+    alg_table = (ALG_BYTES_TET_MIXED if case.tritetra
+                 else ALG_BYTES_HEX_MIXED_BOX if box else ALG_BYTES_HEX_MIXED)
     phase_bytes = {p: alg_table[p][0] * E + alg_table[p][1] * case.n_node for p in PHASES}
     phases = PHASES
     if mode == 3:
@@ -353,9 +359,10 @@ def run_ours(args):
     ph = phases[dom]
     alg_bytes = phase_bytes[ph]
     achieved = alg_bytes / (ms_phase[dom] * 1e-3) / 1e9
-    roof = {"bound": "hbm", "kernel": KERNEL_NAMES[ph], "achieved": round(achieved, 1),
+    roof = {"bound": "hbm", "kernel": KERNEL_NAMES[ph], "box_indexing": box,
+            "achieved": round(achieved, 1),
             "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
-            "frac": round(achieved / peak, 4), "traffic": kernel_traffic(ph, case.name, E),
+            "frac": round(achieved / peak, 4), "traffic": kernel_traffic(ph + ("_box" if box else ""), case.name, E),
             "alg_bytes_per_launch": int(alg_bytes),
             "ms_per_launch": round(float(ms_phase[dom]), 4),
             "phases_ms": {p: round(float(m), 4) for p, m in zip(phases, ms_phase)},
@@ -749,9 +756,14 @@ def run_profile_case(args):
     W.apply(d, case)
     if args.no_autotune:
         d.set_autotune(False)
+    if args.step_mode is not None:
+        d.set_step_mode(args.step_mode)
+    if args.no_box:
+        d.set_box_indexing(False)
     d.init()
     d.run(args.warmup)
     d.sync()
+    d.prepare_run(args.steps)
     st = torch.cuda.ExternalStream(d.stream_handle(), device=0)
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     a.record(st)
@@ -759,9 +771,15 @@ def run_profile_case(args):
     b.record(st)
     b.synchronize()
     d.sync()
-    print(json.dumps({"profile_case": case.name, "precision": args.profile,
-                      "elements": case.n_elem, "step_mode": d.step_mode()[0],
-                      "ms_per_step": round(a.elapsed_time(b) / args.steps, 4)}), flush=True)
+    out = {"profile_case": case.name, "precision": args.profile, "elements": case.n_elem,
+           "step_mode": d.step_mode()[0], "box": d.box(),
+           "ms_per_step": round(a.elapsed_time(b) / args.steps, 4)}
+    if args.phase_steps:
+        d.set_phase_timing(True)
+        d.run(args.phase_steps)
+        ms, n = d.phase_times()
+        out["phases_ms"] = [round(float(v) / max(n, 1), 4) for v in ms]
+    print(json.dumps(out), flush=True)
 
 
 def main():
@@ -777,6 +795,12 @@ def main():
     ap.add_argument("--profile", choices=["mixed", "fp64"], default=None,
                     help="bare run of one domain for kernel profiles (no other measurement)")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--step-mode", type=int, default=None,
+                    help="profiling runs: step mode (1 per-phase, 2 cluster, 3 tiled)")
+    ap.add_argument("--no-box", action="store_true",
+                    help="profiling runs: read the connectivity arrays on box meshes too")
+    ap.add_argument("--phase-steps", type=int, default=0,
+                    help="profiling runs: also time this many steps phase by phase")
     ap.add_argument("--short-error", action="store_true",
                     help="mixed-vs-FP64 errors over W + K steps instead of the whole run")
     ap.add_argument("--n-spec", type=int, default=1024)

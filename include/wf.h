@@ -337,11 +337,24 @@ WF_API wf_status wf_set_launch_config(wf_domain *d, int32_t phase, int32_t block
  * AddBoxLength's, every node's force is summed in mode 1's order, so the
  * state is bitwise that of mode 1; the reaction sum runs in another order.
  * Not with specimens, thermal coupling, the energy history or triangle-mesh
- * contact; wf_get_tiles tells whether the mesh was tiled. Mode 0 (default)
+ * contact; the tiles are built by wf_init when mode 3 is set before it, and
+ * wf_get_tiles tells whether the mesh was tiled. Mode 0 (default)
  * picks mode 2 for meshes of at most 3000 elements, else mode 1. wf_get_step_mode reports the mode the next
  * wf_run uses and, for mode 2, the cluster's blocks and block size, for mode
  * 3 the tiles and threads per tile (0 otherwise). */
 WF_API wf_status wf_set_step_mode(wf_domain *d, int32_t mode);
+/* No counterpart in the reference. Box meshes: when the connectivity is the
+ * AddBoxLength numbering of nx x ny x nz hexahedra (checked element by element
+ * at wf_init, however the mesh was uploaded), the mixed-precision kernels
+ * compute each element's corners and each node's element list (in list
+ * order, with the node's corner in each element) from the indices instead of
+ * reading the connectivity and list arrays: the same values in the same
+ * order, so the same results bit for bit, with 128 bytes less HBM traffic per
+ * element and step. On by default; wf_set_box_indexing(d, 0) before wf_init
+ * keeps reading the arrays. wf_get_box gives nx, ny, nz, or zeros when the
+ * domain does not use it. */
+WF_API wf_status wf_set_box_indexing(wf_domain *d, int32_t on);
+WF_API wf_status wf_get_box(const wf_domain *d, int32_t dims[3]);
 /* No counterpart in the reference. The tiles built at wf_init for step mode
  * 3: their number, the number of shared nodes, the sum over tiles of their
  * distinct nodes and the node-list entries of the shared nodes (the counts

@@ -35,6 +35,7 @@
 #include "Domain_d.h"
 #include "Material.cuh"
 #include "Mesh.h"
+#include "VTKWriter.h"
 // NastranReader::read is an inline member defined in this source file, so it
 // is compiled here, where the harness constructs a reader.
 #include "NastranReader.cpp"
@@ -695,6 +696,14 @@ int wfr_get_energies(void *h, double *ekin, double *eint, int maxn) {
     eint[i] = d->eint_hist[i];
   }
   return (int)d->ekin_hist.size();
+}
+
+// The reference's own legacy VTK writer on the current state
+// (VTKWriter::VTKWriter + writeFile, VTKWriter.C:238-672).
+void wfr_write_vtk(void *h, const char *path) {
+  RefDomain *d = static_cast<RefDomain *>(h);
+  VTKWriter w(d, path);
+  w.writeFile();
 }
 
 }  // extern "C"

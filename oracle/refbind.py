@@ -79,6 +79,7 @@ def lib():
         "wfr_get_trimesh_nodes": ([vp, _dp, C.c_int], C.c_int),
         "wfr_get_surface": ([vp, _u8, _dp, _dp], C.c_int),
         "wfr_get_contforce": ([vp, _dp], C.c_int),
+        "wfr_write_vtk": ([vp, C.c_char_p], None),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -289,6 +290,11 @@ class RefDomain:
                 lib().wfr_solve_verbatim(self.h)
         finally:
             os.chdir(cwd)
+
+    def write_vtk(self, path):
+        """The reference's VTKWriter on the current state (writes `path`)."""
+        with _Silence():
+            lib().wfr_write_vtk(self.h, os.fsencode(path))
 
     # readback ---------------------------------------------------------
     def node_vec(self, name):

@@ -7,7 +7,10 @@ reference's validation/ files into validation_kats.json. The fixtures travel
 with the repository so that tests can pin the oracle where the reference
 checkout is absent.
 
-Usage: python tests/golden/gen_golden.py /path/to/reference
+Usage: python tests/golden/gen_golden.py /path/to/reference [--vtk-only]
+
+The VTK fixtures (vtk_*.npz) hold the data blocks that the reference's own
+VTKWriter prints for the state after a run (--vtk-only writes only those).
 """
 from __future__ import annotations
 
@@ -125,8 +128,8 @@ def cases():
     return out
 
 
-def run_case(name, case, steps, mode, extra):
-    d = R.RefDomain()
+def setup_ref(d, case, extra):
+    """Applies a case and its extra options to a reference domain; returns dt."""
     dt = W.apply(d, case)
     if extra.get("linear"):
         d.set_linear_hardening(True)
@@ -151,6 +154,12 @@ def run_case(name, case, steps, mode, extra):
         d.set_material_thermal(0, t["k"], t["cp"], t.get("exp", 0.0))
         if "hc" in t:
             d.set_contact_heat(t["hc"], t["T_die"])
+    return dt
+
+
+def run_case(name, case, steps, mode, extra):
+    d = R.RefDomain()
+    dt = setup_ref(d, case, extra)
     if mode == "verbatim":
         d.set_end_time(steps * dt)
         with tempfile.TemporaryDirectory() as td:
@@ -181,6 +190,39 @@ def run_case(name, case, steps, mode, extra):
     meta = dict(name=name, mode=mode, steps=steps, extra={k: list(v) if isinstance(v, tuple) else v
                                                            for k, v in extra.items()})
     return meta
+
+
+def vtk_cases():
+    """Cases whose state the reference's own VTKWriter writes (VTKWriter.C:238-664)."""
+    c = W.config(0, scale=(4, 4, 4))
+    out = [("vtk_hex4", c, 300, dict(linear=True))]
+    c = W.config(1, scale=(3, 3, 4))
+    c.perturb = 0.1
+    c.bc = "bottom_z"
+    out.append(("vtk_tet_die", c, 300, dict(linear=True, die=DIE)))
+    return out
+
+
+def run_vtk_case(name, case, steps, extra):
+    """Runs the case on the reference (stepwise loop), writes the VTK file with
+    the reference's VTKWriter and stores its data blocks as {section/name:
+    values} in tests/golden/<name>.npz (the text file is parsed here, so the
+    fixture holds exactly the numbers the reference printed)."""
+    from tests import helpers as H
+
+    d = R.RefDomain()
+    setup_ref(d, case, extra)
+    d.init()
+    d.step(steps)
+    with tempfile.TemporaryDirectory() as td:
+        path = os.path.join(td, "ref.vtk")
+        d.write_vtk(path)
+        blocks = H.parse_vtk(path)
+    res = {f"{sec}/{nm}": v for (sec, nm), v in blocks.items()}
+    res["steps"] = np.int64(steps)
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **res)
+    return dict(name=name, steps=steps, extra={k: list(v) if isinstance(v, tuple) else v
+                                               for k, v in extra.items()})
 
 
 def parse_validation(ref_root):
@@ -219,6 +261,12 @@ def main():
         sys.exit(2)
     ref_root = sys.argv[1]
     subprocess.check_call([os.path.join(ROOT, "oracle", "build_ref.sh"), ref_root])
+    vmetas = [run_vtk_case(*c) for c in vtk_cases()]
+    with open(os.path.join(HERE, "vtk_cases.json"), "w") as f:
+        json.dump(vmetas, f, indent=1)
+    if "--vtk-only" in sys.argv:
+        print("wrote", len(vmetas), "VTK fixtures")
+        return
     metas = [run_case(*c) for c in cases()]
     with open(os.path.join(HERE, "cases.json"), "w") as f:
         json.dump(metas, f, indent=1)

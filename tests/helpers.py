@@ -89,3 +89,46 @@ def compare_state(a, b, fields=STATE_FIELDS):
     for kind, name in fields:
         out[name] = rel_err(getattr(a, kind)(name), getattr(b, kind)(name))
     return out
+
+
+def parse_vtk(path):
+    """Point and cell data blocks of a legacy ASCII VTK file: {(section, name):
+    array}, section "point" or "cell", vectors as [n, 3], tensors as [n, 3, 3],
+    scalars as [n]; also ("points", "POINTS") and ("cells", "CELLS")."""
+    toks = open(path).read().split()
+    out = {}
+    i, section, count = 0, None, 0
+    while i < len(toks):
+        t = toks[i]
+        if t == "POINTS":
+            n = int(toks[i + 1])
+            out[("points", "POINTS")] = np.array(toks[i + 3:i + 3 + 3 * n], float).reshape(n, 3)
+            i += 3 + 3 * n
+        elif t == "CELLS":
+            n, items = int(toks[i + 1]), int(toks[i + 2])
+            out[("cells", "CELLS")] = np.array(toks[i + 3:i + 3 + items], np.int64)
+            i += 3 + items
+        elif t == "CELL_TYPES":
+            n = int(toks[i + 1])
+            i += 2 + n
+        elif t in ("POINT_DATA", "CELL_DATA"):
+            section, count = ("point" if t == "POINT_DATA" else "cell"), int(toks[i + 1])
+            i += 2
+        elif t == "VECTORS":
+            name = toks[i + 1]
+            out[(section, name)] = np.array(toks[i + 3:i + 3 + 3 * count], float).reshape(-1, 3)
+            i += 3 + 3 * count
+        elif t == "TENSORS":
+            name = toks[i + 1]
+            out[(section, name)] = np.array(toks[i + 3:i + 3 + 9 * count],
+                                            float).reshape(-1, 3, 3)
+            i += 3 + 9 * count
+        elif t == "SCALARS":
+            name = toks[i + 1]
+            j = i + 3 if toks[i + 3] == "LOOKUP_TABLE" else i + 4   # component count optional
+            assert toks[j] == "LOOKUP_TABLE", toks[i:j + 2]
+            out[(section, name)] = np.array(toks[j + 2:j + 2 + count], float)
+            i = j + 2 + count
+        else:
+            i += 1
+    return out

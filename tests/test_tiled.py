@@ -134,8 +134,8 @@ def test_renumbered_mesh_tiles_and_matches_fp64():
 
 def test_rotated_element_is_not_tiled_and_falls_back():
     """An element whose nodes are listed from another corner shares a node
-    with a neighbour at the same corner index: the mesh is not tiled and the
-    default mode runs the per-phase kernels."""
+    with a neighbour at the same corner index: the mesh is not tiled, a tiled
+    run is refused and the automatic mode runs the per-phase kernels."""
     case = W.config(0, scale=(16, 16, 16))
     x = case.coords()
     el = case.elnod().copy()
@@ -144,16 +144,25 @@ def test_rotated_element_is_not_tiled_and_falls_back():
     d = wf.Domain(wf.WF_MIXED)
     d.set_mesh(x, el)
     W.apply_options(d, case, x=x)
+    d.set_step_mode(3)
     d.init()
     ntiles, _, why = d.tiles()
     assert ntiles == 0 and "same corner" in why
-    assert d.step_mode()[0] == 1            # mode 0 without tiles: per-phase kernels
-    d.run(20)
-    d.sync()
-    d.set_step_mode(3)
+    assert d.step_mode()[0] == 1            # reported: the kernels a run could use
     with pytest.raises(wf.WfError) as err:
         d.run(1)
     assert err.value.status == wf.WF_ERR_UNSUPPORTED
+    d.set_step_mode(0)                      # automatic: per-phase kernels
+    d.run(20)
+    d.sync()
+
+
+def test_tiles_are_built_only_for_mode_3():
+    case = W.config(0, scale=(16, 16, 16))
+    d = wf.Domain(wf.WF_MIXED)
+    W.apply(d, case)
+    d.init()
+    assert d.tiles()[0] == 0 and "step mode 3" in d.tiles()[2]
 
 
 def test_tetrahedra_are_not_tiled():

@@ -133,6 +133,8 @@ _SIGS = {
     "wf_set_step_mode": [C.c_void_p, C.c_int32],
     "wf_get_step_mode": [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                          C.POINTER(C.c_int32)],
+    "wf_set_box_indexing": [C.c_void_p, C.c_int32],
+    "wf_get_box": [C.c_void_p, _ip],
     "wf_get_tiles": [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                      C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.c_char_p, C.c_int64],
     "wf_adjoint_forward": [C.c_void_p, C.c_int64, C.c_int64],
@@ -408,6 +410,16 @@ class Domain:
     def set_step_mode(self, mode):
         """0 automatic, 1 per-phase kernels, 2 one cluster launch per run, 3 tiled."""
         self._call("wf_set_step_mode", int(mode))
+
+    def set_box_indexing(self, on=True):
+        """Box meshes: corners and node lists computed in the kernels (before init)."""
+        self._call("wf_set_box_indexing", int(bool(on)))
+
+    def box(self):
+        """(nx, ny, nz) of a box mesh the kernels index arithmetically, else zeros."""
+        dims = np.zeros(3, np.int32)
+        self._call("wf_get_box", dims)
+        return tuple(int(v) for v in dims)
 
     def tiles(self):
         """(tiles, shared nodes, why the mesh was not tiled) of step mode 3."""

@@ -210,6 +210,7 @@ struct wf_domain {
   // hexahedra that the tiled kernels cover
   int32_t step_mode = 0;
   bool tiled = false;             // tiles built (TileParams T valid)
+  bool use_box = true;            // box meshes: connectivity computed in the mixed kernels
   TileParams T{};
   std::string tile_why;           // why the mesh was not tiled
   int cl_blocks = 0, cl_bs = 0;
@@ -1232,6 +1233,25 @@ void host_bbox(const wf_domain *d, double bb[6]) {
   });
 }
 
+// Element counts per axis if the host connectivity starts like an
+// AddBoxLength box (the device check then confirms every element); else zeros.
+void box_dims(const wf_domain *d, int *nx, int *ny, int *nz) {
+  *nx = *ny = *nz = 0;
+  if (d->npe != 8 || d->ne <= 0) return;
+  const int32_t *e0 = d->elnod.data();
+  const int64_t px = (int64_t)e0[3] - e0[0];
+  if (e0[0] != 0 || px < 2 || e0[4] % px != 0) return;
+  const int64_t py = e0[4] / px;
+  if (py < 2) return;
+  const int64_t exy = (px - 1) * (py - 1);
+  if (d->ne % exy != 0) return;
+  const int64_t ez = d->ne / exy;
+  if (px * py * (ez + 1) != d->nn || ez >= INT32_MAX) return;
+  *nx = (int)(px - 1);
+  *ny = (int)(py - 1);
+  *nz = (int)ez;
+}
+
 // Device allocation kept with the domain (build_tiles' tables).
 cudaError_t keep_alloc(void *ctx, void **p, size_t bytes) {
   return dalloc_raw(static_cast<wf_domain *>(ctx), reinterpret_cast<char **>(p), bytes);
@@ -1430,6 +1450,22 @@ WF_API wf_status wf_get_step_mode(const wf_domain *d, int32_t *mode, int32_t *bl
   if (mode) *mode = c ? 2 : (t ? 3 : 1);
   if (blocks) *blocks = c ? d->cl_blocks : (t ? d->T.ntiles : 0);
   if (block_size) *block_size = c ? d->cl_bs : (t ? kTileElems : 0);
+  return WF_OK;
+}
+
+WF_API wf_status wf_set_box_indexing(wf_domain *d, int32_t on) {
+  if (!d) return WF_ERR_ARG;
+  if (d->initialized) return fail(d, WF_ERR_STATE, "box indexing is chosen before init");
+  d->use_box = on != 0;
+  return WF_OK;
+}
+
+WF_API wf_status wf_get_box(const wf_domain *d, int32_t dims[3]) {
+  if (!d || !dims) return WF_ERR_ARG;
+  const bool on = d->initialized && d->P.box;
+  dims[0] = on ? d->P.bx : 0;
+  dims[1] = on ? d->P.by : 0;
+  dims[2] = on ? d->P.bz : 0;
   return WF_OK;
 }
 
@@ -1859,6 +1895,24 @@ WF_API wf_status wf_init(wf_domain *d) {
     mix_init(P, M, S, d->stream);
     CUDA_TRY(cudaGetLastError());
     d->mix_valid_fp64 = true;
+    // a box mesh (AddBoxLength numbering, however it was uploaded): the
+    // per-phase kernels compute corners and node lists instead of loading them
+    {
+      int bnx = 0, bny = 0, bnz = 0, is_box = 0;
+      box_dims(d, &bnx, &bny, &bnz);
+      if (d->npe == 8 && !d->nspec && d->use_box && bnx > 0)
+        CUDA_TRY(check_box(P.elnod, ne, nn, bnx, bny, bnz, d->stream, &is_box));
+      P.box = is_box;
+      if (is_box) {
+        P.bx = bnx;
+        P.by = bny;
+        P.bz = bnz;
+        P.fd_ex = make_fastdiv((uint32_t)bnx);
+        P.fd_exy = make_fastdiv((uint32_t)bnx * (uint32_t)bny);
+        P.fd_nx = make_fastdiv((uint32_t)bnx + 1u);
+        P.fd_nxy = make_fastdiv(((uint32_t)bnx + 1u) * ((uint32_t)bny + 1u));
+      }
+    }
     // element tiles of the tiled step (hexahedra; the kernels leave out
     // specimens, thermal coupling, the energy history and triangle-mesh dies)
     d->tiled = false;
@@ -1868,6 +1922,7 @@ WF_API wf_status wf_init(wf_domain *d) {
     else if (P.thermal) d->tile_why = "thermal coupling";
     else if (P.energy_on) d->tile_why = "energy history";
     else if (P.tri_on) d->tile_why = "triangle-mesh contact";
+    else if (d->step_mode != 3) d->tile_why = "step mode 3 not set before wf_init";
     if (d->tile_why.empty()) {
       double bb[6];
       host_bbox(d, bb);

@@ -36,6 +36,31 @@ struct SpecF {
   float dt, cu_pred, cu_corr, cv_corr, cv_pred, pad0, pad1, pad2;
 };
 
+// Division of 32-bit unsigned values by a divisor fixed at init without a
+// divide instruction (Granlund and Montgomery's round-up method):
+// q = (t + ((n - t) >> 1)) >> (s - 1) with t = umulhi(m, n), s = ceil(log2 d),
+// m = floor(2^32 (2^s - d) / d) + 1; exact for every 32-bit n.
+struct FastDiv {
+  uint32_t d, m;
+  int32_t s;
+};
+inline FastDiv make_fastdiv(uint32_t d) {
+  FastDiv f{d, 0u, 0};
+  if (d <= 1) return f;
+  int s = 0;
+  while ((1ull << s) < d) s++;
+  f.m = (uint32_t)((((unsigned long long)1 << 32) * ((1ull << s) - d)) / d + 1);
+  f.s = s;
+  return f;
+}
+#ifdef __CUDACC__
+__device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv &f) {
+  if (f.d == 1) return n;
+  const uint32_t t = __umulhi(f.m, n);
+  return (t + ((n - t) >> 1)) >> (f.s - 1);
+}
+#endif
+
 // Device-resident scalars advanced by the node kernel of every step.
 struct StepState {
   double time;        // Time of the reference loop (start of the current step)
@@ -133,6 +158,12 @@ struct StepParams {
   double *epart;          // [2 * grid of the energy kernel]
   double *ekin_hist, *eint_hist;  // [hist_cap]
   StepState *st;
+  // box mesh of bx x by x bz hexahedra in the AddBoxLength numbering (box = 1,
+  // checked at init): the mixed per-phase kernels compute element corners and
+  // node lists from the indices instead of loading elnod / off / slot
+  int32_t box, bx, by, bz;
+  FastDiv fd_ex, fd_exy;  // bx, bx by: element index -> (i, j, k)
+  FastDiv fd_nx, fd_nxy;  // bx + 1, (bx + 1)(by + 1): node index -> (i, j, k)
 };
 
 // FP64 state (all doubles).
@@ -277,6 +308,11 @@ cudaError_t build_tiles(const int32_t *el_soa, const double *x_soa, int64_t np, 
                         int64_t nn, const int32_t *off, const double bbox[6], int shared_threads,
                         DeviceAlloc keep, void *keep_ctx, cudaStream_t st, TileParams &T,
                         std::string &why);
+
+// Whether the SoA connectivity is the AddBoxLength numbering of nx x ny x nz
+// hexahedra (*is_box = 1): a device check of every element.
+cudaError_t check_box(const int32_t *el_soa, int64_t ne, int64_t nn, int nx, int ny, int nz,
+                      cudaStream_t st, int *is_box);
 
 // AoS [nn][3] -> SoA [3][np], zero padded
 void coords_soa(const double *x_aos, int64_t nn, int64_t np, double *out, cudaStream_t st);

@@ -38,6 +38,11 @@ __device__ __forceinline__ float2 split_d(double v) {
   const float hi = (float)v;
   return make_float2(hi, (float)(v - (double)hi));
 }
+// Height of the rigid plane z0 + vz t (FP64) as a (hi, lo) pair.
+__device__ __forceinline__ float2 die_height(const StepParams &P, double time) {
+  return split_d(P.c_z0 + P.c_vz * time);
+}
+
 // (hi, lo) + b with TwoSum and renormalisation (Knuth / Dekker).
 __device__ __forceinline__ float2 pair_add(float2 a, float b) {
   const float s = __fadd_rn(a.x, b);
@@ -65,16 +70,64 @@ __device__ __forceinline__ T ldx(const T *p) {
     return __ldg(p);
 }
 
+// Box meshes (P.box): the corners of element e in the AddBoxLength numbering.
+__device__ __forceinline__ void box_corners(const StepParams &P, int64_t e, int32_t (&nid)[8]) {
+  const uint32_t ue = (uint32_t)e;
+  const uint32_t k = fdiv(ue, P.fd_exy);
+  const uint32_t r = ue - k * P.fd_exy.d;
+  const uint32_t j = fdiv(r, P.fd_ex);
+  const uint32_t i = r - j * P.fd_ex.d;
+  const int32_t px = (int32_t)P.fd_nx.d, pxy = (int32_t)P.fd_nxy.d;
+  const int32_t n0 = (int32_t)i + px * (int32_t)j + pxy * (int32_t)k;
+  nid[0] = n0;
+  nid[1] = n0 + 1;
+  nid[2] = n0 + 1 + px;
+  nid[3] = n0 + px;
+  nid[4] = n0 + pxy;
+  nid[5] = n0 + 1 + pxy;
+  nid[6] = n0 + 1 + px + pxy;
+  nid[7] = n0 + px + pxy;
+}
+
+// Box meshes: the node list of node n (the elements around it in ascending
+// order, which is the list order, and n's corner in each); el[q] = -1 for
+// the positions outside the box.
+__device__ __forceinline__ void box_node_list(const StepParams &P, int64_t n, int32_t (&el)[8],
+                                              int32_t (&cor)[8]) {
+  const uint32_t un = (uint32_t)n;
+  const int32_t k = (int32_t)fdiv(un, P.fd_nxy);
+  const uint32_t r = un - (uint32_t)k * P.fd_nxy.d;
+  const int32_t j = (int32_t)fdiv(r, P.fd_nx);
+  const int32_t i = (int32_t)(r - (uint32_t)j * P.fd_nx.d);
+#pragma unroll
+  for (int dk = 0; dk < 2; dk++)
+#pragma unroll
+    for (int dj = 0; dj < 2; dj++)
+#pragma unroll
+      for (int di = 0; di < 2; di++) {
+        const int32_t ii = i - 1 + di, jj = j - 1 + dj, kk = k - 1 + dk;
+        const bool ok = ii >= 0 && ii < P.bx && jj >= 0 && jj < P.by && kk >= 0 && kk < P.bz;
+        // corner at (x, y, z) = (1 - di, 1 - dj, 1 - dk) of the element: 4 z + (x ^ 3 y)
+        const int q = dk * 4 + dj * 2 + di;
+        el[q] = ok ? ii + P.bx * (jj + P.by * kk) : -1;
+        cor[q] = 4 * (1 - dk) + ((1 - di) ^ (3 * (1 - dj)));
+      }
+}
+
 template <int NPE>
 __device__ __forceinline__ float weightf() {
   return NPE == 8 ? 8.0f : 1.0f / 6.0f;
 }
 
-template <int NPE, bool CG>
+template <int NPE, bool CG, bool BOX = false>
 __device__ __forceinline__ void rel_coords(const StepParams &P, const MixState &M, int64_t e,
                                            float (&r)[NPE][3], int32_t (&nid)[NPE]) {
+  if constexpr (BOX && NPE == 8) {
+    box_corners(P, e, nid);
+  } else {
 #pragma unroll
-  for (int a = 0; a < NPE; a++) nid[a] = __ldg(&P.elnod[a * P.ne + e]);
+    for (int a = 0; a < NPE; a++) nid[a] = __ldg(&P.elnod[a * P.ne + e]);
+  }
   float2 o[3];
 #pragma unroll
   for (int k = 0; k < 3; k++) o[k] = ldx<CG>(&M.xh[k * P.np + nid[0]]);
@@ -148,12 +201,12 @@ __device__ __forceinline__ void shape_derivs_f(const float J[3][3], float dH[3][
 }
 
 // ---------------------------------------------------------------------------
-template <int NPE, bool CG>
+template <int NPE, bool CG, bool BOX = false>
 __device__ __forceinline__ void geometry_one(const StepParams &P, const MixState &M, float *vol,
                                              int64_t e) {
   float r[NPE][3];
   int32_t nid[NPE];
-  rel_coords<NPE, CG>(P, M, e, r, nid);
+  rel_coords<NPE, CG, BOX>(P, M, e, r, nid);
   float J[3][3];
   jacobian_f<NPE>(r, J);
   vol[e] = det3f(J) * weightf<NPE>();
@@ -161,10 +214,10 @@ __device__ __forceinline__ void geometry_one(const StepParams &P, const MixState
 
 // Launch shapes are chosen at run time by the autotuner (wf_api.cu): block
 // size BS and a grid-stride loop (several elements per thread).
-template <int NPE, int BS>
+template <int NPE, int BS, bool BOX>
 __global__ void __launch_bounds__(BS) k_mix_geometry(StepParams P, MixState M, float *vol) {
   for (int64_t e = (int64_t)blockIdx.x * BS + threadIdx.x; e < P.ne; e += (int64_t)gridDim.x * BS)
-    geometry_one<NPE, false>(P, M, vol, e);
+    geometry_one<NPE, false, BOX>(P, M, vol, e);
 }
 
 // Rigid triangle-mesh contact of one external node in FP32 (the FP64 step's
@@ -253,21 +306,38 @@ __device__ __forceinline__ void tri_contact_mixed(const StepParams &P, const Mix
 // Nodal volumes -> J ratio and lumped mass; for contact candidates also the
 // rigid-plane contact force (it needs only x, the predicted velocity and the
 // step's mass, all final here, so it is computed before the element phase).
-template <int NPE, bool CG>
+// zd: the rigid plane's height at the step's time as a (hi, lo) float pair,
+// formed once per thread by the caller (die_height), so that the gap of a
+// contact node takes no FP64 instruction.
+template <int NPE, bool CG, bool BOX = false>
 __device__ __forceinline__ void nodal_one(const StepParams &P, const MixState &M,
-                                          const float *vol, int64_t n, double time) {
-  const int32_t b = __ldg(&P.off[n]), c = __ldg(&P.off[n + 1]) - b;
-  const float2 nc = __ldg(&M.nc[n]);   // issued before the gather, used after it
+                                          const float *vol, int64_t n, float2 zd) {
   float s = 0.0f;
-  for (int32_t k0 = 0; k0 < c; k0 += 8) {
-    int32_t sl[8];
-#pragma unroll
-    for (int j = 0; j < 8; j++) sl[j] = (k0 + j < c) ? __ldg(&P.slot[b + k0 + j]) : -1;
+  float2 nc;
+  if constexpr (BOX && NPE == 8) {
+    // the node's elements in list order, computed from its indices
+    int32_t el[8], cor[8];
+    box_node_list(P, n, el, cor);
+    nc = __ldg(&M.nc[n]);
     float g[8];
 #pragma unroll
-    for (int j = 0; j < 8; j++) g[j] = (sl[j] >= 0) ? ldx<CG>(&vol[sl[j] / NPE]) : 0.0f;
+    for (int j = 0; j < 8; j++) g[j] = (el[j] >= 0) ? ldx<CG>(&vol[el[j]]) : 0.0f;
 #pragma unroll
-    for (int j = 0; j < 8; j++) s += g[j];
+    for (int j = 0; j < 8; j++)
+      if (el[j] >= 0) s += g[j];
+  } else {
+    const int32_t b = __ldg(&P.off[n]), c = __ldg(&P.off[n + 1]) - b;
+    nc = __ldg(&M.nc[n]);   // issued before the gather, used after it
+    for (int32_t k0 = 0; k0 < c; k0 += 8) {
+      int32_t sl[8];
+#pragma unroll
+      for (int j = 0; j < 8; j++) sl[j] = (k0 + j < c) ? __ldg(&P.slot[b + k0 + j]) : -1;
+      float g[8];
+#pragma unroll
+      for (int j = 0; j < 8; j++) g[j] = (sl[j] >= 0) ? ldx<CG>(&vol[sl[j] / NPE]) : 0.0f;
+#pragma unroll
+      for (int j = 0; j < 8; j++) s += g[j];
+    }
   }
   M.jr[n] = s * nc.x;
   float mass;
@@ -285,8 +355,8 @@ __device__ __forceinline__ void nodal_one(const StepParams &P, const MixState &M
     const int64_t np = P.np;
     const float2 xz = M.xh[2 * np + n];
     const float vp0 = M.vp[n], vp1 = M.vp[np + n], vp2 = M.vp[2 * np + n];
-    const double zd = P.c_z0 + P.c_vz * time;
-    const float gap = (float)(zd - ((double)xz.x + (double)xz.y));
+    // hi parts subtract exactly near contact (within a factor 2)
+    const float gap = __fadd_rn(__fsub_rn(zd.x, xz.x), __fsub_rn(zd.y, xz.y));
     float cf0 = 0.f, cf1 = 0.f, cf2 = 0.f;
     if (gap < 0.f) {
       const float kmass = 0.2f * mass / (P.f_dt * P.f_dt);
@@ -318,10 +388,11 @@ __device__ __forceinline__ void nodal_one(const StepParams &P, const MixState &M
   }
 }
 
-template <int NPE, int BS>
+template <int NPE, int BS, bool BOX>
 __global__ void __launch_bounds__(BS) k_mix_nodal(StepParams P, MixState M, const float *vol) {
+  const float2 zd = die_height(P, P.st->time);
   for (int64_t n = (int64_t)blockIdx.x * BS + threadIdx.x; n < P.nn; n += (int64_t)gridDim.x * BS)
-    nodal_one<NPE, false>(P, M, vol, n, P.st->time);
+    nodal_one<NPE, false, BOX>(P, M, vol, n, zd);
 }
 
 // Jaumann rate + radial return, shared by both element types. The
@@ -511,7 +582,7 @@ __device__ __forceinline__ void thermal_rates(const StepParams &P, const MixStat
 // TileNodes (below): a tile's node arrays staged in shared memory through
 // tile-local indices. Both return the same values, so an element computes
 // the same forces bit for bit from either.
-template <bool CG>
+template <bool CG, bool BOX = false>
 struct GlobalNodes {
   const float2 *xh;
   const float *vp, *jr;
@@ -519,8 +590,12 @@ struct GlobalNodes {
   int32_t nid[8];
   __device__ __forceinline__ GlobalNodes(const StepParams &P, const MixState &M, int64_t e)
       : xh(M.xh), vp(M.vp), jr(M.jr), np(P.np) {
+    if constexpr (BOX) {
+      box_corners(P, e, nid);
+    } else {
 #pragma unroll
-    for (int a = 0; a < 8; a++) nid[a] = __ldg(&P.elnod[a * P.ne + e]);
+      for (int a = 0; a < 8; a++) nid[a] = __ldg(&P.elnod[a * P.ne + e]);
+    }
   }
   __device__ __forceinline__ float2 x(int a, int k) const { return ldx<CG>(&xh[k * np + nid[a]]); }
   __device__ __forceinline__ float v(int a, int k) const { return ldx<CG>(&vp[k * np + nid[a]]); }
@@ -670,10 +745,10 @@ __device__ __forceinline__ void element_hex_core(const StepParams &P, const MixS
 }
 
 // Per-phase kernels and the cluster run: node values from HBM, forces to HBM.
-template <int LAW, bool CG, bool TH>
+template <int LAW, bool CG, bool TH, bool BOX = false>
 __device__ __forceinline__ void element_hex(const StepParams &P, const MixState &M, int64_t e,
                                             float *stash, int stride, long long step) {
-  const GlobalNodes<CG> nd(P, M, e);
+  const GlobalNodes<CG, BOX> nd(P, M, e);
   ForcesToHbm out{M.fe, P.ne, e};
   element_hex_core<LAW, !CG, TH>(P, M, e, nd, stash, stride, step, out);
 }
@@ -765,11 +840,11 @@ __device__ __forceinline__ void element_tet(const StepParams &P, const MixState 
   }
 }
 
-template <int NPE, int LAW, bool CG, bool TH>
+template <int NPE, int LAW, bool CG, bool TH, bool BOX = false>
 __device__ __forceinline__ void element_one(const StepParams &P, const MixState &M, int64_t e,
                                             float *stash, int stride, long long step) {
   if constexpr (NPE == 8)
-    element_hex<LAW, CG, TH>(P, M, e, stash, stride, step);
+    element_hex<LAW, CG, TH, BOX>(P, M, e, stash, stride, step);
   else
     element_tet<LAW, CG, TH>(P, M, e, step);
 }
@@ -781,13 +856,13 @@ __device__ __forceinline__ void element_one(const StepParams &P, const MixState 
 #endif
 constexpr int elem_min_blocks(int bs) { return WF_ELEM_THREADS_PER_SM / bs; }
 
-template <int NPE, int BS, int LAW, bool TH>
+template <int NPE, int BS, int LAW, bool TH, bool BOX>
 __global__ void __launch_bounds__(BS, elem_min_blocks(BS)) k_mix_elements(StepParams P,
                                                                           MixState M) {
   __shared__ float stash[NPE == 8 ? 12 * BS : 1];
   const long long step = TH ? P.st->step : 0;
   for (int64_t e = (int64_t)blockIdx.x * BS + threadIdx.x; e < P.ne; e += (int64_t)gridDim.x * BS)
-    element_one<NPE, LAW, false, TH>(P, M, e, &stash[threadIdx.x], BS, step);
+    element_one<NPE, LAW, false, TH, BOX>(P, M, e, &stash[threadIdx.x], BS, step);
 }
 
 // ---------------------------------------------------------------------------
@@ -904,14 +979,47 @@ __device__ __forceinline__ float node_finish(const StepParams &P, const MixState
 
 // Node update of one node: gather of the element forces in list order, then
 // node_finish. Returns the node's reaction contribution.
-template <int NPE, bool CG>
+template <int NPE, bool CG, bool BOX = false>
 __device__ __forceinline__ float node_one(const StepParams &P, const MixState &M, int64_t n,
                                           long long step) {
-  const int32_t b = __ldg(&P.off[n]), c = __ldg(&P.off[n + 1]) - b;
   const int64_t ne = P.ne;
+  float fi0 = 0.f, fi1 = 0.f, fi2 = 0.f;
+  if constexpr (BOX && NPE == 8) {
+    // the node's elements in list order, from its indices; all loads issued
+    // before the sum, which adds the existing entries in list order
+    int32_t el[8], cor[8];
+    box_node_list(P, n, el, cor);
+    float g0[8], g1[8], g2[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      g0[j] = g1[j] = g2[j] = 0.f;
+      if (el[j] >= 0) {
+        const int64_t base = (int64_t)cor[j] * 3 * ne + el[j];
+        g0[j] = ldx<CG>(&M.fe[base]);
+        g1[j] = ldx<CG>(&M.fe[base + ne]);
+        g2[j] = ldx<CG>(&M.fe[base + 2 * ne]);
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < 8; j++)
+      if (el[j] >= 0) {
+        fi0 += g0[j];
+        fi1 += g1[j];
+        fi2 += g2[j];
+      }
+    const int64_t np = P.np;
+    float2 x[3];
+    float vp[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      x[k] = M.xh[k * np + n];
+      vp[k] = M.vp[k * np + n];
+    }
+    return node_finish<NPE, CG>(P, M, n, step, fi0, fi1, fi2, x, vp);
+  }
+  const int32_t b = __ldg(&P.off[n]), c = __ldg(&P.off[n + 1]) - b;
   // gather over the node's element list in list order, eight entries at a
   // time so that the slot and force loads of a chunk are all in flight
-  float fi0 = 0.f, fi1 = 0.f, fi2 = 0.f;
   for (int32_t k0 = 0; k0 < c; k0 += 8) {
     int32_t sl[8];
 #pragma unroll
@@ -945,13 +1053,13 @@ __device__ __forceinline__ float node_one(const StepParams &P, const MixState &M
   return node_finish<NPE, CG>(P, M, n, step, fi0, fi1, fi2, x, vp);
 }
 
-template <int NPE>
+template <int NPE, bool BOX>
 __global__ void __launch_bounds__(kNodeThreads, WF_NODE_MIN_BLOCKS) k_mix_nodes(StepParams P,
                                                                              MixState M) {
   __shared__ double sh[kNodeThreads / 32];
   __shared__ bool am_last;
   const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const float r = (n < P.nn) ? node_one<NPE, false>(P, M, n, P.st->step) : 0.0f;
+  const float r = (n < P.nn) ? node_one<NPE, false, BOX>(P, M, n, P.st->step) : 0.0f;
   // reaction: only warps holding a contribution reduce (FP64, fixed order);
   // the last block to finish sums all block partials with the whole block.
   const double bs = block_sum_sparse(r, sh);
@@ -1105,14 +1213,15 @@ __global__ void __launch_bounds__(kTileElems, 2) k_mix_tile(StepParams P, MixSta
 // The shared nodes: list-order gather from HBM and node update; the last
 // block adds the reaction partials of the tiles and of its own blocks in a
 // fixed order and advances the step state.
+template <bool BOX>
 __global__ void __launch_bounds__(kNodeThreads, WF_NODE_MIN_BLOCKS) k_mix_shared(StepParams P,
                                                                               MixState M,
                                                                               TileParams T) {
   __shared__ double sh[kNodeThreads / 32];
   __shared__ bool am_last;
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const float r = (i < T.nshared) ? node_one<8, false>(P, M, __ldg(&T.shared[i]), P.st->step)
-                                  : 0.0f;
+  const float r =
+      (i < T.nshared) ? node_one<8, false, BOX>(P, M, __ldg(&T.shared[i]), P.st->step) : 0.0f;
   const double bs = block_sum_sparse(r, sh);
   if (threadIdx.x == 0) {
     T.partials[T.ntiles + blockIdx.x] = bs;
@@ -1170,7 +1279,10 @@ __global__ void __launch_bounds__(BS) k_mix_cluster_run(StepParams P, MixState M
   for (int64_t it = 0; it < nsteps; it++) {
     for (int64_t e = e0 + t; e < e1; e += BS) geometry_one<NPE, true>(P, M, vol, e);
     cluster_barrier();
-    for (int64_t n = n0 + t; n < n1; n += BS) nodal_one<NPE, true>(P, M, vol, n, time);
+    {
+      const float2 zd = die_height(P, time);
+      for (int64_t n = n0 + t; n < n1; n += BS) nodal_one<NPE, true>(P, M, vol, n, zd);
+    }
     cluster_barrier();
     for (int64_t e = e0 + t; e < e1; e += BS)
       element_one<NPE, LAW, true, TH>(P, M, e, &stash[t], BS, step0 + it);
@@ -1320,23 +1432,52 @@ unsigned tuned_grid(Kernel kernel, int bs, int ept, int64_t n) {
   return g < full ? g : full;
 }
 
-template <int NPE>
-void launch_geometry(const StepParams &P, const MixState &M, float *vol, cudaStream_t st,
-                     LaunchCfg c) {
+template <int NPE, bool BOX>
+void launch_geometry_box(const StepParams &P, const MixState &M, float *vol, cudaStream_t st,
+                         LaunchCfg c) {
   switch (c.bs) {
     case 64: {
-      const unsigned g = tuned_grid(k_mix_geometry<NPE, 64>, 64, c.ept, P.ne);
-      k_mix_geometry<NPE, 64><<<g, 64, 0, st>>>(P, M, vol);
+      const unsigned g = tuned_grid(k_mix_geometry<NPE, 64, BOX>, 64, c.ept, P.ne);
+      k_mix_geometry<NPE, 64, BOX><<<g, 64, 0, st>>>(P, M, vol);
       break;
     }
     case 256: {
-      const unsigned g = tuned_grid(k_mix_geometry<NPE, 256>, 256, c.ept, P.ne);
-      k_mix_geometry<NPE, 256><<<g, 256, 0, st>>>(P, M, vol);
+      const unsigned g = tuned_grid(k_mix_geometry<NPE, 256, BOX>, 256, c.ept, P.ne);
+      k_mix_geometry<NPE, 256, BOX><<<g, 256, 0, st>>>(P, M, vol);
       break;
     }
     default: {
-      const unsigned g = tuned_grid(k_mix_geometry<NPE, 128>, 128, c.ept, P.ne);
-      k_mix_geometry<NPE, 128><<<g, 128, 0, st>>>(P, M, vol);
+      const unsigned g = tuned_grid(k_mix_geometry<NPE, 128, BOX>, 128, c.ept, P.ne);
+      k_mix_geometry<NPE, 128, BOX><<<g, 128, 0, st>>>(P, M, vol);
+      break;
+    }
+  }
+}
+
+template <int NPE>
+void launch_geometry(const StepParams &P, const MixState &M, float *vol, cudaStream_t st,
+                     LaunchCfg c) {
+  if (NPE == 8 && P.box) launch_geometry_box<NPE, true>(P, M, vol, st, c);
+  else launch_geometry_box<NPE, false>(P, M, vol, st, c);
+}
+
+template <int NPE, bool BOX>
+void launch_nodal_box(const StepParams &P, const MixState &M, const float *vol, cudaStream_t st,
+                      LaunchCfg c) {
+  switch (c.bs) {
+    case 64: {
+      const unsigned g = tuned_grid(k_mix_nodal<NPE, 64, BOX>, 64, c.ept, P.nn);
+      k_mix_nodal<NPE, 64, BOX><<<g, 64, 0, st>>>(P, M, vol);
+      break;
+    }
+    case 128: {
+      const unsigned g = tuned_grid(k_mix_nodal<NPE, 128, BOX>, 128, c.ept, P.nn);
+      k_mix_nodal<NPE, 128, BOX><<<g, 128, 0, st>>>(P, M, vol);
+      break;
+    }
+    default: {
+      const unsigned g = tuned_grid(k_mix_nodal<NPE, 256, BOX>, 256, c.ept, P.nn);
+      k_mix_nodal<NPE, 256, BOX><<<g, 256, 0, st>>>(P, M, vol);
       break;
     }
   }
@@ -1345,44 +1486,42 @@ void launch_geometry(const StepParams &P, const MixState &M, float *vol, cudaStr
 template <int NPE>
 void launch_nodal(const StepParams &P, const MixState &M, const float *vol, cudaStream_t st,
                   LaunchCfg c) {
+  if (NPE == 8 && P.box) launch_nodal_box<NPE, true>(P, M, vol, st, c);
+  else launch_nodal_box<NPE, false>(P, M, vol, st, c);
+}
+
+template <int NPE, int LAW, bool TH, bool BOX>
+void launch_elements_box(const StepParams &P, const MixState &M, cudaStream_t st, LaunchCfg c) {
   switch (c.bs) {
     case 64: {
-      const unsigned g = tuned_grid(k_mix_nodal<NPE, 64>, 64, c.ept, P.nn);
-      k_mix_nodal<NPE, 64><<<g, 64, 0, st>>>(P, M, vol);
+      const unsigned g = tuned_grid(k_mix_elements<NPE, 64, LAW, TH, BOX>, 64, c.ept, P.ne);
+      k_mix_elements<NPE, 64, LAW, TH, BOX><<<g, 64, 0, st>>>(P, M);
       break;
     }
-    case 128: {
-      const unsigned g = tuned_grid(k_mix_nodal<NPE, 128>, 128, c.ept, P.nn);
-      k_mix_nodal<NPE, 128><<<g, 128, 0, st>>>(P, M, vol);
+    case 256: {
+      const unsigned g = tuned_grid(k_mix_elements<NPE, 256, LAW, TH, BOX>, 256, c.ept, P.ne);
+      k_mix_elements<NPE, 256, LAW, TH, BOX><<<g, 256, 0, st>>>(P, M);
       break;
     }
     default: {
-      const unsigned g = tuned_grid(k_mix_nodal<NPE, 256>, 256, c.ept, P.nn);
-      k_mix_nodal<NPE, 256><<<g, 256, 0, st>>>(P, M, vol);
+      const unsigned g = tuned_grid(k_mix_elements<NPE, 128, LAW, TH, BOX>, 128, c.ept, P.ne);
+      k_mix_elements<NPE, 128, LAW, TH, BOX><<<g, 128, 0, st>>>(P, M);
       break;
     }
   }
 }
 
+// Box variants are built for hexahedra without thermal coupling (the thermal
+// element kernels keep the loaded connectivity).
 template <int NPE, int LAW, bool TH>
 void launch_elements_law(const StepParams &P, const MixState &M, cudaStream_t st, LaunchCfg c) {
-  switch (c.bs) {
-    case 64: {
-      const unsigned g = tuned_grid(k_mix_elements<NPE, 64, LAW, TH>, 64, c.ept, P.ne);
-      k_mix_elements<NPE, 64, LAW, TH><<<g, 64, 0, st>>>(P, M);
-      break;
-    }
-    case 256: {
-      const unsigned g = tuned_grid(k_mix_elements<NPE, 256, LAW, TH>, 256, c.ept, P.ne);
-      k_mix_elements<NPE, 256, LAW, TH><<<g, 256, 0, st>>>(P, M);
-      break;
-    }
-    default: {
-      const unsigned g = tuned_grid(k_mix_elements<NPE, 128, LAW, TH>, 128, c.ept, P.ne);
-      k_mix_elements<NPE, 128, LAW, TH><<<g, 128, 0, st>>>(P, M);
-      break;
+  if constexpr (NPE == 8 && !TH) {
+    if (P.box) {
+      launch_elements_box<NPE, LAW, TH, true>(P, M, st, c);
+      return;
     }
   }
+  launch_elements_box<NPE, LAW, TH, false>(P, M, st, c);
 }
 
 template <int NPE>
@@ -1474,10 +1613,12 @@ void mix_elements(const StepParams &P, const MixState &M, const float *, cudaStr
 }
 
 void mix_nodes(const StepParams &P, const MixState &M, cudaStream_t st, int node_grid) {
-  if (P.npe == 8)
-    k_mix_nodes<8><<<node_grid, kNodeThreads, 0, st>>>(P, M);
+  if (P.npe == 8 && P.box)
+    k_mix_nodes<8, true><<<node_grid, kNodeThreads, 0, st>>>(P, M);
+  else if (P.npe == 8)
+    k_mix_nodes<8, false><<<node_grid, kNodeThreads, 0, st>>>(P, M);
   else
-    k_mix_nodes<4><<<node_grid, kNodeThreads, 0, st>>>(P, M);
+    k_mix_nodes<4, false><<<node_grid, kNodeThreads, 0, st>>>(P, M);
 }
 
 static_assert(kSharedThreads == kNodeThreads, "the shared-node kernel runs node-kernel blocks");
@@ -1503,7 +1644,10 @@ void mix_tile(const StepParams &P, const MixState &M, const TileParams &T, cudaS
 }
 
 void mix_shared(const StepParams &P, const MixState &M, const TileParams &T, cudaStream_t st) {
-  k_mix_shared<<<(unsigned)mix_shared_grid(T), kNodeThreads, 0, st>>>(P, M, T);
+  if (P.box)
+    k_mix_shared<true><<<(unsigned)mix_shared_grid(T), kNodeThreads, 0, st>>>(P, M, T);
+  else
+    k_mix_shared<false><<<(unsigned)mix_shared_grid(T), kNodeThreads, 0, st>>>(P, M, T);
 }
 
 int mix_cluster_fits(const StepParams &P, const MixState &M, float *vol, int blocks, int bs) {

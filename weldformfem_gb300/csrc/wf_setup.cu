@@ -358,7 +358,42 @@ __global__ void k_shared_scatter(const int32_t *f, const int32_t *soff, int64_t 
   GRID_STRIDE(n, nn) if (f[n]) shared[soff[n]] = (int32_t)n;
 }
 
+// Flags elements whose corners differ from the AddBoxLength numbering.
+__global__ void k_box_check(const int32_t *el, int64_t ne, int nx, int ny, int32_t *err) {
+  GRID_STRIDE(e, ne) {
+    const int64_t i = e % nx, j = (e / nx) % ny, k = e / ((int64_t)nx * ny);
+    const int64_t px = nx + 1, pxy = (int64_t)(nx + 1) * (ny + 1);
+    const int64_t n0 = i + px * j + pxy * k;
+    const int64_t c[8] = {n0, n0 + 1, n0 + 1 + px, n0 + px,
+                          n0 + pxy, n0 + 1 + pxy, n0 + 1 + px + pxy, n0 + px + pxy};
+    bool ok = true;
+    for (int a = 0; a < 8; a++) ok &= el[a * ne + e] == c[a];
+    if (!ok) atomicOr(err, 1);
+  }
+}
+
 }  // namespace
+
+cudaError_t check_box(const int32_t *el_soa, int64_t ne, int64_t nn, int nx, int ny, int nz,
+                      cudaStream_t st, int *is_box) {
+  *is_box = 0;
+  if (nx <= 0 || ny <= 0 || nz <= 0 || (int64_t)nx * ny * nz != ne ||
+      (int64_t)(nx + 1) * (ny + 1) * (nz + 1) != nn)
+    return cudaSuccess;
+  int32_t *err = nullptr;
+  cudaError_t e = cudaMalloc(&err, sizeof(int32_t));
+  if (e != cudaSuccess) return e;
+  int32_t herr = 1;
+  if ((e = cudaMemsetAsync(err, 0, sizeof(int32_t), st)) == cudaSuccess) {
+    k_box_check<<<grid_for(ne), kThreads, 0, st>>>(el_soa, ne, nx, ny, err);
+    if ((e = cudaMemcpyAsync(&herr, err, sizeof(int32_t), cudaMemcpyDeviceToHost, st)) ==
+        cudaSuccess)
+      e = cudaStreamSynchronize(st);
+  }
+  cudaFree(err);
+  if (e == cudaSuccess && herr == 0) *is_box = 1;
+  return e;
+}
 
 cudaError_t build_tiles(const int32_t *el_soa, const double *x_soa, int64_t np, int64_t ne,
                         int64_t nn, const int32_t *off, const double bbox[6], int shared_threads,
