@@ -278,6 +278,26 @@ WF_API wf_status wf_run(wf_domain *d, int64_t nsteps);
  * a following wf_run(d, nsteps) replays (and grows the histories it fills),
  * so that the run itself does no capture. Runs nothing. */
 WF_API wf_status wf_prepare_run(wf_domain *d, int64_t nsteps);
+/* No counterpart in the reference. One FP64 step in two halves, for a slab
+ * decomposition of one mesh over several domains (weldformfem_gb300/slabs.py):
+ * wf_step_begin queues the predictor, geometry, nodal and element phases
+ * (the loop body up to the element forces, Solver_explicit.C:346-760),
+ * wf_step_end the assembly and node update (assemblyForces onwards). Between
+ * them wf_get_halo_forces / wf_set_halo_forces read and overwrite the element
+ * and hourglass forces of elements [e0, e1) (2 x (e1 - e0) x npe x 3 doubles:
+ * forces, then hourglass forces, per element and local node); after
+ * wf_step_end, wf_get_halo_nodes / wf_set_halo_nodes read and overwrite the
+ * node state a step starts from for nodes [n0, n1): positions, velocities,
+ * previous accelerations and displacements (12 x (n1 - n0) doubles: field,
+ * then component, then node). Host buffers; the calls wait for the domain's
+ * stream. FP64 step only, without specimens, thermal coupling, triangle-mesh
+ * contact or the energy history (WF_ERR_UNSUPPORTED). */
+WF_API wf_status wf_step_begin(wf_domain *d);
+WF_API wf_status wf_step_end(wf_domain *d);
+WF_API wf_status wf_get_halo_forces(wf_domain *d, int64_t e0, int64_t e1, double *out);
+WF_API wf_status wf_set_halo_forces(wf_domain *d, int64_t e0, int64_t e1, const double *in);
+WF_API wf_status wf_get_halo_nodes(wf_domain *d, int64_t n0, int64_t n1, double *out);
+WF_API wf_status wf_set_halo_nodes(wf_domain *d, int64_t n0, int64_t n1, const double *in);
 /* Domain_d::SolveChungHulbert: steps while Time < end time; *nsteps = count. */
 WF_API wf_status wf_solve(wf_domain *d, int64_t *nsteps);
 WF_API wf_status wf_get_time(const wf_domain *d, double *t, int64_t *step);
@@ -528,10 +548,29 @@ WF_API wf_status wf_load_deck(wf_domain *d, const char *path, wf_deck_info *info
  * cards (fixed columns or comma-separated), nodes numbered in card order,
  * elements with n5..n8 equal to n4 read as tetrahedra. */
 WF_API wf_status wf_load_lsdyna(wf_domain *d, const char *path);
-/* Legacy VTK file of the current state (VTKWriter.C field names: DISP,
- * Velocity, Acceleration, ContForce, nod_mass; pressure, pl_strain, Vol, Rho,
- * sigy, SIGMA). */
+/* VTKWriter (VTKWriter.C:238-672): legacy ASCII VTK file of the current
+ * state in the reference writer's layout. Points: the part's nodes, then the
+ * rigid triangle meshes' nodes; cells: the part's elements, then the
+ * triangles. Point data Position, DISP, Acceleration, Velocity, Part_ID,
+ * Temp (thermal coupling), ContForce, nod_mass, stress (von Mises of the
+ * node-averaged stress), ext_nodes, nod_area, nod_p, SIGMAT (node-averaged
+ * stress), EPSR (node-averaged strain rate, FP64 step only); cell data
+ * ele_area (written as 0), pressure, pl_strain, DDEVT (strain rate, FP64
+ * step only), J, Vol, Rho, Vol_0, sigy. Values with 9 significant digits
+ * (coordinates 17). Waits for the domain's stream. */
 WF_API wf_status wf_write_vtk(wf_domain *d, const char *path);
+/* No counterpart in the reference, whose loop stops to write each output
+ * (Solver_explicit.C:1036-1156). Asynchronous output: wf_snapshot queues on
+ * the domain's stream a device copy of the fields wf_write_vtk writes, then
+ * on a second stream a copy of them into pinned host memory, and returns at
+ * once with the slot (0 or 1) that holds them; the steps queued after it run
+ * while the copy proceeds. wf_write_snapshot_vtk(d, slot, path) waits for
+ * that slot's copy (not for later steps), writes the file exactly as
+ * wf_write_vtk would have written it at the snapshot's step (byte for byte),
+ * and frees the slot. Two slots: a third wf_snapshot before one of them is
+ * written returns WF_ERR_STATE. */
+WF_API wf_status wf_snapshot(wf_domain *d, int32_t *slot);
+WF_API wf_status wf_write_snapshot_vtk(wf_domain *d, int32_t slot, const char *path);
 
 /* ---- readback (host buffers) -------------------------------------------------- */
 WF_API wf_status wf_get_node_field(wf_domain *d, int32_t field, double *out);   /* 3*nn */

@@ -95,6 +95,12 @@ def lib():
         "wfo_add_contact_trimesh": ([vp, i64, _dp, i64, _ip, _dp], C.c_int),
         "wfo_get_trimesh_nodes": ([vp, _dp, i64], i64),
         "wfo_get_surface": ([vp, _u8, _dp, _dp], i64),
+        "wfo_step_begin": ([vp], None),
+        "wfo_step_end": ([vp], None),
+        "wfo_get_elem_forces_range": ([vp, i64, i64, _dp], C.c_int),
+        "wfo_set_elem_forces_range": ([vp, i64, i64, _dp], C.c_int),
+        "wfo_get_node_state_range": ([vp, i64, i64, _dp], C.c_int),
+        "wfo_set_node_state_range": ([vp, i64, i64, _dp], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -271,6 +277,35 @@ class OracleDomain:
 
     def solve(self):
         return lib().wfo_solve(self.h)
+
+    # step halves and halo data (slab decomposition) -------------------
+    def step_begin(self):
+        lib().wfo_step_begin(self.h)
+
+    def step_end(self):
+        lib().wfo_step_end(self.h)
+
+    def elem_forces(self, e0, e1):
+        """Element and hourglass forces of elements [e0, e1), flat."""
+        out = np.zeros(2 * (e1 - e0) * self.npe * 3)
+        self._check(lib().wfo_get_elem_forces_range(self.h, int(e0), int(e1), out), "elem forces")
+        return out
+
+    def set_elem_forces(self, e0, e1, data):
+        self._check(lib().wfo_set_elem_forces_range(self.h, int(e0), int(e1),
+                                              np.ascontiguousarray(data, np.float64)),
+                    "set elem forces")
+
+    def node_state(self, n0, n1):
+        """Node state of nodes [n0, n1), flat."""
+        out = np.zeros(15 * (n1 - n0))
+        self._check(lib().wfo_get_node_state_range(self.h, int(n0), int(n1), out), "node state")
+        return out
+
+    def set_node_state_range(self, n0, n1, data):
+        self._check(lib().wfo_set_node_state_range(self.h, int(n0), int(n1),
+                                             np.ascontiguousarray(data, np.float64)),
+                    "set node state")
 
     @property
     def time(self):

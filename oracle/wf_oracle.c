@@ -1552,8 +1552,19 @@ static void compute_energies(const wfo_domain *d, double *ekin, double *deint) {
 }
 
 /* One iteration of the loop body of SolveChungHulbert, CPU branch with default
- * options (Solver_explicit.C:346-1167). */
+ * options (Solver_explicit.C:346-1167), in two halves: step_begin runs up to
+ * the element and contact forces, step_end from assemblyForces on (the split
+ * a slab decomposition exchanges its halo element forces at). */
+static void one_step(wfo_domain *d);
+static void step_begin(wfo_domain *d);
+static void step_end(wfo_domain *d);
+
 static void one_step(wfo_domain *d) {
+  step_begin(d);
+  step_end(d);
+}
+
+static void step_begin(wfo_domain *d) {
   update_prediction(d);
   for (int k = 0; k < 3; k++) impose_bcv(d, k);
   calc_jacobian_derivs(d);
@@ -1577,6 +1588,9 @@ static void one_step(wfo_domain *d) {
     calc_contact_trimesh(d);
   else if (d->contact)
     calc_contact(d);
+}
+
+static void step_end(wfo_domain *d) {
   assembly_forces(d);
   double r = 0.0;
   if (d->contact) {
@@ -1601,6 +1615,42 @@ static void one_step(wfo_domain *d) {
   }
   d->time += d->dt;
   d->step_count++;
+}
+
+void wfo_step_begin(wfo_domain *d) { step_begin(d); }
+void wfo_step_end(wfo_domain *d) { step_end(d); }
+
+/* Element forces of elements [e0, e1): f_elem then f_hg, npe x 3 each. */
+int wfo_get_elem_forces_range(const wfo_domain *d, int64_t e0, int64_t e1, double *out) {
+  if (e0 < 0 || e1 > d->ne || e0 > e1) return -1;
+  const size_t k = (size_t)(e1 - e0) * d->npe * 3;
+  memcpy(out, d->f_elem + e0 * d->npe * 3, sizeof(double) * k);
+  memcpy(out + k, d->f_hg + e0 * d->npe * 3, sizeof(double) * k);
+  return 0;
+}
+int wfo_set_elem_forces_range(wfo_domain *d, int64_t e0, int64_t e1, const double *in) {
+  if (e0 < 0 || e1 > d->ne || e0 > e1) return -1;
+  const size_t k = (size_t)(e1 - e0) * d->npe * 3;
+  memcpy(d->f_elem + e0 * d->npe * 3, in, sizeof(double) * k);
+  memcpy(d->f_hg + e0 * d->npe * 3, in + k, sizeof(double) * k);
+  return 0;
+}
+
+/* Node state of nodes [n0, n1): x, v, a, prev_a, u (3 each per node, field
+ * after field). */
+int wfo_get_node_state_range(const wfo_domain *d, int64_t n0, int64_t n1, double *out) {
+  if (n0 < 0 || n1 > d->nn || n0 > n1) return -1;
+  const size_t k = (size_t)(n1 - n0) * 3;
+  const double *src[5] = {d->x, d->v, d->a, d->prev_a, d->u};
+  for (int f = 0; f < 5; f++) memcpy(out + f * k, src[f] + 3 * n0, sizeof(double) * k);
+  return 0;
+}
+int wfo_set_node_state_range(wfo_domain *d, int64_t n0, int64_t n1, const double *in) {
+  if (n0 < 0 || n1 > d->nn || n0 > n1) return -1;
+  const size_t k = (size_t)(n1 - n0) * 3;
+  double *dst[5] = {d->x, d->v, d->a, d->prev_a, d->u};
+  for (int f = 0; f < 5; f++) memcpy(dst[f] + 3 * n0, in + f * k, sizeof(double) * k);
+  return 0;
 }
 
 int wfo_run(wfo_domain *d, int64_t nsteps) {

@@ -108,6 +108,16 @@ int64_t wfo_get_surface(const wfo_domain *d, uint8_t *ext, double *node_area, do
 /* Kinetic energy and accumulated internal energy after each step
  * (Domain_d::computeEnergies, Mechanical.C:2145-2185; Solver_explicit.C:1029-1031). */
 int64_t wfo_get_energies(const wfo_domain *d, double *ekin, double *eint, int64_t cap);
+/* The loop body in two halves (up to the element and contact forces; from
+ * assemblyForces on) and the halo data a slab decomposition exchanges:
+ * element forces of [e0, e1) (f_elem then f_hg) and node state of [n0, n1)
+ * (x, v, a, prev_a, u). */
+void wfo_step_begin(wfo_domain *d);
+void wfo_step_end(wfo_domain *d);
+int wfo_get_elem_forces_range(const wfo_domain *d, int64_t e0, int64_t e1, double *out);
+int wfo_set_elem_forces_range(wfo_domain *d, int64_t e0, int64_t e1, const double *in);
+int wfo_get_node_state_range(const wfo_domain *d, int64_t n0, int64_t n1, double *out);
+int wfo_set_node_state_range(wfo_domain *d, int64_t n0, int64_t n1, const double *in);
 
 #ifdef __cplusplus
 }

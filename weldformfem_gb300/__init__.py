@@ -148,6 +148,14 @@ _SIGS = {
     "wf_load_deck": [C.c_void_p, C.c_char_p, C.POINTER(WfDeckInfo), C.c_char_p, C.c_int64],
     "wf_load_lsdyna": [C.c_void_p, C.c_char_p],
     "wf_write_vtk": [C.c_void_p, C.c_char_p],
+    "wf_snapshot": [C.c_void_p, C.POINTER(C.c_int32)],
+    "wf_step_begin": [C.c_void_p],
+    "wf_step_end": [C.c_void_p],
+    "wf_get_halo_forces": [C.c_void_p, C.c_int64, C.c_int64, _dp],
+    "wf_set_halo_forces": [C.c_void_p, C.c_int64, C.c_int64, _dp],
+    "wf_get_halo_nodes": [C.c_void_p, C.c_int64, C.c_int64, _dp],
+    "wf_set_halo_nodes": [C.c_void_p, C.c_int64, C.c_int64, _dp],
+    "wf_write_snapshot_vtk": [C.c_void_p, C.c_int32, C.c_char_p],
     "wf_set_contact_trimesh": [C.c_void_p, C.c_int64, _dp, C.c_int64, _ip, _dp, C.c_double,
                                C.c_double, C.c_double],
     "wf_get_trimesh_nodes": [C.c_void_p, _dp, C.c_int64, C.POINTER(C.c_int64)],
@@ -374,6 +382,31 @@ class Domain:
         self._call("wf_adjoint_backward", seed, int(bool(fp32)), grad)
         return grad.reshape(-1, 3)
 
+    # step halves and halo data (slab decomposition) -------------------
+    def step_begin(self):
+        self._call("wf_step_begin")
+
+    def step_end(self):
+        self._call("wf_step_end")
+
+    def elem_forces(self, e0, e1):
+        """Element and hourglass forces of elements [e0, e1), flat."""
+        out = np.zeros(2 * (e1 - e0) * self.npe * 3)
+        self._call("wf_get_halo_forces", int(e0), int(e1), out)
+        return out
+
+    def set_elem_forces(self, e0, e1, data):
+        self._call("wf_set_halo_forces", int(e0), int(e1), np.ascontiguousarray(data, np.float64))
+
+    def node_state(self, n0, n1):
+        """Node state a step starts from, nodes [n0, n1), flat."""
+        out = np.zeros(12 * (n1 - n0))
+        self._call("wf_get_halo_nodes", int(n0), int(n1), out)
+        return out
+
+    def set_node_state_range(self, n0, n1, data):
+        self._call("wf_set_halo_nodes", int(n0), int(n1), np.ascontiguousarray(data, np.float64))
+
     def solve(self):
         n = C.c_int64()
         self._call("wf_solve", C.byref(n))
@@ -544,6 +577,16 @@ class Domain:
 
     def write_vtk(self, path):
         self._call("wf_write_vtk", os.fsencode(path))
+
+    def snapshot(self):
+        """Queues a copy of the output fields to pinned host memory; returns its slot."""
+        slot = C.c_int32()
+        self._call("wf_snapshot", C.byref(slot))
+        return slot.value
+
+    def write_snapshot_vtk(self, slot, path):
+        """Writes a snapshot (see snapshot()) as wf_write_vtk would have at its step."""
+        self._call("wf_write_snapshot_vtk", int(slot), os.fsencode(path))
 
     def set_energy_history(self, on=True):
         self._call("wf_set_energy_history", int(bool(on)))

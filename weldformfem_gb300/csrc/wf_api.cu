@@ -195,6 +195,18 @@ struct wf_domain {
   int64_t launches = 0;
   int64_t graph_launches = 0;     // step graphs replayed since wf_init
   int64_t h2d_bytes = 0, d2h_bytes = 0;
+  // asynchronous output: two snapshot slots, each a device copy of the state
+  // fields and a pinned host copy filled on the output stream
+  struct Snapshot {
+    double *dev = nullptr, *host = nullptr;
+    size_t count = 0;
+    cudaEvent_t ready = nullptr, done = nullptr;
+    int state = 0;                // 0 free, 1 queued or copied, not yet written
+  } snap[2];
+  cudaStream_t out_stream = nullptr;
+  int snap_next = 0;
+  std::vector<uint8_t> surf_ext;  // external-surface flags and areas (contact), for the VTK
+  std::vector<double> surf_area;
   // pinned copy of the device step state, queued after every wf_run and
   // read by the next wf_sync (the non-finite force check)
   StepState *st_host = nullptr;
@@ -211,6 +223,7 @@ struct wf_domain {
   int32_t step_mode = 0;
   bool tiled = false;             // tiles built (TileParams T valid)
   bool use_box = true;            // box meshes: connectivity computed in the mixed kernels
+  bool half_open = false;         // wf_step_begin called, wf_step_end not yet
   TileParams T{};
   std::string tile_why;           // why the mesh was not tiled
   int cl_blocks = 0, cl_bs = 0;
@@ -302,6 +315,16 @@ void free_device(wf_domain *d) {
   if (d->st_host) cudaFreeHost(d->st_host);
   d->st_host = nullptr;
   d->st_pending = false;
+  for (auto &sn : d->snap) {
+    if (sn.dev) cudaFree(sn.dev);
+    if (sn.host) cudaFreeHost(sn.host);
+    if (sn.ready) cudaEventDestroy(sn.ready);
+    if (sn.done) cudaEventDestroy(sn.done);
+    sn = wf_domain::Snapshot{};
+  }
+  d->snap_next = 0;
+  d->surf_ext.clear();
+  d->surf_area.clear();
   if (d->init_stage) cudaFree(d->init_stage);
   d->init_stage = nullptr;
   for (cudaEvent_t ev : d->ev_pool) cudaEventDestroy(ev);
@@ -678,8 +701,10 @@ WF_API wf_status wf_domain_destroy(wf_domain *d) {
   if (!d) return WF_ERR_ARG;
   cudaSetDevice(d->device);
   if (d->stream) cudaStreamSynchronize(d->stream);
+  if (d->out_stream) cudaStreamSynchronize(d->out_stream);
   free_device(d);
   if (d->stream) cudaStreamDestroy(d->stream);
+  if (d->out_stream) cudaStreamDestroy(d->out_stream);
   delete d;
   return WF_OK;
 }
@@ -2220,6 +2245,132 @@ WF_API wf_status wf_prepare_run(wf_domain *d, int64_t nsteps) {
   return WF_OK;
 }
 
+// ---- step halves and halo data (slab decomposition) ------------------------------
+namespace {
+wf_status need_halves(wf_domain *d) {
+  if (!d) return WF_ERR_ARG;
+  if (!d->initialized) return fail(d, WF_ERR_STATE, "wf_init not called");
+  if (d->precision != WF_FP64 || d->nspec || d->thermal || d->P.tri_on || d->P.energy_on)
+    return fail(d, WF_ERR_UNSUPPORTED, "step halves need the FP64 step without specimens, "
+                                       "thermal coupling, triangle-mesh contact or energies");
+  if (!(d->dt > 0.0)) return fail(d, WF_ERR_STATE, "time step not set (SetDT)");
+  return WF_OK;
+}
+}  // namespace
+
+WF_API wf_status wf_step_begin(wf_domain *d) {
+  wf_status s = need_halves(d);
+  if (s) return s;
+  if (d->half_open) return fail(d, WF_ERR_STATE, "wf_step_end not called after wf_step_begin");
+  CUDA_TRY(cudaSetDevice(d->device));
+  if ((s = grow_history(d, d->host_step + 1))) return s;
+  set_dt_constants(d->P, d->dt);
+  const StepParams &P = d->P;
+  fp64_predict(P, d->S, d->stream);
+  fp64_geometry(P, d->S, d->stream, false);
+  fp64_nodal(P, d->S, d->stream, 0);
+  fp64_elements(P, d->S, d->stream);
+  CUDA_TRY(cudaGetLastError());
+  d->launches += 4;
+  d->half_open = true;
+  return WF_OK;
+}
+
+WF_API wf_status wf_step_end(wf_domain *d) {
+  wf_status s = need_halves(d);
+  if (s) return s;
+  if (!d->half_open) return fail(d, WF_ERR_STATE, "wf_step_begin not called");
+  CUDA_TRY(cudaSetDevice(d->device));
+  fp64_nodes(d->P, d->S, d->stream, d->node_grid);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaMemcpyAsync(d->st_host, d->P.st, sizeof(StepState), cudaMemcpyDeviceToHost,
+                           d->stream));
+  d->st_pending = true;
+  d->launches += 1;
+  d->half_open = false;
+  d->host_time += d->dt;
+  d->host_step += 1;
+  return WF_OK;
+}
+
+WF_API wf_status wf_get_halo_forces(wf_domain *d, int64_t e0, int64_t e1, double *out) {
+  wf_status s = need_halves(d);
+  if (s) return s;
+  if (!out || e0 < 0 || e1 > d->ne || e0 > e1) return WF_ERR_ARG;
+  CUDA_TRY(cudaSetDevice(d->device));
+  const size_t k = (size_t)(e1 - e0) * d->npe * 3, at = (size_t)e0 * d->npe * 3;
+  CUDA_TRY(cudaMemcpyAsync(out, d->S.fe + at, sizeof(double) * k, cudaMemcpyDeviceToHost,
+                           d->stream));
+  if (d->S.fhg)
+    CUDA_TRY(cudaMemcpyAsync(out + k, d->S.fhg + at, sizeof(double) * k, cudaMemcpyDeviceToHost,
+                             d->stream));
+  else
+    std::fill(out + k, out + 2 * k, 0.0);
+  CUDA_TRY(cudaStreamSynchronize(d->stream));
+  d->d2h_bytes += (int64_t)(sizeof(double) * 2 * k);
+  return WF_OK;
+}
+
+WF_API wf_status wf_set_halo_forces(wf_domain *d, int64_t e0, int64_t e1, const double *in) {
+  wf_status s = need_halves(d);
+  if (s) return s;
+  if (!in || e0 < 0 || e1 > d->ne || e0 > e1) return WF_ERR_ARG;
+  CUDA_TRY(cudaSetDevice(d->device));
+  const size_t k = (size_t)(e1 - e0) * d->npe * 3, at = (size_t)e0 * d->npe * 3;
+  CUDA_TRY(cudaMemcpyAsync(d->S.fe + at, in, sizeof(double) * k, cudaMemcpyHostToDevice,
+                           d->stream));
+  if (d->S.fhg)
+    CUDA_TRY(cudaMemcpyAsync(d->S.fhg + at, in + k, sizeof(double) * k, cudaMemcpyHostToDevice,
+                             d->stream));
+  CUDA_TRY(cudaStreamSynchronize(d->stream));
+  d->h2d_bytes += (int64_t)(sizeof(double) * 2 * k);
+  return WF_OK;
+}
+
+namespace {
+// The node state a halo carries between steps: x, v, prev_a, u (SoA fields).
+void halo_fields(wf_domain *d, double *f[4]) {
+  f[0] = d->S.x;
+  f[1] = d->S.v;
+  f[2] = d->S.pa;
+  f[3] = d->S.u;
+}
+}  // namespace
+
+WF_API wf_status wf_get_halo_nodes(wf_domain *d, int64_t n0, int64_t n1, double *out) {
+  wf_status s = need_halves(d);
+  if (s) return s;
+  if (!out || n0 < 0 || n1 > d->nn || n0 > n1) return WF_ERR_ARG;
+  CUDA_TRY(cudaSetDevice(d->device));
+  double *f[4];
+  halo_fields(d, f);
+  const size_t m = (size_t)(n1 - n0);
+  for (int q = 0; q < 4; q++)
+    for (int k = 0; k < 3; k++)
+      CUDA_TRY(cudaMemcpyAsync(out + (3 * q + k) * m, f[q] + k * d->np + n0, sizeof(double) * m,
+                               cudaMemcpyDeviceToHost, d->stream));
+  CUDA_TRY(cudaStreamSynchronize(d->stream));
+  d->d2h_bytes += (int64_t)(sizeof(double) * 12 * m);
+  return WF_OK;
+}
+
+WF_API wf_status wf_set_halo_nodes(wf_domain *d, int64_t n0, int64_t n1, const double *in) {
+  wf_status s = need_halves(d);
+  if (s) return s;
+  if (!in || n0 < 0 || n1 > d->nn || n0 > n1) return WF_ERR_ARG;
+  CUDA_TRY(cudaSetDevice(d->device));
+  double *f[4];
+  halo_fields(d, f);
+  const size_t m = (size_t)(n1 - n0);
+  for (int q = 0; q < 4; q++)
+    for (int k = 0; k < 3; k++)
+      CUDA_TRY(cudaMemcpyAsync(f[q] + k * d->np + n0, in + (3 * q + k) * m, sizeof(double) * m,
+                               cudaMemcpyHostToDevice, d->stream));
+  CUDA_TRY(cudaStreamSynchronize(d->stream));
+  d->h2d_bytes += (int64_t)(sizeof(double) * 12 * m);
+  return WF_OK;
+}
+
 WF_API wf_status wf_solve(wf_domain *d, int64_t *nsteps) {
   if (!d) return WF_ERR_ARG;
   if (!d->initialized) return fail(d, WF_ERR_STATE, "wf_init not called");
@@ -2427,6 +2578,187 @@ WF_API wf_status wf_get_disp(wf_domain *d, double *out) { return wf_get_node_fie
 WF_API wf_status wf_get_vel(wf_domain *d, double *out) { return wf_get_node_field(d, WF_NODE_V, out); }
 WF_API wf_status wf_get_pl_strain(wf_domain *d, double *out) {
   return wf_get_elem_scalar(d, WF_ELEM_PL_STRAIN, out);
+}
+
+// ---- VTK output: synchronous and from snapshots ---------------------------------
+namespace {
+
+// Offsets (in doubles) of the fields in a snapshot slot.
+struct SnapLayout {
+  size_t x, u, v, a, cf, mass, T, p, pl, vol, vol0, rho, sy, sig, sr, tri, count;
+};
+
+SnapLayout snap_layout(const wf_domain *d) {
+  const size_t n3 = 3 * (size_t)d->nn, nn = d->nn, ne = d->ne;
+  SnapLayout L{};
+  size_t o = 0;
+  L.x = o; o += n3;
+  L.u = o; o += n3;
+  L.v = o; o += n3;
+  L.a = o; o += n3;
+  L.cf = o; o += n3;
+  L.mass = o; o += nn;
+  L.T = o; o += d->thermal ? nn : 0;
+  L.p = o; o += ne;
+  L.pl = o; o += ne;
+  L.vol = o; o += ne;
+  L.vol0 = o; o += ne;
+  L.rho = o; o += ne;
+  L.sy = o; o += ne;
+  L.sig = o; o += 6 * ne;
+  L.sr = o; o += d->S.sr ? 6 * ne : 0;
+  L.tri = o; o += d->P.tri_on ? 3 * (size_t)d->P.tri_nn : 0;
+  L.count = o;
+  return L;
+}
+
+// The static parts of a VTK view: connectivity, surface, die triangles.
+wf_status vtk_static(wf_domain *d, VtkView &v) {
+  v.nn = d->nn;
+  v.ne = d->ne;
+  v.npe = d->npe;
+  v.elnod = d->elnod.data();
+  if (d->P.tri_on) {
+    if (d->surf_ext.empty()) {
+      std::vector<double> nodlen;
+      part_surface(d, d->surf_ext, d->surf_area, nodlen);
+    }
+    v.ext = d->surf_ext.data();
+    v.area = d->surf_area.data();
+    v.tri_nn = d->P.tri_nn;
+    v.tri_ne = d->P.tri_ne;
+    v.tri_el = d->tri_el.data();
+    v.T_die = d->tri_Tdie;
+  }
+  return WF_OK;
+}
+
+// The view's field pointers into one buffer of snapshot layout.
+void vtk_fields(const wf_domain *d, const SnapLayout &L, const double *b, VtkView &v) {
+  v.x = b + L.x;
+  v.u = b + L.u;
+  v.v = b + L.v;
+  v.a = b + L.a;
+  v.cf = b + L.cf;
+  v.mass = b + L.mass;
+  v.T = d->thermal ? b + L.T : nullptr;
+  v.p = b + L.p;
+  v.pl = b + L.pl;
+  v.vol = b + L.vol;
+  v.vol0 = b + L.vol0;
+  v.rho = b + L.rho;
+  v.sy = b + L.sy;
+  v.sig = b + L.sig;
+  v.sig_soa = true;
+  v.sr = d->S.sr ? b + L.sr : nullptr;
+  v.sr_soa = true;
+  if (d->P.tri_on) v.tri_x = b + L.tri;
+}
+
+// Queues on the domain's stream the device copies of the state into dst
+// (snapshot layout): node vectors transposed to AoS, the rest as stored.
+wf_status queue_state_copy(wf_domain *d, const SnapLayout &L, double *dst) {
+  const Fp64State &S = d->S;
+  const int64_t nn = d->nn, np = d->np, ne = d->ne;
+  const double *node3[5] = {S.x, S.u, S.v, S.pa, S.cf};
+  const size_t off3[5] = {L.x, L.u, L.v, L.a, L.cf};
+  for (int i = 0; i < 5; i++) coords_aos(node3[i], nn, np, dst + off3[i], d->stream);
+  CUDA_TRY(cudaGetLastError());
+  auto d2d = [&](size_t off, const double *src, size_t count) {
+    return cudaMemcpyAsync(dst + off, src, sizeof(double) * count, cudaMemcpyDeviceToDevice,
+                           d->stream);
+  };
+  CUDA_TRY(d2d(L.mass, S.mass, nn));
+  if (d->thermal) CUDA_TRY(d2d(L.T, S.T, nn));
+  CUDA_TRY(d2d(L.p, S.p, ne));
+  CUDA_TRY(d2d(L.pl, S.pls, ne));
+  CUDA_TRY(d2d(L.vol, S.vol, ne));
+  CUDA_TRY(d2d(L.vol0, S.vol0, ne));
+  CUDA_TRY(d2d(L.rho, S.rho, ne));
+  CUDA_TRY(d2d(L.sy, S.sy, ne));
+  CUDA_TRY(d2d(L.sig, S.sig, 6 * (size_t)ne));
+  if (S.sr) CUDA_TRY(d2d(L.sr, S.sr, 6 * (size_t)ne));
+  if (d->P.tri_on) CUDA_TRY(d2d(L.tri, d->P.tri_x, 3 * (size_t)d->P.tri_nn));
+  return WF_OK;
+}
+
+}  // namespace
+
+WF_API wf_status wf_write_vtk(wf_domain *d, const char *path) {
+  if (!path) return WF_ERR_ARG;
+  wf_status s = ready_for_readback(d);
+  if (s) return s;
+  // the same device copies a snapshot takes, read back at once
+  const SnapLayout L = snap_layout(d);
+  double *dev = nullptr;
+  CUDA_TRY(cudaMalloc(&dev, sizeof(double) * std::max<size_t>(L.count, 1)));
+  std::vector<double> host(L.count);
+  s = queue_state_copy(d, L, dev);
+  cudaError_t e = cudaSuccess;
+  if (!s) e = cudaMemcpyAsync(host.data(), dev, sizeof(double) * L.count, cudaMemcpyDeviceToHost,
+                              d->stream);
+  if (!s && e == cudaSuccess) e = cudaStreamSynchronize(d->stream);
+  cudaFree(dev);
+  if (s) return s;
+  if (e != cudaSuccess) return fail(d, WF_ERR_CUDA, "wf_write_vtk: %s", cudaGetErrorString(e));
+  d->d2h_bytes += (int64_t)(sizeof(double) * L.count);
+  VtkView v;
+  vtk_static(d, v);
+  vtk_fields(d, L, host.data(), v);
+  if (!write_vtk_text(path, v)) return fail(d, WF_ERR_ARG, "cannot write %s", path);
+  return WF_OK;
+}
+
+WF_API wf_status wf_snapshot(wf_domain *d, int32_t *slot) {
+  if (!slot) return WF_ERR_ARG;
+  wf_status s = ready_for_readback(d);
+  if (s) return s;
+  int k = d->snap_next;
+  if (d->snap[k].state != 0) k = 1 - k;
+  if (d->snap[k].state != 0)
+    return fail(d, WF_ERR_STATE, "both snapshot slots hold states not yet written");
+  wf_domain::Snapshot &sn = d->snap[k];
+  const SnapLayout L = snap_layout(d);
+  if (!d->out_stream) CUDA_TRY(cudaStreamCreateWithFlags(&d->out_stream, cudaStreamNonBlocking));
+  if (sn.count != L.count) {
+    if (sn.dev) cudaFree(sn.dev);
+    if (sn.host) cudaFreeHost(sn.host);
+    sn.dev = nullptr;
+    sn.host = nullptr;
+    CUDA_TRY(cudaMalloc(&sn.dev, sizeof(double) * std::max<size_t>(L.count, 1)));
+    CUDA_TRY(cudaMallocHost(&sn.host, sizeof(double) * std::max<size_t>(L.count, 1)));
+    sn.count = L.count;
+  }
+  if (!sn.ready) CUDA_TRY(cudaEventCreateWithFlags(&sn.ready, cudaEventDisableTiming));
+  if (!sn.done) CUDA_TRY(cudaEventCreateWithFlags(&sn.done, cudaEventDisableTiming));
+  s = queue_state_copy(d, L, sn.dev);
+  if (s) return s;
+  CUDA_TRY(cudaEventRecord(sn.ready, d->stream));
+  // the host copy runs on the output stream, beside the next steps
+  CUDA_TRY(cudaStreamWaitEvent(d->out_stream, sn.ready, 0));
+  CUDA_TRY(cudaMemcpyAsync(sn.host, sn.dev, sizeof(double) * L.count, cudaMemcpyDeviceToHost,
+                           d->out_stream));
+  CUDA_TRY(cudaEventRecord(sn.done, d->out_stream));
+  d->d2h_bytes += (int64_t)(sizeof(double) * L.count);
+  sn.state = 1;
+  d->snap_next = 1 - k;
+  *slot = k;
+  return WF_OK;
+}
+
+WF_API wf_status wf_write_snapshot_vtk(wf_domain *d, int32_t slot, const char *path) {
+  if (!d || !path || slot < 0 || slot > 1) return WF_ERR_ARG;
+  wf_domain::Snapshot &sn = d->snap[slot];
+  if (sn.state != 1) return fail(d, WF_ERR_STATE, "snapshot slot %d holds no state", slot);
+  CUDA_TRY(cudaSetDevice(d->device));
+  CUDA_TRY(cudaEventSynchronize(sn.done));
+  const SnapLayout L = snap_layout(d);
+  VtkView v;
+  vtk_static(d, v);
+  vtk_fields(d, L, sn.host, v);
+  sn.state = 0;
+  if (!write_vtk_text(path, v)) return fail(d, WF_ERR_ARG, "cannot write %s", path);
+  return WF_OK;
 }
 
 WF_API wf_status wf_get_reaction_history(wf_domain *d, double *out, int64_t cap, int64_t *n) {

@@ -1115,78 +1115,151 @@ WF_API wf_status wf_load_lsdyna(wf_domain *d, const char *path) {
 // the reference's VTKWriter (VTKWriter.C:246-650): point data DISP, Velocity,
 // Acceleration, nod_mass, ContForce and, with thermal coupling, Temp; cell data
 // pressure, pl_strain, Vol, Rho, sigy and the stress tensor SIGMA.
-WF_API wf_status wf_write_vtk(wf_domain *d, const char *path) {
-  if (!d || !path) return WF_ERR_ARG;
-  int64_t nn = 0, ne = 0, tot = 0;
-  int32_t npe = 0;
-  wf_status s = wf_get_sizes(d, &nn, &ne, &npe, &tot);
-  if (s) return s;
-  std::vector<double> x(3 * nn), u(3 * nn), v(3 * nn), a(3 * nn), cf(3 * nn), mass(nn);
-  std::vector<double> p(ne), pl(ne), vol(ne), rho(ne), sy(ne), sig(6 * ne);
-  std::vector<int32_t> el(ne * npe);
-  if ((s = wf_get_node_field(d, WF_NODE_X, x.data()))) return s;
-  if ((s = wf_get_node_field(d, WF_NODE_U, u.data()))) return s;
-  if ((s = wf_get_node_field(d, WF_NODE_V, v.data()))) return s;
-  if ((s = wf_get_node_field(d, WF_NODE_A, a.data()))) return s;
-  if ((s = wf_get_node_field(d, WF_NODE_CONTFORCE, cf.data()))) return s;
-  if ((s = wf_get_node_scalar(d, WF_NODE_MASS, mass.data()))) return s;
-  if ((s = wf_get_elem_scalar(d, WF_ELEM_P, p.data()))) return s;
-  if ((s = wf_get_elem_scalar(d, WF_ELEM_PL_STRAIN, pl.data()))) return s;
-  if ((s = wf_get_elem_scalar(d, WF_ELEM_VOL, vol.data()))) return s;
-  if ((s = wf_get_elem_scalar(d, WF_ELEM_RHO, rho.data()))) return s;
-  if ((s = wf_get_elem_scalar(d, WF_ELEM_SIGMA_Y, sy.data()))) return s;
-  if ((s = wf_get_elem_tensor(d, WF_ELEM_SIGMA, sig.data()))) return s;
-  if ((s = wf_get_connectivity(d, el.data(), nullptr, nullptr, nullptr, nullptr))) return s;
+// The reference's legacy VTK layout (VTKWriter::VTKWriter, VTKWriter.C:238-664):
+// the part's nodes and elements, then the rigid triangle meshes as extra
+// points and triangle cells; point data Position, DISP, Acceleration,
+// Velocity, Part_ID, Temp (thermal), ContForce, nod_mass, stress (von Mises of
+// the node-averaged stress), ext_nodes, nod_area, nod_p, SIGMAT (node-averaged
+// stress) and EPSR (node-averaged strain rate, when kept); cell data ele_area,
+// pressure, pl_strain, DDEVT (strain rate, when kept), J, Vol, Rho, Vol_0,
+// sigy. Node averages are plain means over the node's elements, summed in
+// element order (the reference's avgScalar). Tensors are written as the
+// reference writes them, upper triangle with zeros below. Die points and
+// triangles carry zeros (Part_ID 1, Temp the die temperature). Values are
+// printed with 9 significant digits.
+bool wf::write_vtk_text(const char *path, const wf::VtkView &v) {
+  const int64_t nn = v.nn, ne = v.ne, tn = v.tri_nn, te = v.tri_ne, npe = v.npe;
   FILE *f = std::fopen(path, "w");
-  if (!f) return WF_ERR_ARG;
+  if (!f) return false;
+  auto ten = [&](const double *t, bool soa, int64_t i, int64_t n, int c) {
+    return soa ? t[c * n + i] : t[6 * i + c];
+  };
+  // node averages of a 6-component element field, element order
+  auto node_avg = [&](const double *t, bool soa, std::vector<double> &out) {
+    out.assign(6 * nn, 0.0);
+    std::vector<int32_t> cnt(nn, 0);
+    for (int64_t e = 0; e < ne; e++)
+      for (int64_t q = 0; q < npe; q++) {
+        const int32_t n = v.elnod[e * npe + q];
+        for (int c = 0; c < 6; c++) out[6 * n + c] += ten(t, soa, e, ne, c);
+        cnt[n]++;
+      }
+    for (int64_t n = 0; n < nn; n++)
+      if (cnt[n] > 0)
+        for (int c = 0; c < 6; c++) out[6 * n + c] /= cnt[n];
+  };
   std::fprintf(f, "# vtk DataFile Version 3.0\nweldform-gb300 results\nASCII\n"
-                  "DATASET UNSTRUCTURED_GRID\nPOINTS %lld double\n", (long long)nn);
+                  "DATASET UNSTRUCTURED_GRID\nPOINTS %lld double\n", (long long)(nn + tn));
   for (int64_t n = 0; n < nn; n++)
-    std::fprintf(f, "%.17g %.17g %.17g\n", x[3 * n], x[3 * n + 1], x[3 * n + 2]);
-  std::fprintf(f, "CELLS %lld %lld\n", (long long)ne, (long long)(ne * (npe + 1)));
+    std::fprintf(f, "%.17g %.17g %.17g\n", v.x[3 * n], v.x[3 * n + 1], v.x[3 * n + 2]);
+  for (int64_t n = 0; n < tn; n++)
+    std::fprintf(f, "%.17g %.17g %.17g\n", v.tri_x[3 * n], v.tri_x[3 * n + 1],
+                 v.tri_x[3 * n + 2]);
+  std::fprintf(f, "CELLS %lld %lld\n", (long long)(ne + te), (long long)(ne * (npe + 1) + 4 * te));
   for (int64_t e = 0; e < ne; e++) {
-    std::fprintf(f, "%d", npe);
-    for (int q = 0; q < npe; q++) std::fprintf(f, " %d", el[e * npe + q]);
+    std::fprintf(f, "%d", (int)npe);
+    for (int64_t q = 0; q < npe; q++) std::fprintf(f, " %d", v.elnod[e * npe + q]);
     std::fprintf(f, "\n");
   }
-  std::fprintf(f, "CELL_TYPES %lld\n", (long long)ne);
+  for (int64_t e = 0; e < te; e++)
+    std::fprintf(f, "3 %lld %lld %lld\n", (long long)(v.tri_el[3 * e] + nn),
+                 (long long)(v.tri_el[3 * e + 1] + nn), (long long)(v.tri_el[3 * e + 2] + nn));
+  std::fprintf(f, "CELL_TYPES %lld\n", (long long)(ne + te));
   for (int64_t e = 0; e < ne; e++) std::fprintf(f, "%d\n", npe == 8 ? 12 : 10);
-  std::fprintf(f, "POINT_DATA %lld\n", (long long)nn);
-  auto vec = [&](const char *name, const std::vector<double> &w) {
+  for (int64_t e = 0; e < te; e++) std::fprintf(f, "5\n");
+  std::fprintf(f, "POINT_DATA %lld\n", (long long)(nn + tn));
+  auto vec = [&](const char *name, const double *w) {
     std::fprintf(f, "VECTORS %s double\n", name);
     for (int64_t n = 0; n < nn; n++)
       std::fprintf(f, "%.9g %.9g %.9g\n", w[3 * n], w[3 * n + 1], w[3 * n + 2]);
+    for (int64_t n = 0; n < tn; n++) std::fprintf(f, "0 0 0\n");
   };
-  vec("DISP", u);
-  vec("Velocity", v);
-  vec("Acceleration", a);
-  vec("ContForce", cf);
-  std::fprintf(f, "SCALARS nod_mass double 1\nLOOKUP_TABLE default\n");
-  for (int64_t n = 0; n < nn; n++) std::fprintf(f, "%.9g\n", mass[n]);
-  {
-    // temperature (VTKWriter.C:434-441), when the thermal coupling is on
-    std::vector<double> T(nn);
-    if (wf_get_node_scalar(d, WF_NODE_TEMP, T.data()) == WF_OK) {
-      std::fprintf(f, "SCALARS Temp double 1\nLOOKUP_TABLE default\n");
-      for (int64_t n = 0; n < nn; n++) std::fprintf(f, "%.9g\n", T[n]);
-    }
-  }
-  std::fprintf(f, "CELL_DATA %lld\n", (long long)ne);
-  auto scal = [&](const char *name, const std::vector<double> &w) {
+  // scalar per node (w null: zeros) with the die points' value after it
+  auto nscal = [&](const char *name, const double *w, double die) {
     std::fprintf(f, "SCALARS %s double 1\nLOOKUP_TABLE default\n", name);
-    for (int64_t e = 0; e < ne; e++) std::fprintf(f, "%.9g\n", w[e]);
+    for (int64_t n = 0; n < nn; n++) std::fprintf(f, "%.9g\n", w ? w[n] : 0.0);
+    for (int64_t n = 0; n < tn; n++) std::fprintf(f, "%.9g\n", die);
   };
-  scal("pressure", p);
-  scal("pl_strain", pl);
-  scal("Vol", vol);
-  scal("Rho", rho);
-  scal("sigy", sy);
-  std::fprintf(f, "TENSORS SIGMA double\n");
-  for (int64_t e = 0; e < ne; e++) {
-    const double *t = &sig[6 * e];  // xx yy zz xy yz xz
-    std::fprintf(f, "%.9g %.9g %.9g\n%.9g %.9g %.9g\n%.9g %.9g %.9g\n\n", t[0], t[3], t[5], t[3],
-                 t[1], t[4], t[5], t[4], t[2]);
+  auto tens = [&](const char *name, const std::vector<double> &t, int64_t count, int64_t dummies) {
+    std::fprintf(f, "TENSORS %s double\n", name);
+    for (int64_t i = 0; i < count; i++) {
+      const double *q = &t[6 * i];  // xx yy zz xy yz xz
+      std::fprintf(f, "%.9g %.9g %.9g\n0 %.9g %.9g\n0 0 %.9g\n", q[0], q[3], q[5], q[1], q[4],
+                   q[2]);
+    }
+    for (int64_t i = 0; i < dummies; i++) std::fprintf(f, "0 0 0\n0 0 0\n0 0 0\n");
+  };
+  vec("Position", v.x);
+  vec("DISP", v.u);
+  vec("Acceleration", v.a);
+  vec("Velocity", v.v);
+  nscal("Part_ID", nullptr, 1.0);
+  if (v.T) nscal("Temp", v.T, v.T_die);
+  vec("ContForce", v.cf);
+  nscal("nod_mass", v.mass, 0.0);
+  std::vector<double> avg;
+  node_avg(v.sig, v.sig_soa, avg);
+  {
+    std::vector<double> seq(nn);
+    for (int64_t n = 0; n < nn; n++) {
+      const double *s6 = &avg[6 * n];
+      const double tr = (s6[0] + s6[1] + s6[2]) / 3.0;
+      const double dx = s6[0] - tr, dy = s6[1] - tr, dz = s6[2] - tr;
+      const double J2 = 0.5 * (dx * dx + 2.0 * s6[3] * s6[3] + 2.0 * s6[5] * s6[5] + dy * dy +
+                               2.0 * s6[4] * s6[4] + dz * dz);
+      seq[n] = std::sqrt(3.0 * J2);
+    }
+    nscal("stress", seq.data(), 0.0);
   }
-  const bool ok = std::fclose(f) == 0;
-  return ok ? WF_OK : WF_ERR_ARG;
+  {
+    std::vector<double> ext(nn, 0.0);
+    if (v.ext)
+      for (int64_t n = 0; n < nn; n++) ext[n] = v.ext[n] ? 1.0 : 0.0;
+    nscal("ext_nodes", ext.data(), 0.0);
+  }
+  nscal("nod_area", v.area, 0.0);
+  {
+    // calcNodalPressureFromElemental (Mechanical.C:1187-1213): volume-weighted
+    // mean of the element pressures, element order
+    std::vector<double> pn(nn, 0.0), wsum(nn, 0.0);
+    for (int64_t e = 0; e < ne; e++)
+      for (int64_t q = 0; q < npe; q++) {
+        const int32_t n = v.elnod[e * npe + q];
+        pn[n] += v.p[e] * v.vol[e];
+        wsum[n] += v.vol[e];
+      }
+    for (int64_t n = 0; n < nn; n++)
+      if (wsum[n] > 0.0) pn[n] /= wsum[n];
+    nscal("nod_p", pn.data(), 0.0);
+  }
+  tens("SIGMAT", avg, nn, tn);
+  if (v.sr) {
+    node_avg(v.sr, v.sr_soa, avg);
+    tens("EPSR", avg, nn, tn);
+  }
+  std::fprintf(f, "CELL_DATA %lld\n", (long long)(ne + te));
+  auto escal = [&](const char *name, const double *w) {
+    std::fprintf(f, "SCALARS %s double 1\nLOOKUP_TABLE default\n", name);
+    for (int64_t e = 0; e < ne; e++) std::fprintf(f, "%.9g\n", w ? w[e] : 0.0);
+    for (int64_t e = 0; e < te; e++) std::fprintf(f, "0\n");
+  };
+  escal("ele_area", nullptr);
+  escal("pressure", v.p);
+  escal("pl_strain", v.pl);
+  if (v.sr) {
+    std::vector<double> d6(6 * ne);
+    for (int64_t e = 0; e < ne; e++)
+      for (int c = 0; c < 6; c++) d6[6 * e + c] = ten(v.sr, v.sr_soa, e, ne, c);
+    tens("DDEVT", d6, ne, te);
+  }
+  {
+    std::vector<double> J(ne);
+    for (int64_t e = 0; e < ne; e++) J[e] = v.vol[e] / v.vol0[e];
+    escal("J", J.data());
+  }
+  escal("Vol", v.vol);
+  escal("Rho", v.rho);
+  escal("Vol_0", v.vol0);
+  escal("sigy", v.sy);
+  return std::fclose(f) == 0;
 }

@@ -226,6 +226,31 @@ struct TileParams {
   int64_t shared_slots;    // node-list entries of the shared nodes (host-side statistic)
 };
 
+// Host-side view of one state for the legacy VTK writer (write_vtk_text,
+// wf_deck.cpp). Node vectors are AoS [nn][3]; element tensors hold 6 values
+// per element (Voigt xx yy zz xy yz xz), AoS [ne][6] or SoA [6][ne]. Null
+// optional arrays are written as zeros (or left out: T, sr).
+struct VtkView {
+  int64_t nn = 0, ne = 0;
+  int32_t npe = 0;
+  const double *x = nullptr, *u = nullptr, *v = nullptr, *a = nullptr, *cf = nullptr;
+  const double *mass = nullptr, *T = nullptr;         // T: thermal coupling only
+  const double *p = nullptr, *pl = nullptr, *vol = nullptr, *vol0 = nullptr;
+  const double *rho = nullptr, *sy = nullptr;
+  const double *sig = nullptr, *sr = nullptr;         // sr: FP64 step only
+  bool sig_soa = false, sr_soa = false;
+  const int32_t *elnod = nullptr;                     // [ne][npe]
+  const uint8_t *ext = nullptr;                       // external-surface flags (contact)
+  const double *area = nullptr;                       // external-surface area shares
+  int64_t tri_nn = 0, tri_ne = 0;                     // rigid triangle meshes (contact)
+  const double *tri_x = nullptr;                      // [tri_nn][3]
+  const int32_t *tri_el = nullptr;                    // [tri_ne][3]
+  double T_die = 0.0;
+};
+// Writes the view as the reference's legacy VTK writer lays it out
+// (VTKWriter.C:238-664: same blocks, names and order); false on an I/O error.
+bool write_vtk_text(const char *path, const VtkView &v);
+
 // Records `msg` as the domain's last error and returns s (wf_api.cu).
 wf_status domain_fail(wf_domain *d, wf_status s, const std::string &msg);
 

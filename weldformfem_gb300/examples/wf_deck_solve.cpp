@@ -1,7 +1,8 @@
 // Runs a JSON deck of the reference's explicit driver on the GPU: the
 // counterpart of `weldform_exp deck.json` (src/explicit/main.C:125-1005 then
 // Domain_d::SolveChungHulbert). Writes <deck>_NNNNN.vtk at t = 0 and every
-// outTime, <deck>_res.json listing them (ResultsJson, Solver_explicit.C:48-78)
+// outTime (from snapshots, written while the next steps run), <deck>_res.json
+// listing them (ResultsJson, Solver_explicit.C:48-78)
 // and, with --energy, <deck>_energy.csv with t, Eint, Ekin per step; prints a
 // one-line JSON summary.
 //
@@ -58,12 +59,18 @@ int main(int argc, char **argv) {
   const auto t0 = std::chrono::steady_clock::now();
   if ((s = wf_init(d))) return fail(d, s, "wf_init");
   std::vector<std::pair<std::string, double>> files;
-  auto write = [&](double t) -> wf_status {
-    if (!vtk) return WF_OK;
+  // outputs go through snapshots: the state of an output time is copied to
+  // host memory beside the next steps, and its file is written while the GPU
+  // runs them (the reference loop stops for each output instead)
+  int32_t pending = -1;
+  double pending_t = 0.0;
+  auto flush = [&]() -> wf_status {
+    if (pending < 0) return WF_OK;
     const std::string f = vtk_name(base, (int)files.size());
-    const wf_status ws = wf_write_vtk(d, f.c_str());
+    const wf_status ws = wf_write_snapshot_vtk(d, pending, f.c_str());
+    pending = -1;
     if (ws) return ws;
-    files.emplace_back(f, t);
+    files.emplace_back(f, pending_t);
     FILE *j = std::fopen((base + "_res.json").c_str(), "w");
     if (j) {
       std::fprintf(j, "{\n  \"vtk_files\": [\n");
@@ -75,7 +82,17 @@ int main(int argc, char **argv) {
     }
     return WF_OK;
   };
-  if ((s = write(0.0))) return fail(d, s, "wf_write_vtk");
+  auto write = [&](double t) -> wf_status {
+    if (!vtk) return WF_OK;
+    int32_t slot = -1;
+    wf_status ws = wf_snapshot(d, &slot);   // queued after the steps run so far
+    if (ws) return ws;
+    ws = flush();                           // the previous output, written meanwhile
+    pending = slot;
+    pending_t = t;
+    return ws;
+  };
+  if ((s = write(0.0))) return fail(d, s, "wf_snapshot");
   // the loop runs while Time < end time; outputs when Time reaches tout
   double t = 0.0, tout = info.out_time > 0.0 ? info.out_time : info.end_time;
   int64_t steps = 0;
@@ -91,11 +108,11 @@ int main(int argc, char **argv) {
     int64_t st = 0;
     wf_get_time(d, &t, &st);
     if (t >= tout || t >= info.end_time) {
-      if ((s = wf_sync(d))) return fail(d, s, "wf_sync");
-      if ((s = write(t))) return fail(d, s, "wf_write_vtk");
+      if ((s = write(t))) return fail(d, s, "wf_snapshot");
       while (tout <= t) tout += info.out_time > 0.0 ? info.out_time : info.end_time;
     }
   }
+  if ((s = flush())) return fail(d, s, "wf_write_snapshot_vtk");
   if ((s = wf_sync(d))) return fail(d, s, "wf_sync");
   const double secs =
       std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
