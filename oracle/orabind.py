@@ -285,24 +285,24 @@ class OracleDomain:
     def step_end(self):
         lib().wfo_step_end(self.h)
 
-    def elem_forces(self, e0, e1):
+    def halo_forces(self, e0, e1):
         """Element and hourglass forces of elements [e0, e1), flat."""
         out = np.zeros(2 * (e1 - e0) * self.npe * 3)
         self._check(lib().wfo_get_elem_forces_range(self.h, int(e0), int(e1), out), "elem forces")
         return out
 
-    def set_elem_forces(self, e0, e1, data):
+    def set_halo_forces(self, e0, e1, data):
         self._check(lib().wfo_set_elem_forces_range(self.h, int(e0), int(e1),
                                               np.ascontiguousarray(data, np.float64)),
                     "set elem forces")
 
-    def node_state(self, n0, n1):
+    def halo_nodes(self, n0, n1):
         """Node state of nodes [n0, n1), flat."""
         out = np.zeros(15 * (n1 - n0))
         self._check(lib().wfo_get_node_state_range(self.h, int(n0), int(n1), out), "node state")
         return out
 
-    def set_node_state_range(self, n0, n1, data):
+    def set_halo_nodes(self, n0, n1, data):
         self._check(lib().wfo_set_node_state_range(self.h, int(n0), int(n1),
                                              np.ascontiguousarray(data, np.float64)),
                     "set node state")

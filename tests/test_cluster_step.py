@@ -80,8 +80,13 @@ def test_automatic_mode_and_fallbacks():
     W.apply(d, big)
     d.init()
     assert d.step_mode()[0] == 1
-    d.set_step_mode(3)
-    assert d.step_mode()[0] == 3            # tiled hexahedra
+    d.set_step_mode(3)                      # tiles are built by init: not after it
+    assert d.step_mode()[0] == 1
+    t = wf.Domain(wf.WF_MIXED)
+    W.apply(t, big)
+    t.set_step_mode(3)
+    t.init()
+    assert t.step_mode()[0] == 3            # tiled hexahedra
     d.set_step_mode(2)
     assert d.step_mode()[0] == 2
     with pytest.raises(wf.WfError):

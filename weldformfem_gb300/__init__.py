@@ -389,22 +389,22 @@ class Domain:
     def step_end(self):
         self._call("wf_step_end")
 
-    def elem_forces(self, e0, e1):
+    def halo_forces(self, e0, e1):
         """Element and hourglass forces of elements [e0, e1), flat."""
         out = np.zeros(2 * (e1 - e0) * self.npe * 3)
         self._call("wf_get_halo_forces", int(e0), int(e1), out)
         return out
 
-    def set_elem_forces(self, e0, e1, data):
+    def set_halo_forces(self, e0, e1, data):
         self._call("wf_set_halo_forces", int(e0), int(e1), np.ascontiguousarray(data, np.float64))
 
-    def node_state(self, n0, n1):
+    def halo_nodes(self, n0, n1):
         """Node state a step starts from, nodes [n0, n1), flat."""
         out = np.zeros(12 * (n1 - n0))
         self._call("wf_get_halo_nodes", int(n0), int(n1), out)
         return out
 
-    def set_node_state_range(self, n0, n1, data):
+    def set_halo_nodes(self, n0, n1, data):
         self._call("wf_set_halo_nodes", int(n0), int(n1), np.ascontiguousarray(data, np.float64))
 
     def solve(self):
