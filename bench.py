@@ -326,15 +326,24 @@ def run_ours(args):
     t0 = time.perf_counter()
     de = wf.Domain(wf.WF_MIXED, device=device)
     de.set_mesh(x, elnod)
+    t_mesh = time.perf_counter()
     W.apply_options(de, case, x=x, set_dt=False, bcs=bcs)
+    t_opts = time.perf_counter()
     de.init()
+    t_init = time.perf_counter()
     de.set_dt(W.cfl_dt(case, de.min_edge_length()))   # CFL step from the device reduction
     t_setup = time.perf_counter() - t0
     de.run(K)
+    de.sync()
+    t_run = time.perf_counter()
     u_host = de.node_vec("u")
     r_host = de.reaction()
     de.sync()
     t_e2e = time.perf_counter() - t0
+    e2e_parts = {"set_mesh": round(t_mesh - t0, 4), "options_bcs": round(t_opts - t_mesh, 4),
+                 "init": round(t_init - t_opts, 4), "cfl_dt": round(t0 + t_setup - t_init, 4),
+                 "steps": round(t_run - t0 - t_setup, 4),
+                 "readback": round(t0 + t_e2e - t_run, 4)}
     h2d, d2h = de.transfer_bytes()
     assert u_host.shape[0] == case.n_node and r_host.shape[0] == K
     del de
@@ -403,6 +412,7 @@ def run_ours(args):
             "e2e": {"value": round(E * K / t_e2e, 1), "unit": UNIT,
                     "h2d_bytes_per_step": int(h2d / K), "d2h_bytes_per_step": int(d2h / K),
                     "seconds": round(t_e2e, 3), "setup_seconds": round(t_setup, 3),
+                    "parts_seconds": e2e_parts,
                     "setup_share": round(t_setup / t_e2e, 3),
                     "includes": "mesh + BC upload, init (launch shapes from the library's "
                                 "per-process autotune cache: an earlier domain of this size "

@@ -166,3 +166,28 @@ def test_adjoint_rejects_unsupported():
     with pytest.raises(wf.WfError) as e:
         d.adjoint_backward(np.zeros(10))
     assert e.value.status == 2
+
+
+@pytest.mark.gpu
+def test_adjoint_full_c4_against_oracle_finite_differences():
+    """Configuration 4 as specified (32^3 hexahedra, 8 octant materials, 4000
+    steps, checkpoints every 64 steps): two gradient components against
+    central differences of the CPU oracle (the FP64 restatement of the
+    reference step), each within 1e-3 of the difference quotient."""
+    c = W.config(4)
+    c.dt = c.time_step()
+    n = c.steps
+    th0 = W.material_params(c)
+    Rstar = oracle_reaction(c, th0 * W.target_factors(c), n)
+    R, d = A.solve_with_adjoint(c, th0, n, every=64)
+    assert H.rel_err(R, oracle_reaction(c, th0, n)) <= 1e-9
+    g = d.adjoint_backward(2.0 * (R - Rstar))
+    for i, k in ((0, 0), (5, 1)):          # E of octant 0, sigma_y0 of octant 5
+        h = REL_STEP * th0[i, k]
+        tp, tm = th0.copy(), th0.copy()
+        tp[i, k] += h
+        tm[i, k] -= h
+        Lp = np.sum((oracle_reaction(c, tp, n) - Rstar) ** 2)
+        Lm = np.sum((oracle_reaction(c, tm, n) - Rstar) ** 2)
+        gfd = (Lp - Lm) / (2 * h)
+        assert abs(g[i, k] - gfd) <= 1e-3 * abs(gfd), (i, k, g[i, k], gfd)

@@ -125,3 +125,32 @@ def test_batched_rejects_bad_tables():
     with pytest.raises(wf.WfError) as e:
         d.set_specimens(eoff, bad, b.dts())
     assert e.value.status == 1
+
+
+@pytest.mark.gpu
+def test_specimen_shards_equal_the_whole_batch():
+    """bench.py's C3 sharding: each rank runs a contiguous block of the
+    specimens as its own batched domain. Every specimen computes exactly what
+    it computes in the whole batch, so the shards' displacements and
+    per-specimen reactions equal the whole batch's bit for bit."""
+    import bench
+
+    full = W.ensemble(n_spec=9, nmin=3, nmax=7, steps=120)
+    steps = 120
+    whole = wf.Domain(wf.WF_MIXED)
+    W.apply_batch(whole, full)
+    whole.init()
+    whole.run(steps)
+    u = whole.node_vec("u")
+    _, noff = full.offsets()
+    world = 2
+    for rank in range(world):
+        lo, hi = bench.shard(len(full.cases), rank, world)
+        part = W.Batch(full.name, full.cases[lo:hi], full.hg)
+        d = wf.Domain(wf.WF_MIXED)
+        W.apply_batch(d, part)
+        d.init()
+        d.run(steps)
+        np.testing.assert_array_equal(d.node_vec("u"), u[noff[lo]:noff[hi]])
+        for s in range(hi - lo):
+            np.testing.assert_array_equal(d.specimen_reaction(s), whole.specimen_reaction(lo + s))

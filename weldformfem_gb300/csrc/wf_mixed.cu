@@ -214,10 +214,25 @@ __device__ __forceinline__ void geometry_one(const StepParams &P, const MixState
 
 // Launch shapes are chosen at run time by the autotuner (wf_api.cu): block
 // size BS and a grid-stride loop (several elements per thread).
+// Two elements per iteration when the grid strides (a persistent grid or
+// several items per thread): both elements' coordinate gathers are issued
+// before either's arithmetic, so twice the loads are in flight.
 template <int NPE, int BS, bool BOX>
 __global__ void __launch_bounds__(BS) k_mix_geometry(StepParams P, MixState M, float *vol) {
-  for (int64_t e = (int64_t)blockIdx.x * BS + threadIdx.x; e < P.ne; e += (int64_t)gridDim.x * BS)
-    geometry_one<NPE, false, BOX>(P, M, vol, e);
+  const int64_t stride = (int64_t)gridDim.x * BS;
+  int64_t e = (int64_t)blockIdx.x * BS + threadIdx.x;
+  for (; e + stride < P.ne; e += 2 * stride) {
+    float r0[NPE][3], r1[NPE][3];
+    int32_t n0[NPE], n1[NPE];
+    rel_coords<NPE, false, BOX>(P, M, e, r0, n0);
+    rel_coords<NPE, false, BOX>(P, M, e + stride, r1, n1);
+    float J0[3][3], J1[3][3];
+    jacobian_f<NPE>(r0, J0);
+    jacobian_f<NPE>(r1, J1);
+    vol[e] = det3f(J0) * weightf<NPE>();
+    vol[e + stride] = det3f(J1) * weightf<NPE>();
+  }
+  if (e < P.ne) geometry_one<NPE, false, BOX>(P, M, vol, e);
 }
 
 // Rigid triangle-mesh contact of one external node in FP32 (the FP64 step's
@@ -306,14 +321,16 @@ __device__ __forceinline__ void tri_contact_mixed(const StepParams &P, const Mix
 // Nodal volumes -> J ratio and lumped mass; for contact candidates also the
 // rigid-plane contact force (it needs only x, the predicted velocity and the
 // step's mass, all final here, so it is computed before the element phase).
+// Nodal phase of one node, in two parts: nodal_gather sums the volumes of the
+// node's elements in list order (and loads its constants), nodal_rest forms
+// the J ratio, the lumped mass and, for contact candidates, the contact force.
 // zd: the rigid plane's height at the step's time as a (hi, lo) float pair,
 // formed once per thread by the caller (die_height), so that the gap of a
 // contact node takes no FP64 instruction.
 template <int NPE, bool CG, bool BOX = false>
-__device__ __forceinline__ void nodal_one(const StepParams &P, const MixState &M,
-                                          const float *vol, int64_t n, float2 zd) {
-  float s = 0.0f;
-  float2 nc;
+__device__ __forceinline__ void nodal_gather(const StepParams &P, const MixState &M,
+                                             const float *vol, int64_t n, float &s, float2 &nc) {
+  s = 0.0f;
   if constexpr (BOX && NPE == 8) {
     // the node's elements in list order, computed from its indices
     int32_t el[8], cor[8];
@@ -339,6 +356,13 @@ __device__ __forceinline__ void nodal_one(const StepParams &P, const MixState &M
       for (int j = 0; j < 8; j++) s += g[j];
     }
   }
+}
+
+// The rest of a node's nodal phase from its volume sum s and constants nc:
+// J ratio, lumped mass, contact force.
+template <int NPE, bool CG>
+__device__ __forceinline__ void nodal_rest(const StepParams &P, const MixState &M, int64_t n,
+                                           float s, float2 nc, float2 zd) {
   M.jr[n] = s * nc.x;
   float mass;
   if (P.mass_mode == 0) {
@@ -388,11 +412,31 @@ __device__ __forceinline__ void nodal_one(const StepParams &P, const MixState &M
   }
 }
 
+template <int NPE, bool CG, bool BOX = false>
+__device__ __forceinline__ void nodal_one(const StepParams &P, const MixState &M,
+                                          const float *vol, int64_t n, float2 zd) {
+  float s;
+  float2 nc;
+  nodal_gather<NPE, CG, BOX>(P, M, vol, n, s, nc);
+  nodal_rest<NPE, CG>(P, M, n, s, nc, zd);
+}
+
+// Two nodes per iteration when the grid strides: both nodes' volume gathers
+// are in flight before either's rest.
 template <int NPE, int BS, bool BOX>
 __global__ void __launch_bounds__(BS) k_mix_nodal(StepParams P, MixState M, const float *vol) {
   const float2 zd = die_height(P, P.st->time);
-  for (int64_t n = (int64_t)blockIdx.x * BS + threadIdx.x; n < P.nn; n += (int64_t)gridDim.x * BS)
-    nodal_one<NPE, false, BOX>(P, M, vol, n, zd);
+  const int64_t stride = (int64_t)gridDim.x * BS;
+  int64_t n = (int64_t)blockIdx.x * BS + threadIdx.x;
+  for (; n + stride < P.nn; n += 2 * stride) {
+    float s0, s1;
+    float2 c0, c1;
+    nodal_gather<NPE, false, BOX>(P, M, vol, n, s0, c0);
+    nodal_gather<NPE, false, BOX>(P, M, vol, n + stride, s1, c1);
+    nodal_rest<NPE, false>(P, M, n, s0, c0, zd);
+    nodal_rest<NPE, false>(P, M, n + stride, s1, c1, zd);
+  }
+  if (n < P.nn) nodal_one<NPE, false, BOX>(P, M, vol, n, zd);
 }
 
 // Jaumann rate + radial return, shared by both element types. The
