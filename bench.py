@@ -57,8 +57,24 @@ ALG_BYTES_HEX_MIXED_BOX = {"geometry": (4, 24), "nodal": (4, 16), "elements": (1
                            "nodes": (96, 117)}
 KERNEL_NAMES = {"geometry": "k_mix_geometry", "nodal": "k_mix_nodal",
                 "elements": "k_mix_elements", "nodes": "k_mix_nodes",
-                "tile": "k_mix_tile", "shared": "k_mix_shared"}
+                "tile": "k_mix_tile", "shared": "k_mix_shared", "sweep": "k_mix_sweep",
+                "flow": "k_mix_flow"}
 TILED_PHASES = ["geometry", "nodal", "tile", "shared"]
+# column sweep (box meshes): element and node phases in one kernel, the
+# element forces kept in shared memory
+#   sweep: deviatoric stress RW 48 E + plastic strain RW 8 E
+#          + staged node inputs 40 N (positions 24, predicted velocity 12, J ratio 4)
+#          + node update 93 N (BC code, flags, mass 9; velocity RW 24, accel RW 24;
+#            positions 24 and predicted velocity 12 written)
+ALG_BYTES_SWEEP = {"sweep": (56, 133)}
+SWEEP_PHASES = ["geometry", "nodal", "sweep"]
+# dataflow step (box meshes): the four phases in one persistent kernel; every
+# array touched once, the intermediates written once (read back from L2)
+#   flow: deviatoric stress RW 48 E + plastic strain RW 8 E + volume 4 E
+#         + element forces 96 E; positions RW 48 N + predicted velocity RW 24 N
+#         + velocity RW 24 N + accel RW 24 N + node constants 8 N + BC code and
+#         flags 5 N + J ratio 4 N + mass 4 N
+ALG_BYTES_FLOW = {"flow": (156, 141)}
 
 
 def tiled_alg_bytes(E, N, stats):
@@ -364,6 +380,18 @@ def run_ours(args):
     if mode == 3:
         phases = TILED_PHASES
         phase_bytes["tile"], phase_bytes["shared"] = tiled_alg_bytes(E, case.n_node, tile_stats)
+    elif mode == 5:
+        # the dataflow step is timed as the element phase
+        phases = ["flow"]
+        ms_phase = ms_phase[2:3]
+        phase_bytes["flow"] = ALG_BYTES_FLOW["flow"][0] * E + ALG_BYTES_FLOW["flow"][1] * case.n_node
+    elif mode == 4:
+        # the sweep is timed as the element phase; the node phase's slot times
+        # no kernel of the step
+        phases = SWEEP_PHASES
+        ms_phase = ms_phase[:3]
+        phase_bytes["sweep"] = ALG_BYTES_SWEEP["sweep"][0] * E + \
+            ALG_BYTES_SWEEP["sweep"][1] * case.n_node
     dom = int(np.argmax(ms_phase))
     ph = phases[dom]
     alg_bytes = phase_bytes[ph]
@@ -442,11 +470,17 @@ def step_mode_label(mode, cl_blocks, cl_bs, K, graph_replays, launches, tile_sta
                 "note": "roofline phases are the per-phase kernels, timed apart"}
     full, rem = divmod(K, 32)
     kernels = ("geometry, nodal, tiled element+assembly, shared-node kernels" if mode == 3
+               else "geometry, nodal, column-sweep kernels" if mode == 4
+               else "dataflow kernel (one persistent launch per step)" if mode == 5
                else "per-phase kernels")
     extra = {}
     if mode == 3 and tile_stats:
         extra = {"tiles": tile_stats[0], "shared_nodes": tile_stats[1],
                  "threads_per_tile": cl_bs}
+    if mode == 4:
+        extra = {"columns": cl_blocks, "threads_per_column": cl_bs}
+    if mode == 5:
+        extra = {"blocks": cl_blocks, "threads_per_block": cl_bs}
     return {**extra, "mode": f"{kernels} replayed from CUDA graphs" if graph_replays
             else f"{kernels}, direct launches",
             "graph_replays": int(graph_replays),
@@ -770,6 +804,10 @@ def run_profile_case(args):
         d.set_step_mode(args.step_mode)
     if args.no_box:
         d.set_box_indexing(False)
+    if args.sweep_rows:
+        d.set_sweep_rows(args.sweep_rows)
+    if args.flow_tiles:
+        d.set_flow_tiles(*args.flow_tiles)
     d.init()
     d.run(args.warmup)
     d.sync()
@@ -806,7 +844,12 @@ def main():
                     help="bare run of one domain for kernel profiles (no other measurement)")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--step-mode", type=int, default=None,
-                    help="profiling runs: step mode (1 per-phase, 2 cluster, 3 tiled)")
+                    help="profiling runs: step mode (1 per-phase, 2 cluster, 3 tiled, 4 sweep, "
+                         "5 dataflow)")
+    ap.add_argument("--sweep-rows", type=int, default=0, choices=[0, 4, 8],
+                    help="profiling runs: node rows per column of the column sweep")
+    ap.add_argument("--flow-tiles", type=int, nargs=2, default=None,
+                    help="profiling runs: dataflow tile size and node-update lag")
     ap.add_argument("--no-box", action="store_true",
                     help="profiling runs: read the connectivity arrays on box meshes too")
     ap.add_argument("--phase-steps", type=int, default=0,

@@ -358,11 +358,50 @@ WF_API wf_status wf_set_launch_config(wf_domain *d, int32_t phase, int32_t block
  * state is bitwise that of mode 1; the reaction sum runs in another order.
  * Not with specimens, thermal coupling, the energy history or triangle-mesh
  * contact; the tiles are built by wf_init when mode 3 is set before it, and
- * wf_get_tiles tells whether the mesh was tiled. Mode 0 (default)
- * picks mode 2 for meshes of at most 3000 elements, else mode 1. wf_get_step_mode reports the mode the next
- * wf_run uses and, for mode 2, the cluster's blocks and block size, for mode
- * 3 the tiles and threads per tile (0 otherwise). */
+ * wf_get_tiles tells whether the mesh was tiled. Mode 4 (box meshes of
+ * hexahedra, see wf_set_box_indexing): the element and node phases become one
+ * column sweep. The node grid is cut into columns of at most 31 x 8 nodes
+ * (x, y; or 31 x 4, wf_set_sweep_rows), one block each, which sweeps its
+ * column's element layers upwards with the element forces in shared memory:
+ * it computes the elements around its nodes (those of the neighbouring
+ * columns' ring included, again), and each node adds its eight element forces
+ * in list order, so the state is bitwise that of mode 1; the reaction sum
+ * runs in another order. Positions, predicted velocities, tau and eps_p are
+ * held twice (read one copy, write the other). Not with specimens, thermal
+ * coupling or triangle-mesh contact; wf_get_sweep tells whether the mesh is
+ * swept. Mode 5 (the same meshes): each step is one persistent launch that
+ * runs the four phases as a wavefront through the element layers. The work is
+ * cut into tiles of 512 elements or nodes of one layer or plane (wf_set_flow_
+ * tiles); blocks take tiles in a fixed ticket order (geometry of layer s,
+ * nodal phase of plane s-1, element phase of layer s-2, node update of plane
+ * s-lag) and wait, with bounded waits, for the tiles they read, so the element
+ * forces are read back from L2 shortly after they are written. Each element
+ * and node runs mode 1's arithmetic: the state is bitwise that of mode 1; the
+ * reaction sum runs in another order. A wait that runs out (a bug, never
+ * expected) makes the next wf_sync return WF_ERR_CUDA. On GB300 mode 5 is
+ * slower than modes 4 and 1 (the blocks' waits and ticket traffic cost more
+ * than the L2 reuse saves) and is only run when asked for. Mode 0 (default)
+ * picks mode 2 for meshes of at most 3000 elements, else mode 4 where the mesh
+ * is swept, else mode 1. wf_get_step_mode reports the mode the next wf_run uses and,
+ * for mode 2, the cluster's blocks and block size, for mode 3 the tiles and
+ * threads per tile, for mode 4 the columns and threads per column, for mode 5
+ * the blocks and threads per block (0 otherwise). */
 WF_API wf_status wf_set_step_mode(wf_domain *d, int32_t mode);
+/* No counterpart in the reference. Node rows per column of the column sweep
+ * (4 or 8, default 8), before wf_init. wf_get_sweep: the columns along x and
+ * y and the rows per column, or zeros and, in why (NUL-terminated, at most
+ * why_cap bytes), the reason the mesh is not swept. Any output may be NULL. */
+WF_API wf_status wf_set_sweep_rows(wf_domain *d, int32_t rows);
+/* No counterpart in the reference. Dataflow step (mode 5): items per tile (a
+ * multiple of 256, 256 to 8192; default 512) and the stages the node update
+ * lags the geometry (3 to 16; default 12), before wf_init. wf_get_flow: tiles
+ * per step and blocks per launch, or zeros and, in why, the reason the mesh
+ * has no dataflow step. Any output may be NULL. */
+WF_API wf_status wf_set_flow_tiles(wf_domain *d, int32_t tile, int32_t lag);
+WF_API wf_status wf_get_flow(const wf_domain *d, int32_t *tiles, int32_t *grid, char *why,
+                             int64_t why_cap);
+WF_API wf_status wf_get_sweep(const wf_domain *d, int32_t *columns_x, int32_t *columns_y,
+                              int32_t *rows, char *why, int64_t why_cap);
 /* No counterpart in the reference. Box meshes: when the connectivity is the
  * AddBoxLength numbering of nx x ny x nz hexahedra (checked element by element
  * at wf_init, however the mesh was uploaded), the mixed-precision kernels

@@ -31,8 +31,10 @@ def test_clean_run_syncs_ok(prec):
     assert np.all(np.isfinite(d.node_vec("u")))
 
 
-@pytest.mark.parametrize("prec,mode", [(wf.WF_FP64, 1), (wf.WF_MIXED, 1), (wf.WF_MIXED, 2)],
-                         ids=["fp64", "mixed-per-phase", "mixed-cluster"])
+@pytest.mark.parametrize("prec,mode", [(wf.WF_FP64, 1), (wf.WF_MIXED, 1), (wf.WF_MIXED, 2),
+                                       (wf.WF_MIXED, 4), (wf.WF_MIXED, 5)],
+                         ids=["fp64", "mixed-per-phase", "mixed-cluster", "mixed-sweep",
+                              "mixed-flow"])
 def test_nan_velocity_bc_is_reported(prec, mode):
     case = small_case()
     d = wf.Domain(prec)

@@ -134,6 +134,12 @@ _SIGS = {
     "wf_get_step_mode": [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                          C.POINTER(C.c_int32)],
     "wf_set_box_indexing": [C.c_void_p, C.c_int32],
+    "wf_set_sweep_rows": [C.c_void_p, C.c_int32],
+    "wf_set_flow_tiles": [C.c_void_p, C.c_int32, C.c_int32],
+    "wf_get_flow": [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_char_p,
+                    C.c_int64],
+    "wf_get_sweep": [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                     C.POINTER(C.c_int32), C.c_char_p, C.c_int64],
     "wf_get_box": [C.c_void_p, _ip],
     "wf_get_tiles": [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                      C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.c_char_p, C.c_int64],
@@ -441,7 +447,8 @@ class Domain:
         self._call("wf_set_autotune", int(bool(on)))
 
     def set_step_mode(self, mode):
-        """0 automatic, 1 per-phase kernels, 2 one cluster launch per run, 3 tiled."""
+        """0 automatic, 1 per-phase kernels, 2 one cluster launch per run, 3 tiled,
+        4 column sweep, 5 dataflow step (4 and 5: box meshes)."""
         self._call("wf_set_step_mode", int(mode))
 
     def set_box_indexing(self, on=True):
@@ -453,6 +460,28 @@ class Domain:
         dims = np.zeros(3, np.int32)
         self._call("wf_get_box", dims)
         return tuple(int(v) for v in dims)
+
+    def set_sweep_rows(self, rows):
+        """Node rows per column of the column sweep, 4 or 8 (before init)."""
+        self._call("wf_set_sweep_rows", int(rows))
+
+    def sweep(self):
+        """(columns along x, columns along y, node rows per column, why not swept)."""
+        cx, cy, r = C.c_int32(), C.c_int32(), C.c_int32()
+        buf = C.create_string_buffer(256)
+        self._call("wf_get_sweep", C.byref(cx), C.byref(cy), C.byref(r), buf, 256)
+        return cx.value, cy.value, r.value, buf.value.decode()
+
+    def set_flow_tiles(self, tile=512, lag=4):
+        """Dataflow step: items per tile and the node update's lag in stages (before init)."""
+        self._call("wf_set_flow_tiles", int(tile), int(lag))
+
+    def flow(self):
+        """(tiles per step, blocks of the launch, why the mesh has no dataflow step)."""
+        t, g = C.c_int32(), C.c_int32()
+        buf = C.create_string_buffer(256)
+        self._call("wf_get_flow", C.byref(t), C.byref(g), buf, 256)
+        return t.value, g.value, buf.value.decode()
 
     def tiles(self):
         """(tiles, shared nodes, why the mesh was not tiled) of step mode 3."""
@@ -467,7 +496,7 @@ class Domain:
         return nt.value, ns.value, tn.value, ss.value, buf.value.decode()
 
     def step_mode(self):
-        """(mode the next run uses, cluster blocks or tiles, block size)."""
+        """(mode the next run uses, cluster blocks, tiles or columns, block size)."""
         m, b, t = C.c_int32(), C.c_int32(), C.c_int32()
         self._call("wf_get_step_mode", C.byref(m), C.byref(b), C.byref(t))
         return m.value, b.value, t.value

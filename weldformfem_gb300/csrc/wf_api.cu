@@ -182,9 +182,10 @@ struct wf_domain {
   int64_t host_step = 0;          // steps launched since init
   double host_time = 0.0;         // Time accumulated on the host (mirror)
   bool mix_valid_fp64 = false;    // FP64 export of the mixed state is current
-  // step graphs keyed by their number of steps: kGraphSteps for long runs and
-  // one per remainder length wf_run has met (built on first use, or ahead of
-  // time by wf_prepare_run)
+  // step graphs keyed by their number of steps (times 2, plus the sweep's
+  // buffer parity at their start): kGraphSteps for long runs and one per
+  // remainder length wf_run has met (built on first use, or ahead of time by
+  // wf_prepare_run)
   std::map<int64_t, cudaGraphExec_t> graphs;
   // per-phase timing
   bool phase_timing = false;
@@ -217,15 +218,35 @@ struct wf_domain {
   LaunchCfg cfg[3] = {LaunchCfg{128, 1}, LaunchCfg{256, 1}, LaunchCfg{128, 1}};
   double cfg_ms[3] = {0, 0, 0};
   // step scheduling (mixed): 0 automatic, 1 per-phase kernels, 2 one cluster
-  // launch per run, 3 tiled element + assembly kernels; the cluster shape is
-  // found at init for small meshes, the tiles are built at init for meshes of
-  // hexahedra that the tiled kernels cover
+  // launch per run, 3 tiled element + assembly kernels, 4 column sweep; the
+  // cluster shape is found at init for small meshes, the tiles are built at
+  // init for meshes of hexahedra that the tiled kernels cover, the sweep's
+  // buffers for box meshes
   int32_t step_mode = 0;
   bool tiled = false;             // tiles built (TileParams T valid)
   bool use_box = true;            // box meshes: connectivity computed in the mixed kernels
   bool half_open = false;         // wf_step_begin called, wf_step_end not yet
   TileParams T{};
   std::string tile_why;           // why the mesh was not tiled
+  // column sweep (step mode 4, box meshes): the pairs of buffers of the
+  // arrays it reads for neighbouring columns; pair[parity] is the current one
+  // (in M), pair[parity ^ 1] the one the next sweep writes (in W)
+  bool sweep = false;             // set up at init (W valid)
+  int32_t sweep_rows = 8;         // node rows per column (4 or 8), chosen before init
+  SweepParams W{};
+  std::string sweep_why;          // why the mesh has no column sweep
+  int parity = 0;
+  float2 *xh_pair[2] = {nullptr, nullptr};
+  float *vp_pair[2] = {nullptr, nullptr}, *tau_pair[2] = {nullptr, nullptr};
+  float *pls_pair[2] = {nullptr, nullptr};
+  // dataflow step (step mode 5, box meshes): its item table and two counter
+  // sets, flow_cnt[flow_par] counted by the next step
+  bool flow = false;
+  FlowParams F{};
+  std::string flow_why;
+  unsigned *flow_cnt[2] = {nullptr, nullptr};
+  int flow_par = 0;
+  int32_t flow_tile = 512, flow_lag = 12;
   int cl_blocks = 0, cl_bs = 0;
   double *cl_part = nullptr;      // [kClusterChunk][cl_blocks] reaction partials
   // batched ensemble
@@ -1308,10 +1329,19 @@ struct TuneResult {
 std::mutex g_tune_mu;
 std::map<TuneKey, TuneResult> g_tune_cache;
 
+bool tiled_mode(const wf_domain *d);
+bool sweep_mode(const wf_domain *d);
+// Whether the steps run the per-phase element kernel (the tiled step and the
+// column sweep do not: it is not tuned for them).
+bool flow_mode(const wf_domain *d);
+bool runs_element_kernel(const wf_domain *d) {
+  return !tiled_mode(d) && !sweep_mode(d) && !flow_mode(d);
+}
+
 TuneKey tune_key(const wf_domain *d) {
   const StepParams &P = d->P;
   return TuneKey{d->device, P.npe, P.mat_general, P.thermal, P.contact, P.tri_on, P.energy_on,
-                 P.nspec ? 1 : 0, (d->tiled && d->step_mode != 1) ? 1 : 0, d->ne, d->nn};
+                 P.nspec ? 1 : 0, runs_element_kernel(d) ? 0 : 1, d->ne, d->nn};
 }
 
 wf_status autotune_launches(wf_domain *d) {
@@ -1354,8 +1384,9 @@ wf_status autotune_launches(wf_domain *d) {
   constexpr int kRounds = 2;
   const int reps = ne >= (int64_t(1) << 20) ? 1 : 2;
   constexpr double kKeep = 1.25;
-  // the per-phase element kernel is not run by tiled steps: not tuned then
-  const int nphase = (d->tiled && d->step_mode != 1) ? 2 : 3;
+  // the per-phase element kernel is not run by tiled or swept steps: not
+  // tuned then
+  const int nphase = runs_element_kernel(d) ? 3 : 2;
   for (int phase = 0; phase < nphase; phase++) {
     std::vector<LaunchCfg> cands;
     for (int bs : sizes)
@@ -1458,10 +1489,40 @@ bool tiled_mode(const wf_domain *d) {
   if (d->precision != WF_MIXED || !d->tiled) return false;
   return d->step_mode == 3 || (kTiledAuto && d->step_mode == 0 && !cluster_mode(d));
 }
+// Whether the automatic mode picks the column sweep for box meshes.
+constexpr bool kSweepAuto = true;
+// Whether the steps of d run as the column sweep.
+bool flow_mode(const wf_domain *d);
+bool sweep_mode(const wf_domain *d) {
+  if (d->precision != WF_MIXED || !d->sweep) return false;
+  return d->step_mode == 4 ||
+         (kSweepAuto && d->step_mode == 0 && !cluster_mode(d) && !flow_mode(d));
+}
+// Whether the automatic mode picks the dataflow step for box meshes (before
+// the column sweep): not, the sweep is faster on GB300.
+constexpr bool kFlowAuto = false;
+// Whether the steps of d run as the dataflow step.
+bool flow_mode(const wf_domain *d) {
+  if (d->precision != WF_MIXED || !d->flow) return false;
+  return d->step_mode == 5 || (kFlowAuto && d->step_mode == 0 && !cluster_mode(d));
+}
+// Makes buffer p of each pair the current one (in M) and the other the one
+// the next sweep writes (in W).
+void set_parity(wf_domain *d, int p) {
+  d->parity = p;
+  d->M.xh = d->xh_pair[p];
+  d->M.vp = d->vp_pair[p];
+  d->M.tau = d->tau_pair[p];
+  d->M.pls = d->pls_pair[p];
+  d->W.xh_o = d->xh_pair[p ^ 1];
+  d->W.vp_o = d->vp_pair[p ^ 1];
+  d->W.tau_o = d->tau_pair[p ^ 1];
+  d->W.pls_o = d->pls_pair[p ^ 1];
+}
 }  // namespace
 
 WF_API wf_status wf_set_step_mode(wf_domain *d, int32_t mode) {
-  if (!d || mode < 0 || mode > 3) return WF_ERR_ARG;
+  if (!d || mode < 0 || mode > 5) return WF_ERR_ARG;
   if (mode != d->step_mode) drop_graphs(d);   // the graphs hold the other kernels
   d->step_mode = mode;
   return WF_OK;
@@ -1472,9 +1533,65 @@ WF_API wf_status wf_get_step_mode(const wf_domain *d, int32_t *mode, int32_t *bl
   if (!d) return WF_ERR_ARG;
   const bool c = d->initialized && cluster_mode(d);
   const bool t = d->initialized && !c && tiled_mode(d);
-  if (mode) *mode = c ? 2 : (t ? 3 : 1);
-  if (blocks) *blocks = c ? d->cl_blocks : (t ? d->T.ntiles : 0);
-  if (block_size) *block_size = c ? d->cl_bs : (t ? kTileElems : 0);
+  const bool f = d->initialized && !c && !t && flow_mode(d);
+  const bool w = d->initialized && !c && !t && !f && sweep_mode(d);
+  if (mode) *mode = c ? 2 : (t ? 3 : (f ? 5 : (w ? 4 : 1)));
+  if (blocks)
+    *blocks = c ? d->cl_blocks
+                : (t ? d->T.ntiles : (f ? d->F.grid : (w ? d->W.ncx * d->W.ncy : 0)));
+  if (block_size)
+    *block_size =
+        c ? d->cl_bs : (t ? kTileElems : (f ? 256 : (w ? 32 * (d->W.cy + 1) : 0)));
+  return WF_OK;
+}
+
+WF_API wf_status wf_set_flow_tiles(wf_domain *d, int32_t tile, int32_t lag) {
+  if (!d) return WF_ERR_ARG;
+  if (tile < 256 || tile > 8192 || (tile & 255))
+    return fail(d, WF_ERR_ARG, "dataflow tiles hold a multiple of 256 items, 256 to 8192");
+  if (lag < 3 || lag > 16) return fail(d, WF_ERR_ARG, "the node-update lag is 3 to 16 stages");
+  if (d->initialized) return fail(d, WF_ERR_STATE, "the dataflow tiles are chosen before init");
+  d->flow_tile = tile;
+  d->flow_lag = lag;
+  return WF_OK;
+}
+
+WF_API wf_status wf_get_flow(const wf_domain *d, int32_t *tiles, int32_t *grid, char *why,
+                             int64_t why_cap) {
+  if (!d) return WF_ERR_ARG;
+  const bool on = d->initialized && d->flow;
+  if (tiles) *tiles = on ? d->F.total : 0;
+  if (grid) *grid = on ? d->F.grid : 0;
+  if (why && why_cap > 0) {
+    const std::string &w = d->initialized ? d->flow_why : std::string("wf_init not called");
+    const size_t n = std::min<size_t>(w.size(), (size_t)why_cap - 1);
+    std::memcpy(why, w.data(), n);
+    why[n] = 0;
+  }
+  return WF_OK;
+}
+
+WF_API wf_status wf_set_sweep_rows(wf_domain *d, int32_t rows) {
+  if (!d) return WF_ERR_ARG;
+  if (rows != 4 && rows != 8) return fail(d, WF_ERR_ARG, "sweep columns have 4 or 8 node rows");
+  if (d->initialized) return fail(d, WF_ERR_STATE, "the sweep's columns are chosen before init");
+  d->sweep_rows = rows;
+  return WF_OK;
+}
+
+WF_API wf_status wf_get_sweep(const wf_domain *d, int32_t *columns_x, int32_t *columns_y,
+                              int32_t *rows, char *why, int64_t why_cap) {
+  if (!d) return WF_ERR_ARG;
+  const bool on = d->initialized && d->sweep;
+  if (columns_x) *columns_x = on ? d->W.ncx : 0;
+  if (columns_y) *columns_y = on ? d->W.ncy : 0;
+  if (rows) *rows = on ? d->W.cy : 0;
+  if (why && why_cap > 0) {
+    const std::string &w = d->initialized ? d->sweep_why : std::string("wf_init not called");
+    const size_t n = std::min<size_t>(w.size(), (size_t)why_cap - 1);
+    std::memcpy(why, w.data(), n);
+    why[n] = 0;
+  }
   return WF_OK;
 }
 
@@ -1955,6 +2072,63 @@ WF_API wf_status wf_init(wf_domain *d) {
                            d->stream, d->T, d->tile_why));
       d->tiled = d->tile_why.empty();
     }
+    // the column sweep (box meshes of hexahedra; the kernel leaves out
+    // specimens, thermal coupling and triangle-mesh dies): the second buffer
+    // of each pair it reads for neighbouring columns, and the column partials
+    d->sweep = false;
+    d->sweep_why.clear();
+    d->xh_pair[0] = M.xh;
+    d->vp_pair[0] = M.vp;
+    d->tau_pair[0] = M.tau;
+    d->pls_pair[0] = M.pls;
+    d->xh_pair[1] = nullptr;
+    d->vp_pair[1] = d->tau_pair[1] = d->pls_pair[1] = nullptr;
+    d->parity = 0;
+    if (!P.box) d->sweep_why = "not a box mesh of hexahedra";
+    else if (d->nspec) d->sweep_why = "specimens";
+    else if (P.thermal) d->sweep_why = "thermal coupling";
+    else if (P.tri_on) d->sweep_why = "triangle-mesh contact";
+    // the dataflow step (same meshes): item table, counters, partials
+    d->flow = false;
+    d->flow_why = d->sweep_why;
+    if (d->flow_why.empty()) {
+      d->F = FlowParams{};
+      d->F.grid = flow_grid(P);
+      if (P.bz + d->flow_lag + 1 > kFlowMaxLayers + 19) {
+        d->flow_why = "more element layers than the dataflow step's stage table holds";
+      } else if (d->F.grid <= 0) {
+        d->flow_why = "the dataflow kernel cannot launch on this device";
+      } else {
+        std::vector<int> first;
+        flow_stages(P, d->flow_tile, d->flow_lag, first, d->F);
+        int *fs = nullptr;
+        CUDA_TRY(upload(d, &fs, first));
+        d->F.stage_first = fs;
+        for (int k = 0; k < 2; k++) {
+          CUDA_TRY(dalloc(d, &d->flow_cnt[k], d->F.ncnt));
+          CUDA_TRY(cudaMemsetAsync(d->flow_cnt[k], 0, sizeof(unsigned) * d->F.ncnt, d->stream));
+        }
+        CUDA_TRY(dalloc(d, &d->F.partials, (size_t)d->F.bz1 * d->F.ntiles[3]));
+        d->flow_par = 0;
+        d->flow = true;
+      }
+    }
+    if (d->sweep_why.empty()) {
+      d->W = SweepParams{};
+      d->W.cy = d->sweep_rows;
+      const int cols = sweep_columns(P, d->W);
+      if (!sweep_fits(P, d->W)) {
+        d->sweep_why = "the sweep kernel cannot launch on this device";
+      } else {
+        CUDA_TRY(dalloc(d, &d->xh_pair[1], 3 * np));
+        CUDA_TRY(dalloc(d, &d->vp_pair[1], 3 * np));
+        CUDA_TRY(dalloc(d, &d->tau_pair[1], 6 * ne));
+        CUDA_TRY(dalloc(d, &d->pls_pair[1], ne));
+        CUDA_TRY(dalloc(d, &d->W.partials, cols));
+        d->sweep = true;
+        set_parity(d, 0);
+      }
+    }
     if (d->autotune) {
       wf_status ts = autotune_launches(d);
       if (ts) return ts;
@@ -1990,6 +2164,14 @@ WF_API wf_status wf_init(wf_domain *d) {
 // ---- run --------------------------------------------------------------------------
 namespace {
 
+// One dataflow step: counts in the current counter set, zeroes the other.
+void launch_flow(wf_domain *d) {
+  d->F.cnt = d->flow_cnt[d->flow_par];
+  d->F.cnt_next = d->flow_cnt[d->flow_par ^ 1];
+  mix_flow(d->P, d->M, d->mvol, d->F, d->stream);
+  d->flow_par ^= 1;
+}
+
 void launch_step(wf_domain *d) {
   const StepParams &P = d->P;
   if (d->precision == WF_FP64) {
@@ -2002,6 +2184,13 @@ void launch_step(wf_domain *d) {
     mix_nodal(P, d->M, d->mvol, d->stream, d->cfg[1]);
     mix_tile(P, d->M, d->T, d->stream);
     mix_shared(P, d->M, d->T, d->stream);
+  } else if (flow_mode(d)) {
+    launch_flow(d);
+  } else if (sweep_mode(d)) {
+    mix_geometry(P, d->M, d->mvol, d->stream, d->cfg[0]);
+    mix_nodal(P, d->M, d->mvol, d->stream, d->cfg[1]);
+    mix_sweep(P, d->M, d->W, d->stream);
+    set_parity(d, d->parity ^ 1);
   } else {
     mix_geometry(P, d->M, d->mvol, d->stream, d->cfg[0]);
     mix_nodal(P, d->M, d->mvol, d->stream, d->cfg[1]);
@@ -2028,16 +2217,26 @@ void launch_step_timed(wf_domain *d, cudaEvent_t *ev) {
     fp64_elements(P, d->S, d->stream);
     cudaEventRecord(ev[3], d->stream);
     fp64_nodes(P, d->S, d->stream, d->node_grid);
+  } else if (flow_mode(d)) {
+    // the dataflow step is one kernel: timed as the element phase
+    cudaEventRecord(ev[1], d->stream);
+    cudaEventRecord(ev[2], d->stream);
+    launch_flow(d);
+    cudaEventRecord(ev[3], d->stream);
   } else {
-    const bool tl = tiled_mode(d);
+    // the column sweep is timed as the element phase (the node phase then
+    // times nothing but the energy history)
+    const bool tl = tiled_mode(d), sw = !tl && sweep_mode(d);
     mix_geometry(P, d->M, d->mvol, d->stream, d->cfg[0]);
     cudaEventRecord(ev[1], d->stream);
     mix_nodal(P, d->M, d->mvol, d->stream, d->cfg[1]);
     cudaEventRecord(ev[2], d->stream);
     if (tl) mix_tile(P, d->M, d->T, d->stream);
+    else if (sw) mix_sweep(P, d->M, d->W, d->stream);
     else mix_elements(P, d->M, d->mvol, d->stream, d->cfg[2]);
     cudaEventRecord(ev[3], d->stream);
     if (tl) mix_shared(P, d->M, d->T, d->stream);
+    else if (sw) set_parity(d, d->parity ^ 1);
     else mix_nodes(P, d->M, d->stream, d->node_grid);
   }
   if (P.nspec) spec_reaction(P, d->stream);
@@ -2077,25 +2276,41 @@ void set_dt_constants(StepParams &P, double dt) {
 
 constexpr int kGraphSteps = 32;
 
-// The graph of `steps` consecutive steps (captured and instantiated on first
-// use; kept until the launch parameters change).
+// The graph of `steps` consecutive steps from the current buffer parity
+// (captured and instantiated on first use; kept until the launch parameters
+// change). Capturing launches nothing: the parity the captured steps advance
+// is put back, and launch_graph advances it.
 wf_status ensure_graph(wf_domain *d, int64_t steps, cudaGraphExec_t *out) {
-  auto it = d->graphs.find(steps);
+  const int64_t key = 4 * steps + 2 * d->flow_par + d->parity;
+  auto it = d->graphs.find(key);
   if (it != d->graphs.end()) {
     *out = it->second;
     return WF_OK;
   }
+  const int parity = d->parity, flow_par = d->flow_par;
   cudaGraph_t g = nullptr;
   CUDA_TRY(cudaStreamBeginCapture(d->stream, cudaStreamCaptureModeThreadLocal));
   for (int64_t i = 0; i < steps; i++) launch_step(d);
   cudaError_t e = cudaStreamEndCapture(d->stream, &g);
+  if (d->sweep) set_parity(d, parity);
+  d->flow_par = flow_par;
   if (e != cudaSuccess) return fail(d, WF_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
   cudaGraphExec_t x = nullptr;
   e = cudaGraphInstantiate(&x, g, 0);
   cudaGraphDestroy(g);
   if (e != cudaSuccess) return fail(d, WF_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
-  d->graphs[steps] = x;
+  d->graphs[key] = x;
   *out = x;
+  return WF_OK;
+}
+
+// Replays a graph of `steps` steps captured by ensure_graph at the current
+// parity.
+wf_status launch_graph(wf_domain *d, cudaGraphExec_t g, int64_t steps) {
+  CUDA_TRY(cudaGraphLaunch(g, d->stream));
+  if (flow_mode(d) && (steps & 1)) d->flow_par ^= 1;
+  else if (sweep_mode(d) && (steps & 1)) set_parity(d, d->parity ^ 1);
+  d->graph_launches++;
   return WF_OK;
 }
 
@@ -2175,6 +2390,14 @@ WF_API wf_status wf_run(wf_domain *d, int64_t nsteps) {
   if (d->step_mode == 3 && !tiled_mode(d))
     return fail(d, WF_ERR_UNSUPPORTED, "tiled steps need mixed precision and a mesh the tiles "
                                        "cover (%s)", d->tile_why.c_str());
+  if (d->step_mode == 5 && !flow_mode(d))
+    return fail(d, WF_ERR_UNSUPPORTED, "the dataflow step needs mixed precision and a box mesh "
+                                       "of hexahedra (%s)",
+                d->precision != WF_MIXED ? "FP64 step" : d->flow_why.c_str());
+  if (d->step_mode == 4 && !sweep_mode(d))
+    return fail(d, WF_ERR_UNSUPPORTED, "the column sweep needs mixed precision and a box mesh "
+                                       "of hexahedra (%s)",
+                d->precision != WF_MIXED ? "FP64 step" : d->sweep_why.c_str());
   if (d->step_mode == 2 && !cluster_mode(d))
     return fail(d, WF_ERR_UNSUPPORTED,
                 "the cluster run needs mixed precision, a mesh of at most %lld elements, and no "
@@ -2189,24 +2412,25 @@ WF_API wf_status wf_run(wf_domain *d, int64_t nsteps) {
       left -= chunk;
     }
   }
-  d->launches += (4 + (d->nspec ? 1 : 0) + (d->P.energy_on ? 1 : 0)) * left;
+  const int per_step = flow_mode(d) ? 1 : (sweep_mode(d) ? 3 : 4);
+  d->launches += (per_step + (d->nspec ? 1 : 0) + (d->P.energy_on ? 1 : 0)) * left;
   // graph replays: kGraphSteps at a time, then one graph of the remainder
   if (left >= kGraphSteps) {
     cudaGraphExec_t g = nullptr;
     wf_status s = ensure_graph(d, kGraphSteps, &g);
     if (s) return s;
     while (left >= kGraphSteps) {
-      CUDA_TRY(cudaGraphLaunch(g, d->stream));
+      s = launch_graph(d, g, kGraphSteps);
+      if (s) return s;
       left -= kGraphSteps;
-      d->graph_launches++;
     }
   }
   if (left > 1) {
     cudaGraphExec_t g = nullptr;
     wf_status s = ensure_graph(d, left, &g);
     if (s) return s;
-    CUDA_TRY(cudaGraphLaunch(g, d->stream));
-    d->graph_launches++;
+    s = launch_graph(d, g, left);
+    if (s) return s;
     left = 0;
   }
   for (int64_t i = 0; i < left; i++) launch_step(d);
@@ -2398,6 +2622,13 @@ WF_API wf_status wf_sync(wf_domain *d) {
     // flag, reported once by this call and then reset on the device
     d->st_pending = false;
     const StepState st = *d->st_host;
+    if (st.status & 2u) {
+      d->st_host->status &= ~2u;
+      CUDA_TRY(cudaMemcpy(&d->P.st->status, &d->st_host->status, sizeof(unsigned),
+                          cudaMemcpyHostToDevice));
+      return fail(d, WF_ERR_CUDA, "a dependency wait of the dataflow step ran out, in the "
+                                  "steps up to step %lld", (long long)st.step);
+    }
     if (st.status & 1u) {
       d->st_host->status = 0u;
       d->st_host->first_bad_node = LLONG_MAX;

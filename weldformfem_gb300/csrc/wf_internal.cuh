@@ -226,6 +226,47 @@ struct TileParams {
   int64_t shared_slots;    // node-list entries of the shared nodes (host-side statistic)
 };
 
+// Column sweep of box meshes (mix_sweep): the node grid cut into ncx x ncy
+// columns, one block each. The arrays a block reads for its neighbours'
+// elements come in pairs: a step reads MixState's buffer (xh, vp, tau, pls)
+// and writes the other one, given here; the host swaps the two after each
+// step.
+struct SweepParams {
+  int32_t ncx = 0, ncy = 0;
+  int32_t cy = 0;                 // node rows per column (the kernel variant)
+  float2 *xh_o = nullptr;         // [3][np]
+  float *vp_o = nullptr;          // [3][np]
+  float *tau_o = nullptr;         // [6][ne]
+  float *pls_o = nullptr;         // [ne]
+  double *partials = nullptr;     // [ncx * ncy] reaction per column
+};
+
+// Dataflow step of box meshes (mix_flow): one persistent launch per step. Its
+// work is cut into tiles of elements or nodes of one layer or plane; items
+// (kind, layer) are the four phases of one layer: 0 geometry of element layer
+// l, 1 nodal phase of node plane l, 2 element phase of layer l, 3 node update
+// of plane l. Stage s holds the items G(s), N1(s - off[1]), E(s - off[2]),
+// N2(s - off[3]) that exist, in that order; blocks take tiles in ticket order
+// (stages in order, the tiles of an item consecutively) and wait for the
+// items a tile reads through per-item done counters. Two counter sets
+// alternate between steps: a launch counts in cnt and zeroes cnt_next.
+constexpr int kFlowKinds = 4;
+constexpr int kFlowMaxLayers = 4096;   // element layers the stage table holds at most
+struct FlowParams {
+  const int *stage_first = nullptr;  // [nstages + 1] first ticket of each stage
+  int32_t nstages = 0;
+  int32_t off[kFlowKinds] = {0, 1, 3, 4};   // stage offset of each kind
+  int32_t tsize[kFlowKinds] = {0, 0, 0, 0};   // elements or nodes per tile
+  int32_t ntiles[kFlowKinds] = {0, 0, 0, 0};  // tiles per item
+  int32_t total = 0;              // tickets (tiles) per step
+  int32_t bz1 = 0;                // layers + 1: counter stride per kind
+  int32_t grid = 0;               // blocks of the launch
+  int32_t ncnt = 0;               // counters per set: 1 + kFlowKinds * bz1
+  unsigned *cnt = nullptr;        // [0] next ticket, [1 + kind * bz1 + l] tiles done of an item
+  unsigned *cnt_next = nullptr;   // the next step's set
+  double *partials = nullptr;     // [bz1 * ntiles[3]] reaction per node-update tile
+};
+
 // Host-side view of one state for the legacy VTK writer (write_vtk_text,
 // wf_deck.cpp). Node vectors are AoS [nn][3]; element tensors hold 6 values
 // per element (Voigt xx yy zz xy yz xz), AoS [ne][6] or SoA [6][ne]. Null
@@ -289,6 +330,21 @@ void mix_predict(const StepParams &P, const MixState &M, cudaStream_t st);
 void mix_tile(const StepParams &P, const MixState &M, const TileParams &T, cudaStream_t st);
 void mix_shared(const StepParams &P, const MixState &M, const TileParams &T, cudaStream_t st);
 int mix_shared_grid(const TileParams &T);
+// Column sweep of a box mesh (replaces mix_elements + mix_nodes): reads M's
+// positions, predicted velocities, tau and eps_p and writes W's. The column
+// shape: sweep_columns fills W.ncx, W.ncy, W.cy for the box and returns the
+// number of blocks; sweep_fits tells whether the kernel can launch here.
+int sweep_columns(const StepParams &P, SweepParams &W);
+bool sweep_fits(const StepParams &P, const SweepParams &W);
+void mix_sweep(const StepParams &P, const MixState &M, const SweepParams &W, cudaStream_t st);
+// Dataflow step of a box mesh (replaces the four phase kernels): flow_stages
+// builds the stage table on the host and fills F's sizes, mix_flow launches
+// one step. flow_grid: the persistent grid (0: the
+// kernel cannot launch here).
+int flow_grid(const StepParams &P);
+void flow_stages(const StepParams &P, int tile, int lag, std::vector<int> &first, FlowParams &F);
+void mix_flow(const StepParams &P, const MixState &M, float *vol, const FlowParams &F,
+              cudaStream_t st);
 // Whole runs of steps in one launch of one cluster of `blocks` blocks of `bs`
 // threads (64, 128 or 256), for small meshes; mix_cluster_fits returns how
 // many such clusters can be resident (0: the shape cannot launch).

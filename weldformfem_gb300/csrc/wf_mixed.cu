@@ -447,15 +447,37 @@ __global__ void __launch_bounds__(BS) k_mix_nodal(StepParams P, MixState M, cons
 // Writes the new tau and eps_p; returns sigma = tau - p I in sg.
 // LAW = 0: linear hardening only (the common case, fewer registers); LAW = 1:
 // every material model.
-template <int LAW, bool TH>
-__device__ __forceinline__ void stress_update(const StepParams &P, const MixState &M, int64_t e,
+// Element state (tau [6][ne], eps_p [ne]) in HBM, read and written in place.
+struct StateInPlace {
+  float *tau, *pls;
+  int64_t ne, e;
+  __device__ __forceinline__ void load(float &t0, float &t1, float &t2, float &t3, float &t4,
+                                       float &t5, float &p) const {
+    t0 = tau[e]; t1 = tau[ne + e]; t2 = tau[2 * ne + e];
+    t3 = tau[3 * ne + e]; t4 = tau[4 * ne + e]; t5 = tau[5 * ne + e];
+    p = pls[e];
+  }
+  __device__ __forceinline__ void store(float t0, float t1, float t2, float t3, float t4,
+                                        float t5, float p) const {
+    pls[e] = p;
+    tau[e] = t0; tau[ne + e] = t1; tau[2 * ne + e] = t2;
+    tau[3 * ne + e] = t3; tau[4 * ne + e] = t4; tau[5 * ne + e] = t5;
+  }
+  __device__ __forceinline__ bool owns() const { return true; }
+};
+
+// IO: where the element's tau and eps_p come from and go to (StateInPlace:
+// HBM, read and written in place; StateSwept: loaded ahead by the column
+// sweep, written to the other buffer of a pair, or not at all for a halo
+// element).
+template <int LAW, bool TH, class IO>
+__device__ __forceinline__ void stress_update(const StepParams &P, int64_t e, const IO &io,
                                               const MatF &m, const float (&sr)[6], float w01,
                                               float w12, float w02, float p, float jTh,
                                               float (&sg)[6], float &sdot, float &qpl) {
-  const int64_t ne = P.ne;
   const float dt = P.espec ? P.specf[P.espec[e]].dt : P.f_dt;
-  float t0 = M.tau[e], t1 = M.tau[ne + e], t2 = M.tau[2 * ne + e];
-  float t3 = M.tau[3 * ne + e], t4 = M.tau[4 * ne + e], t5 = M.tau[5 * ne + e];
+  float t0, t1, t2, t3, t4, t5, pls;
+  io.load(t0, t1, t2, t3, t4, t5, pls);
   {
     // tau W^T                      W tau
     const float srt0 = t3 * w01 + t5 * w02, rs0 = w01 * t3 + w02 * t5;    // xx
@@ -479,7 +501,6 @@ __device__ __forceinline__ void stress_update(const StepParams &P, const MixStat
   const float J2 = 0.5f * (d0s * d0s + 2.0f * t3 * t3 + 2.0f * t5 * t5 + d1s * d1s +
                            2.0f * t4 * t4 + d2s * d2s);
   const float sig_trial = sqrtf(3.0f * J2);
-  float pls = M.pls[e];
   float sy;
   float eff = 0.f;
   float dep = 0.f;
@@ -520,9 +541,7 @@ __device__ __forceinline__ void stress_update(const StepParams &P, const MixStat
     pls += dgamma;
     dep = dgamma;
   }
-  M.pls[e] = pls;
-  M.tau[e] = t0; M.tau[ne + e] = t1; M.tau[2 * ne + e] = t2;
-  M.tau[3 * ne + e] = t3; M.tau[4 * ne + e] = t4; M.tau[5 * ne + e] = t5;
+  io.store(t0, t1, t2, t3, t4, t5, pls);
   sg[0] = t0 - p; sg[1] = t1 - p; sg[2] = t2 - p;
   sg[3] = t3; sg[4] = t4; sg[5] = t5;
   // plastic heat 0.9 sigma : (d eps_p / dt) (Mechanical.C:1783-1810)
@@ -626,7 +645,10 @@ __device__ __forceinline__ void thermal_rates(const StepParams &P, const MixStat
 // TileNodes (below): a tile's node arrays staged in shared memory through
 // tile-local indices. Both return the same values, so an element computes
 // the same forces bit for bit from either.
-template <bool CG, bool BOX = false>
+// CGX: positions and predicted velocities through L2 as well (the cluster
+// run); the dataflow step reads them through L1 (no tile of its launch writes
+// them before every read of them is done) and only the J ratios through L2.
+template <bool CG, bool BOX = false, bool CGX = CG>
 struct GlobalNodes {
   const float2 *xh;
   const float *vp, *jr;
@@ -641,8 +663,8 @@ struct GlobalNodes {
       for (int a = 0; a < 8; a++) nid[a] = __ldg(&P.elnod[a * P.ne + e]);
     }
   }
-  __device__ __forceinline__ float2 x(int a, int k) const { return ldx<CG>(&xh[k * np + nid[a]]); }
-  __device__ __forceinline__ float v(int a, int k) const { return ldx<CG>(&vp[k * np + nid[a]]); }
+  __device__ __forceinline__ float2 x(int a, int k) const { return ldx<CGX>(&xh[k * np + nid[a]]); }
+  __device__ __forceinline__ float v(int a, int k) const { return ldx<CGX>(&vp[k * np + nid[a]]); }
   __device__ __forceinline__ float j(int a) const { return ldx<CG>(&jr[nid[a]]); }
 };
 
@@ -661,10 +683,11 @@ struct ForcesToHbm {
 // EARLY_JR: gather the nodes' volume ratios with the positions, so that their
 // loads are in flight during the Jacobian arithmetic (the cluster run, one
 // element per thread, gathers them later: early it spills there).
-template <int LAW, bool EARLY_JR, bool TH, class Nodes, class Out>
+template <int LAW, bool EARLY_JR, bool TH, class Nodes, class Out, class IO>
 __device__ __forceinline__ void element_hex_core(const StepParams &P, const MixState &M,
                                                  int64_t e, const Nodes &nd, float *stash,
-                                                 int stride, long long step, Out &out) {
+                                                 int stride, long long step, Out &out,
+                                                 const IO &io) {
   float A[3][3], detJ;
   float J_avg = 0.f;
   {
@@ -752,8 +775,8 @@ __device__ __forceinline__ void element_hex_core(const StepParams &P, const MixS
   if (J_bar < 0.0f) J_bar = 0.2f;
   const float p = -m.K * (J_bar - 1.0f);
   float sg[6], sdot = 0.f, qpl = 0.f;
-  stress_update<LAW, TH>(P, M, e, m, sr, w01, w12, w02, p, jTh, sg, sdot, qpl);
-  if (P.energy_on) M.edot[e] = sdot * vol;
+  stress_update<LAW, TH>(P, e, io, m, sr, w01, w12, w02, p, jTh, sg, sdot, qpl);
+  if (P.energy_on && io.owns()) M.edot[e] = sdot * vol;
   // sigma as a symmetric 3x3: S[i][k]
   const float S[3][3] = {{sg[0], sg[3], sg[5]}, {sg[3], sg[1], sg[4]}, {sg[5], sg[4], sg[2]}};
 #pragma unroll
@@ -794,7 +817,8 @@ __device__ __forceinline__ void element_hex(const StepParams &P, const MixState 
                                             float *stash, int stride, long long step) {
   const GlobalNodes<CG, BOX> nd(P, M, e);
   ForcesToHbm out{M.fe, P.ne, e};
-  element_hex_core<LAW, !CG, TH>(P, M, e, nd, stash, stride, step, out);
+  element_hex_core<LAW, !CG, TH>(P, M, e, nd, stash, stride, step, out,
+                                 StateInPlace{M.tau, M.pls, P.ne, e});
 }
 
 // Tetrahedron: per-node shape derivatives (Domain_d.C:1866-1887).
@@ -853,7 +877,8 @@ __device__ __forceinline__ void element_tet(const StepParams &P, const MixState 
   if (J_bar < 0.0f) J_bar = 0.2f;
   const float p = -m.K * (J_bar - 1.0f);
   float sg[6], sdot = 0.f, qpl = 0.f;
-  stress_update<LAW, TH>(P, M, e, m, sr, w01, w12, w02, p, jTh, sg, sdot, qpl);
+  stress_update<LAW, TH>(P, e, StateInPlace{M.tau, M.pls, ne, e}, m, sr, w01, w12, w02, p,
+                         jTh, sg, sdot, qpl);
   const float w = weightf<4>();
   if (P.energy_on) M.edot[e] = sdot * (detJ * w);
 #pragma unroll
@@ -944,11 +969,37 @@ __device__ __forceinline__ double block_sum_dense(double v, double *sh) {
 // summed in list order): non-finite check, accelerations, velocity BCs,
 // Chung-Hulbert corrector and the next predictor. x and vp are the node's
 // position pair and predicted velocity (read by the caller from HBM or from
-// a tile's staged copy). Returns the node's reaction contribution.
+// a staged copy); the new ones go to xo and vpo (the arrays they were read
+// from, or the other buffers of the column sweep's pairs). Returns the node's
+// reaction contribution.
+// A node's own state read by its update (loaded ahead of the gather by the
+// column sweep, where the gather does not wait for HBM).
+struct NodeIn {
+  float vold[3], pa[3];
+  float mass;
+  uint32_t code;
+  uint8_t fl;
+};
+template <bool CG = false>
+__device__ __forceinline__ NodeIn node_in(const StepParams &P, const MixState &M, int64_t n) {
+  NodeIn in;
+  const int64_t np = P.np;
+  in.fl = P.nflag[n];
+  in.mass = CG ? __ldcg(&M.mass[n]) : M.mass[n];   // written by the nodal phase
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    in.vold[k] = M.v[k * np + n];
+    in.pa[k] = M.pa[k * np + n];
+  }
+  in.code = P.bc[n];
+  return in;
+}
+
 template <int NPE, bool CG>
 __device__ __forceinline__ float node_finish(const StepParams &P, const MixState &M, int64_t n,
                                              long long step, float fi0, float fi1, float fi2,
-                                             float2 (&x)[3], const float (&vp)[3]) {
+                                             float2 (&x)[3], const float (&vp)[3], float2 *xo,
+                                             float *vpo, const NodeIn &in) {
   float r = 0.0f;
   const int64_t np = P.np;
   const int64_t ne = P.ne;
@@ -960,21 +1011,21 @@ __device__ __forceinline__ float node_finish(const StepParams &P, const MixState
       atomicOr(&P.st->status, 1u);
       atomicMin(&P.st->first_bad_node, (long long)n);
     }
-  const uint8_t fl = P.nflag[n];
-  const float mass = M.mass[n];
+  const uint8_t fl = in.fl;
+  const float mass = in.mass;
   const float inv_m = 1.0f / mass;
   float vold[3], pa[3];
 #pragma unroll
   for (int k = 0; k < 3; k++) {
-    vold[k] = M.v[k * np + n];
-    pa[k] = M.pa[k * np + n];
+    vold[k] = in.vold[k];
+    pa[k] = in.pa[k];
   }
   float cf[3] = {0.f, 0.f, 0.f};
   if (P.contact && (fl & NF_CONTACT)) {
-    cf[0] = M.cf[n];
-    cf[1] = M.cf[np + n];
-    cf[2] = M.cf[2 * np + n];
-    r = P.tri_on ? M.cfn[n] : fabsf(cf[2]);
+    cf[0] = ldx<CG>(&M.cf[n]);
+    cf[1] = ldx<CG>(&M.cf[np + n]);
+    cf[2] = ldx<CG>(&M.cf[2 * np + n]);
+    r = P.tri_on ? ldx<CG>(&M.cfn[n]) : fabsf(cf[2]);
   }
   if (!P.contact && (fl & NF_REACTION)) {
     if (P.rnode)
@@ -989,7 +1040,7 @@ __device__ __forceinline__ float node_finish(const StepParams &P, const MixState
     c_dt = sf.dt; c_cu_pred = sf.cu_pred; c_cu_corr = sf.cu_corr;
     c_cv_corr = sf.cv_corr; c_cv_pred = sf.cv_pred;
   }
-  const uint32_t code = P.bc[n];
+  const uint32_t code = in.code;
   const double *bvd = &P.bcval[3 * (code >> 3)];
 #pragma unroll
   for (int k = 0; k < 3; k++) {
@@ -1004,10 +1055,10 @@ __device__ __forceinline__ float node_finish(const StepParams &P, const MixState
     x[k] = pair_add(x[k], udt);
     float vnext = v + c_cv_pred * a;
     if (fixed) vnext = bv;
-    M.xh[k * np + n] = x[k];
+    xo[k * np + n] = x[k];
     M.v[k * np + n] = v;
     M.pa[k * np + n] = a;
-    M.vp[k * np + n] = vnext;
+    vpo[k * np + n] = vnext;
   }
   if (P.thermal) {
     // ThermalCalcs node part: the step's element-node rates in list order and
@@ -1059,7 +1110,8 @@ __device__ __forceinline__ float node_one(const StepParams &P, const MixState &M
       x[k] = M.xh[k * np + n];
       vp[k] = M.vp[k * np + n];
     }
-    return node_finish<NPE, CG>(P, M, n, step, fi0, fi1, fi2, x, vp);
+    return node_finish<NPE, CG>(P, M, n, step, fi0, fi1, fi2, x, vp, M.xh, M.vp,
+                                node_in<CG>(P, M, n));
   }
   const int32_t b = __ldg(&P.off[n]), c = __ldg(&P.off[n + 1]) - b;
   // gather over the node's element list in list order, eight entries at a
@@ -1094,7 +1146,8 @@ __device__ __forceinline__ float node_one(const StepParams &P, const MixState &M
     x[k] = M.xh[k * np + n];
     vp[k] = M.vp[k * np + n];
   }
-  return node_finish<NPE, CG>(P, M, n, step, fi0, fi1, fi2, x, vp);
+  return node_finish<NPE, CG>(P, M, n, step, fi0, fi1, fi2, x, vp, M.xh, M.vp,
+                              node_in<CG>(P, M, n));
 }
 
 template <int NPE, bool BOX>
@@ -1212,7 +1265,8 @@ __global__ void __launch_bounds__(kTileElems, 2) k_mix_tile(StepParams P, MixSta
 #pragma unroll
     for (int a = 0; a < 8; a++) nd.loc[a] = __ldg(&T.lel[a * ne + pos]);
     ForcesToRegs out{f};
-    element_hex_core<LAW, true, false>(P, M, e, nd, &stash[tid], kTileElems, step, out);
+    element_hex_core<LAW, true, false>(P, M, e, nd, &stash[tid], kTileElems, step, out,
+                                       StateInPlace{M.tau, M.pls, ne, e});
     // corner forces of shared nodes: to HBM, for the shared-node gather
 #pragma unroll
     for (int a = 0; a < 8; a++)
@@ -1247,7 +1301,8 @@ __global__ void __launch_bounds__(kTileElems, 2) k_mix_tile(StepParams P, MixSta
         vp[k] = svp[k * kTileNodes + i];
       }
       r += (double)node_finish<8, false>(P, M, id, step, acc[i], acc[kTileNodes + i],
-                                         acc[2 * kTileNodes + i], x, vp);
+                                         acc[2 * kTileNodes + i], x, vp, M.xh, M.vp,
+                                         node_in(P, M, id));
     }
   }
   const double bsum = block_sum_dense(r, sh);
@@ -1289,6 +1344,472 @@ __global__ void __launch_bounds__(kNodeThreads, WF_NODE_MIN_BLOCKS) k_mix_shared
       P.st->time = time + P.dt;
       P.st->done_blocks = 0u;
     }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Column sweep for box meshes (hexahedra in the AddBoxLength numbering): the
+// element and node phases of a step in one kernel, the element forces kept in
+// shared memory.
+//
+// The node grid (nx+1) x (ny+1) is cut into columns of at most 31 x CY nodes,
+// one block each; a block sweeps its column's node planes k = 0..nz. It holds
+// the elements that touch its nodes (its own and a one-element ring on the -x
+// and -y sides, at most 32 x (CY+1) per layer, one thread each) and computes
+// the ring elements again rather than exchanging forces with the neighbour
+// column, so every node gathers all its element forces inside its block.
+//   * Node planes are staged in shared memory (cp.async, three slots, issued
+//     a layer ahead): positions (hi, lo), predicted velocities, J ratios.
+//   * Each element of layer k computes its forces from the staged planes k
+//     and k+1 with the per-phase element arithmetic (so bit for bit the same
+//     forces) into a shared-memory buffer; an element owned by the block (its
+//     corner 0 is one of the block's nodes) writes its tau and eps_p, a ring
+//     element writes nothing.
+//   * Each node of plane k adds the forces of its elements in list order: the
+//     four of layer k-1 (corners 6, 7, 5, 4), summed in the previous layer and
+//     carried in registers, then the four of layer k (corners 2, 3, 1, 0) --
+//     the per-phase gather's order, so bit for bit its sum -- and is updated
+//     (node_finish); it starts the sum of plane k+1 from layer k.
+// Two barriers per layer separate the element and node phases; a thread's
+// next element state and its node's next own state are loaded a phase ahead.
+// Every array a block reads for its ring (positions, predicted velocities,
+// tau, eps_p) is one of a pair: the step reads one buffer and writes the
+// other, so no block sees another's update of the same step. The reaction is
+// summed per thread over its planes (FP64), per block, and over blocks in
+// block order by the last block, which advances the step state; its order
+// differs from the node kernel's.
+constexpr int kSwEX = 32;            // elements per row of a column layer (one warp)
+constexpr int kSwNX = kSwEX + 1;     // staged nodes per row
+template <int CY>
+struct SweepShape {
+  static constexpr int threads = kSwEX * (CY + 1);
+  static constexpr int plane = kSwNX * (CY + 2);   // staged nodes per plane
+  // per staged plane: positions [3][plane] float2, predicted velocities
+  // [3][plane], J ratios [plane]
+  static constexpr size_t slot_bytes = (size_t)plane * (3 * 8 + 3 * 4 + 4);
+  // three staged planes, the element forces [24][threads], the hourglass
+  // stash
+  static constexpr size_t smem = 3 * slot_bytes + sizeof(float) * 36 * threads;
+};
+
+__device__ __forceinline__ void cp_async4(void *dst, const void *src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async8(void *dst, const void *src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+}
+
+// An element's corners in the staged planes: corner a at staged index
+// b + {0, 1, kSwNX + 1, kSwNX}[a & 3] of the lower (a < 4) or upper plane.
+template <int PL>
+struct SweepNodes {
+  const float2 *x0, *x1;
+  const float *v0, *v1, *j0, *j1;
+  int b;
+  static __device__ __forceinline__ int off(int a) {
+    return (a & 3) == 0 ? 0 : (a & 3) == 1 ? 1 : (a & 3) == 2 ? kSwNX + 1 : kSwNX;
+  }
+  __device__ __forceinline__ float2 x(int a, int k) const {
+    return (a < 4 ? x0 : x1)[k * PL + b + off(a)];
+  }
+  __device__ __forceinline__ float v(int a, int k) const {
+    return (a < 4 ? v0 : v1)[k * PL + b + off(a)];
+  }
+  __device__ __forceinline__ float j(int a) const { return (a < 4 ? j0 : j1)[b + off(a)]; }
+};
+
+// Element forces into shared memory, [corner * 3 + component][thread].
+template <int NT>
+struct ForcesToSmem {
+  float *sf;
+  int t;
+  __device__ __forceinline__ void put(int a, int k, float f) { sf[(a * 3 + k) * NT + t] = f; }
+};
+
+// tau and eps_p loaded a layer ahead (t[0..5] tau, t[6] eps_p); written to
+// the other buffers of the pairs by the owning block (tau_o non-null), not by
+// a ring.
+__device__ __forceinline__ void load_elem_state(const MixState &M, int64_t ne, int64_t e,
+                                                float (&t)[7]) {
+#pragma unroll
+  for (int c = 0; c < 6; c++) t[c] = M.tau[c * ne + e];
+  t[6] = M.pls[e];
+}
+struct StateSwept {
+  float t[6], p;
+  float *tau_o, *pls_o;
+  int64_t ne, e;
+  __device__ __forceinline__ StateSwept(const float (&in)[7], int64_t ne_, int64_t e_, bool own,
+                                        float *to, float *po)
+      : p(in[6]), tau_o(own ? to : nullptr), pls_o(po), ne(ne_), e(e_) {
+#pragma unroll
+    for (int c = 0; c < 6; c++) t[c] = in[c];
+  }
+  __device__ __forceinline__ void load(float &t0, float &t1, float &t2, float &t3, float &t4,
+                                       float &t5, float &pp) const {
+    t0 = t[0]; t1 = t[1]; t2 = t[2]; t3 = t[3]; t4 = t[4]; t5 = t[5];
+    pp = p;
+  }
+  __device__ __forceinline__ void store(float t0, float t1, float t2, float t3, float t4,
+                                        float t5, float pp) const {
+    if (tau_o) {
+      pls_o[e] = pp;
+      tau_o[e] = t0; tau_o[ne + e] = t1; tau_o[2 * ne + e] = t2;
+      tau_o[3 * ne + e] = t3; tau_o[4 * ne + e] = t4; tau_o[5 * ne + e] = t5;
+    }
+  }
+  __device__ __forceinline__ bool owns() const { return tau_o != nullptr; }
+};
+
+template <int LAW, int CY>
+__global__ void __launch_bounds__(SweepShape<CY>::threads, 2) k_mix_sweep(StepParams P,
+                                                                         MixState M,
+                                                                         SweepParams W) {
+  using S = SweepShape<CY>;
+  constexpr int NT = S::threads, PL = S::plane;
+  extern __shared__ __align__(16) unsigned char smem[];
+  float *sf = reinterpret_cast<float *>(smem + 3 * S::slot_bytes);
+  float *stash = sf + 24 * NT;
+  __shared__ double sh[NT / 32];
+  __shared__ bool am_last;
+  const int t = threadIdx.x, lx = t & 31, ly = t >> 5;
+  const int bx = P.bx, by = P.by, bz = P.bz;
+  const int nx1 = bx + 1, ny1 = by + 1;
+  const int cx = (int)(blockIdx.x % (unsigned)W.ncx), cy = (int)(blockIdx.x / (unsigned)W.ncx);
+  const int i0 = (int)((int64_t)cx * nx1 / W.ncx), i1 = (int)((int64_t)(cx + 1) * nx1 / W.ncx);
+  const int j0 = (int)((int64_t)cy * ny1 / W.ncy), j1 = (int)((int64_t)(cy + 1) * ny1 / W.ncy);
+  // the column's elements: [ea, ea + nex) x [fa, fa + ney) in each layer;
+  // its staged nodes: (nex + 1) x (ney + 1) from (ea, fa)
+  const int ea = max(i0 - 1, 0), fa = max(j0 - 1, 0);
+  const int nex = min(i1, bx) - ea, ney = min(j1, by) - fa;
+  const int snx = nex + 1, sn = snx * (ney + 1);
+  const int64_t np = P.np, ne = P.ne;
+  const int64_t pxy = (int64_t)nx1 * ny1, exy = (int64_t)bx * by;
+  // element role: element (ea + lx, fa + ly) of each layer
+  const bool e_act = lx < nex && ly < ney;
+  const bool e_own = e_act && ea + lx >= i0 && fa + ly >= j0;
+  const int64_t e_col = (int64_t)(ea + lx) + (int64_t)bx * (fa + ly);
+  // node role: node (i0 + lx, j0 + ly) of each plane, and the column-local
+  // indices of its elements (-1,-1), (0,-1), (-1,0), (0,0) in a layer (-1: none)
+  const bool n_act = lx < i1 - i0 && ly < j1 - j0;
+  const int gi = i0 + lx, gj = j0 + ly;
+  int q[4];
+#pragma unroll
+  for (int dj = 0; dj < 2; dj++)
+#pragma unroll
+    for (int di = 0; di < 2; di++) {
+      const int ei = gi - 1 + di, ej = gj - 1 + dj;
+      q[dj * 2 + di] =
+          (ei >= 0 && ei < bx && ej >= 0 && ej < by) ? (ei - ea) + kSwEX * (ej - fa) : -1;
+    }
+  const int ns = (gi - ea) + kSwNX * (gj - fa);
+  const int64_t n_col = (int64_t)gi + (int64_t)nx1 * gj;
+
+  auto slot_x = [&](int pz) {
+    return reinterpret_cast<float2 *>(smem + (pz % 3) * S::slot_bytes);
+  };
+  auto stage = [&](int pz) {
+    float2 *sx = slot_x(pz);
+    float *sv = reinterpret_cast<float *>(sx + 3 * PL);
+    float *sj = sv + 3 * PL;
+    for (int idx = t; idx < sn; idx += NT) {
+      const int si = idx % snx, sy = idx / snx;
+      const int64_t n = (int64_t)(ea + si) + (int64_t)nx1 * (fa + sy) + pxy * pz;
+      const int o = si + kSwNX * sy;
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        cp_async8(&sx[k * PL + o], &M.xh[k * np + n]);
+        cp_async4(&sv[k * PL + o], &M.vp[k * np + n]);
+      }
+      cp_async4(&sj[o], &M.jr[n]);
+    }
+  };
+  // the node's own staged position and predicted velocity of plane pz
+  auto own_node = [&](int pz, float2 (&x)[3], float (&vp)[3]) {
+    const float2 *sx = slot_x(pz);
+    const float *sv = reinterpret_cast<const float *>(sx + 3 * PL);
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      x[k] = sx[k * PL + ns];
+      vp[k] = sv[k * PL + ns];
+    }
+  };
+
+  stage(0);
+  stage(1);
+  cp_async_commit();
+  const long long step = P.st->step;
+  float pf0 = 0.f, pf1 = 0.f, pf2 = 0.f;   // plane k's sum over layer k-1
+  double racc = 0.0;
+  // the element state of the thread's element in the next layer, and the
+  // node's own state of the next plane: loaded one phase ahead of their use
+  float tn[7];
+  if (e_act) load_elem_state(M, ne, e_col, tn);
+  NodeIn nin;
+  if (n_act) nin = node_in(P, M, n_col);
+  for (int k = 0; k < bz; k++) {
+    cp_async_wait_all();
+    __syncthreads();   // planes k, k+1 staged; the previous layer's reads done
+    if (k + 2 <= bz) stage(k + 2);
+    cp_async_commit();
+    if (e_act) {
+      const int64_t e = e_col + exy * k;
+      const StateSwept io(tn, ne, e, e_own, W.tau_o, W.pls_o);
+      const float2 *x0 = slot_x(k), *x1 = slot_x(k + 1);
+      const float *v0 = reinterpret_cast<const float *>(x0 + 3 * PL);
+      const float *v1 = reinterpret_cast<const float *>(x1 + 3 * PL);
+      const SweepNodes<PL> nd{x0, x1, v0, v1, v0 + 3 * PL, v1 + 3 * PL, lx + kSwNX * ly};
+      ForcesToSmem<NT> out{sf, t};
+      element_hex_core<LAW, true, false>(P, M, e, nd, &stash[t], NT, step, out, io);
+      if (k + 1 < bz) load_elem_state(M, ne, e + exy, tn);
+    }
+    __syncthreads();
+    if (n_act) {
+      constexpr int cb[4] = {2, 3, 1, 0}, ct[4] = {6, 7, 5, 4};
+      float f0 = pf0, f1 = pf1, f2 = pf2;
+      float u0 = 0.f, u1 = 0.f, u2 = 0.f;
+#pragma unroll
+      for (int j = 0; j < 4; j++)
+        if (q[j] >= 0) {
+          f0 += sf[(cb[j] * 3) * NT + q[j]];
+          f1 += sf[(cb[j] * 3 + 1) * NT + q[j]];
+          f2 += sf[(cb[j] * 3 + 2) * NT + q[j]];
+          u0 += sf[(ct[j] * 3) * NT + q[j]];
+          u1 += sf[(ct[j] * 3 + 1) * NT + q[j]];
+          u2 += sf[(ct[j] * 3 + 2) * NT + q[j]];
+        }
+      float2 x[3];
+      float vp[3];
+      own_node(k, x, vp);
+      const NodeIn cur = nin;
+      nin = node_in(P, M, n_col + pxy * (k + 1));   // plane k+1 <= nz exists
+      racc += (double)node_finish<8, false>(P, M, n_col + pxy * k, step, f0, f1, f2, x, vp,
+                                            W.xh_o, W.vp_o, cur);
+      pf0 = u0;
+      pf1 = u1;
+      pf2 = u2;
+    }
+  }
+  // the top plane: layer nz-1's forces only (staged by the last layer's wait)
+  if (n_act) {
+    float2 x[3];
+    float vp[3];
+    own_node(bz, x, vp);
+    racc += (double)node_finish<8, false>(P, M, n_col + pxy * bz, step, pf0, pf1, pf2, x, vp,
+                                          W.xh_o, W.vp_o, nin);
+  }
+  const double bs = block_sum_dense(racc, sh);
+  if (t == 0) {
+    W.partials[blockIdx.x] = bs;
+    __threadfence();
+    const unsigned prev = atomicAdd(&P.st->done_blocks, 1u);
+    am_last = (prev == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (am_last) {
+    __threadfence();
+    const double time = P.st->time;
+    double tt = 0.0;
+    for (unsigned i = t; i < gridDim.x; i += NT) tt += ((volatile double *)W.partials)[i];
+    const double tot = block_sum_dense(tt, sh);
+    if (t == 0) {
+      const long long s = P.st->step;
+      if (s < P.hist_cap) P.hist[s] = tot;
+      P.st->step = s + 1;
+      P.st->time = time + P.dt;
+      P.st->done_blocks = 0u;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Dataflow step for box meshes: the four phases of a step in one persistent
+// launch, run as a wavefront through the element layers.
+//
+// The step's work is cut into tiles (FlowParams.tile elements or nodes of one
+// layer or plane); the items are the phases of a layer: geometry G(l) and
+// element phase E(l) of element layer l, nodal phase N1(p) and node update
+// N2(p) of node plane p. Each block takes tiles by ticket (one atomic counter)
+// in the order of the item table, built on the host in wavefront order: stage
+// s holds G(s), N1(s-1), E(s-3), N2(s-lag). A tile waits until the items it
+// reads are done:
+//   N1(p) <- G(p-1), G(p)      (the volumes around the plane)
+//   E(l)  <- N1(l), N1(l+1)    (the J ratios, masses, contact forces)
+//   N2(p) <- E(p-1), E(p)      (the element forces of the plane's elements)
+// Every tile an item depends on has a smaller ticket, so it was taken by a
+// running block that waits only on smaller tickets in turn: the launch cannot
+// deadlock however many blocks are resident. The node update of plane p writes
+// its positions and predicted velocities only after every phase that reads
+// them (G(p-1), G(p), N1(p), E(p-1), E(p)) is done: they are all in its
+// dependency chain. Data written in the launch is read through L2 (__ldcg);
+// a producer fences before its tile is counted, and a consumer's block waits
+// on the counters with an acquire load in one thread and a barrier. The
+// element forces of a layer are read while they are still in L2, a stage or
+// two after they were written. Each element and node runs the per-phase
+// arithmetic, so the state is bitwise the per-phase step's; the reaction is
+// summed per node tile, and over tiles in a fixed order by a one-block kernel
+// after the launch, which advances the step state.
+//
+// The waits are bounded (kFlowSpin polls): a wait that runs out sets bit 1 of
+// the step status, which wf_sync reports, and the tile goes on.
+constexpr int kFlowThreads = 256;
+constexpr int kFlowSpin = 1 << 18;
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// a[i] without a runtime index into a kernel parameter (which would copy the
+// array to local memory)
+__device__ __forceinline__ int pick4(const int32_t (&a)[4], int i) {
+  return i == 0 ? a[0] : (i == 1 ? a[1] : (i == 2 ? a[2] : a[3]));
+}
+
+__device__ __forceinline__ void red_release(unsigned *p, unsigned v) {
+  asm volatile("red.release.gpu.global.add.u32 [%0], %1;\n" ::"l"(p), "r"(v) : "memory");
+}
+
+template <int LAW>
+__global__ void __launch_bounds__(kFlowThreads, 1024 / kFlowThreads) k_mix_flow(StepParams P,
+                                                                               MixState M,
+                                                                               float *vol,
+                                                                               FlowParams F) {
+  extern __shared__ int s_first[];   // [nstages + 1] the stage table
+  __shared__ float stash[12 * kFlowThreads];
+  __shared__ double sh[kFlowThreads / 32];
+  __shared__ int s_tk[1];
+  const int tid = threadIdx.x;
+  // the next step's counters (no block of this launch reads them)
+  if (blockIdx.x == 0)
+    for (int i = tid; i < F.ncnt; i += kFlowThreads) F.cnt_next[i] = 0u;
+  for (int i = tid; i <= F.nstages; i += kFlowThreads) s_first[i] = __ldg(&F.stage_first[i]);
+  const int bz = P.bz;
+  const int64_t exy = (int64_t)P.bx * P.by;
+  const int64_t pxy = (int64_t)(P.bx + 1) * (P.by + 1);
+  // the tile of ticket tk: its stage (binary search in the table), then the
+  // stage's items in kind order
+  auto decode = [&](int tk, int &kind, int &l, int &tile) {
+    int lo = 0, hi = F.nstages - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (s_first[mid] <= tk) lo = mid;
+      else hi = mid - 1;
+    }
+    int rem = tk - s_first[lo];
+    kind = 0;
+    l = 0;
+#pragma unroll
+    for (int q = 0; q < kFlowKinds; q++) {
+      const int lq = lo - F.off[q], lmax = (q == 0 || q == 2) ? bz - 1 : bz;
+      if (lq < 0 || lq > lmax) continue;
+      if (rem < F.ntiles[q]) {
+        kind = q;
+        l = lq;
+        break;
+      }
+      rem -= F.ntiles[q];
+    }
+    tile = rem;
+  };
+  __syncthreads();   // the stage table
+  for (;;) {
+    if (tid == 0) {
+      const int tk = (int)atomicAdd(&F.cnt[0], 1u);
+      s_tk[0] = tk;
+      if (tk < F.total) {
+        int kind, l, tile;
+        decode(tk, kind, l, tile);
+        // the items this tile reads (kind dk, layers d0..d1), each complete
+        int dk = -1, d0 = 0, d1 = 0;
+        if (kind == 1) { dk = 0; d0 = l - 1; d1 = l; }
+        if (kind == 2) { dk = 1; d0 = l; d1 = l + 1; }
+        if (kind == 3) { dk = 2; d0 = l - 1; d1 = l; }
+        if (dk >= 0) {
+          const unsigned need = (unsigned)pick4(F.ntiles, dk);
+          const int lmax = (dk == 1) ? bz : bz - 1;
+          for (int dl = d0; dl <= d1; dl++) {
+            if (dl < 0 || dl > lmax) continue;
+            const unsigned *c = F.cnt + 1 + dk * F.bz1 + dl;
+            int spins = 0;
+            while (ld_acquire(c) < need) {
+              if (++spins > kFlowSpin) {
+                atomicOr(&P.st->status, 2u);
+                break;
+              }
+              __nanosleep(64);
+            }
+          }
+        }
+      }
+    }
+    __syncthreads();
+    const int tk = s_tk[0];
+    if (tk >= F.total) break;
+    int kind, l, tile;
+    decode(tk, kind, l, tile);
+    const int T = pick4(F.tsize, kind);
+    if (kind == 0 || kind == 2) {
+      const int64_t e0 = exy * l + (int64_t)tile * T;
+      const int64_t e1 = min(e0 + T, exy * (l + 1));
+      if (kind == 0) {
+        // positions: not written before this read (L1 is safe)
+        for (int64_t e = e0 + tid; e < e1; e += kFlowThreads)
+          geometry_one<8, false, true>(P, M, vol, e);
+      } else {
+        const long long step = 0;   // thermal coupling is not run here
+        for (int64_t e = e0 + tid; e < e1; e += kFlowThreads) {
+          const GlobalNodes<true, true, false> nd(P, M, e);
+          ForcesToHbm out{M.fe, P.ne, e};
+          element_hex_core<LAW, true, false>(P, M, e, nd, &stash[tid], kFlowThreads, step, out,
+                                             StateInPlace{M.tau, M.pls, P.ne, e});
+        }
+      }
+    } else {
+      const int64_t n0 = pxy * l + (int64_t)tile * T;
+      const int64_t n1 = min(n0 + T, pxy * (l + 1));
+      if (kind == 1) {
+        const float2 zd = die_height(P, P.st->time);   // the step's time (set by the finish)
+        for (int64_t n = n0 + tid; n < n1; n += kFlowThreads)
+          nodal_one<8, true, true>(P, M, vol, n, zd);
+      } else {
+        double r = 0.0;
+        for (int64_t n = n0 + tid; n < n1; n += kFlowThreads)
+          r += (double)node_one<8, true, true>(P, M, n, 0);
+        const double bs = block_sum_dense(r, sh);
+        if (tid == 0) F.partials[(int64_t)l * F.ntiles[3] + tile] = bs;
+      }
+    }
+    // the tile's writes, then its count: a release by one thread after the
+    // barrier (which orders the block's writes before it), by another warp
+    // than the one that takes the next ticket
+    __syncthreads();
+    if (tid == 32) red_release(&F.cnt[1 + kind * F.bz1 + l], 1u);
+  }
+}
+
+// After the dataflow launch: the reaction over the node tiles in (plane,
+// tile) order, and the step state.
+__global__ void __launch_bounds__(kFlowThreads) k_mix_flow_finish(StepParams P, FlowParams F) {
+  __shared__ double sh[kFlowThreads / 32];
+  const int64_t np_t = (int64_t)F.bz1 * F.ntiles[3];
+  double t = 0.0;
+  for (int64_t i = threadIdx.x; i < np_t; i += kFlowThreads) t += F.partials[i];
+  const double tot = block_sum_dense(t, sh);
+  if (threadIdx.x == 0) {
+    const long long s = P.st->step;
+    if (s < P.hist_cap) P.hist[s] = tot;
+    P.st->step = s + 1;
+    P.st->time = P.st->time + P.dt;
   }
 }
 
@@ -1692,6 +2213,127 @@ void mix_shared(const StepParams &P, const MixState &M, const TileParams &T, cud
     k_mix_shared<true><<<(unsigned)mix_shared_grid(T), kNodeThreads, 0, st>>>(P, M, T);
   else
     k_mix_shared<false><<<(unsigned)mix_shared_grid(T), kNodeThreads, 0, st>>>(P, M, T);
+}
+
+namespace {
+using SweepKernel = void (*)(StepParams, MixState, SweepParams);
+template <int CY>
+SweepKernel sweep_kernel_cy(const StepParams &P) {
+  return P.mat_general ? k_mix_sweep<1, CY> : k_mix_sweep<0, CY>;
+}
+// The kernel, its block size and shared memory for W.cy (set up once per
+// kernel and device: the dynamic shared memory above the default 48 KB).
+SweepKernel sweep_kernel(const StepParams &P, const SweepParams &W, int *threads, size_t *smem) {
+  SweepKernel k;
+  if (W.cy == 4) {
+    k = sweep_kernel_cy<4>(P);
+    *threads = SweepShape<4>::threads;
+    *smem = SweepShape<4>::smem;
+  } else {
+    k = sweep_kernel_cy<8>(P);
+    *threads = SweepShape<8>::threads;
+    *smem = SweepShape<8>::smem;
+  }
+  static std::mutex mu;
+  static std::map<std::pair<const void *, int>, bool> set;   // (kernel, device)
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lock(mu);
+  bool &done = set[std::make_pair((const void *)k, dev)];
+  if (!done) {
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)*smem);
+    done = true;
+  }
+  return k;
+}
+}  // namespace
+
+int sweep_columns(const StepParams &P, SweepParams &W) {
+  if (W.cy != 4) W.cy = 8;
+  W.ncx = (P.bx + 1 + (kSwEX - 1) - 1) / (kSwEX - 1);
+  W.ncy = (P.by + 1 + W.cy - 1) / W.cy;
+  return W.ncx * W.ncy;
+}
+
+bool sweep_fits(const StepParams &P, const SweepParams &W) {
+  int threads = 0;
+  size_t smem = 0;
+  const SweepKernel k = sweep_kernel(P, W, &threads, &smem);
+  int blocks = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k, threads, smem) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return blocks >= 1;
+}
+
+void mix_sweep(const StepParams &P, const MixState &M, const SweepParams &W, cudaStream_t st) {
+  int threads = 0;
+  size_t smem = 0;
+  const SweepKernel k = sweep_kernel(P, W, &threads, &smem);
+  k<<<(unsigned)(W.ncx * W.ncy), threads, smem, st>>>(P, M, W);
+}
+
+int flow_grid(const StepParams &P) {
+  auto kern = P.mat_general ? k_mix_flow<1> : k_mix_flow<0>;
+  // the stage table's shared memory at the largest mesh the step takes
+  const size_t smem = sizeof(int) * (kFlowMaxLayers + 20);
+  static std::mutex mu;
+  static std::map<std::pair<const void *, int>, bool> set;   // (kernel, device)
+  int dev = 0;
+  cudaGetDevice(&dev);
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    bool &done = set[std::make_pair((const void *)kern, dev)];
+    if (!done) {
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      done = true;
+    }
+  }
+  int per = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, kFlowThreads, smem) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return per * P.sms;
+}
+
+void flow_stages(const StepParams &P, int tile, int lag, std::vector<int> &first, FlowParams &F) {
+  const int64_t exy = (int64_t)P.bx * P.by, pxy = (int64_t)(P.bx + 1) * (P.by + 1);
+  const int bz = P.bz;
+  // the light phases (geometry, nodal) in tiles four times larger
+  F.tsize[0] = F.tsize[1] = 4 * tile;
+  F.tsize[2] = F.tsize[3] = tile;
+  const int64_t per[kFlowKinds] = {exy, pxy, exy, pxy};
+  for (int q = 0; q < kFlowKinds; q++)
+    F.ntiles[q] = (int)((per[q] + F.tsize[q] - 1) / F.tsize[q]);
+  // stage offsets 0, lag/3, 2 lag/3, lag: each phase a third of the lag
+  // behind the one it reads
+  F.off[0] = 0;
+  F.off[1] = std::max(1, lag / 3);
+  F.off[2] = std::max(F.off[1] + 1, 2 * lag / 3);
+  F.off[3] = std::max(F.off[2] + 1, lag);
+  F.nstages = bz + F.off[3] + 1;
+  first.assign(F.nstages + 1, 0);
+  int t = 0;
+  for (int s = 0; s < F.nstages; s++) {
+    first[s] = t;
+    for (int q = 0; q < kFlowKinds; q++) {
+      const int l = s - F.off[q], lmax = (q == 0 || q == 2) ? bz - 1 : bz;
+      if (l >= 0 && l <= lmax) t += F.ntiles[q];
+    }
+  }
+  first[F.nstages] = t;
+  F.total = t;
+  F.bz1 = bz + 1;
+  F.ncnt = 1 + kFlowKinds * F.bz1;
+}
+
+void mix_flow(const StepParams &P, const MixState &M, float *vol, const FlowParams &F,
+              cudaStream_t st) {
+  auto kern = P.mat_general ? k_mix_flow<1> : k_mix_flow<0>;
+  kern<<<(unsigned)F.grid, kFlowThreads, sizeof(int) * (F.nstages + 1), st>>>(P, M, vol, F);
+  k_mix_flow_finish<<<1, kFlowThreads, 0, st>>>(P, F);
 }
 
 int mix_cluster_fits(const StepParams &P, const MixState &M, float *vol, int blocks, int bs) {
