@@ -86,3 +86,28 @@ def test_non_box_numbering_reads_the_arrays():
     W.apply(t, W.config(1, scale=(4, 4, 4)))
     t.init()
     assert t.box() == (0, 0, 0)             # tetrahedra
+
+
+@pytest.mark.parametrize("cid,scale", [(2, (40, 36, 24)), (0, (20, 20, 20)), (2, (70, 9, 3))])
+def test_min_edge_length_over_grid_edges_equals_element_edges(cid, scale):
+    """Box meshes take the shortest edge over the grid edges (each once); the
+    value is the element loop's bit for bit, and the oracle's."""
+    case = W.config(cid, scale=scale)
+    a = run(case, True, 0)
+    b = run(case, False, 0)
+    assert a.box() == case.nel and b.box() == (0, 0, 0)
+    ha, hb = a.min_edge_length(), b.min_edge_length()
+    assert ha == hb
+    assert ha == W.min_edge_length(case.coords(), case.elnod())
+
+
+def test_node_vec_into_caller_buffer():
+    case = W.config(0, scale=(6, 6, 6))
+    d = run(case, True, 30)
+    want = d.node_vec("u")
+    buf = np.full(case.n_node * 3, np.nan)
+    got = d.node_vec("u", out=buf)
+    assert got.base is buf or got is buf or np.shares_memory(got, buf)
+    np.testing.assert_array_equal(got, want)
+    with pytest.raises(ValueError):
+        d.node_vec("u", out=np.zeros(case.n_node * 3, np.float32))

@@ -538,9 +538,15 @@ class Domain:
         self._call("wf_prepare_run", int(n))
 
     # readback ---------------------------------------------------------
-    def node_vec(self, name):
-        out = np.zeros(self.nn * 3)
-        self._call("wf_get_node_field", NODE_VEC[name], out)
+    def node_vec(self, name, out=None):
+        """A node field as [nn, 3]; `out` (a C-contiguous float64 array of nn * 3
+        values, pinned or already written to for the fastest copy) is filled
+        instead of a new array."""
+        if out is None:
+            out = np.zeros(self.nn * 3)
+        elif not (out.dtype == np.float64 and out.flags.c_contiguous and out.size == self.nn * 3):
+            raise ValueError("out must be a C-contiguous float64 array of nn * 3 values")
+        self._call("wf_get_node_field", NODE_VEC[name], out.reshape(-1))
         return out.reshape(-1, 3)
 
     def node_scalar(self, name):

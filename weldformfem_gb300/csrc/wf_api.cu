@@ -126,6 +126,14 @@ struct wf_domain {
   // host mesh
   int32_t npe = 0;
   int64_t nn = 0, ne = 0, np = 0;
+  // the mesh as set, on the device ([nn][3] coordinates, [ne][npe]
+  // connectivity, from the library's pool): uploaded by wf_set_mesh and
+  // wf_add_box_length; x and elnod mirror it on the host once a host caller
+  // needs them (mesh_host)
+  double *mesh_x = nullptr;
+  int32_t *mesh_el = nullptr;
+  int32_t *mesh_flag = nullptr;   // scratch of the connectivity check
+  bool mesh_host = false;
   hvec<double> x;                 // interleaved [3 nn]
   hvec<int32_t> elnod;            // [ne npe]
   // node -> element lists on the host, built when a host caller needs them
@@ -249,6 +257,7 @@ struct wf_domain {
   int32_t flow_tile = 512, flow_lag = 12;
   int cl_blocks = 0, cl_bs = 0;
   double *cl_part = nullptr;      // [kClusterChunk][cl_blocks] reaction partials
+  double *edge_min = nullptr;     // the shortest edge (wf_min_edge_length's device result)
   // batched ensemble
   int32_t nspec = 0;
   std::vector<int64_t> spec_eoff, spec_noff;
@@ -296,10 +305,51 @@ wf_status fail(wf_domain *d, wf_status s, const char *fmt, ...) {
 
 // Device allocation freed with the domain, left uninitialised (the caller
 // writes every element).
+// Device memory of the domains comes from one stream-ordered pool per device
+// that keeps what domains give back (release threshold: all of it): a domain
+// set up after another of its size takes memory that is already mapped
+// instead of mapping new pages. Allocations and frees are ordered on the
+// domain's stream.
+cudaError_t device_pool(int dev, cudaMemPool_t *out) {
+  static std::mutex mu;
+  static std::map<int, cudaMemPool_t> pools;
+  std::lock_guard<std::mutex> lock(mu);
+  auto it = pools.find(dev);
+  if (it != pools.end()) {
+    *out = it->second;
+    return cudaSuccess;
+  }
+  cudaMemPoolProps props = {};
+  props.allocType = cudaMemAllocationTypePinned;
+  props.location.type = cudaMemLocationTypeDevice;
+  props.location.id = dev;
+  cudaMemPool_t pool = nullptr;
+  cudaError_t e = cudaMemPoolCreate(&pool, &props);
+  if (e != cudaSuccess) return e;
+  uint64_t keep = UINT64_MAX;
+  e = cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  if (e != cudaSuccess) return e;
+  pools[dev] = pool;
+  *out = pool;
+  return cudaSuccess;
+}
+
+cudaError_t pool_alloc(wf_domain *d, void **q, size_t bytes) {
+  cudaMemPool_t pool = nullptr;
+  cudaError_t e = device_pool(d->device, &pool);
+  if (e != cudaSuccess) return e;
+  return cudaMallocFromPoolAsync(q, std::max<size_t>(bytes, 1), pool, d->stream);
+}
+
+// The device copy of the mesh and its host mirror (defined with the mesh
+// entry points).
+void free_mesh_dev(wf_domain *d);
+wf_status host_mesh(const wf_domain *cd);
+
 template <typename T>
 cudaError_t dalloc_raw(wf_domain *d, T **p, size_t count) {
   void *q = nullptr;
-  cudaError_t e = cudaMalloc(&q, std::max<size_t>(count, 1) * sizeof(T));
+  cudaError_t e = pool_alloc(d, &q, std::max<size_t>(count, 1) * sizeof(T));
   if (e != cudaSuccess) return e;
   d->allocs.push_back(q);
   *p = static_cast<T *>(q);
@@ -309,7 +359,7 @@ cudaError_t dalloc_raw(wf_domain *d, T **p, size_t count) {
 template <typename T>
 cudaError_t dalloc(wf_domain *d, T **p, size_t count) {
   void *q = nullptr;
-  cudaError_t e = cudaMalloc(&q, std::max<size_t>(count, 1) * sizeof(T));
+  cudaError_t e = pool_alloc(d, &q, std::max<size_t>(count, 1) * sizeof(T));
   if (e != cudaSuccess) return e;
   d->allocs.push_back(q);
   *p = static_cast<T *>(q);
@@ -331,7 +381,10 @@ void free_adjoint(wf_domain *d) {
 void free_device(wf_domain *d) {
   free_adjoint(d);
   drop_graphs(d);
-  for (void *p : d->allocs) cudaFree(p);
+  // nothing of the domain's may still run when its memory goes back
+  if (d->stream) cudaStreamSynchronize(d->stream);
+  if (d->out_stream) cudaStreamSynchronize(d->out_stream);
+  for (void *p : d->allocs) cudaFreeAsync(p, d->stream);
   d->allocs.clear();
   if (d->st_host) cudaFreeHost(d->st_host);
   d->st_host = nullptr;
@@ -346,7 +399,7 @@ void free_device(wf_domain *d) {
   d->snap_next = 0;
   d->surf_ext.clear();
   d->surf_area.clear();
-  if (d->init_stage) cudaFree(d->init_stage);
+  if (d->init_stage) cudaFreeAsync(d->init_stage, d->stream);
   d->init_stage = nullptr;
   for (cudaEvent_t ev : d->ev_pool) cudaEventDestroy(ev);
   d->ev_pool.clear();
@@ -357,6 +410,15 @@ void free_device(wf_domain *d) {
   d->mvol = nullptr;
   d->tiled = false;
   d->T = TileParams{};
+  d->edge_min = nullptr;
+  d->sweep = d->flow = false;
+  d->W = SweepParams{};
+  d->F = FlowParams{};
+  for (int k = 0; k < 2; k++) {
+    d->xh_pair[k] = nullptr;
+    d->vp_pair[k] = d->tau_pair[k] = d->pls_pair[k] = nullptr;
+    d->flow_cnt[k] = nullptr;
+  }
   d->initialized = false;
 }
 
@@ -523,6 +585,7 @@ bool ensure_host_lists(const wf_domain *cd) {
   wf_domain *d = const_cast<wf_domain *>(cd);
   if (d->nodel_off.size() == (size_t)d->nn + 1) return true;
   if (d->initialized && d->P.slot) return download_lists(d);
+  if (host_mesh(d) != WF_OK) return false;
   build_nodel(d);
   return true;
 }
@@ -640,6 +703,10 @@ void part_surface(const wf_domain *d, std::vector<uint8_t> &ext, std::vector<dou
 
 void reset_mesh(wf_domain *d) {
   free_device(d);
+  free_mesh_dev(d);
+  d->x = hvec<double>();
+  d->elnod = hvec<int32_t>();
+  d->mesh_host = false;
   for (int k = 0; k < 3; k++) {
     d->bc_nod[k].clear();
     d->bc_val[k].clear();
@@ -668,6 +735,52 @@ void reset_mesh(wf_domain *d) {
 wf_status need_mesh(wf_domain *d) {
   if (!d) return WF_ERR_ARG;
   if (d->nn <= 0) return fail(d, WF_ERR_STATE, "no mesh defined");
+  return WF_OK;
+}
+
+// Frees the device copy of the mesh.
+void free_mesh_dev(wf_domain *d) {
+  if (d->stream) cudaStreamSynchronize(d->stream);
+  if (d->mesh_x) cudaFreeAsync(d->mesh_x, d->stream);
+  if (d->mesh_el) cudaFreeAsync(d->mesh_el, d->stream);
+  if (d->mesh_flag) cudaFreeAsync(d->mesh_flag, d->stream);
+  d->mesh_x = nullptr;
+  d->mesh_el = nullptr;
+  d->mesh_flag = nullptr;
+}
+
+// Uploads the mesh (nn, ne, npe set) into its device copy and checks there
+// that every connectivity entry names a node in [0, nn). Returns once the
+// copies are done: the caller's arrays can go.
+wf_status mesh_upload(wf_domain *d, const double *xyz, const int32_t *el) {
+  CUDA_TRY(cudaSetDevice(d->device));
+  free_mesh_dev(d);
+  const size_t xb = sizeof(double) * 3 * d->nn, eb = sizeof(int32_t) * d->ne * d->npe;
+  CUDA_TRY(pool_alloc(d, reinterpret_cast<void **>(&d->mesh_x), xb));
+  CUDA_TRY(pool_alloc(d, reinterpret_cast<void **>(&d->mesh_el), eb));
+  CUDA_TRY(pool_alloc(d, reinterpret_cast<void **>(&d->mesh_flag), sizeof(int32_t)));
+  CUDA_TRY(cudaMemcpyAsync(d->mesh_x, xyz, xb, cudaMemcpyHostToDevice, d->stream));
+  CUDA_TRY(cudaMemcpyAsync(d->mesh_el, el, eb, cudaMemcpyHostToDevice, d->stream));
+  d->h2d_bytes += (int64_t)(xb + eb);
+  int bad = 1;
+  CUDA_TRY(check_connectivity(d->mesh_el, d->ne * d->npe, d->nn, d->mesh_flag, d->stream, &bad));
+  if (bad) return fail(d, WF_ERR_ARG, "connectivity references a node outside [0, nn)");
+  return WF_OK;
+}
+
+// The host mirror of the mesh, downloaded from the device copy on first use.
+wf_status host_mesh(const wf_domain *cd) {
+  wf_domain *d = const_cast<wf_domain *>(cd);
+  if (d->mesh_host || d->nn <= 0) return WF_OK;
+  CUDA_TRY(cudaSetDevice(d->device));
+  d->x.resize(3 * d->nn);
+  d->elnod.resize(d->ne * d->npe);
+  CUDA_TRY(cudaMemcpyAsync(d->x.data(), d->mesh_x, sizeof(double) * 3 * d->nn,
+                           cudaMemcpyDeviceToHost, d->stream));
+  CUDA_TRY(cudaMemcpyAsync(d->elnod.data(), d->mesh_el, sizeof(int32_t) * d->ne * d->npe,
+                           cudaMemcpyDeviceToHost, d->stream));
+  CUDA_TRY(cudaStreamSynchronize(d->stream));
+  d->mesh_host = true;
   return WF_OK;
 }
 
@@ -724,6 +837,7 @@ WF_API wf_status wf_domain_destroy(wf_domain *d) {
   if (d->stream) cudaStreamSynchronize(d->stream);
   if (d->out_stream) cudaStreamSynchronize(d->out_stream);
   free_device(d);
+  free_mesh_dev(d);
   if (d->stream) cudaStreamDestroy(d->stream);
   if (d->out_stream) cudaStreamDestroy(d->out_stream);
   delete d;
@@ -747,9 +861,15 @@ WF_API wf_status wf_add_box_length(wf_domain *d, const double V[3], const double
   }
   d->x.assign(bx.begin(), bx.end());
   d->elnod.assign(be.begin(), be.end());
+  d->mesh_host = true;
   d->npe = tritetra ? 4 : 8;
   d->nn = (int64_t)(d->x.size() / 3);
   d->ne = (int64_t)(d->elnod.size() / d->npe);
+  const wf_status s = mesh_upload(d, d->x.data(), d->elnod.data());
+  if (s) {
+    d->nn = d->ne = 0;
+    return s;
+  }
   return WF_OK;
 }
 
@@ -764,27 +884,13 @@ WF_API wf_status wf_set_mesh(wf_domain *d, int64_t nn, int64_t ne, int32_t npe, 
   d->npe = npe;
   d->nn = nn;
   d->ne = ne;
-  d->x.resize(3 * nn);
-  d->elnod.resize(ne * npe);
-  double *xd = d->x.data();
-  int32_t *ed = d->elnod.data();
-  host_parallel(3 * nn, [&](int64_t i0, int64_t i1) {
-    std::memcpy(xd + i0, xyz + i0, sizeof(double) * (i1 - i0));
-  });
-  // copied and checked in one pass: every entry names a node in [0, nn)
-  std::atomic<bool> bad{false};
-  host_parallel(ne * npe, [&](int64_t i0, int64_t i1) {
-    bool b = false;
-    for (int64_t i = i0; i < i1; i++) {
-      const int32_t v = elnod[i];
-      ed[i] = v;
-      b |= (v < 0) | (v >= nn);
-    }
-    if (b) bad = true;
-  });
-  if (bad) {
+  // straight to the device copy (no host copy: the host mirror is made when
+  // a host caller needs it); the range check runs there
+  const wf_status s = mesh_upload(d, xyz, elnod);
+  if (s) {
     d->nn = d->ne = 0;
-    return fail(d, WF_ERR_ARG, "connectivity references a node outside [0, nn)");
+    free_mesh_dev(d);
+    return s;
   }
   return WF_OK;
 }
@@ -794,9 +900,11 @@ WF_API wf_status wf_set_node(wf_domain *d, int64_t n, double x, double y, double
   if (s) return s;
   if (n < 0 || n >= d->nn) return fail(d, WF_ERR_ARG, "node %lld out of range", (long long)n);
   if (d->initialized) return fail(d, WF_ERR_STATE, "setNode after init");
-  d->x[3 * n] = x;
-  d->x[3 * n + 1] = y;
-  d->x[3 * n + 2] = z;
+  const double v[3] = {x, y, z};
+  if (d->mesh_host) std::memcpy(&d->x[3 * n], v, sizeof(v));
+  CUDA_TRY(cudaSetDevice(d->device));
+  CUDA_TRY(cudaMemcpyAsync(d->mesh_x + 3 * n, v, sizeof(v), cudaMemcpyHostToDevice, d->stream));
+  CUDA_TRY(cudaStreamSynchronize(d->stream));
   return WF_OK;
 }
 
@@ -805,7 +913,12 @@ WF_API wf_status wf_set_nodes(wf_domain *d, const double *xyz) {
   if (s) return s;
   if (!xyz) return WF_ERR_ARG;
   if (d->initialized) return fail(d, WF_ERR_STATE, "setNode after init");
-  std::memcpy(d->x.data(), xyz, sizeof(double) * 3 * d->nn);
+  if (d->mesh_host) std::memcpy(d->x.data(), xyz, sizeof(double) * 3 * d->nn);
+  CUDA_TRY(cudaSetDevice(d->device));
+  CUDA_TRY(cudaMemcpyAsync(d->mesh_x, xyz, sizeof(double) * 3 * d->nn, cudaMemcpyHostToDevice,
+                           d->stream));
+  CUDA_TRY(cudaStreamSynchronize(d->stream));
+  d->h2d_bytes += (int64_t)(sizeof(double) * 3 * d->nn);
   return WF_OK;
 }
 
@@ -824,7 +937,11 @@ WF_API wf_status wf_get_connectivity(const wf_domain *d, int32_t *elnod, int32_t
   if (!d) return WF_ERR_ARG;
   if ((nodel || nodel_loc || offset || count) && !ensure_host_lists(d))
     return fail(const_cast<wf_domain *>(d), WF_ERR_CUDA, "reading back the node lists failed");
-  if (elnod) std::copy(d->elnod.begin(), d->elnod.end(), elnod);
+  if (elnod) {
+    const wf_status hs = host_mesh(d);
+    if (hs) return hs;
+    std::copy(d->elnod.begin(), d->elnod.end(), elnod);
+  }
   if (nodel) std::copy(d->nodel.begin(), d->nodel.end(), nodel);
   if (nodel_loc) std::copy(d->nodel_loc.begin(), d->nodel_loc.end(), nodel_loc);
   if (offset) std::copy(d->nodel_off.begin(), d->nodel_off.begin() + d->nn, offset);
@@ -948,6 +1065,8 @@ WF_API wf_status wf_add_bc_vel_zone(wf_domain *d, const double start[3], const d
   wf_status s = need_mesh(d);
   if (s) return s;
   if (!start || !end || !vel) return WF_ERR_ARG;
+  s = host_mesh(d);
+  if (s) return s;
   int64_t c = 0;
   for (int64_t a = 0; a < d->nn; a++) {
     bool in = true;
@@ -1144,6 +1263,8 @@ WF_API wf_status wf_set_specimens(wf_domain *d, int32_t nspec, const int64_t *el
   if (d->initialized) return fail(d, WF_ERR_STATE, "specimens must be set before init");
   if (elem_off[0] != 0 || node_off[0] != 0 || elem_off[nspec] != d->ne || node_off[nspec] != d->nn)
     return fail(d, WF_ERR_ARG, "specimen offsets must start at 0 and end at the mesh sizes");
+  s = host_mesh(d);
+  if (s) return s;
   for (int32_t k = 0; k < nspec; k++) {
     if (elem_off[k + 1] <= elem_off[k] || node_off[k + 1] <= node_off[k])
       return fail(d, WF_ERR_ARG, "specimen %d is empty or offsets decrease", k);
@@ -1284,7 +1405,15 @@ void host_bbox(const wf_domain *d, double bb[6]) {
 void box_dims(const wf_domain *d, int *nx, int *ny, int *nz) {
   *nx = *ny = *nz = 0;
   if (d->npe != 8 || d->ne <= 0) return;
-  const int32_t *e0 = d->elnod.data();
+  int32_t first[8];
+  const int32_t *e0 = first;
+  if (d->mesh_host) {
+    e0 = d->elnod.data();
+  } else if (cudaMemcpy(first, d->mesh_el, sizeof(first), cudaMemcpyDeviceToHost) !=
+             cudaSuccess) {
+    cudaGetLastError();
+    return;
+  }
   const int64_t px = (int64_t)e0[3] - e0[0];
   if (e0[0] != 0 || px < 2 || e0[4] % px != 0) return;
   const int64_t py = e0[4] / px;
@@ -1364,7 +1493,7 @@ wf_status autotune_launches(wf_domain *d) {
   // the state the trials advance, saved in a device scratch buffer
   const size_t n_tau = 6 * ne, n_pls = ne, n_ut = 3 * np, n_cf = 3 * np;
   float *save = nullptr;
-  CUDA_TRY(cudaMalloc(&save, 4 * (n_tau + n_pls + n_ut + n_cf)));
+  CUDA_TRY(pool_alloc(d, reinterpret_cast<void **>(&save), 4 * (n_tau + n_pls + n_ut + n_cf)));
   float *s_tau = save, *s_pls = s_tau + n_tau, *s_ut = s_pls + n_pls, *s_cf = s_ut + n_ut;
   CUDA_TRY(cudaMemcpyAsync(s_tau, M.tau, 4 * n_tau, cudaMemcpyDeviceToDevice, d->stream));
   CUDA_TRY(cudaMemcpyAsync(s_pls, M.pls, 4 * n_pls, cudaMemcpyDeviceToDevice, d->stream));
@@ -1434,7 +1563,7 @@ wf_status autotune_launches(wf_domain *d) {
   CUDA_TRY(cudaMemcpyAsync(M.ut, s_ut, 4 * n_ut, cudaMemcpyDeviceToDevice, d->stream));
   CUDA_TRY(cudaMemcpyAsync(M.cf, s_cf, 4 * n_cf, cudaMemcpyDeviceToDevice, d->stream));
   CUDA_TRY(cudaStreamSynchronize(d->stream));
-  CUDA_TRY(cudaFree(save));
+  CUDA_TRY(cudaFreeAsync(save, d->stream));
   {
     std::lock_guard<std::mutex> lock(g_tune_mu);
     TuneResult r;
@@ -1714,23 +1843,15 @@ WF_API wf_status wf_init(wf_domain *d) {
   P.elnod = el;
   P.off = off;
   P.slot = sl;
-  double *x_aos = nullptr;
+  // the AoS uploads are the mesh's device copy (wf_set_mesh); only the
+  // connectivity scratch is allocated here
+  const double *x_aos = d->mesh_x;
   {
-    const size_t el_bytes = sizeof(int32_t) * ent, x_bytes = sizeof(double) * 3 * nn;
-    const size_t scratch_bytes = sizeof(int32_t) * connectivity_scratch_ints(nn);
-    const size_t x_at = (el_bytes + 255) / 256 * 256, sc_at = x_at + (x_bytes + 255) / 256 * 256;
     void *stage = nullptr;
-    CUDA_TRY(cudaMalloc(&stage, sc_at + scratch_bytes));
+    CUDA_TRY(pool_alloc(d, &stage, sizeof(int32_t) * connectivity_scratch_ints(nn)));
     d->init_stage = stage;
-    char *base = static_cast<char *>(stage);
-    int32_t *el_aos = reinterpret_cast<int32_t *>(base);
-    x_aos = reinterpret_cast<double *>(base + x_at);
-    CUDA_TRY(cudaMemcpyAsync(el_aos, d->elnod.data(), el_bytes, cudaMemcpyHostToDevice,
-                             d->stream));
-    CUDA_TRY(cudaMemcpyAsync(x_aos, d->x.data(), x_bytes, cudaMemcpyHostToDevice, d->stream));
-    d->h2d_bytes += (int64_t)(el_bytes + x_bytes);
-    CUDA_TRY(build_connectivity(el_aos, ne, d->npe, nn, el, off, sl,
-                                reinterpret_cast<int32_t *>(base + sc_at), d->stream));
+    CUDA_TRY(build_connectivity(d->mesh_el, ne, d->npe, nn, el, off, sl,
+                                static_cast<int32_t *>(stage), d->stream));
   }
   std::vector<uint32_t> code;
   std::vector<double> vals;
@@ -1749,6 +1870,10 @@ WF_API wf_status wf_init(wf_domain *d) {
     std::vector<uint8_t> ext;
     std::vector<double> area, nodlen, nrm, pp;
     if (!ensure_host_lists(d)) return fail(d, WF_ERR_CUDA, "reading back the node lists failed");
+    {
+      const wf_status hs = host_mesh(d);
+      if (hs) return hs;
+    }
     part_surface(d, ext, area, nodlen);
     for (int64_t n = 0; n < nn; n++)
       if (ext[n]) flags[n] |= NF_CONTACT;
@@ -1966,6 +2091,10 @@ WF_API wf_status wf_init(wf_domain *d) {
     }
     if (d->tri) {
       // FP32 die copies relative to the centre of the part's bounding box
+      {
+        const wf_status hs = host_mesh(d);
+        if (hs) return hs;
+      }
       double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
       for (int64_t n = 0; n < nn; n++)
         for (int k = 0; k < 3; k++) {
@@ -2067,6 +2196,10 @@ WF_API wf_status wf_init(wf_domain *d) {
     else if (d->step_mode != 3) d->tile_why = "step mode 3 not set before wf_init";
     if (d->tile_why.empty()) {
       double bb[6];
+      {
+        const wf_status hs = host_mesh(d);
+        if (hs) return hs;
+      }
       host_bbox(d, bb);
       CUDA_TRY(build_tiles(P.elnod, S.x, np, ne, nn, P.off, bb, kSharedThreads, keep_alloc, d,
                            d->stream, d->T, d->tile_why));
@@ -2151,7 +2284,7 @@ WF_API wf_status wf_init(wf_domain *d) {
     }
   }
   CUDA_TRY(cudaStreamSynchronize(d->stream));
-  CUDA_TRY(cudaFree(d->init_stage));
+  CUDA_TRY(cudaFreeAsync(d->init_stage, d->stream));
   d->init_stage = nullptr;
   d->initialized = true;
   d->host_step = 0;
@@ -2658,13 +2791,16 @@ WF_API wf_status wf_min_edge_length(wf_domain *d, double *hmin) {
   if (!hmin) return WF_ERR_ARG;
   if (!d->initialized) return fail(d, WF_ERR_STATE, "wf_init not called");
   CUDA_TRY(cudaSetDevice(d->device));
-  double *out = nullptr;
-  CUDA_TRY(dalloc(d, &out, 1));
+  if (!d->edge_min) CUDA_TRY(dalloc(d, &d->edge_min, 1));
+  double *out = d->edge_min;
   if (d->precision == WF_MIXED && !d->mix_valid_fp64) {
     mix_export(d->P, d->M, d->S, d->mvol, d->stream);
     d->mix_valid_fp64 = true;
   }
-  min_edge_length(d->P.elnod, d->S.x, d->np, d->ne, d->npe, out, d->stream);
+  if (d->P.box)
+    min_edge_length_box(d->S.x, d->np, d->P.bx, d->P.by, d->P.bz, out, d->stream);
+  else
+    min_edge_length(d->P.elnod, d->S.x, d->np, d->ne, d->npe, out, d->stream);
   CUDA_TRY(cudaGetLastError());
   CUDA_TRY(cudaMemcpyAsync(hmin, out, sizeof(double), cudaMemcpyDeviceToHost, d->stream));
   CUDA_TRY(cudaStreamSynchronize(d->stream));
@@ -2738,6 +2874,8 @@ WF_API wf_status wf_get_node_scalar(wf_domain *d, int32_t field, double *out) {
   }
   if (field == WF_NODE_PRESSURE) {
     // calcNodalPressureFromElemental (Mechanical.C:1187-1213), serial order
+    s = host_mesh(d);
+    if (s) return s;
     std::vector<double> p(d->ne), vol(d->ne);
     s = copy_plain(d, d->S.p, p.data(), d->ne);
     if (s) return s;
@@ -2845,6 +2983,10 @@ SnapLayout snap_layout(const wf_domain *d) {
 
 // The static parts of a VTK view: connectivity, surface, die triangles.
 wf_status vtk_static(wf_domain *d, VtkView &v) {
+  {
+    const wf_status hs = host_mesh(d);
+    if (hs) return hs;
+  }
   v.nn = d->nn;
   v.ne = d->ne;
   v.npe = d->npe;
@@ -2934,7 +3076,8 @@ WF_API wf_status wf_write_vtk(wf_domain *d, const char *path) {
   if (e != cudaSuccess) return fail(d, WF_ERR_CUDA, "wf_write_vtk: %s", cudaGetErrorString(e));
   d->d2h_bytes += (int64_t)(sizeof(double) * L.count);
   VtkView v;
-  vtk_static(d, v);
+  s = vtk_static(d, v);
+  if (s) return s;
   vtk_fields(d, L, host.data(), v);
   if (!write_vtk_text(path, v)) return fail(d, WF_ERR_ARG, "cannot write %s", path);
   return WF_OK;
@@ -2985,7 +3128,10 @@ WF_API wf_status wf_write_snapshot_vtk(wf_domain *d, int32_t slot, const char *p
   CUDA_TRY(cudaEventSynchronize(sn.done));
   const SnapLayout L = snap_layout(d);
   VtkView v;
-  vtk_static(d, v);
+  {
+    const wf_status vs = vtk_static(d, v);
+    if (vs) return vs;
+  }
   vtk_fields(d, L, sn.host, v);
   sn.state = 0;
   if (!write_vtk_text(path, v)) return fail(d, WF_ERR_ARG, "cannot write %s", path);

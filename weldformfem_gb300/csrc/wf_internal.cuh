@@ -367,6 +367,10 @@ void energy_mixed(const StepParams &P, const MixState &M, cudaStream_t st);
 // Minimum element edge length over the mesh (exact: min is order-free).
 void min_edge_length(const int32_t *elnod, const double *x, int64_t np, int64_t ne, int npe,
                      double *out_dev, cudaStream_t st);
+// Box meshes (AddBoxLength numbering, nx x ny x nz elements): the same
+// minimum over the grid edges, each edge once.
+void min_edge_length_box(const double *x, int64_t np, int32_t bx, int32_t by, int32_t bz,
+                         double *out_dev, cudaStream_t st);
 
 // ---- device setup (wf_setup.cu) ------------------------------------------------
 // Node -> element lists from the AoS connectivity on the device: SoA element
@@ -374,6 +378,10 @@ void min_edge_length(const int32_t *elnod, const double *x, int64_t np, int64_t 
 // node's list (the host build's order). scratch holds
 // connectivity_scratch_ints(nn) ints.
 int64_t connectivity_scratch_ints(int64_t nn);
+// Whether every entry of el[0, n) names a node in [0, nn) (*bad = 0), on the
+// device; flag: one device int of scratch. Synchronises st.
+cudaError_t check_connectivity(const int32_t *el, int64_t n, int64_t nn, int32_t *flag,
+                               cudaStream_t st, int *bad);
 cudaError_t build_connectivity(const int32_t *el_aos, int64_t ne, int npe, int64_t nn,
                                int32_t *el_soa, int32_t *off, int32_t *slot, int32_t *scratch,
                                cudaStream_t st);

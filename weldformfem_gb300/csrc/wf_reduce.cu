@@ -10,9 +10,12 @@ namespace {
 
 constexpr int kThreads = 256;
 
-__device__ __forceinline__ double edge_len(const double *x, int64_t np, int32_t a, int32_t b) {
+__device__ __forceinline__ double edge_len2(const double *x, int64_t np, int64_t a, int64_t b) {
   const double dx = x[b] - x[a], dy = x[np + b] - x[np + a], dz = x[2 * np + b] - x[2 * np + a];
-  return sqrt(dx * dx + dy * dy + dz * dz);
+  return dx * dx + dy * dy + dz * dz;
+}
+__device__ __forceinline__ double edge_len(const double *x, int64_t np, int32_t a, int32_t b) {
+  return sqrt(edge_len2(x, np, a, b));
 }
 
 // Shortest element edge (hexahedron: 12 edges, tetrahedron: 6), reduced with
@@ -35,6 +38,34 @@ __global__ void k_min_edge(const int32_t *elnod, const double *x, int64_t np, in
       for (int k = 0; k < 6; k++) best = fmin(best, edge_len(x, np, n[E[k][0]], n[E[k][1]]));
     }
   }
+  for (int o = 16; o > 0; o >>= 1) best = fmin(best, __shfl_down_sync(0xffffffffu, best, o));
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = best;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int i = 1; i < kThreads / 32; i++) best = fmin(best, sh[i]);
+    atomicMin(out, (unsigned long long)__double_as_longlong(best));
+  }
+}
+
+// Box meshes: every element edge joins a node to its +x, +y or +z neighbour,
+// so the shortest edge is the shortest of those grid edges, each taken once
+// (a quarter of the element edges). The squared lengths are the element
+// kernel's (a reversed edge negates the differences exactly), and sqrt is
+// correctly rounded and monotone, so the minimum of the squares' root is the
+// element kernel's minimum bit for bit.
+__global__ void k_min_edge_box(const double *x, int64_t np, int32_t bx, int32_t by, int32_t bz,
+                               unsigned long long *out) {
+  __shared__ double sh[kThreads / 32];
+  const int64_t nx1 = bx + 1, nxy = nx1 * (by + 1), nn = nxy * (bz + 1);
+  double best2 = 1.0e300;
+  for (int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; n < nn;
+       n += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t k = n / nxy, r = n - k * nxy, j = r / nx1, i = r - j * nx1;
+    if (i < bx) best2 = fmin(best2, edge_len2(x, np, n, n + 1));
+    if (j < by) best2 = fmin(best2, edge_len2(x, np, n, n + nx1));
+    if (k < bz) best2 = fmin(best2, edge_len2(x, np, n, n + nxy));
+  }
+  double best = sqrt(best2);
   for (int o = 16; o > 0; o >>= 1) best = fmin(best, __shfl_down_sync(0xffffffffu, best, o));
   if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = best;
   __syncthreads();
@@ -174,6 +205,18 @@ void min_edge_length(const int32_t *elnod, const double *x, int64_t np, int64_t 
   k_set<<<1, 1, 0, st>>>(o, bits);
   int grid = (int)std::min<int64_t>((ne + kThreads - 1) / kThreads, 152 * 8);
   k_min_edge<<<grid, kThreads, 0, st>>>(elnod, x, np, ne, npe, o);
+}
+
+void min_edge_length_box(const double *x, int64_t np, int32_t bx, int32_t by, int32_t bz,
+                         double *out_dev, cudaStream_t st) {
+  unsigned long long *o = reinterpret_cast<unsigned long long *>(out_dev);
+  const double big = 1.0e300;
+  unsigned long long bits;
+  std::memcpy(&bits, &big, sizeof(bits));
+  k_set<<<1, 1, 0, st>>>(o, bits);
+  const int64_t nn = (int64_t)(bx + 1) * (by + 1) * (bz + 1);
+  int grid = (int)std::min<int64_t>((nn + kThreads - 1) / kThreads, 152 * 8);
+  k_min_edge_box<<<grid, kThreads, 0, st>>>(x, np, bx, by, bz, o);
 }
 
 }  // namespace wf

@@ -374,6 +374,34 @@ __global__ void k_box_check(const int32_t *el, int64_t ne, int nx, int ny, int32
 
 }  // namespace
 
+namespace {
+__global__ void k_check_range(const int32_t *el, int64_t n, int64_t nn, int32_t *bad) {
+  bool b = false;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t v = el[i];
+    b |= (v < 0) | ((int64_t)v >= nn);
+  }
+  if (__any_sync(0xffffffffu, b) && (threadIdx.x & 31) == 0) atomicOr(bad, 1);
+}
+}  // namespace
+
+cudaError_t check_connectivity(const int32_t *el, int64_t n, int64_t nn, int32_t *flag,
+                               cudaStream_t st, int *bad) {
+  *bad = 1;
+  int32_t h = 1;
+  cudaError_t e = cudaMemsetAsync(flag, 0, sizeof(int32_t), st);
+  if (e != cudaSuccess) return e;
+  const int64_t grid = std::min<int64_t>((n + kThreads - 1) / kThreads, 152 * 16);
+  k_check_range<<<(unsigned)std::max<int64_t>(grid, 1), kThreads, 0, st>>>(el, n, nn, flag);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if ((e = cudaMemcpyAsync(&h, flag, sizeof(int32_t), cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+    return e;
+  if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+  *bad = h;
+  return cudaSuccess;
+}
+
 cudaError_t check_box(const int32_t *el_soa, int64_t ne, int64_t nn, int nx, int ny, int nz,
                       cudaStream_t st, int *is_box) {
   *is_box = 0;
