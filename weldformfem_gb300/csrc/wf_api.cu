@@ -1321,31 +1321,23 @@ cudaError_t upload(wf_domain *d, T **dst, const std::vector<T, A> &src) {
 // Per-node BC code: bits 0..2 = constrained dofs, bits 3.. = index of the
 // node's value triple; for repeated entries the later one wins, as the serial
 // BC loops of the reference (Domain_d.C:1109-1134) leave it.
-void bc_tables(wf_domain *d, std::vector<uint32_t> &code, std::vector<double> &vals) {
-  // compact per-BC-node records (mask, value triple), later entries winning
-  std::vector<int32_t> slot(d->nn, -1);
-  std::vector<int64_t> nodes;
-  std::vector<std::array<double, 3>> v3;
-  std::vector<uint8_t> mask;
+void bc_tables(wf_domain *d, std::vector<int32_t> &bnode, std::vector<uint32_t> &bcode,
+               std::vector<double> &vals) {
+  // the records in call order; for a node and dimension the last one wins
+  struct Rec {
+    int64_t n;
+    int k;
+    double v;
+  };
+  std::vector<Rec> r;
   for (int k = 0; k < 3; k++)
-    for (size_t i = 0; i < d->bc_nod[k].size(); i++) {
-      const int64_t n = d->bc_nod[k][i];
-      int32_t &sl = slot[n];
-      if (sl < 0) {
-        sl = (int32_t)nodes.size();
-        nodes.push_back(n);
-        v3.push_back({0.0, 0.0, 0.0});
-        mask.push_back(0);
-      }
-      mask[sl] |= (uint8_t)(1u << k);
-      v3[sl][k] = d->bc_val[k][i];
-    }
-  // value sets numbered in ascending node order
-  std::vector<int32_t> order(nodes.size());
-  for (size_t i = 0; i < order.size(); i++) order[i] = (int32_t)i;
-  std::sort(order.begin(), order.end(), [&](int32_t a, int32_t b) { return nodes[a] < nodes[b]; });
+    for (size_t i = 0; i < d->bc_nod[k].size(); i++) r.push_back({d->bc_nod[k][i], k, d->bc_val[k][i]});
+  std::stable_sort(r.begin(), r.end(), [](const Rec &a, const Rec &b) {
+    return a.n < b.n || (a.n == b.n && a.k < b.k);
+  });
   // keyed on the values' bit patterns: every value keeps its own set, NaN
-  // included (double comparisons would merge a NaN into another set)
+  // included (double comparisons would merge a NaN into another set); sets
+  // numbered in ascending node order
   auto bits = [](double v) {
     uint64_t u;
     std::memcpy(&u, &v, sizeof u);
@@ -1354,21 +1346,28 @@ void bc_tables(wf_domain *d, std::vector<uint32_t> &code, std::vector<double> &v
   std::map<std::tuple<uint64_t, uint64_t, uint64_t>, uint32_t> sets;
   vals.assign(3, 0.0);
   sets[std::make_tuple(bits(0.0), bits(0.0), bits(0.0))] = 0;
-  code.assign(d->nn, 0u);
-  for (int32_t i : order) {
-    auto key = std::make_tuple(bits(v3[i][0]), bits(v3[i][1]), bits(v3[i][2]));
+  bnode.clear();
+  bcode.clear();
+  for (size_t i = 0; i < r.size();) {
+    const int64_t n = r[i].n;
+    double v3[3] = {0.0, 0.0, 0.0};
+    uint32_t mask = 0;
+    for (; i < r.size() && r[i].n == n; i++) {
+      v3[r[i].k] = r[i].v;
+      mask |= 1u << r[i].k;
+    }
+    const auto key = std::make_tuple(bits(v3[0]), bits(v3[1]), bits(v3[2]));
     uint32_t id;
     auto it = sets.find(key);
     if (it == sets.end()) {
       id = (uint32_t)(vals.size() / 3);
       sets[key] = id;
-      vals.push_back(v3[i][0]);
-      vals.push_back(v3[i][1]);
-      vals.push_back(v3[i][2]);
+      vals.insert(vals.end(), v3, v3 + 3);
     } else {
       id = it->second;
     }
-    code[nodes[i]] = (id << 3) | mask[i];
+    bnode.push_back((int32_t)n);
+    bcode.push_back((id << 3) | mask);
   }
 }
 
@@ -1853,18 +1852,40 @@ WF_API wf_status wf_init(wf_domain *d) {
     CUDA_TRY(build_connectivity(d->mesh_el, ne, d->npe, nn, el, off, sl,
                                 static_cast<int32_t *>(stage), d->stream));
   }
-  std::vector<uint32_t> code;
+  // BC codes per node (value set << 3 | fixed dimensions), zero but at the
+  // BC nodes: scattered on the device from the BC nodes' records
+  std::vector<int32_t> bnode;
+  std::vector<uint32_t> bcode;
   std::vector<double> vals;
-  bc_tables(d, code, vals);
+  bc_tables(d, bnode, bcode, vals);
   uint32_t *bc = nullptr;
   double *bcv = nullptr;
-  CUDA_TRY(upload(d, &bc, code));
+  CUDA_TRY(dalloc(d, &bc, nn));
+  {
+    int32_t *bn = nullptr;
+    uint32_t *bv = nullptr;
+    CUDA_TRY(upload(d, &bn, bnode));
+    CUDA_TRY(upload(d, &bv, bcode));
+    scatter_u32(bc, bn, bv, (int64_t)bnode.size(), d->stream);
+    CUDA_TRY(cudaGetLastError());
+  }
   CUDA_TRY(upload(d, &bcv, vals));
   P.bc = bc;
   P.bcval = bcv;
-  std::vector<uint8_t> flags(nn, 0);
-  for (int32_t n : d->react_nodes) flags[n] |= NF_REACTION;
-  for (int32_t n : d->cand) flags[n] |= NF_CONTACT;
+  // node flags: zero but at the reaction and contact-candidate nodes (and
+  // the external surface with a triangle-mesh die), set on the device
+  uint8_t *fl = nullptr;
+  CUDA_TRY(dalloc(d, &fl, nn));
+  for (const auto &lst : {std::make_pair(&d->react_nodes, (uint8_t)NF_REACTION),
+                          std::make_pair(&d->cand, (uint8_t)NF_CONTACT)}) {
+    std::vector<int32_t> u(*lst.first);
+    std::sort(u.begin(), u.end());
+    u.erase(std::unique(u.begin(), u.end()), u.end());
+    int32_t *ud = nullptr;
+    CUDA_TRY(upload(d, &ud, u));
+    or_flags(fl, ud, lst.second, (int64_t)u.size(), d->stream);
+    CUDA_TRY(cudaGetLastError());
+  }
   P.end_t = d->end_t;
   if (d->tri) {
     std::vector<uint8_t> ext;
@@ -1875,8 +1896,15 @@ WF_API wf_status wf_init(wf_domain *d) {
       if (hs) return hs;
     }
     part_surface(d, ext, area, nodlen);
-    for (int64_t n = 0; n < nn; n++)
-      if (ext[n]) flags[n] |= NF_CONTACT;
+    {
+      std::vector<int32_t> en;
+      for (int64_t n = 0; n < nn; n++)
+        if (ext[n]) en.push_back((int32_t)n);
+      int32_t *ed = nullptr;
+      CUDA_TRY(upload(d, &ed, en));
+      or_flags(fl, ed, (uint8_t)NF_CONTACT, (int64_t)en.size(), d->stream);
+      CUDA_TRY(cudaGetLastError());
+    }
     tri_normals_planes(d->tri_x, d->tri_el, nrm, pp);
     double *tx = nullptr, *tvd = nullptr, *tn = nullptr, *tp = nullptr, *na = nullptr,
            *nl = nullptr;
@@ -1905,8 +1933,6 @@ WF_API wf_status wf_init(wf_domain *d) {
     P.tri_pf = d->tri_pf;
     P.tri_E0 = d->mats[0].E;
   }
-  uint8_t *fl = nullptr;
-  CUDA_TRY(upload(d, &fl, flags));
   P.nflag = fl;
   // materials (Elastic_, Material.cuh:24-27; InitHollomon, :90-104)
   std::vector<MatDev> md(d->mats.size());

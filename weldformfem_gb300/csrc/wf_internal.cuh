@@ -378,6 +378,10 @@ void min_edge_length_box(const double *x, int64_t np, int32_t bx, int32_t by, in
 // node's list (the host build's order). scratch holds
 // connectivity_scratch_ints(nn) ints.
 int64_t connectivity_scratch_ints(int64_t nn);
+// dst[idx[i]] = val[i] and dst[idx[i]] |= bit for i < n (distinct indices).
+void scatter_u32(uint32_t *dst, const int32_t *idx, const uint32_t *val, int64_t n,
+                 cudaStream_t st);
+void or_flags(uint8_t *dst, const int32_t *idx, uint8_t bit, int64_t n, cudaStream_t st);
 // Whether every entry of el[0, n) names a node in [0, nn) (*bad = 0), on the
 // device; flag: one device int of scratch. Synchronises st.
 cudaError_t check_connectivity(const int32_t *el, int64_t n, int64_t nn, int32_t *flag,

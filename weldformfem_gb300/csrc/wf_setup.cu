@@ -386,6 +386,26 @@ __global__ void k_check_range(const int32_t *el, int64_t n, int64_t nn, int32_t 
 }
 }  // namespace
 
+namespace {
+__global__ void k_scatter_u32(uint32_t *dst, const int32_t *idx, const uint32_t *val, int64_t n) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[idx[i]] = val[i];
+}
+__global__ void k_or_u8(uint8_t *dst, const int32_t *idx, uint8_t bit, int64_t n) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[idx[i]] |= bit;   // the lists hold each node once
+}
+}  // namespace
+
+void scatter_u32(uint32_t *dst, const int32_t *idx, const uint32_t *val, int64_t n,
+                 cudaStream_t st) {
+  if (n > 0) k_scatter_u32<<<grid_for(n), kThreads, 0, st>>>(dst, idx, val, n);
+}
+
+void or_flags(uint8_t *dst, const int32_t *idx, uint8_t bit, int64_t n, cudaStream_t st) {
+  if (n > 0) k_or_u8<<<grid_for(n), kThreads, 0, st>>>(dst, idx, bit, n);
+}
+
 cudaError_t check_connectivity(const int32_t *el, int64_t n, int64_t nn, int32_t *flag,
                                cudaStream_t st, int *bad) {
   *bad = 1;
