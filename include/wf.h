@@ -378,11 +378,12 @@ WF_API wf_status wf_set_launch_config(wf_domain *d, int32_t phase, int32_t block
  * forces are read back from L2 shortly after they are written. Each element
  * and node runs mode 1's arithmetic: the state is bitwise that of mode 1; the
  * reaction sum runs in another order. A wait that runs out (a bug, never
- * expected) makes the next wf_sync return WF_ERR_CUDA. On GB300 mode 5 is
+ * expected) makes the next wf_sync return WF_ERR_TIMEOUT. On GB300 mode 5 is
  * slower than modes 4 and 1 (the blocks' waits and ticket traffic cost more
  * than the L2 reuse saves) and is only run when asked for. Mode 0 (default)
  * picks mode 2 for meshes of at most 3000 elements, else mode 4 where the mesh
- * is swept, else mode 1. wf_get_step_mode reports the mode the next wf_run uses and,
+ * is swept and its columns fill the GPU (at least 95 % of two per SM: a
+ * column is a sequence of layers), else mode 1. wf_get_step_mode reports the mode the next wf_run uses and,
  * for mode 2, the cluster's blocks and block size, for mode 3 the tiles and
  * threads per tile, for mode 4 the columns and threads per column, for mode 5
  * the blocks and threads per block (0 otherwise). */

@@ -146,11 +146,20 @@ def test_energy_history(mode):
 
 
 def test_selection():
+    # 257 x 257 nodes per plane (C2's): 9 x 33 columns, enough to fill the GPU
+    wide = W.config(0, scale=(256, 256, 2))
+    w = wf.Domain(wf.WF_MIXED)
+    W.apply(w, wide)
+    w.init()
+    assert w.step_mode()[0] == 4                   # automatic: the column sweep
     big = W.config(0, scale=(16, 16, 16))          # above the cluster run's 3000 elements
     d = wf.Domain(wf.WF_MIXED)
     W.apply(d, big)
     d.init()
-    assert d.step_mode()[0] == 4                   # automatic: the column sweep on a box mesh
+    assert d.sweep()[:2] == (1, 3)                 # swept, but 3 columns leave the GPU idle:
+    assert d.step_mode()[0] == 1                   # automatic: the per-phase kernels
+    d.set_step_mode(4)
+    assert d.step_mode()[0] == 4
     d.set_step_mode(5)
     assert d.step_mode()[0] == 5
     d.set_step_mode(1)

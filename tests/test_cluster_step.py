@@ -66,7 +66,7 @@ def test_automatic_mode_and_fallbacks():
     W.apply(d, case)
     d.set_energy_history(True)
     d.init()
-    assert d.step_mode()[0] == 4            # energy history: no cluster run; the column sweep
+    assert d.step_mode()[0] == 1            # energy history: no cluster run; per-phase kernels
     d.set_step_mode(2)
     with pytest.raises(wf.WfError) as e:
         d.run(4)
@@ -79,7 +79,7 @@ def test_automatic_mode_and_fallbacks():
     d = wf.Domain(wf.WF_MIXED)
     W.apply(d, big)
     d.init()
-    assert d.step_mode()[0] == 4            # a box mesh: the column sweep
+    assert d.step_mode()[0] == 1            # too few sweep columns: per-phase kernels
     d.set_step_mode(3)                      # tiles are built by init: not after it
     assert d.step_mode()[0] == 1
     t = wf.Domain(wf.WF_MIXED)

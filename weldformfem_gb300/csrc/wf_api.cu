@@ -1617,14 +1617,20 @@ bool tiled_mode(const wf_domain *d) {
   if (d->precision != WF_MIXED || !d->tiled) return false;
   return d->step_mode == 3 || (kTiledAuto && d->step_mode == 0 && !cluster_mode(d));
 }
-// Whether the automatic mode picks the column sweep for box meshes.
+// Whether the automatic mode picks the column sweep for box meshes: when its
+// columns fill the GPU (the kernel holds two blocks per SM; each column is a
+// sequence of layers, so fewer columns leave SMs idle and the per-phase
+// kernels are faster: a 32^3 box has 10 columns).
 constexpr bool kSweepAuto = true;
+bool sweep_fills_gpu(const wf_domain *d) {
+  return 20 * (int64_t)d->W.ncx * d->W.ncy >= 19 * 2 * (int64_t)d->P.sms;
+}
 // Whether the steps of d run as the column sweep.
 bool flow_mode(const wf_domain *d);
 bool sweep_mode(const wf_domain *d) {
   if (d->precision != WF_MIXED || !d->sweep) return false;
-  return d->step_mode == 4 ||
-         (kSweepAuto && d->step_mode == 0 && !cluster_mode(d) && !flow_mode(d));
+  return d->step_mode == 4 || (kSweepAuto && d->step_mode == 0 && !cluster_mode(d) &&
+                               !flow_mode(d) && sweep_fills_gpu(d));
 }
 // Whether the automatic mode picks the dataflow step for box meshes (before
 // the column sweep): not, the sweep is faster on GB300.
@@ -2785,8 +2791,8 @@ WF_API wf_status wf_sync(wf_domain *d) {
       d->st_host->status &= ~2u;
       CUDA_TRY(cudaMemcpy(&d->P.st->status, &d->st_host->status, sizeof(unsigned),
                           cudaMemcpyHostToDevice));
-      return fail(d, WF_ERR_CUDA, "a dependency wait of the dataflow step ran out, in the "
-                                  "steps up to step %lld", (long long)st.step);
+      return fail(d, WF_ERR_TIMEOUT, "a dependency wait of the dataflow step ran out, in the "
+                                     "steps up to step %lld", (long long)st.step);
     }
     if (st.status & 1u) {
       d->st_host->status = 0u;
