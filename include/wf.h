@@ -154,6 +154,12 @@ WF_API wf_status wf_allocate_bcs(wf_domain *d);
 /* ---- options ---------------------------------------------------------------- */
 WF_API wf_status wf_set_dt(wf_domain *d, double dt);         /* SetDT (Domain_d.h:635) */
 WF_API wf_status wf_set_end_time(wf_domain *d, double t);    /* SetEndTime (Domain_d.h:636) */
+/* WF_FP64 (default) or WF_MIXED. The mixed path takes every option of the
+ * step but non-default stabilisation parameters and pressure algorithm 1
+ * (WF_ERR_UNSUPPORTED at wf_init: algorithm 1 adds k0 (1 - J ratio) to each
+ * element's pressure every step, and an FP32 J ratio near 1 resolves the
+ * volume change only to about 6e-8). Its exported sigma leaves out the
+ * artificial viscosity term (the strain rate is not kept). */
 WF_API wf_status wf_set_precision(wf_domain *d, int32_t precision);
 /* Viscous hourglass coefficient of 1-point hexahedra (0 = off): the 3-D form
  * of the reference's test driver (src/common/test_1el_3D.cpp:159-199). */

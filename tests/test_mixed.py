@@ -91,10 +91,49 @@ def test_mixed_deterministic():
 def test_mixed_rejects_unsupported_options():
     d = wf.Domain(wf.WF_MIXED)
     W.apply(d, W.config(1, scale=(2, 2, 2)))
+    stab = np.zeros(10)
+    stab[0] = 0.5
+    d.set_stab(stab)
+    with pytest.raises(wf.WfError) as e:
+        d.init()
+    assert e.value.status == 5
+    d = wf.Domain(wf.WF_MIXED)
+    W.apply(d, W.config(1, scale=(2, 2, 2)))
     d.set_press_algorithm(1)
     with pytest.raises(wf.WfError) as e:
         d.init()
     assert e.value.status == 5
+
+
+def run_pair(case, steps, av=None):
+    out = []
+    for dom in (wf.Domain(wf.WF_MIXED), O.OracleDomain()):
+        W.apply(dom, case)
+        if av:
+            dom.set_artif_visc(*av)
+        dom.init()
+        dom.run(steps) if hasattr(dom, "run") else dom.step(steps)
+        out.append(dom)
+    return out
+
+
+@pytest.mark.parametrize("cid,scale", [(0, (6, 6, 6)), (1, (4, 4, 6)), (0, (16, 16, 16))],
+                         ids=["hex-cluster", "tet-cluster", "hex-per-phase"])
+def test_mixed_artificial_viscosity_vs_fp64(cid, scale):
+    """calcArtificialViscosity in FP32: within the mixed path's bounds of the
+    FP64 oracle with the same viscosity, and ten times closer to it than the
+    mixed run without viscosity is (coefficients large enough for the viscous
+    stress to show in the reaction)."""
+    case = W.config(cid, scale=scale)
+    case.perturb = 0.1
+    case.seed = W.SEED_BASE + 11
+    case.materials = [dict(H.HOLLOMON)]
+    m, o = run_pair(case, 300, av=(50.0, 10.0))
+    assert H.rel_err(m.node_vec("u"), o.node_vec("u")) <= 1e-4
+    e_av = H.rel_err(m.reaction(), o.reaction())
+    assert e_av <= 1e-3
+    plain, _ = run_pair(case, 300)
+    assert e_av < 0.1 * H.rel_err(plain.reaction(), o.reaction())
 
 
 def test_autotuned_and_default_launch_shapes_agree_bitwise():

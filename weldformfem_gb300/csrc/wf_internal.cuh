@@ -115,6 +115,7 @@ struct StepParams {
   float f_cv_corr;        // gamma * dt
   float f_cv_pred;        // (1 - gamma) * dt
   float f_hg_coef, f_c_k, f_c_mu;
+  float f_av0, f_av1;               // artificial viscosity coefficients (mixed)
   const struct MatF *matf;
   // batched ensemble (all null / zero for a single domain)
   int32_t nspec;

@@ -447,21 +447,24 @@ __global__ void __launch_bounds__(BS) k_mix_nodal(StepParams P, MixState M, cons
 // Writes the new tau and eps_p; returns sigma = tau - p I in sg.
 // LAW = 0: linear hardening only (the common case, fewer registers); LAW = 1:
 // every material model.
-// Element state (tau [6][ne], eps_p [ne]) in HBM, read and written in place.
+// Element state (tau [6][ne], eps_p [ne]) in HBM, read and written in place
+// (the mixed state's arrays, addressed from the kernel parameters).
 struct StateInPlace {
-  float *tau, *pls;
-  int64_t ne, e;
-  __device__ __forceinline__ void load(float &t0, float &t1, float &t2, float &t3, float &t4,
+  __device__ __forceinline__ void load(const StepParams &P, const MixState &M, int64_t e,
+                                       float &t0, float &t1, float &t2, float &t3, float &t4,
                                        float &t5, float &p) const {
-    t0 = tau[e]; t1 = tau[ne + e]; t2 = tau[2 * ne + e];
-    t3 = tau[3 * ne + e]; t4 = tau[4 * ne + e]; t5 = tau[5 * ne + e];
-    p = pls[e];
+    const int64_t ne = P.ne;
+    t0 = M.tau[e]; t1 = M.tau[ne + e]; t2 = M.tau[2 * ne + e];
+    t3 = M.tau[3 * ne + e]; t4 = M.tau[4 * ne + e]; t5 = M.tau[5 * ne + e];
+    p = M.pls[e];
   }
-  __device__ __forceinline__ void store(float t0, float t1, float t2, float t3, float t4,
+  __device__ __forceinline__ void store(const StepParams &P, const MixState &M, int64_t e,
+                                        float t0, float t1, float t2, float t3, float t4,
                                         float t5, float p) const {
-    pls[e] = p;
-    tau[e] = t0; tau[ne + e] = t1; tau[2 * ne + e] = t2;
-    tau[3 * ne + e] = t3; tau[4 * ne + e] = t4; tau[5 * ne + e] = t5;
+    const int64_t ne = P.ne;
+    M.pls[e] = p;
+    M.tau[e] = t0; M.tau[ne + e] = t1; M.tau[2 * ne + e] = t2;
+    M.tau[3 * ne + e] = t3; M.tau[4 * ne + e] = t4; M.tau[5 * ne + e] = t5;
   }
   __device__ __forceinline__ bool owns() const { return true; }
 };
@@ -471,13 +474,14 @@ struct StateInPlace {
 // sweep, written to the other buffer of a pair, or not at all for a halo
 // element).
 template <int LAW, bool TH, class IO>
-__device__ __forceinline__ void stress_update(const StepParams &P, int64_t e, const IO &io,
+__device__ __forceinline__ void stress_update(const StepParams &P, const MixState &M, int64_t e,
+                                              const IO &io,
                                               const MatF &m, const float (&sr)[6], float w01,
                                               float w12, float w02, float p, float jTh,
                                               float (&sg)[6], float &sdot, float &qpl) {
   const float dt = P.espec ? P.specf[P.espec[e]].dt : P.f_dt;
   float t0, t1, t2, t3, t4, t5, pls;
-  io.load(t0, t1, t2, t3, t4, t5, pls);
+  io.load(P, M, e, t0, t1, t2, t3, t4, t5, pls);
   {
     // tau W^T                      W tau
     const float srt0 = t3 * w01 + t5 * w02, rs0 = w01 * t3 + w02 * t5;    // xx
@@ -541,7 +545,7 @@ __device__ __forceinline__ void stress_update(const StepParams &P, int64_t e, co
     pls += dgamma;
     dep = dgamma;
   }
-  io.store(t0, t1, t2, t3, t4, t5, pls);
+  io.store(P, M, e, t0, t1, t2, t3, t4, t5, pls);
   sg[0] = t0 - p; sg[1] = t1 - p; sg[2] = t2 - p;
   sg[3] = t3; sg[4] = t4; sg[5] = t5;
   // plastic heat 0.9 sigma : (d eps_p / dt) (Mechanical.C:1783-1810)
@@ -668,6 +672,27 @@ struct GlobalNodes {
   __device__ __forceinline__ float j(int a) const { return ldx<CG>(&jr[nid[a]]); }
 };
 
+// Artificial viscosity (calcArtificialViscosity, Mechanical.C:1948-1977) of
+// one element: q = av0 c |eps_v| l + av1 (eps_v l)^2, capped at 1e9, with
+// c = sqrt(K / rho), l = vol^(1/3) and eps_v the trace of the strain rate,
+// added to the normal stresses with the sign opposite to eps_v. Returns the
+// signed term qs (0 when |eps_v| <= 1e-12); it adds qs eps_v to the stress
+// power.
+__device__ __forceinline__ float artificial_viscosity(const StepParams &P, const MatF &m,
+                                                      float eps_v, float vol, float (&sg)[6]) {
+  if (!(fabsf(eps_v) > 1e-12f)) return 0.f;
+  const float c = sqrtf(m.K / m.rho);
+  const float l = cbrtf(vol);
+  const float el = eps_v * l;
+  float q = P.f_av0 * c * fabsf(eps_v) * l + P.f_av1 * (el * el);
+  q = (1e9f < q) ? 1e9f : q;
+  const float qs = (eps_v > 0.f) ? -q : q;
+  sg[0] += qs;
+  sg[1] += qs;
+  sg[2] += qs;
+  return qs;
+}
+
 // Element forces to HBM, SoA by (local node, component): fe[(a * 3 + k) * ne + e].
 struct ForcesToHbm {
   float *fe;
@@ -775,7 +800,9 @@ __device__ __forceinline__ void element_hex_core(const StepParams &P, const MixS
   if (J_bar < 0.0f) J_bar = 0.2f;
   const float p = -m.K * (J_bar - 1.0f);
   float sg[6], sdot = 0.f, qpl = 0.f;
-  stress_update<LAW, TH>(P, e, io, m, sr, w01, w12, w02, p, jTh, sg, sdot, qpl);
+  const float eps_v = sr[0] + sr[1] + sr[2];
+  stress_update<LAW, TH>(P, M, e, io, m, sr, w01, w12, w02, p, jTh, sg, sdot, qpl);
+  if (P.av_on) sdot += artificial_viscosity(P, m, eps_v, vol, sg) * eps_v;
   if (P.energy_on && io.owns()) M.edot[e] = sdot * vol;
   // sigma as a symmetric 3x3: S[i][k]
   const float S[3][3] = {{sg[0], sg[3], sg[5]}, {sg[3], sg[1], sg[4]}, {sg[5], sg[4], sg[2]}};
@@ -818,7 +845,7 @@ __device__ __forceinline__ void element_hex(const StepParams &P, const MixState 
   const GlobalNodes<CG, BOX> nd(P, M, e);
   ForcesToHbm out{M.fe, P.ne, e};
   element_hex_core<LAW, !CG, TH>(P, M, e, nd, stash, stride, step, out,
-                                 StateInPlace{M.tau, M.pls, P.ne, e});
+                                 StateInPlace{});
 }
 
 // Tetrahedron: per-node shape derivatives (Domain_d.C:1866-1887).
@@ -877,9 +904,11 @@ __device__ __forceinline__ void element_tet(const StepParams &P, const MixState 
   if (J_bar < 0.0f) J_bar = 0.2f;
   const float p = -m.K * (J_bar - 1.0f);
   float sg[6], sdot = 0.f, qpl = 0.f;
-  stress_update<LAW, TH>(P, e, StateInPlace{M.tau, M.pls, ne, e}, m, sr, w01, w12, w02, p,
-                         jTh, sg, sdot, qpl);
+  stress_update<LAW, TH>(P, M, e, StateInPlace{}, m, sr, w01, w12, w02, p, jTh, sg, sdot,
+                         qpl);
   const float w = weightf<4>();
+  if (P.av_on) sdot += artificial_viscosity(P, m, sr[0] + sr[1] + sr[2], detJ * w, sg) *
+                       (sr[0] + sr[1] + sr[2]);
   if (P.energy_on) M.edot[e] = sdot * (detJ * w);
 #pragma unroll
   for (int a = 0; a < 4; a++) {
@@ -1266,7 +1295,7 @@ __global__ void __launch_bounds__(kTileElems, 2) k_mix_tile(StepParams P, MixSta
     for (int a = 0; a < 8; a++) nd.loc[a] = __ldg(&T.lel[a * ne + pos]);
     ForcesToRegs out{f};
     element_hex_core<LAW, true, false>(P, M, e, nd, &stash[tid], kTileElems, step, out,
-                                       StateInPlace{M.tau, M.pls, ne, e});
+                                       StateInPlace{});
     // corner forces of shared nodes: to HBM, for the shared-node gather
 #pragma unroll
     for (int a = 0; a < 8; a++)
@@ -1453,13 +1482,15 @@ struct StateSwept {
 #pragma unroll
     for (int c = 0; c < 6; c++) t[c] = in[c];
   }
-  __device__ __forceinline__ void load(float &t0, float &t1, float &t2, float &t3, float &t4,
-                                       float &t5, float &pp) const {
+  __device__ __forceinline__ void load(const StepParams &, const MixState &, int64_t, float &t0,
+                                       float &t1, float &t2, float &t3, float &t4, float &t5,
+                                       float &pp) const {
     t0 = t[0]; t1 = t[1]; t2 = t[2]; t3 = t[3]; t4 = t[4]; t5 = t[5];
     pp = p;
   }
-  __device__ __forceinline__ void store(float t0, float t1, float t2, float t3, float t4,
-                                        float t5, float pp) const {
+  __device__ __forceinline__ void store(const StepParams &, const MixState &, int64_t, float t0,
+                                        float t1, float t2, float t3, float t4, float t5,
+                                        float pp) const {
     if (tau_o) {
       pls_o[e] = pp;
       tau_o[e] = t0; tau_o[ne + e] = t1; tau_o[2 * ne + e] = t2;
@@ -1771,7 +1802,7 @@ __global__ void __launch_bounds__(kFlowThreads, 1024 / kFlowThreads) k_mix_flow(
           const GlobalNodes<true, true, false> nd(P, M, e);
           ForcesToHbm out{M.fe, P.ne, e};
           element_hex_core<LAW, true, false>(P, M, e, nd, &stash[tid], kFlowThreads, step, out,
-                                             StateInPlace{M.tau, M.pls, P.ne, e});
+                                             StateInPlace{});
         }
       }
     } else {
