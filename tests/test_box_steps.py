@@ -202,3 +202,17 @@ def test_selection():
     for bad in ((300, 4), (128, 4), (512, 2), (512, 17)):
         with pytest.raises(wf.WfError):
             n.set_flow_tiles(*bad)
+
+
+@pytest.mark.parametrize("nel", [(1, 1, 5), (31, 1, 3), (30, 7, 2), (32, 9, 1), (2, 40, 3),
+                                 (62, 17, 2)], ids=str)
+@pytest.mark.parametrize("mode", [4, 5])
+def test_ragged_and_thin_boxes(nel, mode):
+    """Columns of one node, a single element layer, rows that end mid-column,
+    widths at the 31-node column limit and just past it: the sweep and the
+    dataflow step still equal the per-phase step bit for bit."""
+    case = W.config(0, scale=nel)
+    s = run(case, mode, 60)
+    p = run(case, 1, 60)
+    assert s.step_mode()[0] == mode
+    assert_same_state(s, p)
