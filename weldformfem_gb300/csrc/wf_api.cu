@@ -1330,11 +1330,34 @@ void bc_tables(wf_domain *d, std::vector<int32_t> &bnode, std::vector<uint32_t> 
     double v;
   };
   std::vector<Rec> r;
-  for (int k = 0; k < 3; k++)
-    for (size_t i = 0; i < d->bc_nod[k].size(); i++) r.push_back({d->bc_nod[k][i], k, d->bc_val[k][i]});
-  std::stable_sort(r.begin(), r.end(), [](const Rec &a, const Rec &b) {
-    return a.n < b.n || (a.n == b.n && a.k < b.k);
-  });
+  bool sorted = true;   // each dimension's list ascending (the usual case): a merge suffices
+  for (int k = 0; k < 3; k++) {
+    const auto &nk = d->bc_nod[k];
+    for (size_t i = 1; i < nk.size() && sorted; i++) sorted = nk[i - 1] <= nk[i];
+  }
+  if (sorted) {
+    // three-way merge by (node, dimension); within a dimension the list
+    // order is kept, so a repeated node's later value stays later
+    size_t at[3] = {0, 0, 0};
+    r.reserve(d->bc_nod[0].size() + d->bc_nod[1].size() + d->bc_nod[2].size());
+    for (;;) {
+      int kb = -1;
+      for (int k = 0; k < 3; k++)
+        if (at[k] < d->bc_nod[k].size() &&
+            (kb < 0 || d->bc_nod[k][at[k]] < d->bc_nod[kb][at[kb]]))
+          kb = k;
+      if (kb < 0) break;
+      r.push_back({d->bc_nod[kb][at[kb]], kb, d->bc_val[kb][at[kb]]});
+      at[kb]++;
+    }
+  } else {
+    for (int k = 0; k < 3; k++)
+      for (size_t i = 0; i < d->bc_nod[k].size(); i++)
+        r.push_back({d->bc_nod[k][i], k, d->bc_val[k][i]});
+    std::stable_sort(r.begin(), r.end(), [](const Rec &a, const Rec &b) {
+      return a.n < b.n || (a.n == b.n && a.k < b.k);
+    });
+  }
   // keyed on the values' bit patterns: every value keeps its own set, NaN
   // included (double comparisons would merge a NaN into another set); sets
   // numbered in ascending node order
@@ -1888,7 +1911,7 @@ WF_API wf_status wf_init(wf_domain *d) {
   for (const auto &lst : {std::make_pair(&d->react_nodes, (uint8_t)NF_REACTION),
                           std::make_pair(&d->cand, (uint8_t)NF_CONTACT)}) {
     std::vector<int32_t> u(*lst.first);
-    std::sort(u.begin(), u.end());
+    if (!std::is_sorted(u.begin(), u.end())) std::sort(u.begin(), u.end());
     u.erase(std::unique(u.begin(), u.end()), u.end());
     int32_t *ud = nullptr;
     CUDA_TRY(upload(d, &ud, u));
