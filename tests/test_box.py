@@ -111,3 +111,14 @@ def test_node_vec_into_caller_buffer():
     np.testing.assert_array_equal(got, want)
     with pytest.raises(ValueError):
         d.node_vec("u", out=np.zeros(case.n_node * 3, np.float32))
+
+
+def test_direct_displacement_readback_equals_export():
+    """Mixed positions and displacements read straight from the state equal
+    those of the full FP64 export bit for bit."""
+    case = W.config(2, scale=(24, 20, 16))
+    d = run(case, True, 40)
+    u1, x1 = d.node_vec("u"), d.node_vec("x")      # direct
+    d.elem_scalar("pl_strain")                       # exports every field
+    np.testing.assert_array_equal(d.node_vec("u"), u1)
+    np.testing.assert_array_equal(d.node_vec("x"), x1)

@@ -2905,6 +2905,20 @@ wf_status copy_plain(wf_domain *d, const double *src, double *out, size_t count)
 }  // namespace
 
 WF_API wf_status wf_get_node_field(wf_domain *d, int32_t field, double *out) {
+  if (d && out && d->initialized && d->precision == WF_MIXED && !d->mix_valid_fp64 &&
+      (field == WF_NODE_U || field == WF_NODE_X)) {
+    // positions and displacements straight from the mixed state (no export
+    // of the other fields)
+    CUDA_TRY(cudaSetDevice(d->device));
+    if (!d->readback) CUDA_TRY(dalloc_raw(d, &d->readback, 3 * d->np));
+    mix_node_aos(d->P, d->M, field == WF_NODE_U, d->readback, d->stream);
+    CUDA_TRY(cudaGetLastError());
+    const size_t bytes = sizeof(double) * 3 * d->nn;
+    d->d2h_bytes += (int64_t)bytes;
+    CUDA_TRY(cudaMemcpyAsync(out, d->readback, bytes, cudaMemcpyDeviceToHost, d->stream));
+    CUDA_TRY(cudaStreamSynchronize(d->stream));
+    return WF_OK;
+  }
   wf_status s = ready_for_readback(d);
   if (s) return s;
   if (!out) return WF_ERR_ARG;

@@ -353,6 +353,10 @@ int mix_cluster_fits(const StepParams &P, const MixState &M, float *vol, int blo
 // part: [nsteps][blocks] staging for the reaction's block partials.
 cudaError_t mix_cluster_run(const StepParams &P, const MixState &M, float *vol, double *part,
                             int64_t nsteps, int blocks, int bs, cudaStream_t st);
+// The mixed state's displacements (or positions) as AoS [nn][3] doubles, as
+// the export forms them, without exporting the other fields.
+void mix_node_aos(const StepParams &P, const MixState &M, bool displacement, double *out,
+                  cudaStream_t st);
 void mix_export(const StepParams &P, const MixState &M, const Fp64State &S, const float *vol,
                 cudaStream_t st);
 int mix_node_grid(int64_t nn);

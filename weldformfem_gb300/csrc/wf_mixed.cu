@@ -1958,6 +1958,17 @@ __global__ void k_mix_export_nodes(StepParams P, MixState M, Fp64State S) {
   if (P.thermal) S.T[n] = (double)M.T[n].x + (double)M.T[n].y;
 }
 
+// Displacement (u = x - x0) or position of the mixed state straight into an
+// AoS [nn][3] buffer, as k_mix_export_nodes forms them.
+__global__ void k_mix_node_aos(StepParams P, MixState M, int displacement, double *out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= 3 * P.nn) return;
+  const int64_t n = i / 3, k = i - 3 * n, np = P.np;
+  const float2 h = M.xh[k * np + n];
+  const double x = (double)h.x + (double)h.y;
+  out[i] = displacement ? x - M.x0[k * np + n] : x;
+}
+
 template <int NPE>
 __global__ void k_mix_export_elems(StepParams P, MixState M, Fp64State S, const float *vol) {
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -2383,6 +2394,12 @@ cudaError_t mix_cluster_run(const StepParams &P, const MixState &M, float *vol, 
 
 void mix_predict(const StepParams &P, const MixState &M, cudaStream_t st) {
   k_mix_predict<<<grid_for(P.nn, kNodeThreads), kNodeThreads, 0, st>>>(P, M);
+}
+
+void mix_node_aos(const StepParams &P, const MixState &M, bool displacement, double *out,
+                  cudaStream_t st) {
+  k_mix_node_aos<<<grid_for(3 * P.nn, kNodeThreads), kNodeThreads, 0, st>>>(P, M, displacement ? 1 : 0,
+                                                                             out);
 }
 
 void mix_export(const StepParams &P, const MixState &M, const Fp64State &S, const float *vol,
