@@ -1862,26 +1862,50 @@ WF_API wf_status wf_init(wf_domain *d) {
   P.c_k = d->c_k;
   P.c_mu = d->c_mu;
 
-  // connectivity (SoA elnod), node lists as slots e*npe + local, built on
-  // the device from one upload of the AoS connectivity and the AoS
-  // coordinates (transposed into S.x below); the staging buffer is freed at
-  // the end of init
+  // connectivity (SoA elnod) and node lists (slots e*npe + local), built on
+  // the device from the mesh's device copy (wf_set_mesh)
   const int64_t ent = ne * d->npe;
-  int32_t *el = nullptr, *off = nullptr, *sl = nullptr;
+  int32_t *el = nullptr;
   CUDA_TRY(dalloc_raw(d, &el, ent));
-  CUDA_TRY(dalloc_raw(d, &off, nn + 1));
-  CUDA_TRY(dalloc_raw(d, &sl, ent));
   P.elnod = el;
-  P.off = off;
-  P.slot = sl;
-  // the AoS uploads are the mesh's device copy (wf_set_mesh); only the
-  // connectivity scratch is allocated here
   const double *x_aos = d->mesh_x;
-  {
+  CUDA_TRY(build_connectivity(d->mesh_el, ne, d->npe, nn, el, nullptr, nullptr, nullptr,
+                              d->stream));
+  // a box mesh (AddBoxLength numbering, however it was uploaded; mixed
+  // precision): the mixed kernels compute corners and node lists instead of
+  // loading them
+  if (d->precision == WF_MIXED) {
+    int bnx = 0, bny = 0, bnz = 0, is_box = 0;
+    box_dims(d, &bnx, &bny, &bnz);
+    if (d->npe == 8 && !d->nspec && d->use_box && bnx > 0)
+      CUDA_TRY(check_box(P.elnod, ne, nn, bnx, bny, bnz, d->stream, &is_box));
+    P.box = is_box;
+    if (is_box) {
+      P.bx = bnx;
+      P.by = bny;
+      P.bz = bnz;
+      P.fd_ex = make_fastdiv((uint32_t)bnx);
+      P.fd_exy = make_fastdiv((uint32_t)bnx * (uint32_t)bny);
+      P.fd_nx = make_fastdiv((uint32_t)bnx + 1u);
+      P.fd_nxy = make_fastdiv(((uint32_t)bnx + 1u) * ((uint32_t)bny + 1u));
+    }
+  }
+  // the node lists, unless no kernel of the domain can read them: a mixed box
+  // mesh without thermal coupling or triangle-mesh contact, too large for the
+  // cluster run, and no tiled steps (host lists are then built from the host
+  // mirror if a host caller asks)
+  const bool lists = !(P.box && !d->thermal && !d->tri && d->step_mode != 3 &&
+                       ne > kClusterMaxElems);
+  if (lists) {
+    int32_t *off = nullptr, *sl = nullptr;
+    CUDA_TRY(dalloc_raw(d, &off, nn + 1));
+    CUDA_TRY(dalloc_raw(d, &sl, ent));
+    P.off = off;
+    P.slot = sl;
     void *stage = nullptr;
     CUDA_TRY(pool_alloc(d, &stage, sizeof(int32_t) * connectivity_scratch_ints(nn)));
     d->init_stage = stage;
-    CUDA_TRY(build_connectivity(d->mesh_el, ne, d->npe, nn, el, off, sl,
+    CUDA_TRY(build_connectivity(d->mesh_el, ne, d->npe, nn, nullptr, off, sl,
                                 static_cast<int32_t *>(stage), d->stream));
   }
   // BC codes per node (value set << 3 | fixed dimensions), zero but at the
@@ -2226,24 +2250,6 @@ WF_API wf_status wf_init(wf_domain *d) {
     mix_init(P, M, S, d->stream);
     CUDA_TRY(cudaGetLastError());
     d->mix_valid_fp64 = true;
-    // a box mesh (AddBoxLength numbering, however it was uploaded): the
-    // per-phase kernels compute corners and node lists instead of loading them
-    {
-      int bnx = 0, bny = 0, bnz = 0, is_box = 0;
-      box_dims(d, &bnx, &bny, &bnz);
-      if (d->npe == 8 && !d->nspec && d->use_box && bnx > 0)
-        CUDA_TRY(check_box(P.elnod, ne, nn, bnx, bny, bnz, d->stream, &is_box));
-      P.box = is_box;
-      if (is_box) {
-        P.bx = bnx;
-        P.by = bny;
-        P.bz = bnz;
-        P.fd_ex = make_fastdiv((uint32_t)bnx);
-        P.fd_exy = make_fastdiv((uint32_t)bnx * (uint32_t)bny);
-        P.fd_nx = make_fastdiv((uint32_t)bnx + 1u);
-        P.fd_nxy = make_fastdiv(((uint32_t)bnx + 1u) * ((uint32_t)bny + 1u));
-      }
-    }
     // element tiles of the tiled step (hexahedra; the kernels leave out
     // specimens, thermal coupling, the energy history and triangle-mesh dies)
     d->tiled = false;
@@ -2344,7 +2350,7 @@ WF_API wf_status wf_init(wf_domain *d) {
     }
   }
   CUDA_TRY(cudaStreamSynchronize(d->stream));
-  CUDA_TRY(cudaFreeAsync(d->init_stage, d->stream));
+  if (d->init_stage) CUDA_TRY(cudaFreeAsync(d->init_stage, d->stream));
   d->init_stage = nullptr;
   d->initialized = true;
   d->host_step = 0;

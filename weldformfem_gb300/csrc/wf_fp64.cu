@@ -138,15 +138,34 @@ __global__ void __launch_bounds__(kElemThreads) k_fp64_geometry(StepParams P, Fp
 // nodal: CalcNodalVol (Mechanical.C:1555-1572), CalcNodalMassFromVol
 // (:1576-1601) and the nodal volume ratio of calcElemPressure (:694-705).
 // init_mode 1 also forms the constant sum of initial volumes.
-template <int NPE>
+// BOX: the node's elements computed from its indices (box meshes of a mixed
+// domain, whose preamble runs this kernel), in the lists' order.
+template <int NPE, bool BOX>
 __global__ void __launch_bounds__(kNodeThreads) k_fp64_nodal(StepParams P, Fp64State S,
                                                         int init_mode) {
   int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= P.nn) return;
-  const int32_t b = __ldg(&P.off[n]), c = __ldg(&P.off[n + 1]) - b;
+  int32_t b = 0, c = 0;
+  int32_t bel[8];
+  if constexpr (BOX) {
+    int32_t el[8], cor[8];
+    box_node_list(P, n, el, cor);
+#pragma unroll
+    for (int j = 0; j < 8; j++)
+      if (el[j] >= 0) bel[c++] = el[j];
+  } else {
+    b = __ldg(&P.off[n]);
+    c = __ldg(&P.off[n + 1]) - b;
+  }
+  auto elem = [&](int32_t k) -> int32_t {
+    if constexpr (BOX)
+      return bel[k];
+    else
+      return __ldg(&P.slot[b + k]) / NPE;
+  };
   double s = 0.0, s0 = 0.0;
   for (int32_t k = 0; k < c; k++) {
-    int32_t e = __ldg(&P.slot[b + k]) / NPE;
+    int32_t e = elem(k);
     s += __ldg(&S.vol[e]);
     if (init_mode) s0 += __ldg(&S.vol0[e]);
   }
@@ -159,7 +178,7 @@ __global__ void __launch_bounds__(kNodeThreads) k_fp64_nodal(StepParams P, Fp64S
     double mass = 0.0;
     const double f = 1.0;
     for (int32_t k = 0; k < c; k++) {
-      int32_t e = __ldg(&P.slot[b + k]) / NPE;
+      int32_t e = elem(k);
       mass += f * __ldg(&S.rho[e]) * voln / c;
     }
     S.mass[n] = mass;
@@ -837,10 +856,12 @@ void fp64_geometry(const StepParams &P, const Fp64State &S, cudaStream_t st, boo
 
 void fp64_nodal(const StepParams &P, const Fp64State &S, cudaStream_t st, int init_mode) {
   const int t = spread(P.nn, kNodeThreads, P.sms);
-  if (P.npe == 8)
-    k_fp64_nodal<8><<<grid_for(P.nn, t), t, 0, st>>>(P, S, init_mode);
+  if (P.npe == 8 && P.box)
+    k_fp64_nodal<8, true><<<grid_for(P.nn, t), t, 0, st>>>(P, S, init_mode);
+  else if (P.npe == 8)
+    k_fp64_nodal<8, false><<<grid_for(P.nn, t), t, 0, st>>>(P, S, init_mode);
   else
-    k_fp64_nodal<4><<<grid_for(P.nn, t), t, 0, st>>>(P, S, init_mode);
+    k_fp64_nodal<4, false><<<grid_for(P.nn, t), t, 0, st>>>(P, S, init_mode);
 }
 
 void fp64_elements(const StepParams &P, const Fp64State &S, cudaStream_t st) {

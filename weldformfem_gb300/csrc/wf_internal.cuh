@@ -377,11 +377,41 @@ void min_edge_length(const int32_t *elnod, const double *x, int64_t np, int64_t 
 void min_edge_length_box(const double *x, int64_t np, int32_t bx, int32_t by, int32_t bz,
                          double *out_dev, cudaStream_t st);
 
+#ifdef __CUDACC__
+// ---- box meshes (AddBoxLength numbering, P.box) -----------------------------------
+// The elements around node n in list order (ascending, the node lists'
+// order) and n's corner in each; el[q] = -1 where the box has none. q = dk * 4
+// + dj * 2 + di for the element (i - 1 + di, j - 1 + dj, k - 1 + dk); the
+// corner at (1 - di, 1 - dj, 1 - dk) of the element is 4 z + (x ^ 3 y).
+__device__ __forceinline__ void box_node_list(const StepParams &P, int64_t n, int32_t (&el)[8],
+                                              int32_t (&cor)[8]) {
+  const uint32_t un = (uint32_t)n;
+  const int32_t k = (int32_t)fdiv(un, P.fd_nxy);
+  const uint32_t r = un - (uint32_t)k * P.fd_nxy.d;
+  const int32_t j = (int32_t)fdiv(r, P.fd_nx);
+  const int32_t i = (int32_t)(r - (uint32_t)j * P.fd_nx.d);
+#pragma unroll
+  for (int dk = 0; dk < 2; dk++)
+#pragma unroll
+    for (int dj = 0; dj < 2; dj++)
+#pragma unroll
+      for (int di = 0; di < 2; di++) {
+        const int32_t ii = i - 1 + di, jj = j - 1 + dj, kk = k - 1 + dk;
+        const bool ok = ii >= 0 && ii < P.bx && jj >= 0 && jj < P.by && kk >= 0 && kk < P.bz;
+        const int q = dk * 4 + dj * 2 + di;
+        el[q] = ok ? ii + P.bx * (jj + P.by * kk) : -1;
+        cor[q] = 4 * (1 - dk) + ((1 - di) ^ (3 * (1 - dj)));
+      }
+}
+#endif
+
 // ---- device setup (wf_setup.cu) ------------------------------------------------
 // Node -> element lists from the AoS connectivity on the device: SoA element
 // nodes, CSR offsets [nn + 1] and slots e * npe + a, ascending within each
 // node's list (the host build's order). scratch holds
-// connectivity_scratch_ints(nn) ints.
+// connectivity_scratch_ints(nn) ints. With off null only the SoA element nodes
+// are built (box meshes whose kernels compute the lists), with el_soa null
+// only the lists.
 int64_t connectivity_scratch_ints(int64_t nn);
 // dst[idx[i]] = val[i] and dst[idx[i]] |= bit for i < n (distinct indices).
 void scatter_u32(uint32_t *dst, const int32_t *idx, const uint32_t *val, int64_t n,

@@ -89,31 +89,6 @@ __device__ __forceinline__ void box_corners(const StepParams &P, int64_t e, int3
   nid[7] = n0 + px + pxy;
 }
 
-// Box meshes: the node list of node n (the elements around it in ascending
-// order, which is the list order, and n's corner in each); el[q] = -1 for
-// the positions outside the box.
-__device__ __forceinline__ void box_node_list(const StepParams &P, int64_t n, int32_t (&el)[8],
-                                              int32_t (&cor)[8]) {
-  const uint32_t un = (uint32_t)n;
-  const int32_t k = (int32_t)fdiv(un, P.fd_nxy);
-  const uint32_t r = un - (uint32_t)k * P.fd_nxy.d;
-  const int32_t j = (int32_t)fdiv(r, P.fd_nx);
-  const int32_t i = (int32_t)(r - (uint32_t)j * P.fd_nx.d);
-#pragma unroll
-  for (int dk = 0; dk < 2; dk++)
-#pragma unroll
-    for (int dj = 0; dj < 2; dj++)
-#pragma unroll
-      for (int di = 0; di < 2; di++) {
-        const int32_t ii = i - 1 + di, jj = j - 1 + dj, kk = k - 1 + dk;
-        const bool ok = ii >= 0 && ii < P.bx && jj >= 0 && jj < P.by && kk >= 0 && kk < P.bz;
-        // corner at (x, y, z) = (1 - di, 1 - dj, 1 - dk) of the element: 4 z + (x ^ 3 y)
-        const int q = dk * 4 + dj * 2 + di;
-        el[q] = ok ? ii + P.bx * (jj + P.by * kk) : -1;
-        cor[q] = 4 * (1 - dk) + ((1 - di) ^ (3 * (1 - dj)));
-      }
-}
-
 template <int NPE>
 __device__ __forceinline__ float weightf() {
   return NPE == 8 ? 8.0f : 1.0f / 6.0f;
@@ -1932,9 +1907,22 @@ __global__ void k_mix_init_nodes(StepParams P, MixState M, Fp64State S) {
     M.pa[k * np + n] = 0.f;
   }
   M.mass[n] = (float)S.mass[n];
-  const int32_t b = P.off[n], c = P.off[n + 1] - b;
   double rs = 0.0;
-  for (int32_t k = 0; k < c; k++) rs += S.rho[P.slot[b + k] / NPE];
+  int32_t c = 0;
+  if (NPE == 8 && P.box) {
+    int32_t el[8], cor[8];
+    box_node_list(P, n, el, cor);
+#pragma unroll
+    for (int j = 0; j < 8; j++)
+      if (el[j] >= 0) {
+        rs += S.rho[el[j]];
+        c++;
+      }
+  } else {
+    const int32_t b = P.off[n];
+    c = P.off[n + 1] - b;
+    for (int32_t k = 0; k < c; k++) rs += S.rho[P.slot[b + k] / NPE];
+  }
   M.nc[n] = make_float2((float)(1.0 / S.s0[n]), (float)(rs / c));
 }
 

@@ -605,7 +605,10 @@ int64_t connectivity_scratch_ints(int64_t nn) {
 cudaError_t build_connectivity(const int32_t *el_aos, int64_t ne, int npe, int64_t nn,
                                int32_t *el_soa, int32_t *off, int32_t *slot, int32_t *scratch,
                                cudaStream_t st) {
-  const int64_t ent = ne * npe, ntiles = (nn + kScanTile - 1) / kScanTile;
+  const int64_t ent = ne * npe;
+  if (el_soa) k_elnod_soa<<<grid_for(ent), kThreads, 0, st>>>(el_aos, ne, npe, el_soa);
+  if (!off) return cudaGetLastError();
+  const int64_t ntiles = (nn + kScanTile - 1) / kScanTile;
   int32_t *cnt = scratch, *fill = scratch + nn, *tsum = scratch + 2 * nn;
   cudaError_t e = cudaMemsetAsync(scratch, 0, sizeof(int32_t) * 2 * nn, st);
   if (e != cudaSuccess) return e;
@@ -615,7 +618,6 @@ cudaError_t build_connectivity(const int32_t *el_aos, int64_t ne, int npe, int64
   k_tile_offsets<<<(unsigned)ntiles, kThreads, 0, st>>>(cnt, nn, tsum, off);
   k_place<<<grid_for(ent), kThreads, 0, st>>>(el_aos, ent, off, fill, slot);
   k_sort_lists<<<grid_for(nn), kThreads, 0, st>>>(off, nn, slot);
-  k_elnod_soa<<<grid_for(ent), kThreads, 0, st>>>(el_aos, ne, npe, el_soa);
   return cudaGetLastError();
 }
 
