@@ -375,15 +375,16 @@ WF_API wf_status wf_set_launch_config(wf_domain *d, int32_t phase, int32_t block
  * runs in another order. Positions, predicted velocities, tau and eps_p are
  * held twice (read one copy, write the other). Not with specimens, thermal
  * coupling or triangle-mesh contact; wf_get_sweep tells whether the mesh is
- * swept. Mode 5 (the same meshes): each step is one persistent launch that
- * runs the four phases as a wavefront through the element layers. The work is
- * cut into tiles of 512 elements or nodes of one layer or plane (wf_set_flow_
- * tiles); blocks take tiles in a fixed ticket order (geometry of layer s,
- * nodal phase of plane s-1, element phase of layer s-2, node update of plane
- * s-lag) and wait, with bounded waits, for the tiles they read, so the element
- * forces are read back from L2 shortly after they are written. Each element
- * and node runs mode 1's arithmetic: the state is bitwise that of mode 1; the
- * reaction sum runs in another order. A wait that runs out (a bug, never
+ * swept. Mode 5 (the same meshes): after the geometry and nodal kernels, one
+ * persistent launch runs the element and node phases as a wavefront through
+ * the element layers. The work is cut into tiles of 512 elements or nodes of
+ * one layer or plane (wf_set_flow_tiles); blocks take tiles in a fixed ticket
+ * order (the elements of layer s, then the node update of plane s-lag) and a
+ * node tile waits, with a bounded wait, for the element tiles it reads, so
+ * the element forces are read back from L2 shortly after they are written.
+ * Each element and node runs mode 1's arithmetic: the state is bitwise that
+ * of mode 1; the reaction sum runs in another order. A wait that runs out (a
+ * bug, never
  * expected) makes the next wf_sync return WF_ERR_TIMEOUT. On GB300 mode 5 is
  * slower than modes 4 and 1 (the blocks' waits and ticket traffic cost more
  * than the L2 reuse saves) and is only run when asked for. Mode 0 (default)
@@ -400,8 +401,8 @@ WF_API wf_status wf_set_step_mode(wf_domain *d, int32_t mode);
  * why_cap bytes), the reason the mesh is not swept. Any output may be NULL. */
 WF_API wf_status wf_set_sweep_rows(wf_domain *d, int32_t rows);
 /* No counterpart in the reference. Dataflow step (mode 5): items per tile (a
- * multiple of 256, 256 to 8192; default 512) and the stages the node update
- * lags the geometry (3 to 16; default 12), before wf_init. wf_get_flow: tiles
+ * multiple of 256, 256 to 8192; default 512) and the layers the node update
+ * lags the elements (1 to 16; default 4), before wf_init. wf_get_flow: tiles
  * per step and blocks per launch, or zeros and, in why, the reason the mesh
  * has no dataflow step. Any output may be NULL. */
 WF_API wf_status wf_set_flow_tiles(wf_domain *d, int32_t tile, int32_t lag);

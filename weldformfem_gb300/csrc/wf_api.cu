@@ -254,7 +254,7 @@ struct wf_domain {
   std::string flow_why;
   unsigned *flow_cnt[2] = {nullptr, nullptr};
   int flow_par = 0;
-  int32_t flow_tile = 512, flow_lag = 12;
+  int32_t flow_tile = 512, flow_lag = 4;
   int cl_blocks = 0, cl_bs = 0;
   double *cl_part = nullptr;      // [kClusterChunk][cl_blocks] reaction partials
   double *edge_min = nullptr;     // the shortest edge (wf_min_edge_length's device result)
@@ -1658,6 +1658,9 @@ bool sweep_mode(const wf_domain *d) {
 // Whether the automatic mode picks the dataflow step for box meshes (before
 // the column sweep): not, the sweep is faster on GB300.
 constexpr bool kFlowAuto = false;
+// Whether the dataflow step leaves the geometry and nodal phases to their own
+// kernels (its launch then pipelines element and node-update tiles only).
+constexpr bool kFlowSplit = true;
 // Whether the steps of d run as the dataflow step.
 bool flow_mode(const wf_domain *d) {
   if (d->precision != WF_MIXED || !d->flow) return false;
@@ -1706,7 +1709,7 @@ WF_API wf_status wf_set_flow_tiles(wf_domain *d, int32_t tile, int32_t lag) {
   if (!d) return WF_ERR_ARG;
   if (tile < 256 || tile > 8192 || (tile & 255))
     return fail(d, WF_ERR_ARG, "dataflow tiles hold a multiple of 256 items, 256 to 8192");
-  if (lag < 3 || lag > 16) return fail(d, WF_ERR_ARG, "the node-update lag is 3 to 16 stages");
+  if (lag < 1 || lag > 16) return fail(d, WF_ERR_ARG, "the node-update lag is 1 to 16 stages");
   if (d->initialized) return fail(d, WF_ERR_STATE, "the dataflow tiles are chosen before init");
   d->flow_tile = tile;
   d->flow_lag = lag;
@@ -2299,7 +2302,7 @@ WF_API wf_status wf_init(wf_domain *d) {
         d->flow_why = "the dataflow kernel cannot launch on this device";
       } else {
         std::vector<int> first;
-        flow_stages(P, d->flow_tile, d->flow_lag, first, d->F);
+        flow_stages(P, d->flow_tile, d->flow_lag, kFlowSplit, first, d->F);
         int *fs = nullptr;
         CUDA_TRY(upload(d, &fs, first));
         d->F.stage_first = fs;
@@ -2365,6 +2368,10 @@ namespace {
 
 // One dataflow step: counts in the current counter set, zeroes the other.
 void launch_flow(wf_domain *d) {
+  if (d->F.split) {
+    mix_geometry(d->P, d->M, d->mvol, d->stream, d->cfg[0]);
+    mix_nodal(d->P, d->M, d->mvol, d->stream, d->cfg[1]);
+  }
   d->F.cnt = d->flow_cnt[d->flow_par];
   d->F.cnt_next = d->flow_cnt[d->flow_par ^ 1];
   mix_flow(d->P, d->M, d->mvol, d->F, d->stream);

@@ -266,6 +266,8 @@ struct FlowParams {
   unsigned *cnt = nullptr;        // [0] next ticket, [1 + kind * bz1 + l] tiles done of an item
   unsigned *cnt_next = nullptr;   // the next step's set
   double *partials = nullptr;     // [bz1 * ntiles[3]] reaction per node-update tile
+  int32_t split = 0;              // 1: the geometry and nodal phases run as their own
+                                  // kernels before the launch (no G, N1 tiles)
 };
 
 // Host-side view of one state for the legacy VTK writer (write_vtk_text,
@@ -343,7 +345,8 @@ void mix_sweep(const StepParams &P, const MixState &M, const SweepParams &W, cud
 // one step. flow_grid: the persistent grid (0: the
 // kernel cannot launch here).
 int flow_grid(const StepParams &P);
-void flow_stages(const StepParams &P, int tile, int lag, std::vector<int> &first, FlowParams &F);
+void flow_stages(const StepParams &P, int tile, int lag, bool split, std::vector<int> &first,
+                 FlowParams &F);
 void mix_flow(const StepParams &P, const MixState &M, float *vol, const FlowParams &F,
               cudaStream_t st);
 // Whole runs of steps in one launch of one cluster of `blocks` blocks of `bs`

@@ -2328,7 +2328,8 @@ int flow_grid(const StepParams &P) {
   return per * P.sms;
 }
 
-void flow_stages(const StepParams &P, int tile, int lag, std::vector<int> &first, FlowParams &F) {
+void flow_stages(const StepParams &P, int tile, int lag, bool split, std::vector<int> &first,
+                 FlowParams &F) {
   const int64_t exy = (int64_t)P.bx * P.by, pxy = (int64_t)(P.bx + 1) * (P.by + 1);
   const int bz = P.bz;
   // the light phases (geometry, nodal) in tiles four times larger
@@ -2337,12 +2338,22 @@ void flow_stages(const StepParams &P, int tile, int lag, std::vector<int> &first
   const int64_t per[kFlowKinds] = {exy, pxy, exy, pxy};
   for (int q = 0; q < kFlowKinds; q++)
     F.ntiles[q] = (int)((per[q] + F.tsize[q] - 1) / F.tsize[q]);
-  // stage offsets 0, lag/3, 2 lag/3, lag: each phase a third of the lag
-  // behind the one it reads
-  F.off[0] = 0;
-  F.off[1] = std::max(1, lag / 3);
-  F.off[2] = std::max(F.off[1] + 1, 2 * lag / 3);
-  F.off[3] = std::max(F.off[2] + 1, lag);
+  F.split = split ? 1 : 0;
+  if (split) {
+    // geometry and nodal phases done before the launch: element tiles wait on
+    // nothing (their items need zero tiles of the nodal phase), node-update
+    // tiles lag them by `lag` layers
+    F.ntiles[0] = F.ntiles[1] = 0;
+    F.off[0] = F.off[1] = F.off[2] = 0;
+    F.off[3] = lag;
+  } else {
+    // stage offsets 0, lag/3, 2 lag/3, lag: each phase a third of the lag
+    // behind the one it reads
+    F.off[0] = 0;
+    F.off[1] = std::max(1, lag / 3);
+    F.off[2] = std::max(F.off[1] + 1, 2 * lag / 3);
+    F.off[3] = std::max(F.off[2] + 1, lag);
+  }
   F.nstages = bz + F.off[3] + 1;
   first.assign(F.nstages + 1, 0);
   int t = 0;
