@@ -284,7 +284,7 @@ WF_API wf_status wf_run(wf_domain *d, int64_t nsteps);
  * a following wf_run(d, nsteps) replays (and grows the histories it fills),
  * so that the run itself does no capture. Runs nothing. */
 WF_API wf_status wf_prepare_run(wf_domain *d, int64_t nsteps);
-/* No counterpart in the reference. One FP64 step in two halves, for a slab
+/* No counterpart in the reference. One step in two halves, for a slab
  * decomposition of one mesh over several domains (weldformfem_gb300/slabs.py):
  * wf_step_begin queues the predictor, geometry, nodal and element phases
  * (the loop body up to the element forces, Solver_explicit.C:346-760),
@@ -296,12 +296,20 @@ WF_API wf_status wf_prepare_run(wf_domain *d, int64_t nsteps);
  * node state a step starts from for nodes [n0, n1): positions, velocities,
  * previous accelerations and displacements (12 x (n1 - n0) doubles: field,
  * then component, then node). Host buffers; the calls wait for the domain's
- * stream. FP64 step only, without specimens, thermal coupling, triangle-mesh
- * contact or the energy history (WF_ERR_UNSUPPORTED). */
+ * stream. In mixed precision the halves run the per-phase kernels (whatever
+ * the step mode of wf_run); the forces are the FP32 element-minus-hourglass
+ * forces widened to doubles (npe x 3 rows of (e1 - e0) values, then as many
+ * zeros), and the node state is 18 x (n1 - n0) doubles: position hi and lo
+ * parts, velocity, previous acceleration, predicted velocity and contact slip,
+ * each exact. Not with specimens, thermal coupling, triangle-mesh contact or
+ * the energy history (WF_ERR_UNSUPPORTED). */
 WF_API wf_status wf_step_begin(wf_domain *d);
 WF_API wf_status wf_step_end(wf_domain *d);
 WF_API wf_status wf_get_halo_forces(wf_domain *d, int64_t e0, int64_t e1, double *out);
 WF_API wf_status wf_set_halo_forces(wf_domain *d, int64_t e0, int64_t e1, const double *in);
+/* Values per node of wf_get_halo_nodes / wf_set_halo_nodes: 12 (FP64) or 18
+ * (mixed); the buffers hold that many times (n1 - n0) doubles. */
+WF_API wf_status wf_get_halo_node_width(const wf_domain *d, int32_t *values_per_node);
 WF_API wf_status wf_get_halo_nodes(wf_domain *d, int64_t n0, int64_t n1, double *out);
 WF_API wf_status wf_set_halo_nodes(wf_domain *d, int64_t n0, int64_t n1, const double *in);
 /* Domain_d::SolveChungHulbert: steps while Time < end time; *nsteps = count. */

@@ -129,6 +129,37 @@ def test_two_gloo_ranks_equal_one_domain():
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", list(CASES))
+def test_gpu_mixed_slabs_equal_one_domain(name):
+    """The mixed step in halves: three slabs equal one domain of the whole mesh
+    run by the per-phase kernels, bit for bit in positions, velocities and
+    displacements (every owned node gathers its element forces in list order,
+    the halo layers' forces and the halo planes' state coming from their
+    owners); the reaction is summed per rank and then in rank order."""
+    import weldformfem_gb300 as wf
+
+    cid, scale, steps = CASES[name]
+    case = W.config(cid, scale=scale)
+
+    def mixed():
+        d = wf.Domain(wf.WF_MIXED)
+        return d
+
+    whole = mixed()
+    W.apply(whole, case)
+    whole.set_step_mode(1)
+    whole.init()
+    whole.run(steps)
+    plan = SL.plan(*case.nel, 3)
+    run = SL.SlabRun(plan, slab_domains(mixed, case, plan, case.time_step(), range(3)),
+                     SL.LocalTransport())
+    run.step(steps)
+    check_equal(run, whole)
+    assert float(np.max(np.abs(run.reaction() - whole.reaction()))) <= \
+        1e-12 * float(np.max(np.abs(whole.reaction())))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", list(CASES))
 def test_gpu_slabs_equal_one_domain(name):
     import weldformfem_gb300 as wf
 

@@ -135,6 +135,7 @@ _SIGS = {
                          C.POINTER(C.c_int32)],
     "wf_set_box_indexing": [C.c_void_p, C.c_int32],
     "wf_set_sweep_rows": [C.c_void_p, C.c_int32],
+    "wf_get_halo_node_width": [C.c_void_p, C.POINTER(C.c_int32)],
     "wf_set_flow_tiles": [C.c_void_p, C.c_int32, C.c_int32],
     "wf_get_flow": [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_char_p,
                     C.c_int64],
@@ -402,16 +403,28 @@ class Domain:
         return out
 
     def set_halo_forces(self, e0, e1, data):
-        self._call("wf_set_halo_forces", int(e0), int(e1), np.ascontiguousarray(data, np.float64))
+        data = np.ascontiguousarray(data, np.float64).reshape(-1)
+        if data.size != 2 * (e1 - e0) * self.npe * 3:
+            raise ValueError("halo forces of the wrong size")
+        self._call("wf_set_halo_forces", int(e0), int(e1), data)
+
+    def halo_node_width(self):
+        """Values per node of halo_nodes: 12 (FP64 step) or 18 (mixed)."""
+        w = C.c_int32()
+        self._call("wf_get_halo_node_width", C.byref(w))
+        return w.value
 
     def halo_nodes(self, n0, n1):
         """Node state a step starts from, nodes [n0, n1), flat."""
-        out = np.zeros(12 * (n1 - n0))
+        out = np.zeros(self.halo_node_width() * (n1 - n0))
         self._call("wf_get_halo_nodes", int(n0), int(n1), out)
         return out
 
     def set_halo_nodes(self, n0, n1, data):
-        self._call("wf_set_halo_nodes", int(n0), int(n1), np.ascontiguousarray(data, np.float64))
+        data = np.ascontiguousarray(data, np.float64).reshape(-1)
+        if data.size != self.halo_node_width() * (n1 - n0):
+            raise ValueError("halo node state of the wrong size")
+        self._call("wf_set_halo_nodes", int(n0), int(n1), data)
 
     def solve(self):
         n = C.c_int64()

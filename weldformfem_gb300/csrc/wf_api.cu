@@ -2680,9 +2680,9 @@ namespace {
 wf_status need_halves(wf_domain *d) {
   if (!d) return WF_ERR_ARG;
   if (!d->initialized) return fail(d, WF_ERR_STATE, "wf_init not called");
-  if (d->precision != WF_FP64 || d->nspec || d->thermal || d->P.tri_on || d->P.energy_on)
-    return fail(d, WF_ERR_UNSUPPORTED, "step halves need the FP64 step without specimens, "
-                                       "thermal coupling, triangle-mesh contact or energies");
+  if (d->nspec || d->thermal || d->P.tri_on || d->P.energy_on)
+    return fail(d, WF_ERR_UNSUPPORTED, "step halves need a step without specimens, thermal "
+                                       "coupling, triangle-mesh contact or energies");
   if (!(d->dt > 0.0)) return fail(d, WF_ERR_STATE, "time step not set (SetDT)");
   return WF_OK;
 }
@@ -2696,10 +2696,19 @@ WF_API wf_status wf_step_begin(wf_domain *d) {
   if ((s = grow_history(d, d->host_step + 1))) return s;
   set_dt_constants(d->P, d->dt);
   const StepParams &P = d->P;
-  fp64_predict(P, d->S, d->stream);
-  fp64_geometry(P, d->S, d->stream, false);
-  fp64_nodal(P, d->S, d->stream, 0);
-  fp64_elements(P, d->S, d->stream);
+  if (d->precision == WF_FP64) {
+    fp64_predict(P, d->S, d->stream);
+    fp64_geometry(P, d->S, d->stream, false);
+    fp64_nodal(P, d->S, d->stream, 0);
+    fp64_elements(P, d->S, d->stream);
+  } else {
+    // the mixed per-phase kernels, whatever the step mode of wf_run
+    mix_predict(P, d->M, d->stream);
+    mix_geometry(P, d->M, d->mvol, d->stream, d->cfg[0]);
+    mix_nodal(P, d->M, d->mvol, d->stream, d->cfg[1]);
+    mix_elements(P, d->M, d->mvol, d->stream, d->cfg[2]);
+    d->mix_valid_fp64 = false;
+  }
   CUDA_TRY(cudaGetLastError());
   d->launches += 4;
   d->half_open = true;
@@ -2711,7 +2720,10 @@ WF_API wf_status wf_step_end(wf_domain *d) {
   if (s) return s;
   if (!d->half_open) return fail(d, WF_ERR_STATE, "wf_step_begin not called");
   CUDA_TRY(cudaSetDevice(d->device));
-  fp64_nodes(d->P, d->S, d->stream, d->node_grid);
+  if (d->precision == WF_FP64)
+    fp64_nodes(d->P, d->S, d->stream, d->node_grid);
+  else
+    mix_nodes(d->P, d->M, d->stream, d->node_grid);
   CUDA_TRY(cudaGetLastError());
   CUDA_TRY(cudaMemcpyAsync(d->st_host, d->P.st, sizeof(StepState), cudaMemcpyDeviceToHost,
                            d->stream));
@@ -2729,6 +2741,21 @@ WF_API wf_status wf_get_halo_forces(wf_domain *d, int64_t e0, int64_t e1, double
   if (!out || e0 < 0 || e1 > d->ne || e0 > e1) return WF_ERR_ARG;
   CUDA_TRY(cudaSetDevice(d->device));
   const size_t k = (size_t)(e1 - e0) * d->npe * 3, at = (size_t)e0 * d->npe * 3;
+  if (d->precision == WF_MIXED) {
+    // FP32 forces (element force minus hourglass force) [npe * 3][ne]: the
+    // element range of every (corner, component) row, widened exactly; the
+    // second half (the FP64 step's hourglass forces) is zero
+    const size_t m = (size_t)(e1 - e0), rows = (size_t)d->npe * 3;
+    std::vector<float> h(rows * m);
+    CUDA_TRY(cudaMemcpy2DAsync(h.data(), sizeof(float) * m, d->M.fe + e0,
+                               sizeof(float) * d->ne, sizeof(float) * m, rows,
+                               cudaMemcpyDeviceToHost, d->stream));
+    CUDA_TRY(cudaStreamSynchronize(d->stream));
+    for (size_t i = 0; i < rows * m; i++) out[i] = (double)h[i];
+    std::fill(out + k, out + 2 * k, 0.0);
+    d->d2h_bytes += (int64_t)(sizeof(float) * rows * m);
+    return WF_OK;
+  }
   CUDA_TRY(cudaMemcpyAsync(out, d->S.fe + at, sizeof(double) * k, cudaMemcpyDeviceToHost,
                            d->stream));
   if (d->S.fhg)
@@ -2747,6 +2774,16 @@ WF_API wf_status wf_set_halo_forces(wf_domain *d, int64_t e0, int64_t e1, const 
   if (!in || e0 < 0 || e1 > d->ne || e0 > e1) return WF_ERR_ARG;
   CUDA_TRY(cudaSetDevice(d->device));
   const size_t k = (size_t)(e1 - e0) * d->npe * 3, at = (size_t)e0 * d->npe * 3;
+  if (d->precision == WF_MIXED) {
+    const size_t m = (size_t)(e1 - e0), rows = (size_t)d->npe * 3;
+    std::vector<float> h(rows * m);
+    for (size_t i = 0; i < rows * m; i++) h[i] = (float)in[i];
+    CUDA_TRY(cudaMemcpy2DAsync(d->M.fe + e0, sizeof(float) * d->ne, h.data(), sizeof(float) * m,
+                               sizeof(float) * m, rows, cudaMemcpyHostToDevice, d->stream));
+    CUDA_TRY(cudaStreamSynchronize(d->stream));
+    d->h2d_bytes += (int64_t)(sizeof(float) * rows * m);
+    return WF_OK;
+  }
   CUDA_TRY(cudaMemcpyAsync(d->S.fe + at, in, sizeof(double) * k, cudaMemcpyHostToDevice,
                            d->stream));
   if (d->S.fhg)
@@ -2765,13 +2802,61 @@ void halo_fields(wf_domain *d, double *f[4]) {
   f[2] = d->S.pa;
   f[3] = d->S.u;
 }
+
+// The mixed step's node state between steps, 18 values per node as doubles
+// (exact): positions hi and lo, velocity, previous acceleration, predicted
+// velocity, contact slip; read into out or written from in.
+wf_status mixed_halo_nodes(wf_domain *d, int64_t n0, int64_t n1, double *out, const double *in) {
+  const size_t m = (size_t)(n1 - n0);
+  const int64_t np = d->np;
+  std::vector<float2> xh(3 * m);
+  std::vector<float> f(12 * m);
+  float *rows[4] = {d->M.v, d->M.pa, d->M.vp, d->M.ut};
+  if (out) {
+    for (int k = 0; k < 3; k++)
+      CUDA_TRY(cudaMemcpyAsync(xh.data() + k * m, d->M.xh + k * np + n0, sizeof(float2) * m,
+                               cudaMemcpyDeviceToHost, d->stream));
+    for (int q = 0; q < 4; q++)
+      for (int k = 0; k < 3; k++)
+        CUDA_TRY(cudaMemcpyAsync(f.data() + (3 * q + k) * m, rows[q] + k * np + n0,
+                                 sizeof(float) * m, cudaMemcpyDeviceToHost, d->stream));
+    CUDA_TRY(cudaStreamSynchronize(d->stream));
+    for (size_t i = 0; i < 3 * m; i++) {
+      out[i] = (double)xh[i].x;
+      out[3 * m + i] = (double)xh[i].y;
+    }
+    for (size_t i = 0; i < 12 * m; i++) out[6 * m + i] = (double)f[i];
+    d->d2h_bytes += (int64_t)(sizeof(float) * 18 * m);
+    return WF_OK;
+  }
+  for (size_t i = 0; i < 3 * m; i++) xh[i] = make_float2((float)in[i], (float)in[3 * m + i]);
+  for (size_t i = 0; i < 12 * m; i++) f[i] = (float)in[6 * m + i];
+  for (int k = 0; k < 3; k++)
+    CUDA_TRY(cudaMemcpyAsync(d->M.xh + k * np + n0, xh.data() + k * m, sizeof(float2) * m,
+                             cudaMemcpyHostToDevice, d->stream));
+  for (int q = 0; q < 4; q++)
+    for (int k = 0; k < 3; k++)
+      CUDA_TRY(cudaMemcpyAsync(rows[q] + k * np + n0, f.data() + (3 * q + k) * m,
+                               sizeof(float) * m, cudaMemcpyHostToDevice, d->stream));
+  CUDA_TRY(cudaStreamSynchronize(d->stream));
+  d->h2d_bytes += (int64_t)(sizeof(float) * 18 * m);
+  d->mix_valid_fp64 = false;
+  return WF_OK;
+}
 }  // namespace
+
+WF_API wf_status wf_get_halo_node_width(const wf_domain *d, int32_t *values_per_node) {
+  if (!d || !values_per_node) return WF_ERR_ARG;
+  *values_per_node = d->precision == WF_MIXED ? 18 : 12;
+  return WF_OK;
+}
 
 WF_API wf_status wf_get_halo_nodes(wf_domain *d, int64_t n0, int64_t n1, double *out) {
   wf_status s = need_halves(d);
   if (s) return s;
   if (!out || n0 < 0 || n1 > d->nn || n0 > n1) return WF_ERR_ARG;
   CUDA_TRY(cudaSetDevice(d->device));
+  if (d->precision == WF_MIXED) return mixed_halo_nodes(d, n0, n1, out, nullptr);
   double *f[4];
   halo_fields(d, f);
   const size_t m = (size_t)(n1 - n0);
@@ -2789,6 +2874,7 @@ WF_API wf_status wf_set_halo_nodes(wf_domain *d, int64_t n0, int64_t n1, const d
   if (s) return s;
   if (!in || n0 < 0 || n1 > d->nn || n0 > n1) return WF_ERR_ARG;
   CUDA_TRY(cudaSetDevice(d->device));
+  if (d->precision == WF_MIXED) return mixed_halo_nodes(d, n0, n1, nullptr, in);
   double *f[4];
   halo_fields(d, f);
   const size_t m = (size_t)(n1 - n0);
