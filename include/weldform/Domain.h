@@ -38,7 +38,8 @@ class Elastic_ {
   double E_m, nu_m;
 };
 
-enum { BILINEAR = 0, HOLLOMON = 1, JOHNSON_COOK = 2 };
+// model numbers of Material.cuh:9-12 (GMT_MODEL is the reference's _GMT_)
+enum { BILINEAR = 0, HOLLOMON = 1, JOHNSON_COOK = 2, GMT_MODEL = 3 };
 
 // Material_ (Material.cuh:36-156): the fields the explicit step reads.
 class Material_ {
@@ -77,9 +78,28 @@ class Material_ {
   double K = 1.0, m = 1.0;
   double cs0 = 0.0;     // informational; the library uses sqrt(K_bulk / rho)
   double k_T = 0.0, cp_T = 0.0, exp_T = 0.0;  // thermal (Material.cuh:81-83)
+  // GMT constants and ranges (Material.cuh:63-78)
+  double C1 = 0.0, C2 = 0.0, m1 = 0.0, m2 = 0.0, n1 = 0.0, n2 = 0.0, I1 = 0.0, I2 = 0.0;
+  double e_min = 0.0, e_max = 1.0e10, er_min = 0.0, er_max = 1.0e10, T_min = 0.0, T_max = 1.0e10;
 
  private:
   Elastic_ elastic_m;
+};
+
+// GMT (Material.cuh:255-290) with the constructor's argument order. The
+// constants go to the Material_ fields the law reads; T (inherited) is the
+// temperature without thermal coupling. e_min must be > 0 (wf_set_gmt).
+class GMT : public Material_ {
+ public:
+  GMT(const Elastic_ &el, double n1_, double n2_, double C1_, double C2_, double m1_, double m2_,
+      double I1_, double I2_, double e_min_ = 0.0, double e_max_ = 1.0e10, double er_min_ = 0.0,
+      double er_max_ = 1.0e10, double T_min_ = 0.0, double T_max_ = 1.0e10)
+      : Material_(el) {
+    Material_model = GMT_MODEL;
+    n1 = n1_; n2 = n2_; C1 = C1_; C2 = C2_; m1 = m1_; m2 = m2_; I1 = I1_; I2 = I2_;
+    e_min = e_min_; e_max = e_max_; er_min = er_min_; er_max = er_max_;
+    T_min = T_min_; T_max = T_max_;
+  }
 };
 
 class Domain_d {
@@ -128,6 +148,11 @@ class Domain_d {
       if (m.Material_model == JOHNSON_COOK)
         check(wf_set_johnson_cook(d_, (int32_t)i, m.B, m.n, m.C, m.eps_0, m.m, m.T_m, m.T_t, m.T),
               "Init_JohnsonCook");
+      if (m.Material_model == GMT_MODEL) {
+        const double c[8] = {m.n1, m.n2, m.C1, m.C2, m.m1, m.m2, m.I1, m.I2};
+        const double r[6] = {m.e_min, m.e_max, m.er_min, m.er_max, m.T_min, m.T_max};
+        check(wf_set_gmt(d_, (int32_t)i, c, r, m.T), "GMT");
+      }
       if (m.cp_T > 0.0)
         check(wf_set_material_thermal(d_, (int32_t)i, m.k_T, m.cp_T, m.exp_T), "thermal");
     }

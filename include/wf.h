@@ -44,7 +44,9 @@ typedef enum {
 
 typedef enum { WF_FP64 = 0, WF_MIXED = 1 } wf_precision;
 
-typedef enum { WF_MAT_BILINEAR = 0, WF_MAT_HOLLOMON = 1, WF_MAT_JOHNSON_COOK = 2 } wf_material_model;
+typedef enum {
+  WF_MAT_BILINEAR = 0, WF_MAT_HOLLOMON = 1, WF_MAT_JOHNSON_COOK = 2, WF_MAT_GMT = 3
+} wf_material_model;
 
 /* Material_ + Elastic_ (include/common/Material.cuh:15-156). BILINEAR is
  * linear isotropic hardening sigma_y = sy0 + H eps_p. HOLLOMON is the
@@ -131,11 +133,31 @@ WF_API wf_status wf_set_materials(wf_domain *d, int32_t nmat, const wf_material 
  * Mechanical.C:1701-1770). edot is the element's effective strain rate
  * sqrt(((Dxx-Dyy)^2 + (Dyy-Dzz)^2 + (Dzz-Dxx)^2) / 2 + 3 (Dxy^2 + Dyz^2 + Dxz^2))
  * (1e-5 where it is exactly 0) and edot' = min(edot, 1e6). T is the
- * (uniform) temperature of the material's elements: thermal coupling is not
- * built. Call after wf_set_materials and before wf_init. */
+ * (uniform) temperature of the material's elements; with thermal coupling
+ * (wf_set_thermal) each element takes the mean of its node temperatures
+ * instead. Call after wf_set_materials and before wf_init. */
 WF_API wf_status wf_set_johnson_cook(wf_domain *d, int32_t mat, double B, double n, double C,
                                      double eps0_dot, double m, double T_melt,
                                      double T_transition, double T);
+/* The GMT law (class GMT, Material.cuh:255-290; CalcGMTYieldStress and
+ * CalcGMTTangentModulus, Material.cuh:417-478) for a material of model
+ * WF_MAT_GMT. With e = eps_p, r = edot and T each clamped to its range,
+ *   sigma_y = C1 exp(C2 T) e^(n1 T + n2) exp((I1 T + I2) / e) r^(m1 T + m2),
+ *   Et = C1 exp(C2 T) r^(m1 T + m2) e^(n1 T + n2 - 2)
+ *        (e (n1 T + n2) - I1 T - I2) exp((I1 T + I2) / e),
+ * sigma_y at the element's effective strain rate edot (as for Johnson-Cook,
+ * without its 1e-5 floor) and Et at min(edot, 1e6) (CalcStressStrain,
+ * Mechanical.C:1727-1749). c = {n1, n2, C1, C2, m1, m2, I1, I2}, the order of
+ * the input deck's "const" (main.C:548-551). range = {e_min, e_max, er_min,
+ * er_max, T_min, T_max} (the class defaults are {0, 1e10, 0, 1e10, 0, 1e10});
+ * e_min must be > 0, since at e = 0 both functions are 0 * inf.
+ * T is the temperature as for wf_set_johnson_cook. (The reference's GMT
+ * constructor stores the eight constants in members of the derived class that
+ * hide Material_'s, which the two functions read, so a reference deck's GMT
+ * material runs with Material_'s uninitialised values; here the constants
+ * reach the law.) Call after wf_set_materials and before wf_init. */
+WF_API wf_status wf_set_gmt(wf_domain *d, int32_t mat, const double c[8], const double range[6],
+                            double T);
 /* Per-element material index (the reference's mat[e] pointers). */
 WF_API wf_status wf_set_elem_materials(wf_domain *d, const int32_t *ids);
 
@@ -515,7 +537,11 @@ WF_API wf_status wf_adjoint_backward(wf_domain *d, const double *dL_dR, int32_t 
  * (Bilinear: const[0] = tangent modulus Et, H = E Et / (E - Et); Hollomon:
  * const = [K, n]; JohnsonCook: A = yieldStress0, const = [B, n, C, eps0_dot]
  * with m = 1, T_melt = 1e10, T_transition = 0 as the non-thermal driver sets
- * them, temperature 0), DomainBlocks[0] (File: an LS-DYNA .k mesh, path relative to
+ * them, temperature 0; GMT: const = [n1, n2, C1, C2, m1, m2, I1, I2] with
+ * e_range, er_range, T_range, see wf_set_gmt; NortonHoff is rejected, since no
+ * function of the reference's step reads its constants: CalcStressStrain keeps
+ * the initial yield stress and, once the element yields, reads an unset
+ * tangent modulus), DomainBlocks[0] (File: an LS-DYNA .k mesh, path relative to
  * the deck; Box: a 3-D box of elemLength cells, elemType TriTet for
  * tetrahedra) and BoundaryConditions (one velocity zone per condition, from
  * its start/end box or, when it has none, from the DomainZones entry of its
@@ -565,6 +591,9 @@ typedef struct {
    * heatCondCoeff / dieTemp (default 20) */
   int32_t thermal;
   double T0, thermal_k, thermal_cp, thermal_exp, heat_cond, die_temp;
+  /* GMT material: const n1, n2, C1, C2, m1, m2, I1, I2 and e_range, er_range,
+   * T_range (main.C:548-552) */
+  double gmt[8], gmt_range[6];
 } wf_deck_info;
 WF_API wf_status wf_deck_read(const char *path, wf_deck **out, char *err, int64_t err_len);
 WF_API wf_status wf_deck_free(wf_deck *k);

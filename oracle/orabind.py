@@ -64,6 +64,7 @@ def lib():
         "wfo_set_materials": ([vp, C.c_int, C.POINTER(WfoMaterial)], C.c_int),
         "wfo_set_elem_materials": ([vp, _ip], C.c_int),
         "wfo_set_johnson_cook": ([vp, C.c_int] + [C.c_double] * 8, C.c_int),
+        "wfo_set_gmt": ([vp, C.c_int, _dp, _dp, C.c_double], C.c_int),
         "wfo_add_bc_vel_node": ([vp, i64, C.c_int, C.c_double], C.c_int),
         "wfo_allocate_bcs": ([vp], C.c_int),
         "wfo_set_reaction_nodes": ([vp, i64, _ip, C.c_int], C.c_int),
@@ -199,6 +200,13 @@ class OracleDomain:
         self._check(lib().wfo_set_johnson_cook(self.h, int(mat), float(B), float(n), float(C),
                                                float(eps0), float(m), float(Tm), float(Tt),
                                                float(T)), "set_johnson_cook")
+
+    def set_gmt(self, mat, c, rng, T=0.0):
+        """GMT law: c = (n1, n2, C1, C2, m1, m2, I1, I2), rng = (e_min, e_max,
+        er_min, er_max, T_min, T_max), T the uniform element temperature."""
+        self._check(lib().wfo_set_gmt(self.h, int(mat), np.ascontiguousarray(c, np.float64),
+                                      np.ascontiguousarray(rng, np.float64), float(T)),
+                    "set_gmt")
 
     def set_hourglass(self, coef):
         lib().wfo_set_hourglass(self.h, float(coef))

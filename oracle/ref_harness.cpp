@@ -531,6 +531,24 @@ void wfr_set_johnson_cook(void *h, int mat, double B, double n, double C, double
   if (mat == 0) d->AssignMaterial(&d->mats[0]);
 }
 
+// The GMT law on material `mat`: the reference's CalcStressStrain reads the
+// constants from the Material_ fields (Material.cuh:63-78), which the GMT
+// class constructor leaves unset (its own members of the same names hide
+// them), so they are set here directly; c = {n1, n2, C1, C2, m1, m2, I1, I2},
+// range = {e_min, e_max, er_min, er_max, T_min, T_max}; T the uniform T[].
+void wfr_set_gmt(void *h, int mat, const double *c, const double *range, double T) {
+  RefDomain *d = static_cast<RefDomain *>(h);
+  Material_ &M = d->mats[mat];
+  M.Material_model = _GMT_;
+  M.n1 = c[0]; M.n2 = c[1]; M.C1 = c[2]; M.C2 = c[3];
+  M.m1 = c[4]; M.m2 = c[5]; M.I1 = c[6]; M.I2 = c[7];
+  M.e_min = range[0]; M.e_max = range[1];
+  M.er_min = range[2]; M.er_max = range[3];
+  M.T_min = range[4]; M.T_max = range[5];
+  d->temp = T;
+  if (mat == 0) d->AssignMaterial(&d->mats[0]);
+}
+
 // Thermal coupling as the JSON driver sets it (main.C:424-441): every node at T0.
 void wfr_set_thermal(void *h, int on, double T0) {
   RefDomain *d = static_cast<RefDomain *>(h);

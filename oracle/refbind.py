@@ -45,6 +45,7 @@ def lib():
         "wfr_set_materials": ([vp, C.c_int, _dp, _dp, _dp, _dp, _dp, _ip, _dp, _dp], None),
         "wfr_set_elem_materials": ([vp, _ip], None),
         "wfr_set_johnson_cook": ([vp, C.c_int] + [C.c_double] * 8, None),
+        "wfr_set_gmt": ([vp, C.c_int, _dp, _dp, C.c_double], None),
         "wfr_set_linear_hardening": ([vp, C.c_int], None),
         "wfr_set_hourglass": ([vp, C.c_double], None),
         "wfr_set_press_algorithm": ([vp, C.c_int], None),
@@ -202,6 +203,10 @@ class RefDomain:
     def set_johnson_cook(self, mat, B, n, C, eps0, m, Tm, Tt, T=0.0):
         lib().wfr_set_johnson_cook(self.h, int(mat), float(B), float(n), float(C), float(eps0),
                                    float(m), float(Tm), float(Tt), float(T))
+
+    def set_gmt(self, mat, c, rng, T=0.0):
+        lib().wfr_set_gmt(self.h, int(mat), np.ascontiguousarray(c, np.float64),
+                          np.ascontiguousarray(rng, np.float64), float(T))
 
     def set_linear_hardening(self, on=True):
         lib().wfr_set_linear_hardening(self.h, int(on))

@@ -24,6 +24,10 @@ typedef struct {
   /* Johnson-Cook (Material_::Init_JohnsonCook, Material.cuh:105-114) and the
    * element temperature it reads (uniform here) */
   double jc_B, jc_n, jc_C, jc_eps0, jc_m, jc_Tm, jc_Tt, jc_T;
+  /* GMT (Material_ C1, C2, n1, n2, m1, m2, I1, I2 and the e, er, T ranges,
+   * Material.cuh:63-78) and its (uniform) element temperature */
+  double g_C1, g_C2, g_n1, g_n2, g_m1, g_m2, g_I1, g_I2;
+  double g_emin, g_emax, g_rmin, g_rmax, g_Tmin, g_Tmax, g_T;
   /* thermal constants (Material_ k_T, cp_T, exp_T, Material.cuh:81-83) */
   double k_T, cp_T, exp_T;
 } mat_t;
@@ -346,6 +350,22 @@ int wfo_set_johnson_cook(wfo_domain *d, int mat, double B, double n, double C, d
   t->jc_Tm = Tm;
   t->jc_Tt = Tt;
   t->jc_T = T;
+  return 0;
+}
+
+/* GMT(el, n1, n2, C1, C2, m1, m2, I1, I2, e_min, e_max, er_min, er_max, T_min,
+ * T_max) (Material.cuh:271-290) with the constants reaching the Material_
+ * fields that CalcGMTYieldStress reads; c = {n1, n2, C1, C2, m1, m2, I1, I2},
+ * range = {e_min, e_max, er_min, er_max, T_min, T_max}. */
+int wfo_set_gmt(wfo_domain *d, int mat, const double *c, const double *range, double T) {
+  if (mat < 0 || mat >= d->nmat || !c || !range) return -1;
+  mat_t *t = &d->mats[mat];
+  t->g_n1 = c[0]; t->g_n2 = c[1]; t->g_C1 = c[2]; t->g_C2 = c[3];
+  t->g_m1 = c[4]; t->g_m2 = c[5]; t->g_I1 = c[6]; t->g_I2 = c[7];
+  t->g_emin = range[0]; t->g_emax = range[1];
+  t->g_rmin = range[2]; t->g_rmax = range[3];
+  t->g_Tmin = range[4]; t->g_Tmax = range[5];
+  t->g_T = T;
   return 0;
 }
 
@@ -841,6 +861,35 @@ static double jc_et(double plstrain, double strain_rate, const mat_t *m, double 
   return Et;
 }
 
+/* CalcGMTYieldStress (Material.cuh:417-452): strain, rate and temperature
+ * clamped to their ranges. */
+static double gmt_sy(double strain, double strain_rate, double temp, const mat_t *m) {
+  double e = strain, er = strain_rate, T = temp;
+  if (e < m->g_emin) e = m->g_emin;
+  else if (e > m->g_emax) e = m->g_emax;
+  if (er < m->g_rmin) er = m->g_rmin;
+  else if (er > m->g_rmax) er = m->g_rmax;
+  if (T < m->g_Tmin) T = m->g_Tmin;
+  else if (T > m->g_Tmax) T = m->g_Tmax;
+  return m->g_C1 * exp(m->g_C2 * T) * pow(e, m->g_n1 * T + m->g_n2) *
+         exp((m->g_I1 * T + m->g_I2) / e) * pow(er, m->g_m1 * T + m->g_m2);
+}
+
+/* CalcGMTTangentModulus (Material.cuh:454-478): d sigma_y / d e. */
+static double gmt_et(double plstrain, double strain_rate, double temp, const mat_t *m) {
+  double e = plstrain, er = strain_rate, T = temp;
+  if (plstrain < m->g_emin) e = m->g_emin;
+  else if (plstrain > m->g_emax) e = m->g_emax;
+  if (strain_rate < m->g_rmin) er = m->g_rmin;
+  else if (strain_rate > m->g_rmax) er = m->g_rmax;
+  if (temp < m->g_Tmin) T = m->g_Tmin;
+  else if (temp > m->g_Tmax) T = m->g_Tmax;
+  return m->g_C1 * exp(m->g_C2 * T) * pow(er, m->g_m1 * T + m->g_m2) *
+         pow(e, T * m->g_n1 + m->g_n2 - 2.0) *
+         (-m->g_I1 * T - m->g_I2 + e * (m->g_n1 * T + m->g_n2)) *
+         exp((m->g_I1 * T + m->g_I2) / e);
+}
+
 static double hollomon_sy(double strain, const mat_t *m) {
   if (strain + m->eps0 > m->eps1) return m->hol_K * pow(strain + m->eps0, m->hol_m);
   return m->sy0;
@@ -892,17 +941,20 @@ static void calc_stress_strain(wfo_domain *d) {
                              (SR[YY] - SR[ZZ]) * (SR[YY] - SR[ZZ]) +
                              (SR[ZZ] - SR[XX]) * (SR[ZZ] - SR[XX])) +
                       3.0 * (SR[XY] * SR[XY] + SR[YZ] * SR[YZ] + SR[XZ] * SR[XZ]));
-    /* Johnson-Cook temperature: the material's (uniform) temperature, or
-     * with thermal coupling the mean of the element's node temperatures (the
-     * reference reads T[e], a node array indexed by element) */
-    double temp = m->jc_T;
-    if (d->thermal && m->model == 2) {
+    /* Johnson-Cook and GMT temperature: the material's (uniform)
+     * temperature, or with thermal coupling the mean of the element's node
+     * temperatures (the reference reads T[e], a node array indexed by
+     * element) */
+    double temp = (m->model == 3) ? m->g_T : m->jc_T;
+    if (d->thermal && (m->model == 2 || m->model == 3)) {
       double ts = 0.0;
       for (int a = 0; a < d->npe; a++) ts += d->T[d->elnod[e * d->npe + a]];
       temp = ts / d->npe;
     }
     if (m->model == 2) {
       d->sigma_y[e] = jc_sy(d->pl_strain[e], eff, m, temp);
+    } else if (m->model == 3) {
+      d->sigma_y[e] = gmt_sy(d->pl_strain[e], eff, temp, m);
     } else if (m->model == 1) {
       d->sigma_y[e] = hollomon_sy(d->pl_strain[e], m);
     } else {
@@ -913,6 +965,8 @@ static void calc_stress_strain(wfo_domain *d) {
     if (d->sigma_y[e] < sig_trial) {
       if (m->model == 2)
         H = jc_et(d->pl_strain[e], eff, m, temp);
+      else if (m->model == 3)
+        H = gmt_et(d->pl_strain[e], eff, temp, m);
       else
         H = (m->model == 1) ? hollomon_et(d->pl_strain[e], m) : m->H;
       double G = m->G;

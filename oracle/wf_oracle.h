@@ -50,6 +50,9 @@ int wfo_set_elem_materials(wfo_domain *d, const int32_t *ids);
 /* Johnson-Cook constants of material `mat` (model 2) and its temperature. */
 int wfo_set_johnson_cook(wfo_domain *d, int mat, double B, double n, double C, double eps0,
                          double m, double Tm, double Tt, double T);
+/* GMT law: c = {n1, n2, C1, C2, m1, m2, I1, I2}, range = {e_min, e_max,
+ * er_min, er_max, T_min, T_max}, T the uniform element temperature. */
+int wfo_set_gmt(wfo_domain *d, int mat, const double *c, const double *range, double T);
 /* Thermal coupling (Domain_d::setThermalOn / setTemp): every node at T0 at init. */
 void wfo_set_thermal(wfo_domain *d, int on, double T0);
 /* Conductivity, heat capacity and expansion coefficient of material `mat`. */

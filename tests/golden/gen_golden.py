@@ -7,7 +7,10 @@ reference's validation/ files into validation_kats.json. The fixtures travel
 with the repository so that tests can pin the oracle where the reference
 checkout is absent.
 
-Usage: python tests/golden/gen_golden.py /path/to/reference [--vtk-only]
+Usage: python tests/golden/gen_golden.py /path/to/reference [--vtk-only] [--only NAME ...]
+
+--only regenerates the named step fixtures alone and keeps the other entries
+of cases.json (and their .npz files) as they are.
 
 The VTK fixtures (vtk_*.npz) hold the data blocks that the reference's own
 VTKWriter prints for the state after a run (--vtk-only writes only those).
@@ -34,6 +37,10 @@ HOLLOMON = dict(model=1, E=200e9, nu=0.3, rho=7850.0, sy0=300e6, hol_K=600e6, ho
 STAB = [0.3, 0.7, 0.2, 0.08, 0.15, 0.15, 0.8, 0.2, 0.05, 0.0]
 # Johnson-Cook B, n, C, eps0_dot, m, T_melt, T_transition, T
 JC = [400e6, 0.35, 0.02, 1.0, 1.0, 1500.0, 20.0, 300.0]
+# GMT constants n1, n2, C1, C2, m1, m2, I1, I2, the e / edot / T ranges and the
+# temperature: about 300 MPa at eps_p = 0.01 and a strain rate of 100 /s
+GMT = dict(c=[-2e-4, 0.2, 1200e6, -1.5e-3, 1e-4, 0.02, -1e-5, -2e-3],
+           range=[0.01, 2.0, 1e-2, 1e5, 0.0, 1500.0], T=300.0)
 # a 2x2-cell plane of triangles just below the top face of the 3x3x4-cell
 # tetrahedral block (top at z = 2 mm), normal -z, moving down at 5 m/s
 DIE = dict(start=[-0.001, -0.001, 0.002 - 1e-5], end=[0.004, 0.004, 0.0], dens=2, flip=True,
@@ -125,6 +132,14 @@ def cases():
     c.top_vz = -5.0
     c.materials = [dict(model=2, E=200e9, nu=0.3, rho=7850.0, sy0=250e6)]
     out.append(("hex_johnson_cook", c, 400, "step", dict(jc=JC)))
+    # GMT through the reference's own CalcGMTYieldStress / CalcGMTTangentModulus
+    # (the harness sets the Material_ fields those functions read)
+    c = W.config(0, scale=(3, 3, 4))
+    c.perturb = 0.1
+    c.seed = W.SEED_BASE + 19
+    c.top_vz = -5.0
+    c.materials = [dict(model=3, E=200e9, nu=0.3, rho=7850.0, sy0=250e6)]
+    out.append(("hex_gmt", c, 400, "step", dict(gmt=GMT)))
     return out
 
 
@@ -139,6 +154,9 @@ def setup_ref(d, case, extra):
         d.set_artif_visc(*extra["av"])
     if "jc" in extra:
         d.set_johnson_cook(0, *extra["jc"])
+    if "gmt" in extra:
+        g = extra["gmt"]
+        d.set_gmt(0, g["c"], g["range"], g["T"])
     if "die" in extra:
         die = extra["die"]
         xyz, tri = W.axis_plane_mesh(die["start"], die["end"], die["dens"], die["flip"])
@@ -261,6 +279,15 @@ def main():
         sys.exit(2)
     ref_root = sys.argv[1]
     subprocess.check_call([os.path.join(ROOT, "oracle", "build_ref.sh"), ref_root])
+    if "--only" in sys.argv:
+        names = sys.argv[sys.argv.index("--only") + 1:]
+        with open(os.path.join(HERE, "cases.json")) as f:
+            old = {m["name"]: m for m in json.load(f)}
+        metas = [run_case(*c) if c[0] in names else old[c[0]] for c in cases()]
+        with open(os.path.join(HERE, "cases.json"), "w") as f:
+            json.dump(metas, f, indent=1)
+        print("wrote", len(names), "fixtures")
+        return
     vmetas = [run_vtk_case(*c) for c in vtk_cases()]
     with open(os.path.join(HERE, "vtk_cases.json"), "w") as f:
         json.dump(vmetas, f, indent=1)

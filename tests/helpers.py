@@ -48,6 +48,9 @@ def setup(dom, case, extra=None):
         dom.set_artif_visc(*extra["av"])
     if "jc" in extra:
         dom.set_johnson_cook(0, *extra["jc"])
+    if "gmt" in extra:
+        g = extra["gmt"]
+        dom.set_gmt(0, g["c"], g["range"], g["T"])
     if "die" in extra:
         die = extra["die"]
         xyz, tri = W.axis_plane_mesh(die["start"], die["end"], die["dens"], die["flip"])

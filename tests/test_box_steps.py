@@ -32,11 +32,20 @@ CASES = {
 }
 
 
-def run(case, mode, steps, rows=8, hollomon=False, energy=False, runs=None, flow=None):
+GMT_MAT = dict(model=3, E=200e9, nu=0.3, rho=7850.0, sy0=250e6)
+GMT = dict(c=[-2e-4, 0.2, 1200e6, -1.5e-3, 1e-4, 0.02, -1e-5, -2e-3],
+           range=[0.01, 2.0, 1e-2, 1e5, 0.0, 1500.0], T=300.0)
+
+
+def run(case, mode, steps, rows=8, hollomon=False, energy=False, runs=None, flow=None,
+        gmt=False):
     d = wf.Domain(wf.WF_MIXED)
     W.apply(d, case)
     if hollomon:
         d.set_materials([H.HOLLOMON])
+    if gmt:
+        d.set_materials([GMT_MAT])
+        d.set_gmt(0, GMT["c"], GMT["range"], GMT["T"])
     if energy:
         d.set_energy_history(True)
     d.set_sweep_rows(rows)
@@ -95,10 +104,12 @@ def test_flow_equals_per_phase_bitwise(name, flow):
 
 
 @pytest.mark.parametrize("mode", [4, 5])
-def test_general_law_equals_per_phase_bitwise(mode):
+@pytest.mark.parametrize("law", ["hollomon", "gmt"])
+def test_general_law_equals_per_phase_bitwise(mode, law):
     case = W.config(0, scale=(12, 12, 12))
-    s = run(case, mode, 800, hollomon=True)
-    p = run(case, 1, 800, hollomon=True)
+    case.top_vz = -20.0
+    s = run(case, mode, 400, **{law: True})
+    p = run(case, 1, 400, **{law: True})
     assert s.elem_scalar("pl_strain").max() > 0.0
     assert_same_state(s, p)
 

@@ -163,7 +163,8 @@ def test_deck_errors(tmp_path):
         (dict(RigidBodies=[{"type": "Line", "dim": [1.0, 0.0, 0.0]}]), 5),
         (dict(RigidBodies=[{"type": "Plane"}, {"type": "Sphere"}]), 5),
         (dict(RigidBodies=[{"zoneId": 1}, {"type": "Plane"}]), 1),
-        (dict(Materials=[dict(STEEL, type="GMT")]), 5),
+        (dict(Materials=[dict(STEEL, type="NortonHoff")]), 5),
+        (dict(Materials=[dict(STEEL, type="GMT")]), 1),      # strRange missing: e_min = 0
         (dict(DomainBlocks=[{"type": "File", "fileName": "missing.k"}]), 1),
         (dict(BoundaryConditions=[{"zoneId": 3, "value": [0, 0, 1.0]}]), 1),
     ]

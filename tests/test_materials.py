@@ -1,11 +1,12 @@
-"""Material laws beyond linear hardening on the GPU: Johnson-Cook.
+"""Material laws beyond linear hardening on the GPU: Johnson-Cook and GMT.
 
-The oracle's Johnson-Cook restatement is pinned bit-for-bit to the
-reference's own CalcStressStrain (Material_::Init_JohnsonCook) by the
-hex_johnson_cook fixture in tests/test_oracle.py. Here the GPU paths are
-checked against the oracle on the same inputs: FP64 within 1e-9 relative
-(log and pow of the device and the host libm can differ by an ulp), mixed
-precision within the mixed-path bounds.
+The oracle's restatements are pinned bit-for-bit to the reference's own
+CalcStressStrain (Material_::Init_JohnsonCook; CalcGMTYieldStress and
+CalcGMTTangentModulus with the Material_ fields they read) by the
+hex_johnson_cook and hex_gmt fixtures in tests/test_oracle.py. Here the GPU
+paths are checked against the oracle on the same inputs: FP64 within 1e-9
+relative (log, exp and pow of the device and the host libm can differ by an
+ulp), mixed precision within the mixed-path bounds in each of its step modes.
 """
 import numpy as np
 import pytest
@@ -17,6 +18,10 @@ from weldformfem_gb300 import workloads as W
 
 JC_MAT = dict(model=2, E=200e9, nu=0.3, rho=7850.0, sy0=250e6)
 JC = [400e6, 0.35, 0.02, 1.0, 1.0, 1500.0, 20.0, 300.0]
+GMT_MAT = dict(model=3, E=200e9, nu=0.3, rho=7850.0, sy0=250e6)
+# n1, n2, C1, C2, m1, m2, I1, I2; e, edot and T ranges; temperature
+GMT = dict(c=[-2e-4, 0.2, 1200e6, -1.5e-3, 1e-4, 0.02, -1e-5, -2e-3],
+           range=[0.01, 2.0, 1e-2, 1e5, 0.0, 1500.0], T=300.0)
 
 
 def cases():
@@ -98,3 +103,108 @@ def test_johnson_cook_deck(tmp_path):
     k = wf.Deck(str(p))
     assert k.info["material"]["model"] == 2 and k.info["material"]["sy0"] == 250e6
     assert k.info["johnson_cook"] == [400e6, 0.35, 0.02, 1.0, 1.0, 1.0e10, 0.0, 0.0]
+
+
+def gmt_cases():
+    h = W.config(0, scale=(3, 3, 4))
+    h.perturb = 0.1
+    h.seed = W.SEED_BASE + 19
+    h.top_vz = -5.0
+    h.materials = [dict(GMT_MAT)]
+    t = W.config(1, scale=(3, 3, 4))
+    t.top_vz = -3.0
+    t.materials = [dict(GMT_MAT)]
+    # a box of hexahedra (no perturbation) large enough for the per-phase,
+    # column-sweep and dataflow steps
+    b = W.config(0, scale=(12, 12, 12))
+    b.top_vz = -20.0
+    b.materials = [dict(GMT_MAT)]
+    return {"hex": (h, 400), "tet": (t, 300), "box": (b, 300)}
+
+
+def gmt_oracle(case, steps):
+    o = O.OracleDomain()
+    H.setup(o, case, {"gmt": GMT})
+    o.init()
+    o.step(steps)
+    return o
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["hex", "tet", "box"])
+def test_gmt_fp64_matches_oracle(name):
+    case, steps = gmt_cases()[name]
+    o = gmt_oracle(case, steps)
+    assert o.elem_scalar("pl_strain").max() > 0.005   # well into yield, past e_min
+    d = wf.Domain(wf.WF_FP64)
+    H.setup(d, case, {"gmt": GMT})
+    d.init()
+    d.run(steps)
+    for kind, f in [("node_vec", "u"), ("elem_scalar", "pl_strain"), ("elem_scalar", "sigma_y"),
+                    ("elem_tensor", "sigma")]:
+        assert H.rel_err(getattr(d, kind)(f), getattr(o, kind)(f)) <= 1e-9, f
+    assert H.rel_err(d.reaction(), o.reaction()) <= 1e-9
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name,mode", [("hex", 0), ("hex", 1), ("tet", 0), ("tet", 1),
+                                       ("box", 1), ("box", 4), ("box", 5)])
+def test_gmt_mixed(name, mode):
+    """FP32 GMT (the law's temperature terms reduced once on the host) in the
+    automatic mode (the cluster run for these sizes), the per-phase kernels,
+    the column sweep and the dataflow step."""
+    case, steps = gmt_cases()[name]
+    o = gmt_oracle(case, steps)
+    d = wf.Domain(wf.WF_MIXED)
+    H.setup(d, case, {"gmt": GMT})
+    if mode:
+        d.set_step_mode(mode)
+    d.init()
+    d.run(steps)
+    assert H.rel_err(d.node_vec("u"), o.node_vec("u")) <= 1e-4
+    assert H.rel_err(d.elem_scalar("pl_strain"), o.elem_scalar("pl_strain")) <= 1e-2
+    assert H.rel_err(d.reaction(), o.reaction()) <= 1e-3
+
+
+@pytest.mark.gpu
+def test_gmt_argument_checks():
+    case, _ = gmt_cases()["hex"]
+    d = wf.Domain(wf.WF_FP64)
+    W.apply(d, case)
+    with pytest.raises(wf.WfError) as e:          # constants never set
+        d.init()
+    assert e.value.status == 2
+    d = wf.Domain(wf.WF_FP64)
+    W.apply(d, case)
+    for rng in ([0.0, 2.0, 1e-2, 1e5, 0.0, 1500.0],      # e_min = 0: the law is 0 * inf
+                [0.01, 2.0, 1e5, 1e-2, 0.0, 1500.0]):    # er_min > er_max
+        with pytest.raises(wf.WfError) as e:
+            d.set_gmt(0, GMT["c"], rng, 300.0)
+        assert e.value.status == 1
+    with pytest.raises(wf.WfError) as e:          # material 0 of another model
+        j = wf.Domain(wf.WF_FP64)
+        W.apply(j, W.config(0, scale=(2, 2, 2)))
+        j.set_gmt(0, GMT["c"], GMT["range"], 300.0)
+    assert e.value.status == 2
+
+
+def test_gmt_deck(tmp_path):
+    """The GMT deck keys (main.C:466-493, 548-553) and NortonHoff's rejection."""
+    import json
+    mat = {"type": "GMT", "const": GMT["c"], "strRange": [0.01, 2.0],
+           "strdotRange": [1e-2, 1e5], "density0": 7850.0, "youngsModulus": 200e9,
+           "poissonsRatio": 0.3, "yieldStress0": 250e6}
+    deck = {"Configuration": {"simTime": 1e-6, "cflFactor": 0.3}, "Materials": [mat],
+            "DomainBlocks": [{"type": "Box", "dim": [0.002, 0.002, 0.002],
+                              "elemLength": 0.001}]}
+    p = tmp_path / "gmt.json"
+    p.write_text(json.dumps(deck))
+    k = wf.Deck(str(p))
+    assert k.info["material"]["model"] == 3
+    assert k.info["gmt"] == GMT["c"]
+    assert k.info["gmt_range"] == [0.01, 2.0, 1e-2, 1e5, 0.0, 1.0e10]   # tempRange default
+    mat["type"] = "NortonHoff"
+    p.write_text(json.dumps(deck))
+    with pytest.raises(wf.WfError) as e:
+        wf.Deck(str(p))
+    assert e.value.status == 5

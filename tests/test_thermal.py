@@ -4,8 +4,8 @@ The oracle's restatement of ThermalCalcs, calcThermalExpansion, the plastic
 heat of the radial return and the die heat transfer is pinned bit-for-bit to
 the reference by the fixtures tet_die_thermal and tet_hollomon_thermal
 (tests/test_oracle.py). Here the GPU step runs the same cases, a hexahedral
-one with hourglass control and a Johnson-Cook one (whose element temperature
-is the mean of its node temperatures), against the oracle: displacements,
+one with hourglass control, a Johnson-Cook one and a GMT one (whose element
+temperatures are the mean of their node temperatures), against the oracle: displacements,
 temperatures and the reaction history within 1e-9 relative.
 """
 import numpy as np
@@ -22,6 +22,8 @@ THERMAL_DIE = dict(T0=20.0, k=50.0, cp=460.0, exp=1.2e-5, hc=2.0e6, T_die=600.0)
 THERMAL = dict(T0=25.0, k=45.0, cp=480.0, exp=1.0e-5)
 HOLLOMON = dict(model=1, E=200e9, nu=0.3, rho=7850.0, sy0=300e6, hol_K=600e6, hol_m=0.2)
 JC = [400e6, 0.35, 0.02, 1.0, 1.0, 1500.0, 20.0, 300.0]
+GMT = dict(c=[-2e-4, 0.2, 1200e6, -1.5e-3, 1e-4, 0.02, -1e-5, -2e-3],
+           range=[0.01, 2.0, 1e-2, 1e5, 0.0, 1500.0], T=300.0)
 
 
 def cases():
@@ -47,6 +49,13 @@ def cases():
     c.top_vz = -15.0
     c.materials = [dict(model=2, E=200e9, nu=0.3, rho=7850.0, sy0=250e6)]
     out["hex_jc"] = (c, dict(jc=JC, thermal=dict(T0=300.0, k=40.0, cp=450.0, exp=1.1e-5)), 400)
+    c = W.config(0, scale=(3, 3, 4))
+    c.perturb = 0.1
+    c.seed = W.SEED_BASE + 19
+    c.top_vz = -15.0
+    c.materials = [dict(model=3, E=200e9, nu=0.3, rho=7850.0, sy0=250e6)]
+    out["hex_gmt"] = (c, dict(gmt=GMT, thermal=dict(T0=300.0, k=40.0, cp=450.0, exp=1.1e-5)),
+                      400)
     return out
 
 
@@ -67,7 +76,7 @@ def test_oracle_heats_the_part():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("name", ["tet_die", "tet_hollomon", "hex_hg", "hex_jc"])
+@pytest.mark.parametrize("name", ["tet_die", "tet_hollomon", "hex_hg", "hex_jc", "hex_gmt"])
 def test_thermal_step_matches_oracle(name):
     case, extra, steps = cases()[name]
     o = run(O.OracleDomain(), case, extra, steps)
@@ -103,7 +112,7 @@ def mixed_case(name):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("name", ["tet_die", "tet_hollomon", "hex_hg", "hex_jc"])
+@pytest.mark.parametrize("name", ["tet_die", "tet_hollomon", "hex_hg", "hex_jc", "hex_gmt"])
 def test_mixed_thermal_against_fp64(name):
     """FP32 conduction (the hexahedron's in Walsh form), plastic heat and
     expansion, the temperature kept as a compensated pair, against the FP64

@@ -64,7 +64,8 @@ class WfDeckInfo(C.Structure):
                 ("johnson_cook", C.c_double * 8), ("rigid_bodies", C.c_int32),
                 ("thermal", C.c_int32), ("T0", C.c_double), ("thermal_k", C.c_double),
                 ("thermal_cp", C.c_double), ("thermal_exp", C.c_double),
-                ("heat_cond", C.c_double), ("die_temp", C.c_double)]
+                ("heat_cond", C.c_double), ("die_temp", C.c_double),
+                ("gmt", C.c_double * 8), ("gmt_range", C.c_double * 6)]
 
 
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
@@ -177,6 +178,7 @@ _SIGS = {
                         C.c_int64],
     "wf_set_energy_history": [C.c_void_p, C.c_int32],
     "wf_set_johnson_cook": [C.c_void_p, C.c_int32] + [C.c_double] * 8,
+    "wf_set_gmt": [C.c_void_p, C.c_int32, _dp, _dp, C.c_double],
     "wf_get_energy_history": [C.c_void_p, _dp, _dp, C.c_int64, C.POINTER(C.c_int64)],
     "wf_adjoint_backward": [C.c_void_p, _dp, C.c_int32, _dp],
     # allocation-free nodal volumes: device pointers in, device pointer out
@@ -309,6 +311,16 @@ class Domain:
         """Material_::Init_JohnsonCook constants of material `mat` (model 2)."""
         self._call("wf_set_johnson_cook", int(mat), float(B), float(n), float(C), float(eps0),
                    float(m), float(Tm), float(Tt), float(T))
+
+    def set_gmt(self, mat, c, rng, T=0.0):
+        """GMT law of material `mat` (model 3): c = (n1, n2, C1, C2, m1, m2, I1,
+        I2), rng = (e_min, e_max, er_min, er_max, T_min, T_max), T the
+        temperature without thermal coupling."""
+        c = np.ascontiguousarray(c, np.float64)
+        rng = np.ascontiguousarray(rng, np.float64)
+        if c.size != 8 or rng.size != 6:
+            raise ValueError("set_gmt takes 8 constants and 6 range bounds")
+        self._call("wf_set_gmt", int(mat), c, rng, float(T))
 
     def set_hourglass(self, coef):
         self._call("wf_set_hourglass", float(coef))
@@ -694,8 +706,11 @@ class Deck:
     @staticmethod
     def _info_dict(info):
         out = {f: getattr(info, f) for f, _ in WfDeckInfo._fields_
-               if f not in ("artif_visc", "stab", "material", "die_vel", "johnson_cook")}
+               if f not in ("artif_visc", "stab", "material", "die_vel", "johnson_cook", "gmt",
+                            "gmt_range")}
         out["johnson_cook"] = [info.johnson_cook[k] for k in range(8)]
+        out["gmt"] = [info.gmt[k] for k in range(8)]
+        out["gmt_range"] = [info.gmt_range[k] for k in range(6)]
         out["artif_visc"] = (info.artif_visc[0], info.artif_visc[1])
         out["die_vel"] = tuple(info.die_vel[k] for k in range(3))
         out["stab"] = [getattr(info.stab, f) for f, _ in WfStab._fields_]
@@ -760,6 +775,8 @@ class Deck:
         dom.set_materials([i["material"]])
         if i["material"]["model"] == 2:
             dom.set_johnson_cook(0, *i["johnson_cook"])
+        if i["material"]["model"] == 3:
+            dom.set_gmt(0, i["gmt"], i["gmt_range"], i["T0"] if i["thermal"] else 0.0)
         dom.add_bcs(self.bcs())
         if i["has_stab"]:
             dom.set_stab(np.array(i["stab"]))

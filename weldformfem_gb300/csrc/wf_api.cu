@@ -6,6 +6,7 @@
 #include <algorithm>
 #include <array>
 #include <cmath>
+#include <cfloat>
 #include <cstdarg>
 #include <cstddef>
 #include <climits>
@@ -143,6 +144,8 @@ struct wf_domain {
   // materials
   std::vector<wf_material> mats;
   std::vector<std::array<double, 8>> jc;  // Johnson-Cook B, n, C, eps0_dot, m, T_melt, T_t, T
+  // GMT n1, n2, C1, C2, m1, m2, I1, I2, e_min, e_max, er_min, er_max, T_min, T_max, T
+  std::vector<std::array<double, 15>> gmt;
   std::vector<std::array<double, 3>> mat_thermal;  // k_T, cp_T, exp_T per material
   bool thermal = false;
   double T0 = 20.0;
@@ -964,13 +967,14 @@ WF_API wf_status wf_set_materials(wf_domain *d, int32_t nmat, const wf_material 
     if (!(m.E > 0) || !(m.rho > 0) || !(m.nu > -1.0 && m.nu < 0.5))
       return fail(d, WF_ERR_ARG, "material %d: need E > 0, rho > 0, -1 < nu < 0.5", i);
     if (m.model != WF_MAT_BILINEAR && m.model != WF_MAT_HOLLOMON &&
-        m.model != WF_MAT_JOHNSON_COOK)
+        m.model != WF_MAT_JOHNSON_COOK && m.model != WF_MAT_GMT)
       return fail(d, WF_ERR_UNSUPPORTED, "material %d: model %d", i, m.model);
     if (m.model == WF_MAT_HOLLOMON && !(m.hol_K > 0 && m.hol_m > 0))
       return fail(d, WF_ERR_ARG, "material %d: Hollomon needs K > 0, m > 0", i);
   }
   d->mats.assign(mats, mats + nmat);
   d->jc.assign(nmat, std::array<double, 8>{0, 0, 0, 0, 0, 0, 0, 0});
+  d->gmt.assign(nmat, std::array<double, 15>{});
   d->mat_thermal.assign(nmat, std::array<double, 3>{0, 0, 0});
   d->rho_all = mats[0].rho;
   d->rho_set = true;
@@ -989,6 +993,28 @@ WF_API wf_status wf_set_johnson_cook(wf_domain *d, int32_t mat, double B, double
   if (!(eps0_dot > 0) || !(T_melt != T_transition))
     return fail(d, WF_ERR_ARG, "Johnson-Cook needs eps0_dot > 0 and T_melt != T_transition");
   d->jc[mat] = {B, n, C, eps0_dot, m, T_melt, T_transition, T};
+  return WF_OK;
+}
+
+WF_API wf_status wf_set_gmt(wf_domain *d, int32_t mat, const double c[8], const double range[6],
+                            double T) {
+  if (!d) return WF_ERR_ARG;
+  if (d->initialized) return fail(d, WF_ERR_STATE, "materials are set before init");
+  if (mat < 0 || mat >= (int32_t)d->mats.size())
+    return fail(d, WF_ERR_ARG, "material %d out of range", mat);
+  if (d->mats[mat].model != WF_MAT_GMT)
+    return fail(d, WF_ERR_STATE, "material %d is not of model WF_MAT_GMT", mat);
+  if (!c || !range) return fail(d, WF_ERR_ARG, "GMT needs its constants and ranges");
+  for (int q = 0; q < 8; q++)
+    if (!std::isfinite(c[q])) return fail(d, WF_ERR_ARG, "GMT constant %d is not finite", q);
+  for (int q = 0; q < 6; q += 2)
+    if (!(range[q] <= range[q + 1])) return fail(d, WF_ERR_ARG, "GMT range %d: need min <= max", q / 2);
+  if (!(range[0] > 0))
+    return fail(d, WF_ERR_ARG, "GMT needs e_min > 0 (at e = 0 the law is 0 * inf)");
+  std::array<double, 15> &g = d->gmt[mat];
+  for (int q = 0; q < 8; q++) g[q] = c[q];
+  for (int q = 0; q < 6; q++) g[8 + q] = range[q];
+  g[14] = T;
   return WF_OK;
 }
 
@@ -2025,6 +2051,15 @@ WF_API wf_status wf_init(wf_domain *d) {
       t.jc_Tm = j[5];
       t.jc_Tt = j[6];
     }
+    if (m.model == WF_MAT_GMT) {
+      // GMT(el, n1, n2, C1, C2, m1, m2, I1, I2, ranges) (Material.cuh:271-290)
+      const std::array<double, 15> &g = d->gmt[i];
+      if (!(g[8] > 0)) return fail(d, WF_ERR_STATE, "material %zu: wf_set_gmt not called", i);
+      t.g_n1 = g[0]; t.g_n2 = g[1]; t.g_C1 = g[2]; t.g_C2 = g[3];
+      t.g_m1 = g[4]; t.g_m2 = g[5]; t.g_I1 = g[6]; t.g_I2 = g[7];
+      t.g_emin = g[8]; t.g_emax = g[9]; t.g_rmin = g[10]; t.g_rmax = g[11];
+      t.g_Tmin = g[12]; t.g_Tmax = g[13]; t.g_T = g[14];
+    }
     t.k_T = d->mat_thermal[i][0];
     t.cp_T = d->mat_thermal[i][1];
     t.exp_T = d->mat_thermal[i][2];
@@ -2238,6 +2273,24 @@ WF_API wf_status wf_init(wf_domain *d) {
       mf[i].k_T = (float)md[i].k_T;
       mf[i].cp_T = (float)md[i].cp_T;
       mf[i].exp_T = (float)md[i].exp_T;
+      if (md[i].model == WF_MAT_GMT) {
+        const MatDev &g = md[i];
+        mf[i].jc_Th = (float)g.g_T;
+        const double *src[14] = {&g.g_C1, &g.g_C2, &g.g_n1, &g.g_n2, &g.g_m1, &g.g_m2, &g.g_I1,
+                                 &g.g_I2, &g.g_emin, &g.g_emax, &g.g_rmin, &g.g_rmax, &g.g_Tmin,
+                                 &g.g_Tmax};
+        float *dst[14] = {&mf[i].g_C1, &mf[i].g_C2, &mf[i].g_n1, &mf[i].g_n2, &mf[i].g_m1,
+                          &mf[i].g_m2, &mf[i].g_I1, &mf[i].g_I2, &mf[i].g_emin, &mf[i].g_emax,
+                          &mf[i].g_rmin, &mf[i].g_rmax, &mf[i].g_Tmin, &mf[i].g_Tmax};
+        // ranges past the float range (the class defaults are 1e10) stay
+        // finite: FLT_MAX keeps their clamps inactive
+        for (int q = 0; q < 14; q++) *dst[q] = (float)std::min(*src[q], (double)FLT_MAX);
+        const double Tc = std::min(std::max(g.g_T, g.g_Tmin), g.g_Tmax);
+        mf[i].g_A = (float)(g.g_C1 * std::exp(g.g_C2 * Tc));
+        mf[i].g_n = (float)(g.g_n1 * Tc + g.g_n2);
+        mf[i].g_I = (float)(g.g_I1 * Tc + g.g_I2);
+        mf[i].g_q = (float)(g.g_m1 * Tc + g.g_m2);
+      }
       mf[i].model = md[i].model;
     }
     MatF *mfd = nullptr;

@@ -795,6 +795,23 @@ WF_API wf_status wf_deck_read(const char *path, wf_deck **out, char *err, int64_
     const double jc[8] = {c[0], c[1], c[2], c[3], thermal ? c[4] : 1.0, thermal ? c[5] : 1.0e10,
                           thermal ? c[6] : 0.0, thermal ? I.T0 : 0.0};
     for (int q = 0; q < 8; q++) I.johnson_cook[q] = jc[q];
+  } else if (mtype == "GMT") {
+    // GMT(el, n1, n2, C1, C2, m1, m2, I1, I2, e_range, er_range, T_range) from
+    // const and strRange / strdotRange / tempRange, each range defaulting to
+    // [0, 1e10] (main.C:466-493, 548-553)
+    M.model = WF_MAT_GMT;
+    for (int q = 0; q < 8; q++) I.gmt[q] = c[q];
+    double er[2] = {0.0, 1.0e10}, rr[2] = {0.0, 1.0e10}, tr[2] = {0.0, 1.0e10};
+    jvec(m0, "strRange", er, 2);
+    jvec(m0, "strdotRange", rr, 2);
+    jvec(m0, "tempRange", tr, 2);
+    const double rg[6] = {er[0], er[1], rr[0], rr[1], tr[0], tr[1]};
+    for (int q = 0; q < 6; q++) I.gmt_range[q] = rg[q];
+    if (!(er[0] > 0.0))
+      return bad("GMT needs strRange with a lower bound > 0 (at zero strain the law is 0 * inf)");
+  } else if (mtype == "NortonHoff") {
+    return bad("material type NortonHoff is not supported: the reference's stress update reads "
+               "none of its constants", WF_ERR_UNSUPPORTED);
   } else {
     return bad("material type " + mtype + " is not supported", WF_ERR_UNSUPPORTED);
   }
@@ -1057,6 +1074,8 @@ WF_API wf_status wf_deck_apply(const wf_deck *k, wf_domain *d) {
     const double *j = I.johnson_cook;
     WF_DECK_TRY(wf_set_johnson_cook(d, 0, j[0], j[1], j[2], j[3], j[4], j[5], j[6], j[7]));
   }
+  if (I.material.model == WF_MAT_GMT)
+    WF_DECK_TRY(wf_set_gmt(d, 0, I.gmt, I.gmt_range, I.thermal ? I.T0 : 0.0));
   WF_DECK_TRY(wf_set_density(d, I.material.rho));
   if (I.n_bc)
     WF_DECK_TRY(wf_add_bc_vel_nodes(d, I.n_bc, k->bc_node.data(), k->bc_dim.data(),

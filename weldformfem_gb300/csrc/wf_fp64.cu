@@ -186,6 +186,28 @@ __global__ void __launch_bounds__(kNodeThreads) k_fp64_nodal(StepParams P, Fp64S
   S.jr[n] = s / s0;
 }
 
+// GMT law (CalcGMTYieldStress and CalcGMTTangentModulus, Material.cuh:417-478)
+// in FP64: strain e, strain rate r and temperature T clamped to the
+// material's ranges, then the reference's products in its order; mp points to
+// the material in global memory. Not inlined: the law's temporaries stay out
+// of the element kernel's register budget.
+static __device__ __noinline__ double gmt_sy(double e, double r, double T, const MatDev *mp) {
+  const MatDev &m = *mp;
+  e = clamp_range(e, m.g_emin, m.g_emax);
+  r = clamp_range(r, m.g_rmin, m.g_rmax);
+  T = clamp_range(T, m.g_Tmin, m.g_Tmax);
+  return m.g_C1 * exp(m.g_C2 * T) * pow(e, m.g_n1 * T + m.g_n2) * exp((m.g_I1 * T + m.g_I2) / e) *
+         pow(r, m.g_m1 * T + m.g_m2);
+}
+static __device__ __noinline__ double gmt_et(double e, double r, double T, const MatDev *mp) {
+  const MatDev &m = *mp;
+  e = clamp_range(e, m.g_emin, m.g_emax);
+  r = clamp_range(r, m.g_rmin, m.g_rmax);
+  T = clamp_range(T, m.g_Tmin, m.g_Tmax);
+  return m.g_C1 * exp(m.g_C2 * T) * pow(r, m.g_m1 * T + m.g_m2) * pow(e, T * m.g_n1 + m.g_n2 - 2.0) *
+         (-m.g_I1 * T - m.g_I2 + e * (m.g_n1 * T + m.g_n2)) * exp((m.g_I1 * T + m.g_I2) / e);
+}
+
 __device__ __forceinline__ double hollomon_sy(double strain, const MatDev &m) {
   if (strain + m.eps0 > m.eps1) return m.hol_K * pow(strain + m.eps0, m.hol_m);
   return m.sy0;
@@ -220,7 +242,8 @@ __global__ void __launch_bounds__(kElemThreads) k_fp64_elements(StepParams P, Fp
   }
   double vol = 0.0;
   vol += detJ * weight<NPE>() * 1.0;
-  const MatDev m = P.mats[P.emat ? __ldg(&P.emat[e]) : 0];
+  const int32_t mat_id = P.emat ? __ldg(&P.emat[e]) : 0;
+  const MatDev m = P.mats[mat_id];
 
   // strain rate and spin (str_rate / rot_rate, upper triangle)
   double s00 = 0.0, s11 = 0.0, s22 = 0.0, s01 = 0.0, s12 = 0.0, s02 = 0.0;
@@ -372,23 +395,28 @@ __global__ void __launch_bounds__(kElemThreads) k_fp64_elements(StepParams P, Fp
   double sy;
   double eff = 0.0;
   double jTh = m.jc_Th;
-  if (m.model == WF_MAT_JOHNSON_COOK) {
-    // effective strain rate (Mechanical.C:1701-1705) and the Johnson-Cook yield
-    // stress (CalcJohnsonCookYieldStress, Material.cuh:377-392)
+  double temp = m.g_T;  // GMT element temperature
+  if (m.model == WF_MAT_JOHNSON_COOK || m.model == WF_MAT_GMT) {
+    // effective strain rate (Mechanical.C:1701-1705)
     eff = sqrt(0.5 * ((s00 - s11) * (s00 - s11) + (s11 - s22) * (s11 - s22) +
                       (s22 - s00) * (s22 - s00)) +
                3.0 * (s01 * s01 + s12 * s12 + s02 * s02));
-    const double sr = (eff == 0.0) ? 1.e-5 : eff;
     if constexpr (TH) {
       // element temperature: mean of its node temperatures (the reference
       // reads T[e], a node array indexed by element)
       double ts = 0.0;
 #pragma unroll
       for (int a = 0; a < NPE; a++) ts += S.T[nid[a]];
-      const double th = (ts / NPE - m.jc_Tt) / (m.jc_Tm - m.jc_Tt);
-      jTh = 1.0 - pow(th, m.jc_m);
+      temp = ts / NPE;
+      if (m.model == WF_MAT_JOHNSON_COOK) jTh = 1.0 - pow((temp - m.jc_Tt) / (m.jc_Tm - m.jc_Tt), m.jc_m);
     }
-    sy = (m.sy0 + m.jc_B * pow(pls, m.jc_n)) * (1.0 + m.jc_C * log(sr / m.jc_eps0)) * jTh;
+    if (m.model == WF_MAT_JOHNSON_COOK) {
+      // CalcJohnsonCookYieldStress (Material.cuh:377-392)
+      const double sr = (eff == 0.0) ? 1.e-5 : eff;
+      sy = (m.sy0 + m.jc_B * pow(pls, m.jc_n)) * (1.0 + m.jc_C * log(sr / m.jc_eps0)) * jTh;
+    } else {
+      sy = gmt_sy(pls, eff, temp, P.mats + mat_id);
+    }
   } else if (m.model == WF_MAT_HOLLOMON) {
     sy = hollomon_sy(pls, m);
   } else {
@@ -403,6 +431,8 @@ __global__ void __launch_bounds__(kElemThreads) k_fp64_elements(StepParams P, Fp
       H = (pls > 0.) ? m.jc_n * m.jc_B * pow(pls, m.jc_n - 1.) *
                            (1.0 + m.jc_C * log(er / m.jc_eps0)) * jTh
                      : m.E * 0.1;
+    } else if (m.model == WF_MAT_GMT) {
+      H = gmt_et(pls, (1.0e6 < eff) ? 1.0e6 : eff, temp, P.mats + mat_id);
     } else {
       H = (m.model == WF_MAT_HOLLOMON) ? hollomon_et(pls, m) : m.H;
     }

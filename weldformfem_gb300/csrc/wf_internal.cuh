@@ -18,15 +18,26 @@ struct MatDev {
   double jc_B, jc_n, jc_C, jc_eps0, jc_Th;  // Johnson-Cook; jc_Th = 1 - T_h^m (host-computed)
   double jc_m, jc_Tm, jc_Tt;                 // its temperature terms (thermal coupling)
   double k_T, cp_T, exp_T;                   // conductivity, heat capacity, expansion
+  // GMT constants, the clamping ranges of strain, strain rate and temperature,
+  // and the element temperature without thermal coupling
+  double g_C1, g_C2, g_n1, g_n2, g_m1, g_m2, g_I1, g_I2;
+  double g_emin, g_emax, g_rmin, g_rmax, g_Tmin, g_Tmax, g_T;
   int32_t model;
   int32_t pad;
 };
 
 // FP32 material constants of the mixed kernels.
 struct MatF {
+  // jc_Th: 1 - T_h^m of Johnson-Cook, or the GMT temperature (uniform; the
+  // thermal step takes both from the element's node temperatures instead)
   float K, G, sy0, H, cs0, rho, hol_K, hol_m, eps0, eps1;
   float jc_B, jc_n, jc_C, jc_eps0, jc_Th, E;
   float jc_m, jc_Tm, jc_Tt, k_T, cp_T, exp_T;
+  // GMT: the constants (thermal step), the ranges, and A = C1 exp(C2 T),
+  // n = n1 T + n2, I = I1 T + I2, q = m1 T + m2 at the uniform temperature
+  float g_C1, g_C2, g_n1, g_n2, g_m1, g_m2, g_I1, g_I2;
+  float g_emin, g_emax, g_rmin, g_rmax, g_Tmin, g_Tmax;
+  float g_A, g_n, g_I, g_q;
   int32_t model;
   int32_t pad;
 };
@@ -58,6 +69,14 @@ __device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv &f) {
   if (f.d == 1) return n;
   const uint32_t t = __umulhi(f.m, n);
   return (t + ((n - t) >> 1)) >> (f.s - 1);
+}
+
+// clamp of the GMT law's strain, strain rate and temperature to their ranges
+__device__ __forceinline__ double clamp_range(double v, double lo, double hi) {
+  return (v < lo) ? lo : (v > hi) ? hi : v;
+}
+__device__ __forceinline__ float clamp_range(float v, float lo, float hi) {
+  return (v < lo) ? lo : (v > hi) ? hi : v;
 }
 #endif
 

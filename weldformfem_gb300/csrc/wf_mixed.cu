@@ -448,6 +448,38 @@ struct StateInPlace {
 // HBM, read and written in place; StateSwept: loaded ahead by the column
 // sweep, written to the other buffer of a pair, or not at all for a halo
 // element).
+// GMT law in FP32 (CalcGMTYieldStress and CalcGMTTangentModulus,
+// Material.cuh:417-478) from its temperature-reduced constants
+// A = C1 exp(C2 T), n = n1 T + n2, I = I1 T + I2, q = m1 T + m2: reduced on the
+// host at the material's uniform temperature, or here from the element's
+// temperature under thermal coupling. With e and r clamped to their ranges,
+// sigma_y = A e^n exp(I / e) r^q and Et = A r^q e^(n - 2) (e n - I) exp(I / e).
+// Returns (sigma_y at rate r, Et at rate rt). Not inlined: the law's
+// temporaries stay out of the register budget of the element kernels.
+struct GmtF {
+  float A, n, I, q;
+};
+template <bool TH>
+__device__ __forceinline__ GmtF gmt_consts(const MatF &m, float T) {
+  if constexpr (TH) {
+    T = clamp_range(T, m.g_Tmin, m.g_Tmax);
+    return GmtF{m.g_C1 * expf(m.g_C2 * T), m.g_n1 * T + m.g_n2, m.g_I1 * T + m.g_I2,
+                m.g_m1 * T + m.g_m2};
+  } else {
+    return GmtF{m.g_A, m.g_n, m.g_I, m.g_q};
+  }
+}
+__device__ __noinline__ float2 gmt_law_f(GmtF g, float emin, float emax, float rmin, float rmax,
+                                         float e, float r, float rt) {
+  e = clamp_range(e, emin, emax);
+  r = clamp_range(r, rmin, rmax);
+  rt = clamp_range(rt, rmin, rmax);
+  const float ex = expf(g.I / e);
+  const float sy = g.A * powf(e, g.n) * ex * powf(r, g.q);
+  const float et = g.A * powf(rt, g.q) * powf(e, g.n - 2.0f) * (e * g.n - g.I) * ex;
+  return make_float2(sy, et);
+}
+
 template <int LAW, bool TH, class IO>
 __device__ __forceinline__ void stress_update(const StepParams &P, const MixState &M, int64_t e,
                                               const IO &io,
@@ -483,15 +515,23 @@ __device__ __forceinline__ void stress_update(const StepParams &P, const MixStat
   float sy;
   float eff = 0.f;
   float dep = 0.f;
+  float et_gmt = 0.f;
   if (LAW == 0) {
     sy = m.sy0 + m.H * pls;
-  } else if (m.model == WF_MAT_JOHNSON_COOK) {
+  } else if (m.model == WF_MAT_JOHNSON_COOK || m.model == WF_MAT_GMT) {
     eff = sqrtf(0.5f * ((sr[0] - sr[1]) * (sr[0] - sr[1]) + (sr[1] - sr[2]) * (sr[1] - sr[2]) +
                         (sr[2] - sr[0]) * (sr[2] - sr[0])) +
                 3.0f * (sr[3] * sr[3] + sr[4] * sr[4] + sr[5] * sr[5]));
-    const float srate = (eff == 0.f) ? 1.e-5f : eff;
-    sy = (m.sy0 + m.jc_B * powf(pls, m.jc_n)) * (1.0f + m.jc_C * logf(srate / m.jc_eps0)) *
-         jTh;
+    if (m.model == WF_MAT_JOHNSON_COOK) {
+      const float srate = (eff == 0.f) ? 1.e-5f : eff;
+      sy = (m.sy0 + m.jc_B * powf(pls, m.jc_n)) * (1.0f + m.jc_C * logf(srate / m.jc_eps0)) *
+           jTh;
+    } else {
+      const float2 yt = gmt_law_f(gmt_consts<TH>(m, jTh), m.g_emin, m.g_emax, m.g_rmin,
+                                  m.g_rmax, pls, eff, (1.0e6f < eff) ? 1.0e6f : eff);
+      sy = yt.x;
+      et_gmt = yt.y;
+    }
   } else if (m.model == WF_MAT_HOLLOMON) {
     sy = (pls + m.eps0 > m.eps1) ? m.hol_K * powf(pls + m.eps0, m.hol_m) : m.sy0;
   } else {
@@ -506,6 +546,8 @@ __device__ __forceinline__ void stress_update(const StepParams &P, const MixStat
       H = (pls > 0.f) ? m.jc_n * m.jc_B * powf(pls, m.jc_n - 1.f) *
                             (1.0f + m.jc_C * logf(er / m.jc_eps0)) * jTh
                       : m.E * 0.1f;
+    } else if (m.model == WF_MAT_GMT) {
+      H = et_gmt;
     } else {
       H = (m.model == WF_MAT_HOLLOMON)
               ? ((pls + m.eps0 > m.eps1)
@@ -600,6 +642,8 @@ __device__ __forceinline__ void thermal_pre(const StepParams &P, const MixState 
   sr[2] -= c;
   if (m.model == WF_MAT_JOHNSON_COOK)
     jTh = 1.0f - powf((ts * (1.0f / NPE) - m.jc_Tt) / (m.jc_Tm - m.jc_Tt), m.jc_m);
+  else if (m.model == WF_MAT_GMT)
+    jTh = ts * (1.0f / NPE);
 }
 
 // After the forces: the element-node temperature rates -(K T)_a / m_a plus the
@@ -1971,11 +2015,15 @@ __global__ void k_mix_export_elems(StepParams P, MixState M, Fp64State S, const 
   S.vol[e] = vol[e];
   const float pls = M.pls[e];
   S.pls[e] = pls;
-  // exported yield stress; for Johnson-Cook its rate-independent part
+  // exported yield stress; for Johnson-Cook and GMT its value at unit rate
+  // factor (edot = eps0_dot, resp. edot = 1 clamped to the GMT range) and the
+  // material's uniform temperature
   S.sy[e] = (m.model == WF_MAT_HOLLOMON)
                 ? ((pls + m.eps0 > m.eps1) ? m.hol_K * powf(pls + m.eps0, m.hol_m) : m.sy0)
-                : (m.model == WF_MAT_JOHNSON_COOK) ? (m.sy0 + m.jc_B * powf(pls, m.jc_n)) * m.jc_Th
-                                                   : m.sy0 + m.H * pls;
+            : (m.model == WF_MAT_JOHNSON_COOK) ? (m.sy0 + m.jc_B * powf(pls, m.jc_n)) * m.jc_Th
+            : (m.model == WF_MAT_GMT)          ? gmt_law_f(gmt_consts<false>(m, 0.f), m.g_emin, m.g_emax,
+                                                         m.g_rmin, m.g_rmax, pls, 1.0f, 1.0f).x
+                                               : m.sy0 + m.H * pls;
   for (int c = 0; c < 6; c++) {
     const double t = M.tau[c * ne + e];
     S.tau[c * ne + e] = t;
