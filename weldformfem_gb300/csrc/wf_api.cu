@@ -2671,7 +2671,8 @@ WF_API wf_status wf_run(wf_domain *d, int64_t nsteps) {
       left -= chunk;
     }
   }
-  const int per_step = flow_mode(d) ? 1 : (sweep_mode(d) ? 3 : 4);
+  // the split dataflow step launches the geometry and nodal kernels first
+  const int per_step = flow_mode(d) ? (d->F.split ? 3 : 1) : (sweep_mode(d) ? 3 : 4);
   d->launches += (per_step + (d->nspec ? 1 : 0) + (d->P.energy_on ? 1 : 0)) * left;
   // graph replays: kGraphSteps at a time, then one graph of the remainder
   if (left >= kGraphSteps) {
