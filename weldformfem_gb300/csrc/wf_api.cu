@@ -2185,11 +2185,16 @@ WF_API wf_status wf_init(wf_domain *d) {
   // loop, so only the last dimension's BC values survive into step 1.
   initial_yield(P, S.sy, d->stream);
   initial_velocity(P, S.v, d->stream);
-  fp64_geometry(P, S, d->stream, true);
-  CUDA_TRY(cudaMemcpyAsync(S.vol0, S.vol, sizeof(double) * ne, cudaMemcpyDeviceToDevice,
-                           d->stream));
-  fp64_density(P, S, d->rho0_dev, d->stream);
-  fp64_nodal(P, S, d->stream, 1);
+  if (fp64) {
+    // initial volumes, densities, nodal volumes and masses (CalcElemInitialVol,
+    // calcElemDensity, CalcNodalVol, CalcNodalMassFromVol); the mixed state
+    // forms its own in FP32 (mix_init)
+    fp64_geometry(P, S, d->stream, true);
+    CUDA_TRY(cudaMemcpyAsync(S.vol0, S.vol, sizeof(double) * ne, cudaMemcpyDeviceToDevice,
+                             d->stream));
+    fp64_density(P, S, d->rho0_dev, d->stream);
+    fp64_nodal(P, S, d->stream, 1);
+  }
   CUDA_TRY(cudaGetLastError());
   if (!fp64) {
     MixState &M = d->M;
@@ -2303,7 +2308,7 @@ WF_API wf_status wf_init(wf_domain *d) {
     P.f_c_mu = (float)P.c_mu;
     P.f_av0 = (float)P.av[0];
     P.f_av1 = (float)P.av[1];
-    mix_init(P, M, S, d->stream);
+    mix_init(P, M, S, d->mvol, d->rho0_dev, d->stream);
     CUDA_TRY(cudaGetLastError());
     d->mix_valid_fp64 = true;
     // element tiles of the tiled step (hexahedra; the kernels leave out

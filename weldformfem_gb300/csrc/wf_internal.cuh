@@ -338,7 +338,11 @@ struct LaunchCfg {
 };
 
 // ---- Mixed launchers (wf_mixed.cu) ----------------------------------------
-void mix_init(const StepParams &P, const MixState &M, const Fp64State &S, cudaStream_t st);
+// The mixed state from the preamble's positions and velocities: initial
+// element volumes (mixed geometry kernel, into vol), node constants, masses
+// and the FP64 copies of the initial volumes, masses and densities.
+void mix_init(const StepParams &P, const MixState &M, const Fp64State &S, float *vol,
+              const double *rho0, cudaStream_t st);
 void mix_geometry(const StepParams &P, const MixState &M, float *vol, cudaStream_t st,
                   LaunchCfg c);
 void mix_nodal(const StepParams &P, const MixState &M, const float *vol, cudaStream_t st,

@@ -1938,7 +1938,8 @@ __global__ void k_mix_predict(StepParams P, MixState M) {
 }
 
 // Copies the FP64 initial state (after the preamble) into the mixed arrays.
-template <int NPE>
+// The mixed state of the nodes from the FP64 preamble values: positions as
+// compensated pairs, initial positions, velocities.
 __global__ void k_mix_init_nodes(StepParams P, MixState M, Fp64State S) {
   const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= P.nn) return;
@@ -1950,7 +1951,19 @@ __global__ void k_mix_init_nodes(StepParams P, MixState M, Fp64State S) {
     M.v[k * np + n] = (float)S.v[k * np + n];
     M.pa[k * np + n] = 0.f;
   }
-  M.mass[n] = (float)S.mass[n];
+}
+
+// The nodes' constant part of the nodal phase from the initial element
+// volumes (FP32, from the mixed geometry kernel): s0 = the sum of the node's
+// element volumes in list order (CalcNodalVol, Mechanical.C:1555-1572),
+// nc = (1 / s0, the mean initial density of its elements), and the initial
+// lumped mass, J ratio and the FP64 copies read back by the host.
+template <int NPE>
+__global__ void k_mix_init_nodal(StepParams P, MixState M, Fp64State S, const float *vol,
+                                 const double *rho0) {
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= P.nn) return;
+  float s = 0.0f;
   double rs = 0.0;
   int32_t c = 0;
   if (NPE == 8 && P.box) {
@@ -1959,15 +1972,40 @@ __global__ void k_mix_init_nodes(StepParams P, MixState M, Fp64State S) {
 #pragma unroll
     for (int j = 0; j < 8; j++)
       if (el[j] >= 0) {
-        rs += S.rho[el[j]];
+        s += vol[el[j]];
+        rs += rho0[el[j]];
         c++;
       }
   } else {
     const int32_t b = P.off[n];
     c = P.off[n + 1] - b;
-    for (int32_t k = 0; k < c; k++) rs += S.rho[P.slot[b + k] / NPE];
+    for (int32_t k = 0; k < c; k++) {
+      const int32_t e = P.slot[b + k] / NPE;
+      s += vol[e];
+      rs += rho0[e];
+    }
   }
-  M.nc[n] = make_float2((float)(1.0 / S.s0[n]), (float)(rs / c));
+  const float2 nc = make_float2(1.0f / s, (float)(rs / c));
+  M.nc[n] = nc;
+  const float mass = (s * (1.0f / NPE)) * nc.y;
+  M.mass[n] = mass;
+  M.jr[n] = s * nc.x;
+  S.s0[n] = s;
+  S.voln[n] = (double)s / NPE;
+  S.mass[n] = mass;
+}
+
+// The elements' FP64 copies: volume, initial volume, detJ, density.
+template <int NPE>
+__global__ void k_mix_init_elems(StepParams P, Fp64State S, const float *vol,
+                                 const double *rho0) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= P.ne) return;
+  const double v = vol[e];
+  S.vol[e] = v;
+  S.vol0[e] = v;
+  S.detJ[e] = v / (NPE == 8 ? 8.0 : 1.0 / 6.0);
+  S.rho[e] = rho0[e];
 }
 
 // Writes the mixed state into the FP64 arrays read back by the host.
@@ -2039,11 +2077,17 @@ inline unsigned grid_for(int64_t n, int threads) {
 
 int mix_node_grid(int64_t nn) { return (int)grid_for(nn, kNodeThreads); }
 
-void mix_init(const StepParams &P, const MixState &M, const Fp64State &S, cudaStream_t st) {
-  if (P.npe == 8)
-    k_mix_init_nodes<8><<<grid_for(P.nn, kNodeThreads), kNodeThreads, 0, st>>>(P, M, S);
-  else
-    k_mix_init_nodes<4><<<grid_for(P.nn, kNodeThreads), kNodeThreads, 0, st>>>(P, M, S);
+void mix_init(const StepParams &P, const MixState &M, const Fp64State &S, float *vol,
+              const double *rho0, cudaStream_t st) {
+  k_mix_init_nodes<<<grid_for(P.nn, kNodeThreads), kNodeThreads, 0, st>>>(P, M, S);
+  mix_geometry(P, M, vol, st, LaunchCfg{});
+  if (P.npe == 8) {
+    k_mix_init_nodal<8><<<grid_for(P.nn, kNodeThreads), kNodeThreads, 0, st>>>(P, M, S, vol, rho0);
+    k_mix_init_elems<8><<<grid_for(P.ne, kElemThreads), kElemThreads, 0, st>>>(P, S, vol, rho0);
+  } else {
+    k_mix_init_nodal<4><<<grid_for(P.nn, kNodeThreads), kNodeThreads, 0, st>>>(P, M, S, vol, rho0);
+    k_mix_init_elems<4><<<grid_for(P.ne, kElemThreads), kElemThreads, 0, st>>>(P, S, vol, rho0);
+  }
 }
 
 namespace {
