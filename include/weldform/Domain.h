@@ -193,6 +193,11 @@ class Domain_d {
   void setHourglass(double coef) { check(wf_set_hourglass(d_, coef), "setHourglass"); }
   void setPressAlgorithm(int alg) { check(wf_set_press_algorithm(d_, alg), "m_press_algorithm"); }
   void setArtifVisc(double a, double b) { check(wf_set_artif_visc(d_, a, b), "m_artifvisc"); }
+  // m_plheatfraction and m_max_edot (Domain_d.h:783, 824)
+  void setPlasticHeatFraction(double f) {
+    check(wf_set_plastic_heat_fraction(d_, f), "m_plheatfraction");
+  }
+  void setMaxStrainRate(double r) { check(wf_set_max_strain_rate(d_, r), "m_max_edot"); }
   void setContactPlane(double z0, double vz, double kpen, double mu,
                        const std::vector<int32_t> &cand) {
     check(wf_set_contact_plane(d_, z0, vz, kpen, mu, (int64_t)cand.size(), cand.data()),

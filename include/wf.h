@@ -132,7 +132,8 @@ WF_API wf_status wf_set_materials(wf_domain *d, int32_t nmat, const wf_material 
  * CalcJohnsonCookTangentModulus, Material.cuh:377-410; CalcStressStrain,
  * Mechanical.C:1701-1770). edot is the element's effective strain rate
  * sqrt(((Dxx-Dyy)^2 + (Dyy-Dzz)^2 + (Dzz-Dxx)^2) / 2 + 3 (Dxy^2 + Dyz^2 + Dxz^2))
- * (1e-5 where it is exactly 0) and edot' = min(edot, 1e6). T is the
+ * (1e-5 where it is exactly 0) and edot' = min(edot, cap), cap from
+ * wf_set_max_strain_rate (default 1e6). T is the
  * (uniform) temperature of the material's elements; with thermal coupling
  * (wf_set_thermal) each element takes the mean of its node temperatures
  * instead. Call after wf_set_materials and before wf_init. */
@@ -146,7 +147,7 @@ WF_API wf_status wf_set_johnson_cook(wf_domain *d, int32_t mat, double B, double
  *   Et = C1 exp(C2 T) r^(m1 T + m2) e^(n1 T + n2 - 2)
  *        (e (n1 T + n2) - I1 T - I2) exp((I1 T + I2) / e),
  * sigma_y at the element's effective strain rate edot (as for Johnson-Cook,
- * without its 1e-5 floor) and Et at min(edot, 1e6) (CalcStressStrain,
+ * without its 1e-5 floor) and Et at min(edot, cap) (CalcStressStrain,
  * Mechanical.C:1727-1749). c = {n1, n2, C1, C2, m1, m2, I1, I2}, the order of
  * the input deck's "const" (main.C:548-551). range = {e_min, e_max, er_min,
  * er_max, T_min, T_max} (the class defaults are {0, 1e10, 0, 1e10, 0, 1e10});
@@ -158,6 +159,16 @@ WF_API wf_status wf_set_johnson_cook(wf_domain *d, int32_t mat, double B, double
  * reach the law.) Call after wf_set_materials and before wf_init. */
 WF_API wf_status wf_set_gmt(wf_domain *d, int32_t mat, const double c[8], const double range[6],
                             double T);
+/* Domain_d::m_plheatfraction (Domain_d.h:783, default 0.9; deck key
+ * Configuration.plHeatFrac): the fraction of the plastic work rate that
+ * CalcStressStrain turns into the element's heat source (Mechanical.C:1804);
+ * thermal coupling only. In [0, 1], before wf_init. */
+WF_API wf_status wf_set_plastic_heat_fraction(wf_domain *d, double f);
+/* Domain_d::m_max_edot (Domain_d.h:824, default 1e6; deck key
+ * Configuration.maxStrRate): the effective strain rate at which the
+ * Johnson-Cook and GMT tangent moduli are evaluated is capped there
+ * (Mechanical.C:1737). > 0, before wf_init. */
+WF_API wf_status wf_set_max_strain_rate(wf_domain *d, double r);
 /* Per-element material index (the reference's mat[e] pointers). */
 WF_API wf_status wf_set_elem_materials(wf_domain *d, const int32_t *ids);
 
@@ -532,8 +543,8 @@ WF_API wf_status wf_adjoint_backward(wf_domain *d, const double *dL_dR, int32_t 
 /* ---- input files and output ------------------------------------------------------- */
 /* JSON deck of the reference's explicit driver (src/explicit/main.C:125-1005),
  * read on the host into a deck object that wf_deck_apply replays on a domain.
- * Read: Configuration (simTime, outTime, cflFactor, pressAlgorithm,
- * artifViscCoeffs, xSymm/ySymm/zSymm, symtol), Stabilization, Materials[0]
+ * Read: Configuration (simTime, outTime, cflFactor, pressAlgorithm, plHeatFrac,
+ * maxStrRate, artifViscCoeffs, xSymm/ySymm/zSymm, symtol), Stabilization, Materials[0]
  * (Bilinear: const[0] = tangent modulus Et, H = E Et / (E - Et); Hollomon:
  * const = [K, n]; JohnsonCook: A = yieldStress0, const = [B, n, C, eps0_dot]
  * with m = 1, T_melt = 1e10, T_transition = 0 as the non-thermal driver sets
@@ -594,6 +605,8 @@ typedef struct {
   /* GMT material: const n1, n2, C1, C2, m1, m2, I1, I2 and e_range, er_range,
    * T_range (main.C:548-552) */
   double gmt[8], gmt_range[6];
+  /* Configuration plHeatFrac (default 0.9) and maxStrRate (default 1e6) */
+  double plheat_frac, max_edot;
 } wf_deck_info;
 WF_API wf_status wf_deck_read(const char *path, wf_deck **out, char *err, int64_t err_len);
 WF_API wf_status wf_deck_free(wf_deck *k);

@@ -74,6 +74,8 @@ def lib():
         "wfo_set_press_algorithm": ([vp, C.c_int], None),
         "wfo_set_stab": ([vp, _dp], None),
         "wfo_set_artif_visc": ([vp, C.c_double, C.c_double], None),
+        "wfo_set_plastic_heat_fraction": ([vp, C.c_double], None),
+        "wfo_set_max_strain_rate": ([vp, C.c_double], None),
         "wfo_set_mass_mode": ([vp, C.c_int], None),
         "wfo_set_contact_plane": ([vp, C.c_double, C.c_double, C.c_double, C.c_double, _ip, i64], None),
         "wfo_init": ([vp], C.c_int),
@@ -219,6 +221,12 @@ class OracleDomain:
 
     def set_artif_visc(self, a, b):
         lib().wfo_set_artif_visc(self.h, float(a), float(b))
+
+    def set_plastic_heat_fraction(self, f):
+        lib().wfo_set_plastic_heat_fraction(self.h, float(f))
+
+    def set_max_strain_rate(self, r):
+        lib().wfo_set_max_strain_rate(self.h, float(r))
 
     def set_mass_mode(self, mode):
         lib().wfo_set_mass_mode(self.h, int(mode))

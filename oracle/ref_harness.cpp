@@ -587,6 +587,12 @@ void wfr_set_stab(void *h, const double *s10) { static_cast<RefDomain *>(h)->set
 void wfr_set_artif_visc(void *h, double al, double be) {
   static_cast<RefDomain *>(h)->set_artif_visc(al, be);
 }
+// Domain_d::m_plheatfraction and m_max_edot, as the JSON driver sets them
+// from plHeatFrac and maxStrRate (main.C:218, 228).
+void wfr_set_plastic_heat_fraction(void *h, double f) {
+  static_cast<RefDomain *>(h)->m_plheatfraction = f;
+}
+void wfr_set_max_strain_rate(void *h, double r) { static_cast<RefDomain *>(h)->m_max_edot = r; }
 
 void wfr_add_bc_vel_node(void *h, int node, int dim, double val) {
   static_cast<RefDomain *>(h)->AddBCVelNode(node, dim, val);

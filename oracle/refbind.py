@@ -51,6 +51,8 @@ def lib():
         "wfr_set_press_algorithm": ([vp, C.c_int], None),
         "wfr_set_stab": ([vp, _dp], None),
         "wfr_set_artif_visc": ([vp, C.c_double, C.c_double], None),
+        "wfr_set_plastic_heat_fraction": ([vp, C.c_double], None),
+        "wfr_set_max_strain_rate": ([vp, C.c_double], None),
         "wfr_add_bc_vel_node": ([vp, C.c_int, C.c_int, C.c_double], None),
         "wfr_allocate_bcs": ([vp], None),
         "wfr_set_reaction_nodes": ([vp, C.c_int, _ip, C.c_int], None),
@@ -222,6 +224,12 @@ class RefDomain:
 
     def set_artif_visc(self, a, b):
         lib().wfr_set_artif_visc(self.h, float(a), float(b))
+
+    def set_plastic_heat_fraction(self, f):
+        lib().wfr_set_plastic_heat_fraction(self.h, float(f))
+
+    def set_max_strain_rate(self, r):
+        lib().wfr_set_max_strain_rate(self.h, float(r))
 
     def add_bcs(self, bcs):
         L = lib()

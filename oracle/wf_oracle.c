@@ -54,6 +54,7 @@ struct wfo_domain {
   int press_alg, mass_mode;
   double stab[10];
   double artif[2];
+  double plheat_frac, max_edot;  /* m_plheatfraction, m_max_edot (Domain_d.h:783, 824) */
   int32_t *react_nodes;
   int64_t n_react;
   int react_dim;
@@ -100,6 +101,8 @@ wfo_domain *wfo_create(void) {
   d->c_mu = 0.0;
   d->nthreads = 0;
   d->T_die = 20.0;  /* TriMesh_d T_const as the driver sets it (main.C:714) */
+  d->plheat_frac = 0.9;   /* Domain_d constructor (Domain_d.h:271) */
+  d->max_edot = 1.0e6;    /* Domain_d.h:824 */
   return d;
 }
 
@@ -411,6 +414,8 @@ void wfo_set_hourglass(wfo_domain *d, double c) { d->hg_coef = c; }
 void wfo_set_press_algorithm(wfo_domain *d, int alg) { d->press_alg = alg; }
 void wfo_set_stab(wfo_domain *d, const double s[10]) { memcpy(d->stab, s, sizeof(d->stab)); }
 void wfo_set_artif_visc(wfo_domain *d, double al, double be) { d->artif[0] = al; d->artif[1] = be; }
+void wfo_set_plastic_heat_fraction(wfo_domain *d, double f) { d->plheat_frac = f; }
+void wfo_set_max_strain_rate(wfo_domain *d, double r) { d->max_edot = r; }
 void wfo_set_mass_mode(wfo_domain *d, int mode) { d->mass_mode = mode; }
 
 /* Triangle-mesh normals (TriMesh_d::CalcNormals, Mesh.h:236-262) and plane
@@ -960,7 +965,7 @@ static void calc_stress_strain(wfo_domain *d) {
     } else {
       d->sigma_y[e] = m->sy0 + m->H * d->pl_strain[e];
     }
-    eff = (1.0e6 < eff) ? 1.0e6 : eff;  /* min(eff, m_max_edot) */
+    eff = (d->max_edot < eff) ? d->max_edot : eff;  /* min(eff, m_max_edot) */
     double dep = 0.0;
     if (d->sigma_y[e] < sig_trial) {
       if (m->model == 2)
@@ -998,7 +1003,7 @@ static void calc_stress_strain(wfo_domain *d) {
         const double idt = 1. / dt;
         const double dxx = pi[0] * idt, dyy = pi[1] * idt, dzz = pi[2] * idt;
         const double dxy = pi[3] * idt, dyz = pi[4] * idt, dxz = pi[5] * idt;
-        d->q_plheat[e] = 0.9 * (SG[XX] * dxx + 2.0 * SG[XY] * dxy + 2.0 * SG[XZ] * dxz +
+        d->q_plheat[e] = d->plheat_frac * (SG[XX] * dxx + 2.0 * SG[XY] * dxy + 2.0 * SG[XZ] * dxz +
                                 SG[YY] * dyy + 2.0 * SG[YZ] * dyz + SG[ZZ] * dzz);
       }
     }

@@ -69,6 +69,9 @@ void wfo_set_hourglass(wfo_domain *d, double coef);
 void wfo_set_press_algorithm(wfo_domain *d, int alg);
 void wfo_set_stab(wfo_domain *d, const double s[10]);
 void wfo_set_artif_visc(wfo_domain *d, double alpha, double beta);
+/* m_plheatfraction and m_max_edot (defaults 0.9 and 1e6). */
+void wfo_set_plastic_heat_fraction(wfo_domain *d, double f);
+void wfo_set_max_strain_rate(wfo_domain *d, double r);
 /* 0: lumped mass recomputed every step from the current volume, as the
  * reference loop does (Solver_explicit.C:605-607); 1: mass fixed at its
  * initial value, as the reference's one-element test driver does

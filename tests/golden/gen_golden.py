@@ -140,6 +140,21 @@ def cases():
     c.top_vz = -5.0
     c.materials = [dict(model=3, E=200e9, nu=0.3, rho=7850.0, sy0=250e6)]
     out.append(("hex_gmt", c, 400, "step", dict(gmt=GMT)))
+    # the strain-rate cap of the rate-dependent tangent (m_max_edot) below the
+    # element rates, and the plastic heat fraction (m_plheatfraction) other
+    # than 0.9, each through the reference's own CalcStressStrain
+    c = W.config(0, scale=(3, 3, 4))
+    c.perturb = 0.1
+    c.seed = W.SEED_BASE + 9
+    c.top_vz = -5.0
+    c.materials = [dict(model=2, E=200e9, nu=0.3, rho=7850.0, sy0=250e6)]
+    out.append(("hex_jc_rate_cap", c, 400, "step", dict(jc=JC, max_edot=50.0)))
+    c = W.config(1, scale=(2, 3, 3))
+    c.perturb = 0.1
+    c.seed = W.SEED_BASE + 17
+    c.top_vz = -20.0
+    c.materials = [dict(HOLLOMON)]
+    out.append(("tet_hollomon_heat_frac", c, 300, "step", dict(thermal=THERMAL, plheat=0.6)))
     return out
 
 
@@ -157,6 +172,10 @@ def setup_ref(d, case, extra):
     if "gmt" in extra:
         g = extra["gmt"]
         d.set_gmt(0, g["c"], g["range"], g["T"])
+    if "plheat" in extra:
+        d.set_plastic_heat_fraction(extra["plheat"])
+    if "max_edot" in extra:
+        d.set_max_strain_rate(extra["max_edot"])
     if "die" in extra:
         die = extra["die"]
         xyz, tri = W.axis_plane_mesh(die["start"], die["end"], die["dens"], die["flip"])

@@ -51,6 +51,10 @@ def setup(dom, case, extra=None):
     if "gmt" in extra:
         g = extra["gmt"]
         dom.set_gmt(0, g["c"], g["range"], g["T"])
+    if "plheat" in extra:
+        dom.set_plastic_heat_fraction(extra["plheat"])
+    if "max_edot" in extra:
+        dom.set_max_strain_rate(extra["max_edot"])
     if "die" in extra:
         die = extra["die"]
         xyz, tri = W.axis_plane_mesh(die["start"], die["end"], die["dens"], die["flip"])

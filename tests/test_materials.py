@@ -75,6 +75,28 @@ def test_johnson_cook_mixed(name):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("prec", [wf.WF_FP64, wf.WF_MIXED])
+def test_johnson_cook_strain_rate_cap(prec):
+    """m_max_edot below the element rates (the hex_jc_rate_cap fixture pins
+    the oracle to the reference): the GPU against the oracle with the same
+    cap, FP64 within 1e-9 and mixed within its bounds."""
+    case, steps = cases()["hex"]
+    extra = {"jc": JC, "max_edot": 50.0}
+    o = O.OracleDomain()
+    H.setup(o, case, extra)
+    o.init()
+    o.step(steps)
+    d = wf.Domain(prec)
+    H.setup(d, case, extra)
+    d.init()
+    d.run(steps)
+    tol = 1e-9 if prec == wf.WF_FP64 else 1e-4
+    assert H.rel_err(d.node_vec("u"), o.node_vec("u")) <= tol
+    assert H.rel_err(d.elem_scalar("pl_strain"), o.elem_scalar("pl_strain")) <= (
+        1e-9 if prec == wf.WF_FP64 else 1e-2)
+
+
+@pytest.mark.gpu
 def test_johnson_cook_needs_its_constants():
     case, _ = cases()["hex"]
     d = wf.Domain(wf.WF_FP64)
@@ -208,3 +230,27 @@ def test_gmt_deck(tmp_path):
     with pytest.raises(wf.WfError) as e:
         wf.Deck(str(p))
     assert e.value.status == 5
+
+
+def test_plasticity_options_deck(tmp_path):
+    """Configuration.plHeatFrac and maxStrRate (main.C:218, 228) and their
+    defaults."""
+    import json
+    mat = {"type": "Bilinear", "const": [2.0e9], "density0": 7850.0, "youngsModulus": 200e9,
+           "poissonsRatio": 0.3, "yieldStress0": 300e6}
+    deck = {"Configuration": {"simTime": 1e-6, "cflFactor": 0.3}, "Materials": [mat],
+            "DomainBlocks": [{"type": "Box", "dim": [0.002, 0.002, 0.002],
+                              "elemLength": 0.001}]}
+    p = tmp_path / "opts.json"
+    p.write_text(json.dumps(deck))
+    k = wf.Deck(str(p))
+    assert k.info["plheat_frac"] == 0.9 and k.info["max_edot"] == 1.0e6
+    deck["Configuration"].update(plHeatFrac=0.6, maxStrRate=50.0)
+    p.write_text(json.dumps(deck))
+    k = wf.Deck(str(p))
+    assert k.info["plheat_frac"] == 0.6 and k.info["max_edot"] == 50.0
+    deck["Configuration"]["plHeatFrac"] = 1.5
+    p.write_text(json.dumps(deck))
+    with pytest.raises(wf.WfError) as e:
+        wf.Deck(str(p))
+    assert e.value.status == 1

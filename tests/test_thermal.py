@@ -56,6 +56,12 @@ def cases():
     c.materials = [dict(model=3, E=200e9, nu=0.3, rho=7850.0, sy0=250e6)]
     out["hex_gmt"] = (c, dict(gmt=GMT, thermal=dict(T0=300.0, k=40.0, cp=450.0, exp=1.1e-5)),
                       400)
+    c = W.config(1, scale=(2, 3, 3))
+    c.perturb = 0.1
+    c.seed = W.SEED_BASE + 17
+    c.top_vz = -20.0
+    c.materials = [dict(HOLLOMON)]
+    out["tet_heat_frac"] = (c, dict(thermal=THERMAL, plheat=0.6), 300)
     return out
 
 
@@ -112,7 +118,8 @@ def mixed_case(name):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("name", ["tet_die", "tet_hollomon", "hex_hg", "hex_jc", "hex_gmt"])
+@pytest.mark.parametrize("name", ["tet_die", "tet_hollomon", "hex_hg", "hex_jc", "hex_gmt",
+                                  "tet_heat_frac"])
 def test_mixed_thermal_against_fp64(name):
     """FP32 conduction (the hexahedron's in Walsh form), plastic heat and
     expansion, the temperature kept as a compensated pair, against the FP64

@@ -65,7 +65,8 @@ class WfDeckInfo(C.Structure):
                 ("thermal", C.c_int32), ("T0", C.c_double), ("thermal_k", C.c_double),
                 ("thermal_cp", C.c_double), ("thermal_exp", C.c_double),
                 ("heat_cond", C.c_double), ("die_temp", C.c_double),
-                ("gmt", C.c_double * 8), ("gmt_range", C.c_double * 6)]
+                ("gmt", C.c_double * 8), ("gmt_range", C.c_double * 6),
+                ("plheat_frac", C.c_double), ("max_edot", C.c_double)]
 
 
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
@@ -101,6 +102,8 @@ _SIGS = {
     "wf_set_press_algorithm": [C.c_void_p, C.c_int32],
     "wf_set_stab": [C.c_void_p, C.POINTER(WfStab)],
     "wf_set_artif_visc": [C.c_void_p, C.c_double, C.c_double],
+    "wf_set_plastic_heat_fraction": [C.c_void_p, C.c_double],
+    "wf_set_max_strain_rate": [C.c_void_p, C.c_double],
     "wf_set_mass_mode": [C.c_void_p, C.c_int32],
     "wf_set_reaction_nodes": [C.c_void_p, C.c_int64, _ip, C.c_int32],
     "wf_set_contact_plane": [C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_double,
@@ -334,6 +337,14 @@ class Domain:
 
     def set_artif_visc(self, a, b):
         self._call("wf_set_artif_visc", float(a), float(b))
+
+    def set_plastic_heat_fraction(self, f):
+        """m_plheatfraction: plastic work fraction turned into heat (before init)."""
+        self._call("wf_set_plastic_heat_fraction", float(f))
+
+    def set_max_strain_rate(self, r):
+        """m_max_edot: cap of the strain rate of the rate-dependent tangents (before init)."""
+        self._call("wf_set_max_strain_rate", float(r))
 
     def set_mass_mode(self, mode):
         self._call("wf_set_mass_mode", int(mode))
@@ -784,6 +795,8 @@ class Deck:
             dom.set_press_algorithm(i["press_alg"])
         if any(i["artif_visc"]):
             dom.set_artif_visc(*i["artif_visc"])
+        dom.set_plastic_heat_fraction(i["plheat_frac"])
+        dom.set_max_strain_rate(i["max_edot"])
         if i["hourglass"]:
             dom.set_hourglass(i["hourglass"])
         if i["thermal"]:

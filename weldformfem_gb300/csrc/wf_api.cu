@@ -143,6 +143,8 @@ struct wf_domain {
   std::vector<int32_t> nodel, nodel_loc, nodel_off, nodel_cnt;
   // materials
   std::vector<wf_material> mats;
+  double plheat_frac = 0.9;        // m_plheatfraction (Domain_d.h:271)
+  double max_edot = 1.0e6;         // m_max_edot (Domain_d.h:824)
   std::vector<std::array<double, 8>> jc;  // Johnson-Cook B, n, C, eps0_dot, m, T_melt, T_t, T
   // GMT n1, n2, C1, C2, m1, m2, I1, I2, e_min, e_max, er_min, er_max, T_min, T_max, T
   std::vector<std::array<double, 15>> gmt;
@@ -993,6 +995,22 @@ WF_API wf_status wf_set_johnson_cook(wf_domain *d, int32_t mat, double B, double
   if (!(eps0_dot > 0) || !(T_melt != T_transition))
     return fail(d, WF_ERR_ARG, "Johnson-Cook needs eps0_dot > 0 and T_melt != T_transition");
   d->jc[mat] = {B, n, C, eps0_dot, m, T_melt, T_transition, T};
+  return WF_OK;
+}
+
+WF_API wf_status wf_set_plastic_heat_fraction(wf_domain *d, double f) {
+  if (!d) return WF_ERR_ARG;
+  if (d->initialized) return fail(d, WF_ERR_STATE, "the plastic heat fraction is set before init");
+  if (!(f >= 0.0 && f <= 1.0)) return fail(d, WF_ERR_ARG, "plastic heat fraction %g not in [0, 1]", f);
+  d->plheat_frac = f;
+  return WF_OK;
+}
+
+WF_API wf_status wf_set_max_strain_rate(wf_domain *d, double r) {
+  if (!d) return WF_ERR_ARG;
+  if (d->initialized) return fail(d, WF_ERR_STATE, "the strain-rate cap is set before init");
+  if (!(r > 0.0)) return fail(d, WF_ERR_ARG, "strain-rate cap %g <= 0", r);
+  d->max_edot = r;
   return WF_OK;
 }
 
@@ -1877,6 +1895,10 @@ WF_API wf_status wf_init(wf_domain *d) {
   }
   P.av[0] = d->av[0];
   P.av[1] = d->av[1];
+  P.plheat_frac = d->plheat_frac;
+  P.max_edot = d->max_edot;
+  P.f_plheat = (float)d->plheat_frac;
+  P.f_max_edot = (float)std::min(d->max_edot, (double)FLT_MAX);
   P.av_on = (d->av[0] != 0.0 || d->av[1] != 0.0) ? 1 : 0;
   P.hg_on = (d->hg != 0.0 && d->npe == 8) ? 1 : 0;
   P.hg_coef = d->hg;

@@ -725,6 +725,13 @@ WF_API wf_status wf_deck_read(const char *path, wf_deck **out, char *err, int64_
   jnum(config, "cflFactor", I.cfl);
   jint(config, "pressAlgorithm", I.press_alg);
   if (I.press_alg < 0) I.press_alg = 0;
+  // plastic heat fraction and strain-rate cap of the stress update (main.C:218, 228)
+  I.plheat_frac = 0.9;
+  I.max_edot = 1.0e6;
+  jnum(config, "plHeatFrac", I.plheat_frac);
+  jnum(config, "maxStrRate", I.max_edot);
+  if (!(I.plheat_frac >= 0.0 && I.plheat_frac <= 1.0)) return bad("plHeatFrac not in [0, 1]");
+  if (!(I.max_edot > 0.0)) return bad("maxStrRate must be > 0");
   {
     double av[3] = {0, 0, 0};
     jvec(config, "artifViscCoeffs", av, 3);
@@ -1086,6 +1093,8 @@ WF_API wf_status wf_deck_apply(const wf_deck *k, wf_domain *d) {
   if (I.artif_visc[0] != 0.0 || I.artif_visc[1] != 0.0)
     WF_DECK_TRY(wf_set_artif_visc(d, I.artif_visc[0], I.artif_visc[1]));
   if (I.hourglass != 0.0) WF_DECK_TRY(wf_set_hourglass(d, I.hourglass));
+  WF_DECK_TRY(wf_set_plastic_heat_fraction(d, I.plheat_frac));
+  WF_DECK_TRY(wf_set_max_strain_rate(d, I.max_edot));
   if (I.thermal) {
     WF_DECK_TRY(wf_set_thermal(d, 1, I.T0));
     WF_DECK_TRY(wf_set_material_thermal(d, 0, I.thermal_k, I.thermal_cp, I.thermal_exp));

@@ -426,13 +426,13 @@ __global__ void __launch_bounds__(kElemThreads) k_fp64_elements(StepParams P, Fp
   if (sy < sig_trial) {
     double H;
     if (m.model == WF_MAT_JOHNSON_COOK) {
-      // CalcJohnsonCookTangentModulus (Material.cuh:397-410) at min(edot, 1e6)
-      const double er = (1.0e6 < eff) ? 1.0e6 : eff;
+      // CalcJohnsonCookTangentModulus (Material.cuh:397-410) at min(edot, m_max_edot)
+      const double er = (P.max_edot < eff) ? P.max_edot : eff;
       H = (pls > 0.) ? m.jc_n * m.jc_B * pow(pls, m.jc_n - 1.) *
                            (1.0 + m.jc_C * log(er / m.jc_eps0)) * jTh
                      : m.E * 0.1;
     } else if (m.model == WF_MAT_GMT) {
-      H = gmt_et(pls, (1.0e6 < eff) ? 1.0e6 : eff, temp, P.mats + mat_id);
+      H = gmt_et(pls, (P.max_edot < eff) ? P.max_edot : eff, temp, P.mats + mat_id);
     } else {
       H = (m.model == WF_MAT_HOLLOMON) ? hollomon_et(pls, m) : m.H;
     }
@@ -445,7 +445,7 @@ __global__ void __launch_bounds__(kElemThreads) k_fp64_elements(StepParams P, Fp
     dep = dgamma;
   }
   double SG[6] = {t0 - p, t1 - p, t2 - p, t3, t4, t5};
-  // plastic heat (Mechanical.C:1783-1810): 0.9 sigma : (d eps_p / dt), the
+  // plastic heat (Mechanical.C:1783-1810): m_plheatfraction sigma : (d eps_p / dt), the
   // plastic strain increment along the returned stress, shear terms doubled
   double q_pl = 0.0;
   if (TH && dep > 0.0) {
@@ -455,8 +455,9 @@ __global__ void __launch_bounds__(kElemThreads) k_fp64_elements(StepParams P, Fp
     const double iyy = f * (SG[1] - 0.5 * (SG[0] + SG[2]));
     const double izz = f * (SG[2] - 0.5 * (SG[0] + SG[1]));
     const double ixy = 1.5 * f * (SG[3]), ixz = 1.5 * f * (SG[5]), iyz = 1.5 * f * (SG[4]);
-    q_pl = 0.9 * (SG[0] * (ixx * idt) + 2.0 * SG[3] * (ixy * idt) + 2.0 * SG[5] * (ixz * idt) +
-                  SG[1] * (iyy * idt) + 2.0 * SG[4] * (iyz * idt) + SG[2] * (izz * idt));
+    q_pl = P.plheat_frac * (SG[0] * (ixx * idt) + 2.0 * SG[3] * (ixy * idt) +
+                            2.0 * SG[5] * (ixz * idt) + SG[1] * (iyy * idt) +
+                            2.0 * SG[4] * (iyz * idt) + SG[2] * (izz * idt));
   }
   // total strain: eps = eps + dt * D
   {

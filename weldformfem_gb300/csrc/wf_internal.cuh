@@ -111,6 +111,8 @@ struct StepParams {
   double hg_coef;
   double stab[10];
   double av[2];
+  double plheat_frac;     // plastic work fraction turned into heat (m_plheatfraction)
+  double max_edot;        // strain-rate cap of the rate-dependent tangents (m_max_edot)
   // Chung-Hulbert constants (Solver_explicit.C:193-197), host-computed
   double alpha, beta, gamma, fcorr;  // fcorr = 1 / (1 - alpha)
   double dt;
@@ -135,6 +137,7 @@ struct StepParams {
   float f_cv_pred;        // (1 - gamma) * dt
   float f_hg_coef, f_c_k, f_c_mu;
   float f_av0, f_av1;               // artificial viscosity coefficients (mixed)
+  float f_plheat, f_max_edot;       // plheat_frac, max_edot (mixed)
   const struct MatF *matf;
   // batched ensemble (all null / zero for a single domain)
   int32_t nspec;

@@ -528,7 +528,7 @@ __device__ __forceinline__ void stress_update(const StepParams &P, const MixStat
            jTh;
     } else {
       const float2 yt = gmt_law_f(gmt_consts<TH>(m, jTh), m.g_emin, m.g_emax, m.g_rmin,
-                                  m.g_rmax, pls, eff, (1.0e6f < eff) ? 1.0e6f : eff);
+                                  m.g_rmax, pls, eff, (P.f_max_edot < eff) ? P.f_max_edot : eff);
       sy = yt.x;
       et_gmt = yt.y;
     }
@@ -542,7 +542,7 @@ __device__ __forceinline__ void stress_update(const StepParams &P, const MixStat
     if (LAW == 0) {
       H = m.H;
     } else if (m.model == WF_MAT_JOHNSON_COOK) {
-      const float er = (1.0e6f < eff) ? 1.0e6f : eff;
+      const float er = (P.f_max_edot < eff) ? P.f_max_edot : eff;
       H = (pls > 0.f) ? m.jc_n * m.jc_B * powf(pls, m.jc_n - 1.f) *
                             (1.0f + m.jc_C * logf(er / m.jc_eps0)) * jTh
                       : m.E * 0.1f;
@@ -565,15 +565,15 @@ __device__ __forceinline__ void stress_update(const StepParams &P, const MixStat
   io.store(P, M, e, t0, t1, t2, t3, t4, t5, pls);
   sg[0] = t0 - p; sg[1] = t1 - p; sg[2] = t2 - p;
   sg[3] = t3; sg[4] = t4; sg[5] = t5;
-  // plastic heat 0.9 sigma : (d eps_p / dt) (Mechanical.C:1783-1810)
+  // plastic heat m_plheatfraction sigma : (d eps_p / dt) (Mechanical.C:1783-1810)
   if (TH && dep > 0.f) {
     const float f = dep / sy;
     const float ixx = f * (sg[0] - 0.5f * (sg[1] + sg[2]));
     const float iyy = f * (sg[1] - 0.5f * (sg[0] + sg[2]));
     const float izz = f * (sg[2] - 0.5f * (sg[0] + sg[1]));
     const float ixy = 1.5f * f * sg[3], iyz = 1.5f * f * sg[4], ixz = 1.5f * f * sg[5];
-    qpl = 0.9f * (sg[0] * ixx + 2.0f * sg[3] * ixy + 2.0f * sg[5] * ixz + sg[1] * iyy +
-                  2.0f * sg[4] * iyz + sg[2] * izz) / dt;
+    qpl = P.f_plheat * (sg[0] * ixx + 2.0f * sg[3] * ixy + 2.0f * sg[5] * ixz + sg[1] * iyy +
+                        2.0f * sg[4] * iyz + sg[2] * izz) / dt;
   }
   // sigma . str_rate over the six stored components (energy history)
   if (P.energy_on)
