@@ -1979,6 +1979,15 @@ WF_API wf_status wf_init(wf_domain *d) {
   CUDA_TRY(upload(d, &bcv, vals));
   P.bc = bc;
   P.bcval = bcv;
+  {
+    // FP32 copies for the mixed node update, which would otherwise convert
+    // an FP64 value (an FP64-pipe instruction) per constrained component
+    std::vector<float> vf(vals.size());
+    for (size_t i = 0; i < vals.size(); i++) vf[i] = (float)vals[i];
+    float *bcf = nullptr;
+    CUDA_TRY(upload(d, &bcf, vf));
+    P.bcvalf = bcf;
+  }
   // node flags: zero but at the reaction and contact-candidate nodes (and
   // the external surface with a triangle-mesh die), set on the device
   uint8_t *fl = nullptr;

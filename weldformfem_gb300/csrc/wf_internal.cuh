@@ -124,6 +124,7 @@ struct StepParams {
   const int32_t *slot;    // [total]: e * npe + local node
   const uint32_t *bc;     // [nn]: bits 0..2 constrained dofs, bits 3.. value set
   const double *bcval;    // [nsets][3]
+  const float *bcvalf;    // [nsets][3] the same values rounded to FP32 (mixed kernels)
   const uint8_t *nflag;   // [nn]
   const MatDev *mats;
   const int32_t *emat;    // [ne] or null

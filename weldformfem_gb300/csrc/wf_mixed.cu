@@ -400,7 +400,12 @@ __device__ __forceinline__ void nodal_one(const StepParams &P, const MixState &M
 // are in flight before either's rest.
 template <int NPE, int BS, bool BOX>
 __global__ void __launch_bounds__(BS) k_mix_nodal(StepParams P, MixState M, const float *vol) {
-  const float2 zd = die_height(P, P.st->time);
+  // the die height once per block: FP64 runs at 1/64 of the FP32 rate, and
+  // formed by every thread it kept the FP64 pipe two-thirds busy
+  __shared__ float2 s_zd;
+  if (threadIdx.x == 0) s_zd = P.contact ? die_height(P, P.st->time) : make_float2(0.f, 0.f);
+  __syncthreads();
+  const float2 zd = s_zd;
   const int64_t stride = (int64_t)gridDim.x * BS;
   int64_t n = (int64_t)blockIdx.x * BS + threadIdx.x;
   for (; n + stride < P.nn; n += 2 * stride) {
@@ -1089,7 +1094,7 @@ __device__ __forceinline__ float node_finish(const StepParams &P, const MixState
     c_cv_corr = sf.cv_corr; c_cv_pred = sf.cv_pred;
   }
   const uint32_t code = in.code;
-  const double *bvd = &P.bcval[3 * (code >> 3)];
+  const float *bvf = &P.bcvalf[3 * (code >> 3)];
 #pragma unroll
   for (int k = 0; k < 3; k++) {
     const bool fixed = (code >> k) & 1u;
@@ -1097,7 +1102,7 @@ __device__ __forceinline__ float node_finish(const StepParams &P, const MixState
     if (fixed) a = 0.f;
     a = P.f_fcorr * (a - P.f_alpha * pa[k]);
     float v = vp[k] + c_cv_corr * a;
-    const float bv = fixed ? (float)__ldg(&bvd[k]) : 0.f;
+    const float bv = fixed ? __ldg(&bvf[k]) : 0.f;
     if (fixed) v = bv;
     const float udt = c_dt * (vold[k] + c_cu_pred * pa[k]) + c_cu_corr * a;
     x[k] = pair_add(x[k], udt);
@@ -1885,6 +1890,7 @@ __global__ void __launch_bounds__(BS) k_mix_cluster_run(StepParams P, MixState M
                                                         double *part, int64_t nsteps) {
   __shared__ float stash[NPE == 8 ? 12 * BS : 1];
   __shared__ double sh[BS / 32];
+  __shared__ float2 s_zd;
   const int64_t nb = gridDim.x, b = blockIdx.x;
   const int t = threadIdx.x;
   const int64_t e0 = P.ne * b / nb, e1 = P.ne * (b + 1) / nb;
@@ -1892,10 +1898,12 @@ __global__ void __launch_bounds__(BS) k_mix_cluster_run(StepParams P, MixState M
   double time = __ldcg(&P.st->time);
   const long long step0 = __ldcg(&P.st->step);
   for (int64_t it = 0; it < nsteps; it++) {
+    // the die height once per block (FP64), read after the barrier
+    if (t == 0) s_zd = P.contact ? die_height(P, time) : make_float2(0.f, 0.f);
     for (int64_t e = e0 + t; e < e1; e += BS) geometry_one<NPE, true>(P, M, vol, e);
     cluster_barrier();
     {
-      const float2 zd = die_height(P, time);
+      const float2 zd = s_zd;
       for (int64_t n = n0 + t; n < n1; n += BS) nodal_one<NPE, true>(P, M, vol, n, zd);
     }
     cluster_barrier();
@@ -1932,7 +1940,7 @@ __global__ void k_mix_predict(StepParams P, MixState M) {
   for (int k = 0; k < 3; k++) {
     const float cv = P.nspec_of ? P.specf[P.nspec_of[n]].cv_pred : P.f_cv_pred;
     float v = M.v[k * P.np + n] + cv * M.pa[k * P.np + n];
-    if ((code >> k) & 1u) v = (float)P.bcval[3 * (code >> 3) + k];
+    if ((code >> k) & 1u) v = P.bcvalf[3 * (code >> 3) + k];
     M.vp[k * P.np + n] = v;
   }
 }
