@@ -1415,6 +1415,12 @@ void bc_tables(wf_domain *d, std::vector<int32_t> &bnode, std::vector<uint32_t> 
   sets[std::make_tuple(bits(0.0), bits(0.0), bits(0.0))] = 0;
   bnode.clear();
   bcode.clear();
+  bnode.reserve(r.size());
+  bcode.reserve(r.size());
+  // neighbouring BC nodes mostly share their values: the last set found is
+  // checked before the map
+  auto last_key = std::make_tuple(bits(0.0), bits(0.0), bits(0.0));
+  uint32_t last_id = 0;
   for (size_t i = 0; i < r.size();) {
     const int64_t n = r[i].n;
     double v3[3] = {0.0, 0.0, 0.0};
@@ -1425,13 +1431,19 @@ void bc_tables(wf_domain *d, std::vector<int32_t> &bnode, std::vector<uint32_t> 
     }
     const auto key = std::make_tuple(bits(v3[0]), bits(v3[1]), bits(v3[2]));
     uint32_t id;
-    auto it = sets.find(key);
-    if (it == sets.end()) {
-      id = (uint32_t)(vals.size() / 3);
-      sets[key] = id;
-      vals.insert(vals.end(), v3, v3 + 3);
+    if (key == last_key) {
+      id = last_id;
     } else {
-      id = it->second;
+      auto it = sets.find(key);
+      if (it == sets.end()) {
+        id = (uint32_t)(vals.size() / 3);
+        sets[key] = id;
+        vals.insert(vals.end(), v3, v3 + 3);
+      } else {
+        id = it->second;
+      }
+      last_key = key;
+      last_id = id;
     }
     bnode.push_back((int32_t)n);
     bcode.push_back((id << 3) | mask);
