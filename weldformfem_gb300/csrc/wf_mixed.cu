@@ -1571,11 +1571,12 @@ __global__ void __launch_bounds__(SweepShape<CY>::threads, 2) k_mix_sweep(StepPa
   auto slot_x = [&](int pz) {
     return reinterpret_cast<float2 *>(smem + (pz % 3) * S::slot_bytes);
   };
-  auto stage = [&](int pz) {
+  // plane pz into its slot, by the threads first, first + stride, ...
+  auto stage = [&](int pz, int first, int stride) {
     float2 *sx = slot_x(pz);
     float *sv = reinterpret_cast<float *>(sx + 3 * PL);
     float *sj = sv + 3 * PL;
-    for (int idx = t; idx < sn; idx += NT) {
+    for (int idx = first; idx < sn; idx += stride) {
       const int si = idx % snx, sy = idx / snx;
       const int64_t n = (int64_t)(ea + si) + (int64_t)nx1 * (fa + sy) + pxy * pz;
       const int o = si + kSwNX * sy;
@@ -1598,8 +1599,8 @@ __global__ void __launch_bounds__(SweepShape<CY>::threads, 2) k_mix_sweep(StepPa
     }
   };
 
-  stage(0);
-  stage(1);
+  stage(0, t, NT);
+  stage(1, t, NT);
   cp_async_commit();
   const long long step = P.st->step;
   float pf0 = 0.f, pf1 = 0.f, pf2 = 0.f;   // plane k's sum over layer k-1
@@ -1613,8 +1614,6 @@ __global__ void __launch_bounds__(SweepShape<CY>::threads, 2) k_mix_sweep(StepPa
   for (int k = 0; k < bz; k++) {
     cp_async_wait_all();
     __syncthreads();   // planes k, k+1 staged; the previous layer's reads done
-    if (k + 2 <= bz) stage(k + 2);
-    cp_async_commit();
     if (e_act) {
       const int64_t e = e_col + exy * k;
       const StateSwept io(tn, ne, e, e_own, W.tau_o, W.pls_o);
@@ -1627,6 +1626,13 @@ __global__ void __launch_bounds__(SweepShape<CY>::threads, 2) k_mix_sweep(StepPa
       if (k + 1 < bz) load_elem_state(M, ne, e + exy, tn);
     }
     __syncthreads();
+    // the last row of warps holds no nodes: it stages plane k + 2 while the
+    // others update plane k (its slot held plane k - 1, read in the layer
+    // before)
+    if (ly == CY) {
+      if (k + 2 <= bz) stage(k + 2, lx, 32);
+      cp_async_commit();
+    }
     if (n_act) {
       constexpr int cb[4] = {2, 3, 1, 0}, ct[4] = {6, 7, 5, 4};
       float f0 = pf0, f1 = pf1, f2 = pf2;
