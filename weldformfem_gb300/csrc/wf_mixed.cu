@@ -1588,6 +1588,25 @@ __global__ void __launch_bounds__(SweepShape<CY>::threads, 2) k_mix_sweep(StepPa
       cp_async4(&sj[o], &M.jr[n]);
     }
   };
+  // plane pz by one warp, row by row (no division per node)
+  auto stage_rows = [&](int pz) {
+    float2 *sx = slot_x(pz);
+    float *sv = reinterpret_cast<float *>(sx + 3 * PL);
+    float *sj = sv + 3 * PL;
+    for (int sy = 0; sy <= ney; sy++) {
+      const int64_t row = (int64_t)ea + (int64_t)nx1 * (fa + sy) + pxy * pz;
+      for (int si = lx; si < snx; si += 32) {
+        const int64_t n = row + si;
+        const int o = si + kSwNX * sy;
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+          cp_async8(&sx[k * PL + o], &M.xh[k * np + n]);
+          cp_async4(&sv[k * PL + o], &M.vp[k * np + n]);
+        }
+        cp_async4(&sj[o], &M.jr[n]);
+      }
+    }
+  };
   // the node's own staged position and predicted velocity of plane pz
   auto own_node = [&](int pz, float2 (&x)[3], float (&vp)[3]) {
     const float2 *sx = slot_x(pz);
@@ -1630,7 +1649,7 @@ __global__ void __launch_bounds__(SweepShape<CY>::threads, 2) k_mix_sweep(StepPa
     // others update plane k (its slot held plane k - 1, read in the layer
     // before)
     if (ly == CY) {
-      if (k + 2 <= bz) stage(k + 2, lx, 32);
+      if (k + 2 <= bz) stage_rows(k + 2);
       cp_async_commit();
     }
     if (n_act) {
