@@ -261,10 +261,20 @@ def test_deck_drives_the_oracle(tmp_path):
 
 # ---- GPU -------------------------------------------------------------------------
 @pytest.mark.gpu
-@pytest.mark.parametrize("kind", ["box", "k_tet", "k_hex_hollomon"])
+@pytest.mark.parametrize("kind", ["box", "k_tet", "k_hex_hollomon", "box_gmt"])
 def test_deck_on_gpu_matches_oracle(tmp_path, kind):
     if kind == "box":
         p, _ = box_deck(tmp_path)
+    elif kind == "box_gmt":
+        # the GMT law with its ranges, and a strain-rate cap below the rates
+        gmt = dict(STEEL, type="GMT", const=[-2e-4, 0.2, 1200e6, -1.5e-3, 1e-4, 0.02, -1e-5, -2e-3],
+                   strRange=[0.01, 2.0], strdotRange=[1e-2, 1e5], tempRange=[0.0, 1500.0])
+        p, deck = box_deck(tmp_path, Materials=[gmt])
+        deck["Configuration"]["maxStrRate"] = 50.0
+        deck["Configuration"]["simTime"] = 2.0e-5
+        deck["BoundaryConditions"][0]["value"] = [0.0, 0.0, -20.0]
+        with open(p, "w") as f:
+            json.dump(deck, f)
     else:
         tet = kind == "k_tet"
         c = W.config(1 if tet else 0, scale=(3, 3, 4))
